@@ -1,0 +1,53 @@
+"""Loader for the golden fixtures made by ``tests/golden/make_golden.py``."""
+
+from __future__ import annotations
+
+import functools
+import json
+import pathlib
+
+import numpy as np
+
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
+CASES = ("g2_explicit", "g2_mono")
+
+
+@functools.lru_cache(maxsize=None)
+def load_case(name: str):
+    meta = json.loads((GOLDEN / f"{name}.json").read_text())
+    state = dict(np.load(GOLDEN / f"{name}_state.npz"))
+    taps = dict(np.load(GOLDEN / f"{name}_taps.npz"))
+    return meta, state, taps
+
+
+def group(state: dict, prefix: str) -> dict:
+    p = prefix + "/"
+    return {k[len(p):]: v for k, v in state.items() if k.startswith(p)}
+
+
+def tap_calls(name: str, stage: str):
+    """Yield ``(inputs, outputs, entry)`` for every recorded call of ``stage``."""
+    meta, state, taps = load_case(name)
+    loaded = group(state, "loaded")
+    for entry in meta["taps"]:
+        if entry["stage"] != stage:
+            continue
+        pre = f"{stage}/{entry['index']}"
+        inp = {k: loaded[k] for k in entry["static_in"]}
+        for k in entry["arrays_in"]:
+            inp[k] = taps[f"{pre}/in/{k}"]
+        for k, v in entry["scalars"].items():
+            if not k.startswith("out:"):
+                inp[k] = v
+        out = {k: taps[f"{pre}/out/{k}"] for k in entry["arrays_out"]}
+        yield inp, out, entry
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.linalg.norm(b.ravel())
+    num = np.linalg.norm((a - b).ravel())
+    if den == 0.0:
+        return float(num)
+    return float(num / den)

@@ -1,0 +1,253 @@
+"""Generate the golden fixtures under tests/golden/ by running the reference itself.
+
+This script is the only place that executes the reference (mpas_pytorch, pure
+Python + PyTorch, CPU float64).  It needs the reference source tree (default
+``/root/reference``, override with ``MPAS_REFERENCE``) and runs in a container
+without netCDF4, so it puts a two-name stub module on ``sys.path`` first (the
+reference imports netCDF4 at package import, ``utils/checkpoint_reader.py:13``,
+but the dynamics never touch it).
+
+For each case it
+  1. builds the raw MPAS grid/init arrays with ``mpas_dycore_pytorch_gb300.cases``;
+  2. feeds them through the reference's own ``load_initial_state``
+     (``ic_loader.py:1243``) by replacing ``load_checkpoint`` with an in-memory reader;
+  3. runs ``run_simulation`` (``atmosphere_model.py:1474``) for ``nsteps`` steps,
+     recording the prepared boundary (``on_initial``), the state after each step
+     (``on_step``) and, for the first large step, the inputs and outputs of every
+     stage call the step driver makes (``profiled_call`` in
+     ``dynamics/time_integration.py``; the tendency stage through
+     ``pack_dynamics_tendency_numeric_outputs``, ``dyn_tend.py:11239``).
+
+Outputs: ``<case>_state.npz`` (prepared/step boundaries), ``<case>_taps.npz`` (stage
+arrays) and ``<case>.json`` (config, dims, scalar stage arguments, tap index).
+
+Run:  python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import pathlib
+import sys
+import tempfile
+
+os.environ["PYTHONDONTWRITEBYTECODE"] = "1"
+os.environ.setdefault("ATEN_CPU_CAPABILITY", "default")
+
+HERE = pathlib.Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+REF = pathlib.Path(os.environ.get("MPAS_REFERENCE", "/root/reference"))
+
+_STUB = '''
+class Dataset:
+    def __init__(self, *a, **k):
+        raise RuntimeError("netCDF4 stub: no file I/O")
+class Variable:
+    pass
+__version__ = "0.0-stub"
+'''
+
+
+def _import_reference():
+    stub_dir = pathlib.Path(tempfile.mkdtemp(prefix="ncstub_"))
+    (stub_dir / "netCDF4").mkdir()
+    (stub_dir / "netCDF4" / "__init__.py").write_text(_STUB)
+    sys.path.insert(0, str(stub_dir))
+    sys.path.insert(0, str(REF))
+    sys.path.insert(0, str(REPO))
+    import mpas_pytorch  # noqa: F401
+    return mpas_pytorch
+
+
+CASES = {
+    # configs[0]-style: uniform levels, one cosine-bell tracer, non-monotone transport
+    "g2_explicit": dict(spec=dict(level=2, nlev=12, seed=0, n_bumps=8, n_tracers=1),
+                        config=dict(config_monotonic=False), dt=1800.0, nsteps=2),
+    # configs[1]-style: stretched levels, three tracers, monotone transport
+    "g2_mono": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=1, n_bumps=8, n_tracers=3),
+                    config=dict(config_monotonic=True), dt=1800.0, nsteps=2),
+}
+
+BASE_CONFIG = {
+    "config_time_integration_order": 3,
+    "config_len_disp": 120000.0,
+    "config_number_of_sub_steps": 2,
+    "config_dynamics_split_steps": 3,
+}
+
+
+def _np(v):
+    import torch
+    return v.detach().cpu().numpy().copy() if isinstance(v, torch.Tensor) else v
+
+
+def _scalar(v):
+    import numpy as np
+    import torch
+    if isinstance(v, torch.Tensor) and v.ndim == 0:
+        return v.item()
+    if isinstance(v, (bool, int, float, str)) or v is None:
+        return v
+    if isinstance(v, (np.integer, np.floating)):
+        return v.item()
+    return Ellipsis
+
+
+def run_case(mp, name: str, case: dict) -> None:
+    import numpy as np
+    import torch
+
+    import mpas_pytorch.dynamics.dyn_tend as dyn_tend_mod
+    import mpas_pytorch.dynamics.time_integration as ti
+    import mpas_pytorch.ic_loader as icl
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec, make_case
+
+    spec = CaseSpec(**case["spec"])
+    init, mesh = make_case(spec)
+
+    def to_torch(d):
+        out = {}
+        for k, v in d.items():
+            if isinstance(v, np.ndarray):
+                out[k] = torch.from_numpy(v.copy())
+            elif isinstance(v, (int, np.integer)):
+                out[k] = torch.tensor(int(v), dtype=torch.int32)
+            else:
+                out[k] = torch.tensor(float(v), dtype=torch.float64)
+        return out
+
+    tmp = pathlib.Path(tempfile.mkdtemp())
+    (tmp / "init.nc").write_bytes(b"")
+    (tmp / "grid.nc").write_bytes(b"")
+    raw = {str(tmp / "init.nc"): to_torch(init), str(tmp / "grid.nc"): to_torch(mesh)}
+    icl.load_checkpoint = lambda path, validated_fields=None, **kw: {
+        k: v.clone() for k, v in raw[str(path)].items()}
+
+    cfg = dict(BASE_CONFIG)
+    cfg.update(case["config"])
+    cfg["config_dt"] = case["dt"]
+    state, meshd = mp.load_initial_state(tmp / "init.nc", tmp / "grid.nc", config=cfg)
+
+    arrays: dict[str, np.ndarray] = {}
+    meta: dict = {"spec": case["spec"], "config": cfg, "dt": case["dt"],
+                  "nsteps": case["nsteps"], "torch": torch.__version__, "taps": []}
+    for key, value in state.items():
+        if isinstance(value, torch.Tensor):
+            arrays[f"loaded/{key}"] = _np(value)
+        elif _scalar(value) is not Ellipsis:
+            meta.setdefault("loaded_scalars", {})[key] = _scalar(value)
+
+    taps: dict[str, np.ndarray] = {}
+    recording = {"on": True}
+    counts: dict[str, int] = {}
+    keep_per_stage = {"mpas.acoustic_step_acoustic_step": 3, "mpas.divergence_damping": 2,
+                      "mpas.large_step_recovery_recover_large_step": 3,
+                      "mpas.diagnostic_solve_solve_diagnostics": 3,
+                      "mpas.dynamics_tendency_dyn_tend": 3,
+                      "mpas.vertical_implicit_coefficients_vert_imp_coefs": 2,
+                      "mpas.explicit_scalar_transport_advance_scalars_transport": 3,
+                      "mpas.monotonic_scalar_transport_advance_scalars_mono_transport": 1}
+
+    def record(stage: str, kwargs: dict, out: dict) -> None:
+        i = counts.get(stage, 0)
+        counts[stage] = i + 1
+        if not recording["on"] or i >= keep_per_stage.get(stage, 1):
+            return
+        entry = {"stage": stage, "index": i, "scalars": {}, "arrays_in": [], "arrays_out": [],
+                 "static_in": []}
+        prefix = f"{stage}/{i}"
+        for k, v in kwargs.items():
+            if isinstance(v, torch.Tensor):
+                a = _np(v)
+                ref = arrays.get(f"loaded/{k}")
+                if ref is not None and ref.shape == a.shape and ref.dtype == a.dtype \
+                        and np.array_equal(ref, a):
+                    entry["static_in"].append(k)  # identical to the loaded mesh/static array
+                    continue
+                taps[f"{prefix}/in/{k}"] = a
+                entry["arrays_in"].append(k)
+            else:
+                s = _scalar(v)
+                if s is not Ellipsis:
+                    entry["scalars"][k] = s
+        for k, v in out.items():
+            if isinstance(v, torch.Tensor):
+                taps[f"{prefix}/out/{k}"] = _np(v)
+                entry["arrays_out"].append(k)
+            else:
+                s = _scalar(v)
+                if s is not Ellipsis:
+                    entry["scalars"]["out:" + k] = s
+        meta["taps"].append(entry)
+
+    orig_profiled = ti.profiled_call
+
+    snapshots: dict[int, torch.Tensor] = {}
+
+    def profiled(name, config, fn, *args, **kwargs):
+        # stages update some inputs in place: record the values they were called with
+        snapshots.clear()
+        for v in list(args) + list(kwargs.values()):
+            if isinstance(v, torch.Tensor):
+                snapshots[id(v)] = v.detach().clone()
+        before = {k: snapshots.get(id(v), v) for k, v in kwargs.items()}
+        out = orig_profiled(name, config, fn, *args, **kwargs)
+        if name in ("mpas.dynamics_tendency_dyn_tend", "mpas.rk_integration_setup"):
+            return out
+        if isinstance(out, dict):
+            record(name, before, out)
+        return out
+
+    ti.profiled_call = profiled
+    orig_pack = dyn_tend_mod.pack_dynamics_tendency_numeric_outputs
+
+    def pack(compact, call_arguments, *a, **k):
+        out = orig_pack(compact, call_arguments, *a, **k)
+        args = {kk: snapshots.get(id(vv), vv) for kk, vv in call_arguments.items()
+                if not kk.startswith("_")}
+        record("mpas.dynamics_tendency_dyn_tend", args, out)
+        return out
+
+    dyn_tend_mod.pack_dynamics_tendency_numeric_outputs = pack
+
+    def on_initial(s):
+        for key, value in s.items():
+            if isinstance(value, torch.Tensor):
+                arrays[f"prepared/{key}"] = _np(value)
+            elif _scalar(value) is not Ellipsis:
+                meta.setdefault("prepared_scalars", {})[key] = _scalar(value)
+
+    def on_step(i, s):
+        recording["on"] = False
+        for key in ("u", "w", "theta_m", "rho_zz", "scalars", "rho_p", "rtheta_p", "exner",
+                    "pressure_p", "ru", "rw", "v", "divergence", "vorticity", "ke", "pv_edge",
+                    "rho_edge", "h_edge", "uReconstructX", "uReconstructY", "uReconstructZ",
+                    "uReconstructZonal", "uReconstructMeridional", "ur_cell", "vr_cell", "ruAvg",
+                    "wwAvg", "theta", "rho"):
+            if key in s and isinstance(s[key], torch.Tensor):
+                arrays[f"step{i}/{key}"] = _np(s[key])
+
+    try:
+        mp.run_simulation(state, meshd, config=cfg, dt=case["dt"], nsteps=case["nsteps"],
+                          on_step=on_step, on_initial=on_initial)
+    finally:
+        ti.profiled_call = orig_profiled
+        dyn_tend_mod.pack_dynamics_tendency_numeric_outputs = orig_pack
+
+    np.savez_compressed(HERE / f"{name}_state.npz", **arrays)
+    np.savez_compressed(HERE / f"{name}_taps.npz", **taps)
+    (HERE / f"{name}.json").write_text(json.dumps(meta, indent=1, default=str))
+    size = sum((HERE / f).stat().st_size for f in (f"{name}_state.npz", f"{name}_taps.npz"))
+    print(f"{name}: {len(arrays)} state arrays, {len(taps)} tap arrays, {size / 1e6:.1f} MB")
+
+
+def main() -> None:
+    mp = _import_reference()
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        run_case(mp, name, CASES[name])
+
+
+if __name__ == "__main__":
+    main()
