@@ -27,6 +27,7 @@ __all__ = [
     "idx0", "moist_coefficients", "vert_imp_coefs", "tridiagonal_solve",
     "acoustic_step", "divergence_damping", "smlstep_pert", "recover_large_step",
     "solve_diagnostics", "reconstruct_2d", "dyn_tend", "flux3", "flux4",
+    "advance_scalars", "advance_scalars_mono",
 ]
 
 
@@ -63,7 +64,8 @@ def moist_coefficients(a):
     qtot = np.zeros((nc + 1, nl))
     for s in range(ms - 1, me):
         qtot[:nc] = qtot[:nc] + sc[:nc, :, s]
-    cqw = np.ones((nc + 1, nl + 1))
+    cqw = np.zeros((nc + 1, nl + 1))
+    cqw[:nc, 1:nl] = 1.0
     cqu = np.ones((ne + 1, nl))
     if me >= ms:
         cqw[:nc, 1:nl] = 1.0 / (1.0 + 0.5 * (qtot[:nc, 1:] + qtot[:nc, :-1]))
@@ -785,3 +787,206 @@ def dyn_tend(a):
             "tend_u_euler": tend_u_euler, "tend_w_euler": tend_w_euler,
             "tend_theta_euler": tend_theta_euler, "h_divergence": h_div_p, "kdiff": kdiff,
             "rthdynten": zpad(rthdynten)}
+
+
+# --------------------------------------------------------------------------------------
+# scalar transport  (dynamics/advance_scalars.py:1272, composition :861, Pattern-C
+# pattern_c.py:234-305; monotone: dynamics/advance_scalars_mono.py:3332, tile :1476,
+# neighbour bounds autodiff/soft_limiter.py:72)
+# --------------------------------------------------------------------------------------
+
+def _pattern_c(a, sfield, uh, ne, nc):
+    """Edge high-order value sum_m (adv_coefs + sign(uh) adv_coefs_3rd) q[advCell_m]."""
+    adv = idx0(a["advCellsForEdge"][:ne], nc)
+    n_adv = np.asarray(a["nAdvCellsForEdge"][:ne]).astype(np.int64)
+    acoef, acoef3 = a["adv_coefs"][:ne], a["adv_coefs_3rd"][:ne]
+    sg = _sgn(uh[:ne])
+    out = None
+    for m in range(adv.shape[1]):
+        vm = m < n_adv
+        cell = np.where(vm, adv[:, m], nc)
+        wgt = acoef[:, m, None] + sg * acoef3[:, m, None]
+        c = wgt[:, :, None] * sfield[cell]
+        c = np.where(vm[:, None, None], c, 0.0)
+        out = c if out is None else out + c
+    return out
+
+
+def _time_weights(advance_density, rk_step, order):
+    if advance_density == 0:
+        w_new = 1.0
+    elif rk_step == 1 and order == 3:
+        w_new = 1.0 / 3.0
+    elif (rk_step == 1 and order == 2) or rk_step == 2:
+        w_new = 1.0 / 2.0
+    else:
+        w_new = 1.0
+    return 1.0 - w_new, w_new
+
+
+def advance_scalars(a):
+    """Explicit flux-form RK-stage scalar update (non-monotone)."""
+    nc, ne, nl = _i(a, "nCells"), _i(a, "nEdges"), _i(a, "nVertLevels")
+    dt, coef3 = _f(a, "dt"), _f(a, "coef_3rd_order")
+    w_old, w_new = _time_weights(_i(a, "advance_density"), _i(a, "rk_step"),
+                                 _i(a, "config_time_integration_order"))
+    s_new = a["scalar_new"]
+    s_old = a["scalar_old"]
+    uh = a["uhAvg"]
+    ww = a["wwAvg"][:nc]
+    sn_pad = s_new.copy()
+    sn_pad[nc] = 0.0
+    hf = _pattern_c(a, sn_pad, uh, ne, nc)
+    eoc = idx0(a["edgesOnCell"][:nc], ne)
+    n_eoc = np.asarray(a["nEdgesOnCell"][:nc]).astype(np.int64)
+    sign = a["edgesOnCell_sign"][:nc]
+    div = None
+    for j in range(eoc.shape[1]):
+        valid = (j < n_eoc) & (eoc[:, j] < ne)
+        e = np.where(valid, eoc[:, j], 0)
+        c = (-sign[:, j, None] * uh[e])[:, :, None] * hf[e]
+        c = np.where(valid[:, None, None], c, 0.0)
+        div = c if div is None else div + c
+    tend_save = np.zeros_like(a["scalar_tend_save"][:nc]) if not a.get("do_physics", False) \
+        else a["scalar_tend_save"][:nc]
+    tend_col = div * a["invAreaCell"][:nc, None, None] + tend_save
+    fnm, fnp, rdnw = a["fnm"][:nl], a["fnp"][:nl], a["rdnw"][:nl]
+    sn = s_new[:nc]
+    wdtn = np.zeros((nc, nl + 1, sn.shape[2]))
+    wdtn[:, 1] = ww[:, 1:2] * (fnm[1] * sn[:, 1] + fnp[1] * sn[:, 0])
+    for k in range(2, nl - 1):
+        wdtn[:, k] = flux3(sn[:, k - 2], sn[:, k - 1], sn[:, k], sn[:, k + 1], ww[:, k:k + 1], coef3)
+    k = nl - 1
+    wdtn[:, k] = ww[:, k:k + 1] * (fnm[k] * sn[:, k] + fnp[k] * sn[:, k - 1])
+    vdiv = rdnw[None, :, None] * (wdtn[:, 1:] - wdtn[:, :nl])
+    rho_old = a["rho_zz_old"][:nc]
+    rho_i = w_old * rho_old + w_new * a["rho_zz_new"][:nc]
+    out = s_new.copy()
+    out[:nc] = (s_old[:nc] * rho_old[:, :, None] + dt * (tend_col - vdiv)) * (1.0 / rho_i)[:, :, None]
+    hfa = a["horiz_flux_arr"].copy()
+    hfa[:ne] = hf
+    tso = a["scalar_tend_save"].copy()
+    tso[:nc] = tend_save
+    return {"scalar_new": out, "scalar_tend_save": tso, "horiz_flux_arr": hfa}
+
+
+def advance_scalars_mono(a):
+    """Monotone (flux-corrected) scalar update for the final transport RK stage."""
+    nc, ne, nl = _i(a, "nCells"), _i(a, "nEdges"), _i(a, "nVertLevels")
+    dt, coef3 = _f(a, "dt"), _f(a, "coef_3rd_order")
+    eps = 1.0e-20
+    uh = a["uhAvg"]
+    ww = a["wwAvg"][:nc]
+    rho_old = a["rho_zz_old"][:nc]
+    fnm, fnp, rdnw = a["fnm"][:nl], a["fnp"][:nl], a["rdnw"][:nl]
+    dv = a["dvEdge"]
+    inv_area = a["invAreaCell"][:nc]
+    eoc = idx0(a["edgesOnCell"][:nc], ne)
+    n_eoc = np.asarray(a["nEdgesOnCell"][:nc]).astype(np.int64)
+    sign = a["edgesOnCell_sign"][:nc]
+    coe = idx0(a["cellsOnEdge"][:ne], nc)
+    e1, e2 = coe[:, 0], coe[:, 1]
+
+    scalars_old = a["scalars_old"].copy()
+    scalars_old[:nc] = scalars_old[:nc] + dt * a["scalar_tend"][:nc] / rho_old[:, :, None]
+    scalars_new_in = a["scalars_new"]
+
+    # density at the end of the stage from the averaged mass fluxes
+    hdiv = None
+    for j in range(eoc.shape[1]):
+        valid = (j < n_eoc) & (eoc[:, j] < ne)
+        e = np.where(valid, eoc[:, j], 0)
+        c = (uh[e] * (-sign[:, j] * dv[e])[:, None]) * np.where(valid, inv_area, 0.0)[:, None]
+        hdiv = c if hdiv is None else hdiv + c
+    vdiv = rdnw[None, :] * (ww[:, 1:nl + 1] - ww[:, :nl])
+    rho_int = rho_old + dt * (hdiv - vdiv)
+
+    so_all = scalars_old.copy()
+    so_all[nc] = 0.0
+    sn_all = scalars_new_in.copy()
+    sn_all[nc] = 0.0
+    so = so_all[:nc]
+    sn = sn_all[:nc]
+    ns = so.shape[2]
+    smax = np.empty((nc, nl, ns))
+    smin = np.empty((nc, nl, ns))
+    smax[:, 0] = np.maximum(so[:, 0], so[:, 1])
+    smin[:, 0] = np.minimum(so[:, 0], so[:, 1])
+    for k in range(1, nl - 1):
+        smax[:, k] = np.maximum(np.maximum(so[:, k - 1], so[:, k]), so[:, k + 1])
+        smin[:, k] = np.minimum(np.minimum(so[:, k - 1], so[:, k]), so[:, k + 1])
+    smax[:, nl - 1] = np.maximum(so[:, nl - 1], so[:, nl - 2])
+    smin[:, nl - 1] = np.minimum(so[:, nl - 1], so[:, nl - 2])
+    wdtn = np.zeros((nc, nl + 1, ns))
+    wdtn[:, 1] = ww[:, 1:2] * (fnm[1] * sn[:, 1] + fnp[1] * sn[:, 0])
+    for k in range(2, nl - 1):
+        wdtn[:, k] = flux3(sn[:, k - 2], sn[:, k - 1], sn[:, k], sn[:, k + 1], ww[:, k:k + 1], coef3)
+    k = nl - 1
+    wdtn[:, k] = ww[:, k:k + 1] * (fnm[k] * sn[:, k] + fnp[k] * sn[:, k - 1])
+    coc = idx0(a["cellsOnCell"][:nc], nc)
+    nmax = None
+    nmin = None
+    for j in range(coc.shape[1]):
+        valid = (j < n_eoc) & (coc[:, j] < nc)
+        val = so_all[coc[:, j]]
+        vm = valid[:, None, None]
+        if nmax is None:
+            nmax = np.where(vm, val, -np.finfo(np.float64).max)
+            nmin = np.where(vm, val, np.finfo(np.float64).max)
+            seen = valid.copy()
+        else:
+            comb = (valid & seen)[:, None, None]
+            repl = (valid & ~seen)[:, None, None]
+            nmax = np.where(comb, np.maximum(nmax, val), np.where(repl, val, nmax))
+            nmin = np.where(comb, np.minimum(nmin, val), np.where(repl, val, nmin))
+            seen = seen | valid
+    smax = np.maximum(smax, nmax)
+    smin = np.minimum(smin, nmin)
+
+    # high-order and upwind fluxes
+    flux_edge = uh[:ne, :, None] * _pattern_c(a, sn_all, uh, ne, nc)
+    wmid = ww[:, 1:nl, None]
+    flux_up_mid = dt * (wmid * np.where(wmid >= 0.0, so[:, :nl - 1], so[:, 1:nl]))
+    rows = so * rho_old[:, :, None]
+    rows[:, :nl - 1] = rows[:, :nl - 1] - flux_up_mid * rdnw[None, :nl - 1, None]
+    rows[:, 1:nl] = rows[:, 1:nl] + flux_up_mid * rdnw[None, 1:nl, None]
+    wmid_flux = dt * wdtn[:, 1:nl] - flux_up_mid
+    mz = lambda x: np.maximum(x, 0.0)
+    prev = np.concatenate([wdtn[:, 0:1], wmid_flux], axis=1)
+    nxt = np.concatenate([wmid_flux, wdtn[:, nl:nl + 1]], axis=1)
+    r = rdnw[None, :, None]
+    scale_in = -r * ((-mz(-nxt)) - mz(prev))
+    scale_out = -r * (mz(nxt) - (-mz(-prev)))
+    up = uh[:ne, :, None]
+    flux_up_edge = dv[:ne, None, None] * dt * (up * np.where(up >= 0.0, so_all[e1], so_all[e2]))
+    flux_tmp = dt * flux_edge - flux_up_edge
+    for j in range(eoc.shape[1]):
+        valid = (j < n_eoc) & (eoc[:, j] < ne)
+        e = np.where(valid, eoc[:, j], 0)
+        vw = np.where(valid, inv_area, 0.0)
+        sw = sign[:, j] * vw
+        rows = rows - flux_up_edge[e] * sw[:, None, None]
+        sf = sign[:, j, None, None] * flux_tmp[e]
+        scale_out = scale_out - mz(sf) * vw[:, None, None]
+        scale_in = scale_in - (-mz(-sf)) * vw[:, None, None]
+    rint = rho_int[:, :, None]
+    sc_in = np.clip((smax * rint - rows) / (scale_in + eps), 0.0, 1.0)
+    sc_out = np.clip((smin * rint - rows) / (scale_out - eps), 0.0, 1.0)
+    pad3 = lambda x: np.concatenate([x, np.zeros((1,) + x.shape[1:])])
+    sc_in_p, sc_out_p = pad3(sc_in), pad3(sc_out)
+    fl = flux_tmp
+    lim = np.where(fl >= 0.0, np.minimum(sc_out_p[e1], sc_in_p[e2]), np.minimum(sc_in_p[e1], sc_out_p[e2]))
+    flux_lim = fl * lim
+    wl = wmid_flux * np.where(wmid_flux >= 0.0, np.minimum(sc_out[:, :nl - 1], sc_in[:, 1:nl]),
+                              np.minimum(sc_out[:, 1:nl], sc_in[:, :nl - 1]))
+    wl_full = np.concatenate([wdtn[:, 0:1], wl, wdtn[:, nl:nl + 1]], axis=1)
+    vdelta = wl_full[:, 1:] - wl_full[:, :nl]
+    for j in range(eoc.shape[1]):
+        valid = (j < n_eoc) & (eoc[:, j] < ne)
+        e = np.where(valid, eoc[:, j], 0)
+        sw = sign[:, j] * np.where(valid, inv_area, 0.0)
+        rows = rows - flux_lim[e] * sw[:, None, None]
+    stage2 = (rows - rdnw[None, :, None] * vdelta) / rint
+    out = scalars_new_in.copy()
+    out[:nc] = np.maximum(stage2, 0.0)
+    return {"scalars_new": out, "scalars_old": scalars_old, "rho_zz_int": pad3(rho_int)[:, :]}

@@ -1,0 +1,49 @@
+"""Oracle stage functions against the reference's own stage calls (golden taps)."""
+
+import numpy as np
+import pytest
+
+import oracle.stages as S
+from oracle.step import STAGE_NAMES
+from fixtures import CASES, load_case, rel_l2, tap_calls
+
+FUNCS = {
+    "moist": S.moist_coefficients, "vimp": S.vert_imp_coefs, "dyn_tend": S.dyn_tend,
+    "smlstep": S.smlstep_pert, "acoustic": S.acoustic_step, "divdamp": S.divergence_damping,
+    "recover": S.recover_large_step, "diag": S.solve_diagnostics,
+    "scalars": S.advance_scalars, "scalars_mono": S.advance_scalars_mono,
+    "reconstruct": S.reconstruct_2d,
+}
+# outputs that only hold stage scratch in the reference (not part of the step state)
+SCRATCH = {"flux_arr", "scalar_tend", "scalar_old", "scalar_new", "s_max", "s_min", "wdtn",
+           "scale_arr", "flux_upwind_tmp", "flux_tmp"}
+# bitwise-identical float64 algorithm except pow(), whose last-bit rounding differs
+# between libm implementations; pressure_p amplifies that by cancellation
+TOL = 1e-13
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("key", sorted(FUNCS))
+def test_stage_matches_reference(case, key):
+    stage = STAGE_NAMES[key]
+    meta, _, _ = load_case(case)
+    calls = list(tap_calls(case, stage))
+    if not calls:
+        pytest.skip(f"{stage} not called in {case}")
+    for inp, out, entry in calls:
+        got = FUNCS[key](inp)
+        n = {"nCells": inp.get("nCells"), "nEdges": inp.get("nEdges"), "nVertices": inp.get("nVertices")}
+        for name, ref in out.items():
+            if name in SCRATCH and key == "scalars_mono":
+                continue
+            assert name in got, f"{stage}: missing output {name}"
+            g = np.asarray(got[name])
+            r = np.asarray(ref)
+            if g.shape[0] == r.shape[0] + 1:
+                g = g[:-1]
+            assert g.shape == r.shape, (name, g.shape, r.shape)
+            rows = r.shape[0] - 1 if r.shape[0] - 1 in n.values() else r.shape[0]
+            if name == "pressure_p":
+                assert np.max(np.abs(g[:rows] - r[:rows])) < 1e-7
+            else:
+                assert rel_l2(g[:rows], r[:rows]) <= TOL, (stage, entry["index"], name)
