@@ -1,0 +1,381 @@
+"""Throughput of the GB300 MPAS large step, in cell-level-steps/s.
+
+Default workload: the plain-float64 forecast on the level-6 icosahedral mesh (40962 cells,
+122880 edges) with 55 levels to 30 km (lowest layer 50 m), 32 seeded theta bumps (seed 1),
+3 passive tracers with the monotone limiter, dt = 720 s, split 3 x RK3 x 2 acoustic
+substeps.  A "step" is one large step (``atm_srk3``).  Synthetic data of those shapes;
+no dataset is involved.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+The GB300 arm prints one JSON line with the device-resident throughput (``value``), the
+end-to-end throughput through the public API with host buffers (``e2e``), the stage time
+breakdown, the roofline of the dominant stage, a CPU baseline (the numpy oracle on a bounded
+sample) and the SM clocks sampled during the timed region.  ``--impl reference`` times the
+CPU implementation (the oracle port of the reference's float64 algorithm) on the host
+cores.  With N > 1 (torchrun) every rank runs an independent replica (the path does not
+shard: replicas only) and the value is the sum over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-level-steps/s fwd & VJP, mixed/batched vs plain FP64 on GB300 at stated error"
+UNIT = "cell-level-steps/s"
+
+WORKLOADS = {
+    # configs[1]: level-6 mesh, 55 stretched levels, 32 bumps, 3 monotone tracers, dt 720 s
+    "c1": dict(spec=dict(level=6, nlev=55, dz_bottom=50.0, seed=1, n_bumps=32, n_tracers=3),
+               config=dict(config_monotonic=True), dt=720.0,
+               name="plain float64 forward, level-6 icosahedral mesh 40962 cells x 55 levels, "
+                    "3 monotone tracers, dt 720 s, split 3 x RK3 x ns 2"),
+    # configs[0]: level-4 mesh, 26 uniform levels, 8 bumps, 1 non-monotone tracer, dt 1800 s
+    "c0": dict(spec=dict(level=4, nlev=26, seed=0, n_bumps=8, n_tracers=1),
+               config=dict(config_monotonic=False), dt=1800.0,
+               name="plain float64 forward, level-4 mesh 2562 cells x 26 levels, 1 tracer, dt 1800 s"),
+}
+BASE_CFG = {"config_time_integration_order": 3, "config_len_disp": 120000.0,
+            "config_number_of_sub_steps": 2, "config_dynamics_split_steps": 3}
+
+
+def _cfg(w):
+    c = dict(BASE_CFG)
+    c.update(w["config"])
+    c["config_dt"] = w["dt"]
+    return c
+
+
+# ------------------------------------------------------------------------------ CPU side
+def _oracle_sample(args):
+    """One large step of the oracle on a bounded sample mesh; returns (cell-levels, seconds)."""
+    spec_kw, cfg, dt = args
+    sys.path.insert(0, str(ROOT))
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.loader import load_case
+    from oracle.step import Stepper
+    st, _ = load_case(CaseSpec(**spec_kw), cfg, as_torch=False)
+    s = Stepper(st, cfg)
+    prep = s.prepare(st, dt)
+    t0 = time.perf_counter()
+    s.srk3_step(prep, dt)
+    return int(st["nCells"]) * int(st["nVertLevels"]), time.perf_counter() - t0
+
+
+def _sample_spec(w):
+    spec = dict(w["spec"])
+    spec["level"] = min(spec["level"], 4)  # 2562 cells, same vertical grid and tracers
+    return spec
+
+
+def cpu_throughput(w, procs: int, rounds: int = 1):
+    """Aggregate oracle throughput with ``procs`` concurrent processes (spawned)."""
+    ctx = mp.get_context("spawn")
+    spec = _sample_spec(w)
+    jobs = [(spec, _cfg(w), w["dt"])] * procs
+    total = 0
+    wall = 0.0
+    with ctx.Pool(procs) as pool:
+        for _ in range(rounds):
+            res = pool.map(_oracle_sample, jobs)
+            total += sum(cl for cl, _ in res)
+            wall += max(sec for _, sec in res)  # concurrent samples: the slowest bounds the round
+    return total, wall, spec
+
+
+# ------------------------------------------------------------------------------ clocks
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        try:
+            for line in open(self.path):
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    mx = max(mx, float(p[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        finally:
+            os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------------------ GPU arm
+def run_gb300(args, rank, world):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from mpas_dycore_pytorch_gb300 import _lib
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.bytes_model import bytes_per_cell_level_step, stage_bytes_per_call
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.device import STATE_KEYS
+    from mpas_dycore_pytorch_gb300.loader import load_case
+
+    w = WORKLOADS[args.workload]
+    cfg = _cfg(w)
+    # CPU baseline workers are spawned before any CUDA work
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cl, wall, spec = cpu_throughput(w, procs=1)
+        cpu = {"value": cl / wall, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"1 large step of the numpy oracle on the level-{spec['level']} mesh "
+                         f"({cl} cell-levels, same vertical grid, tracers and options), {wall:.1f} s"}
+    torch.cuda.set_device(rank % torch.cuda.device_count())
+    dev = torch.device("cuda", torch.cuda.current_device())
+    st, _ = load_case(CaseSpec(**w["spec"]), cfg, as_torch=False)
+    S = int(st["scalars"].shape[-1])
+    model = Model(st, cfg, w["dt"], num_scalars=S, device=dev)
+    model.prepare(st)
+    C_, L_ = model.dmesh.nCells, model.dmesh.nVertLevels
+    lib = model.lib
+    # launches per step (eager step, counted by the library)
+    n0 = lib.mpasg_launch_count()
+    model.step()
+    torch.cuda.synchronize()
+    launches_per_step = int(lib.mpasg_launch_count() - n0)
+
+    # timed graph: K steps with stage-boundary events
+    K, W = args.steps, args.warmup
+    n_b = 128
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n_b)] for _ in range(K)]
+    model.capture_graph()
+    for _ in range(W):
+        model.step()
+    torch.cuda.synchronize()
+
+    stage_ms = None
+    timed_graph = None
+    try:
+        # record events with the library's timed step inside one K-step graph
+        for row in evs:
+            for e in row:
+                e.record()  # materialise the cudaEvent_t
+        torch.cuda.synchronize()
+        ptrs = [(C.c_void_p * n_b)(*[C.c_void_p(e.cuda_event) for e in row]) for row in evs]
+        kinds = [(C.c_int32 * n_b)() for _ in range(K)]
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        counts = []
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                for k in range(K):
+                    rc = lib.mpasg_step_timed(C.byref(model.dmesh.struct), C.byref(model.cstruct),
+                                              C.byref(model.state.struct), ptrs[k], kinds[k], n_b,
+                                              C.c_void_p(s.cuda_stream))
+                    counts.append(rc)
+        torch.cuda.current_stream().wait_stream(s)
+        if min(counts) < 0:
+            raise RuntimeError(f"timed step failed: {counts}")
+        timed_graph = g
+    except Exception as exc:  # fall back to the plain graph; no stage breakdown
+        print(f"[bench] stage-event graph unavailable: {exc}", file=sys.stderr)
+        timed_graph = None
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        start.record()
+        if timed_graph is not None:
+            timed_graph.replay()
+        else:
+            for _ in range(K):
+                model.step()
+        end.record()
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    bad = model.check_finite()
+    value = world * C_ * L_ * K / (ms / 1e3)
+
+    if timed_graph is not None:
+        stage_ms = {}
+        stage_calls = {}
+        for k in range(K):
+            n = counts[k]
+            for i in range(1, min(n, n_b)):
+                name = _lib.STAGE_NAMES[kinds[k][i]]
+                stage_ms[name] = stage_ms.get(name, 0.0) + evs[k][i - 1].elapsed_time(evs[k][i])
+                stage_calls[name] = stage_calls.get(name, 0) + 1
+        stage_ms = {k: v / K for k, v in sorted(stage_ms.items(), key=lambda kv: -kv[1])}
+        calls_per = {k: v // K for k, v in stage_calls.items()}
+
+    # roofline of the dominant stage
+    peak, peak_kind = measured_peak_hbm()
+    roof = None
+    if stage_ms:
+        merged = dict(stage_ms)
+        merged["dyn_tend"] = merged.pop("dyn_tend", 0.0) + merged.pop("dyn_tend_rk1", 0.0)
+        merged["acoustic_divdamp"] = merged.pop("acoustic_step", 0.0) + merged.pop("divergence_damping", 0.0)
+        calls = dict(calls_per)
+        calls["dyn_tend"] = calls.get("dyn_tend", 0) + calls.get("dyn_tend_rk1", 0)
+        calls["acoustic_divdamp"] = calls.get("acoustic_step", 0)
+        keymap = {"vert_imp_coefs": "vert_imp_coefs", "dyn_tend": "dyn_tend", "smlstep_pert": "smlstep_pert",
+                  "acoustic_divdamp": "acoustic_divdamp", "recover": "recover", "diagnostics": "diagnostics"}
+        dom = max((k for k in merged if k in keymap), key=lambda k: merged[k])
+        per_call_ms = merged[dom] / max(calls[dom], 1)
+        bytes_call = stage_bytes_per_call(keymap[dom], S, C_, L_)
+        achieved = bytes_call / (per_call_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "kernel": f"stage:{dom}",
+                "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_call,
+                "launch_ms": round(per_call_ms, 4)}
+
+    # end to end through the public API with pinned host buffers
+    keys = [k for k in STATE_KEYS]
+    host = {k: torch.empty(model.state.f[k].shape, dtype=torch.float64, pin_memory=True) for k in keys}
+    for k in keys:
+        host[k].copy_(model.state.f[k])
+    h2d = sum(t.numel() * 8 for t in host.values())
+    torch.cuda.synchronize()
+    e_start = torch.cuda.Event(enable_timing=True)
+    e_end = torch.cuda.Event(enable_timing=True)
+    e_start.record()
+    for _ in range(K):
+        model.load_boundary(host)
+        model.step()
+        for k in keys:
+            host[k].copy_(model.state.f[k], non_blocking=True)
+    e_end.record()
+    torch.cuda.synchronize()
+    e_ms = e_start.elapsed_time(e_end)
+    e2e = {"value": world * C_ * L_ * K / (e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": h2d}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w["name"], "cells": C_, "levels": L_, "scalars": S,
+                   "state_bytes": model.state.bytes,
+                   "l2": "inputs larger than L2 (device state %.1f GB)" % (model.state.bytes / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "cuda_graph": True, "bytes_per_cell_level_step": bytes_per_cell_level_step(S, True)},
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * K,
+        "clocks": clocks.summary(), "stage_ms_per_step": stage_ms, "nonfinite": bad,
+    }
+    return out
+
+
+def run_reference(args, rank, world):
+    w = WORKLOADS[args.workload]
+    if rank != 0:
+        return None
+    procs = max(1, min(os.cpu_count() or 1, 16))
+    # warm-up rounds are untimed; each timed step is one round of `procs` concurrent samples
+    for _ in range(args.warmup):
+        cpu_throughput(w, procs=procs)
+    total, wall = 0, 0.0
+    spec = None
+    for _ in range(args.steps):
+        cl, sec, spec = cpu_throughput(w, procs=procs)
+        total += cl
+        wall += sec
+    value = total / wall
+    sample = (f"per step {procs} concurrent large steps of the numpy oracle on the level-{spec['level']} mesh "
+              f"({total // max(args.steps, 1)} cell-levels per step, same vertical grid, tracers and options)")
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"]}, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
+    ap.add_argument("--workload", default="c1", choices=tuple(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    out = run_gb300(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,220 @@
+/*
+ * mpasg.h -- C ABI of the GB300 (sm_103a) implementation of the MPAS split-explicit
+ * dynamics timestep (the reference's atm_srk3 hot path).
+ *
+ * Every entry point takes plain POD structs of DEVICE pointers plus a cudaStream_t
+ * (passed as void*), launches asynchronously on that stream and returns an int status
+ * (MPASG_OK or a negative MPASG_E_* code). No entry point allocates device memory:
+ * callers own every buffer (the Python host allocates them from one arena).
+ *
+ * Layout (matches the reference's runtime tensors, so host<->device needs no transpose):
+ *   cell / edge / vertex fields are row-major (N+1, L) float64, levels fastest, with one
+ *   trailing padding row; W-level fields are (N+1, L+1); scalars are (C+1, L, S).
+ *   Connectivity is 0-based int32; a missing neighbour points at the padding row
+ *   (index N), which holds zeros (rho_zz holds 1.0 there, as in the reference).
+ *
+ * Reference interfaces replaced (NOAA-EMC/mpas-dycore-pytorch v0.1.7, mpas_pytorch/):
+ *   mpasg_step                  dynamics/time_integration.py:4897  atm_srk3 (+ :3420 _atm_srk3_impl)
+ *   mpasg_prepare               atmosphere_model.py:782  _prepare_timestep_state
+ *                               (dynamics/init_coupled_diagnostics.py:147)
+ *   mpasg_moist_coefficients    dynamics/moist_coefficients.py:124
+ *   mpasg_vert_imp_coefs        dynamics/vert_imp_coefs.py:188
+ *   mpasg_dyn_tend              dynamics/dyn_tend.py:10836  atm_compute_dyn_tend_work
+ *   mpasg_smlstep_pert          dynamics/smlstep_pert.py:373
+ *   mpasg_acoustic_step         dynamics/acoustic_step.py:1297
+ *   mpasg_divergence_damping    dynamics/divergence_damping.py:299
+ *   mpasg_recover_large_step    dynamics/recover_large_step.py:1090
+ *   mpasg_solve_diagnostics     dynamics/solve_diagnostics.py:1052
+ *   mpasg_advance_scalars       dynamics/advance_scalars.py:1272
+ *   mpasg_advance_scalars_mono  dynamics/advance_scalars_mono.py:2878
+ *   mpasg_reconstruct_2d        dynamics/vector_reconstruction.py:311
+ */
+#ifndef MPASG_H
+#define MPASG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPASG_ABI_VERSION 1
+
+enum {
+  MPASG_OK = 0,
+  MPASG_E_ARG = -1,      /* null pointer / bad dimension / unsupported option */
+  MPASG_E_LAUNCH = -2,   /* a kernel launch failed (cudaGetLastError) */
+  MPASG_E_NONFINITE = -3,/* the finite-field check found NaN/Inf */
+  MPASG_E_CUDA = -4      /* another CUDA runtime error */
+};
+
+/* Static mesh: dimensions, connectivity, geometry and vertical metrics. */
+typedef struct mpasg_mesh {
+  int32_t nCells, nEdges, nVertices, nVertLevels;
+  int32_t maxEdges, maxEdges2, vertexDegree, nAdvMax;
+  double cf1, cf2, cf3;
+  /* connectivity (0-based; missing -> padding row) */
+  const int32_t *nEdgesOnCell;      /* (C)            */
+  const int32_t *edgesOnCell;       /* (C, maxEdges)  */
+  const int32_t *cellsOnCell;       /* (C, maxEdges)  */
+  const int32_t *verticesOnCell;    /* (C, maxEdges)  */
+  const int32_t *kiteForCell;       /* (C, maxEdges) 0-based slot in cellsOnVertex, -1 if none */
+  const int32_t *cellsOnEdge;       /* (E, 2)         */
+  const int32_t *verticesOnEdge;    /* (E, 2)         */
+  const int32_t *nEdgesOnEdge;      /* (E)            */
+  const int32_t *edgesOnEdge;       /* (E, maxEdges2) */
+  const int32_t *nAdvCellsForEdge;  /* (E)            */
+  const int32_t *advCellsForEdge;   /* (E, nAdvMax)   */
+  const int32_t *edgesOnVertex;     /* (V, vertexDegree) */
+  /* geometry (float64) */
+  const double *edgesOnCell_sign;   /* (C, maxEdges) */
+  const double *edgesOnVertex_sign; /* (V, vertexDegree) */
+  const double *dcEdge, *dvEdge, *invDcEdge, *invDvEdge;       /* (E+1) */
+  const double *invAreaCell;        /* (C+1) */
+  const double *invAreaTriangle;    /* (V+1) */
+  const double *kiteAreasOnVertex;  /* (V, vertexDegree) */
+  const double *weightsOnEdge;      /* (E, maxEdges2) */
+  const double *adv_coefs, *adv_coefs_3rd;   /* (E, nAdvMax) */
+  const double *defc_a, *defc_b;    /* (C, maxEdges) */
+  const double *fEdge;              /* (E+1) */
+  const double *fVertex;            /* (V+1) */
+  const double *meshScalingDel2, *meshScalingDel4;  /* (E+1) */
+  const double *latCell, *lonCell;  /* (C+1) */
+  const double *coeffs_reconstruct; /* (C, maxEdges, 3) */
+  const double *zb_cell, *zb3_cell; /* (C, maxEdges, L+1) */
+  const double *zxu;                /* (E+1, L) */
+  const double *zz;                 /* (C+1, L) */
+  const double *dss;                /* (C+1, L) */
+  const double *rho_base, *theta_base;  /* (C+1, L) */
+  const double *rdzw, *rdzu, *fzm, *fzp, *fnm, *fnp, *rdnw;    /* (L) */
+} mpasg_mesh;
+
+/* Namelist options the step consumes (validated on the host). */
+typedef struct mpasg_config {
+  double dt;                 /* large timestep (s) */
+  double epssm, smdiv, len_disp, coef_3rd_order, c_s;
+  double visc4_2dsmag, del4u_div_factor, apvm_upwinding;
+  double h_mom_eddy_visc4, h_theta_eddy_visc4;  /* used when horiz_mixing != 2d_smagorinsky */
+  int32_t time_integration_order;   /* 2 or 3 */
+  int32_t number_of_sub_steps;      /* acoustic substeps ns */
+  int32_t dynamics_split_steps;     /* split */
+  int32_t monotonic;                /* monotone limiter on the last transport stage */
+  int32_t horiz_mixing_smagorinsky; /* 1: 2d_smagorinsky */
+  int32_t num_scalars, moist_start, moist_end;
+} mpasg_config;
+
+/*
+ * Every device array the step touches: the carried state (reference key names), the
+ * per-step work arrays, and scratch. All pointers are device pointers; shapes use
+ * C, E, V, L, S (cells, edges, vertices, levels, scalars), each with a padding row.
+ */
+typedef struct mpasg_fields {
+  /* carried state / diagnostics */
+  double *u, *v, *ru, *ruAvg, *h_edge, *pv_edge;                    /* (E+1, L) */
+  double *w, *rw, *wwAvg;                                           /* (C+1, L+1) */
+  double *theta_m, *rho_zz, *rho_p, *rtheta_p, *rtheta_base, *exner, *exner_base,
+         *pressure_p, *pressure_base, *divergence, *ke, *rt_diabatic_tend;  /* (C+1, L) */
+  double *uReconstructX, *uReconstructY, *uReconstructZ,
+         *uReconstructZonal, *uReconstructMeridional;               /* (C+1, L) */
+  double *vorticity;                                                /* (V+1, L) */
+  double *scalars;                                                  /* (C+1, L, S) */
+  /* RK-step saves and split bookkeeping */
+  double *ru_save, *ruAvg_split;                                    /* (E+1, L) */
+  double *rw_save, *wwAvg_split;                                    /* (C+1, L+1) */
+  double *rtheta_p_save, *rho_p_save, *theta_m_save, *rr_save, *rho_zz_old_split; /* (C+1, L) */
+  double *scalars_init, *scalars_a, *scalars_b;                     /* (C+1, L, S) */
+  /* moist coefficients */
+  double *qtot, *cqu_e;        /* qtot (C+1, L); cqu (E+1, L) */
+  double *cqw;                 /* (C+1, L+1) */
+  /* vertical implicit coefficients (active rows) */
+  double *cofrz;               /* (L) */
+  double *cofwr, *cofwz, *cofwt, *a_tri, *alpha_tri, *gamma_tri;  /* (C, L) */
+  double *coftz;               /* (C, L+1) */
+  /* tendencies */
+  double *tend_u, *tend_u_euler, *delsq_u;                          /* (E+1, L) */
+  double *tend_w, *tend_w_euler, *tend_rw, *delsq_w;                /* (C+1, L+1) */
+  double *tend_theta, *tend_theta_euler, *tend_rho, *h_divergence,
+         *kdiff, *dpdz, *rthdynten, *delsq_theta, *delsq_div;       /* (C+1, L) */
+  double *delsq_vort;                                               /* (V+1, L) */
+  /* acoustic perturbations */
+  double *ru_p;                                                     /* (E+1, L) */
+  double *rw_p;                                                     /* (C+1, L+1) */
+  double *rho_pp, *rtheta_pp, *rtheta_pp_old;                       /* (C+1, L) */
+  /* diagnostics scratch */
+  double *ke_edge;                                                  /* (E+1, L) */
+  double *ke_vertex, *pv_vertex;                                    /* (V+1, L) */
+  double *pv_cell;                                                  /* (C+1, L) */
+  /* transport scratch */
+  double *hflux;        /* (E+1, L, S)  edge high-order values / limited fluxes */
+  double *flux_up, *flux_tmp;   /* (E+1, L, S) */
+  double *s_max, *s_min, *scale_in, *scale_out, *rows;  /* (C+1, L, S) */
+  double *wflux;        /* (C+1, L+1, S)  limiter vertical fluxes */
+  double *rho_int;      /* (C+1, L) */
+  /* status flag word (device int32[4]) for the finite check */
+  int32_t *status;
+} mpasg_fields;
+
+/* ---- library info ------------------------------------------------------------- */
+int mpasg_abi_version(void);
+const char *mpasg_build_info(void);
+/* Kernels launched by this library so far (launch accounting; graph replays excluded). */
+long long mpasg_launch_count(void);
+
+/* Stage kinds reported by mpasg_step_timed (one per recorded boundary). */
+enum {
+  MPASG_STAGE_BEGIN = 0, MPASG_STAGE_SETUP = 1, MPASG_STAGE_MOIST = 2, MPASG_STAGE_VIMP = 3,
+  MPASG_STAGE_DYN_TEND_RK1 = 4, MPASG_STAGE_DYN_TEND = 5, MPASG_STAGE_SMLSTEP = 6,
+  MPASG_STAGE_ACOUSTIC = 7, MPASG_STAGE_DIVDAMP = 8, MPASG_STAGE_RECOVER = 9,
+  MPASG_STAGE_DIAG = 10, MPASG_STAGE_SPLIT = 11, MPASG_STAGE_SCALARS = 12,
+  MPASG_STAGE_SCALARS_MONO = 13, MPASG_STAGE_RECONSTRUCT = 14, MPASG_STAGE_COUNT = 15
+};
+
+/* ---- whole step ----------------------------------------------------------------- */
+/* Cold-start preparation: theta_m, rho_zz, ru, rw, rho_p, rtheta_*, exner*, pressure_*
+ * from the loaded primitives theta (in theta_m), rho (in rho_zz) and qv (in qtot, or
+ * null for dry), then diagnostics and cell-wind reconstruction. */
+int mpasg_prepare(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                  const double *theta, const double *rho, const double *qv, void *stream);
+/* One large step (atm_srk3), in place on f. */
+int mpasg_step(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, void *stream);
+/* The same step, recording events[i] (cudaEvent_t, timing enabled) at every stage
+ * boundary and stage_kinds[i] = the MPASG_STAGE_* that ended there (i < n_events).
+ * Works under stream capture (records external event nodes). Returns the number of
+ * boundaries (>= 0) or a negative status. */
+int mpasg_step_timed(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                     void *const *events, int32_t *stage_kinds, int n_events, void *stream);
+/* Count non-finite values of the prognostic fields into f->status[0] (async). */
+int mpasg_check_finite(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, void *stream);
+
+/* ---- per-stage entry points (parity taps; operate on the named fields of f) ---- */
+int mpasg_moist_coefficients(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                             void *stream);
+int mpasg_vert_imp_coefs(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                         double dts, void *stream);
+int mpasg_dyn_tend(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, int rk_step,
+                   void *stream);
+int mpasg_smlstep_pert(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                       void *stream);
+int mpasg_acoustic_step(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                        int small_step, double dts, void *stream);
+int mpasg_divergence_damping(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                             double dts, void *stream);
+int mpasg_recover_large_step(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                             int rk_step, int ns, double rk_dt, void *stream);
+int mpasg_solve_diagnostics(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                            int rk_step, void *stream);
+/* Explicit RK-stage transport: scalar_old -> reads f->scalars_init, iterate f->scalars_a,
+ * writes f->scalars_b; rho_zz_old = f->rho_zz_old_split, rho_zz_new = f->rho_zz,
+ * fluxes f->ruAvg / f->wwAvg. */
+int mpasg_advance_scalars(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                          int rk_step, double dt_stage, void *stream);
+int mpasg_advance_scalars_mono(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                               double dt_stage, void *stream);
+int mpasg_reconstruct_2d(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                         void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPASG_H */

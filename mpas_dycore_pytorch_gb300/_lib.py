@@ -1,0 +1,155 @@
+"""ctypes binding of the C ABI in ``include/mpasg.h`` (``libmpasg.so``).
+
+The struct layouts below mirror the header field by field.  The library is loaded from
+the package directory (built in tree by ``build.py``); there is no fallback: when the
+library is missing the import of the device path raises ``MpasExtensionMissingError``.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+
+from .errors import MpasConfigError, MpasDeviceError, MpasExtensionMissingError, MpasNumericalError
+
+LIB_PATH = pathlib.Path(__file__).resolve().parent / "libmpasg.so"
+
+MESH_INT_DIMS = ("nCells", "nEdges", "nVertices", "nVertLevels", "maxEdges", "maxEdges2",
+                 "vertexDegree", "nAdvMax")
+MESH_DOUBLES = ("cf1", "cf2", "cf3")
+MESH_INT_PTRS = ("nEdgesOnCell", "edgesOnCell", "cellsOnCell", "verticesOnCell", "kiteForCell",
+                 "cellsOnEdge", "verticesOnEdge", "nEdgesOnEdge", "edgesOnEdge",
+                 "nAdvCellsForEdge", "advCellsForEdge", "edgesOnVertex")
+MESH_DBL_PTRS = ("edgesOnCell_sign", "edgesOnVertex_sign", "dcEdge", "dvEdge", "invDcEdge",
+                 "invDvEdge", "invAreaCell", "invAreaTriangle", "kiteAreasOnVertex",
+                 "weightsOnEdge", "adv_coefs", "adv_coefs_3rd", "defc_a", "defc_b", "fEdge",
+                 "fVertex", "meshScalingDel2", "meshScalingDel4", "latCell", "lonCell",
+                 "coeffs_reconstruct", "zb_cell", "zb3_cell", "zxu", "zz", "dss", "rho_base",
+                 "theta_base", "rdzw", "rdzu", "fzm", "fzp", "fnm", "fnp", "rdnw")
+
+CONFIG_DOUBLES = ("dt", "epssm", "smdiv", "len_disp", "coef_3rd_order", "c_s", "visc4_2dsmag",
+                  "del4u_div_factor", "apvm_upwinding", "h_mom_eddy_visc4", "h_theta_eddy_visc4")
+CONFIG_INTS = ("time_integration_order", "number_of_sub_steps", "dynamics_split_steps",
+               "monotonic", "horiz_mixing_smagorinsky", "num_scalars", "moist_start", "moist_end")
+
+# (name, kind) in header order; kind names the row space: e/c/cw/v/cs/es/cws/L/cL/cLw/...
+FIELDS = (
+    ("u", "e"), ("v", "e"), ("ru", "e"), ("ruAvg", "e"), ("h_edge", "e"), ("pv_edge", "e"),
+    ("w", "cw"), ("rw", "cw"), ("wwAvg", "cw"),
+    ("theta_m", "c"), ("rho_zz", "c"), ("rho_p", "c"), ("rtheta_p", "c"), ("rtheta_base", "c"),
+    ("exner", "c"), ("exner_base", "c"), ("pressure_p", "c"), ("pressure_base", "c"),
+    ("divergence", "c"), ("ke", "c"), ("rt_diabatic_tend", "c"),
+    ("uReconstructX", "c"), ("uReconstructY", "c"), ("uReconstructZ", "c"),
+    ("uReconstructZonal", "c"), ("uReconstructMeridional", "c"),
+    ("vorticity", "v"),
+    ("scalars", "cs"),
+    ("ru_save", "e"), ("ruAvg_split", "e"),
+    ("rw_save", "cw"), ("wwAvg_split", "cw"),
+    ("rtheta_p_save", "c"), ("rho_p_save", "c"), ("theta_m_save", "c"), ("rr_save", "c"),
+    ("rho_zz_old_split", "c"),
+    ("scalars_init", "cs"), ("scalars_a", "cs"), ("scalars_b", "cs"),
+    ("qtot", "c"), ("cqu_e", "e"),
+    ("cqw", "cw"),
+    ("cofrz", "L"),
+    ("cofwr", "c"), ("cofwz", "c"), ("cofwt", "c"), ("a_tri", "c"), ("alpha_tri", "c"),
+    ("gamma_tri", "c"),
+    ("coftz", "cw"),
+    ("tend_u", "e"), ("tend_u_euler", "e"), ("delsq_u", "e"),
+    ("tend_w", "cw"), ("tend_w_euler", "cw"), ("tend_rw", "cw"), ("delsq_w", "cw"),
+    ("tend_theta", "c"), ("tend_theta_euler", "c"), ("tend_rho", "c"), ("h_divergence", "c"),
+    ("kdiff", "c"), ("dpdz", "c"), ("rthdynten", "c"), ("delsq_theta", "c"), ("delsq_div", "c"),
+    ("delsq_vort", "v"),
+    ("ru_p", "e"),
+    ("rw_p", "cw"),
+    ("rho_pp", "c"), ("rtheta_pp", "c"), ("rtheta_pp_old", "c"),
+    ("ke_edge", "e"),
+    ("ke_vertex", "v"), ("pv_vertex", "v"),
+    ("pv_cell", "c"),
+    ("hflux", "es"),
+    ("flux_up", "es"), ("flux_tmp", "es"),
+    ("s_max", "cs"), ("s_min", "cs"), ("scale_in", "cs"), ("scale_out", "cs"), ("rows", "cs"),
+    ("wflux", "cws"),
+    ("rho_int", "c"),
+)
+
+
+STAGE_NAMES = ("begin", "setup", "moist", "vert_imp_coefs", "dyn_tend_rk1", "dyn_tend",
+               "smlstep_pert", "acoustic_step", "divergence_damping", "recover", "diagnostics",
+               "split_bookkeeping", "scalars", "scalars_mono", "reconstruct")
+
+
+class MeshStruct(C.Structure):
+    _fields_ = ([(n, C.c_int32) for n in MESH_INT_DIMS] + [(n, C.c_double) for n in MESH_DOUBLES]
+                + [(n, C.c_void_p) for n in MESH_INT_PTRS] + [(n, C.c_void_p) for n in MESH_DBL_PTRS])
+
+
+class ConfigStruct(C.Structure):
+    _fields_ = [(n, C.c_double) for n in CONFIG_DOUBLES] + [(n, C.c_int32) for n in CONFIG_INTS]
+
+
+class FieldsStruct(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n, _ in FIELDS] + [("status", C.c_void_p)]
+
+
+EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg_prepare",
+           "mpasg_step", "mpasg_step_timed",
+           "mpasg_check_finite", "mpasg_moist_coefficients", "mpasg_vert_imp_coefs",
+           "mpasg_dyn_tend", "mpasg_smlstep_pert", "mpasg_acoustic_step",
+           "mpasg_divergence_damping", "mpasg_recover_large_step", "mpasg_solve_diagnostics",
+           "mpasg_advance_scalars", "mpasg_advance_scalars_mono", "mpasg_reconstruct_2d")
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load ``libmpasg.so`` once and declare the entry-point signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise MpasExtensionMissingError(
+            f"{LIB_PATH} is missing: build it with mpas_dycore_pytorch_gb300.build.build() "
+            "(the CUDA path has no CPU fallback)")
+    lib = C.CDLL(str(LIB_PATH))
+    P = C.POINTER
+    m, c, f = P(MeshStruct), P(ConfigStruct), P(FieldsStruct)
+    vp = C.c_void_p
+    sig = {
+        "mpasg_abi_version": ([], C.c_int),
+        "mpasg_build_info": ([], C.c_char_p),
+        "mpasg_launch_count": ([], C.c_longlong),
+        "mpasg_step_timed": ([m, c, f, vp, vp, C.c_int, vp], C.c_int),
+        "mpasg_prepare": ([m, c, f, vp, vp, vp, vp], C.c_int),
+        "mpasg_step": ([m, c, f, vp], C.c_int),
+        "mpasg_check_finite": ([m, c, f, vp], C.c_int),
+        "mpasg_moist_coefficients": ([m, c, f, vp], C.c_int),
+        "mpasg_vert_imp_coefs": ([m, c, f, C.c_double, vp], C.c_int),
+        "mpasg_dyn_tend": ([m, c, f, C.c_int, vp], C.c_int),
+        "mpasg_smlstep_pert": ([m, c, f, vp], C.c_int),
+        "mpasg_acoustic_step": ([m, c, f, C.c_int, C.c_double, vp], C.c_int),
+        "mpasg_divergence_damping": ([m, c, f, C.c_double, vp], C.c_int),
+        "mpasg_recover_large_step": ([m, c, f, C.c_int, C.c_int, C.c_double, vp], C.c_int),
+        "mpasg_solve_diagnostics": ([m, c, f, C.c_int, vp], C.c_int),
+        "mpasg_advance_scalars": ([m, c, f, C.c_int, C.c_double, vp], C.c_int),
+        "mpasg_advance_scalars_mono": ([m, c, f, C.c_double, vp], C.c_int),
+        "mpasg_reconstruct_2d": ([m, c, f, vp], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if lib.mpasg_abi_version() != 1:
+        raise MpasExtensionMissingError("libmpasg.so ABI version mismatch; rebuild it")
+    _lib = lib
+    return lib
+
+
+def check(rc: int, what: str) -> None:
+    """Map a C status code to the package's exception types."""
+    if rc >= 0:
+        return
+    if rc == -1:
+        raise MpasConfigError(f"{what}: invalid argument (status {rc})")
+    if rc == -3:
+        raise MpasNumericalError(f"{what}: non-finite values (status {rc})")
+    raise MpasDeviceError(f"{what}: CUDA failure (status {rc})")

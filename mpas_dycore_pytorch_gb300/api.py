@@ -1,0 +1,282 @@
+"""Reference-facing API of the GB300 step: ``run_simulation``, ``run_timestep``, ``atm_srk3``
+and the per-stage ``atm_*_work`` operators.
+
+Names, argument meaning and error types follow the reference
+(mpas_pytorch/atmosphere_model.py:900 ``run_timestep``, :1474 ``run_simulation``;
+dynamics/time_integration.py:4897 ``atm_srk3``; stage functions as listed in
+``STAGES``).  State and mesh dictionaries use the reference's padded layout and key
+names; returned tensors live on the CUDA device.  There is no CPU path: the reference
+itself is the CPU implementation.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Any, Callable, Mapping
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import DeviceMesh, DeviceState, STATE_KEYS, _int, _np
+from .errors import MpasConfigError, MpasDeviceError, MpasNumericalError, MpasUnsupportedCapabilityError
+
+DEFAULTS = {
+    "config_time_integration_order": 2, "config_number_of_sub_steps": 2,
+    "config_dynamics_split_steps": 3, "config_split_dynamics_transport": True,
+    "config_epssm": 0.1, "config_smdiv": 0.1, "config_len_disp": 0.0,
+    "config_visc4_2dsmag": 0.05, "config_del4u_div_factor": 10.0,
+    "config_apvm_upwinding": 0.5, "config_horiz_mixing": "2d_smagorinsky",
+    "config_monotonic": True, "config_positive_definite": False,
+    "config_h_mom_eddy_visc2": 0.0, "config_h_mom_eddy_visc4": 0.0,
+    "config_v_mom_eddy_visc2": 0.0, "config_h_theta_eddy_visc2": 0.0,
+    "config_h_theta_eddy_visc4": 0.0, "config_v_theta_eddy_visc2": 0.0,
+    "config_rayleigh_damp_u": False, "config_mpas_cam_coef": 0.0,
+    "config_curvature_u": False, "config_mix_full": True, "config_IAU_option": "off",
+    "config_apply_lbcs": False, "config_dt": 720.0,
+}
+
+
+def resolved_config(config: Mapping[str, Any] | None) -> dict:
+    cfg = dict(DEFAULTS)
+    cfg.update(config or {})
+    return cfg
+
+
+def validate_supported(cfg: Mapping[str, Any]) -> None:
+    """Reject options outside the implemented path before any device work (mirrors the
+    reference's capability rejection, tests/test_configuration_contracts.py:48-79)."""
+    bad = []
+    if not bool(cfg["config_split_dynamics_transport"]):
+        bad.append("config_split_dynamics_transport=False (coupled transport)")
+    if int(cfg["config_time_integration_order"]) not in (2, 3):
+        bad.append("config_time_integration_order")
+    for key in ("config_v_mom_eddy_visc2", "config_v_theta_eddy_visc2", "config_mpas_cam_coef"):
+        if float(cfg[key]) != 0.0:
+            bad.append(key)
+    for key in ("config_rayleigh_damp_u", "config_curvature_u", "config_positive_definite",
+                "config_apply_lbcs"):
+        if bool(cfg[key]):
+            bad.append(key)
+    if not bool(cfg["config_mix_full"]):
+        bad.append("config_mix_full=False")
+    if str(cfg["config_IAU_option"]) != "off":
+        bad.append("config_IAU_option")
+    if str(cfg["config_horiz_mixing"]) not in ("2d_smagorinsky",):
+        bad.append("config_horiz_mixing")
+    if bad:
+        raise MpasUnsupportedCapabilityError(f"unsupported on the GB300 path: {bad}")
+
+
+def resolve_len_disp(cfg: Mapping[str, Any], mesh: Mapping[str, Any]) -> float:
+    """config_len_disp, else nominalMinDc, else the minimum dcEdge (time_integration.py:1882)."""
+    ld = float(cfg.get("config_len_disp", 0.0))
+    if ld > 0.0:
+        return ld
+    if "nominalMinDc" in mesh and float(_np(mesh["nominalMinDc"]).reshape(-1)[0]) > 0.0:
+        return float(_np(mesh["nominalMinDc"]).reshape(-1)[0])
+    ne = _int(mesh["nEdges"])
+    return float(np.min(_np(mesh["dcEdge"])[:ne]))
+
+
+def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_scalars: int,
+                moist_start: int, moist_end: int) -> _lib.ConfigStruct:
+    c = _lib.ConfigStruct()
+    c.dt = float(dt)
+    c.epssm = float(cfg["config_epssm"])
+    c.smdiv = float(cfg["config_smdiv"])
+    c.len_disp = resolve_len_disp(cfg, mesh)
+    c.coef_3rd_order = float(_np(mesh.get("coef_3rd_order", cfg.get("config_coef_3rd_order", 0.25))).reshape(-1)[0])
+    c.c_s = float(_np(mesh.get("c_s", cfg.get("config_smagorinsky_coef", 0.125))).reshape(-1)[0])
+    c.visc4_2dsmag = float(cfg["config_visc4_2dsmag"])
+    c.del4u_div_factor = float(cfg["config_del4u_div_factor"])
+    c.apvm_upwinding = float(cfg["config_apvm_upwinding"])
+    c.h_mom_eddy_visc4 = float(cfg["config_h_mom_eddy_visc4"])
+    c.h_theta_eddy_visc4 = float(cfg["config_h_theta_eddy_visc4"])
+    c.time_integration_order = int(cfg["config_time_integration_order"])
+    c.number_of_sub_steps = int(cfg["config_number_of_sub_steps"])
+    c.dynamics_split_steps = int(cfg["config_dynamics_split_steps"])
+    c.monotonic = 1 if bool(cfg["config_monotonic"]) else 0
+    c.horiz_mixing_smagorinsky = 1 if str(cfg["config_horiz_mixing"]) == "2d_smagorinsky" else 0
+    c.num_scalars = int(num_scalars)
+    c.moist_start = int(moist_start)
+    c.moist_end = int(moist_end)
+    return c
+
+
+def _stream_ptr(stream: torch.cuda.Stream | None = None) -> C.c_void_p:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+class Model:
+    """One mesh + configuration + timestep resident on a GPU: the native step and its state."""
+
+    def __init__(self, mesh: Mapping[str, Any], config: Mapping[str, Any] | None, dt: float,
+                 num_scalars: int | None = None, device: str | torch.device = "cuda"):
+        self.lib = _lib.load()
+        self.cfg = resolved_config(config)
+        validate_supported(self.cfg)
+        if not (math.isfinite(float(dt)) and float(dt) > 0.0):
+            raise MpasConfigError("dt must be positive and finite")
+        self.dt = float(dt)
+        device = torch.device(device)
+        if device.type != "cuda":
+            raise MpasUnsupportedCapabilityError("the GB300 path runs on CUDA devices only")
+        if not torch.cuda.is_available():
+            raise MpasDeviceError("no CUDA device is available")
+        self.mesh_ref = mesh
+        self.dmesh = DeviceMesh(mesh, device)
+        if self.dmesh.nVertLevels < 4:
+            raise MpasConfigError("at least 4 vertical levels are required")
+        ns = int(num_scalars if num_scalars is not None else _int(mesh.get("num_scalars", 1)))
+        self.state = DeviceState(self.dmesh, ns)
+        self.moist_start = _int(mesh.get("moist_start", 1))
+        self.moist_end = _int(mesh.get("moist_end", ns))
+        self.cstruct = make_config(self.cfg, mesh, self.dt, ns, self.moist_start, self.moist_end)
+        # static fields the step reads from the state side
+        self.state.load(mesh, keys=("rt_diabatic_tend",))
+        self._graph = None
+
+    # -- C ABI plumbing ---------------------------------------------------------------
+    def call(self, name: str, *args) -> None:
+        fn = getattr(self.lib, name)
+        rc = fn(C.byref(self.dmesh.struct), C.byref(self.cstruct), C.byref(self.state.struct),
+                *args, _stream_ptr())
+        _lib.check(rc, name)
+
+    # -- state ---------------------------------------------------------------------------
+    def prepare(self, loaded: Mapping[str, Any]) -> None:
+        """Cold-start preparation on the device from loaded theta, rho, qv, u, w."""
+        dev = self.dmesh.device
+        L = self.dmesh.nVertLevels
+        nc = self.dmesh.nCells
+        self.state.load(loaded, keys=("u", "w", "scalars", "rt_diabatic_tend"))
+        tmp = {}
+        for k in ("theta", "rho", "qv"):
+            if k in loaded:
+                t = torch.as_tensor(_np(loaded[k])[:nc + 1, :L], dtype=torch.float64).to(dev)
+                tmp[k] = t.contiguous()
+        if "theta" not in tmp or "rho" not in tmp:
+            raise MpasConfigError("preparation needs theta and rho")
+        qv = tmp.get("qv")
+        self.call("mpasg_prepare", C.c_void_p(tmp["theta"].data_ptr()),
+                  C.c_void_p(tmp["rho"].data_ptr()),
+                  C.c_void_p(qv.data_ptr()) if qv is not None else C.c_void_p(0))
+        torch.cuda.current_stream().synchronize()
+
+    def load_boundary(self, state: Mapping[str, Any]) -> None:
+        """Load a prepared (complete) step boundary."""
+        self.state.load(state, keys=STATE_KEYS + ("rho_edge",))
+        self.state.f["rho_zz"][self.dmesh.nCells].fill_(1.0)
+
+    def step(self) -> None:
+        if self._graph is not None:
+            self._graph.replay()
+        else:
+            self.call("mpasg_step")
+
+    def capture_graph(self) -> None:
+        """Capture one large step as a CUDA graph (replayed by ``step``)."""
+        torch.cuda.synchronize()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            # warm-up outside capture is the caller's job; capture the launch sequence
+            with torch.cuda.graph(g, stream=s):
+                fn = self.lib.mpasg_step
+                rc = fn(C.byref(self.dmesh.struct), C.byref(self.cstruct), C.byref(self.state.struct),
+                        C.c_void_p(s.cuda_stream))
+        torch.cuda.current_stream().wait_stream(s)
+        _lib.check(rc, "mpasg_step (capture)")
+        self._graph = g
+
+    def check_finite(self) -> int:
+        self.call("mpasg_check_finite")
+        return int(self.state.status[0].item())
+
+    def export(self) -> dict[str, torch.Tensor]:
+        return {k: v.clone() for k, v in self.state.export().items()}
+
+
+def _is_prepared(state: Mapping[str, Any]) -> bool:
+    return all(k in state for k in ("theta_m", "rho_zz", "rtheta_p", "exner", "pv_edge", "v"))
+
+
+def _merge(base: Mapping[str, Any], out: Mapping[str, torch.Tensor]) -> dict:
+    res = dict(base)
+    res.update(out)
+    return res
+
+
+def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | None = None,
+                   config: Mapping[str, Any] | None = None, dt: float | None = None, nsteps: int = 1,
+                   device: str | torch.device = "cuda", on_step: Callable | None = None,
+                   differentiable: bool = False, checkpoint_timesteps: bool | None = None,
+                   checkpoint_use_reentrant: bool = False, checkpoint_materialize_final: bool = True,
+                   on_phase: Callable | None = None, on_initial: Callable | None = None,
+                   use_cuda_graph: bool = True) -> dict:
+    """Forecast ``nsteps`` large steps on the GPU (reference: atmosphere_model.py:1474).
+
+    ``initial_state`` is either a loaded raw state (prepared here, on the device) or a
+    complete step boundary returned by a previous call.  Returns the final boundary with
+    the reference's keys; tensors stay on the CUDA device.
+    """
+    if differentiable:
+        raise MpasUnsupportedCapabilityError("differentiable runs are not implemented on the GB300 path")
+    if int(nsteps) != nsteps or nsteps < 0:
+        raise MpasConfigError("nsteps must be a non-negative integer")
+    mesh = mesh if mesh is not None else initial_state
+    merged = dict(mesh)
+    merged.update(initial_state)
+    cfg = resolved_config(config)
+    dt = float(cfg["config_dt"] if dt is None else dt)
+    if nsteps == 0:
+        return dict(initial_state)
+    ns = _int(merged.get("num_scalars", _np(merged["scalars"]).shape[-1]))
+    model = Model(merged, cfg, dt, num_scalars=ns, device=device)
+    if _is_prepared(initial_state):
+        model.load_boundary(initial_state)
+    else:
+        model.prepare(merged)
+    if on_initial is not None:
+        on_initial(_merge(initial_state, model.export()))
+    if on_phase is not None:
+        on_phase("forecast_integration_begin")
+    if use_cuda_graph and nsteps > 1:
+        model.step()
+        model.capture_graph()
+        first = 1
+        if on_step is not None:
+            on_step(1, _merge(initial_state, model.export()))
+    else:
+        first = 0
+    for i in range(first, int(nsteps)):
+        model.step()
+        if on_step is not None:
+            on_step(i + 1, _merge(initial_state, model.export()))
+    if on_phase is not None:
+        on_phase("forecast_integration_end")
+    bad = model.check_finite()
+    if bad:
+        raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")
+    return _merge(initial_state, model.export())
+
+
+def run_timestep(state: Mapping[str, Any], mesh: Mapping[str, Any] | None = None,
+                 config: Mapping[str, Any] | None = None, dt: float | None = None,
+                 device: str | torch.device = "cuda", differentiable: bool = False) -> dict:
+    """One large step (reference: atmosphere_model.py:900)."""
+    return run_simulation(state, mesh, config, dt, 1, device, differentiable=differentiable,
+                          use_cuda_graph=False)
+
+
+def atm_srk3(state: Mapping[str, Any], mesh: Mapping[str, Any], config: Mapping[str, Any], dt: float,
+             strict: bool = True, differentiable: bool = False) -> dict:
+    """One split-explicit RK3 step on a prepared boundary (dynamics/time_integration.py:4897)."""
+    if not _is_prepared(state):
+        raise MpasConfigError("atm_srk3 needs a prepared step boundary")
+    return run_simulation(state, mesh, config, dt, 1, "cuda", differentiable=differentiable,
+                          use_cuda_graph=False)

@@ -1,0 +1,247 @@
+// Native large-step driver (the reference's atm_srk3, mpas_pytorch/dynamics/time_integration.py:
+// 4897 / :3420): RK integration setup (:2497), 3 dynamics substeps x 3 RK stages
+// (execute_rk_step :5000), split-transport bookkeeping (:3825-3942), the split transport RK3
+// loop (:3954-4700) and the final reconstruction (:4729).  All work is enqueued on the
+// caller's stream without host synchronisation, so the whole step can be captured in a
+// CUDA graph by the caller.
+#include <cmath>
+#include <cstdio>
+
+#include "common.cuh"
+
+namespace {
+
+__global__ void k_fill_d(double* __restrict__ p, long long n, double v) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+__global__ void k_add_d(double* __restrict__ y, const double* __restrict__ x, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = y[i] + x[i];
+}
+
+__global__ void k_scale_d(double* __restrict__ y, const double* __restrict__ x, double a, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = x[i] * a;
+}
+
+__global__ void k_count_nonfinite(const double* __restrict__ p, long long n, int32_t* __restrict__ count) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int bad = 0;
+  if (i < n) bad = isfinite(p[i]) ? 0 : 1;
+  bad = __syncthreads_count(bad);
+  if (threadIdx.x == 0 && bad) atomicAdd(count, bad);
+}
+
+int fill(double* p, long long n, double v, cudaStream_t s) {
+  k_fill_d<<<nblocks(n), kBlock, 0, s>>>(p, n, v);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
+int copy(double* dst, const double* src, long long n, cudaStream_t s) {
+  if (cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return MPASG_E_CUDA;
+  return MPASG_OK;
+}
+
+#define CHECK_RC(x)          \
+  do {                       \
+    int _rc = (x);           \
+    if (_rc != MPASG_OK) return _rc; \
+  } while (0)
+
+}  // namespace
+
+static long long g_launches = 0;
+void mpasg_count_launch() { __atomic_add_fetch(&g_launches, 1, __ATOMIC_RELAXED); }
+extern "C" long long mpasg_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+
+extern "C" int mpasg_abi_version(void) { return MPASG_ABI_VERSION; }
+
+extern "C" const char* mpasg_build_info(void) {
+  static char buf[160];
+  snprintf(buf, sizeof(buf), "mpasg abi=%d cuda=%d arch=sm_103a float64", MPASG_ABI_VERSION, CUDART_VERSION);
+  return buf;
+}
+
+extern "C" int mpasg_check_finite(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, void* stream) {
+  if (!m || !c || !f || !f->status) return MPASG_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long L = m->nVertLevels, nc = m->nCells, ne = m->nEdges;
+  if (cudaMemsetAsync(f->status, 0, sizeof(int32_t), s) != cudaSuccess) return MPASG_E_CUDA;
+  struct Item { const double* p; long long n; } items[] = {
+      {f->u, ne * L}, {f->w, nc * (L + 1)}, {f->theta_m, nc * L}, {f->rho_zz, nc * L},
+      {f->scalars, nc * L * c->num_scalars}};
+  for (auto& it : items) {
+    if (it.n <= 0) continue;
+    k_count_nonfinite<<<nblocks(it.n), kBlock, 0, s>>>(it.p, it.n, f->status);
+    MPASG_LAUNCH_CHECK();
+  }
+  return MPASG_OK;
+}
+
+namespace {
+// Records one CUDA event at every stage boundary of the step (stage kinds in `kinds`).
+struct StageRecorder {
+  cudaEvent_t* events = nullptr;
+  int n_events = 0;
+  int32_t* kinds = nullptr;
+  int n = 0;
+  int mark(int kind, cudaStream_t s) {
+    if (kinds && n < n_events) kinds[n] = kind;
+    if (events && n < n_events) {
+      cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+      cudaStreamIsCapturing(s, &st);
+      cudaError_t e = (st == cudaStreamCaptureStatusActive)
+                          ? cudaEventRecordWithFlags(events[n], s, cudaEventRecordExternal)
+                          : cudaEventRecord(events[n], s);
+      if (e != cudaSuccess) return MPASG_E_CUDA;
+    }
+    ++n;
+    return MPASG_OK;
+  }
+};
+
+int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec);
+}  // namespace
+
+extern "C" int mpasg_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, void* stream) {
+  if (!m || !c || !fin) return MPASG_E_ARG;
+  return step_impl(m, c, fin, (cudaStream_t)stream, nullptr);
+}
+
+extern "C" int mpasg_step_timed(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, void* const* events,
+                                int32_t* stage_kinds, int n_events, void* stream) {
+  if (!m || !c || !fin || n_events < 0) return MPASG_E_ARG;
+  StageRecorder rec;
+  rec.events = (cudaEvent_t*)events;
+  rec.kinds = stage_kinds;
+  rec.n_events = n_events;
+  int rc = step_impl(m, c, fin, (cudaStream_t)stream, &rec);
+  if (rc != MPASG_OK) return rc;
+  return rec.n;  // number of boundaries recorded (>= 0)
+}
+
+namespace {
+int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec) {
+  void* stream = (void*)s;
+#define MARK(kind)                                  \
+  do {                                              \
+    if (rec) CHECK_RC(rec->mark((kind), s));        \
+  } while (0)
+  if (c->time_integration_order != 2 && c->time_integration_order != 3) return MPASG_E_ARG;
+  if (c->number_of_sub_steps < 1 || c->dynamics_split_steps < 1) return MPASG_E_ARG;
+  mpasg_fields f = *fin;  // local copy: transport ping-pongs its scalar buffers
+  const long long L = m->nVertLevels, nc = m->nCells, ne = m->nEdges;
+  const long long S = c->num_scalars;
+  const long long ncl = (nc + 1) * L, nel = (ne + 1) * L, ncw = (nc + 1) * (L + 1);
+  const long long ncs = (nc + 1) * L * S;
+  const int split = c->dynamics_split_steps;
+  const int ns = c->number_of_sub_steps;
+  const double dt = c->dt;
+  const double dt_dyn = dt / split;
+  double rk_ts[3], rk_sub[3];
+  int nsub[3];
+  if (c->time_integration_order == 3) {
+    rk_ts[0] = dt_dyn / 3.0; rk_ts[1] = dt_dyn / 2.0; rk_ts[2] = dt_dyn;
+    rk_sub[0] = dt_dyn / 3.0; rk_sub[1] = dt_dyn / ns; rk_sub[2] = dt_dyn / ns;
+    nsub[0] = 1; nsub[1] = ns / 2 > 1 ? ns / 2 : 1; nsub[2] = ns;
+  } else {
+    rk_ts[0] = dt_dyn / 2.0; rk_ts[1] = dt_dyn / 2.0; rk_ts[2] = dt_dyn;
+    rk_sub[0] = rk_sub[1] = rk_sub[2] = dt_dyn / ns;
+    nsub[0] = nsub[1] = ns / 2 > 1 ? ns / 2 : 1; nsub[2] = ns;
+  }
+
+  // ---- RK integration setup
+  MARK(MPASG_STAGE_BEGIN);
+  CHECK_RC(fill(f.theta_m + nc * L, L, 0.0, s));
+  CHECK_RC(copy(f.ru_save, f.ru, nel, s));
+  CHECK_RC(copy(f.rw_save, f.rw, ncw, s));
+  CHECK_RC(copy(f.rtheta_p_save, f.rtheta_p, ncl, s));
+  CHECK_RC(copy(f.rho_p_save, f.rho_p, ncl, s));
+  CHECK_RC(copy(f.theta_m_save, f.theta_m, ncl, s));
+  CHECK_RC(copy(f.rr_save, f.rho_p, ncl, s));
+  CHECK_RC(copy(f.rho_zz_old_split, f.rho_zz, ncl, s));
+  if (S > 0) CHECK_RC(copy(f.scalars_init, f.scalars, ncs, s));
+  MARK(MPASG_STAGE_SETUP);
+  CHECK_RC(mpasg_moist_coefficients(m, c, &f, stream));
+  MARK(MPASG_STAGE_MOIST);
+
+  for (int sub = 1; sub <= split; ++sub) {
+    for (int rk = 1; rk <= 3; ++rk) {
+      const double dts = rk_sub[rk - 1];
+      if (rk == 1 || (rk == 2 && c->time_integration_order == 3))
+      {
+        CHECK_RC(mpasg_vert_imp_coefs(m, c, &f, dts, stream));
+        MARK(MPASG_STAGE_VIMP);
+      }
+      CHECK_RC(mpasg_dyn_tend(m, c, &f, rk, stream));
+      MARK(rk == 1 ? MPASG_STAGE_DYN_TEND_RK1 : MPASG_STAGE_DYN_TEND);
+      CHECK_RC(mpasg_smlstep_pert(m, c, &f, stream));
+      MARK(MPASG_STAGE_SMLSTEP);
+      for (int small = 1; small <= nsub[rk - 1]; ++small) {
+        CHECK_RC(mpasg_acoustic_step(m, c, &f, small, dts, stream));
+        MARK(MPASG_STAGE_ACOUSTIC);
+        CHECK_RC(mpasg_divergence_damping(m, c, &f, dts, stream));
+        MARK(MPASG_STAGE_DIVDAMP);
+      }
+      CHECK_RC(mpasg_recover_large_step(m, c, &f, rk, nsub[rk - 1], rk_ts[rk - 1], stream));
+      MARK(MPASG_STAGE_RECOVER);
+      CHECK_RC(mpasg_solve_diagnostics(m, c, &f, rk, stream));
+      MARK(MPASG_STAGE_DIAG);
+    }
+    // split bookkeeping
+    if (sub == 1) {
+      CHECK_RC(copy(f.ruAvg_split, f.ruAvg, nel, s));
+      CHECK_RC(copy(f.wwAvg_split, f.wwAvg, ncw, s));
+    } else {
+      k_add_d<<<nblocks(nel), kBlock, 0, s>>>(f.ruAvg_split, f.ruAvg, nel);
+      MPASG_LAUNCH_CHECK();
+      k_add_d<<<nblocks(ncw), kBlock, 0, s>>>(f.wwAvg_split, f.wwAvg, ncw);
+      MPASG_LAUNCH_CHECK();
+    }
+    if (sub < split) {
+      CHECK_RC(fill(f.theta_m + nc * L, L, 0.0, s));
+      CHECK_RC(copy(f.ru_save, f.ru, nel, s));
+      CHECK_RC(copy(f.rw_save, f.rw, ncw, s));
+      CHECK_RC(copy(f.rtheta_p_save, f.rtheta_p, ncl, s));
+      CHECK_RC(copy(f.rho_p_save, f.rho_p, ncl, s));
+      CHECK_RC(copy(f.theta_m_save, f.theta_m, ncl, s));
+      CHECK_RC(copy(f.rr_save, f.rho_p, ncl, s));
+    }
+  }
+  MARK(MPASG_STAGE_SPLIT);
+  const double inv = 1.0 / (double)split;
+  k_scale_d<<<nblocks(nel), kBlock, 0, s>>>(f.ruAvg, f.ruAvg_split, inv, nel);
+  MPASG_LAUNCH_CHECK();
+  k_scale_d<<<nblocks(ncw), kBlock, 0, s>>>(f.wwAvg, f.wwAvg_split, inv, ncw);
+  MPASG_LAUNCH_CHECK();
+
+  // ---- split transport RK3 with the substep-averaged mass fluxes
+  if (S > 0) {
+    CHECK_RC(copy(f.scalars_a, f.scalars_init, ncs, s));
+    const double dts_t[3] = {dt / 3.0, dt / 2.0, dt};
+    MARK(MPASG_STAGE_SPLIT);
+    for (int rk = 1; rk <= 3; ++rk) {
+      if (rk == 3 && c->monotonic) {
+        CHECK_RC(mpasg_advance_scalars_mono(m, c, &f, dts_t[rk - 1], stream));
+        MARK(MPASG_STAGE_SCALARS_MONO);
+      } else {
+        CHECK_RC(mpasg_advance_scalars(m, c, &f, rk, dts_t[rk - 1], stream));
+        MARK(MPASG_STAGE_SCALARS);
+      }
+      double* t = f.scalars_a;
+      f.scalars_a = f.scalars_b;
+      f.scalars_b = t;
+    }
+    CHECK_RC(copy(f.scalars, f.scalars_a, ncs, s));
+  }
+  MARK(MPASG_STAGE_SPLIT);
+  CHECK_RC(mpasg_reconstruct_2d(m, c, &f, stream));
+  MARK(MPASG_STAGE_RECONSTRUCT);
+  return MPASG_OK;
+#undef MARK
+}
+}  // namespace

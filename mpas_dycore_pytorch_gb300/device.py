@@ -1,0 +1,182 @@
+"""Device-resident mesh and state for the CUDA step.
+
+``DeviceMesh`` uploads the reference's static arrays once (1-based padded connectivity is
+converted to 0-based int32 whose missing neighbours point at the padding row).
+``DeviceState`` owns every field of ``mpasg_fields`` (include/mpasg.h) as float64 device
+tensors in the reference layout (rows = entity, levels fastest, one padding row) and
+converts to and from the reference's state dictionaries.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Any, Mapping
+
+import numpy as np
+import torch
+
+from . import _lib
+from .errors import MpasConfigError, MpasUnsupportedCapabilityError
+
+# carried state keys (reference names) <-> field names
+STATE_KEYS = ("u", "v", "ru", "ruAvg", "pv_edge", "w", "rw", "wwAvg", "theta_m", "rho_zz",
+              "rho_p", "rtheta_p", "rtheta_base", "exner", "exner_base", "pressure_p",
+              "pressure_base", "divergence", "ke", "rt_diabatic_tend", "uReconstructX",
+              "uReconstructY", "uReconstructZ", "uReconstructZonal", "uReconstructMeridional",
+              "vorticity", "scalars")
+ALIASES = {"rho_edge": "h_edge", "h_edge": "h_edge", "ur_cell": "uReconstructZonal",
+           "vr_cell": "uReconstructMeridional"}
+
+
+def _np(x) -> np.ndarray:
+    if isinstance(x, torch.Tensor):
+        return x.detach().cpu().numpy()
+    return np.asarray(x)
+
+
+def _int(x) -> int:
+    return int(_np(x).reshape(-1)[0]) if not isinstance(x, (int, np.integer)) else int(x)
+
+
+def _conn0(a, n_target: int, rows: int) -> np.ndarray:
+    """1-based padded connectivity -> 0-based active rows; sentinels -> padding row index."""
+    a = _np(a).astype(np.int64)[:rows]
+    return np.where((a >= 1) & (a <= n_target), a - 1, n_target).astype(np.int32)
+
+
+class DeviceMesh:
+    """Static mesh arrays on the device plus the ``mpasg_mesh`` struct that points at them."""
+
+    def __init__(self, ref: Mapping[str, Any], device: torch.device | str = "cuda"):
+        self.device = torch.device(device)
+        nc, ne, nv = _int(ref["nCells"]), _int(ref["nEdges"]), _int(ref["nVertices"])
+        nl = _int(ref["nVertLevels"])
+        me = _int(ref["maxEdges"])
+        me2 = _int(ref["maxEdges2"])
+        vd = _int(ref["vertexDegree"])
+        self.nCells, self.nEdges, self.nVertices, self.nVertLevels = nc, ne, nv, nl
+        self.maxEdges, self.maxEdges2, self.vertexDegree = me, me2, vd
+        adv = _np(ref["advCellsForEdge"])
+        self.nAdvMax = int(adv.shape[1])
+        self._keep: dict[str, torch.Tensor] = {}
+        kite = _np(ref["kiteForCell"]).astype(np.int64)[:nc, :me]
+        ints = {
+            "nEdgesOnCell": _np(ref["nEdgesOnCell"]).astype(np.int32)[:nc],
+            "edgesOnCell": _conn0(ref["edgesOnCell"], ne, nc)[:, :me],
+            "cellsOnCell": _conn0(ref["cellsOnCell"], nc, nc)[:, :me],
+            "verticesOnCell": _conn0(ref["verticesOnCell"], nv, nc)[:, :me],
+            "kiteForCell": np.where((kite >= 1) & (kite <= vd), kite - 1, -1).astype(np.int32),
+            "cellsOnEdge": _conn0(ref["cellsOnEdge"], nc, ne),
+            "verticesOnEdge": _conn0(ref["verticesOnEdge"], nv, ne),
+            "nEdgesOnEdge": _np(ref["nEdgesOnEdge"]).astype(np.int32)[:ne],
+            "edgesOnEdge": _conn0(ref["edgesOnEdge"], ne, ne)[:, :me2],
+            "nAdvCellsForEdge": _np(ref["nAdvCellsForEdge"]).astype(np.int32)[:ne],
+            "advCellsForEdge": _conn0(ref["advCellsForEdge"], nc, ne),
+            "edgesOnVertex": _conn0(ref["edgesOnVertex"], ne, nv)[:, :vd],
+        }
+        # slots beyond nEdgesOnCell / nEdgesOnEdge / nAdvCellsForEdge are never read
+        dbls = {}
+        for name in _lib.MESH_DBL_PTRS:
+            if name not in ref:
+                raise MpasConfigError(f"mesh is missing {name}")
+            dbls[name] = np.ascontiguousarray(_np(ref[name]), dtype=np.float64)
+        if dbls["weightsOnEdge"].shape[1] > me2:
+            dbls["weightsOnEdge"] = dbls["weightsOnEdge"][:, :me2]
+        for key in ("edgesOnCell_sign", "defc_a", "defc_b"):
+            dbls[key] = dbls[key][:, :me]
+        dbls["coeffs_reconstruct"] = dbls["coeffs_reconstruct"][:, :me, :]
+        dbls["zb_cell"] = dbls["zb_cell"][:, :me, :]
+        dbls["zb3_cell"] = dbls["zb3_cell"][:, :me, :]
+        for k in ("rdzw", "rdzu", "fzm", "fzp", "fnm", "fnp", "rdnw"):
+            dbls[k] = dbls[k][:nl]
+        st = _lib.MeshStruct()
+        for n in ("nCells", "nEdges", "nVertices", "nVertLevels", "maxEdges", "maxEdges2",
+                  "vertexDegree", "nAdvMax"):
+            setattr(st, n, getattr(self, n))
+        for n in _lib.MESH_DOUBLES:
+            setattr(st, n, float(_np(ref[n]).reshape(-1)[0]))
+        for n, a in ints.items():
+            t = torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
+            self._keep[n] = t
+            setattr(st, n, t.data_ptr())
+        for n, a in dbls.items():
+            t = torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
+            self._keep[n] = t
+            setattr(st, n, t.data_ptr())
+        self.struct = st
+        self.ints = ints
+
+
+ROWS = {"e": lambda m: (m.nEdges + 1, m.nVertLevels),
+        "c": lambda m: (m.nCells + 1, m.nVertLevels),
+        "cw": lambda m: (m.nCells + 1, m.nVertLevels + 1),
+        "v": lambda m: (m.nVertices + 1, m.nVertLevels),
+        "L": lambda m: (m.nVertLevels,)}
+
+
+class DeviceState:
+    """All device fields of one model instance (state, step work arrays and scratch)."""
+
+    def __init__(self, mesh: DeviceMesh, num_scalars: int):
+        self.mesh = mesh
+        self.num_scalars = int(num_scalars)
+        if not 1 <= self.num_scalars <= 8:
+            raise MpasUnsupportedCapabilityError("1 to 8 scalars are supported")
+        S = self.num_scalars
+        shapes = dict((k, f(mesh)) for k, f in ROWS.items())
+        shapes["cs"] = (mesh.nCells + 1, mesh.nVertLevels, S)
+        shapes["es"] = (mesh.nEdges + 1, mesh.nVertLevels, S)
+        shapes["cws"] = (mesh.nCells + 1, mesh.nVertLevels + 1, S)
+        sizes = {name: int(np.prod(shapes[kind])) for name, kind in _lib.FIELDS}
+        total = sum(sizes.values())
+        # one arena; each field is a contiguous view (256-byte aligned)
+        align = 32
+        offs = {}
+        pos = 0
+        for name, _ in _lib.FIELDS:
+            offs[name] = pos
+            pos += (sizes[name] + align - 1) // align * align
+        self.arena = torch.zeros(pos, dtype=torch.float64, device=mesh.device)
+        self.f: dict[str, torch.Tensor] = {}
+        st = _lib.FieldsStruct()
+        for name, kind in _lib.FIELDS:
+            view = self.arena[offs[name]:offs[name] + sizes[name]].view(shapes[kind])
+            self.f[name] = view
+            setattr(st, name, view.data_ptr())
+        self.status = torch.zeros(4, dtype=torch.int32, device=mesh.device)
+        st.status = self.status.data_ptr()
+        self.struct = st
+        self.bytes = total * 8
+        # rho_zz padding row holds 1.0 (the reference's sentinel)
+        self.f["rho_zz"][mesh.nCells].fill_(1.0)
+
+    def field(self, name: str) -> torch.Tensor:
+        return self.f[ALIASES.get(name, name)]
+
+    def load(self, state: Mapping[str, Any], keys=None) -> None:
+        """Copy reference-layout arrays (numpy or torch) into the named fields."""
+        for key in keys if keys is not None else state.keys():
+            if key not in state:
+                continue
+            name = ALIASES.get(key, key)
+            if name not in self.f:
+                continue
+            src = state[key]
+            if not isinstance(src, (np.ndarray, torch.Tensor)):
+                continue
+            dst = self.f[name]
+            t = torch.as_tensor(src, dtype=torch.float64)
+            if tuple(t.shape) != tuple(dst.shape):
+                if t.dim() == dst.dim() and t.shape[0] == dst.shape[0] - 1:
+                    dst[: t.shape[0]].copy_(t, non_blocking=True)
+                    continue
+                raise MpasConfigError(f"{key}: shape {tuple(t.shape)} != {tuple(dst.shape)}")
+            dst.copy_(t, non_blocking=True)
+
+    def export(self, keys=STATE_KEYS) -> dict[str, torch.Tensor]:
+        out = {k: self.f[k] for k in keys}
+        out["rho_edge"] = self.f["h_edge"]
+        out["h_edge"] = self.f["h_edge"]
+        out["ur_cell"] = self.f["uReconstructZonal"]
+        out["vr_cell"] = self.f["uReconstructMeridional"]
+        return out
