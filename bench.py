@@ -42,6 +42,10 @@ WORKLOADS = {
                config=dict(config_monotonic=True), dt=720.0,
                name="plain float64 forward, level-6 icosahedral mesh 40962 cells x 55 levels, "
                     "3 monotone tracers, dt 720 s, split 3 x RK3 x ns 2"),
+    # configs[2] mesh: level-5 mesh, 41 levels (profiling size: state > L2, a few GB at most)
+    "c2": dict(spec=dict(level=5, nlev=41, seed=2, n_bumps=8, n_tracers=3),
+               config=dict(config_monotonic=True), dt=900.0,
+               name="plain float64 forward, level-5 mesh 10242 cells x 41 levels, 3 monotone tracers, dt 900 s"),
     # configs[0]: level-4 mesh, 26 uniform levels, 8 bumps, 1 non-monotone tracer, dt 1800 s
     "c0": dict(spec=dict(level=4, nlev=26, seed=0, n_bumps=8, n_tracers=1),
                config=dict(config_monotonic=False), dt=1800.0,

@@ -295,7 +295,7 @@ __global__ void k_recover_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int r
       double zz = m.zz[o];
       double ex = pow(zz * (kRgas / kP0) * (rtheta_p + rtb), rcv);
       f.exner[o] = ex;
-      f.pressure_p[o] = zz * kRgas * (ex * rtheta_p + rtb * (ex - f.exner_base[o]));
+      f.pressure_p[o] = zz * kRgas * __dadd_rn(__dmul_rn(ex, rtheta_p), __dmul_rn(rtb, ex - f.exner_base[o]));
     }
   }
   if (k >= 1 && k < (uint32_t)L) {

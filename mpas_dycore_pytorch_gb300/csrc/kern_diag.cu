@@ -164,7 +164,8 @@ __global__ void k_prepare_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, const 
   double rb = m.rho_base[i], tb = m.theta_base[i];
   double rho_p = rho_zz - rb;
   double rtb = tb * rb;
-  double rtp = theta_m * rho_p + rb * (theta_m - tb);
+  // unfused products: rtheta_p cancels to roundoff when the state is near the base state
+  double rtp = __dadd_rn(__dmul_rn(theta_m, rho_p), __dmul_rn(rb, theta_m - tb));
   double ex = pow(zz * (kRgas / kP0) * (rtp + rtb), rcv);
   double exb = pow(zz * (kRgas / kP0) * rtb, rcv);
   f.theta_m[i] = theta_m;
@@ -174,7 +175,7 @@ __global__ void k_prepare_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, const 
   f.rtheta_p[i] = rtp;
   f.exner[i] = ex;
   f.exner_base[i] = exb;
-  f.pressure_p[i] = zz * kRgas * (ex * rtp + rtb * (ex - exb));
+  f.pressure_p[i] = zz * kRgas * __dadd_rn(__dmul_rn(ex, rtp), __dmul_rn(rtb, ex - exb));
   f.pressure_base[i] = zz * kRgas * exb * rtb;
 }
 

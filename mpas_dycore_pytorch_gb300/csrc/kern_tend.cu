@@ -336,7 +336,8 @@ __global__ void k_tend_w_theta(mpasg_mesh m, mpasg_fields f, FastDiv fl1, TendSc
                                wdtz_at(th, ths, rwc, rws, k, L, m.fzm, m.fzp, p.coef3));
     double rz = f.rho_zz[o];
     double rtd = f.rt_diabatic_tend[o];
-    f.rthdynten[o] = (tt - f.tend_rho[o] * th[k]) / rz;
+    // unfused: the difference cancels strongly (as rounded by the reference)
+    f.rthdynten[o] = __dsub_rn(tt, __dmul_rn(f.tend_rho[o], th[k])) / rz;
     tt = tt + rz * rtd;
     tt = tt + f.tend_theta_euler[o];
     f.tend_theta[o] = tt;
