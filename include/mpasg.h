@@ -52,6 +52,8 @@ enum {
 typedef struct mpasg_mesh {
   int32_t nCells, nEdges, nVertices, nVertLevels;
   int32_t maxEdges, maxEdges2, vertexDegree, nAdvMax;
+  int32_t flatTerrain;   /* 1 when zb_cell == zb3_cell == 0: terrain-slope slot sums are skipped */
+  int32_t reserved0;
   double cf1, cf2, cf3;
   /* connectivity (0-based; missing -> padding row) */
   const int32_t *nEdgesOnCell;      /* (C)            */
@@ -75,6 +77,7 @@ typedef struct mpasg_mesh {
   const double *kiteAreasOnVertex;  /* (V, vertexDegree) */
   const double *weightsOnEdge;      /* (E, maxEdges2) */
   const double *adv_coefs, *adv_coefs_3rd;   /* (E, nAdvMax) */
+  const double *adv_coefs_p, *adv_coefs_m;   /* (E, nAdvMax): adv_coefs +/- adv_coefs_3rd */
   const double *defc_a, *defc_b;    /* (C, maxEdges) */
   const double *fEdge;              /* (E+1) */
   const double *fVertex;            /* (V+1) */
@@ -150,6 +153,13 @@ typedef struct mpasg_fields {
   double *s_max, *s_min, *scale_in, *scale_out, *rows;  /* (C+1, L, S) */
   double *wflux;        /* (C+1, L+1, S)  limiter vertical fluxes */
   double *rho_int;      /* (C+1, L) */
+  /* edge-side horizontal advective fluxes of w and theta_m (one value per edge) */
+  double *flux_w_e, *flux_th_e;                                     /* (E+1, L) */
+  /* acoustic-step column scratch: rs / ts right-hand sides, tridiagonal rhs -> solution,
+   * and the b / c diagonals of the implicit system */
+  double *ac_rs, *ac_ts;                                            /* (C+1, L) */
+  double *ac_x;                                                     /* (C+1, L+1) */
+  double *b_tri, *c_tri;                                            /* (C+1, L) */
   /* status flag word (device int32[4]) for the finite check */
   int32_t *status;
 } mpasg_fields;

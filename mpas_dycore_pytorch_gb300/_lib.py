@@ -15,14 +15,15 @@ from .errors import MpasConfigError, MpasDeviceError, MpasExtensionMissingError,
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "libmpasg.so"
 
 MESH_INT_DIMS = ("nCells", "nEdges", "nVertices", "nVertLevels", "maxEdges", "maxEdges2",
-                 "vertexDegree", "nAdvMax")
+                 "vertexDegree", "nAdvMax", "flatTerrain", "reserved0")
 MESH_DOUBLES = ("cf1", "cf2", "cf3")
 MESH_INT_PTRS = ("nEdgesOnCell", "edgesOnCell", "cellsOnCell", "verticesOnCell", "kiteForCell",
                  "cellsOnEdge", "verticesOnEdge", "nEdgesOnEdge", "edgesOnEdge",
                  "nAdvCellsForEdge", "advCellsForEdge", "edgesOnVertex")
 MESH_DBL_PTRS = ("edgesOnCell_sign", "edgesOnVertex_sign", "dcEdge", "dvEdge", "invDcEdge",
                  "invDvEdge", "invAreaCell", "invAreaTriangle", "kiteAreasOnVertex",
-                 "weightsOnEdge", "adv_coefs", "adv_coefs_3rd", "defc_a", "defc_b", "fEdge",
+                 "weightsOnEdge", "adv_coefs", "adv_coefs_3rd", "adv_coefs_p", "adv_coefs_m",
+                 "defc_a", "defc_b", "fEdge",
                  "fVertex", "meshScalingDel2", "meshScalingDel4", "latCell", "lonCell",
                  "coeffs_reconstruct", "zb_cell", "zb3_cell", "zxu", "zz", "dss", "rho_base",
                  "theta_base", "rdzw", "rdzu", "fzm", "fzp", "fnm", "fnp", "rdnw")
@@ -70,6 +71,8 @@ FIELDS = (
     ("s_max", "cs"), ("s_min", "cs"), ("scale_in", "cs"), ("scale_out", "cs"), ("rows", "cs"),
     ("wflux", "cws"),
     ("rho_int", "c"),
+    ("flux_w_e", "e"), ("flux_th_e", "e"),
+    ("ac_rs", "c"), ("ac_ts", "c"), ("ac_x", "cw"), ("b_tri", "c"), ("c_tri", "c"),
 )
 
 

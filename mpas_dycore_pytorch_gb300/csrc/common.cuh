@@ -25,13 +25,20 @@ struct FastDiv {
 // Fortran sign(1.0, x) as the reference's fct_sign_pm: +1 for x >= 0 (and -0.0).
 MPASG_D double sgn(double x) { return x >= 0.0 ? 1.0 : -1.0; }
 
-// Third/fourth-order vertical fluxes (dynamics/dyn_tend.py:839,853).
-MPASG_D double flux4(double qm2, double qm1, double q0, double qp1, double ua) {
-  return ua * (7.0 * (q0 + qm1) - (qp1 + qm2)) / 12.0;
-}
+// Third/fourth-order vertical fluxes (dynamics/dyn_tend.py:839,853):
+//   flux4 = ua (7 (q0 + qm1) - (qp1 + qm2)) / 12
+//   flux3 = flux4 + c3 |ua| ((qp1 - qm2) - 3 (q0 - qm1)) / 12
+// evaluated with one multiply by 1/12 instead of two float64 divisions (float64
+// division is a long instruction sequence on this part); the sum differs from the
+// reference's two-quotient form by at most a couple of units in the last place.
+constexpr double kInv12 = 1.0 / 12.0;
 MPASG_D double flux3(double qm2, double qm1, double q0, double qp1, double ua, double c3) {
-  return flux4(qm2, qm1, q0, qp1, ua) + c3 * fabs(ua) * ((qp1 - qm2) - 3.0 * (q0 - qm1)) / 12.0;
+  return (ua * (7.0 * (q0 + qm1) - (qp1 + qm2)) + c3 * fabs(ua) * ((qp1 - qm2) - 3.0 * (q0 - qm1))) * kInv12;
 }
+
+// x / d with the float64 division skipped when d == 1 (x / 1.0 == x exactly); the
+// height coordinate over flat terrain makes most metric denominators exactly one.
+MPASG_D double div_or_one(double x, double d) { return d == 1.0 ? x : x / d; }
 
 constexpr double kGravity = 9.80616;
 constexpr double kRgas = 287.0;

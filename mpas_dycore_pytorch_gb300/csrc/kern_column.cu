@@ -43,58 +43,95 @@ __global__ void k_moist_edges(int ne, int L, FastDiv fl, int ms, int me, const i
 }
 
 // ---------------------------------------------------------------- vertical implicit coefficients
-// dynamics/vert_imp_coefs.py:188 (coefficients :343-446, Thomas factor :100-121)
-__global__ void k_vert_imp_coefs(mpasg_mesh m, mpasg_fields f, double dts, double epssm) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+// dynamics/vert_imp_coefs.py:188 (coefficients :343-446, Thomas factor :100-121).
+// k_vimp_coefs builds every level's coefficients and tridiagonal diagonals in parallel
+// (neighbour levels shared through shared memory); k_vimp_factor runs the sequential
+// Thomas factorisation, one thread per column.
+struct VimpLevel {
+  double cofwt, coftz;
+};
+
+MPASG_D VimpLevel vimp_level(const mpasg_mesh& m, const mpasg_fields& f, size_t o, size_t ow, int k,
+                             double dtseps, double rcv) {
+  VimpLevel v;
+  double zz = m.zz[o + k], p = f.exner[o + k];
+  double rb = m.rho_base[o + k], rtb = f.rtheta_base[o + k], pb = f.exner_base[o + k];
+  double rt = f.rtheta_p[o + k], q = f.qtot[o + k];
+  v.cofwt = 0.5 * dtseps * rcv * zz * kGravity * rb / (1.0 + q) * p / ((rtb + rt) * pb);
+  v.coftz = (k == 0) ? 0.0 : dtseps * (m.fzm[k] * f.theta_m[o + k] + m.fzp[k] * f.theta_m[o + k - 1]);
+  return v;
+}
+
+__global__ void __launch_bounds__(kBlock) k_vimp_coefs(mpasg_mesh m, mpasg_fields f, FastDiv fl, double dts,
+                                                       double epssm) {
+  __shared__ double s_cw[kBlock], s_ct[kBlock];
   const int L = m.nVertLevels;
   const double dtseps = 0.5 * dts * (1.0 + epssm);
   const double rcv = kRgas / (kCp - kRgas);
   const double c2 = kCp * rcv;
-  if (c == 0) {
-    for (int k = 0; k < L; ++k) f.cofrz[k] = dtseps * m.rdzw[k];
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < (uint32_t)m.nCells * L;
+  uint32_t c = 0, k = 0;
+  size_t o = 0, ow = 0;
+  VimpLevel me_{0.0, 0.0};
+  if (active) {
+    c = fl.div(i);
+    k = i - c * L;
+    o = (size_t)c * L;
+    ow = (size_t)c * (L + 1);
+    me_ = vimp_level(m, f, o, ow, k, dtseps, rcv);
+    if (c == 0) f.cofrz[k] = dtseps * m.rdzw[k];
   }
+  s_cw[threadIdx.x] = me_.cofwt;
+  s_ct[threadIdx.x] = me_.coftz;
+  __syncthreads();
+  if (!active) return;
+  f.cofwt[o + k] = me_.cofwt;
+  f.coftz[ow + k] = me_.coftz;
+  if (k == 0) {
+    f.cofwr[o] = 0.0;
+    f.cofwz[o] = 0.0;
+    f.coftz[ow + L] = 0.0;
+    f.a_tri[o] = 0.0;
+    f.b_tri[o] = 1.0;
+    f.c_tri[o] = 0.0;
+    return;
+  }
+  const double zz = m.zz[o + k], zzm = m.zz[o + k - 1];
+  const double fzm = m.fzm[k], fzp = m.fzp[k];
+  const double cofwr = 0.5 * dtseps * kGravity * (fzm * zz + fzp * zzm);
+  const double z_i = fzm * zz + fzp * zzm;
+  const double p_i = fzm * f.exner[o + k] + fzp * f.exner[o + k - 1];
+  const double cofwz = dtseps * c2 * z_i * m.rdzu[k] * f.cqw[ow + k] * p_i;
+  f.cofwr[o + k] = cofwr;
+  f.cofwz[o + k] = cofwz;
+  // neighbour levels (k-1 below, k+1 above) from shared memory or recomputed at block edges
+  VimpLevel lo = (threadIdx.x >= 1) ? VimpLevel{s_cw[threadIdx.x - 1], s_ct[threadIdx.x - 1]}
+                                    : vimp_level(m, f, o, ow, k - 1, dtseps, rcv);
+  double ct_kp1 = 0.0;
+  if (k + 1 < (uint32_t)L)
+    ct_kp1 = (threadIdx.x + 1 < blockDim.x) ? s_ct[threadIdx.x + 1] : vimp_level(m, f, o, ow, k + 1, dtseps, rcv).coftz;
+  const double ct_km1 = lo.coftz, ct_k = me_.coftz;
+  const double cw_k = me_.cofwt, cw_km1 = lo.cofwt;
+  const double rdzw_k = m.rdzw[k], rdzw_km1 = m.rdzw[k - 1];
+  const double cofrz_k = dtseps * rdzw_k, cofrz_km1 = dtseps * rdzw_km1;
+  f.a_tri[o + k] = -cofwz * ct_km1 * rdzw_km1 * zzm + cofwr * cofrz_km1 - cw_km1 * ct_km1 * rdzw_km1;
+  f.b_tri[o + k] = 1.0 + cofwz * (ct_k * rdzw_k * zz + ct_k * rdzw_km1 * zzm) -
+                   ct_k * (cw_k * rdzw_k - cw_km1 * rdzw_km1) + cofwr * (cofrz_k - cofrz_km1);
+  f.c_tri[o + k] = -cofwz * ct_kp1 * rdzw_k * zz - cofwr * cofrz_k + cw_k * ct_kp1 * rdzw_k;
+}
+
+__global__ void k_vimp_factor(mpasg_mesh m, mpasg_fields f) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nCells) return;
+  const int L = m.nVertLevels;
   const size_t o = (size_t)c * L;
-  const size_t ow = (size_t)c * (L + 1);
-  f.coftz[ow] = 0.0;
-  f.coftz[ow + L] = 0.0;
-  for (int k = 0; k < L; ++k) {
-    double zz = m.zz[o + k], p = f.exner[o + k], t = f.theta_m[o + k];
-    double rb = m.rho_base[o + k], rtb = f.rtheta_base[o + k], pb = f.exner_base[o + k];
-    double rt = f.rtheta_p[o + k], q = f.qtot[o + k];
-    f.cofwt[o + k] = 0.5 * dtseps * rcv * zz * kGravity * rb / (1.0 + q) * p / ((rtb + rt) * pb);
-    if (k == 0) {
-      f.cofwr[o] = 0.0;
-      f.cofwz[o] = 0.0;
-    } else {
-      double zzm = m.zz[o + k - 1];
-      double fzm = m.fzm[k], fzp = m.fzp[k];
-      f.cofwr[o + k] = 0.5 * dtseps * kGravity * (fzm * zz + fzp * zzm);
-      double z_i = fzm * zz + fzp * zzm;
-      double p_i = fzm * p + fzp * f.exner[o + k - 1];
-      double t_i = fzm * t + fzp * f.theta_m[o + k - 1];
-      f.cofwz[o + k] = dtseps * c2 * z_i * m.rdzu[k] * f.cqw[ow + k] * p_i;
-      f.coftz[ow + k] = dtseps * t_i;
-    }
-  }
   double gam = 0.0;
   f.alpha_tri[o] = 0.0;
   f.gamma_tri[o] = 0.0;
-  f.a_tri[o] = 0.0;
   for (int k = 1; k < L; ++k) {
-    double cofwz = f.cofwz[o + k], cofwr = f.cofwr[o + k];
-    double ct_km1 = f.coftz[ow + k - 1], ct_k = f.coftz[ow + k], ct_kp1 = f.coftz[ow + k + 1];
-    double zz_k = m.zz[o + k], zz_km1 = m.zz[o + k - 1];
-    double rdzw_k = m.rdzw[k], rdzw_km1 = m.rdzw[k - 1];
-    double cofrz_k = dtseps * rdzw_k, cofrz_km1 = dtseps * rdzw_km1;
-    double cw_k = f.cofwt[o + k], cw_km1 = f.cofwt[o + k - 1];
-    double a = -cofwz * ct_km1 * rdzw_km1 * zz_km1 + cofwr * cofrz_km1 - cw_km1 * ct_km1 * rdzw_km1;
-    double b = 1.0 + cofwz * (ct_k * rdzw_k * zz_k + ct_k * rdzw_km1 * zz_km1) -
-               ct_k * (cw_k * rdzw_k - cw_km1 * rdzw_km1) + cofwr * (cofrz_k - cofrz_km1);
-    double cc = -cofwz * ct_kp1 * rdzw_k * zz_k - cofwr * cofrz_k + cw_k * ct_kp1 * rdzw_k;
-    double alpha = 1.0 / (b - a * gam);
-    gam = cc * alpha;
-    f.a_tri[o + k] = a;
+    double alpha = 1.0 / (f.b_tri[o + k] - f.a_tri[o + k] * gam);
+    gam = f.c_tri[o + k] * alpha;
     f.alpha_tri[o + k] = alpha;
     f.gamma_tri[o + k] = gam;
   }
@@ -111,7 +148,7 @@ __global__ void k_acoustic_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl, int s
   if (small_step != 1) {
     int c1 = m.cellsOnEdge[2 * e], c2i = m.cellsOnEdge[2 * e + 1];
     size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2i * L + k;
-    double pgrad = ((f.rtheta_pp[i2] - f.rtheta_pp[i1]) * m.invDcEdge[e]) / (0.5 * (m.zz[i2] + m.zz[i1]));
+    double pgrad = div_or_one((f.rtheta_pp[i2] - f.rtheta_pp[i1]) * m.invDcEdge[e], 0.5 * (m.zz[i2] + m.zz[i1]));
     pgrad = f.cqu_e[i] * 0.5 * c2 * (f.exner[i1] + f.exner[i2]) * pgrad;
     pgrad = pgrad + 0.5 * m.zxu[i] * kGravity * (f.rho_pp[i1] + f.rho_pp[i2]);
     double rup = f.ru_p[i] + dts * (f.tend_u[i] - pgrad);
@@ -127,102 +164,150 @@ __global__ void k_acoustic_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl, int s
 // ---------------------------------------------------------------- acoustic substep, columns
 // dynamics/acoustic_step.py:456 (cell flux sums), :675 (RHS), :772 (Thomas solve,
 // implicit Rayleigh damping, post-solve rho_pp / rtheta_pp); Thomas sweeps from
-// autodiff/tridiagonal_solve.py:56-63.  One thread owns one column; pass 1 streams
-// upward (fluxes, RHS, forward elimination), pass 2 downward (back substitution,
-// Rayleigh damping, post-solve update).
-__global__ void k_acoustic_columns(mpasg_mesh m, mpasg_fields f, int small_step, double dts,
-                                   double epssm, double resm) {
+// autodiff/tridiagonal_solve.py:56-63.  Three kernels: k_ac_prep (every level in
+// parallel: flux sums, rs / ts, tridiagonal right-hand side), k_ac_thomas (one thread
+// per column: forward elimination and back substitution only) and k_ac_post (every
+// level in parallel: Rayleigh damping, ww accumulation, rho_pp / rtheta_pp update).
+
+// rs / ts of one level before the implicit solve (acoustic_step.py :456, :675 first half)
+struct AcLevel {
+  double rs, ts, rho_in, rt_in;
+};
+
+MPASG_D AcLevel ac_level(const mpasg_mesh& m, const mpasg_fields& f, int c, int k, bool first, double dts,
+                         double resm) {
+  const int L = m.nVertLevels;
+  const int me = m.maxEdges;
+  const int n = m.nEdgesOnCell[c];
+  const double inv_area = m.invAreaCell[c];
+  const double* th1 = f.theta_m_save;  // time-level-1 theta_m
+  double rs = 0.0, ts = 0.0;
+  for (int j = 0; j < n; ++j) {
+    int e = m.edgesOnCell[c * me + j];
+    double wgt = m.edgesOnCell_sign[c * me + j] * m.dvEdge[e];
+    double flux = dts * wgt * f.ru_p[(size_t)e * L + k] * inv_area;
+    int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
+    double th_e = 0.5 * (th1[(size_t)c2 * L + k] + th1[(size_t)c1 * L + k]);
+    if (j == 0) {
+      rs = -flux;
+      ts = -(flux * th_e);
+    } else {
+      rs = rs + (-flux);
+      ts = ts + (-(flux * th_e));
+    }
+  }
+  const size_t o = (size_t)c * L + k;
+  const size_t ow = (size_t)c * (L + 1) + k;
+  AcLevel a;
+  a.rho_in = first ? 0.0 : f.rho_pp[o];
+  a.rt_in = first ? 0.0 : f.rtheta_pp[o];
+  double rwp_k = first ? 0.0 : f.rw_p[ow];
+  double rwp_k1 = first ? 0.0 : f.rw_p[ow + 1];
+  a.rs = a.rho_in + dts * f.tend_rho[o] + rs - f.cofrz[k] * resm * (rwp_k1 - rwp_k);
+  a.ts = a.rt_in + dts * f.tend_theta[o] + ts -
+         resm * m.rdzw[k] * (f.coftz[ow + 1] * rwp_k1 - f.coftz[ow] * rwp_k);
+  return a;
+}
+
+__global__ void __launch_bounds__(kBlock) k_ac_prep(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int small_step,
+                                                    double dts, double epssm, double resm) {
+  __shared__ AcLevel s_lv[kBlock];
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < (uint32_t)m.nCells * (L + 1);
+  const bool first = (small_step == 1);
+  uint32_t c = 0, k = 0;
+  AcLevel lv{0.0, 0.0, 0.0, 0.0};
+  if (active) {
+    c = fl1.div(i);
+    k = i - c * (L + 1);
+    if (k < (uint32_t)L) lv = ac_level(m, f, c, k, first, dts, resm);
+  }
+  s_lv[threadIdx.x] = lv;
+  __syncthreads();
+  if (!active) return;
+  const size_t o = (size_t)c * L;
+  const size_t ow = (size_t)c * (L + 1);
+  if (k < (uint32_t)L) {
+    f.ac_rs[o + k] = lv.rs;
+    f.ac_ts[o + k] = lv.ts;
+    f.rtheta_pp_old[o + k] = lv.rt_in;
+  }
+  const double rwp_k = first ? 0.0 : f.rw_p[ow + k];
+  if (k == 0 || k == (uint32_t)L) {  // boundary values pass through the solve unchanged
+    f.ac_x[ow + k] = rwp_k;
+    if (first) f.wwAvg[ow + k] = 0.0;
+    return;
+  }
+  AcLevel lo = (threadIdx.x >= 1) ? s_lv[threadIdx.x - 1] : ac_level(m, f, c, k - 1, first, dts, resm);
+  const double ww_in = first ? 0.0 : f.wwAvg[ow + k];
+  f.wwAvg[ow + k] = ww_in + 0.5 * (1.0 - epssm) * rwp_k;
+  const double zz_k = m.zz[o + k], zz_km1 = m.zz[o + k - 1];
+  const double cw_k = f.cofwt[o + k], cw_km1 = f.cofwt[o + k - 1];
+  f.ac_x[ow + k] = rwp_k + dts * f.tend_rw[ow + k] -
+                   f.cofwz[o + k] * ((zz_k * lv.ts - zz_km1 * lo.ts) + resm * (zz_k * lv.rt_in - zz_km1 * lo.rt_in)) -
+                   f.cofwr[o + k] * ((lv.rs + lo.rs) + resm * (lv.rho_in + lo.rho_in)) +
+                   cw_k * (lv.ts + resm * lv.rt_in) + cw_km1 * (lo.ts + resm * lo.rt_in);
+}
+
+__global__ void k_ac_thomas(mpasg_mesh m, mpasg_fields f) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nCells) return;
   const int L = m.nVertLevels;
-  const int me = m.maxEdges;
   const size_t o = (size_t)c * L;
   const size_t ow = (size_t)c * (L + 1);
-  const bool first = (small_step == 1);
-  const int nEoC = m.nEdgesOnCell[c];
-  const double inv_area = m.invAreaCell[c];
-  const double* th1 = f.theta_m_save;  // time-level-1 theta_m
-
-  double rwp_k = first ? 0.0 : f.rw_p[ow];
-  double rwp_top = first ? 0.0 : f.rw_p[ow + L];
-  if (first) {
-    f.rw_p[ow] = 0.0;
-    f.rw_p[ow + L] = 0.0;
-    f.wwAvg[ow] = 0.0;
-    f.wwAvg[ow + L] = 0.0;
+  double* x = f.ac_x + ow;
+  double xp = x[0];
+  for (int k = 1; k < L; ++k) {
+    xp = (x[k] - f.a_tri[o + k] * xp) * f.alpha_tri[o + k];
+    x[k] = xp;
   }
-  double x_prev = rwp_k;  // forward-eliminated value at k-1 (k = 0: boundary)
-  double rs_prev = 0.0, ts_prev = 0.0, rho_prev = 0.0, rt_prev = 0.0;
-  for (int k = 0; k < L; ++k) {
-    double rs = 0.0, ts = 0.0;
-    for (int j = 0; j < nEoC; ++j) {
-      int e = m.edgesOnCell[c * me + j];
-      double wgt = m.edgesOnCell_sign[c * me + j] * m.dvEdge[e];
-      double flux = dts * wgt * f.ru_p[(size_t)e * L + k] * inv_area;
-      int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-      double th_e = 0.5 * (th1[(size_t)c2 * L + k] + th1[(size_t)c1 * L + k]);
-      if (j == 0) {
-        rs = -flux;
-        ts = -(flux * th_e);
-      } else {
-        rs = rs + (-flux);
-        ts = ts + (-(flux * th_e));
-      }
-    }
-    double rho_in = first ? 0.0 : f.rho_pp[o + k];
-    double rt_in = first ? 0.0 : f.rtheta_pp[o + k];
-    double rwp_k1 = (k + 1 < L) ? (first ? 0.0 : f.rw_p[ow + k + 1]) : rwp_top;
-    f.rtheta_pp_old[o + k] = rt_in;
-    double cofrz = f.cofrz[k];
-    double rdzw = m.rdzw[k];
-    rs = rho_in + dts * f.tend_rho[o + k] + rs - cofrz * resm * (rwp_k1 - rwp_k);
-    ts = rt_in + dts * f.tend_theta[o + k] + ts -
-         resm * rdzw * (f.coftz[ow + k + 1] * rwp_k1 - f.coftz[ow + k] * rwp_k);
-    f.rho_pp[o + k] = rs;     // holds rs until pass 2
-    f.rtheta_pp[o + k] = ts;  // holds ts until pass 2
-    if (k >= 1) {
-      double ww_in = first ? 0.0 : f.wwAvg[ow + k];
-      f.wwAvg[ow + k] = ww_in + 0.5 * (1.0 - epssm) * rwp_k;
-      double zz_k = m.zz[o + k], zz_km1 = m.zz[o + k - 1];
-      double cofwz = f.cofwz[o + k], cofwr = f.cofwr[o + k];
-      double cw_k = f.cofwt[o + k], cw_km1 = f.cofwt[o + k - 1];
-      double rhs = rwp_k + dts * f.tend_rw[ow + k] -
-                   cofwz * ((zz_k * ts - zz_km1 * ts_prev) + resm * (zz_k * rt_in - zz_km1 * rt_prev)) -
-                   cofwr * ((rs + rs_prev) + resm * (rho_in + rho_prev)) + cw_k * (ts + resm * rt_in) +
-                   cw_km1 * (ts_prev + resm * rt_prev);
-      double x = (rhs - f.a_tri[o + k] * x_prev) * f.alpha_tri[o + k];
-      f.rw_p[ow + k] = x;
-      x_prev = x;
-    }
-    rs_prev = rs;
-    ts_prev = ts;
-    rho_prev = rho_in;
-    rt_prev = rt_in;
-    rwp_k = rwp_k1;
-  }
-  // pass 2: back substitution, Rayleigh damping, post-solve
-  double xs_next = rwp_top;  // solved (pre-damping) value at k+1
-  double xr_next = rwp_top;  // damped value at k+1
+  double xn = x[L];
   for (int k = L - 1; k >= 0; --k) {
-    double xk = (k >= 1) ? f.rw_p[ow + k] : (first ? 0.0 : f.rw_p[ow]);
-    double xs = xk - f.gamma_tri[o + k] * xs_next;
-    double xr = xs;
-    if (k >= 1) {
-      double fzm = m.fzm[k], fzp = m.fzp[k];
-      double zz_i = fzm * m.zz[o + k] + fzp * m.zz[o + k - 1];
-      double rho_i = fzm * f.rho_zz[o + k] + fzp * f.rho_zz[o + k - 1];
-      double dss = m.dss[o + k];
-      double rw_delta = f.rw_save[ow + k] - f.rw[ow + k];
-      xr = (xs + rw_delta - dts * dss * zz_i * rho_i * f.w[ow + k]) / (1.0 + dts * dss) - rw_delta;
-      f.wwAvg[ow + k] = f.wwAvg[ow + k] + 0.5 * (1.0 + epssm) * xr;
-    }
-    f.rw_p[ow + k] = xr;
-    double rs = f.rho_pp[o + k], ts = f.rtheta_pp[o + k];
-    f.rho_pp[o + k] = rs - f.cofrz[k] * (xr_next - xr);
-    f.rtheta_pp[o + k] = ts - m.rdzw[k] * (f.coftz[ow + k + 1] * xr_next - f.coftz[ow + k] * xr);
-    xs_next = xs;
-    xr_next = xr;
+    xn = x[k] - f.gamma_tri[o + k] * xn;
+    x[k] = xn;
   }
+}
+
+MPASG_D double ac_damped(const mpasg_mesh& m, const mpasg_fields& f, size_t o, size_t ow, int k, int L, double x,
+                         double dts) {
+  if (k == 0 || k == L) return x;
+  double fzm = m.fzm[k], fzp = m.fzp[k];
+  double zz_i = fzm * m.zz[o + k] + fzp * m.zz[o + k - 1];
+  double rho_i = fzm * f.rho_zz[o + k] + fzp * f.rho_zz[o + k - 1];
+  double dss = m.dss[o + k];
+  double rw_delta = f.rw_save[ow + k] - f.rw[ow + k];
+  double num = x + rw_delta - dts * dss * zz_i * rho_i * f.w[ow + k];
+  double den = 1.0 + dts * dss;
+  return (den == 1.0 ? num : num / den) - rw_delta;  // x / 1.0 == x below the damping layer
+}
+
+__global__ void __launch_bounds__(kBlock) k_ac_post(mpasg_mesh m, mpasg_fields f, FastDiv fl1, double dts,
+                                                    double epssm) {
+  __shared__ double s_xr[kBlock];
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < (uint32_t)m.nCells * (L + 1);
+  uint32_t c = 0, k = 0;
+  size_t o = 0, ow = 0;
+  double xr = 0.0;
+  if (active) {
+    c = fl1.div(i);
+    k = i - c * (L + 1);
+    o = (size_t)c * L;
+    ow = (size_t)c * (L + 1);
+    xr = ac_damped(m, f, o, ow, k, L, f.ac_x[ow + k], dts);
+  }
+  s_xr[threadIdx.x] = xr;
+  __syncthreads();
+  if (!active) return;
+  f.rw_p[ow + k] = xr;
+  if (k >= 1 && k < (uint32_t)L) f.wwAvg[ow + k] = f.wwAvg[ow + k] + 0.5 * (1.0 + epssm) * xr;
+  if (k == (uint32_t)L) return;
+  double xr1 = (threadIdx.x + 1 < blockDim.x) ? s_xr[threadIdx.x + 1]
+                                              : ac_damped(m, f, o, ow, k + 1, L, f.ac_x[ow + k + 1], dts);
+  f.rho_pp[o + k] = f.ac_rs[o + k] - f.cofrz[k] * (xr1 - xr);
+  f.rtheta_pp[o + k] = f.ac_ts[o + k] - m.rdzw[k] * (f.coftz[ow + k + 1] * xr1 - f.coftz[ow + k] * xr);
 }
 
 // ---------------------------------------------------------------- divergence damping
@@ -253,7 +338,7 @@ __global__ void k_smlstep_pert(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
   const int me = m.maxEdges;
   double fzm = m.fzm[k], fzp = m.fzp[k];
   double acc = f.tend_w[i];
-  const int n = m.nEdgesOnCell[c];
+  const int n = m.flatTerrain ? 0 : m.nEdgesOnCell[c];  // zero-slope terms add exact zeros
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
     double ut_k = f.tend_u[(size_t)e * L + k];
@@ -305,7 +390,7 @@ __global__ void k_recover_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int r
     double rw = rws + f.rw_p[ow];
     f.rw[ow] = rw;
     size_t oc = (size_t)c * L;
-    f.w[ow] = rw / (m.fzm[k] * m.zz[oc + k] + m.fzp[k] * m.zz[oc + k - 1]);
+    f.w[ow] = div_or_one(rw, m.fzm[k] * m.zz[oc + k] + m.fzp[k] * m.zz[oc + k - 1]);
   }
 }
 
@@ -332,7 +417,7 @@ __global__ void k_recover_w(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
     return;
   }
   const int me = m.maxEdges;
-  const int n = m.nEdgesOnCell[c];
+  const int n = m.flatTerrain ? 0 : m.nEdgesOnCell[c];  // zero-slope terms add exact zeros
   const size_t oc = (size_t)c * L;
   if (k == 0) {
     double surf = 0.0;
@@ -380,7 +465,11 @@ extern "C" int mpasg_moist_coefficients(const mpasg_mesh* m, const mpasg_config*
 extern "C" int mpasg_vert_imp_coefs(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
                                     double dts, void* stream) {
   if (!m || !c || !f) return MPASG_E_ARG;
-  k_vert_imp_coefs<<<nblocks(m->nCells, 128), 128, 0, (cudaStream_t)stream>>>(*m, *f, dts, c->epssm);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int L = m->nVertLevels;
+  k_vimp_coefs<<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), dts, c->epssm);
+  MPASG_LAUNCH_CHECK();
+  k_vimp_factor<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }
@@ -396,7 +485,12 @@ extern "C" int mpasg_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, m
   k_acoustic_edges<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), small_step,
                                                                          dts, c2);
   MPASG_LAUNCH_CHECK();
-  k_acoustic_columns<<<nblocks(m->nCells, 128), 128, 0, s>>>(*m, *f, small_step, dts, c->epssm, resm);
+  const long long ncw = (long long)m->nCells * (L + 1);
+  k_ac_prep<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, dts, c->epssm, resm);
+  MPASG_LAUNCH_CHECK();
+  k_ac_thomas<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
+  MPASG_LAUNCH_CHECK();
+  k_ac_post<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), dts, c->epssm);
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }

@@ -203,7 +203,7 @@ __global__ void k_prepare_rw(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
   double zz_i = fzp * m.zz[oc + k - 1] + fzm * m.zz[oc + k];
   double rw = f.w[i] * rho_i * zz_i;
   const int me = m.maxEdges;
-  const int n = m.nEdgesOnCell[c];
+  const int n = m.flatTerrain ? 0 : m.nEdgesOnCell[c];  // zero-slope terms add exact zeros
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
     double flux = fzm * f.ru[(size_t)e * L + k] + fzp * f.ru[(size_t)e * L + k - 1];

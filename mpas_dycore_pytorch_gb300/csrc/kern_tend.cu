@@ -63,36 +63,57 @@ MPASG_D double wduz_at(const double* __restrict__ u, double rwe, int kk, int L, 
   return flux3(u[kk - 2], u[kk - 1], u[kk], u[kk + 1], rwe, 1.0);
 }
 
-__global__ void k_tend_u(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendScalars p) {
+__global__ void __launch_bounds__(kBlock) k_tend_u(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendScalars p) {
+  __shared__ double s_wd[kBlock];
   const int L = m.nVertLevels;
+  const uint32_t n_all = (uint32_t)m.nEdges * L;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint32_t)m.nEdges * L) return;
-  uint32_t e = fl.div(i), k = i - e * L;
-  const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-  const double* ue = f.u + (size_t)e * L;
-  const size_t w1 = (size_t)c1 * (L + 1), w2 = (size_t)c2 * (L + 1);
-  double rwe_k = 0.5 * (f.rw[w1 + k] + f.rw[w2 + k]);
-  double rwe_k1 = (k + 1 < (uint32_t)L) ? 0.5 * (f.rw[w1 + k + 1] + f.rw[w2 + k + 1]) : 0.0;
-  double wd_k = wduz_at(ue, rwe_k, k, L, m.fzm, m.fzp);
-  double wd_k1 = wduz_at(ue, rwe_k1, k + 1, L, m.fzm, m.fzp);
+  const bool active = i < n_all;
+  uint32_t e = 0, k = 0;
+  int c1 = 0, c2 = 0;
+  const double* ue = f.u;
+  double wd_k = 0.0;
+  if (active) {
+    e = fl.div(i);
+    k = i - e * L;
+    c1 = m.cellsOnEdge[2 * e];
+    c2 = m.cellsOnEdge[2 * e + 1];
+    ue = f.u + (size_t)e * L;
+    double rwe_k = 0.5 * (f.rw[(size_t)c1 * (L + 1) + k] + f.rw[(size_t)c2 * (L + 1) + k]);
+    wd_k = wduz_at(ue, rwe_k, k, L, m.fzm, m.fzp);
+  }
+  s_wd[threadIdx.x] = wd_k;  // vertical flux at the interface below level k
+  __syncthreads();
+  if (!active) return;
+  double wd_k1;
+  if (k + 1 >= (uint32_t)L) {
+    wd_k1 = 0.0;
+  } else if (threadIdx.x + 1 < blockDim.x) {
+    wd_k1 = s_wd[threadIdx.x + 1];  // same edge, next level
+  } else {
+    double rwe_k1 = 0.5 * (f.rw[(size_t)c1 * (L + 1) + k + 1] + f.rw[(size_t)c2 * (L + 1) + k + 1]);
+    wd_k1 = wduz_at(ue, rwe_k1, k + 1, L, m.fzm, m.fzp);
+  }
   double tu = -m.rdzw[k] * (wd_k1 - wd_k);
   // nonlinear Coriolis / PV flux over the TRiSK stencil
   const int n2 = m.nEdgesOnEdge[e];
   const int me2 = m.maxEdges2;
   const double pv_self = f.pv_edge[i];
+  // sum_j (w_j u_j) * 0.5 (pv_self + pv_j): the exact power-of-two factor 0.5 is applied
+  // once to the sum (scaling by 0.5 commutes with every rounding of the sum)
   double q = 0.0;
   for (int j = 0; j < n2; ++j) {
     int eo = m.edgesOnEdge[e * me2 + j];
-    double workpv = 0.5 * (pv_self + f.pv_edge[(size_t)eo * L + k]);
-    double t = m.weightsOnEdge[e * me2 + j] * f.u[(size_t)eo * L + k] * workpv;
+    double t = (m.weightsOnEdge[e * me2 + j] * f.u[(size_t)eo * L + k]) * (pv_self + f.pv_edge[(size_t)eo * L + k]);
     q = (j == 0) ? t : q + t;
   }
+  q = 0.5 * q;
   const size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
   const double inv_dc = m.invDcEdge[e];
   const double rho_e = f.h_edge[i];
   tu = tu + rho_e * (q - (f.ke[i2] - f.ke[i1]) * inv_dc) - ue[k] * 0.5 * (f.h_divergence[i1] + f.h_divergence[i2]);
   if (p.rk_step == 1) {
-    double teu = -f.cqu_e[i] * ((f.pressure_p[i2] - f.pressure_p[i1]) * inv_dc / (0.5 * (m.zz[i2] + m.zz[i1])) -
+    double teu = -f.cqu_e[i] * (div_or_one((f.pressure_p[i2] - f.pressure_p[i1]) * inv_dc, 0.5 * (m.zz[i2] + m.zz[i1])) -
                                0.5 * m.zxu[i] * (f.dpdz[i1] + f.dpdz[i2]));
     int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
     double r_dv = fmin(m.invDvEdge[e], 4.0 * inv_dc);
@@ -258,15 +279,76 @@ MPASG_D double wdtz_at(const double* th, const double* ths, const double* rw, co
   return v + (rws[kk] - rw[kk]) * (fzm[kk] * ths[kk] + fzp[kk] * ths[kk - 1]);
 }
 
-// w and theta tendencies; index space (C, L+1)
-__global__ void k_tend_w_theta(mpasg_mesh m, mpasg_fields f, FastDiv fl1, TendScalars p) {
+// Edge-side horizontal advective fluxes of w and theta_m, computed once per edge:
+// flux_w_e[e,k] = ru_w * sum_a (adv_coefs +/- adv_coefs_3rd)_a w[advCell_a, k] (w levels 1..L-1)
+// flux_th_e[e,k] = ru * sum_a (...)_a theta_m[advCell_a, k] (mass levels 0..L-1).
+// The cell sums then apply edgesOnCell_sign (an exact +/-1 factor), which reproduces
+// the reference's per-slot (sign * ru) * flux products bit for bit.
+__global__ void k_adv_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint32_t)m.nCells * (L + 1)) return;
-  uint32_t c = fl1.div(i), k = i - c * (L + 1);
+  if (i >= (uint32_t)m.nEdges * L) return;
+  uint32_t e = fl.div(i), k = i - e * L;
+  const int na = m.nAdvMax;
+  const int nadv = m.nAdvCellsForEdge[e];
+  const int32_t* cells = m.advCellsForEdge + (size_t)e * na;
+  const double rue = f.ru[i];
+  {
+    const double* cf = (rue >= 0.0 ? m.adv_coefs_p : m.adv_coefs_m) + (size_t)e * na;
+    double acc = 0.0;
+    for (int a = 0; a < nadv; ++a) {
+      double t = cf[a] * f.theta_m[(size_t)cells[a] * L + k];
+      acc = (a == 0) ? t : acc + t;
+    }
+    f.flux_th_e[i] = rue * acc;
+  }
+  if (k >= 1) {
+    double ru_w = m.fzm[k] * rue + m.fzp[k] * f.ru[i - 1];
+    const double* cf = (ru_w >= 0.0 ? m.adv_coefs_p : m.adv_coefs_m) + (size_t)e * na;
+    double acc = 0.0;
+    for (int a = 0; a < nadv; ++a) {
+      double t = cf[a] * f.w[(size_t)cells[a] * (L + 1) + k];
+      acc = (a == 0) ? t : acc + t;
+    }
+    f.flux_w_e[i] = ru_w * acc;
+  }
+}
+
+// w and theta tendencies; index space (C, L+1)
+__global__ void __launch_bounds__(kBlock) k_tend_w_theta(mpasg_mesh m, mpasg_fields f, FastDiv fl1, TendScalars p) {
+  __shared__ double s_wd[kBlock], s_wt[kBlock];
+  const int L = m.nVertLevels;
+  const uint32_t n_all = (uint32_t)m.nCells * (L + 1);
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < n_all;
+  uint32_t c = 0, k = 0;
+  double wd_k = 0.0, wt_k = 0.0;
+  if (active) {
+    c = fl1.div(i);
+    k = i - c * (L + 1);
+    const size_t ow0 = (size_t)c * (L + 1), oc0 = (size_t)c * L;
+    wd_k = wdwz_at(f.w + ow0, f.rw + ow0, k, L);
+    wt_k = wdtz_at(f.theta_m + oc0, f.theta_m_save + oc0, f.rw + ow0, f.rw_save + ow0, k, L, m.fzm, m.fzp,
+                   p.coef3);
+  }
+  s_wd[threadIdx.x] = wd_k;  // interface fluxes owned by this level
+  s_wt[threadIdx.x] = wt_k;
+  __syncthreads();
+  if (!active) return;
+  double wd_k1 = 0.0, wt_k1 = 0.0;
+  if (k < (uint32_t)L) {
+    if (threadIdx.x + 1 < blockDim.x) {
+      wd_k1 = s_wd[threadIdx.x + 1];
+      wt_k1 = s_wt[threadIdx.x + 1];
+    } else {
+      const size_t ow0 = (size_t)c * (L + 1), oc0 = (size_t)c * L;
+      wd_k1 = wdwz_at(f.w + ow0, f.rw + ow0, k + 1, L);
+      wt_k1 = wdtz_at(f.theta_m + oc0, f.theta_m_save + oc0, f.rw + ow0, f.rw_save + ow0, k + 1, L, m.fzm,
+                      m.fzp, p.coef3);
+    }
+  }
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  const int na = m.nAdvMax;
   const double ia = m.invAreaCell[c];
   const size_t oc = (size_t)c * L;
   const size_t ow = (size_t)c * (L + 1);
@@ -275,21 +357,9 @@ __global__ void k_tend_w_theta(mpasg_mesh m, mpasg_fields f, FastDiv fl1, TendSc
     double tw = 0.0;
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
-      double ru_w = fzm * f.ru[(size_t)e * L + k] + fzp * f.ru[(size_t)e * L + k - 1];
-      double sg = sgn(ru_w);
-      int nadv = m.nAdvCellsForEdge[e];
-      double fl = 0.0;
-      for (int a = 0; a < nadv; ++a) {
-        int cell = m.advCellsForEdge[e * na + a];
-        double sw = m.adv_coefs[e * na + a] + sg * m.adv_coefs_3rd[e * na + a];
-        double t = sw * f.w[(size_t)cell * (L + 1) + k];
-        fl = (a == 0) ? t : fl + t;
-      }
-      tw = tw - m.edgesOnCell_sign[c * me + j] * ru_w * fl;
+      tw = tw - m.edgesOnCell_sign[c * me + j] * f.flux_w_e[(size_t)e * L + k];
     }
-    const double* wc = f.w + ow;
-    const double* rwc = f.rw + ow;
-    tw = tw * ia - m.rdzu[k] * (wdwz_at(wc, rwc, k + 1, L) - wdwz_at(wc, rwc, k, L));
+    tw = tw * ia - m.rdzu[k] * (wd_k1 - wd_k);
     double teu = f.tend_w_euler[i];
     if (p.rk_step == 1) {
       teu = teu - f.cqw[ow + k] * (m.rdzu[k] * (f.pressure_p[oc + k] - f.pressure_p[oc + k - 1]) -
@@ -305,17 +375,7 @@ __global__ void k_tend_w_theta(mpasg_mesh m, mpasg_fields f, FastDiv fl1, TendSc
     double tt = 0.0;
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
-      double rue = f.ru[(size_t)e * L + k];
-      double sg = sgn(rue);
-      int nadv = m.nAdvCellsForEdge[e];
-      double fl = 0.0;
-      for (int a = 0; a < nadv; ++a) {
-        int cell = m.advCellsForEdge[e * na + a];
-        double sw = m.adv_coefs[e * na + a] + sg * m.adv_coefs_3rd[e * na + a];
-        double t = sw * f.theta_m[(size_t)cell * L + k];
-        fl = (a == 0) ? t : fl + t;
-      }
-      double x = -(m.edgesOnCell_sign[c * me + j] * rue * fl);
+      double x = -(m.edgesOnCell_sign[c * me + j] * f.flux_th_e[(size_t)e * L + k]);
       tt = (j == 0) ? x : tt + x;
     }
     if (p.rk_step > 1) {
@@ -329,11 +389,7 @@ __global__ void k_tend_w_theta(mpasg_mesh m, mpasg_fields f, FastDiv fl1, TendSc
       }
     }
     const double* th = f.theta_m + oc;
-    const double* ths = f.theta_m_save + oc;
-    const double* rwc = f.rw + ow;
-    const double* rws = f.rw_save + ow;
-    tt = tt * ia - m.rdzw[k] * (wdtz_at(th, ths, rwc, rws, k + 1, L, m.fzm, m.fzp, p.coef3) -
-                               wdtz_at(th, ths, rwc, rws, k, L, m.fzm, m.fzp, p.coef3));
+    tt = tt * ia - m.rdzw[k] * (wt_k1 - wt_k);
     double rz = f.rho_zz[o];
     double rtd = f.rt_diabatic_tend[o];
     // unfused: the difference cancels strongly (as rounded by the reference)
@@ -395,6 +451,8 @@ extern "C" int mpasg_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_
       MPASG_LAUNCH_CHECK();
     }
   }
+  k_adv_edges<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl);
+  MPASG_LAUNCH_CHECK();
   k_tend_w_theta<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, fl1, p);
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;

@@ -16,12 +16,12 @@ __global__ void k_pattern_c(mpasg_mesh m, FastDiv fl, int S, const double* __res
   const int na = m.nAdvMax;
   const int nadv = m.nAdvCellsForEdge[e];
   const double u = uh[i];
-  const double sg = sgn(u);
+  const double* cf = (u >= 0.0 ? m.adv_coefs_p : m.adv_coefs_m) + (size_t)e * na;
   double acc[8];
   for (int s = 0; s < S; ++s) acc[s] = 0.0;
   for (int a = 0; a < nadv; ++a) {
     int cell = m.advCellsForEdge[e * na + a];
-    double w = m.adv_coefs[e * na + a] + sg * m.adv_coefs_3rd[e * na + a];
+    double w = cf[a];
     const double* qc = q + ((size_t)cell * L + k) * S;
     for (int s = 0; s < S; ++s) {
       double t = w * qc[s];
@@ -39,13 +39,25 @@ MPASG_D double wdtn_at(const double* sn, const double* ww, int kk, int L, int S,
 }
 
 // explicit stage update for all scalars at (cell, level)
-__global__ void k_scalars_update(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S, double dt, double w_old,
-                                 double w_new, double coef3, const double* __restrict__ s_old,
-                                 const double* __restrict__ s_new, double* __restrict__ s_out) {
+__global__ void __launch_bounds__(kBlock) k_scalars_update(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S,
+                                                           double dt, double w_old, double w_new, double coef3,
+                                                           const double* __restrict__ s_old,
+                                                           const double* __restrict__ s_new,
+                                                           double* __restrict__ s_out) {
+  extern __shared__ double s_wdtn[];  // [blockDim.x][S]: vertical flux at the interface below
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint32_t)m.nCells * L) return;
-  uint32_t c = fl.div(i), k = i - c * L;
+  const bool active = i < (uint32_t)m.nCells * L;
+  uint32_t c = 0, k = 0;
+  if (active) {
+    c = fl.div(i);
+    k = i - c * L;
+    const double* sn0 = s_new + (size_t)c * L * S;
+    const double* ww0 = f.wwAvg + (size_t)c * (L + 1);
+    for (int s = 0; s < S; ++s) s_wdtn[threadIdx.x * S + s] = wdtn_at(sn0, ww0, k, L, S, s, m.fnm, m.fnp, coef3);
+  }
+  __syncthreads();
+  if (!active) return;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
   double div[8];
@@ -65,10 +77,14 @@ __global__ void k_scalars_update(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S
   double rho_old = f.rho_zz_old_split[i];
   double rho_i = w_old * rho_old + w_new * f.rho_zz[i];
   double inv = 1.0 / rho_i;
+  const bool next_in_block = threadIdx.x + 1 < blockDim.x;
   for (int s = 0; s < S; ++s) {
     double tend_col = div[s] * ia + 0.0;
-    double vdiv = m.rdnw[k] * (wdtn_at(sn, ww, k + 1, L, S, s, m.fnm, m.fnp, coef3) -
-                               wdtn_at(sn, ww, k, L, S, s, m.fnm, m.fnp, coef3));
+    double lo = s_wdtn[threadIdx.x * S + s];
+    double hi = (k + 1 >= (uint32_t)L) ? 0.0
+                : next_in_block ? s_wdtn[(threadIdx.x + 1) * S + s]
+                                : wdtn_at(sn, ww, k + 1, L, S, s, m.fnm, m.fnp, coef3);
+    double vdiv = m.rdnw[k] * (hi - lo);
     s_out[(size_t)i * S + s] = (s_old[(size_t)i * S + s] * rho_old + dt * (tend_col - vdiv)) * inv;
   }
 }
@@ -79,12 +95,34 @@ MPASG_D double mz(double x) { return x > 0.0 ? x : 0.0; }
 // per (cell, level): rho_int, local+neighbour bounds, vertical upwind update,
 // vertical parts of the limiter scale sums; stores the high-minus-upwind vertical flux
 // at the interface below the level (wflux[c, k, s], k >= 1)
-__global__ void k_mono_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S, double dt, double coef3,
-                               const double* __restrict__ so_all, const double* __restrict__ sn_all) {
+__global__ void __launch_bounds__(kBlock) k_mono_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S,
+                                                         double dt, double coef3,
+                                                         const double* __restrict__ so_all,
+                                                         const double* __restrict__ sn_all) {
+  extern __shared__ double s_wm[];  // [blockDim.x][2 S]: high-minus-upwind flux and upwind flux below
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint32_t)m.nCells * L) return;
-  uint32_t c = fl.div(i), k = i - c * L;
+  const bool active = i < (uint32_t)m.nCells * L;
+  uint32_t c = 0, k = 0;
+  if (active) {
+    c = fl.div(i);
+    k = i - c * L;
+    const double* so0 = so_all + (size_t)c * L * S;
+    const double* sn0 = sn_all + (size_t)c * L * S;
+    const double* ww0 = f.wwAvg + (size_t)c * (L + 1);
+    for (int s = 0; s < S; ++s) {
+      double fup = 0.0, wm = 0.0;
+      if (k >= 1) {
+        double wk = ww0[k];
+        fup = dt * (wk * (wk >= 0.0 ? so0[(k - 1) * S + s] : so0[k * S + s]));
+        wm = dt * wdtn_at(sn0, ww0, k, L, S, s, m.fnm, m.fnp, coef3) - fup;
+      }
+      s_wm[threadIdx.x * 2 * S + s] = wm;
+      s_wm[threadIdx.x * 2 * S + S + s] = fup;
+    }
+  }
+  __syncthreads();
+  if (!active) return;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
   const double ia = m.invAreaCell[c];
@@ -137,15 +175,19 @@ __global__ void k_mono_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S, 
     // vertical high-order and upwind fluxes at the interfaces below (k) and above (k+1)
     double fup_lo = 0.0, fup_hi = 0.0, wm_lo = 0.0, wm_hi = 0.0;
     if (k >= 1) {
-      double wk = ww[k];
-      fup_lo = dt * (wk * (wk >= 0.0 ? so[(k - 1) * S + s] : so[k * S + s]));
-      wm_lo = dt * wdtn_at(sn, ww, k, L, S, s, m.fnm, m.fnp, coef3) - fup_lo;
+      wm_lo = s_wm[threadIdx.x * 2 * S + s];
+      fup_lo = s_wm[threadIdx.x * 2 * S + S + s];
       f.wflux[((size_t)c * (L + 1) + k) * S + s] = wm_lo;
     }
     if (k + 1 < (uint32_t)L) {
-      double wk = ww[k + 1];
-      fup_hi = dt * (wk * (wk >= 0.0 ? so[k * S + s] : so[(k + 1) * S + s]));
-      wm_hi = dt * wdtn_at(sn, ww, k + 1, L, S, s, m.fnm, m.fnp, coef3) - fup_hi;
+      if (threadIdx.x + 1 < blockDim.x) {
+        wm_hi = s_wm[(threadIdx.x + 1) * 2 * S + s];
+        fup_hi = s_wm[(threadIdx.x + 1) * 2 * S + S + s];
+      } else {
+        double wk = ww[k + 1];
+        fup_hi = dt * (wk * (wk >= 0.0 ? so[k * S + s] : so[(k + 1) * S + s]));
+        wm_hi = dt * wdtn_at(sn, ww, k + 1, L, S, s, m.fnm, m.fnp, coef3) - fup_hi;
+      }
     }
     double rows = so[k * S + s] * rho_old;
     if (k + 1 < (uint32_t)L) rows = rows - fup_hi * rd;
@@ -290,7 +332,7 @@ extern "C" int mpasg_advance_scalars(const mpasg_mesh* m, const mpasg_config* c,
   MPASG_LAUNCH_CHECK();
   double w_old, w_new;
   time_weights(1, rk_step, c->time_integration_order, &w_old, &w_new);
-  k_scalars_update<<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(
+  k_scalars_update<<<nblocks((long long)m->nCells * L), kBlock, kBlock * S * sizeof(double), s>>>(
       *m, *f, fl, S, dt_stage, w_old, w_new, c->coef_3rd_order, f->scalars_init, f->scalars_a, f->scalars_b);
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
@@ -305,7 +347,7 @@ extern "C" int mpasg_advance_scalars_mono(const mpasg_mesh* m, const mpasg_confi
   const long long nel = (long long)m->nEdges * L, ncl = (long long)m->nCells * L;
   k_pattern_c<<<nblocks(nel), kBlock, 0, s>>>(*m, fl, S, f->ruAvg, f->scalars_a, f->hflux, 1);
   MPASG_LAUNCH_CHECK();
-  k_mono_cells_a<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, S, dt_stage, c->coef_3rd_order, f->scalars_init,
+  k_mono_cells_a<<<nblocks(ncl), kBlock, kBlock * 2 * S * sizeof(double), s>>>(*m, *f, fl, S, dt_stage, c->coef_3rd_order, f->scalars_init,
                                                   f->scalars_a);
   MPASG_LAUNCH_CHECK();
   k_mono_edges_a<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, S, dt_stage, f->scalars_init);

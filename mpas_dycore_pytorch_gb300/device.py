@@ -76,7 +76,12 @@ class DeviceMesh:
         }
         # slots beyond nEdgesOnCell / nEdgesOnEdge / nAdvCellsForEdge are never read
         dbls = {}
+        a, a3 = _np(ref["adv_coefs"]).astype(np.float64), _np(ref["adv_coefs_3rd"]).astype(np.float64)
+        derived = {"adv_coefs_p": a + a3, "adv_coefs_m": a - a3}
         for name in _lib.MESH_DBL_PTRS:
+            if name in derived:
+                dbls[name] = np.ascontiguousarray(derived[name])
+                continue
             if name not in ref:
                 raise MpasConfigError(f"mesh is missing {name}")
             dbls[name] = np.ascontiguousarray(_np(ref[name]), dtype=np.float64)
@@ -93,6 +98,8 @@ class DeviceMesh:
         for n in ("nCells", "nEdges", "nVertices", "nVertLevels", "maxEdges", "maxEdges2",
                   "vertexDegree", "nAdvMax"):
             setattr(st, n, getattr(self, n))
+        st.flatTerrain = int(not np.any(dbls["zb_cell"]) and not np.any(dbls["zb3_cell"]))
+        self.flat_terrain = bool(st.flatTerrain)
         for n in _lib.MESH_DOUBLES:
             setattr(st, n, float(_np(ref[n]).reshape(-1)[0]))
         for n, a in ints.items():

@@ -13,6 +13,9 @@ KEYS = ("moist", "vimp", "dyn_tend", "smlstep", "acoustic", "divdamp", "recover"
         "scalars", "scalars_mono", "reconstruct")
 # float64 with fused multiply-add on the GPU vs the reference's unfused CPU arithmetic
 TOL = 1e-12
+# rthdynten is a diagnostic output (physics coupling) formed as a difference of nearly
+# equal tendencies; its relative error is that cancellation times the roundoff above
+TOL_BY_NAME = {"rthdynten": 1e-10}
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -42,4 +45,4 @@ def test_cuda_stage_matches_reference(case, key):
                 assert np.abs(g[:rows] - r[:rows]).max() <= 1e-9 * scale, (key, entry["index"], name)
             else:
                 err = rel_l2(g[:rows], r[:rows])
-                assert err <= TOL, (key, entry["index"], name, err)
+                assert err <= TOL_BY_NAME.get(name, TOL), (key, entry["index"], name, err)
