@@ -5,7 +5,8 @@
  * Every entry point takes plain POD structs of DEVICE pointers plus a cudaStream_t
  * (passed as void*), launches asynchronously on that stream and returns an int status
  * (MPASG_OK or a negative MPASG_E_* code). No entry point allocates device memory:
- * callers own every buffer (the Python host allocates them from one arena).
+ * callers own every buffer (the Python host allocates them from one arena), except the
+ * fixed edge scratch compiled into the library for mpasg_advance_scalars_static.
  *
  * Layout (matches the reference's runtime tensors, so host<->device needs no transpose):
  *   cell / edge / vertex fields are row-major (N+1, L) float64, levels fastest, with one
@@ -28,6 +29,7 @@
  *   mpasg_advance_scalars       dynamics/advance_scalars.py:1272
  *   mpasg_advance_scalars_mono  dynamics/advance_scalars_mono.py:2878
  *   mpasg_reconstruct_2d        dynamics/vector_reconstruction.py:311
+ *   mpasg_advance_scalars_static  (no counterpart: advance_scalars.py:1272 without caller scratch)
  */
 #ifndef MPASG_H
 #define MPASG_H
@@ -45,7 +47,8 @@ enum {
   MPASG_E_ARG = -1,      /* null pointer / bad dimension / unsupported option */
   MPASG_E_LAUNCH = -2,   /* a kernel launch failed (cudaGetLastError) */
   MPASG_E_NONFINITE = -3,/* the finite-field check found NaN/Inf */
-  MPASG_E_CUDA = -4      /* another CUDA runtime error */
+  MPASG_E_CUDA = -4,     /* another CUDA runtime error */
+  MPASG_E_SCRATCH = -5   /* the problem exceeds the library-owned static scratch */
 };
 
 /* Static mesh: dimensions, connectivity, geometry and vertical metrics. */
@@ -222,6 +225,34 @@ int mpasg_advance_scalars_mono(const mpasg_mesh *m, const mpasg_config *c, mpasg
                                double dt_stage, void *stream);
 int mpasg_reconstruct_2d(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
                          void *stream);
+
+/* ---- transport without caller scratch -------------------------------------------- */
+/* Capacity (float64 values) of the library-owned edge scratch: nEdges * L * S must not
+ * exceed it (32 MiB; e.g. 30720 edges x 41 levels x 3 scalars fits). */
+#define MPASG_STATIC_SCRATCH_DOUBLES (1 << 22)
+/*
+ * mpasg_advance_scalars_static: the same explicit RK-stage transport as
+ * mpasg_advance_scalars (same fields read and written, same results bit for bit), but
+ * its per-edge scratch (f->hflux in the other entry point) is a fixed array inside the
+ * library, so f->hflux may be null and the call allocates and borrows nothing.
+ * No counterpart in the reference: its atm_advance_scalars_work
+ * (dynamics/advance_scalars.py:1272) allocates its work tensors on every call.
+ *
+ * For callers that can hand over only the stage's own arrays (scalar_old/new, rho_zz
+ * old/new, uhAvg, wwAvg) and may not allocate device memory themselves: e.g. a host
+ * model whose device memory is owned by its own pool, or one that may not call an
+ * allocator inside its time loop.
+ *
+ *  - The first call on each device looks up the scratch address (and may load the
+ *    module); make that first call, with that device current, before any stream capture.
+ *  - Returns MPASG_E_SCRATCH, launching nothing, when nEdges * L * S exceeds
+ *    MPASG_STATIC_SCRATCH_DOUBLES.
+ *  - No scratch value needs to start at zero: each call writes every entry it reads.
+ *  - There is one scratch per device: calls that overlap on one device (other streams,
+ *    other threads) race on it. Order them (one stream, or events between streams).
+ */
+int mpasg_advance_scalars_static(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                                 int rk_step, double dt_stage, void *stream);
 
 #ifdef __cplusplus
 }

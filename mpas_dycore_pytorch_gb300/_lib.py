@@ -99,7 +99,11 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_check_finite", "mpasg_moist_coefficients", "mpasg_vert_imp_coefs",
            "mpasg_dyn_tend", "mpasg_smlstep_pert", "mpasg_acoustic_step",
            "mpasg_divergence_damping", "mpasg_recover_large_step", "mpasg_solve_diagnostics",
-           "mpasg_advance_scalars", "mpasg_advance_scalars_mono", "mpasg_reconstruct_2d")
+           "mpasg_advance_scalars", "mpasg_advance_scalars_mono", "mpasg_reconstruct_2d",
+           "mpasg_advance_scalars_static")
+
+# capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
+STATIC_SCRATCH_DOUBLES = 1 << 22
 
 _lib = None
 
@@ -136,6 +140,7 @@ def load() -> C.CDLL:
         "mpasg_advance_scalars": ([m, c, f, C.c_int, C.c_double, vp], C.c_int),
         "mpasg_advance_scalars_mono": ([m, c, f, C.c_double, vp], C.c_int),
         "mpasg_reconstruct_2d": ([m, c, f, vp], C.c_int),
+        "mpasg_advance_scalars_static": ([m, c, f, C.c_int, C.c_double, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -155,4 +160,9 @@ def check(rc: int, what: str) -> None:
         raise MpasConfigError(f"{what}: invalid argument (status {rc})")
     if rc == -3:
         raise MpasNumericalError(f"{what}: non-finite values (status {rc})")
+    if rc == -5:
+        raise MpasConfigError(
+            f"{what}: nEdges * levels * scalars exceeds the library's static scratch of "
+            f"{STATIC_SCRATCH_DOUBLES} values (status {rc}); use the entry point that takes "
+            "caller scratch")
     raise MpasDeviceError(f"{what}: CUDA failure (status {rc})")

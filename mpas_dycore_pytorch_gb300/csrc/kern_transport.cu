@@ -2,6 +2,8 @@
 // composition :861, Pattern-C edge values dynamics/pattern_c.py:234-305) and the monotone
 // flux-corrected final stage (dynamics/advance_scalars_mono.py:3332, tile :1476, neighbour
 // bounds autodiff/soft_limiter.py:72).  Scalar fields are (C+1, L, S), edge fluxes (E+1, L, S).
+#include <mutex>
+
 #include "common.cuh"
 
 namespace {
@@ -357,6 +359,54 @@ extern "C" int mpasg_advance_scalars_mono(const mpasg_mesh* m, const mpasg_confi
   k_mono_edges_b<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, S);
   MPASG_LAUNCH_CHECK();
   k_mono_cells_c<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, S, f->scalars_b);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
+// ---------------------------------------------------------------- library-owned scratch
+// Edge values of mpasg_advance_scalars_static live here instead of in f->hflux.
+static __device__ __align__(256) double g_static_hflux[MPASG_STATIC_SCRATCH_DOUBLES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+double* g_static_ptr[kMaxDevices] = {};
+
+// Device address of g_static_hflux on the current device, looked up once per device.
+int static_scratch(double** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return MPASG_E_CUDA;
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_static_hflux) != cudaSuccess || !p) return MPASG_E_CUDA;
+    g_static_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_static_ptr[dev];
+  return MPASG_OK;
+}
+}  // namespace
+
+extern "C" int mpasg_advance_scalars_static(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
+                                            int rk_step, double dt_stage, void* stream) {
+  if (!m || !c || !f || c->num_scalars < 1 || c->num_scalars > 8) return MPASG_E_ARG;
+  if (m->nEdges < 0 || m->nCells < 0 || m->nVertLevels < 1) return MPASG_E_ARG;
+  const long long need = (long long)m->nEdges * m->nVertLevels * c->num_scalars;
+  if (need > MPASG_STATIC_SCRATCH_DOUBLES) return MPASG_E_SCRATCH;
+  double* scratch = nullptr;
+  const int rc = static_scratch(&scratch);
+  if (rc != MPASG_OK) return rc;
+  mpasg_fields g = *f;  // the caller's struct is left as it is
+  g.hflux = scratch;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int L = m->nVertLevels, S = c->num_scalars;
+  FastDiv fl(L);
+  k_pattern_c<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, fl, S, g.ruAvg, g.scalars_a, g.hflux, 0);
+  MPASG_LAUNCH_CHECK();
+  double w_old, w_new;
+  time_weights(1, rk_step, c->time_integration_order, &w_old, &w_new);
+  k_scalars_update<<<nblocks((long long)m->nCells * L), kBlock, kBlock * S * sizeof(double), s>>>(
+      *m, g, fl, S, dt_stage, w_old, w_new, c->coef_3rd_order, g.scalars_init, g.scalars_a, g.scalars_b);
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }
