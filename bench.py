@@ -51,6 +51,10 @@ WORKLOADS = {
                config=dict(config_monotonic=False), dt=1800.0,
                name="plain float64 forward, level-4 mesh 2562 cells x 26 levels, 1 tracer, dt 1800 s"),
 }
+# DRAM bytes (read + write) per call and cell-level of a float64 stage, from an ncu capture
+# of the level-5 x 41 case (profiles/dyn_tend_dram_traffic_level5_10242x41_fp64.md), scaled
+# to the workload by its cell-levels
+TRAFFIC_B_PER_CELL_LEVEL = {"dyn_tend": 542.7}
 BASE_CFG = {"config_time_integration_order": 3, "config_len_disp": 120000.0,
             "config_number_of_sub_steps": 2, "config_dynamics_split_steps": 3}
 
@@ -64,8 +68,8 @@ def _cfg(w):
 
 # ------------------------------------------------------------------------------ CPU side
 def _oracle_sample(args):
-    """One large step of the oracle on a bounded sample mesh; returns (cell-levels, seconds)."""
-    spec_kw, cfg, dt = args
+    """``nsteps`` large steps of the oracle on a bounded sample mesh; returns (cell-levels, seconds)."""
+    spec_kw, cfg, dt, nsteps = args
     sys.path.insert(0, str(ROOT))
     from mpas_dycore_pytorch_gb300.cases import CaseSpec
     from mpas_dycore_pytorch_gb300.loader import load_case
@@ -74,8 +78,9 @@ def _oracle_sample(args):
     s = Stepper(st, cfg)
     prep = s.prepare(st, dt)
     t0 = time.perf_counter()
-    s.srk3_step(prep, dt)
-    return int(st["nCells"]) * int(st["nVertLevels"]), time.perf_counter() - t0
+    for _ in range(nsteps):
+        prep = s.srk3_step(prep, dt)
+    return nsteps * int(st["nCells"]) * int(st["nVertLevels"]), time.perf_counter() - t0
 
 
 def _sample_spec(w):
@@ -84,11 +89,11 @@ def _sample_spec(w):
     return spec
 
 
-def cpu_throughput(w, procs: int, rounds: int = 1):
+def cpu_throughput(w, procs: int, rounds: int = 1, nsteps: int = 1):
     """Aggregate oracle throughput with ``procs`` concurrent processes (spawned)."""
     ctx = mp.get_context("spawn")
     spec = _sample_spec(w)
-    jobs = [(spec, _cfg(w), w["dt"])] * procs
+    jobs = [(spec, _cfg(w), w["dt"], nsteps)] * procs
     total = 0
     wall = 0.0
     with ctx.Pool(procs) as pool:
@@ -177,10 +182,11 @@ def run_gb300(args, rank, world):
     # CPU baseline workers are spawned before any CUDA work
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cl, wall, spec = cpu_throughput(w, procs=1)
+        n_cpu = 5
+        cl, wall, spec = cpu_throughput(w, procs=1, nsteps=n_cpu)
         cpu = {"value": cl / wall, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"1 large step of the numpy oracle on the level-{spec['level']} mesh "
-                         f"({cl} cell-levels, same vertical grid, tracers and options), {wall:.1f} s"}
+               "sample": f"{n_cpu} large steps of the numpy oracle on the level-{spec['level']} mesh "
+                         f"({cl // n_cpu} cell-levels, same vertical grid, tracers and options), {wall:.1f} s"}
     torch.cuda.set_device(rank % torch.cuda.device_count())
     dev = torch.device("cuda", torch.cuda.current_device())
     st, _ = load_case(CaseSpec(**w["spec"]), cfg, as_torch=False)
@@ -286,8 +292,11 @@ def run_gb300(args, rank, world):
         per_call_ms = merged[dom] / max(calls[dom], 1)
         bytes_call = stage_bytes_per_call(keymap[dom], S, C_, L_)
         achieved = bytes_call / (per_call_ms / 1e3) / 1e9
+        traffic = None
+        if dom in TRAFFIC_B_PER_CELL_LEVEL:
+            traffic = round(TRAFFIC_B_PER_CELL_LEVEL[dom] * C_ * L_)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None, "kernel": f"stage:{dom}",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"stage:{dom}",
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_call,
                 "launch_ms": round(per_call_ms, 4)}
 
