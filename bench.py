@@ -191,7 +191,7 @@ def run_gb300(args, rank, world):
     dev = torch.device("cuda", torch.cuda.current_device())
     st, _ = load_case(CaseSpec(**w["spec"]), cfg, as_torch=False)
     S = int(st["scalars"].shape[-1])
-    model = Model(st, cfg, w["dt"], num_scalars=S, device=dev)
+    model = Model(st, cfg, w["dt"], num_scalars=S, device=dev, precision=args.precision)
     model.prepare(st)
     C_, L_ = model.dmesh.nCells, model.dmesh.nVertLevels
     lib = model.lib
@@ -293,7 +293,7 @@ def run_gb300(args, rank, world):
         bytes_call = stage_bytes_per_call(keymap[dom], S, C_, L_)
         achieved = bytes_call / (per_call_ms / 1e3) / 1e9
         traffic = None
-        if dom in TRAFFIC_B_PER_CELL_LEVEL:
+        if dom in TRAFFIC_B_PER_CELL_LEVEL and args.precision == "float64":
             traffic = round(TRAFFIC_B_PER_CELL_LEVEL[dom] * C_ * L_)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"stage:{dom}",
@@ -324,8 +324,9 @@ def run_gb300(args, rank, world):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
-        "config": {"workload": w["name"], "cells": C_, "levels": L_, "scalars": S,
+        "dtype": "f64" if args.precision == "float64" else "f32 stencils / f64 state", "data": "synthetic",
+        "config": {"workload": w["name"] if args.precision == "float64" else w["name"].replace("plain float64", "mixed-precision"),
+                   "precision": args.precision, "cells": C_, "levels": L_, "scalars": S,
                    "state_bytes": model.state.bytes,
                    "l2": "inputs larger than L2 (device state %.1f GB)" % (model.state.bytes / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU",
@@ -369,6 +370,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--workload", default="c1", choices=tuple(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="float64", choices=("float64", "mixed"))
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

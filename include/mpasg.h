@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define MPASG_ABI_VERSION 1
+#define MPASG_ABI_VERSION 2
 
 enum {
   MPASG_OK = 0,
@@ -93,6 +93,12 @@ typedef struct mpasg_mesh {
   const double *dss;                /* (C+1, L) */
   const double *rho_base, *theta_base;  /* (C+1, L) */
   const double *rdzw, *rdzu, *fzm, *fzp, *fnm, *fnp, *rdnw;    /* (L) */
+  /* Reference theta profile of the mixed form (float64): ref_theta (L) is the level mean
+   * of theta_base; at each w interface k (L+1 values, zero where unused) its vertical
+   * flux weights: ref_theta_w4 / ref_theta_w3 are the centred and upwind parts of the
+   * third-order interpolation (2 <= k <= L-2), ref_theta_w2 = fzm ref_k + fzp ref_(k-1)
+   * (1 <= k <= L-1). */
+  const double *ref_theta, *ref_theta_w4, *ref_theta_w3, *ref_theta_w2;
 } mpasg_mesh;
 
 /* Namelist options the step consumes (validated on the host). */
@@ -107,7 +113,17 @@ typedef struct mpasg_config {
   int32_t monotonic;                /* monotone limiter on the last transport stage */
   int32_t horiz_mixing_smagorinsky; /* 1: 2d_smagorinsky */
   int32_t num_scalars, moist_start, moist_end;
+  int32_t precision;                /* MPASG_PRECISION_FLOAT64 or MPASG_PRECISION_MIXED */
+  int32_t reserved1;
 } mpasg_config;
+
+/* Arithmetic of the step.  FLOAT64: every stage in float64 (the reference's arithmetic).
+ * MIXED: fields stay float64 in memory and the float64 parts below stay float64; the
+ * horizontal stencils (tendencies, fluxes, transport, diagnostics, damping) evaluate
+ * in float32.  Float64 parts: vertically implicit coefficients and the tridiagonal
+ * solve, recovery of the prognostic state including Exner function and pressure
+ * perturbation, accumulation of the acoustic perturbations and of the RK stages. */
+enum { MPASG_PRECISION_FLOAT64 = 0, MPASG_PRECISION_MIXED = 1 };
 
 /*
  * Every device array the step touches: the carried state (reference key names), the
@@ -163,6 +179,8 @@ typedef struct mpasg_fields {
   double *ac_rs, *ac_ts;                                            /* (C+1, L) */
   double *ac_x;                                                     /* (C+1, L+1) */
   double *b_tri, *c_tri;                                            /* (C+1, L) */
+  /* mixed form: theta_m and theta_m_save minus ref_theta (deviations advected in float32) */
+  double *theta_dev, *theta_save_dev;                               /* (C+1, L) */
   /* status flag word (device int32[4]) for the finite check */
   int32_t *status;
 } mpasg_fields;
@@ -196,6 +214,10 @@ int mpasg_step(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, void
  * boundaries (>= 0) or a negative status. */
 int mpasg_step_timed(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
                      void *const *events, int32_t *stage_kinds, int n_events, void *stream);
+/* Applies a helper of the mixed form to n device float64 values (in -> out), for testing
+ * the helpers against CUDA's own conversions and division: which = 0 float64 -> float32 ->
+ * float64 through the integer repacking; which = 1 the Newton-Raphson reciprocal. */
+int mpasg_numerics_check(int which, const double *in, double *out, long long n, void *stream);
 /* Count non-finite values of the prognostic fields into f->status[0] (async). */
 int mpasg_check_finite(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, void *stream);
 

@@ -13,6 +13,7 @@ import pathlib
 from .errors import MpasConfigError, MpasDeviceError, MpasExtensionMissingError, MpasNumericalError
 
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "libmpasg.so"
+ABI_VERSION = 2
 
 MESH_INT_DIMS = ("nCells", "nEdges", "nVertices", "nVertLevels", "maxEdges", "maxEdges2",
                  "vertexDegree", "nAdvMax", "flatTerrain", "reserved0")
@@ -26,12 +27,15 @@ MESH_DBL_PTRS = ("edgesOnCell_sign", "edgesOnVertex_sign", "dcEdge", "dvEdge", "
                  "defc_a", "defc_b", "fEdge",
                  "fVertex", "meshScalingDel2", "meshScalingDel4", "latCell", "lonCell",
                  "coeffs_reconstruct", "zb_cell", "zb3_cell", "zxu", "zz", "dss", "rho_base",
-                 "theta_base", "rdzw", "rdzu", "fzm", "fzp", "fnm", "fnp", "rdnw")
+                 "theta_base", "rdzw", "rdzu", "fzm", "fzp", "fnm", "fnp", "rdnw",
+                 "ref_theta", "ref_theta_w4", "ref_theta_w3", "ref_theta_w2")
 
 CONFIG_DOUBLES = ("dt", "epssm", "smdiv", "len_disp", "coef_3rd_order", "c_s", "visc4_2dsmag",
                   "del4u_div_factor", "apvm_upwinding", "h_mom_eddy_visc4", "h_theta_eddy_visc4")
 CONFIG_INTS = ("time_integration_order", "number_of_sub_steps", "dynamics_split_steps",
-               "monotonic", "horiz_mixing_smagorinsky", "num_scalars", "moist_start", "moist_end")
+               "monotonic", "horiz_mixing_smagorinsky", "num_scalars", "moist_start", "moist_end",
+               "precision", "reserved1")
+PRECISIONS = {"float64": 0, "mixed": 1}
 
 # (name, kind) in header order; kind names the row space: e/c/cw/v/cs/es/cws/L/cL/cLw/...
 FIELDS = (
@@ -73,6 +77,7 @@ FIELDS = (
     ("rho_int", "c"),
     ("flux_w_e", "e"), ("flux_th_e", "e"),
     ("ac_rs", "c"), ("ac_ts", "c"), ("ac_x", "cw"), ("b_tri", "c"), ("c_tri", "c"),
+    ("theta_dev", "c"), ("theta_save_dev", "c"),
 )
 
 
@@ -100,7 +105,7 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_dyn_tend", "mpasg_smlstep_pert", "mpasg_acoustic_step",
            "mpasg_divergence_damping", "mpasg_recover_large_step", "mpasg_solve_diagnostics",
            "mpasg_advance_scalars", "mpasg_advance_scalars_mono", "mpasg_reconstruct_2d",
-           "mpasg_advance_scalars_static")
+           "mpasg_advance_scalars_static", "mpasg_numerics_check")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -141,12 +146,13 @@ def load() -> C.CDLL:
         "mpasg_advance_scalars_mono": ([m, c, f, C.c_double, vp], C.c_int),
         "mpasg_reconstruct_2d": ([m, c, f, vp], C.c_int),
         "mpasg_advance_scalars_static": ([m, c, f, C.c_int, C.c_double, vp], C.c_int),
+        "mpasg_numerics_check": ([C.c_int, vp, vp, C.c_longlong, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = res
-    if lib.mpasg_abi_version() != 1:
+    if lib.mpasg_abi_version() != ABI_VERSION:
         raise MpasExtensionMissingError("libmpasg.so ABI version mismatch; rebuild it")
     _lib = lib
     return lib

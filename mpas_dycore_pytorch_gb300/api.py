@@ -35,6 +35,9 @@ DEFAULTS = {
     "config_rayleigh_damp_u": False, "config_mpas_cam_coef": 0.0,
     "config_curvature_u": False, "config_mix_full": True, "config_IAU_option": "off",
     "config_apply_lbcs": False, "config_dt": 720.0,
+    # GB300 extension (no reference counterpart): "float64" (the reference's arithmetic)
+    # or "mixed" (float32 horizontal stencils over float64 state, see include/mpasg.h)
+    "config_precision": "float64",
 }
 
 
@@ -65,6 +68,8 @@ def validate_supported(cfg: Mapping[str, Any]) -> None:
         bad.append("config_IAU_option")
     if str(cfg["config_horiz_mixing"]) not in ("2d_smagorinsky",):
         bad.append("config_horiz_mixing")
+    if str(cfg["config_precision"]) not in _lib.PRECISIONS:
+        bad.append("config_precision")
     if bad:
         raise MpasUnsupportedCapabilityError(f"unsupported on the GB300 path: {bad}")
 
@@ -102,6 +107,7 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
     c.num_scalars = int(num_scalars)
     c.moist_start = int(moist_start)
     c.moist_end = int(moist_end)
+    c.precision = _lib.PRECISIONS[str(cfg["config_precision"])]
     return c
 
 
@@ -114,9 +120,12 @@ class Model:
     """One mesh + configuration + timestep resident on a GPU: the native step and its state."""
 
     def __init__(self, mesh: Mapping[str, Any], config: Mapping[str, Any] | None, dt: float,
-                 num_scalars: int | None = None, device: str | torch.device = "cuda"):
+                 num_scalars: int | None = None, device: str | torch.device = "cuda",
+                 precision: str | None = None):
         self.lib = _lib.load()
         self.cfg = resolved_config(config)
+        if precision is not None:
+            self.cfg["config_precision"] = precision
         validate_supported(self.cfg)
         if not (math.isfinite(float(dt)) and float(dt) > 0.0):
             raise MpasConfigError("dt must be positive and finite")

@@ -34,6 +34,14 @@ __global__ void k_count_nonfinite(const double* __restrict__ p, long long n, int
   if (threadIdx.x == 0 && bad) atomicAdd(count, bad);
 }
 
+// mixed-form arithmetic helpers applied elementwise (mpasg_numerics_check)
+__global__ void k_numerics(int which, const double* __restrict__ in, double* __restrict__ out, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double x = in[i];
+  out[i] = which == 0 ? f2d_bits(d2f_bits(x)) : rcp_nr(x);
+}
+
 int fill(double* p, long long n, double v, cudaStream_t s) {
   k_fill_d<<<nblocks(n), kBlock, 0, s>>>(p, n, v);
   MPASG_LAUNCH_CHECK();
@@ -62,8 +70,16 @@ extern "C" int mpasg_abi_version(void) { return MPASG_ABI_VERSION; }
 
 extern "C" const char* mpasg_build_info(void) {
   static char buf[160];
-  snprintf(buf, sizeof(buf), "mpasg abi=%d cuda=%d arch=sm_103a float64", MPASG_ABI_VERSION, CUDART_VERSION);
+  snprintf(buf, sizeof(buf), "mpasg abi=%d cuda=%d arch=sm_103a float64+mixed", MPASG_ABI_VERSION, CUDART_VERSION);
   return buf;
+}
+
+extern "C" int mpasg_numerics_check(int which, const double* in, double* out, long long n, void* stream) {
+  if (!in || !out || n < 0 || (which != 0 && which != 1)) return MPASG_E_ARG;
+  if (n == 0) return MPASG_OK;
+  k_numerics<<<nblocks(n), kBlock, 0, (cudaStream_t)stream>>>(which, in, out, n);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
 }
 
 extern "C" int mpasg_check_finite(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, void* stream) {

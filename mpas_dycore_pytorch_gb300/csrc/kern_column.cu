@@ -51,17 +51,21 @@ struct VimpLevel {
   double cofwt, coftz;
 };
 
+// (float64 in both forms; T selects the division: exact in the float64 form, Newton
+// reciprocal in the mixed form)
+template <typename T>
 MPASG_D VimpLevel vimp_level(const mpasg_mesh& m, const mpasg_fields& f, size_t o, size_t ow, int k,
                              double dtseps, double rcv) {
   VimpLevel v;
   double zz = m.zz[o + k], p = f.exner[o + k];
   double rb = m.rho_base[o + k], rtb = f.rtheta_base[o + k], pb = f.exner_base[o + k];
   double rt = f.rtheta_p[o + k], q = f.qtot[o + k];
-  v.cofwt = 0.5 * dtseps * rcv * zz * kGravity * rb / (1.0 + q) * p / ((rtb + rt) * pb);
+  v.cofwt = fdiv<T>(fdiv<T>(0.5 * dtseps * rcv * zz * kGravity * rb, 1.0 + q) * p, (rtb + rt) * pb);
   v.coftz = (k == 0) ? 0.0 : dtseps * (m.fzm[k] * f.theta_m[o + k] + m.fzp[k] * f.theta_m[o + k - 1]);
   return v;
 }
 
+template <typename T>
 __global__ void __launch_bounds__(kBlock) k_vimp_coefs(mpasg_mesh m, mpasg_fields f, FastDiv fl, double dts,
                                                        double epssm) {
   __shared__ double s_cw[kBlock], s_ct[kBlock];
@@ -79,7 +83,7 @@ __global__ void __launch_bounds__(kBlock) k_vimp_coefs(mpasg_mesh m, mpasg_field
     k = i - c * L;
     o = (size_t)c * L;
     ow = (size_t)c * (L + 1);
-    me_ = vimp_level(m, f, o, ow, k, dtseps, rcv);
+    me_ = vimp_level<T>(m, f, o, ow, k, dtseps, rcv);
     if (c == 0) f.cofrz[k] = dtseps * m.rdzw[k];
   }
   s_cw[threadIdx.x] = me_.cofwt;
@@ -107,10 +111,11 @@ __global__ void __launch_bounds__(kBlock) k_vimp_coefs(mpasg_mesh m, mpasg_field
   f.cofwz[o + k] = cofwz;
   // neighbour levels (k-1 below, k+1 above) from shared memory or recomputed at block edges
   VimpLevel lo = (threadIdx.x >= 1) ? VimpLevel{s_cw[threadIdx.x - 1], s_ct[threadIdx.x - 1]}
-                                    : vimp_level(m, f, o, ow, k - 1, dtseps, rcv);
+                                    : vimp_level<T>(m, f, o, ow, k - 1, dtseps, rcv);
   double ct_kp1 = 0.0;
   if (k + 1 < (uint32_t)L)
-    ct_kp1 = (threadIdx.x + 1 < blockDim.x) ? s_ct[threadIdx.x + 1] : vimp_level(m, f, o, ow, k + 1, dtseps, rcv).coftz;
+    ct_kp1 = (threadIdx.x + 1 < blockDim.x) ? s_ct[threadIdx.x + 1]
+                                            : vimp_level<T>(m, f, o, ow, k + 1, dtseps, rcv).coftz;
   const double ct_km1 = lo.coftz, ct_k = me_.coftz;
   const double cw_k = me_.cofwt, cw_km1 = lo.cofwt;
   const double rdzw_k = m.rdzw[k], rdzw_km1 = m.rdzw[k - 1];
@@ -121,6 +126,7 @@ __global__ void __launch_bounds__(kBlock) k_vimp_coefs(mpasg_mesh m, mpasg_field
   f.c_tri[o + k] = -cofwz * ct_kp1 * rdzw_k * zz - cofwr * cofrz_k + cw_k * ct_kp1 * rdzw_k;
 }
 
+template <typename T>
 __global__ void k_vimp_factor(mpasg_mesh m, mpasg_fields f) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.nCells) return;
@@ -130,7 +136,7 @@ __global__ void k_vimp_factor(mpasg_mesh m, mpasg_fields f) {
   f.alpha_tri[o] = 0.0;
   f.gamma_tri[o] = 0.0;
   for (int k = 1; k < L; ++k) {
-    double alpha = 1.0 / (f.b_tri[o + k] - f.a_tri[o + k] * gam);
+    double alpha = fdiv<T>(1.0, f.b_tri[o + k] - f.a_tri[o + k] * gam);
     gam = f.c_tri[o + k] * alpha;
     f.alpha_tri[o + k] = alpha;
     f.gamma_tri[o + k] = gam;
@@ -139,6 +145,9 @@ __global__ void k_vimp_factor(mpasg_mesh m, mpasg_fields f) {
 
 // ---------------------------------------------------------------- acoustic substep, edges
 // dynamics/acoustic_step.py:576 (_acoustic_step_horizontal_momentum_update)
+// The increment dts (tend_u - pgrad) is formed in the stencil type T; ru_p and ruAvg
+// accumulate in float64.
+template <typename T>
 __global__ void k_acoustic_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl, int small_step,
                                  double dts, double c2) {
   const int L = m.nVertLevels;
@@ -148,14 +157,15 @@ __global__ void k_acoustic_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl, int s
   if (small_step != 1) {
     int c1 = m.cellsOnEdge[2 * e], c2i = m.cellsOnEdge[2 * e + 1];
     size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2i * L + k;
-    double pgrad = div_or_one((f.rtheta_pp[i2] - f.rtheta_pp[i1]) * m.invDcEdge[e], 0.5 * (m.zz[i2] + m.zz[i1]));
-    pgrad = f.cqu_e[i] * 0.5 * c2 * (f.exner[i1] + f.exner[i2]) * pgrad;
-    pgrad = pgrad + 0.5 * m.zxu[i] * kGravity * (f.rho_pp[i1] + f.rho_pp[i2]);
-    double rup = f.ru_p[i] + dts * (f.tend_u[i] - pgrad);
+    T pgrad = div_or_one<T>((cv<T>(f.rtheta_pp[i2]) - cv<T>(f.rtheta_pp[i1])) * cv<T>(m.invDcEdge[e]),
+                            T(0.5) * (cv<T>(m.zz[i2]) + cv<T>(m.zz[i1])));
+    pgrad = cv<T>(f.cqu_e[i]) * T(0.5) * cv<T>(c2) * (cv<T>(f.exner[i1]) + cv<T>(f.exner[i2])) * pgrad;
+    pgrad = pgrad + T(0.5) * cv<T>(m.zxu[i]) * T(kGravity) * (cv<T>(f.rho_pp[i1]) + cv<T>(f.rho_pp[i2]));
+    double rup = f.ru_p[i] + f64(cv<T>(dts) * (cv<T>(f.tend_u[i]) - pgrad));
     f.ru_p[i] = rup;
     f.ruAvg[i] = f.ruAvg[i] + rup;
   } else {
-    double rup = dts * f.tend_u[i];
+    double rup = f64(cv<T>(dts) * cv<T>(f.tend_u[i]));
     f.ru_p[i] = rup;
     f.ruAvg[i] = rup;
   }
@@ -174,20 +184,24 @@ struct AcLevel {
   double rs, ts, rho_in, rt_in;
 };
 
+// The horizontal flux sums (and dts times the tendencies) are formed in the stencil
+// type T; the right-hand side combines them with the implicit coefficients in float64.
+template <typename T>
 MPASG_D AcLevel ac_level(const mpasg_mesh& m, const mpasg_fields& f, int c, int k, bool first, double dts,
                          double resm) {
   const int L = m.nVertLevels;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  const double inv_area = m.invAreaCell[c];
+  const T inv_area = cv<T>(m.invAreaCell[c]);
+  const T dts_t = cv<T>(dts);
   const double* th1 = f.theta_m_save;  // time-level-1 theta_m
-  double rs = 0.0, ts = 0.0;
+  T rs = T(0), ts = T(0);
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
-    double wgt = m.edgesOnCell_sign[c * me + j] * m.dvEdge[e];
-    double flux = dts * wgt * f.ru_p[(size_t)e * L + k] * inv_area;
+    T wgt = cv<T>(m.edgesOnCell_sign[c * me + j]) * cv<T>(m.dvEdge[e]);
+    T flux = dts_t * wgt * cv<T>(f.ru_p[(size_t)e * L + k]) * inv_area;
     int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-    double th_e = 0.5 * (th1[(size_t)c2 * L + k] + th1[(size_t)c1 * L + k]);
+    T th_e = T(0.5) * (cv<T>(th1[(size_t)c2 * L + k]) + cv<T>(th1[(size_t)c1 * L + k]));
     if (j == 0) {
       rs = -flux;
       ts = -(flux * th_e);
@@ -203,12 +217,13 @@ MPASG_D AcLevel ac_level(const mpasg_mesh& m, const mpasg_fields& f, int c, int 
   a.rt_in = first ? 0.0 : f.rtheta_pp[o];
   double rwp_k = first ? 0.0 : f.rw_p[ow];
   double rwp_k1 = first ? 0.0 : f.rw_p[ow + 1];
-  a.rs = a.rho_in + dts * f.tend_rho[o] + rs - f.cofrz[k] * resm * (rwp_k1 - rwp_k);
-  a.ts = a.rt_in + dts * f.tend_theta[o] + ts -
+  a.rs = a.rho_in + f64(dts_t * cv<T>(f.tend_rho[o])) + f64(rs) - f.cofrz[k] * resm * (rwp_k1 - rwp_k);
+  a.ts = a.rt_in + f64(dts_t * cv<T>(f.tend_theta[o])) + f64(ts) -
          resm * m.rdzw[k] * (f.coftz[ow + 1] * rwp_k1 - f.coftz[ow] * rwp_k);
   return a;
 }
 
+template <typename T>
 __global__ void __launch_bounds__(kBlock) k_ac_prep(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int small_step,
                                                     double dts, double epssm, double resm) {
   __shared__ AcLevel s_lv[kBlock];
@@ -221,7 +236,7 @@ __global__ void __launch_bounds__(kBlock) k_ac_prep(mpasg_mesh m, mpasg_fields f
   if (active) {
     c = fl1.div(i);
     k = i - c * (L + 1);
-    if (k < (uint32_t)L) lv = ac_level(m, f, c, k, first, dts, resm);
+    if (k < (uint32_t)L) lv = ac_level<T>(m, f, c, k, first, dts, resm);
   }
   s_lv[threadIdx.x] = lv;
   __syncthreads();
@@ -239,7 +254,7 @@ __global__ void __launch_bounds__(kBlock) k_ac_prep(mpasg_mesh m, mpasg_fields f
     if (first) f.wwAvg[ow + k] = 0.0;
     return;
   }
-  AcLevel lo = (threadIdx.x >= 1) ? s_lv[threadIdx.x - 1] : ac_level(m, f, c, k - 1, first, dts, resm);
+  AcLevel lo = (threadIdx.x >= 1) ? s_lv[threadIdx.x - 1] : ac_level<T>(m, f, c, k - 1, first, dts, resm);
   const double ww_in = first ? 0.0 : f.wwAvg[ow + k];
   f.wwAvg[ow + k] = ww_in + 0.5 * (1.0 - epssm) * rwp_k;
   const double zz_k = m.zz[o + k], zz_km1 = m.zz[o + k - 1];
@@ -312,6 +327,8 @@ __global__ void __launch_bounds__(kBlock) k_ac_post(mpasg_mesh m, mpasg_fields f
 
 // ---------------------------------------------------------------- divergence damping
 // dynamics/divergence_damping.py:187-299
+// (the increment in the stencil type T, ru_p accumulated in float64)
+template <typename T>
 __global__ void k_divergence_damping(mpasg_mesh m, mpasg_fields f, FastDiv fl, double coef) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -319,13 +336,14 @@ __global__ void k_divergence_damping(mpasg_mesh m, mpasg_fields f, FastDiv fl, d
   uint32_t e = fl.div(i), k = i - e * L;
   int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
   size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
-  double d1 = -(f.rtheta_pp[i1] - f.rtheta_pp_old[i1]);
-  double d2 = -(f.rtheta_pp[i2] - f.rtheta_pp_old[i2]);
-  f.ru_p[i] = f.ru_p[i] + coef * (d2 - d1) / (f.theta_m_save[i1] + f.theta_m_save[i2]);
+  T d1 = -dif<T>(f.rtheta_pp[i1], f.rtheta_pp_old[i1]);  // substep change: float64 difference
+  T d2 = -dif<T>(f.rtheta_pp[i2], f.rtheta_pp_old[i2]);
+  f.ru_p[i] = f.ru_p[i] + f64(cv<T>(coef) * (d2 - d1) / (cv<T>(f.theta_m_save[i1]) + cv<T>(f.theta_m_save[i2])));
 }
 
 // ---------------------------------------------------------------- small-step perturbation
 // dynamics/smlstep_pert.py:197-373
+template <typename T>
 __global__ void k_smlstep_pert(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -336,25 +354,56 @@ __global__ void k_smlstep_pert(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
     return;
   }
   const int me = m.maxEdges;
-  double fzm = m.fzm[k], fzp = m.fzp[k];
-  double acc = f.tend_w[i];
+  const T fzm = cv<T>(m.fzm[k]), fzp = cv<T>(m.fzp[k]);
+  T acc = cv<T>(f.tend_w[i]);
   const int n = m.flatTerrain ? 0 : m.nEdgesOnCell[c];  // zero-slope terms add exact zeros
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
-    double ut_k = f.tend_u[(size_t)e * L + k];
-    double u_i = fzm * ut_k + fzp * f.tend_u[(size_t)e * L + k - 1];
-    double flux = m.edgesOnCell_sign[c * me + j] * u_i;
+    T ut_k = cv<T>(f.tend_u[(size_t)e * L + k]);
+    T u_i = fzm * ut_k + fzp * cv<T>(f.tend_u[(size_t)e * L + k - 1]);
+    T flux = cv<T>(m.edgesOnCell_sign[c * me + j]) * u_i;
     size_t zi = ((size_t)c * me + j) * (L + 1) + k;
-    double coef = m.zb_cell[zi] + sgn(ut_k) * m.zb3_cell[zi];
+    T coef = cv<T>(m.zb_cell[zi]) + (ut_k >= T(0) ? T(1) : T(-1)) * cv<T>(m.zb3_cell[zi]);
     acc = acc - coef * flux;
   }
   size_t o = (size_t)c * L;
-  f.tend_rw[i] = (fzm * m.zz[o + k] + fzp * m.zz[o + k - 1]) * acc;
+  f.tend_rw[i] = f64((fzm * cv<T>(m.zz[o + k]) + fzp * cv<T>(m.zz[o + k - 1])) * acc);
 }
 
 // ---------------------------------------------------------------- large-step recovery
 // dynamics/recover_large_step.py:414-466 (density / theta / Exner), :485-513 (edges),
 // :329-411 (w from omega with zb/zb3 slot fluxes)
+// Binomial coefficients C(a, n) = a (a-1) ... (a-n+1) / n!, n = 0..11 (compile time).
+struct BinomTable {
+  double c[12];
+};
+__host__ __device__ constexpr BinomTable binom_table(double a) {
+  BinomTable b{};
+  double t = 1.0;
+  b.c[0] = 1.0;
+  for (int n = 1; n < 12; ++n) {
+    t = t * (a - (n - 1)) / n;
+    b.c[n] = t;
+  }
+  return b;
+}
+
+// (1 + x)^(R/cv) - 1 for |x| < 0.02 by its binomial series, 11 terms in float64 Horner
+// form (truncation below 1e-19 relative): no cancellation against 1, unlike pow - 1.
+MPASG_D double pow1p_rcv_m1(double x) {
+  constexpr BinomTable t = binom_table(kRgas / (kCp - kRgas));
+  double p = t.c[11];
+#pragma unroll
+  for (int n = 10; n >= 1; --n) p = fma(p, x, t.c[n]);
+  return p * x;
+}
+
+// Float64 in both forms; T selects the division (exact / Newton reciprocal) and, at
+// rk 3, the Exner function: pow in the float64 form; in the mixed form the identity
+// exner = exner_base (1 + x)^(R/cv), x = rtheta_p / rtheta_base, with the increment
+// exner - exner_base = exner_base pow1p_rcv_m1(x) (pow when |x| >= 0.02), so the
+// pressure perturbation needs no difference of nearly equal Exner values.
+template <typename T>
 __global__ void k_recover_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int rk_step, double inv_ns,
                                 double rk_dt) {
   const int L = m.nVertLevels;
@@ -374,13 +423,28 @@ __global__ void k_recover_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int r
     f.rho_p[o] = rho_p;
     f.rho_zz[o] = rho_zz;
     f.rtheta_p[o] = rtheta_p;
-    f.theta_m[o] = (rtheta_p + rtb) / rho_zz;
+    f.theta_m[o] = fdiv<T>(rtheta_p + rtb, rho_zz);
     if (rk_step == 3) {
       const double rcv = kRgas / (kCp - kRgas);
       double zz = m.zz[o];
-      double ex = pow(zz * (kRgas / kP0) * (rtheta_p + rtb), rcv);
-      f.exner[o] = ex;
-      f.pressure_p[o] = zz * kRgas * __dadd_rn(__dmul_rn(ex, rtheta_p), __dmul_rn(rtb, ex - f.exner_base[o]));
+      if (sizeof(T) == sizeof(double)) {
+        double ex = pow(zz * (kRgas / kP0) * (rtheta_p + rtb), rcv);
+        f.exner[o] = ex;
+        f.pressure_p[o] = zz * kRgas * __dadd_rn(__dmul_rn(ex, rtheta_p), __dmul_rn(rtb, ex - f.exner_base[o]));
+      } else {
+        const double exb = f.exner_base[o];
+        const double x = fdiv<T>(rtheta_p, rtb);
+        double ex, dex;  // exner and exner - exner_base
+        if (fabs(x) < 0.02) {
+          dex = exb * pow1p_rcv_m1(x);
+          ex = exb + dex;
+        } else {
+          ex = pow(zz * (kRgas / kP0) * (rtheta_p + rtb), rcv);
+          dex = ex - exb;
+        }
+        f.exner[o] = ex;
+        f.pressure_p[o] = zz * kRgas * (ex * rtheta_p + rtb * dex);
+      }
     }
   }
   if (k >= 1 && k < (uint32_t)L) {
@@ -390,10 +454,12 @@ __global__ void k_recover_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int r
     double rw = rws + f.rw_p[ow];
     f.rw[ow] = rw;
     size_t oc = (size_t)c * L;
-    f.w[ow] = div_or_one(rw, m.fzm[k] * m.zz[oc + k] + m.fzp[k] * m.zz[oc + k - 1]);
+    const double den = m.fzm[k] * m.zz[oc + k] + m.fzp[k] * m.zz[oc + k - 1];
+    f.w[ow] = den == 1.0 ? rw : fdiv<T>(rw, den);
   }
 }
 
+template <typename T>
 __global__ void k_recover_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl, double inv_ns) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -404,9 +470,10 @@ __global__ void k_recover_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl, double
   f.ruAvg[i] = rus + f.ruAvg[i] * inv_ns;
   double ru = rus + f.ru_p[i];
   f.ru[i] = ru;
-  f.u[i] = 2.0 * ru / (f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k]);
+  f.u[i] = fdiv<T>(2.0 * ru, f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k]);
 }
 
+template <typename T>
 __global__ void k_recover_w(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -442,7 +509,20 @@ __global__ void k_recover_w(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
     double ci = m.zb_cell[zi] + sgn(fi) * m.zb3_cell[zi];
     acc = acc + m.edgesOnCell_sign[c * me + j] * ci * fi;
   }
-  f.w[i] = acc / (fzm * f.rho_zz[oc + k] + fzp * f.rho_zz[oc + k - 1]);
+  f.w[i] = fdiv<T>(acc, fzm * f.rho_zz[oc + k] + fzp * f.rho_zz[oc + k - 1]);
+}
+
+template <typename T>
+int launch_recover(const mpasg_mesh* m, mpasg_fields* f, int rk_step, double inv_ns, double rk_dt, cudaStream_t s) {
+  const int L = m->nVertLevels;
+  const long long ncw = (long long)m->nCells * (L + 1);
+  k_recover_cells<T><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), rk_step, inv_ns, rk_dt);
+  MPASG_LAUNCH_CHECK();
+  k_recover_edges<T><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), inv_ns);
+  MPASG_LAUNCH_CHECK();
+  k_recover_w<T><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1));
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
 }
 
 }  // namespace
@@ -467,9 +547,15 @@ extern "C" int mpasg_vert_imp_coefs(const mpasg_mesh* m, const mpasg_config* c, 
   if (!m || !c || !f) return MPASG_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const int L = m->nVertLevels;
-  k_vimp_coefs<<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), dts, c->epssm);
-  MPASG_LAUNCH_CHECK();
-  k_vimp_factor<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
+  if (c->precision == MPASG_PRECISION_MIXED) {
+    k_vimp_coefs<float><<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), dts, c->epssm);
+    MPASG_LAUNCH_CHECK();
+    k_vimp_factor<float><<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
+  } else {
+    k_vimp_coefs<double><<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), dts, c->epssm);
+    MPASG_LAUNCH_CHECK();
+    k_vimp_factor<double><<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
+  }
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }
@@ -482,12 +568,20 @@ extern "C" int mpasg_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, m
   const double rcv = kRgas / (kCp - kRgas);
   const double c2 = kCp * rcv;
   const double resm = (1.0 - c->epssm) / (1.0 + c->epssm);
-  k_acoustic_edges<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), small_step,
-                                                                         dts, c2);
-  MPASG_LAUNCH_CHECK();
   const long long ncw = (long long)m->nCells * (L + 1);
-  k_ac_prep<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, dts, c->epssm, resm);
-  MPASG_LAUNCH_CHECK();
+  if (c->precision == MPASG_PRECISION_MIXED) {
+    k_acoustic_edges<float><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), small_step,
+                                                                                dts, c2);
+    MPASG_LAUNCH_CHECK();
+    k_ac_prep<float><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, dts, c->epssm, resm);
+    MPASG_LAUNCH_CHECK();
+  } else {
+    k_acoustic_edges<double><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), small_step,
+                                                                                 dts, c2);
+    MPASG_LAUNCH_CHECK();
+    k_ac_prep<double><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, dts, c->epssm, resm);
+    MPASG_LAUNCH_CHECK();
+  }
   k_ac_thomas<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
   MPASG_LAUNCH_CHECK();
   k_ac_post<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), dts, c->epssm);
@@ -500,8 +594,12 @@ extern "C" int mpasg_divergence_damping(const mpasg_mesh* m, const mpasg_config*
   if (!m || !c || !f) return MPASG_E_ARG;
   const int L = m->nVertLevels;
   double coef = 2.0 * c->smdiv * c->len_disp / dts;
-  k_divergence_damping<<<nblocks((long long)m->nEdges * L), kBlock, 0, (cudaStream_t)stream>>>(
-      *m, *f, FastDiv(L), coef);
+  if (c->precision == MPASG_PRECISION_MIXED)
+    k_divergence_damping<float><<<nblocks((long long)m->nEdges * L), kBlock, 0, (cudaStream_t)stream>>>(
+        *m, *f, FastDiv(L), coef);
+  else
+    k_divergence_damping<double><<<nblocks((long long)m->nEdges * L), kBlock, 0, (cudaStream_t)stream>>>(
+        *m, *f, FastDiv(L), coef);
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }
@@ -510,8 +608,12 @@ extern "C" int mpasg_smlstep_pert(const mpasg_mesh* m, const mpasg_config* c, mp
                                   void* stream) {
   if (!m || !c || !f) return MPASG_E_ARG;
   const int L = m->nVertLevels;
-  k_smlstep_pert<<<nblocks((long long)m->nCells * (L + 1)), kBlock, 0, (cudaStream_t)stream>>>(
-      *m, *f, FastDiv(L + 1));
+  if (c->precision == MPASG_PRECISION_MIXED)
+    k_smlstep_pert<float><<<nblocks((long long)m->nCells * (L + 1)), kBlock, 0, (cudaStream_t)stream>>>(
+        *m, *f, FastDiv(L + 1));
+  else
+    k_smlstep_pert<double><<<nblocks((long long)m->nCells * (L + 1)), kBlock, 0, (cudaStream_t)stream>>>(
+        *m, *f, FastDiv(L + 1));
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }
@@ -520,14 +622,8 @@ extern "C" int mpasg_recover_large_step(const mpasg_mesh* m, const mpasg_config*
                                         int rk_step, int ns, double rk_dt, void* stream) {
   if (!m || !c || !f || ns < 1) return MPASG_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
-  const int L = m->nVertLevels;
   const double inv_ns = 1.0 / (double)ns;
-  long long ncw = (long long)m->nCells * (L + 1);
-  k_recover_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), rk_step, inv_ns, rk_dt);
-  MPASG_LAUNCH_CHECK();
-  k_recover_edges<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), inv_ns);
-  MPASG_LAUNCH_CHECK();
-  k_recover_w<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1));
-  MPASG_LAUNCH_CHECK();
-  return MPASG_OK;
+  if (c->precision == MPASG_PRECISION_MIXED)
+    return launch_recover<float>(m, f, rk_step, inv_ns, rk_dt, s);
+  return launch_recover<double>(m, f, rk_step, inv_ns, rk_dt, s);
 }

@@ -5,42 +5,50 @@
 
 namespace {
 
+// Every diagnostic kernel is a template on the stencil arithmetic type T (common.cuh):
+// double for the float64 form, float for the mixed form.
+
 // h_edge and the edge kinetic-energy weights
+template <typename T>
 __global__ void k_diag_edges_a(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)m.nEdges * L) return;
   uint32_t e = fl.div(i), k = i - e * L;
   int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-  f.h_edge[i] = 0.5 * (f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k]);
-  double u = f.u[i];
-  f.ke_edge[i] = (m.dcEdge[e] * m.dvEdge[e]) * (u * u);
+  f.h_edge[i] = f64(T(0.5) * (cv<T>(f.rho_zz[(size_t)c1 * L + k]) + cv<T>(f.rho_zz[(size_t)c2 * L + k])));
+  const T u = cv<T>(f.u[i]);
+  f.ke_edge[i] = f64((cv<T>(m.dcEdge[e]) * cv<T>(m.dvEdge[e])) * (u * u));
 }
 
 // vorticity, vertex kinetic energy and potential vorticity
+template <typename T>
 __global__ void k_diag_vertices(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)m.nVertices * L) return;
   uint32_t v = fl.div(i), k = i - v * L;
   const int vd = m.vertexDegree;
-  double vort = 0.0, kev = 0.0;
+  // the circulation sum cancels strongly: float64 in both forms
+  double vort = 0.0;
+  T kev = T(0);
   for (int j = 0; j < vd; ++j) {
     int e = m.edgesOnVertex[v * vd + j];
     double wgt = m.edgesOnVertex_sign[v * vd + j] * m.dcEdge[e];
     double t = wgt * f.u[(size_t)e * L + k];
-    double ke = f.ke_edge[(size_t)e * L + k];
+    T ke = cv<T>(f.ke_edge[(size_t)e * L + k]);
     vort = (j == 0) ? t : vort + t;
     kev = (j == 0) ? ke : kev + ke;
   }
-  double iat = m.invAreaTriangle[v];
+  const double iat = m.invAreaTriangle[v];
   vort = vort * iat;
   f.vorticity[i] = vort;
-  f.ke_vertex[i] = 0.25 * iat * kev;
+  f.ke_vertex[i] = f64(T(0.25) * cv<T>(iat) * kev);
   f.pv_vertex[i] = m.fVertex[v] + vort;
 }
 
 // divergence, cell kinetic energy (with the vertex-kite blend) and cell PV for APVM
+template <typename T>
 __global__ void k_diag_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, int apvm) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -48,43 +56,46 @@ __global__ void k_diag_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, int apvm)
   uint32_t c = fl.div(i), k = i - c * L;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  double div = 0.0, ke = 0.0;
+  // the divergence sum cancels strongly: float64 in both forms
+  double div = 0.0;
+  T ke = T(0);
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
     double wgt = m.edgesOnCell_sign[c * me + j] * m.dvEdge[e];
     double t = wgt * f.u[(size_t)e * L + k];
-    double kt = 0.25 * f.ke_edge[(size_t)e * L + k];
+    T kt = T(0.25) * cv<T>(f.ke_edge[(size_t)e * L + k]);
     div = (j == 0) ? t : div + t;
     ke = (j == 0) ? kt : ke + kt;
   }
-  const double ia = m.invAreaCell[c];
-  div = div * ia;
+  div = div * m.invAreaCell[c];
+  const T ia = cv<T>(m.invAreaCell[c]);
   ke = ke * ia;
-  const double ke_fact = 1.0 - 0.375;
+  const T ke_fact = T(1.0 - 0.375);
   ke = ke_fact * ke;
   const int vd = m.vertexDegree;
-  double pvc = 0.0;
+  T pvc = T(0);
   for (int j = 0; j < n; ++j) {
     int v = m.verticesOnCell[c * me + j];
     int kk = m.kiteForCell[c * me + j];
     if (v >= m.nVertices || kk < 0) continue;
-    double kite = m.kiteAreasOnVertex[v * vd + kk];
-    double t = (1.0 - ke_fact) * kite;
-    t = t * f.ke_vertex[(size_t)v * L + k];
+    T kite = cv<T>(m.kiteAreasOnVertex[v * vd + kk]);
+    T t = (T(1) - ke_fact) * kite;
+    t = t * cv<T>(f.ke_vertex[(size_t)v * L + k]);
     t = t * ia;
     ke = ke + t;
     if (apvm) {
-      double pt = kite * f.pv_vertex[(size_t)v * L + k];
+      T pt = kite * cv<T>(f.pv_vertex[(size_t)v * L + k]);
       pt = pt * ia;
       pvc = (j == 0) ? pt : pvc + pt;
     }
   }
   f.divergence[i] = div;
-  f.ke[i] = ke;
-  if (apvm) f.pv_cell[i] = pvc;
+  f.ke[i] = f64(ke);
+  if (apvm) f.pv_cell[i] = f64(pvc);
 }
 
 // pv_edge (with APVM upwinding) and, at rk 3 / preparation, the TRiSK tangential wind
+template <typename T>
 __global__ void k_diag_edges_b(mpasg_mesh m, mpasg_fields f, FastDiv fl, int recompute_v, double apvm_dt,
                                int apvm) {
   const int L = m.nVertLevels;
@@ -92,33 +103,39 @@ __global__ void k_diag_edges_b(mpasg_mesh m, mpasg_fields f, FastDiv fl, int rec
   if (i >= (uint32_t)m.nEdges * L) return;
   uint32_t e = fl.div(i), k = i - e * L;
   int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
-  double pv1 = f.pv_vertex[(size_t)v1 * L + k], pv2 = f.pv_vertex[(size_t)v2 * L + k];
-  double pve = 0.5 * (pv1 + pv2);
-  double vv;
+  const T pv1 = cv<T>(f.pv_vertex[(size_t)v1 * L + k]), pv2 = cv<T>(f.pv_vertex[(size_t)v2 * L + k]);
+  T pve = T(0.5) * (pv1 + pv2);
+  T vv;
   if (recompute_v) {
     const int n2 = m.nEdgesOnEdge[e];
     const int me2 = m.maxEdges2;
-    vv = 0.0;
+    vv = T(0);
     for (int j = 0; j < n2; ++j) {
       int eo = m.edgesOnEdge[e * me2 + j];
-      double t = m.weightsOnEdge[e * me2 + j] * f.u[(size_t)eo * L + k];
+      T t = cv<T>(m.weightsOnEdge[e * me2 + j]) * cv<T>(f.u[(size_t)eo * L + k]);
       vv = (j == 0) ? t : vv + t;
     }
-    f.v[i] = vv;
+    f.v[i] = f64(vv);
   } else {
-    vv = f.v[i];
+    vv = cv<T>(f.v[i]);
   }
   if (apvm) {
     int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-    double grad_pvt = (pv2 - pv1) * m.invDvEdge[e];
-    double grad_pvn = (f.pv_cell[(size_t)c2 * L + k] - f.pv_cell[(size_t)c1 * L + k]) * m.invDcEdge[e];
-    double delta = apvm_dt * (vv * grad_pvt + f.u[i] * grad_pvn);
+    T grad_pvt = (pv2 - pv1) * cv<T>(m.invDvEdge[e]);
+    T grad_pvn = (cv<T>(f.pv_cell[(size_t)c2 * L + k]) - cv<T>(f.pv_cell[(size_t)c1 * L + k])) * cv<T>(m.invDcEdge[e]);
+    T delta = cv<T>(apvm_dt) * (vv * grad_pvt + cv<T>(f.u[i]) * grad_pvn);
     pve = pve - delta;
   }
-  f.pv_edge[i] = pve;
+  f.pv_edge[i] = f64(pve);
 }
 
+MPASG_D double vcos(double x) { return cos(x); }
+MPASG_D float vcos(float x) { return cosf(x); }
+MPASG_D double vsin(double x) { return sin(x); }
+MPASG_D float vsin(float x) { return sinf(x); }
+
 // mpas_reconstruct_2d: RBF reconstruction of the cell-centre wind
+template <typename T>
 __global__ void k_reconstruct(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -126,25 +143,25 @@ __global__ void k_reconstruct(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   uint32_t c = fl.div(i), k = i - c * L;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  double x = 0.0, y = 0.0, z = 0.0;
+  T x = T(0), y = T(0), z = T(0);
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
-    double u = f.u[(size_t)e * L + k];
+    T u = cv<T>(f.u[(size_t)e * L + k]);
     const double* cr = m.coeffs_reconstruct + ((size_t)c * me + j) * 3;
-    double tx = cr[0] * u, ty = cr[1] * u, tz = cr[2] * u;
+    T tx = cv<T>(cr[0]) * u, ty = cv<T>(cr[1]) * u, tz = cv<T>(cr[2]) * u;
     if (j == 0) {
       x = tx; y = ty; z = tz;
     } else {
       x = x + tx; y = y + ty; z = z + tz;
     }
   }
-  double lat = m.latCell[c], lon = m.lonCell[c];
-  double clat = cos(lat), slat = sin(lat), clon = cos(lon), slon = sin(lon);
-  f.uReconstructX[i] = x;
-  f.uReconstructY[i] = y;
-  f.uReconstructZ[i] = z;
-  f.uReconstructZonal[i] = -x * slon + y * clon;
-  f.uReconstructMeridional[i] = -(x * clon + y * slon) * slat + z * clat;
+  const T lat = cv<T>(m.latCell[c]), lon = cv<T>(m.lonCell[c]);
+  const T clat = vcos(lat), slat = vsin(lat), clon = vcos(lon), slon = vsin(lon);
+  f.uReconstructX[i] = f64(x);
+  f.uReconstructY[i] = f64(y);
+  f.uReconstructZ[i] = f64(z);
+  f.uReconstructZonal[i] = f64(-x * slon + y * clon);
+  f.uReconstructMeridional[i] = f64(-(x * clon + y * slon) * slat + z * clat);
 }
 
 // ---------------------------------------------------------------- cold-start preparation
@@ -214,31 +231,40 @@ __global__ void k_prepare_rw(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
   f.rw[i] = rw;
 }
 
+template <typename T>
+int launch_diagnostics(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step, cudaStream_t s) {
+  const int L = m->nVertLevels;
+  FastDiv fl(L);
+  const int apvm = c->apvm_upwinding > 0.0 ? 1 : 0;
+  k_diag_edges_a<T><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, fl);
+  MPASG_LAUNCH_CHECK();
+  k_diag_vertices<T><<<nblocks((long long)m->nVertices * L), kBlock, 0, s>>>(*m, *f, fl);
+  MPASG_LAUNCH_CHECK();
+  k_diag_cells<T><<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, fl, apvm);
+  MPASG_LAUNCH_CHECK();
+  k_diag_edges_b<T><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(
+      *m, *f, fl, rk_step == 3 ? 1 : 0, c->apvm_upwinding * c->dt, apvm);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
 }  // namespace
 
 extern "C" int mpasg_solve_diagnostics(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step,
                                        void* stream) {
   if (!m || !c || !f) return MPASG_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
-  const int L = m->nVertLevels;
-  FastDiv fl(L);
-  const int apvm = c->apvm_upwinding > 0.0 ? 1 : 0;
-  k_diag_edges_a<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, fl);
-  MPASG_LAUNCH_CHECK();
-  k_diag_vertices<<<nblocks((long long)m->nVertices * L), kBlock, 0, s>>>(*m, *f, fl);
-  MPASG_LAUNCH_CHECK();
-  k_diag_cells<<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, fl, apvm);
-  MPASG_LAUNCH_CHECK();
-  k_diag_edges_b<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(
-      *m, *f, fl, rk_step == 3 ? 1 : 0, c->apvm_upwinding * c->dt, apvm);
-  MPASG_LAUNCH_CHECK();
-  return MPASG_OK;
+  if (c->precision == MPASG_PRECISION_MIXED) return launch_diagnostics<float>(m, c, f, rk_step, s);
+  return launch_diagnostics<double>(m, c, f, rk_step, s);
 }
 
 extern "C" int mpasg_reconstruct_2d(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, void* stream) {
   if (!m || !c || !f) return MPASG_E_ARG;
   const int L = m->nVertLevels;
-  k_reconstruct<<<nblocks((long long)m->nCells * L), kBlock, 0, (cudaStream_t)stream>>>(*m, *f, FastDiv(L));
+  if (c->precision == MPASG_PRECISION_MIXED)
+    k_reconstruct<float><<<nblocks((long long)m->nCells * L), kBlock, 0, (cudaStream_t)stream>>>(*m, *f, FastDiv(L));
+  else
+    k_reconstruct<double><<<nblocks((long long)m->nCells * L), kBlock, 0, (cudaStream_t)stream>>>(*m, *f, FastDiv(L));
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }
@@ -259,7 +285,9 @@ extern "C" int mpasg_prepare(const mpasg_mesh* m, const mpasg_config* c, mpasg_f
   MPASG_LAUNCH_CHECK();
   k_prepare_rw<<<nblocks((long long)m->nCells * (L + 1)), kBlock, 0, s>>>(*m, *f, fl1);
   MPASG_LAUNCH_CHECK();
-  int rc = mpasg_solve_diagnostics(m, c, f, 3, stream);
+  mpasg_config c64 = *c;  // the cold start is float64 in both precisions
+  c64.precision = MPASG_PRECISION_FLOAT64;
+  int rc = mpasg_solve_diagnostics(m, &c64, f, 3, stream);
   if (rc) return rc;
-  return mpasg_reconstruct_2d(m, c, f, stream);
+  return mpasg_reconstruct_2d(m, &c64, f, stream);
 }

@@ -8,7 +8,12 @@
 
 namespace {
 
+// Every transport kernel is a template on the stencil arithmetic type T (common.cuh).
+// In the mixed form the edge values, flux divergences, bounds and limiter factors are
+// float32; the density weighting and the stage update of each scalar are float64.
+
 // sum_m (adv_coefs + sign(uh) adv_coefs_3rd) q[advCell_m]  for every scalar
+template <typename T>
 __global__ void k_pattern_c(mpasg_mesh m, FastDiv fl, int S, const double* __restrict__ uh,
                             const double* __restrict__ q, double* __restrict__ out, int times_uh) {
   const int L = m.nVertLevels;
@@ -17,37 +22,43 @@ __global__ void k_pattern_c(mpasg_mesh m, FastDiv fl, int S, const double* __res
   uint32_t e = fl.div(i), k = i - e * L;
   const int na = m.nAdvMax;
   const int nadv = m.nAdvCellsForEdge[e];
-  const double u = uh[i];
-  const double* cf = (u >= 0.0 ? m.adv_coefs_p : m.adv_coefs_m) + (size_t)e * na;
-  double acc[8];
-  for (int s = 0; s < S; ++s) acc[s] = 0.0;
+  const T u = cv<T>(uh[i]);
+  const double* cf = (u >= T(0) ? m.adv_coefs_p : m.adv_coefs_m) + (size_t)e * na;
+  T acc[8];
+  for (int s = 0; s < S; ++s) acc[s] = T(0);
   for (int a = 0; a < nadv; ++a) {
     int cell = m.advCellsForEdge[e * na + a];
-    double w = cf[a];
+    T w = cv<T>(cf[a]);
     const double* qc = q + ((size_t)cell * L + k) * S;
     for (int s = 0; s < S; ++s) {
-      double t = w * qc[s];
+      T t = w * cv<T>(qc[s]);
       acc[s] = (a == 0) ? t : acc[s] + t;
     }
   }
-  for (int s = 0; s < S; ++s) out[(size_t)i * S + s] = times_uh ? u * acc[s] : acc[s];
+  for (int s = 0; s < S; ++s) out[(size_t)i * S + s] = f64(times_uh ? u * acc[s] : acc[s]);
 }
 
-MPASG_D double wdtn_at(const double* sn, const double* ww, int kk, int L, int S, int s, const double* fnm,
-                       const double* fnp, double coef3) {
-  if (kk <= 0 || kk >= L) return 0.0;
-  if (kk == 1 || kk == L - 1) return ww[kk] * (fnm[kk] * sn[kk * S + s] + fnp[kk] * sn[(kk - 1) * S + s]);
-  return flux3(sn[(kk - 2) * S + s], sn[(kk - 1) * S + s], sn[kk * S + s], sn[(kk + 1) * S + s], ww[kk], coef3);
+template <typename T>
+MPASG_D T wdtn_at(const double* sn, const double* ww, int kk, int L, int S, int s, const double* fnm,
+                  const double* fnp, T coef3) {
+  if (kk <= 0 || kk >= L) return T(0);
+  if (kk == 1 || kk == L - 1)
+    return cv<T>(ww[kk]) * (cv<T>(fnm[kk]) * cv<T>(sn[kk * S + s]) + cv<T>(fnp[kk]) * cv<T>(sn[(kk - 1) * S + s]));
+  return flux3<T>(cv<T>(sn[(kk - 2) * S + s]), cv<T>(sn[(kk - 1) * S + s]), cv<T>(sn[kk * S + s]),
+                  cv<T>(sn[(kk + 1) * S + s]), cv<T>(ww[kk]), coef3);
 }
 
 // explicit stage update for all scalars at (cell, level)
+template <typename T>
 __global__ void __launch_bounds__(kBlock) k_scalars_update(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S,
                                                            double dt, double w_old, double w_new, double coef3,
                                                            const double* __restrict__ s_old,
                                                            const double* __restrict__ s_new,
                                                            double* __restrict__ s_out) {
-  extern __shared__ double s_wdtn[];  // [blockDim.x][S]: vertical flux at the interface below
+  extern __shared__ __align__(8) unsigned char s_raw[];
+  T* s_wdtn = reinterpret_cast<T*>(s_raw);  // [blockDim.x][S]: vertical flux at the interface below
   const int L = m.nVertLevels;
+  const T c3 = cv<T>(coef3);
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < (uint32_t)m.nCells * L;
   uint32_t c = 0, k = 0;
@@ -56,53 +67,60 @@ __global__ void __launch_bounds__(kBlock) k_scalars_update(mpasg_mesh m, mpasg_f
     k = i - c * L;
     const double* sn0 = s_new + (size_t)c * L * S;
     const double* ww0 = f.wwAvg + (size_t)c * (L + 1);
-    for (int s = 0; s < S; ++s) s_wdtn[threadIdx.x * S + s] = wdtn_at(sn0, ww0, k, L, S, s, m.fnm, m.fnp, coef3);
+    for (int s = 0; s < S; ++s) s_wdtn[threadIdx.x * S + s] = wdtn_at<T>(sn0, ww0, k, L, S, s, m.fnm, m.fnp, c3);
   }
   __syncthreads();
   if (!active) return;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  double div[8];
-  for (int s = 0; s < S; ++s) div[s] = 0.0;
+  T div[8];
+  for (int s = 0; s < S; ++s) div[s] = T(0);
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
-    double w = -m.edgesOnCell_sign[c * me + j] * f.ruAvg[(size_t)e * L + k];
+    T w = -cv<T>(m.edgesOnCell_sign[c * me + j]) * cv<T>(f.ruAvg[(size_t)e * L + k]);
     const double* hf = f.hflux + ((size_t)e * L + k) * S;
     for (int s = 0; s < S; ++s) {
-      double t = w * hf[s];
+      T t = w * cv<T>(hf[s]);
       div[s] = (j == 0) ? t : div[s] + t;
     }
   }
-  const double ia = m.invAreaCell[c];
+  const T ia = cv<T>(m.invAreaCell[c]);
   const double* sn = s_new + (size_t)c * L * S;
   const double* ww = f.wwAvg + (size_t)c * (L + 1);
   double rho_old = f.rho_zz_old_split[i];
   double rho_i = w_old * rho_old + w_new * f.rho_zz[i];
-  double inv = 1.0 / rho_i;
+  double inv = fdiv<T>(1.0, rho_i);
   const bool next_in_block = threadIdx.x + 1 < blockDim.x;
+  const T rd = cv<T>(m.rdnw[k]);
+  const T dt_t = cv<T>(dt);
   for (int s = 0; s < S; ++s) {
-    double tend_col = div[s] * ia + 0.0;
-    double lo = s_wdtn[threadIdx.x * S + s];
-    double hi = (k + 1 >= (uint32_t)L) ? 0.0
-                : next_in_block ? s_wdtn[(threadIdx.x + 1) * S + s]
-                                : wdtn_at(sn, ww, k + 1, L, S, s, m.fnm, m.fnp, coef3);
-    double vdiv = m.rdnw[k] * (hi - lo);
-    s_out[(size_t)i * S + s] = (s_old[(size_t)i * S + s] * rho_old + dt * (tend_col - vdiv)) * inv;
+    T tend_col = div[s] * ia + T(0);
+    T lo = s_wdtn[threadIdx.x * S + s];
+    T hi = (k + 1 >= (uint32_t)L) ? T(0)
+           : next_in_block ? s_wdtn[(threadIdx.x + 1) * S + s]
+                           : wdtn_at<T>(sn, ww, k + 1, L, S, s, m.fnm, m.fnp, c3);
+    T vdiv = rd * (hi - lo);
+    s_out[(size_t)i * S + s] = (s_old[(size_t)i * S + s] * rho_old + f64(dt_t * (tend_col - vdiv))) * inv;
   }
 }
 
 // ---------------------------------------------------------------- monotone stage
-MPASG_D double mz(double x) { return x > 0.0 ? x : 0.0; }
+template <typename T>
+MPASG_D T mz(T x) { return x > T(0) ? x : T(0); }
 
 // per (cell, level): rho_int, local+neighbour bounds, vertical upwind update,
 // vertical parts of the limiter scale sums; stores the high-minus-upwind vertical flux
 // at the interface below the level (wflux[c, k, s], k >= 1)
+template <typename T>
 __global__ void __launch_bounds__(kBlock) k_mono_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S,
                                                          double dt, double coef3,
                                                          const double* __restrict__ so_all,
                                                          const double* __restrict__ sn_all) {
-  extern __shared__ double s_wm[];  // [blockDim.x][2 S]: high-minus-upwind flux and upwind flux below
+  extern __shared__ __align__(8) unsigned char s_raw[];
+  T* s_wm = reinterpret_cast<T*>(s_raw);  // [blockDim.x][2 S]: high-minus-upwind and upwind flux below
   const int L = m.nVertLevels;
+  const T c3 = cv<T>(coef3);
+  const T dt_t = cv<T>(dt);
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < (uint32_t)m.nCells * L;
   uint32_t c = 0, k = 0;
@@ -113,11 +131,11 @@ __global__ void __launch_bounds__(kBlock) k_mono_cells_a(mpasg_mesh m, mpasg_fie
     const double* sn0 = sn_all + (size_t)c * L * S;
     const double* ww0 = f.wwAvg + (size_t)c * (L + 1);
     for (int s = 0; s < S; ++s) {
-      double fup = 0.0, wm = 0.0;
+      T fup = T(0), wm = T(0);
       if (k >= 1) {
-        double wk = ww0[k];
-        fup = dt * (wk * (wk >= 0.0 ? so0[(k - 1) * S + s] : so0[k * S + s]));
-        wm = dt * wdtn_at(sn0, ww0, k, L, S, s, m.fnm, m.fnp, coef3) - fup;
+        T wk = cv<T>(ww0[k]);
+        fup = dt_t * (wk * cv<T>(wk >= T(0) ? so0[(k - 1) * S + s] : so0[k * S + s]));
+        wm = dt_t * wdtn_at<T>(sn0, ww0, k, L, S, s, m.fnm, m.fnp, c3) - fup;
       }
       s_wm[threadIdx.x * 2 * S + s] = wm;
       s_wm[threadIdx.x * 2 * S + S + s] = fup;
@@ -127,87 +145,88 @@ __global__ void __launch_bounds__(kBlock) k_mono_cells_a(mpasg_mesh m, mpasg_fie
   if (!active) return;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  const double ia = m.invAreaCell[c];
+  const T ia = cv<T>(m.invAreaCell[c]);
   // density at the end of the stage
-  double hdiv = 0.0;
+  T hdiv = T(0);
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
-    double t = (f.ruAvg[(size_t)e * L + k] * (-m.edgesOnCell_sign[c * me + j] * m.dvEdge[e])) * ia;
+    T t = (cv<T>(f.ruAvg[(size_t)e * L + k]) * (-cv<T>(m.edgesOnCell_sign[c * me + j]) * cv<T>(m.dvEdge[e]))) * ia;
     hdiv = (j == 0) ? t : hdiv + t;
   }
   const double* ww = f.wwAvg + (size_t)c * (L + 1);
   double rho_old = f.rho_zz_old_split[i];
-  double rho_int = rho_old + dt * (hdiv - m.rdnw[k] * (ww[k + 1] - ww[k]));
+  const T rd = cv<T>(m.rdnw[k]);
+  double rho_int = rho_old + f64(dt_t * (hdiv - rd * (cv<T>(ww[k + 1]) - cv<T>(ww[k]))));
   f.rho_int[i] = rho_int;
   const double* so = so_all + (size_t)c * L * S;
   const double* sn = sn_all + (size_t)c * L * S;
-  const double rd = m.rdnw[k];
   for (int s = 0; s < S; ++s) {
-    double smax, smin;
+    T smax, smin;
     if (k == 0) {
-      smax = fmax(so[0 * S + s], so[1 * S + s]);
-      smin = fmin(so[0 * S + s], so[1 * S + s]);
+      smax = vmax(cv<T>(so[0 * S + s]), cv<T>(so[1 * S + s]));
+      smin = vmin(cv<T>(so[0 * S + s]), cv<T>(so[1 * S + s]));
     } else if (k == (uint32_t)L - 1) {
-      smax = fmax(so[k * S + s], so[(k - 1) * S + s]);
-      smin = fmin(so[k * S + s], so[(k - 1) * S + s]);
+      smax = vmax(cv<T>(so[k * S + s]), cv<T>(so[(k - 1) * S + s]));
+      smin = vmin(cv<T>(so[k * S + s]), cv<T>(so[(k - 1) * S + s]));
     } else {
-      smax = fmax(fmax(so[(k - 1) * S + s], so[k * S + s]), so[(k + 1) * S + s]);
-      smin = fmin(fmin(so[(k - 1) * S + s], so[k * S + s]), so[(k + 1) * S + s]);
+      smax = vmax(vmax(cv<T>(so[(k - 1) * S + s]), cv<T>(so[k * S + s])), cv<T>(so[(k + 1) * S + s]));
+      smin = vmin(vmin(cv<T>(so[(k - 1) * S + s]), cv<T>(so[k * S + s])), cv<T>(so[(k + 1) * S + s]));
     }
     // neighbour extrema (first valid neighbour seeds the running bound)
-    double nmax = 0.0, nmin = 0.0;
+    T nmax = T(0), nmin = T(0);
     bool seen = false;
     for (int j = 0; j < n; ++j) {
       int nb = m.cellsOnCell[c * me + j];
       if (nb >= m.nCells) continue;
-      double val = so_all[((size_t)nb * L + k) * S + s];
+      T val = cv<T>(so_all[((size_t)nb * L + k) * S + s]);
       if (!seen) {
         nmax = val;
         nmin = val;
         seen = true;
       } else {
-        nmax = fmax(nmax, val);
-        nmin = fmin(nmin, val);
+        nmax = vmax(nmax, val);
+        nmin = vmin(nmin, val);
       }
     }
     if (seen) {
-      smax = fmax(smax, nmax);
-      smin = fmin(smin, nmin);
+      smax = vmax(smax, nmax);
+      smin = vmin(smin, nmin);
     }
     // vertical high-order and upwind fluxes at the interfaces below (k) and above (k+1)
-    double fup_lo = 0.0, fup_hi = 0.0, wm_lo = 0.0, wm_hi = 0.0;
+    T fup_lo = T(0), fup_hi = T(0), wm_lo = T(0), wm_hi = T(0);
     if (k >= 1) {
       wm_lo = s_wm[threadIdx.x * 2 * S + s];
       fup_lo = s_wm[threadIdx.x * 2 * S + S + s];
-      f.wflux[((size_t)c * (L + 1) + k) * S + s] = wm_lo;
+      f.wflux[((size_t)c * (L + 1) + k) * S + s] = f64(wm_lo);
     }
     if (k + 1 < (uint32_t)L) {
       if (threadIdx.x + 1 < blockDim.x) {
         wm_hi = s_wm[(threadIdx.x + 1) * 2 * S + s];
         fup_hi = s_wm[(threadIdx.x + 1) * 2 * S + S + s];
       } else {
-        double wk = ww[k + 1];
-        fup_hi = dt * (wk * (wk >= 0.0 ? so[k * S + s] : so[(k + 1) * S + s]));
-        wm_hi = dt * wdtn_at(sn, ww, k + 1, L, S, s, m.fnm, m.fnp, coef3) - fup_hi;
+        T wk = cv<T>(ww[k + 1]);
+        fup_hi = dt_t * (wk * cv<T>(wk >= T(0) ? so[k * S + s] : so[(k + 1) * S + s]));
+        wm_hi = dt_t * wdtn_at<T>(sn, ww, k + 1, L, S, s, m.fnm, m.fnp, c3) - fup_hi;
       }
     }
     double rows = so[k * S + s] * rho_old;
-    if (k + 1 < (uint32_t)L) rows = rows - fup_hi * rd;
-    if (k >= 1) rows = rows + fup_lo * rd;
+    if (k + 1 < (uint32_t)L) rows = rows - f64(fup_hi * rd);
+    if (k >= 1) rows = rows + f64(fup_lo * rd);
     // prev = interface below (0 at the surface), next = interface above (0 at the top)
-    double prev = wm_lo, nxt = wm_hi;
-    double sin_ = -rd * ((-mz(-nxt)) - mz(prev));
-    double sout = -rd * (mz(nxt) - (-mz(-prev)));
+    T prev = wm_lo, nxt = wm_hi;
+    T sin_ = -rd * ((-mz(-nxt)) - mz(prev));
+    T sout = -rd * (mz(nxt) - (-mz(-prev)));
     size_t o = (size_t)i * S + s;
     f.rows[o] = rows;
-    f.scale_in[o] = sin_;
-    f.scale_out[o] = sout;
-    f.s_max[o] = smax;
-    f.s_min[o] = smin;
+    f.scale_in[o] = f64(sin_);
+    f.scale_out[o] = f64(sout);
+    f.s_max[o] = f64(smax);
+    f.s_min[o] = f64(smin);
   }
 }
 
 // per (edge, level): horizontal upwind flux and high-minus-upwind correction flux
+template <typename T>
 __global__ void k_mono_edges_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S, double dt,
                                const double* __restrict__ so_all) {
   const int L = m.nVertLevels;
@@ -215,18 +234,20 @@ __global__ void k_mono_edges_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S, 
   if (i >= (uint32_t)m.nEdges * L) return;
   uint32_t e = fl.div(i), k = i - e * L;
   int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-  double u = f.ruAvg[i];
-  int up = u >= 0.0 ? c1 : c2;
-  double dvdt = m.dvEdge[e] * dt;
+  const T u = cv<T>(f.ruAvg[i]);
+  int up = u >= T(0) ? c1 : c2;
+  const T dt_t = cv<T>(dt);
+  const T dvdt = cv<T>(m.dvEdge[e]) * dt_t;
   for (int s = 0; s < S; ++s) {
     size_t o = (size_t)i * S + s;
-    double fup = dvdt * (u * so_all[((size_t)up * L + k) * S + s]);
-    f.flux_up[o] = fup;
-    f.flux_tmp[o] = dt * f.hflux[o] - fup;
+    T fup = dvdt * (u * cv<T>(so_all[((size_t)up * L + k) * S + s]));
+    f.flux_up[o] = f64(fup);
+    f.flux_tmp[o] = f64(dt_t * cv<T>(f.hflux[o]) - fup);
   }
 }
 
 // per (cell, level): horizontal upwind update and scale sums, then the limiter factors
+template <typename T>
 __global__ void k_mono_cells_b(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -234,31 +255,39 @@ __global__ void k_mono_cells_b(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S) 
   uint32_t c = fl.div(i), k = i - c * L;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  const double ia = m.invAreaCell[c];
-  const double eps = 1.0e-20;
+  const T ia = cv<T>(m.invAreaCell[c]);
+  const T eps = T(1.0e-20);
   const double rint = f.rho_int[i];
   for (int s = 0; s < S; ++s) {
     size_t o = (size_t)i * S + s;
-    double rows = f.rows[o], sin_ = f.scale_in[o], sout = f.scale_out[o];
+    double rows = f.rows[o];
+    T sin_ = cv<T>(f.scale_in[o]), sout = cv<T>(f.scale_out[o]);
+    T hsum = T(0);
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
-      double sgn_ = m.edgesOnCell_sign[c * me + j];
-      double sw = sgn_ * ia;
+      T sgn_ = cv<T>(m.edgesOnCell_sign[c * me + j]);
+      T sw = sgn_ * ia;
       size_t oe = ((size_t)e * L + k) * S + s;
-      rows = rows - f.flux_up[oe] * sw;
-      double sf = sgn_ * f.flux_tmp[oe];
+      if (sizeof(T) == sizeof(double))
+        rows = rows - f64(cv<T>(f.flux_up[oe]) * sw);  // float64: the reference's running sum
+      else
+        hsum = hsum - cv<T>(f.flux_up[oe]) * sw;
+      T sf = sgn_ * cv<T>(f.flux_tmp[oe]);
       sout = sout - mz(sf) * ia;
       sin_ = sin_ - (-mz(-sf)) * ia;
     }
-    double a = (f.s_max[o] * rint - rows) / (sin_ + eps);
-    double b = (f.s_min[o] * rint - rows) / (sout - eps);
+    if (sizeof(T) != sizeof(double)) rows = rows + f64(hsum);
+    const T rows_t = cv<T>(rows), rint_t = cv<T>(rint);
+    T a = (cv<T>(f.s_max[o]) * rint_t - rows_t) / (sin_ + eps);
+    T b = (cv<T>(f.s_min[o]) * rint_t - rows_t) / (sout - eps);
     f.rows[o] = rows;
-    f.scale_in[o] = fmin(fmax(a, 0.0), 1.0);
-    f.scale_out[o] = fmin(fmax(b, 0.0), 1.0);
+    f.scale_in[o] = f64(vmin(vmax(a, T(0)), T(1)));
+    f.scale_out[o] = f64(vmin(vmax(b, T(0)), T(1)));
   }
 }
 
 // per (edge, level): limited horizontal flux (stored in hflux)
+template <typename T>
 __global__ void k_mono_edges_b(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -268,13 +297,15 @@ __global__ void k_mono_edges_b(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S) 
   for (int s = 0; s < S; ++s) {
     size_t o = (size_t)i * S + s;
     size_t o1 = ((size_t)c1 * L + k) * S + s, o2 = ((size_t)c2 * L + k) * S + s;
-    double ft = f.flux_tmp[o];
-    double lim = ft >= 0.0 ? fmin(f.scale_out[o1], f.scale_in[o2]) : fmin(f.scale_in[o1], f.scale_out[o2]);
-    f.hflux[o] = ft * lim;
+    T ft = cv<T>(f.flux_tmp[o]);
+    T lim = ft >= T(0) ? vmin(cv<T>(f.scale_out[o1]), cv<T>(f.scale_in[o2]))
+                       : vmin(cv<T>(f.scale_in[o1]), cv<T>(f.scale_out[o2]));
+    f.hflux[o] = f64(ft * lim);
   }
 }
 
 // per (cell, level): apply limited horizontal and vertical fluxes, positivity
+template <typename T>
 __global__ void k_mono_cells_c(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S, double* __restrict__ s_out) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -282,32 +313,37 @@ __global__ void k_mono_cells_c(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S, 
   uint32_t c = fl.div(i), k = i - c * L;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  const double ia = m.invAreaCell[c];
+  const T ia = cv<T>(m.invAreaCell[c]);
   const double rint = f.rho_int[i];
   const size_t oc = (size_t)c * L;
   for (int s = 0; s < S; ++s) {
     size_t o = (size_t)i * S + s;
     // limited vertical fluxes at the interfaces below (k) and above (k+1)
-    double wl_lo = 0.0, wl_hi = 0.0;
+    T wl_lo = T(0), wl_hi = T(0);
     if (k >= 1) {
-      double wm = f.wflux[((size_t)c * (L + 1) + k) * S + s];
-      double lim = wm >= 0.0 ? fmin(f.scale_out[(oc + k - 1) * S + s], f.scale_in[(oc + k) * S + s])
-                             : fmin(f.scale_out[(oc + k) * S + s], f.scale_in[(oc + k - 1) * S + s]);
+      T wm = cv<T>(f.wflux[((size_t)c * (L + 1) + k) * S + s]);
+      T lim = wm >= T(0) ? vmin(cv<T>(f.scale_out[(oc + k - 1) * S + s]), cv<T>(f.scale_in[(oc + k) * S + s]))
+                         : vmin(cv<T>(f.scale_out[(oc + k) * S + s]), cv<T>(f.scale_in[(oc + k - 1) * S + s]));
       wl_lo = wm * lim;
     }
     if (k + 1 < (uint32_t)L) {
-      double wm = f.wflux[((size_t)c * (L + 1) + k + 1) * S + s];
-      double lim = wm >= 0.0 ? fmin(f.scale_out[(oc + k) * S + s], f.scale_in[(oc + k + 1) * S + s])
-                             : fmin(f.scale_out[(oc + k + 1) * S + s], f.scale_in[(oc + k) * S + s]);
+      T wm = cv<T>(f.wflux[((size_t)c * (L + 1) + k + 1) * S + s]);
+      T lim = wm >= T(0) ? vmin(cv<T>(f.scale_out[(oc + k) * S + s]), cv<T>(f.scale_in[(oc + k + 1) * S + s]))
+                         : vmin(cv<T>(f.scale_out[(oc + k + 1) * S + s]), cv<T>(f.scale_in[(oc + k) * S + s]));
       wl_hi = wm * lim;
     }
     double rows = f.rows[o];
+    T hsum = T(0);
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
-      double sw = m.edgesOnCell_sign[c * me + j] * ia;
-      rows = rows - f.hflux[((size_t)e * L + k) * S + s] * sw;
+      T sw = cv<T>(m.edgesOnCell_sign[c * me + j]) * ia;
+      if (sizeof(T) == sizeof(double))
+        rows = rows - f64(cv<T>(f.hflux[((size_t)e * L + k) * S + s]) * sw);
+      else
+        hsum = hsum - cv<T>(f.hflux[((size_t)e * L + k) * S + s]) * sw;
     }
-    double st2 = (rows - m.rdnw[k] * (wl_hi - wl_lo)) / rint;
+    if (sizeof(T) != sizeof(double)) rows = rows + f64(hsum);
+    double st2 = fdiv<T>(rows - f64(cv<T>(m.rdnw[k]) * (wl_hi - wl_lo)), rint);
     s_out[o] = st2 > 0.0 ? st2 : 0.0;
   }
 }
@@ -324,43 +360,66 @@ static void time_weights(int advance_density, int rk_step, int order, double* w_
   *w_old = 1.0 - wn;
 }
 
+namespace {
+
+// One explicit RK transport stage with the edge values in `hflux` (f->hflux or the
+// library-owned scratch): scalars_init, scalars_a -> scalars_b.
+template <typename T>
+int launch_scalars(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, double* hflux, int rk_step,
+                   double dt_stage, cudaStream_t s) {
+  const int L = m->nVertLevels, S = c->num_scalars;
+  FastDiv fl(L);
+  mpasg_fields g = *f;
+  g.hflux = hflux;
+  k_pattern_c<T><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, fl, S, g.ruAvg, g.scalars_a, hflux, 0);
+  MPASG_LAUNCH_CHECK();
+  double w_old, w_new;
+  time_weights(1, rk_step, c->time_integration_order, &w_old, &w_new);
+  k_scalars_update<T><<<nblocks((long long)m->nCells * L), kBlock, kBlock * S * sizeof(T), s>>>(
+      *m, g, fl, S, dt_stage, w_old, w_new, c->coef_3rd_order, g.scalars_init, g.scalars_a, g.scalars_b);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
+template <typename T>
+int launch_scalars_mono(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, double dt_stage,
+                        cudaStream_t s) {
+  const int L = m->nVertLevels, S = c->num_scalars;
+  FastDiv fl(L);
+  const long long nel = (long long)m->nEdges * L, ncl = (long long)m->nCells * L;
+  k_pattern_c<T><<<nblocks(nel), kBlock, 0, s>>>(*m, fl, S, f->ruAvg, f->scalars_a, f->hflux, 1);
+  MPASG_LAUNCH_CHECK();
+  k_mono_cells_a<T><<<nblocks(ncl), kBlock, kBlock * 2 * S * sizeof(T), s>>>(*m, *f, fl, S, dt_stage,
+                                                                          c->coef_3rd_order, f->scalars_init,
+                                                                          f->scalars_a);
+  MPASG_LAUNCH_CHECK();
+  k_mono_edges_a<T><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, S, dt_stage, f->scalars_init);
+  MPASG_LAUNCH_CHECK();
+  k_mono_cells_b<T><<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, S);
+  MPASG_LAUNCH_CHECK();
+  k_mono_edges_b<T><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, S);
+  MPASG_LAUNCH_CHECK();
+  k_mono_cells_c<T><<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, S, f->scalars_b);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
+}  // namespace
+
 extern "C" int mpasg_advance_scalars(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step,
                                      double dt_stage, void* stream) {
   if (!m || !c || !f || c->num_scalars < 1 || c->num_scalars > 8) return MPASG_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
-  const int L = m->nVertLevels, S = c->num_scalars;
-  FastDiv fl(L);
-  k_pattern_c<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, fl, S, f->ruAvg, f->scalars_a, f->hflux, 0);
-  MPASG_LAUNCH_CHECK();
-  double w_old, w_new;
-  time_weights(1, rk_step, c->time_integration_order, &w_old, &w_new);
-  k_scalars_update<<<nblocks((long long)m->nCells * L), kBlock, kBlock * S * sizeof(double), s>>>(
-      *m, *f, fl, S, dt_stage, w_old, w_new, c->coef_3rd_order, f->scalars_init, f->scalars_a, f->scalars_b);
-  MPASG_LAUNCH_CHECK();
-  return MPASG_OK;
+  if (c->precision == MPASG_PRECISION_MIXED) return launch_scalars<float>(m, c, f, f->hflux, rk_step, dt_stage, s);
+  return launch_scalars<double>(m, c, f, f->hflux, rk_step, dt_stage, s);
 }
 
 extern "C" int mpasg_advance_scalars_mono(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
                                           double dt_stage, void* stream) {
   if (!m || !c || !f || c->num_scalars < 1 || c->num_scalars > 8) return MPASG_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
-  const int L = m->nVertLevels, S = c->num_scalars;
-  FastDiv fl(L);
-  const long long nel = (long long)m->nEdges * L, ncl = (long long)m->nCells * L;
-  k_pattern_c<<<nblocks(nel), kBlock, 0, s>>>(*m, fl, S, f->ruAvg, f->scalars_a, f->hflux, 1);
-  MPASG_LAUNCH_CHECK();
-  k_mono_cells_a<<<nblocks(ncl), kBlock, kBlock * 2 * S * sizeof(double), s>>>(*m, *f, fl, S, dt_stage, c->coef_3rd_order, f->scalars_init,
-                                                  f->scalars_a);
-  MPASG_LAUNCH_CHECK();
-  k_mono_edges_a<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, S, dt_stage, f->scalars_init);
-  MPASG_LAUNCH_CHECK();
-  k_mono_cells_b<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, S);
-  MPASG_LAUNCH_CHECK();
-  k_mono_edges_b<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, S);
-  MPASG_LAUNCH_CHECK();
-  k_mono_cells_c<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, S, f->scalars_b);
-  MPASG_LAUNCH_CHECK();
-  return MPASG_OK;
+  if (c->precision == MPASG_PRECISION_MIXED) return launch_scalars_mono<float>(m, c, f, dt_stage, s);
+  return launch_scalars_mono<double>(m, c, f, dt_stage, s);
 }
 
 // ---------------------------------------------------------------- library-owned scratch
@@ -396,17 +455,7 @@ extern "C" int mpasg_advance_scalars_static(const mpasg_mesh* m, const mpasg_con
   double* scratch = nullptr;
   const int rc = static_scratch(&scratch);
   if (rc != MPASG_OK) return rc;
-  mpasg_fields g = *f;  // the caller's struct is left as it is
-  g.hflux = scratch;
-  cudaStream_t s = (cudaStream_t)stream;
-  const int L = m->nVertLevels, S = c->num_scalars;
-  FastDiv fl(L);
-  k_pattern_c<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, fl, S, g.ruAvg, g.scalars_a, g.hflux, 0);
-  MPASG_LAUNCH_CHECK();
-  double w_old, w_new;
-  time_weights(1, rk_step, c->time_integration_order, &w_old, &w_new);
-  k_scalars_update<<<nblocks((long long)m->nCells * L), kBlock, kBlock * S * sizeof(double), s>>>(
-      *m, g, fl, S, dt_stage, w_old, w_new, c->coef_3rd_order, g.scalars_init, g.scalars_a, g.scalars_b);
-  MPASG_LAUNCH_CHECK();
-  return MPASG_OK;
+  cudaStream_t s = (cudaStream_t)stream;  // the caller's struct is left as it is
+  if (c->precision == MPASG_PRECISION_MIXED) return launch_scalars<float>(m, c, f, scratch, rk_step, dt_stage, s);
+  return launch_scalars<double>(m, c, f, scratch, rk_step, dt_stage, s);
 }

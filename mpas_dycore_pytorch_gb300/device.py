@@ -78,6 +78,9 @@ class DeviceMesh:
         dbls = {}
         a, a3 = _np(ref["adv_coefs"]).astype(np.float64), _np(ref["adv_coefs_3rd"]).astype(np.float64)
         derived = {"adv_coefs_p": a + a3, "adv_coefs_m": a - a3}
+        derived.update(reference_theta_profile(_np(ref["theta_base"])[:nc, :nl].astype(np.float64),
+                                               _np(ref["fzm"])[:nl].astype(np.float64),
+                                               _np(ref["fzp"])[:nl].astype(np.float64)))
         for name in _lib.MESH_DBL_PTRS:
             if name in derived:
                 dbls[name] = np.ascontiguousarray(derived[name])
@@ -112,6 +115,20 @@ class DeviceMesh:
             setattr(st, n, t.data_ptr())
         self.struct = st
         self.ints = ints
+
+
+def reference_theta_profile(theta_base: np.ndarray, fzm: np.ndarray, fzp: np.ndarray) -> dict:
+    """Per-level reference theta of the mixed form and its vertical-flux interface weights
+    (the flux3 / second-order interpolations of kern_tend.cu applied to the profile)."""
+    ref = theta_base.mean(axis=0)
+    nl = ref.shape[0]
+    w4, w3, w2 = np.zeros(nl + 1), np.zeros(nl + 1), np.zeros(nl + 1)
+    for k in range(1, nl):
+        w2[k] = fzm[k] * ref[k] + fzp[k] * ref[k - 1]
+    for k in range(2, nl - 1):
+        w4[k] = (7.0 * (ref[k] + ref[k - 1]) - (ref[k + 1] + ref[k - 2])) / 12.0
+        w3[k] = ((ref[k + 1] - ref[k - 2]) - 3.0 * (ref[k] - ref[k - 1])) / 12.0
+    return {"ref_theta": ref, "ref_theta_w4": w4, "ref_theta_w3": w3, "ref_theta_w2": w2}
 
 
 ROWS = {"e": lambda m: (m.nEdges + 1, m.nVertLevels),

@@ -57,7 +57,8 @@ def test_ctypes_layout_matches_header(cname, pyname):
 
 
 def test_abi_version_and_build_info():
+    from mpas_dycore_pytorch_gb300 import _lib
     lib = ctypes.CDLL(str(_lib_path()))
     lib.mpasg_build_info.restype = ctypes.c_char_p
-    assert lib.mpasg_abi_version() == 1
+    assert lib.mpasg_abi_version() == _lib.ABI_VERSION
     assert b"sm_103a" in lib.mpasg_build_info()
