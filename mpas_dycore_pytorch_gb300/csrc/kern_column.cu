@@ -284,6 +284,61 @@ __global__ void k_ac_thomas(mpasg_mesh m, mpasg_fields f) {
   }
 }
 
+// The same sweeps with the columns staged through shared memory: one warp solves 32
+// columns; the block's x, a, alpha and gamma are loaded and stored with coalesced
+// accesses (consecutive threads read consecutive levels of a column) into a [level][33]
+// layout, so the sequential sweeps read shared memory instead of waiting on one global
+// load per level.  Same arithmetic as k_ac_thomas.
+constexpr int kThomasCols = 32;
+constexpr int kThomasPitch = kThomasCols + 1;
+
+__global__ void __launch_bounds__(kThomasCols) k_ac_thomas_staged(mpasg_mesh m, mpasg_fields f, FastDiv fl,
+                                                                  FastDiv fl1) {
+  extern __shared__ double s_col[];
+  const int L = m.nVertLevels;
+  double* sx = s_col;                              // (L+1) x pitch
+  double* sa = sx + (size_t)(L + 1) * kThomasPitch;  // L x pitch each
+  double* sal = sa + (size_t)L * kThomasPitch;
+  double* sg = sal + (size_t)L * kThomasPitch;
+  const int c0 = blockIdx.x * kThomasCols;
+  const int ncol = min(kThomasCols, m.nCells - c0);
+  const int t = threadIdx.x;
+  const uint32_t nw = (uint32_t)ncol * (L + 1), nl = (uint32_t)ncol * L;
+  const double* gx = f.ac_x + (size_t)c0 * (L + 1);
+  const size_t o0 = (size_t)c0 * L;
+  for (uint32_t idx = t; idx < nw; idx += kThomasCols) {
+    uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
+    sx[k * kThomasPitch + col] = gx[idx];
+  }
+  for (uint32_t idx = t; idx < nl; idx += kThomasCols) {
+    uint32_t col = fl.div(idx), k = idx - col * L;
+    sa[k * kThomasPitch + col] = f.a_tri[o0 + idx];
+    sal[k * kThomasPitch + col] = f.alpha_tri[o0 + idx];
+    sg[k * kThomasPitch + col] = f.gamma_tri[o0 + idx];
+  }
+  __syncwarp();
+  if (t < ncol) {
+    double xp = sx[t];
+    for (int k = 1; k < L; ++k) {
+      xp = (sx[k * kThomasPitch + t] - sa[k * kThomasPitch + t] * xp) * sal[k * kThomasPitch + t];
+      sx[k * kThomasPitch + t] = xp;
+    }
+    double xn = sx[L * kThomasPitch + t];
+    for (int k = L - 1; k >= 0; --k) {
+      xn = sx[k * kThomasPitch + t] - sg[k * kThomasPitch + t] * xn;
+      sx[k * kThomasPitch + t] = xn;
+    }
+  }
+  __syncwarp();
+  double* gxo = f.ac_x + (size_t)c0 * (L + 1);
+  for (uint32_t idx = t; idx < nw; idx += kThomasCols) {
+    uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
+    gxo[idx] = sx[k * kThomasPitch + col];
+  }
+}
+
+size_t thomas_smem_bytes(int L) { return (size_t)(4 * L + 1) * kThomasPitch * sizeof(double); }
+
 MPASG_D double ac_damped(const mpasg_mesh& m, const mpasg_fields& f, size_t o, size_t ow, int k, int L, double x,
                          double dts) {
   if (k == 0 || k == L) return x;
@@ -582,7 +637,20 @@ extern "C" int mpasg_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, m
     k_ac_prep<double><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, dts, c->epssm, resm);
     MPASG_LAUNCH_CHECK();
   }
-  k_ac_thomas<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
+  // the staged solve needs more than 48 KB of dynamic shared memory: opt in once per
+  // device (the first call on a device should come before any stream capture)
+  const size_t smem = thomas_smem_bytes(L);
+  static bool smem_opt_in[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MPASG_E_CUDA;
+  if (!smem_opt_in[dev])
+    smem_opt_in[dev] = cudaFuncSetAttribute(k_ac_thomas_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            200 * 1024) == cudaSuccess;
+  if (smem_opt_in[dev] && smem <= 200 * 1024)
+    k_ac_thomas_staged<<<nblocks(m->nCells, kThomasCols), kThomasCols, smem, s>>>(*m, *f, FastDiv(L),
+                                                                                  FastDiv(L + 1));
+  else
+    k_ac_thomas<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
   MPASG_LAUNCH_CHECK();
   k_ac_post<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), dts, c->epssm);
   MPASG_LAUNCH_CHECK();
