@@ -99,6 +99,13 @@ typedef struct mpasg_mesh {
    * third-order interpolation (2 <= k <= L-2), ref_theta_w2 = fzm ref_k + fzp ref_(k-1)
    * (1 <= k <= L-1). */
   const double *ref_theta, *ref_theta_w4, *ref_theta_w3, *ref_theta_w2;
+  /* float32 copies of the geometry the mixed form's stencils read (same shapes as above) */
+  const float *edgesOnCell_sign_f32, *edgesOnVertex_sign_f32, *dcEdge_f32, *dvEdge_f32,
+      *invDcEdge_f32, *invDvEdge_f32, *invAreaCell_f32, *invAreaTriangle_f32,
+      *kiteAreasOnVertex_f32, *weightsOnEdge_f32, *adv_coefs_p_f32, *adv_coefs_m_f32,
+      *defc_a_f32, *defc_b_f32, *meshScalingDel2_f32, *meshScalingDel4_f32,
+      *coeffs_reconstruct_f32, *zxu_f32, *zz_f32, *rdzw_f32, *rdzu_f32, *fzm_f32, *fzp_f32,
+      *fnm_f32, *fnp_f32, *rdnw_f32;
 } mpasg_mesh;
 
 /* Namelist options the step consumes (validated on the host). */
@@ -179,8 +186,13 @@ typedef struct mpasg_fields {
   double *ac_rs, *ac_ts;                                            /* (C+1, L) */
   double *ac_x;                                                     /* (C+1, L+1) */
   double *b_tri, *c_tri;                                            /* (C+1, L) */
-  /* mixed form: theta_m and theta_m_save minus ref_theta (deviations advected in float32) */
-  double *theta_dev, *theta_save_dev;                               /* (C+1, L) */
+  /* mixed form (float32): copies of u, pv_edge, w, rw kept current by the step, the
+   * deviations theta_m - ref_theta and theta_m_save - ref_theta, and the stencils'
+   * intermediate edge fluxes, edge / vertex kinetic energy and vertex PV */
+  float *u_f32, *pv_edge_f32, *flux_w_e_f32, *flux_th_e_f32, *ke_edge_f32;  /* (E+1, L) */
+  float *w_f32, *rw_f32;                                                     /* (C+1, L+1) */
+  float *theta_dev, *theta_save_dev;                                         /* (C+1, L) */
+  float *pv_vertex_f32;                                                      /* (V+1, L) */
   /* status flag word (device int32[4]) for the finite check */
   int32_t *status;
 } mpasg_fields;

@@ -77,8 +77,20 @@ FIELDS = (
     ("rho_int", "c"),
     ("flux_w_e", "e"), ("flux_th_e", "e"),
     ("ac_rs", "c"), ("ac_ts", "c"), ("ac_x", "cw"), ("b_tri", "c"), ("c_tri", "c"),
-    ("theta_dev", "c"), ("theta_save_dev", "c"),
 )
+# float32 members of mpasg_fields (after FIELDS, before status)
+FIELDS32 = (
+    ("u_f32", "e"), ("pv_edge_f32", "e"), ("flux_w_e_f32", "e"), ("flux_th_e_f32", "e"), ("ke_edge_f32", "e"),
+    ("w_f32", "cw"), ("rw_f32", "cw"),
+    ("theta_dev", "c"), ("theta_save_dev", "c"),
+    ("pv_vertex_f32", "v"),
+)
+# float32 geometry copies of mpasg_mesh (after MESH_DBL_PTRS)
+MESH_F32_PTRS = tuple(n + "_f32" for n in (
+    "edgesOnCell_sign", "edgesOnVertex_sign", "dcEdge", "dvEdge", "invDcEdge", "invDvEdge", "invAreaCell",
+    "invAreaTriangle", "kiteAreasOnVertex", "weightsOnEdge", "adv_coefs_p", "adv_coefs_m", "defc_a", "defc_b",
+    "meshScalingDel2", "meshScalingDel4", "coeffs_reconstruct", "zxu", "zz", "rdzw", "rdzu", "fzm", "fzp", "fnm",
+    "fnp", "rdnw"))
 
 
 STAGE_NAMES = ("begin", "setup", "moist", "vert_imp_coefs", "dyn_tend_rk1", "dyn_tend",
@@ -88,7 +100,8 @@ STAGE_NAMES = ("begin", "setup", "moist", "vert_imp_coefs", "dyn_tend_rk1", "dyn
 
 class MeshStruct(C.Structure):
     _fields_ = ([(n, C.c_int32) for n in MESH_INT_DIMS] + [(n, C.c_double) for n in MESH_DOUBLES]
-                + [(n, C.c_void_p) for n in MESH_INT_PTRS] + [(n, C.c_void_p) for n in MESH_DBL_PTRS])
+                + [(n, C.c_void_p) for n in MESH_INT_PTRS] + [(n, C.c_void_p) for n in MESH_DBL_PTRS]
+                + [(n, C.c_void_p) for n in MESH_F32_PTRS])
 
 
 class ConfigStruct(C.Structure):
@@ -96,7 +109,8 @@ class ConfigStruct(C.Structure):
 
 
 class FieldsStruct(C.Structure):
-    _fields_ = [(n, C.c_void_p) for n, _ in FIELDS] + [("status", C.c_void_p)]
+    _fields_ = ([(n, C.c_void_p) for n, _ in FIELDS] + [(n, C.c_void_p) for n, _ in FIELDS32]
+                + [("status", C.c_void_p)])
 
 
 EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg_prepare",

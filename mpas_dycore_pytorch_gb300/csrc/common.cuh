@@ -57,6 +57,17 @@ MPASG_D double f2d_bits(float x) {
 template <typename T> MPASG_D T cv(double x);
 template <> MPASG_D double cv<double>(double x) { return x; }
 template <> MPASG_D float cv<float>(double x) { return d2f_bits(x); }
+// fp<T>(d, s): a field or geometry array as the stencil type -- the float64 array in the
+// float64 form, its float32 copy in the mixed form (no conversion on load)
+template <typename T> MPASG_D const T* fp(const double* d, const float* s);
+template <> MPASG_D const double* fp<double>(const double* d, const float*) { return d; }
+template <> MPASG_D const float* fp<float>(const double*, const float* s) { return s; }
+template <typename T> MPASG_D T* fpw(double* d, float* s);
+template <> MPASG_D double* fpw<double>(double* d, float*) { return d; }
+template <> MPASG_D float* fpw<float>(double*, float* s) { return s; }
+// G(name): mesh geometry array `name` as the stencil type T (kernel-local shorthand)
+#define G(name) fp<T>(m.name, m.name##_f32)
+
 // dif<T>(a, b): a - b of two float64 values as the stencil type, the difference taken in
 // float64 first (fields with a large mean, e.g. pressure or kinetic energy, whose
 // neighbour differences would otherwise lose their leading digits in float32)
@@ -125,6 +136,19 @@ inline int nblocks(long long n, int block = kBlock) {
   long long b = (n + block - 1) / block;
   return (int)(b < 1 ? 1 : b);
 }
+
+// ---------------------------------------------------------------- internal entry points
+// The mixed form's stencils read float32 copies of u, pv_edge, w and rw.  The step driver
+// keeps them current (pack once at step start; recover and diagnostics rewrite them), so
+// it calls these variants with copies_current = true; the public per-stage entry points
+// refresh the copies first.
+int mpasgi_pack_f32(const mpasg_mesh* m, mpasg_fields* f, cudaStream_t s);
+int mpasgi_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step, cudaStream_t s,
+                    bool copies_current);
+int mpasgi_solve_diagnostics(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step,
+                             cudaStream_t s, bool copies_current);
+int mpasgi_reconstruct(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, cudaStream_t s,
+                       bool copies_current);
 
 // Number of kernels this library has launched (for launch accounting by callers).
 extern "C" long long mpasg_launch_count(void);

@@ -42,6 +42,24 @@ __global__ void k_numerics(int which, const double* __restrict__ in, double* __r
   out[i] = which == 0 ? f2d_bits(d2f_bits(x)) : rcp_nr(x);
 }
 
+// float32 copies of float64 fields (mixed form), one launch for up to four arrays
+struct PackJob {
+  const double* src[4];
+  float* dst[4];
+  long long n[4];
+};
+
+__global__ void k_pack_f32(PackJob job) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int a = blockIdx.y;
+  // select with constant indices (a dynamic index into the parameter struct would copy
+  // it to local memory in every thread)
+  const double* src = a == 0 ? job.src[0] : a == 1 ? job.src[1] : a == 2 ? job.src[2] : job.src[3];
+  float* dst = a == 0 ? job.dst[0] : a == 1 ? job.dst[1] : a == 2 ? job.dst[2] : job.dst[3];
+  const long long n = a == 0 ? job.n[0] : a == 1 ? job.n[1] : a == 2 ? job.n[2] : job.n[3];
+  if (i < n) dst[i] = d2f_bits(src[i]);
+}
+
 int fill(double* p, long long n, double v, cudaStream_t s) {
   k_fill_d<<<nblocks(n), kBlock, 0, s>>>(p, n, v);
   MPASG_LAUNCH_CHECK();
@@ -72,6 +90,18 @@ extern "C" const char* mpasg_build_info(void) {
   static char buf[160];
   snprintf(buf, sizeof(buf), "mpasg abi=%d cuda=%d arch=sm_103a float64+mixed", MPASG_ABI_VERSION, CUDART_VERSION);
   return buf;
+}
+
+int mpasgi_pack_f32(const mpasg_mesh* m, mpasg_fields* f, cudaStream_t s) {
+  const long long L = m->nVertLevels;
+  const long long nel = (m->nEdges + 1) * L, ncw = (m->nCells + 1) * (L + 1);
+  PackJob job{{f->u, f->pv_edge, f->w, f->rw}, {f->u_f32, f->pv_edge_f32, f->w_f32, f->rw_f32}, {nel, nel, ncw, ncw}};
+  for (int a = 0; a < 4; ++a)
+    if (!job.src[a] || !job.dst[a]) return MPASG_E_ARG;
+  dim3 grid(nblocks(nel > ncw ? nel : ncw), 4);
+  k_pack_f32<<<grid, kBlock, 0, s>>>(job);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
 }
 
 extern "C" int mpasg_numerics_check(int which, const double* in, double* out, long long n, void* stream) {
@@ -181,6 +211,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   CHECK_RC(copy(f.rr_save, f.rho_p, ncl, s));
   CHECK_RC(copy(f.rho_zz_old_split, f.rho_zz, ncl, s));
   if (S > 0) CHECK_RC(copy(f.scalars_init, f.scalars, ncs, s));
+  if (c->precision == MPASG_PRECISION_MIXED) CHECK_RC(mpasgi_pack_f32(m, &f, s));
   MARK(MPASG_STAGE_SETUP);
   CHECK_RC(mpasg_moist_coefficients(m, c, &f, stream));
   MARK(MPASG_STAGE_MOIST);
@@ -193,7 +224,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
         CHECK_RC(mpasg_vert_imp_coefs(m, c, &f, dts, stream));
         MARK(MPASG_STAGE_VIMP);
       }
-      CHECK_RC(mpasg_dyn_tend(m, c, &f, rk, stream));
+      CHECK_RC(mpasgi_dyn_tend(m, c, &f, rk, s, true));
       MARK(rk == 1 ? MPASG_STAGE_DYN_TEND_RK1 : MPASG_STAGE_DYN_TEND);
       CHECK_RC(mpasg_smlstep_pert(m, c, &f, stream));
       MARK(MPASG_STAGE_SMLSTEP);
@@ -205,7 +236,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
       }
       CHECK_RC(mpasg_recover_large_step(m, c, &f, rk, nsub[rk - 1], rk_ts[rk - 1], stream));
       MARK(MPASG_STAGE_RECOVER);
-      CHECK_RC(mpasg_solve_diagnostics(m, c, &f, rk, stream));
+      CHECK_RC(mpasgi_solve_diagnostics(m, c, &f, rk, s, true));
       MARK(MPASG_STAGE_DIAG);
     }
     // split bookkeeping
@@ -255,7 +286,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
     CHECK_RC(copy(f.scalars, f.scalars_a, ncs, s));
   }
   MARK(MPASG_STAGE_SPLIT);
-  CHECK_RC(mpasg_reconstruct_2d(m, c, &f, stream));
+  CHECK_RC(mpasgi_reconstruct(m, c, &f, s, true));
   MARK(MPASG_STAGE_RECONSTRUCT);
   return MPASG_OK;
 #undef MARK

@@ -508,6 +508,7 @@ __global__ void k_recover_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int r
     f.wwAvg[ow] = rws + f.wwAvg[ow] * inv_ns;
     double rw = rws + f.rw_p[ow];
     f.rw[ow] = rw;
+    if (sizeof(T) != sizeof(double)) f.rw_f32[ow] = d2f_bits(rw);
     size_t oc = (size_t)c * L;
     const double den = m.fzm[k] * m.zz[oc + k] + m.fzp[k] * m.zz[oc + k - 1];
     f.w[ow] = den == 1.0 ? rw : fdiv<T>(rw, den);
@@ -525,7 +526,9 @@ __global__ void k_recover_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl, double
   f.ruAvg[i] = rus + f.ruAvg[i] * inv_ns;
   double ru = rus + f.ru_p[i];
   f.ru[i] = ru;
-  f.u[i] = fdiv<T>(2.0 * ru, f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k]);
+  const double u = fdiv<T>(2.0 * ru, f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k]);
+  f.u[i] = u;
+  if (sizeof(T) != sizeof(double)) f.u_f32[i] = d2f_bits(u);
 }
 
 template <typename T>
@@ -534,8 +537,10 @@ __global__ void k_recover_w(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)m.nCells * (L + 1)) return;
   uint32_t c = fl1.div(i), k = i - c * (L + 1);
+  constexpr bool kMixed = sizeof(T) != sizeof(double);  // also refresh the float32 copy of w
   if (k == (uint32_t)L) {
     f.w[i] = 0.0;
+    if (kMixed) f.w_f32[i] = 0.0f;
     return;
   }
   const int me = m.maxEdges;
@@ -552,7 +557,9 @@ __global__ void k_recover_w(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
       double sc = m.edgesOnCell_sign[c * me + j] * cs * fs;
       surf = (j == 0) ? sc : surf + sc;
     }
-    f.w[i] = surf / (m.cf1 * f.rho_zz[oc] + m.cf2 * f.rho_zz[oc + 1] + m.cf3 * f.rho_zz[oc + 2]);
+    const double w0 = fdiv<T>(surf, m.cf1 * f.rho_zz[oc] + m.cf2 * f.rho_zz[oc + 1] + m.cf3 * f.rho_zz[oc + 2]);
+    f.w[i] = w0;
+    if (kMixed) f.w_f32[i] = d2f_bits(w0);
     return;
   }
   double fzm = m.fzm[k], fzp = m.fzp[k];
@@ -564,7 +571,9 @@ __global__ void k_recover_w(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
     double ci = m.zb_cell[zi] + sgn(fi) * m.zb3_cell[zi];
     acc = acc + m.edgesOnCell_sign[c * me + j] * ci * fi;
   }
-  f.w[i] = fdiv<T>(acc, fzm * f.rho_zz[oc + k] + fzp * f.rho_zz[oc + k - 1]);
+  const double wk = fdiv<T>(acc, fzm * f.rho_zz[oc + k] + fzp * f.rho_zz[oc + k - 1]);
+  f.w[i] = wk;
+  if (kMixed) f.w_f32[i] = d2f_bits(wk);
 }
 
 template <typename T>

@@ -17,8 +17,8 @@ __global__ void k_diag_edges_a(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   uint32_t e = fl.div(i), k = i - e * L;
   int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
   f.h_edge[i] = f64(T(0.5) * (cv<T>(f.rho_zz[(size_t)c1 * L + k]) + cv<T>(f.rho_zz[(size_t)c2 * L + k])));
-  const T u = cv<T>(f.u[i]);
-  f.ke_edge[i] = f64((cv<T>(m.dcEdge[e]) * cv<T>(m.dvEdge[e])) * (u * u));
+  const T u = fp<T>(f.u, f.u_f32)[i];
+  fpw<T>(f.ke_edge, f.ke_edge_f32)[i] = (G(dcEdge)[e] * G(dvEdge)[e]) * (u * u);
 }
 
 // vorticity, vertex kinetic energy and potential vorticity
@@ -36,15 +36,17 @@ __global__ void k_diag_vertices(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
     int e = m.edgesOnVertex[v * vd + j];
     double wgt = m.edgesOnVertex_sign[v * vd + j] * m.dcEdge[e];
     double t = wgt * f.u[(size_t)e * L + k];
-    T ke = cv<T>(f.ke_edge[(size_t)e * L + k]);
+    T ke = fp<T>(f.ke_edge, f.ke_edge_f32)[(size_t)e * L + k];
     vort = (j == 0) ? t : vort + t;
     kev = (j == 0) ? ke : kev + ke;
   }
   const double iat = m.invAreaTriangle[v];
   vort = vort * iat;
   f.vorticity[i] = vort;
-  f.ke_vertex[i] = f64(T(0.25) * cv<T>(iat) * kev);
-  f.pv_vertex[i] = m.fVertex[v] + vort;
+  f.ke_vertex[i] = f64(T(0.25) * G(invAreaTriangle)[v] * kev);
+  const double pvv = m.fVertex[v] + vort;
+  f.pv_vertex[i] = pvv;
+  if (sizeof(T) != sizeof(double)) f.pv_vertex_f32[i] = d2f_bits(pvv);
 }
 
 // divergence, cell kinetic energy (with the vertex-kite blend) and cell PV for APVM
@@ -63,12 +65,12 @@ __global__ void k_diag_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, int apvm)
     int e = m.edgesOnCell[c * me + j];
     double wgt = m.edgesOnCell_sign[c * me + j] * m.dvEdge[e];
     double t = wgt * f.u[(size_t)e * L + k];
-    T kt = T(0.25) * cv<T>(f.ke_edge[(size_t)e * L + k]);
+    T kt = T(0.25) * fp<T>(f.ke_edge, f.ke_edge_f32)[(size_t)e * L + k];
     div = (j == 0) ? t : div + t;
     ke = (j == 0) ? kt : ke + kt;
   }
   div = div * m.invAreaCell[c];
-  const T ia = cv<T>(m.invAreaCell[c]);
+  const T ia = G(invAreaCell)[c];
   ke = ke * ia;
   const T ke_fact = T(1.0 - 0.375);
   ke = ke_fact * ke;
@@ -78,13 +80,13 @@ __global__ void k_diag_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, int apvm)
     int v = m.verticesOnCell[c * me + j];
     int kk = m.kiteForCell[c * me + j];
     if (v >= m.nVertices || kk < 0) continue;
-    T kite = cv<T>(m.kiteAreasOnVertex[v * vd + kk]);
+    T kite = G(kiteAreasOnVertex)[v * vd + kk];
     T t = (T(1) - ke_fact) * kite;
     t = t * cv<T>(f.ke_vertex[(size_t)v * L + k]);
     t = t * ia;
     ke = ke + t;
     if (apvm) {
-      T pt = kite * cv<T>(f.pv_vertex[(size_t)v * L + k]);
+      T pt = kite * fp<T>(f.pv_vertex, f.pv_vertex_f32)[(size_t)v * L + k];
       pt = pt * ia;
       pvc = (j == 0) ? pt : pvc + pt;
     }
@@ -103,7 +105,9 @@ __global__ void k_diag_edges_b(mpasg_mesh m, mpasg_fields f, FastDiv fl, int rec
   if (i >= (uint32_t)m.nEdges * L) return;
   uint32_t e = fl.div(i), k = i - e * L;
   int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
-  const T pv1 = cv<T>(f.pv_vertex[(size_t)v1 * L + k]), pv2 = cv<T>(f.pv_vertex[(size_t)v2 * L + k]);
+  const T* pvv = fp<T>(f.pv_vertex, f.pv_vertex_f32);
+  const T* u = fp<T>(f.u, f.u_f32);
+  const T pv1 = pvv[(size_t)v1 * L + k], pv2 = pvv[(size_t)v2 * L + k];
   T pve = T(0.5) * (pv1 + pv2);
   T vv;
   if (recompute_v) {
@@ -112,7 +116,7 @@ __global__ void k_diag_edges_b(mpasg_mesh m, mpasg_fields f, FastDiv fl, int rec
     vv = T(0);
     for (int j = 0; j < n2; ++j) {
       int eo = m.edgesOnEdge[e * me2 + j];
-      T t = cv<T>(m.weightsOnEdge[e * me2 + j]) * cv<T>(f.u[(size_t)eo * L + k]);
+      T t = G(weightsOnEdge)[e * me2 + j] * u[(size_t)eo * L + k];
       vv = (j == 0) ? t : vv + t;
     }
     f.v[i] = f64(vv);
@@ -121,12 +125,13 @@ __global__ void k_diag_edges_b(mpasg_mesh m, mpasg_fields f, FastDiv fl, int rec
   }
   if (apvm) {
     int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-    T grad_pvt = (pv2 - pv1) * cv<T>(m.invDvEdge[e]);
-    T grad_pvn = (cv<T>(f.pv_cell[(size_t)c2 * L + k]) - cv<T>(f.pv_cell[(size_t)c1 * L + k])) * cv<T>(m.invDcEdge[e]);
-    T delta = cv<T>(apvm_dt) * (vv * grad_pvt + cv<T>(f.u[i]) * grad_pvn);
+    T grad_pvt = (pv2 - pv1) * G(invDvEdge)[e];
+    T grad_pvn = (cv<T>(f.pv_cell[(size_t)c2 * L + k]) - cv<T>(f.pv_cell[(size_t)c1 * L + k])) * G(invDcEdge)[e];
+    T delta = cv<T>(apvm_dt) * (vv * grad_pvt + u[i] * grad_pvn);
     pve = pve - delta;
   }
   f.pv_edge[i] = f64(pve);
+  if (sizeof(T) != sizeof(double)) f.pv_edge_f32[i] = pve;
 }
 
 MPASG_D double vcos(double x) { return cos(x); }
@@ -146,9 +151,9 @@ __global__ void k_reconstruct(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   T x = T(0), y = T(0), z = T(0);
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
-    T u = cv<T>(f.u[(size_t)e * L + k]);
-    const double* cr = m.coeffs_reconstruct + ((size_t)c * me + j) * 3;
-    T tx = cv<T>(cr[0]) * u, ty = cv<T>(cr[1]) * u, tz = cv<T>(cr[2]) * u;
+    T u = fp<T>(f.u, f.u_f32)[(size_t)e * L + k];
+    const T* cr = G(coeffs_reconstruct) + ((size_t)c * me + j) * 3;
+    T tx = cr[0] * u, ty = cr[1] * u, tz = cr[2] * u;
     if (j == 0) {
       x = tx; y = ty; z = tz;
     } else {
@@ -252,19 +257,39 @@ int launch_diagnostics(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields*
 
 extern "C" int mpasg_solve_diagnostics(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step,
                                        void* stream) {
+  return mpasgi_solve_diagnostics(m, c, f, rk_step, (cudaStream_t)stream, false);
+}
+
+int mpasgi_solve_diagnostics(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step,
+                             cudaStream_t s, bool copies_current) {
   if (!m || !c || !f) return MPASG_E_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (c->precision == MPASG_PRECISION_MIXED) return launch_diagnostics<float>(m, c, f, rk_step, s);
+  if (c->precision == MPASG_PRECISION_MIXED) {
+    if (!copies_current) {
+      const int rc = mpasgi_pack_f32(m, f, s);
+      if (rc != MPASG_OK) return rc;
+    }
+    return launch_diagnostics<float>(m, c, f, rk_step, s);
+  }
   return launch_diagnostics<double>(m, c, f, rk_step, s);
 }
 
 extern "C" int mpasg_reconstruct_2d(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, void* stream) {
+  return mpasgi_reconstruct(m, c, f, (cudaStream_t)stream, false);
+}
+
+int mpasgi_reconstruct(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, cudaStream_t s,
+                       bool copies_current) {
   if (!m || !c || !f) return MPASG_E_ARG;
   const int L = m->nVertLevels;
-  if (c->precision == MPASG_PRECISION_MIXED)
-    k_reconstruct<float><<<nblocks((long long)m->nCells * L), kBlock, 0, (cudaStream_t)stream>>>(*m, *f, FastDiv(L));
-  else
-    k_reconstruct<double><<<nblocks((long long)m->nCells * L), kBlock, 0, (cudaStream_t)stream>>>(*m, *f, FastDiv(L));
+  if (c->precision == MPASG_PRECISION_MIXED) {
+    if (!copies_current) {
+      const int rc = mpasgi_pack_f32(m, f, s);
+      if (rc != MPASG_OK) return rc;
+    }
+    k_reconstruct<float><<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, FastDiv(L));
+  } else {
+    k_reconstruct<double><<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, FastDiv(L));
+  }
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }

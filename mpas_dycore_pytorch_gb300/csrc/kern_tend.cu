@@ -12,7 +12,8 @@
 //
 // Every kernel is a template on the stencil arithmetic type T (common.cuh): double for
 // the float64 form, whose slot sums follow the reference's order (first slot assigned,
-// then left to right); float for the mixed form (float64 fields, float32 arithmetic).
+// then left to right); float for the mixed form, which reads the float32 copies of the
+// geometry and of u, w, rw, pv_edge (fp<T> / G) and float64 fields through cv<T>.
 #include <cmath>
 
 #include "common.cuh"
@@ -49,11 +50,14 @@ __global__ void k_tend_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendSca
   double q = f.qtot[i];
   f.dpdz[i] = -kGravity * (m.rho_base[i] * q + f.rr_save[i] * (1.0 + q));
   if (p.smag) {
+    const T* defc_a = G(defc_a);
+    const T* defc_b = G(defc_b);
+    const T* u = fp<T>(f.u, f.u_f32);
     T dd = T(0), dof = T(0);
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
-      T ca = cv<T>(m.defc_a[c * me + j]), cb = cv<T>(m.defc_b[c * me + j]);
-      T ue = cv<T>(f.u[(size_t)e * L + k]), ve = cv<T>(f.v[(size_t)e * L + k]);
+      T ca = defc_a[c * me + j], cb = defc_b[c * me + j];
+      T ue = u[(size_t)e * L + k], ve = cv<T>(f.v[(size_t)e * L + k]);
       T ndd = (dd + ca * ue) - cb * ve;
       T ndo = (dof + cb * ue) + ca * ve;
       dd = ndd;
@@ -66,10 +70,10 @@ __global__ void k_tend_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendSca
 }
 
 template <typename T>
-MPASG_D T wduz_at(const double* __restrict__ u, T rwe, int kk, int L, const double* fzm, const double* fzp) {
+MPASG_D T wduz_at(const T* __restrict__ u, T rwe, int kk, int L, const T* fzm, const T* fzp) {
   if (kk <= 0 || kk >= L) return T(0);
-  if (kk == 1 || kk == L - 1) return rwe * (cv<T>(fzm[kk]) * cv<T>(u[kk]) + cv<T>(fzp[kk]) * cv<T>(u[kk - 1]));
-  return flux3<T>(cv<T>(u[kk - 2]), cv<T>(u[kk - 1]), cv<T>(u[kk]), cv<T>(u[kk + 1]), rwe, T(1));
+  if (kk == 1 || kk == L - 1) return rwe * (fzm[kk] * u[kk] + fzp[kk] * u[kk - 1]);
+  return flux3<T>(u[kk - 2], u[kk - 1], u[kk], u[kk + 1], rwe, T(1));
 }
 
 template <typename T>
@@ -77,20 +81,24 @@ __global__ void __launch_bounds__(kBlock) k_tend_u(mpasg_mesh m, mpasg_fields f,
   __shared__ T s_wd[kBlock];
   const int L = m.nVertLevels;
   const uint32_t n_all = (uint32_t)m.nEdges * L;
+  const T* u = fp<T>(f.u, f.u_f32);
+  const T* rw = fp<T>(f.rw, f.rw_f32);
+  const T* fzm = G(fzm);
+  const T* fzp = G(fzp);
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < n_all;
   uint32_t e = 0, k = 0;
   int c1 = 0, c2 = 0;
-  const double* ue = f.u;
+  const T* ue = u;
   T wd_k = T(0);
   if (active) {
     e = fl.div(i);
     k = i - e * L;
     c1 = m.cellsOnEdge[2 * e];
     c2 = m.cellsOnEdge[2 * e + 1];
-    ue = f.u + (size_t)e * L;
-    T rwe_k = T(0.5) * (cv<T>(f.rw[(size_t)c1 * (L + 1) + k]) + cv<T>(f.rw[(size_t)c2 * (L + 1) + k]));
-    wd_k = wduz_at<T>(ue, rwe_k, k, L, m.fzm, m.fzp);
+    ue = u + (size_t)e * L;
+    T rwe_k = T(0.5) * (rw[(size_t)c1 * (L + 1) + k] + rw[(size_t)c2 * (L + 1) + k]);
+    wd_k = wduz_at<T>(ue, rwe_k, k, L, fzm, fzp);
   }
   s_wd[threadIdx.x] = wd_k;  // vertical flux at the interface below level k
   __syncthreads();
@@ -101,41 +109,42 @@ __global__ void __launch_bounds__(kBlock) k_tend_u(mpasg_mesh m, mpasg_fields f,
   } else if (threadIdx.x + 1 < blockDim.x) {
     wd_k1 = s_wd[threadIdx.x + 1];  // same edge, next level
   } else {
-    T rwe_k1 = T(0.5) * (cv<T>(f.rw[(size_t)c1 * (L + 1) + k + 1]) + cv<T>(f.rw[(size_t)c2 * (L + 1) + k + 1]));
-    wd_k1 = wduz_at<T>(ue, rwe_k1, k + 1, L, m.fzm, m.fzp);
+    T rwe_k1 = T(0.5) * (rw[(size_t)c1 * (L + 1) + k + 1] + rw[(size_t)c2 * (L + 1) + k + 1]);
+    wd_k1 = wduz_at<T>(ue, rwe_k1, k + 1, L, fzm, fzp);
   }
-  T tu = -cv<T>(m.rdzw[k]) * (wd_k1 - wd_k);
+  T tu = -G(rdzw)[k] * (wd_k1 - wd_k);
   // nonlinear Coriolis / PV flux over the TRiSK stencil:
   // sum_j (w_j u_j) * 0.5 (pv_self + pv_j), with the exact power-of-two factor 0.5
   // applied once to the sum (scaling by 0.5 commutes with every rounding of the sum)
   const int n2 = m.nEdgesOnEdge[e];
   const int me2 = m.maxEdges2;
-  const T pv_self = cv<T>(f.pv_edge[i]);
+  const T* pv = fp<T>(f.pv_edge, f.pv_edge_f32);
+  const T* woe = G(weightsOnEdge);
+  const T pv_self = pv[i];
   T q = T(0);
   for (int j = 0; j < n2; ++j) {
     int eo = m.edgesOnEdge[e * me2 + j];
-    T t = (cv<T>(m.weightsOnEdge[e * me2 + j]) * cv<T>(f.u[(size_t)eo * L + k])) *
-          (pv_self + cv<T>(f.pv_edge[(size_t)eo * L + k]));
+    T t = (woe[e * me2 + j] * u[(size_t)eo * L + k]) * (pv_self + pv[(size_t)eo * L + k]);
     q = (j == 0) ? t : q + t;
   }
   q = T(0.5) * q;
   const size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
-  const T inv_dc = cv<T>(m.invDcEdge[e]);
+  const T inv_dc = G(invDcEdge)[e];
   const T rho_e = cv<T>(f.h_edge[i]);
   tu = tu + rho_e * (q - dif<T>(f.ke[i2], f.ke[i1]) * inv_dc) -
-       cv<T>(ue[k]) * T(0.5) * (cv<T>(f.h_divergence[i1]) + cv<T>(f.h_divergence[i2]));
+       ue[k] * T(0.5) * (cv<T>(f.h_divergence[i1]) + cv<T>(f.h_divergence[i2]));
   if (p.rk_step == 1) {
-    T teu = -cv<T>(f.cqu_e[i]) *
-            (div_or_one<T>(dif<T>(f.pressure_p[i2], f.pressure_p[i1]) * inv_dc,
-                           T(0.5) * (cv<T>(m.zz[i2]) + cv<T>(m.zz[i1]))) -
-             T(0.5) * cv<T>(m.zxu[i]) * (cv<T>(f.dpdz[i1]) + cv<T>(f.dpdz[i2])));
+    const T* zz = G(zz);
+    T teu = -cv<T>(f.cqu_e[i]) * (div_or_one<T>(dif<T>(f.pressure_p[i2], f.pressure_p[i1]) * inv_dc,
+                                                T(0.5) * (zz[i2] + zz[i1])) -
+                                  T(0.5) * G(zxu)[i] * (cv<T>(f.dpdz[i1]) + cv<T>(f.dpdz[i2])));
     int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
-    T r_dv = vmin(cv<T>(m.invDvEdge[e]), T(4) * inv_dc);
+    T r_dv = vmin(G(invDvEdge)[e], T(4) * inv_dc);
     T u_diff = (cv<T>(f.divergence[i2]) - cv<T>(f.divergence[i1])) * inv_dc -
                (cv<T>(f.vorticity[(size_t)v2 * L + k]) - cv<T>(f.vorticity[(size_t)v1 * L + k])) * r_dv;
     f.delsq_u[i] = f64(u_diff);
     T kdiffu = T(0.5) * (cv<T>(f.kdiff[i1]) + cv<T>(f.kdiff[i2]));
-    teu = teu + rho_e * kdiffu * u_diff * cv<T>(m.meshScalingDel2[e]);
+    teu = teu + rho_e * kdiffu * u_diff * G(meshScalingDel2)[e];
     f.tend_u_euler[i] = f64(teu);
     f.tend_u[i] = f64(p.del4 ? tu : tu + teu);
   } else {
@@ -150,10 +159,13 @@ __global__ void k_del4_vertex(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   if (i >= (uint32_t)m.nVertices * L) return;
   uint32_t v = fl.div(i), k = i - v * L;
   const int vd = m.vertexDegree;
+  const T* iat = G(invAreaTriangle);
+  const T* dc = G(dcEdge);
+  const T* sg = G(edgesOnVertex_sign);
   T acc = T(0);
   for (int j = 0; j < vd; ++j) {
     int e = m.edgesOnVertex[v * vd + j];
-    T es = cv<T>(m.invAreaTriangle[v]) * cv<T>(m.dcEdge[e]) * cv<T>(m.edgesOnVertex_sign[v * vd + j]);
+    T es = iat[v] * dc[e] * sg[v * vd + j];
     T t = es * cv<T>(f.delsq_u[(size_t)e * L + k]);
     acc = (j == 0) ? t : acc + t;
   }
@@ -168,10 +180,13 @@ __global__ void k_del4_cell(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   uint32_t c = fl.div(i), k = i - c * L;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
+  const T* ia = G(invAreaCell);
+  const T* dv = G(dvEdge);
+  const T* sg = G(edgesOnCell_sign);
   T acc = T(0);
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
-    T es = cv<T>(m.invAreaCell[c]) * cv<T>(m.dvEdge[e]) * cv<T>(m.edgesOnCell_sign[c * me + j]);
+    T es = ia[c] * dv[e] * sg[c * me + j];
     T t = es * cv<T>(f.delsq_u[(size_t)e * L + k]);
     acc = (j == 0) ? t : acc + t;
   }
@@ -186,10 +201,10 @@ __global__ void k_tend_u_del4(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendScal
   uint32_t e = fl.div(i), k = i - e * L;
   const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
   const int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
-  const T inv_dc = cv<T>(m.invDcEdge[e]);
-  T u_mix = cv<T>(m.meshScalingDel4[e]) * cv<T>(p.h_mom_visc4);
+  const T inv_dc = G(invDcEdge)[e];
+  T u_mix = G(meshScalingDel4)[e] * cv<T>(p.h_mom_visc4);
   T r_dc4 = u_mix * cv<T>(p.del4u_div) * inv_dc;
-  T r_dv4 = u_mix * vmin(cv<T>(m.invDvEdge[e]), T(4) * inv_dc);
+  T r_dv4 = u_mix * vmin(G(invDvEdge)[e], T(4) * inv_dc);
   T u_diff4 = (cv<T>(f.delsq_div[(size_t)c2 * L + k]) - cv<T>(f.delsq_div[(size_t)c1 * L + k])) * r_dc4 -
               (cv<T>(f.delsq_vort[(size_t)v2 * L + k]) - cv<T>(f.delsq_vort[(size_t)v1 * L + k])) * r_dv4;
   T teu = cv<T>(f.tend_u_euler[i]) - cv<T>(f.h_edge[i]) * u_diff4;
@@ -206,17 +221,22 @@ __global__ void k_mix_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
   uint32_t c = fl1.div(i), k = i - c * (L + 1);
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  const T ia = cv<T>(m.invAreaCell[c]);
+  const T ia = G(invAreaCell)[c];
+  const T* sg = G(edgesOnCell_sign);
+  const T* dv = G(dvEdge);
+  const T* idc = G(invDcEdge);
+  const T* msd2 = G(meshScalingDel2);
   if (k >= 1 && k < (uint32_t)L) {  // w
+    const T* w = fp<T>(f.w, f.w_f32);
     T dw = T(0), tw = T(0);
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
       int ec1 = m.cellsOnEdge[2 * e], ec2 = m.cellsOnEdge[2 * e + 1];
-      T es = T(0.5) * ia * cv<T>(m.edgesOnCell_sign[c * me + j]) * cv<T>(m.dvEdge[e]) * cv<T>(m.invDcEdge[e]);
+      T es = T(0.5) * ia * sg[c * me + j] * dv[e] * idc[e];
       T flux = es * (cv<T>(f.h_edge[(size_t)e * L + k]) + cv<T>(f.h_edge[(size_t)e * L + k - 1])) *
-               (cv<T>(f.w[(size_t)ec2 * (L + 1) + k]) - cv<T>(f.w[(size_t)ec1 * (L + 1) + k]));
+               (w[(size_t)ec2 * (L + 1) + k] - w[(size_t)ec1 * (L + 1) + k]);
       dw = dw + flux;
-      flux = flux * cv<T>(m.meshScalingDel2[e]) * T(0.25) *
+      flux = flux * msd2[e] * T(0.25) *
              (cv<T>(f.kdiff[(size_t)ec1 * L + k]) + cv<T>(f.kdiff[(size_t)ec2 * L + k]) +
               cv<T>(f.kdiff[(size_t)ec1 * L + k - 1]) + cv<T>(f.kdiff[(size_t)ec2 * L + k - 1]));
       tw = tw + flux;
@@ -233,8 +253,8 @@ __global__ void k_mix_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
       int ec1 = m.cellsOnEdge[2 * e], ec2 = m.cellsOnEdge[2 * e + 1];
-      T es = ia * cv<T>(m.edgesOnCell_sign[c * me + j]) * cv<T>(m.dvEdge[e]) * cv<T>(m.invDcEdge[e]);
-      T pr = T(1) * cv<T>(m.meshScalingDel2[e]);
+      T es = ia * sg[c * me + j] * dv[e] * idc[e];
+      T pr = T(1) * msd2[e];
       T flux = es * dif<T>(f.theta_m[(size_t)ec2 * L + k], f.theta_m[(size_t)ec1 * L + k]) *
                cv<T>(f.h_edge[(size_t)e * L + k]);
       dt_ = dt_ + flux;
@@ -255,15 +275,18 @@ __global__ void k_mix_cells_b(mpasg_mesh m, mpasg_fields f, FastDiv fl1, TendSca
   uint32_t c = fl1.div(i), k = i - c * (L + 1);
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  const T ia = cv<T>(m.invAreaCell[c]);
+  const T ia = G(invAreaCell)[c];
+  const T* sg = G(edgesOnCell_sign);
+  const T* dv = G(dvEdge);
+  const T* idc = G(invDcEdge);
+  const T* msd4 = G(meshScalingDel4);
   if (k >= 1 && k < (uint32_t)L) {
     T tw = cv<T>(f.tend_w_euler[i]);
     const T hm = cv<T>(p.h_mom_visc4) * ia;
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
       int ec1 = m.cellsOnEdge[2 * e], ec2 = m.cellsOnEdge[2 * e + 1];
-      T es = cv<T>(m.meshScalingDel4[e]) * hm * cv<T>(m.dvEdge[e]) * cv<T>(m.edgesOnCell_sign[c * me + j]) *
-             cv<T>(m.invDcEdge[e]);
+      T es = msd4[e] * hm * dv[e] * sg[c * me + j] * idc[e];
       tw = tw - es * (cv<T>(f.delsq_w[(size_t)ec2 * (L + 1) + k]) - cv<T>(f.delsq_w[(size_t)ec1 * (L + 1) + k]));
     }
     f.tend_w_euler[i] = f64(tw);
@@ -275,8 +298,7 @@ __global__ void k_mix_cells_b(mpasg_mesh m, mpasg_fields f, FastDiv fl1, TendSca
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
       int ec1 = m.cellsOnEdge[2 * e], ec2 = m.cellsOnEdge[2 * e + 1];
-      T es = cv<T>(m.meshScalingDel4[e]) * ht * cv<T>(m.dvEdge[e]) * cv<T>(m.edgesOnCell_sign[c * me + j]) *
-             cv<T>(m.invDcEdge[e]);
+      T es = msd4[e] * ht * dv[e] * sg[c * me + j] * idc[e];
       tt = tt - es * (cv<T>(f.delsq_theta[(size_t)ec2 * L + k]) - cv<T>(f.delsq_theta[(size_t)ec1 * L + k]));
     }
     f.tend_theta_euler[o] = f64(tt);
@@ -284,33 +306,36 @@ __global__ void k_mix_cells_b(mpasg_mesh m, mpasg_fields f, FastDiv fl1, TendSca
 }
 
 template <typename T>
-MPASG_D T wdwz_at(const double* w, const double* rw, int kk, int L) {
+MPASG_D T wdwz_at(const T* w, const T* rw, int kk, int L) {
   if (kk <= 0 || kk >= L) return T(0);
-  if (kk == 1 || kk == L - 1)
-    return T(0.25) * (cv<T>(rw[kk]) + cv<T>(rw[kk - 1])) * (cv<T>(w[kk]) + cv<T>(w[kk - 1]));
-  return flux3<T>(cv<T>(w[kk - 2]), cv<T>(w[kk - 1]), cv<T>(w[kk]), cv<T>(w[kk + 1]),
-                  T(0.5) * (cv<T>(rw[kk]) + cv<T>(rw[kk - 1])), T(1));
+  if (kk == 1 || kk == L - 1) return T(0.25) * (rw[kk] + rw[kk - 1]) * (w[kk] + w[kk - 1]);
+  return flux3<T>(w[kk - 2], w[kk - 1], w[kk], w[kk + 1], T(0.5) * (rw[kk] + rw[kk - 1]), T(1));
 }
 
+// vertical theta flux at interface kk: th / ths are theta_m / theta_m_save (float64 form)
+// or their deviations from the reference profile (mixed form); rw_t is rw as the stencil
+// type, rw / rws the float64 rw and rw_save
 template <typename T>
-MPASG_D T wdtz_at(const double* th, const double* ths, const double* rw, const double* rws, int kk, int L,
-                  const double* fzm, const double* fzp, T coef3) {
+MPASG_D T wdtz_at(const T* th, const T* ths, const T* rw_t, const double* rw, const double* rws, int kk, int L,
+                  const T* fzm, const T* fzp, T coef3) {
   if (kk <= 0 || kk >= L) return T(0);
-  const T fm = cv<T>(fzm[kk]), fp = cv<T>(fzp[kk]);
-  if (kk == L - 1 && kk != 1) return cv<T>(rws[kk]) * (fm * cv<T>(th[kk]) + fp * cv<T>(th[kk - 1]));
+  const T fm = fzm[kk], fp = fzp[kk];
+  if (kk == L - 1 && kk != 1) return cv<T>(rws[kk]) * (fm * th[kk] + fp * th[kk - 1]);
   T v;
   if (kk == 1)
-    v = cv<T>(rw[kk]) * (fm * cv<T>(th[kk]) + fp * cv<T>(th[kk - 1]));
+    v = rw_t[kk] * (fm * th[kk] + fp * th[kk - 1]);
   else
-    v = flux3<T>(cv<T>(th[kk - 2]), cv<T>(th[kk - 1]), cv<T>(th[kk]), cv<T>(th[kk + 1]), cv<T>(rw[kk]), coef3);
-  return v + dif<T>(rws[kk], rw[kk]) * (fm * cv<T>(ths[kk]) + fp * cv<T>(ths[kk - 1]));
+    v = flux3<T>(th[kk - 2], th[kk - 1], th[kk], th[kk + 1], rw_t[kk], coef3);
+  return v + dif<T>(rws[kk], rw[kk]) * (fm * ths[kk] + fp * ths[kk - 1]);
 }
 
 // Edge-side horizontal advective fluxes of w and theta_m, computed once per edge:
 // flux_w_e[e,k] = ru_w * sum_a (adv_coefs +/- adv_coefs_3rd)_a w[advCell_a, k] (w levels 1..L-1)
 // flux_th_e[e,k] = ru * sum_a (...)_a theta_m[advCell_a, k] (mass levels 0..L-1).
 // The cell sums then apply edgesOnCell_sign (an exact +/-1 factor), which reproduces
-// the reference's per-slot (sign * ru) * flux products bit for bit.
+// the reference's per-slot (sign * ru) * flux products bit for bit.  The mixed form
+// advects the deviation theta_m - ref_theta (its reference part is added in float64 by
+// k_tend_w_theta_mixed) and stores float32 fluxes.
 template <typename T>
 __global__ void k_adv_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   const int L = m.nVertLevels;
@@ -320,34 +345,35 @@ __global__ void k_adv_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   const int na = m.nAdvMax;
   const int nadv = m.nAdvCellsForEdge[e];
   const int32_t* cells = m.advCellsForEdge + (size_t)e * na;
+  const T* cfp = G(adv_coefs_p) + (size_t)e * na;
+  const T* cfm = G(adv_coefs_m) + (size_t)e * na;
   const T rue = cv<T>(f.ru[i]);
   {
-    // mixed form: the deviation from the reference profile (its mean part is added in
-    // float64 by k_tend_w_theta_mixed)
-    const double* th = sizeof(T) == sizeof(double) ? f.theta_m : f.theta_dev;
-    const double* cf = (rue >= T(0) ? m.adv_coefs_p : m.adv_coefs_m) + (size_t)e * na;
+    const T* th = fp<T>(f.theta_m, f.theta_dev);
+    const T* cf = rue >= T(0) ? cfp : cfm;
     T acc = T(0);
     for (int a = 0; a < nadv; ++a) {
-      T t = cv<T>(cf[a]) * cv<T>(th[(size_t)cells[a] * L + k]);
+      T t = cf[a] * th[(size_t)cells[a] * L + k];
       acc = (a == 0) ? t : acc + t;
     }
-    f.flux_th_e[i] = f64(rue * acc);
+    fpw<T>(f.flux_th_e, f.flux_th_e_f32)[i] = rue * acc;
   }
   if (k >= 1) {
-    T ru_w = cv<T>(m.fzm[k]) * rue + cv<T>(m.fzp[k]) * cv<T>(f.ru[i - 1]);
-    const double* cf = (ru_w >= T(0) ? m.adv_coefs_p : m.adv_coefs_m) + (size_t)e * na;
+    const T* w = fp<T>(f.w, f.w_f32);
+    T ru_w = G(fzm)[k] * rue + G(fzp)[k] * cv<T>(f.ru[i - 1]);
+    const T* cf = ru_w >= T(0) ? cfp : cfm;
     T acc = T(0);
     for (int a = 0; a < nadv; ++a) {
-      T t = cv<T>(cf[a]) * cv<T>(f.w[(size_t)cells[a] * (L + 1) + k]);
+      T t = cf[a] * w[(size_t)cells[a] * (L + 1) + k];
       acc = (a == 0) ? t : acc + t;
     }
-    f.flux_w_e[i] = f64(ru_w * acc);
+    fpw<T>(f.flux_w_e, f.flux_w_e_f32)[i] = ru_w * acc;
   }
 }
 
-// w and theta tendencies; index space (C, L+1)
-template <typename T>
+// w and theta tendencies (float64 form); index space (C, L+1)
 __global__ void __launch_bounds__(kBlock) k_tend_w_theta(mpasg_mesh m, mpasg_fields f, FastDiv fl1, TendScalars p) {
+  using T = double;
   __shared__ T s_wd[kBlock], s_wt[kBlock];
   const int L = m.nVertLevels;
   const uint32_t n_all = (uint32_t)m.nCells * (L + 1);
@@ -355,13 +381,14 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta(mpasg_mesh m, mpasg_fie
   const bool active = i < n_all;
   uint32_t c = 0, k = 0;
   T wd_k = T(0), wt_k = T(0);
-  const T coef3 = cv<T>(p.coef3);
+  const T coef3 = p.coef3;
   if (active) {
     c = fl1.div(i);
     k = i - c * (L + 1);
     const size_t ow0 = (size_t)c * (L + 1), oc0 = (size_t)c * L;
     wd_k = wdwz_at<T>(f.w + ow0, f.rw + ow0, k, L);
-    wt_k = wdtz_at<T>(f.theta_m + oc0, f.theta_m_save + oc0, f.rw + ow0, f.rw_save + ow0, k, L, m.fzm, m.fzp, coef3);
+    wt_k = wdtz_at<T>(f.theta_m + oc0, f.theta_m_save + oc0, f.rw + ow0, f.rw + ow0, f.rw_save + ow0, k, L, m.fzm,
+                      m.fzp, coef3);
   }
   s_wd[threadIdx.x] = wd_k;  // interface fluxes owned by this level
   s_wt[threadIdx.x] = wt_k;
@@ -375,32 +402,31 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta(mpasg_mesh m, mpasg_fie
     } else {
       const size_t ow0 = (size_t)c * (L + 1), oc0 = (size_t)c * L;
       wd_k1 = wdwz_at<T>(f.w + ow0, f.rw + ow0, k + 1, L);
-      wt_k1 = wdtz_at<T>(f.theta_m + oc0, f.theta_m_save + oc0, f.rw + ow0, f.rw_save + ow0, k + 1, L, m.fzm, m.fzp,
-                         coef3);
+      wt_k1 = wdtz_at<T>(f.theta_m + oc0, f.theta_m_save + oc0, f.rw + ow0, f.rw + ow0, f.rw_save + ow0, k + 1, L,
+                         m.fzm, m.fzp, coef3);
     }
   }
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  const T ia = cv<T>(m.invAreaCell[c]);
+  const T ia = m.invAreaCell[c];
   const size_t oc = (size_t)c * L;
   const size_t ow = (size_t)c * (L + 1);
   if (k >= 1 && k < (uint32_t)L) {
-    const T fzm = cv<T>(m.fzm[k]), fzp = cv<T>(m.fzp[k]);
     T tw = T(0);
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
-      tw = tw - cv<T>(m.edgesOnCell_sign[c * me + j]) * cv<T>(f.flux_w_e[(size_t)e * L + k]);
+      tw = tw - m.edgesOnCell_sign[c * me + j] * f.flux_w_e[(size_t)e * L + k];
     }
-    tw = tw * ia - cv<T>(m.rdzu[k]) * (wd_k1 - wd_k);
-    T teu = cv<T>(f.tend_w_euler[i]);
+    tw = tw * ia - m.rdzu[k] * (wd_k1 - wd_k);
+    T teu = f.tend_w_euler[i];
     if (p.rk_step == 1) {
-      // vertical pressure gradient minus buoyancy: a near-hydrostatic residual, float64
+      // vertical pressure gradient minus buoyancy: a near-hydrostatic residual
       const double res = m.rdzu[k] * (f.pressure_p[oc + k] - f.pressure_p[oc + k - 1]) -
                          (m.fzm[k] * f.dpdz[oc + k] + m.fzp[k] * f.dpdz[oc + k - 1]);
-      teu = teu - cv<T>(f.cqw[ow + k]) * cv<T>(res);
-      f.tend_w_euler[i] = f64(teu);
+      teu = teu - f.cqw[ow + k] * res;
+      f.tend_w_euler[i] = teu;
     }
-    f.tend_w[i] = f64(tw + teu);
+    f.tend_w[i] = tw + teu;
   } else {
     f.tend_w[i] = 0.0;
   }
@@ -409,27 +435,27 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta(mpasg_mesh m, mpasg_fie
     T tt = T(0);
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
-      T x = -(cv<T>(m.edgesOnCell_sign[c * me + j]) * cv<T>(f.flux_th_e[(size_t)e * L + k]));
+      T x = -(m.edgesOnCell_sign[c * me + j] * f.flux_th_e[(size_t)e * L + k]);
       tt = (j == 0) ? x : tt + x;
     }
     if (p.rk_step > 1) {
       for (int j = 0; j < n; ++j) {
         int e = m.edgesOnCell[c * me + j];
         int ec1 = m.cellsOnEdge[2 * e], ec2 = m.cellsOnEdge[2 * e + 1];
-        T wgt = cv<T>(m.edgesOnCell_sign[c * me + j]) * cv<T>(m.dvEdge[e]);
-        T flux = wgt * dif<T>(f.ru_save[(size_t)e * L + k], f.ru[(size_t)e * L + k]) * T(0.5) *
-                 (cv<T>(f.theta_m_save[(size_t)ec2 * L + k]) + cv<T>(f.theta_m_save[(size_t)ec1 * L + k]));
+        T wgt = m.edgesOnCell_sign[c * me + j] * m.dvEdge[e];
+        T flux = wgt * (f.ru_save[(size_t)e * L + k] - f.ru[(size_t)e * L + k]) * T(0.5) *
+                 (f.theta_m_save[(size_t)ec2 * L + k] + f.theta_m_save[(size_t)ec1 * L + k]);
         tt = tt - flux;
       }
     }
-    tt = tt * ia - cv<T>(m.rdzw[k]) * (wt_k1 - wt_k);
-    const T rz = cv<T>(f.rho_zz[o]);
-    const T rtd = cv<T>(f.rt_diabatic_tend[o]);
+    tt = tt * ia - m.rdzw[k] * (wt_k1 - wt_k);
+    const T rz = f.rho_zz[o];
+    const T rtd = f.rt_diabatic_tend[o];
     // unfused: the difference cancels strongly (as rounded by the reference)
-    f.rthdynten[o] = f64(sub_rn(tt, mul_rn(cv<T>(f.tend_rho[o]), cv<T>(f.theta_m[o]))) / rz);
+    f.rthdynten[o] = sub_rn(tt, mul_rn(f.tend_rho[o], f.theta_m[o])) / rz;
     tt = tt + rz * rtd;
-    tt = tt + cv<T>(f.tend_theta_euler[o]);
-    f.tend_theta[o] = f64(tt);
+    tt = tt + f.tend_theta_euler[o];
+    f.tend_theta[o] = tt;
   }
 }
 
@@ -445,8 +471,8 @@ __global__ void k_theta_dev(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   uint32_t c = fl.div(i), k = i - c * L;
   (void)c;
   const double r = m.ref_theta[k];
-  f.theta_dev[i] = f.theta_m[i] - r;
-  f.theta_save_dev[i] = f.theta_m_save[i] - r;
+  f.theta_dev[i] = d2f_bits(f.theta_m[i] - r);
+  f.theta_save_dev[i] = d2f_bits(f.theta_m_save[i] - r);
 }
 
 // float64 vertical flux of the reference profile at interface kk (the reference part of
@@ -466,6 +492,10 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
   __shared__ double s_wr[kBlock];
   const int L = m.nVertLevels;
   const uint32_t n_all = (uint32_t)m.nCells * (L + 1);
+  const T* w = f.w_f32;
+  const T* rw = f.rw_f32;
+  const T* fzm = m.fzm_f32;
+  const T* fzp = m.fzp_f32;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < n_all;
   uint32_t c = 0, k = 0;
@@ -476,9 +506,9 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
     c = fl1.div(i);
     k = i - c * (L + 1);
     const size_t ow0 = (size_t)c * (L + 1), oc0 = (size_t)c * L;
-    wd_k = wdwz_at<T>(f.w + ow0, f.rw + ow0, k, L);
-    wt_k = wdtz_at<T>(f.theta_dev + oc0, f.theta_save_dev + oc0, f.rw + ow0, f.rw_save + ow0, k, L, m.fzm, m.fzp,
-                      coef3);
+    wd_k = wdwz_at<T>(w + ow0, rw + ow0, k, L);
+    wt_k = wdtz_at<T>(f.theta_dev + oc0, f.theta_save_dev + oc0, rw + ow0, f.rw + ow0, f.rw_save + ow0, k, L, fzm,
+                      fzp, coef3);
     if (k < (uint32_t)L) wr_k = ref_wflux(m, f.rw[ow0 + k], f.rw_save[ow0 + k], k, L, p.coef3);
   }
   s_wd[threadIdx.x] = wd_k;
@@ -495,24 +525,25 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
       wr_k1 = s_wr[threadIdx.x + 1];
     } else {
       const size_t ow0 = (size_t)c * (L + 1), oc0 = (size_t)c * L;
-      wd_k1 = wdwz_at<T>(f.w + ow0, f.rw + ow0, k + 1, L);
-      wt_k1 = wdtz_at<T>(f.theta_dev + oc0, f.theta_save_dev + oc0, f.rw + ow0, f.rw_save + ow0, k + 1, L, m.fzm,
-                         m.fzp, coef3);
+      wd_k1 = wdwz_at<T>(w + ow0, rw + ow0, k + 1, L);
+      wt_k1 = wdtz_at<T>(f.theta_dev + oc0, f.theta_save_dev + oc0, rw + ow0, f.rw + ow0, f.rw_save + ow0, k + 1,
+                         L, fzm, fzp, coef3);
       wr_k1 = ref_wflux(m, f.rw[ow0 + k + 1], f.rw_save[ow0 + k + 1], k + 1, L, p.coef3);
     }
   }
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  const T ia = cv<T>(m.invAreaCell[c]);
+  const T ia = m.invAreaCell_f32[c];
+  const T* sg = m.edgesOnCell_sign_f32;
   const size_t oc = (size_t)c * L;
   const size_t ow = (size_t)c * (L + 1);
   if (k >= 1 && k < (uint32_t)L) {
     T tw = T(0);
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
-      tw = tw - cv<T>(m.edgesOnCell_sign[c * me + j]) * cv<T>(f.flux_w_e[(size_t)e * L + k]);
+      tw = tw - sg[c * me + j] * f.flux_w_e_f32[(size_t)e * L + k];
     }
-    tw = tw * ia - cv<T>(m.rdzu[k]) * (wd_k1 - wd_k);
+    tw = tw * ia - m.rdzu_f32[k] * (wd_k1 - wd_k);
     T teu = cv<T>(f.tend_w_euler[i]);
     if (p.rk_step == 1) {
       const double res = m.rdzu[k] * (f.pressure_p[oc + k] - f.pressure_p[oc + k - 1]) -
@@ -530,7 +561,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
     T tt = T(0);
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
-      T x = -(cv<T>(m.edgesOnCell_sign[c * me + j]) * cv<T>(f.flux_th_e[(size_t)e * L + k]));
+      T x = -(sg[c * me + j] * f.flux_th_e_f32[(size_t)e * L + k]);
       tt = (j == 0) ? x : tt + x;
     }
     // reference part of the horizontal flux divergence: the adv_coefs of an edge sum to
@@ -545,12 +576,12 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
         const double dru = f.ru_save[(size_t)e * L + k] - f.ru[(size_t)e * L + k];
         dsum = dsum + wgt * dru;
         T flux = cv<T>(wgt) * cv<T>(dru) * T(0.5) *
-                 (cv<T>(f.theta_save_dev[(size_t)ec2 * L + k]) + cv<T>(f.theta_save_dev[(size_t)ec1 * L + k]));
+                 (f.theta_save_dev[(size_t)ec2 * L + k] + f.theta_save_dev[(size_t)ec1 * L + k]);
         tt = tt - flux;
       }
       tmean = tmean - rt * dsum * m.invAreaCell[c];
     }
-    tt = tt * ia - cv<T>(m.rdzw[k]) * (wt_k1 - wt_k);
+    tt = tt * ia - m.rdzw_f32[k] * (wt_k1 - wt_k);
     tmean = tmean - m.rdzw[k] * (wr_k1 - wr_k);
     const double ttot = f64(tt) + tmean;
     const double rz = f.rho_zz[o];
@@ -594,7 +625,7 @@ int launch_dyn_tend(const mpasg_mesh* m, mpasg_fields* f, const TendScalars& p, 
   k_adv_edges<T><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl);
   MPASG_LAUNCH_CHECK();
   if (sizeof(T) == sizeof(double))
-    k_tend_w_theta<double><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, fl1, p);
+    k_tend_w_theta<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, fl1, p);
   else
     k_tend_w_theta_mixed<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, fl1, p);
   MPASG_LAUNCH_CHECK();
@@ -605,6 +636,11 @@ int launch_dyn_tend(const mpasg_mesh* m, mpasg_fields* f, const TendScalars& p, 
 
 extern "C" int mpasg_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step,
                               void* stream) {
+  return mpasgi_dyn_tend(m, c, f, rk_step, (cudaStream_t)stream, false);
+}
+
+int mpasgi_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step, cudaStream_t s,
+                    bool copies_current) {
   if (!m || !c || !f || rk_step < 1 || rk_step > 3) return MPASG_E_ARG;
   if (m->nVertLevels < 4) return MPASG_E_ARG;
   if (c->precision != MPASG_PRECISION_FLOAT64 && c->precision != MPASG_PRECISION_MIXED) return MPASG_E_ARG;
@@ -626,7 +662,12 @@ extern "C" int mpasg_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_
   p.coef3 = c->coef_3rd_order;
   p.rk_step = rk_step;
   p.del4 = (p.h_mom_visc4 > 0.0) ? 1 : 0;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (c->precision == MPASG_PRECISION_MIXED) return launch_dyn_tend<float>(m, f, p, rk_step, s);
+  if (c->precision == MPASG_PRECISION_MIXED) {
+    if (!copies_current) {
+      const int rc = mpasgi_pack_f32(m, f, s);
+      if (rc != MPASG_OK) return rc;
+    }
+    return launch_dyn_tend<float>(m, f, p, rk_step, s);
+  }
   return launch_dyn_tend<double>(m, f, p, rk_step, s);
 }

@@ -101,6 +101,10 @@ class DeviceMesh:
         for n in ("nCells", "nEdges", "nVertices", "nVertLevels", "maxEdges", "maxEdges2",
                   "vertexDegree", "nAdvMax"):
             setattr(st, n, getattr(self, n))
+        for n in _lib.MESH_F32_PTRS:  # float32 geometry of the mixed form
+            t = torch.from_numpy(np.ascontiguousarray(dbls[n[:-4]], dtype=np.float32)).to(self.device)
+            self._keep[n] = t
+            setattr(st, n, t.data_ptr())
         st.flatTerrain = int(not np.any(dbls["zb_cell"]) and not np.any(dbls["zb3_cell"]))
         self.flat_terrain = bool(st.flatTerrain)
         for n in _lib.MESH_DOUBLES:
@@ -167,10 +171,21 @@ class DeviceState:
             view = self.arena[offs[name]:offs[name] + sizes[name]].view(shapes[kind])
             self.f[name] = view
             setattr(st, name, view.data_ptr())
+        # float32 members (mixed form), one float32 arena
+        sizes32 = {name: int(np.prod(shapes[kind])) for name, kind in _lib.FIELDS32}
+        offs32, pos32 = {}, 0
+        for name, _ in _lib.FIELDS32:
+            offs32[name] = pos32
+            pos32 += (sizes32[name] + 63) // 64 * 64
+        self.arena32 = torch.zeros(pos32, dtype=torch.float32, device=mesh.device)
+        for name, kind in _lib.FIELDS32:
+            view = self.arena32[offs32[name]:offs32[name] + sizes32[name]].view(shapes[kind])
+            self.f[name] = view
+            setattr(st, name, view.data_ptr())
         self.status = torch.zeros(4, dtype=torch.int32, device=mesh.device)
         st.status = self.status.data_ptr()
         self.struct = st
-        self.bytes = total * 8
+        self.bytes = total * 8 + pos32 * 4
         # rho_zz padding row holds 1.0 (the reference's sentinel)
         self.f["rho_zz"][mesh.nCells].fill_(1.0)
 

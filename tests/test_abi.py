@@ -42,7 +42,7 @@ def _struct_fields(name):
         if not decl:
             continue
         parts = decl.replace("\n", " ")
-        names = re.sub(r"^(const\s+)?(int32_t|double)\s*", "", parts)
+        names = re.sub(r"^(const\s+)?(int32_t|double|float)\s*", "", parts)
         for n in names.split(","):
             out.append(n.replace("*", "").strip())
     return out
