@@ -29,6 +29,7 @@
  *   mpasg_advance_scalars       dynamics/advance_scalars.py:1272
  *   mpasg_advance_scalars_mono  dynamics/advance_scalars_mono.py:2878
  *   mpasg_reconstruct_2d        dynamics/vector_reconstruction.py:311
+ *   mpasg_surface_pressure      diagnostics.py:10  physics_interface_surface_pressure
  *   mpasg_advance_scalars_static  (no counterpart: advance_scalars.py:1272 without caller scratch)
  */
 #ifndef MPASG_H
@@ -259,6 +260,21 @@ int mpasg_advance_scalars_mono(const mpasg_mesh *m, const mpasg_config *c, mpasg
                                double dt_stage, void *stream);
 int mpasg_reconstruct_2d(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
                          void *stream);
+
+/* ---- diagnostics outside the step ------------------------------------------------ */
+/* Hydrostatic surface pressure (replaces mpas_pytorch/diagnostics.py:10
+ * physics_interface_surface_pressure): rows = nCells or nCells + 1 (padding row -> 0);
+ * rho_zz, zz, qv, pressure_p, pressure_base are (rows, L) row-major, zgrid (rows, L+1);
+ * qv may be null (dry).  Bit-exact with the reference's float64 arithmetic. */
+int mpasg_surface_pressure(int nCells, int rows, int nVertLevels, const double *rho_zz,
+                           const double *zz, const double *qv, const double *pressure_p,
+                           const double *pressure_base, const double *zgrid, double gravity,
+                           double *out, void *stream);
+/* out[0] = sum_i weight_i (x_i - ref_i)^2 over n values in a fixed summation order
+ * (deterministic); ref and weight may be null (0 and 1).  The area-weighted squared
+ * surface-pressure anomaly functional of the differentiation tests. */
+int mpasg_weighted_sq_sum(long long n, const double *x, const double *ref, const double *weight,
+                          double *out, void *stream);
 
 /* ---- transport without caller scratch -------------------------------------------- */
 /* Capacity (float64 values) of the library-owned edge scratch: nEdges * L * S must not

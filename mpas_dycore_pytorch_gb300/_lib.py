@@ -119,7 +119,8 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_dyn_tend", "mpasg_smlstep_pert", "mpasg_acoustic_step",
            "mpasg_divergence_damping", "mpasg_recover_large_step", "mpasg_solve_diagnostics",
            "mpasg_advance_scalars", "mpasg_advance_scalars_mono", "mpasg_reconstruct_2d",
-           "mpasg_advance_scalars_static", "mpasg_numerics_check")
+           "mpasg_advance_scalars_static", "mpasg_numerics_check", "mpasg_surface_pressure",
+           "mpasg_weighted_sq_sum")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -161,6 +162,9 @@ def load() -> C.CDLL:
         "mpasg_reconstruct_2d": ([m, c, f, vp], C.c_int),
         "mpasg_advance_scalars_static": ([m, c, f, C.c_int, C.c_double, vp], C.c_int),
         "mpasg_numerics_check": ([C.c_int, vp, vp, C.c_longlong, vp], C.c_int),
+        "mpasg_surface_pressure": ([C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, vp, vp],
+                                   C.c_int),
+        "mpasg_weighted_sq_sum": ([C.c_longlong, vp, vp, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

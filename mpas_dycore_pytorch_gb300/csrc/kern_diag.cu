@@ -169,6 +169,51 @@ __global__ void k_reconstruct(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   f.uReconstructMeridional[i] = f64(-(x * clon + y * slon) * slat + z * clat);
 }
 
+// ---------------------------------------------------------------- surface pressure
+// physics_interface_surface_pressure (mpas_pytorch/diagnostics.py:10, formula :77-82):
+// hydrostatic extrapolation of the lowest two layers plus the lowest-level pressure.
+// Separately rounded operations in the reference's order, so the result is bit-exact.
+__global__ void k_surface_pressure(int nc, int rows, int L, const double* __restrict__ rho_zz,
+                                   const double* __restrict__ zz, const double* __restrict__ qv,
+                                   const double* __restrict__ pp, const double* __restrict__ pb,
+                                   const double* __restrict__ zgrid, double half_g, double* __restrict__ out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= rows) return;
+  if (c >= nc) {
+    out[c] = 0.0;  // padding row
+    return;
+  }
+  const size_t o = (size_t)c * L, ow = (size_t)c * (L + 1);
+  const double tem1 = __dsub_rn(zgrid[ow + 1], zgrid[ow]);
+  const double tem2 = __dsub_rn(zgrid[ow + 2], zgrid[ow + 1]);
+  const double q0 = qv ? qv[o] : 0.0, q1 = qv ? qv[o + 1] : 0.0;
+  const double rho1 = __dmul_rn(__dmul_rn(rho_zz[o], zz[o]), __dadd_rn(1.0, q0));
+  const double rho2 = __dmul_rn(__dmul_rn(rho_zz[o + 1], zz[o + 1]), __dadd_rn(1.0, q1));
+  const double corr = __ddiv_rn(__dmul_rn(__dmul_rn(0.5, __dsub_rn(rho2, rho1)), tem1), __dadd_rn(tem1, tem2));
+  const double hyd = __dmul_rn(__dmul_rn(half_g, tem1), __dsub_rn(rho1, corr));
+  out[c] = __dadd_rn(__dadd_rn(hyd, pp[o]), pb[o]);
+}
+
+// area-weighted sum of squared anomalies, sum_c w_c (x_c - r_c)^2, in a fixed order
+// (one block: strided partial sums, then a shared-memory tree), so it is deterministic
+__global__ void __launch_bounds__(1024) k_weighted_sq_sum(long long n, const double* __restrict__ x,
+                                                          const double* __restrict__ r,
+                                                          const double* __restrict__ w, double* out) {
+  __shared__ double part[1024];
+  double acc = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    const double d = x[i] - (r ? r[i] : 0.0);
+    acc = acc + (w ? w[i] : 1.0) * (d * d);
+  }
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) part[threadIdx.x] = part[threadIdx.x] + part[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = part[0];
+}
+
 // ---------------------------------------------------------------- cold-start preparation
 __global__ void k_fill(double* p, int n, double v) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = v;
@@ -315,4 +360,24 @@ extern "C" int mpasg_prepare(const mpasg_mesh* m, const mpasg_config* c, mpasg_f
   int rc = mpasg_solve_diagnostics(m, &c64, f, 3, stream);
   if (rc) return rc;
   return mpasg_reconstruct_2d(m, &c64, f, stream);
+}
+
+extern "C" int mpasg_surface_pressure(int nCells, int rows, int nVertLevels, const double* rho_zz, const double* zz,
+                                      const double* qv, const double* pressure_p, const double* pressure_base,
+                                      const double* zgrid, double gravity, double* out, void* stream) {
+  if (!rho_zz || !zz || !pressure_p || !pressure_base || !zgrid || !out) return MPASG_E_ARG;
+  if (nCells < 0 || (rows != nCells && rows != nCells + 1) || nVertLevels < 2) return MPASG_E_ARG;
+  if (rows == 0) return MPASG_OK;
+  k_surface_pressure<<<nblocks(rows), kBlock, 0, (cudaStream_t)stream>>>(
+      nCells, rows, nVertLevels, rho_zz, zz, qv, pressure_p, pressure_base, zgrid, 0.5 * gravity, out);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
+extern "C" int mpasg_weighted_sq_sum(long long n, const double* x, const double* ref, const double* weight,
+                                     double* out, void* stream) {
+  if (!x || !out || n < 0) return MPASG_E_ARG;
+  k_weighted_sq_sum<<<1, 1024, 0, (cudaStream_t)stream>>>(n, x, ref, weight, out);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
 }

@@ -990,3 +990,19 @@ def advance_scalars_mono(a):
     out = scalars_new_in.copy()
     out[:nc] = np.maximum(stage2, 0.0)
     return {"scalars_new": out, "scalars_old": scalars_old, "rho_zz_int": pad3(rho_int)[:, :]}
+
+
+def surface_pressure(nCells, rho_zz, zz, qv, pressure_p, pressure_base, zgrid, gravity=GRAVITY):
+    """Hydrostatic surface pressure of the MPAS physics interface
+    (mpas_pytorch/diagnostics.py:10, formula :77-82): per active cell, with the padding
+    row (when given) set to zero."""
+    c = int(nCells)
+    tem1 = zgrid[:c, 1] - zgrid[:c, 0]
+    tem2 = zgrid[:c, 2] - zgrid[:c, 1]
+    rho1 = rho_zz[:c, 0] * zz[:c, 0] * (1.0 + qv[:c, 0])
+    rho2 = rho_zz[:c, 1] * zz[:c, 1] * (1.0 + qv[:c, 1])
+    hyd = 0.5 * gravity * tem1 * (rho1 - 0.5 * (rho2 - rho1) * tem1 / (tem1 + tem2))
+    sp = hyd + pressure_p[:c, 0] + pressure_base[:c, 0]
+    if rho_zz.shape[0] == c + 1:
+        sp = np.concatenate([sp, np.zeros(1)])
+    return sp
