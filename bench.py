@@ -156,6 +156,101 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _time_steps(step, K, W):
+    """ms per step of ``step()`` over K calls after W warm-up calls (CUDA events)."""
+    import torch
+    for _ in range(W):
+        step()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(K):
+        step()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / K
+
+
+def _graph_model(model):
+    model.step()  # eager first step (shared-memory opt-ins happen before capture)
+    model.capture_graph()
+    return model
+
+
+def measure_forms(args, dev, st, cfg, w, ms_plain):
+    """The mixed form on the same workload and the batched ensemble of level-5 members
+    (float64 and mixed), each timed like the headline (graph replay, CUDA events)."""
+    import numpy as np
+    import torch
+
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.device import STATE_KEYS
+    from mpas_dycore_pytorch_gb300.ensemble import Ensemble, member_cases
+
+    K, W = args.steps, args.warmup
+    S = int(st["scalars"].shape[-1])
+    forms = {}
+    # mixed form: throughput and its per-field error against float64 after 24 steps
+    nerr = 24
+    ends = {}
+    for prec in ("float64", "mixed"):
+        m = Model(st, cfg, w["dt"], num_scalars=S, device=dev, precision=prec)
+        m.prepare(st)
+        _graph_model(m)
+        for _ in range(nerr - 1):
+            m.step()
+        torch.cuda.synchronize()
+        ends[prec] = {k: m.state.f[k][:-1].clone() for k in STATE_KEYS}
+        if prec == "mixed":
+            ms_mixed = _time_steps(m.step, K, W)
+        del m
+        torch.cuda.empty_cache()
+    err = {}
+    for k in STATE_KEYS:
+        den = torch.linalg.vector_norm(ends["float64"][k]).item()
+        if den > 0:
+            err[k] = torch.linalg.vector_norm(ends["mixed"][k] - ends["float64"][k]).item() / den
+    del ends
+    cl = st_cells_levels(st)
+    forms["mixed"] = {"value": cl / (ms_mixed / 1e3), "ms_per_step": ms_mixed,
+                      "speedup_vs_float64": ms_plain / ms_mixed,
+                      "max_rel_l2_vs_float64_after_24_steps": max(err.values()),
+                      "worst_field": max(err, key=err.get), "dtype": "f32 stencils / f64 state"}
+    if args.ensemble > 0:
+        ew = WORKLOADS["c2"]
+        ecfg = _cfg(ew)
+        spec = CaseSpec(**ew["spec"])
+        single, _ = __import__("mpas_dycore_pytorch_gb300.loader", fromlist=["load_case"]).load_case(
+            spec, ecfg, as_torch=False)
+        m = Model(single, ecfg, ew["dt"], num_scalars=S, device=dev)
+        m.prepare(single)
+        ms_single = _time_steps(_graph_model(m).step, K, W)
+        cl1 = st_cells_levels(single)
+        del m
+        torch.cuda.empty_cache()
+        members = member_cases(spec, seeds=list(range(100, 100 + args.ensemble)), config=ecfg, u_noise=0.5)
+        for prec in ("float64", "mixed"):
+            ens = Ensemble(members, ecfg, ew["dt"], precision=prec, device=dev)
+            _graph_model(ens.model)
+            ms_e = _time_steps(ens.step, K, W)
+            bad = ens.model.check_finite()
+            forms["batched" if prec == "float64" else "batched_mixed"] = {
+                "members": args.ensemble, "member_workload": ew["name"].replace("plain float64 forward, ", ""),
+                "value": ens.cell_levels / (ms_e / 1e3), "ms_per_step": ms_e,
+                "aggregate_vs_single_member_float64": (ens.cell_levels / ms_e) / (cl1 / ms_single),
+                "single_member_float64_value": cl1 / (ms_single / 1e3), "nonfinite": bad,
+                "state_bytes": ens.model.state.bytes}
+            del ens
+            torch.cuda.empty_cache()
+    return forms
+
+
+def st_cells_levels(st):
+    import numpy as np
+    return int(np.asarray(st["nCells"]).reshape(-1)[0]) * int(np.asarray(st["nVertLevels"]).reshape(-1)[0])
+
+
 def measured_peak_hbm():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -321,18 +416,26 @@ def run_gb300(args, rank, world):
     e2e = {"value": world * C_ * L_ * K / (e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": h2d}
 
+    state_bytes = model.state.bytes
+    forms = None
+    if world == 1 and not args.no_forms and args.precision == "float64" and args.workload == "c1":
+        del model, host
+        torch.cuda.empty_cache()
+        forms = measure_forms(args, dev, st, cfg, w, ms / K)
+
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "float64" else "f32 stencils / f64 state", "data": "synthetic",
         "config": {"workload": w["name"] if args.precision == "float64" else w["name"].replace("plain float64", "mixed-precision"),
                    "precision": args.precision, "cells": C_, "levels": L_, "scalars": S,
-                   "state_bytes": model.state.bytes,
-                   "l2": "inputs larger than L2 (device state %.1f GB)" % (model.state.bytes / 1e9),
+                   "state_bytes": state_bytes,
+                   "l2": "inputs larger than L2 (device state %.1f GB)" % (state_bytes / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "cuda_graph": True, "bytes_per_cell_level_step": bytes_per_cell_level_step(S, True)},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * K,
         "clocks": clocks.summary(), "stage_ms_per_step": stage_ms, "nonfinite": bad,
+        "forms": forms,
     }
     return out
 
@@ -371,6 +474,8 @@ def main():
     ap.add_argument("--workload", default="c1", choices=tuple(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="float64", choices=("float64", "mixed"))
+    ap.add_argument("--no-forms", action="store_true", help="skip the mixed and batched forms")
+    ap.add_argument("--ensemble", type=int, default=96, help="members of the batched level-5 ensemble (0: skip)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -94,8 +94,8 @@ typedef struct mpasg_mesh {
   const double *dss;                /* (C+1, L) */
   const double *rho_base, *theta_base;  /* (C+1, L) */
   const double *rdzw, *rdzu, *fzm, *fzp, *fnm, *fnp, *rdnw;    /* (L) */
-  /* Reference theta profile of the mixed form (float64): ref_theta (L) is the level mean
-   * of theta_base; at each w interface k (L+1 values, zero where unused) its vertical
+  /* Reference theta profile of the mixed form (float64): ref_theta (L) is the base-state
+   * theta of the first cell; at each w interface k (L+1 values, zero where unused) its vertical
    * flux weights: ref_theta_w4 / ref_theta_w3 are the centred and upwind parts of the
    * third-order interpolation (2 <= k <= L-2), ref_theta_w2 = fzm ref_k + fzp ref_(k-1)
    * (1 <= k <= L-1). */

@@ -122,9 +122,12 @@ class DeviceMesh:
 
 
 def reference_theta_profile(theta_base: np.ndarray, fzm: np.ndarray, fzp: np.ndarray) -> dict:
-    """Per-level reference theta of the mixed form and its vertical-flux interface weights
-    (the flux3 / second-order interpolations of kern_tend.cu applied to the profile)."""
-    ref = theta_base.mean(axis=0)
+    """Per-level reference theta of the mixed form (the base-state theta of the first cell:
+    any profile near theta works, and this one does not depend on how many cells follow,
+    so an ensemble member gets the same profile alone and in a union) and its
+    vertical-flux interface weights (the flux3 / second-order interpolations of
+    kern_tend.cu applied to the profile)."""
+    ref = theta_base[0].copy()
     nl = ref.shape[0]
     w4, w3, w2 = np.zeros(nl + 1), np.zeros(nl + 1), np.zeros(nl + 1)
     for k in range(1, nl):
