@@ -195,7 +195,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
     nerr = 24
     ends = {}
     for prec in ("float64", "mixed"):
-        m = Model(st, cfg, w["dt"], num_scalars=S, device=dev, precision=prec)
+        m = Model(st, cfg, w["dt"], num_scalars=S, device=dev, precision=prec, order=args.order)
         m.prepare(st)
         _graph_model(m)
         for _ in range(nerr - 1):
@@ -223,7 +223,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
         spec = CaseSpec(**ew["spec"])
         single, _ = __import__("mpas_dycore_pytorch_gb300.loader", fromlist=["load_case"]).load_case(
             spec, ecfg, as_torch=False)
-        m = Model(single, ecfg, ew["dt"], num_scalars=S, device=dev)
+        m = Model(single, ecfg, ew["dt"], num_scalars=S, device=dev, order=args.order)
         m.prepare(single)
         ms_single = _time_steps(_graph_model(m).step, K, W)
         cl1 = st_cells_levels(single)
@@ -231,7 +231,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
         torch.cuda.empty_cache()
         members = member_cases(spec, seeds=list(range(100, 100 + args.ensemble)), config=ecfg, u_noise=0.5)
         for prec in ("float64", "mixed"):
-            ens = Ensemble(members, ecfg, ew["dt"], precision=prec, device=dev)
+            ens = Ensemble(members, ecfg, ew["dt"], precision=prec, device=dev, order=args.order)
             _graph_model(ens.model)
             ms_e = _time_steps(ens.step, K, W)
             bad = ens.model.check_finite()
@@ -286,7 +286,7 @@ def run_gb300(args, rank, world):
     dev = torch.device("cuda", torch.cuda.current_device())
     st, _ = load_case(CaseSpec(**w["spec"]), cfg, as_torch=False)
     S = int(st["scalars"].shape[-1])
-    model = Model(st, cfg, w["dt"], num_scalars=S, device=dev, precision=args.precision)
+    model = Model(st, cfg, w["dt"], num_scalars=S, device=dev, precision=args.precision, order=args.order)
     model.prepare(st)
     C_, L_ = model.dmesh.nCells, model.dmesh.nVertLevels
     lib = model.lib
@@ -398,8 +398,9 @@ def run_gb300(args, rank, world):
     # end to end through the public API with pinned host buffers
     keys = [k for k in STATE_KEYS]
     host = {k: torch.empty(model.state.f[k].shape, dtype=torch.float64, pin_memory=True) for k in keys}
+    ex0 = model.export(clone=False)
     for k in keys:
-        host[k].copy_(model.state.f[k])
+        host[k].copy_(ex0[k])
     h2d = sum(t.numel() * 8 for t in host.values())
     torch.cuda.synchronize()
     e_start = torch.cuda.Event(enable_timing=True)
@@ -408,8 +409,9 @@ def run_gb300(args, rank, world):
     for _ in range(K):
         model.load_boundary(host)
         model.step()
+        ex = model.export(clone=False)
         for k in keys:
-            host[k].copy_(model.state.f[k], non_blocking=True)
+            host[k].copy_(ex[k], non_blocking=True)
     e_end.record()
     torch.cuda.synchronize()
     e_ms = e_start.elapsed_time(e_end)
@@ -428,7 +430,7 @@ def run_gb300(args, rank, world):
         "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "float64" else "f32 stencils / f64 state", "data": "synthetic",
         "config": {"workload": w["name"] if args.precision == "float64" else w["name"].replace("plain float64", "mixed-precision"),
-                   "precision": args.precision, "cells": C_, "levels": L_, "scalars": S,
+                   "precision": args.precision, "mesh_order": args.order, "cells": C_, "levels": L_, "scalars": S,
                    "state_bytes": state_bytes,
                    "l2": "inputs larger than L2 (device state %.1f GB)" % (state_bytes / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU",
@@ -475,6 +477,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="float64", choices=("float64", "mixed"))
     ap.add_argument("--no-forms", action="store_true", help="skip the mixed and batched forms")
+    ap.add_argument("--order", default="sfc", choices=("native", "sfc"),
+                    help="mesh order on the device: generator order or Hilbert curve")
     ap.add_argument("--ensemble", type=int, default=96, help="members of the batched level-5 ensemble (0: skip)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -30,6 +30,7 @@
  *   mpasg_advance_scalars_mono  dynamics/advance_scalars_mono.py:2878
  *   mpasg_reconstruct_2d        dynamics/vector_reconstruction.py:311
  *   mpasg_surface_pressure      diagnostics.py:10  physics_interface_surface_pressure
+ *   mpasg_sfc_order, mpasg_edge_order  mesh_reordering.py:106 compute_rcm_permutation (SFC orders)
  *   mpasg_advance_scalars_static  (no counterpart: advance_scalars.py:1272 without caller scratch)
  */
 #ifndef MPASG_H
@@ -275,6 +276,23 @@ int mpasg_surface_pressure(int nCells, int rows, int nVertLevels, const double *
  * surface-pressure anomaly functional of the differentiation tests. */
 int mpasg_weighted_sq_sum(long long n, const double *x, const double *ref, const double *weight,
                           double *out, void *stream);
+
+/* ---- mesh reordering (host functions; no GPU needed) -------------------------------- */
+/* new_to_old[i] = the old index of the i-th point along the 3-D Hilbert curve through
+ * the points (x, y, z) (cell or vertex centres).  Replaces the reference's RCM orders
+ * (mpas_pytorch/mesh_reordering.py:44-79) with a space-filling-curve order. */
+int mpasg_sfc_order(long long n, const double *x, const double *y, const double *z,
+                    long long *new_to_old);
+/* Edge order of the reference's rule (mesh_reordering.py:82-103): sort by (min, max) of
+ * the edge's new 1-based cell ids (missing cells -> n_cells + 1), then old index.
+ * cells_on_edge is (n_edges, 2) 1-based; cell_old_to_new 0-based. */
+int mpasg_edge_order(long long n_edges, long long n_cells, const long long *cells_on_edge,
+                     const long long *cell_old_to_new, long long *new_to_old);
+
+/* Device row gather for reordered meshes: dst[i, :] = src[rows[i], :] for i < n, rows of
+ * row_len float64 values (rows: device int64).  src and dst must not overlap. */
+int mpasg_permute_rows(const double *src, double *dst, const long long *rows, long long n,
+                       long long row_len, void *stream);
 
 /* ---- transport without caller scratch -------------------------------------------- */
 /* Capacity (float64 values) of the library-owned edge scratch: nEdges * L * S must not

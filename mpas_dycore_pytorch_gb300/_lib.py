@@ -120,7 +120,7 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_divergence_damping", "mpasg_recover_large_step", "mpasg_solve_diagnostics",
            "mpasg_advance_scalars", "mpasg_advance_scalars_mono", "mpasg_reconstruct_2d",
            "mpasg_advance_scalars_static", "mpasg_numerics_check", "mpasg_surface_pressure",
-           "mpasg_weighted_sq_sum")
+           "mpasg_weighted_sq_sum", "mpasg_sfc_order", "mpasg_edge_order", "mpasg_permute_rows")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -165,6 +165,9 @@ def load() -> C.CDLL:
         "mpasg_surface_pressure": ([C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, vp, vp],
                                    C.c_int),
         "mpasg_weighted_sq_sum": ([C.c_longlong, vp, vp, vp, vp, vp], C.c_int),
+        "mpasg_sfc_order": ([C.c_longlong, vp, vp, vp, vp], C.c_int),
+        "mpasg_edge_order": ([C.c_longlong, C.c_longlong, vp, vp, vp], C.c_int),
+        "mpasg_permute_rows": ([vp, vp, vp, C.c_longlong, C.c_longlong, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -38,6 +38,8 @@ DEFAULTS = {
     # GB300 extension (no reference counterpart): "float64" (the reference's arithmetic)
     # or "mixed" (float32 horizontal stencils over float64 state, see include/mpasg.h)
     "config_precision": "float64",
+    # the reference's RCM option (atmosphere_model.py:810-827): results in the RCM order
+    "config_mesh_reordering_rcm": False,
 }
 
 
@@ -121,8 +123,18 @@ class Model:
 
     def __init__(self, mesh: Mapping[str, Any], config: Mapping[str, Any] | None, dt: float,
                  num_scalars: int | None = None, device: str | torch.device = "cuda",
-                 precision: str | None = None):
+                 precision: str | None = None, order: str = "native"):
+        """``order="sfc"`` keeps the mesh and state on the device in Hilbert-curve order
+        (``reorder.py``); inputs and ``export()`` stay in the caller's order."""
         self.lib = _lib.load()
+        if order not in ("native", "sfc"):
+            raise MpasConfigError(f"order must be 'native' or 'sfc', got {order!r}")
+        self._perm = None
+        if order == "sfc":
+            from .reorder import apply_permutation, compute_sfc_permutation
+            self._dims = tuple(_int(mesh[k]) for k in ("nCells", "nEdges", "nVertices"))
+            self._perm = compute_sfc_permutation(mesh)
+            mesh = apply_permutation(mesh, self._perm, self._dims)
         self.cfg = resolved_config(config)
         if precision is not None:
             self.cfg["config_precision"] = precision
@@ -147,6 +159,15 @@ class Model:
         # static fields the step reads from the state side
         self.state.load(mesh, keys=("rt_diabatic_tend",))
         self._graph = None
+        self._rows_in = self._rows_out = None
+        if self._perm is not None:  # device row maps, padding row last
+            dev = self.dmesh.device
+            idx = lambda a, n: torch.as_tensor(np.concatenate([a, [n]]).astype(np.int64), device=dev)
+            nc, ne, nv = self._dims
+            self._rows_in = {"cell": idx(self._perm.cell_new_to_old, nc), "edge": idx(self._perm.edge_new_to_old, ne),
+                             "vertex": idx(self._perm.vertex_new_to_old, nv)}
+            self._rows_out = {"cell": idx(self._perm.cell_old_to_new, nc), "edge": idx(self._perm.edge_old_to_new, ne),
+                              "vertex": idx(self._perm.vertex_old_to_new, nv)}
 
     # -- C ABI plumbing ---------------------------------------------------------------
     def call(self, name: str, *args) -> None:
@@ -156,8 +177,15 @@ class Model:
         _lib.check(rc, name)
 
     # -- state ---------------------------------------------------------------------------
+    def _to_device_order(self, data: Mapping[str, Any]) -> Mapping[str, Any]:
+        if self._perm is None:
+            return data
+        from .reorder import apply_permutation
+        return apply_permutation(data, self._perm, self._dims)
+
     def prepare(self, loaded: Mapping[str, Any]) -> None:
         """Cold-start preparation on the device from loaded theta, rho, qv, u, w."""
+        loaded = self._to_device_order(loaded)
         dev = self.dmesh.device
         L = self.dmesh.nVertLevels
         nc = self.dmesh.nCells
@@ -176,8 +204,8 @@ class Model:
         torch.cuda.current_stream().synchronize()
 
     def load_boundary(self, state: Mapping[str, Any]) -> None:
-        """Load a prepared (complete) step boundary."""
-        self.state.load(state, keys=STATE_KEYS + ("rho_edge",))
+        """Load a prepared (complete) step boundary (caller's order)."""
+        self.state.load(state, keys=STATE_KEYS + ("rho_edge",), rows=self._rows_in)
         self.state.f["rho_zz"][self.dmesh.nCells].fill_(1.0)
 
     def step(self) -> None:
@@ -206,8 +234,18 @@ class Model:
         self.call("mpasg_check_finite")
         return int(self.state.status[0].item())
 
-    def export(self) -> dict[str, torch.Tensor]:
-        return {k: v.clone() for k, v in self.state.export().items()}
+    def export(self, clone: bool = True) -> dict[str, torch.Tensor]:
+        """The step boundary in the caller's order (``clone=False``: views of the device
+        fields where no reordering is needed)."""
+        if self._perm is None:
+            ex = self.state.export()
+            return {k: v.clone() for k, v in ex.items()} if clone else dict(ex)
+        from .device import ENTITY, FIELD_KIND
+        out = {}
+        for k, v in self.state.export().items():
+            name = {"rho_edge": "h_edge", "ur_cell": "uReconstructZonal", "vr_cell": "uReconstructMeridional"}.get(k, k)
+            out[k] = self.state.gather_rows(v, self._rows_out[ENTITY[FIELD_KIND[name]]])
+        return out
 
 
 def _is_prepared(state: Mapping[str, Any]) -> bool:
@@ -244,6 +282,18 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
     dt = float(cfg["config_dt"] if dt is None else dt)
     if nsteps == 0:
         return dict(initial_state)
+    if bool(cfg.get("config_mesh_reordering_rcm", False)) and not merged.get("_rcm_applied", False):
+        # the reference reorders state and mesh and updates the caller's mesh in place
+        # (atmosphere_model.py:810-827); results come back in the RCM order
+        from .reorder import apply_rcm_reordering
+        initial_state, new_mesh = apply_rcm_reordering(initial_state, mesh)
+        if isinstance(mesh, dict):
+            mesh.clear()
+            mesh.update(new_mesh)
+        else:
+            mesh = new_mesh
+        merged = dict(mesh)
+        merged.update(initial_state)
     ns = _int(merged.get("num_scalars", _np(merged["scalars"]).shape[-1]))
     model = Model(merged, cfg, dt, num_scalars=ns, device=device)
     if _is_prepared(initial_state):

@@ -60,6 +60,15 @@ __global__ void k_pack_f32(PackJob job) {
   if (i < n) dst[i] = d2f_bits(src[i]);
 }
 
+// dst row i = src row rows[i] (rows of row_len float64 values)
+__global__ void k_permute_rows(const double* __restrict__ src, double* __restrict__ dst,
+                               const long long* __restrict__ rows, long long n, long long row_len) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * row_len) return;
+  const long long r = i / row_len, j = i - r * row_len;
+  dst[i] = src[rows[r] * row_len + j];
+}
+
 int fill(double* p, long long n, double v, cudaStream_t s) {
   k_fill_d<<<nblocks(n), kBlock, 0, s>>>(p, n, v);
   MPASG_LAUNCH_CHECK();
@@ -100,6 +109,15 @@ int mpasgi_pack_f32(const mpasg_mesh* m, mpasg_fields* f, cudaStream_t s) {
     if (!job.src[a] || !job.dst[a]) return MPASG_E_ARG;
   dim3 grid(nblocks(nel > ncw ? nel : ncw), 4);
   k_pack_f32<<<grid, kBlock, 0, s>>>(job);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
+extern "C" int mpasg_permute_rows(const double* src, double* dst, const long long* rows, long long n,
+                                  long long row_len, void* stream) {
+  if (!src || !dst || !rows || n < 0 || row_len < 1 || src == dst) return MPASG_E_ARG;
+  if (n == 0) return MPASG_OK;
+  k_permute_rows<<<nblocks(n * row_len), kBlock, 0, (cudaStream_t)stream>>>(src, dst, rows, n, row_len);
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }

@@ -138,6 +138,9 @@ def reference_theta_profile(theta_base: np.ndarray, fzm: np.ndarray, fzp: np.nda
     return {"ref_theta": ref, "ref_theta_w4": w4, "ref_theta_w3": w3, "ref_theta_w2": w2}
 
 
+FIELD_KIND = dict(_lib.FIELDS)
+ENTITY = {"e": "edge", "es": "edge", "c": "cell", "cw": "cell", "cs": "cell", "cws": "cell", "v": "vertex"}
+
 ROWS = {"e": lambda m: (m.nEdges + 1, m.nVertLevels),
         "c": lambda m: (m.nCells + 1, m.nVertLevels),
         "cw": lambda m: (m.nCells + 1, m.nVertLevels + 1),
@@ -195,8 +198,21 @@ class DeviceState:
     def field(self, name: str) -> torch.Tensor:
         return self.f[ALIASES.get(name, name)]
 
-    def load(self, state: Mapping[str, Any], keys=None) -> None:
-        """Copy reference-layout arrays (numpy or torch) into the named fields."""
+    def gather_rows(self, src: torch.Tensor, rows: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """out[i] = src[rows[i]] along the first dimension (``mpasg_permute_rows``)."""
+        src = src.contiguous()
+        out = torch.empty_like(src) if out is None else out
+        lib = _lib.load()
+        rc = lib.mpasg_permute_rows(C.c_void_p(src.data_ptr()), C.c_void_p(out.data_ptr()),
+                                    C.c_void_p(rows.data_ptr()), int(src.shape[0]), int(src[0].numel()),
+                                    C.c_void_p(torch.cuda.current_stream(src.device).cuda_stream))
+        _lib.check(rc, "mpasg_permute_rows")
+        return out
+
+    def load(self, state: Mapping[str, Any], keys=None, rows: Mapping[str, torch.Tensor] | None = None) -> None:
+        """Copy reference-layout arrays (numpy or torch) into the named fields; with
+        ``rows`` (entity -> device row index, N+1 entries) the rows are gathered into the
+        device order on the device."""
         for key in keys if keys is not None else state.keys():
             if key not in state:
                 continue
@@ -208,6 +224,15 @@ class DeviceState:
                 continue
             dst = self.f[name]
             t = torch.as_tensor(src, dtype=torch.float64)
+            ent = ENTITY.get(FIELD_KIND.get(name)) if rows is not None else None
+            if ent is not None:
+                if t.dim() != dst.dim() or tuple(t.shape[1:]) != tuple(dst.shape[1:]) or \
+                        t.shape[0] not in (dst.shape[0], dst.shape[0] - 1):
+                    raise MpasConfigError(f"{key}: shape {tuple(t.shape)} != {tuple(dst.shape)}")
+                stage = torch.zeros(dst.shape, dtype=torch.float64, device=dst.device)
+                stage[: t.shape[0]].copy_(t, non_blocking=True)
+                self.gather_rows(stage, rows[ent], out=dst)
+                continue
             if tuple(t.shape) != tuple(dst.shape):
                 if t.dim() == dst.dim() and t.shape[0] == dst.shape[0] - 1:
                     dst[: t.shape[0]].copy_(t, non_blocking=True)

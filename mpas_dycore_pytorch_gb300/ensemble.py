@@ -165,8 +165,24 @@ class Ensemble:
     """B members stepped together on one GPU (see module docstring)."""
 
     def __init__(self, members: Sequence[Mapping[str, Any]], config: Mapping[str, Any] | None, dt: float,
-                 precision: str | None = None, device: str | torch.device = "cuda"):
+                 precision: str | None = None, device: str | torch.device = "cuda", order: str = "native"):
+        """``order="sfc"``: each member is put in Hilbert-curve order before stacking (so a
+        member's neighbours stay close in memory); ``member_state`` returns the member's
+        own order."""
         from .api import Model
+        self._perms = None
+        if order == "sfc":
+            from .reorder import apply_permutation, compute_sfc_permutation
+            self._perms = []
+            reordered = []
+            for m in members:
+                dims = tuple(_int(m[k]) for k in ("nCells", "nEdges", "nVertices"))
+                perm = compute_sfc_permutation(m)
+                self._perms.append((perm, dims))
+                reordered.append(apply_permutation(m, perm, dims))
+            members = reordered
+        elif order != "native":
+            raise MpasConfigError(f"order must be 'native' or 'sfc', got {order!r}")
         union, self.layouts = stack_members(members)
         self.union_dims = {"cell": _int(union["nCells"]), "edge": _int(union["nEdges"]),
                            "vertex": _int(union["nVertices"])}
@@ -182,4 +198,9 @@ class Ensemble:
         self.model.capture_graph()
 
     def member_state(self, b: int) -> dict:
-        return split_member(self.model.export(), self.layouts[b], self.union_dims)
+        out = split_member(self.model.export(), self.layouts[b], self.union_dims)
+        if self._perms is not None:
+            from .reorder import restore_order
+            perm, dims = self._perms[b]
+            out = restore_order(out, perm, dims)
+        return out

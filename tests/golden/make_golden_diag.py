@@ -1,9 +1,12 @@
-"""Golden vectors for the surface-pressure diagnostic, made by the reference itself.
+"""Golden vectors for the surface-pressure diagnostic and the RCM reordering, made by
+the reference itself.
 
 Runs the reference's ``physics_interface_surface_pressure`` (mpas_pytorch/diagnostics.py:10)
 on the evolved states stored in the committed ``g2_*`` fixtures (after step 1 and step 2)
-and writes ``sp_g2.npz`` (one array per case and step).  Imports the reference the same
-way as ``make_golden.py`` (netCDF4 stub).
+and writes ``sp_g2.npz`` (one array per case and step); runs ``apply_rcm_reordering``
+(mpas_pytorch/mesh_reordering.py:243) on the ``g2_explicit`` loaded mesh and writes the
+permutations and the reordered connectivity / fields to ``rcm_g2.npz``.  Imports the
+reference the same way as ``make_golden.py`` (netCDF4 stub).
 
 Run:  python tests/golden/make_golden_diag.py
 """
@@ -43,6 +46,22 @@ def main() -> None:
             out[f"{case}/{step}"] = sp.numpy()
     np.savez_compressed(HERE / "sp_g2.npz", **out)
     print("wrote", HERE / "sp_g2.npz", sorted(out))
+
+    from mpas_pytorch.mesh_reordering import apply_rcm_reordering
+    meta, st, _ = load_case("g2_explicit")
+    loaded = group(st, "loaded")
+    mesh = {k: (torch.as_tensor(np.asarray(v)) if np.ndim(v) > 0 else int(np.asarray(v)) if np.asarray(v).dtype.kind in "iu"
+                else float(np.asarray(v))) for k, v in loaded.items()}
+    state = {k: mesh[k] for k in ("u", "theta", "rho", "w", "scalars")}
+    rst, rmesh = apply_rcm_reordering(state, mesh)
+    rec = {f"perm/{k}": v.numpy() for k, v in rmesh["_rcm_permutation"].items()}
+    for k in ("cellsOnEdge", "edgesOnCell", "cellsOnCell", "verticesOnEdge", "edgesOnEdge", "advCellsForEdge",
+              "edgesOnVertex", "cellsOnVertex", "verticesOnCell", "kiteForCell", "dvEdge", "areaCell", "weightsOnEdge"):
+        rec[f"mesh/{k}"] = rmesh[k].numpy()
+    for k in ("u", "theta", "w", "scalars"):
+        rec[f"state/{k}"] = rst[k].numpy()
+    np.savez_compressed(HERE / "rcm_g2.npz", **rec)
+    print("wrote", HERE / "rcm_g2.npz", len(rec))
 
 
 if __name__ == "__main__":
