@@ -31,6 +31,7 @@
  *   mpasg_reconstruct_2d        dynamics/vector_reconstruction.py:311
  *   mpasg_surface_pressure      diagnostics.py:10  physics_interface_surface_pressure
  *   mpasg_sfc_order, mpasg_edge_order  mesh_reordering.py:106 compute_rcm_permutation (SFC orders)
+ *   mpasg_tridiag_*             autodiff/tridiagonal_solve.py:177, autodiff/tridiagonal_factor.py:145
  *   mpasg_advance_scalars_static  (no counterpart: advance_scalars.py:1272 without caller scratch)
  */
 #ifndef MPASG_H
@@ -276,6 +277,35 @@ int mpasg_surface_pressure(int nCells, int rows, int nVertLevels, const double *
  * surface-pressure anomaly functional of the differentiation tests. */
 int mpasg_weighted_sq_sum(long long n, const double *x, const double *ref, const double *weight,
                           double *out, void *stream);
+
+/* ---- column tridiagonal operators and their derivatives --------------------------- */
+/* One column per row: a / b / c / alpha / gamma are (n, L), rhs / out (n, L+1), float64.
+ *   factor: alpha_k = 1/(b_k - a_k gamma_(k-1)), gamma_k = c_k alpha_k (k >= 1; row 0 zero)
+ *   solve:  u_k = (rhs_k - a_k u_(k-1)) alpha_k (1 <= k < L); out_k = u_k - gamma_k out_(k+1)
+ * *_vjp: reverse mode (gradients of every input from the output cotangents);
+ * *_jvp: forward mode (output tangent from input tangents; a null tangent is zero).
+ * Replace TridiagonalSolve (autodiff/tridiagonal_solve.py:177, VJP :232-291, JVP :294-352)
+ * and TridiagonalFactorize (autodiff/tridiagonal_factor.py:145). */
+int mpasg_tridiag_solve(long long n, int L, const double *a, const double *alpha,
+                        const double *gamma, const double *rhs, double *out, void *stream);
+int mpasg_tridiag_solve_vjp(long long n, int L, const double *a, const double *alpha,
+                            const double *gamma, const double *rhs, const double *out,
+                            const double *grad_out, double *grad_a, double *grad_alpha,
+                            double *grad_gamma, double *grad_rhs, void *stream);
+int mpasg_tridiag_solve_jvp(long long n, int L, const double *a, const double *alpha,
+                            const double *gamma, const double *rhs, const double *out,
+                            const double *da, const double *dalpha, const double *dgamma,
+                            const double *drhs, double *dout, void *stream);
+int mpasg_tridiag_factor(long long n, int L, const double *a, const double *b, const double *c,
+                         double *alpha, double *gamma, void *stream);
+int mpasg_tridiag_factor_vjp(long long n, int L, const double *a, const double *c,
+                             const double *alpha, const double *gamma, const double *grad_alpha,
+                             const double *grad_gamma, double *grad_a, double *grad_b,
+                             double *grad_c, void *stream);
+int mpasg_tridiag_factor_jvp(long long n, int L, const double *a, const double *c,
+                             const double *alpha, const double *gamma, const double *da,
+                             const double *db, const double *dc, double *dalpha, double *dgamma,
+                             void *stream);
 
 /* ---- mesh reordering (host functions; no GPU needed) -------------------------------- */
 /* new_to_old[i] = the old index of the i-th point along the 3-D Hilbert curve through

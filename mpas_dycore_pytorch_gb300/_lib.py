@@ -120,7 +120,9 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_divergence_damping", "mpasg_recover_large_step", "mpasg_solve_diagnostics",
            "mpasg_advance_scalars", "mpasg_advance_scalars_mono", "mpasg_reconstruct_2d",
            "mpasg_advance_scalars_static", "mpasg_numerics_check", "mpasg_surface_pressure",
-           "mpasg_weighted_sq_sum", "mpasg_sfc_order", "mpasg_edge_order", "mpasg_permute_rows")
+           "mpasg_weighted_sq_sum", "mpasg_sfc_order", "mpasg_edge_order", "mpasg_permute_rows",
+           "mpasg_tridiag_solve", "mpasg_tridiag_solve_vjp", "mpasg_tridiag_solve_jvp", "mpasg_tridiag_factor",
+           "mpasg_tridiag_factor_vjp", "mpasg_tridiag_factor_jvp")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -168,6 +170,12 @@ def load() -> C.CDLL:
         "mpasg_sfc_order": ([C.c_longlong, vp, vp, vp, vp], C.c_int),
         "mpasg_edge_order": ([C.c_longlong, C.c_longlong, vp, vp, vp], C.c_int),
         "mpasg_permute_rows": ([vp, vp, vp, C.c_longlong, C.c_longlong, vp], C.c_int),
+        "mpasg_tridiag_solve": ([C.c_longlong, C.c_int] + [vp] * 6, C.c_int),
+        "mpasg_tridiag_solve_vjp": ([C.c_longlong, C.c_int] + [vp] * 11, C.c_int),
+        "mpasg_tridiag_solve_jvp": ([C.c_longlong, C.c_int] + [vp] * 11, C.c_int),
+        "mpasg_tridiag_factor": ([C.c_longlong, C.c_int] + [vp] * 6, C.c_int),
+        "mpasg_tridiag_factor_vjp": ([C.c_longlong, C.c_int] + [vp] * 10, C.c_int),
+        "mpasg_tridiag_factor_jvp": ([C.c_longlong, C.c_int] + [vp] * 10, C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libmpasg.so"
-SOURCES = ("kern_column.cu", "kern_tend.cu", "kern_diag.cu", "kern_transport.cu", "driver.cu", "reorder.cu")
+SOURCES = ("kern_column.cu", "kern_tend.cu", "kern_diag.cu", "kern_transport.cu", "driver.cu", "reorder.cu", "kern_adjoint.cu")
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
 
 

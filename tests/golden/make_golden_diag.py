@@ -5,7 +5,10 @@ Runs the reference's ``physics_interface_surface_pressure`` (mpas_pytorch/diagno
 on the evolved states stored in the committed ``g2_*`` fixtures (after step 1 and step 2)
 and writes ``sp_g2.npz`` (one array per case and step); runs ``apply_rcm_reordering``
 (mpas_pytorch/mesh_reordering.py:243) on the ``g2_explicit`` loaded mesh and writes the
-permutations and the reordered connectivity / fields to ``rcm_g2.npz``.  Imports the
+permutations and the reordered connectivity / fields to ``rcm_g2.npz``; runs the
+reference's ``TridiagonalSolve`` and ``TridiagonalFactorize`` (forward, reverse mode
+through ``torch.autograd.grad``, forward mode through ``torch.autograd.forward_ad``) on
+seeded diagonally dominant column systems and writes ``tridiag_ref.npz``.  Imports the
 reference the same way as ``make_golden.py`` (netCDF4 stub).
 
 Run:  python tests/golden/make_golden_diag.py
@@ -62,6 +65,52 @@ def main() -> None:
         rec[f"state/{k}"] = rst[k].numpy()
     np.savez_compressed(HERE / "rcm_g2.npz", **rec)
     print("wrote", HERE / "rcm_g2.npz", len(rec))
+
+    import torch.autograd.forward_ad as fw
+    from mpas_pytorch.autodiff.tridiagonal_factor import TridiagonalFactorize
+    from mpas_pytorch.autodiff.tridiagonal_solve import TridiagonalSolve
+    rec = {}
+    for n, L in ((3, 6), (17, 41)):
+        g = torch.Generator().manual_seed(1000 * n + L)
+        r = lambda *s: torch.randn(*s, generator=g, dtype=torch.float64)
+        a, c = 0.1 * r(n, L), 0.1 * r(n, L)
+        b = 1.0 + 0.1 * torch.rand(n, L, generator=g, dtype=torch.float64)
+        al, ga = TridiagonalFactorize.apply(a, b, c)
+        rhs = r(n, L + 1)
+        out = TridiagonalSolve.apply(a, al, ga, rhs)
+        tag = f"{n}x{L}"
+        rec.update({f"{tag}/a": a.numpy(), f"{tag}/b": b.numpy(), f"{tag}/c": c.numpy(), f"{tag}/rhs": rhs.numpy(),
+                    f"{tag}/alpha": al.numpy(), f"{tag}/gamma": ga.numpy(), f"{tag}/out": out.numpy()})
+        w, wa, wg = r(n, L + 1), r(n, L), r(n, L)
+        ins = [t.clone().requires_grad_(True) for t in (a, al, ga, rhs)]
+        o = TridiagonalSolve.apply(*ins)
+        grads = torch.autograd.grad((o * w).sum(), ins)
+        for nm, gr in zip(("a", "alpha", "gamma", "rhs"), grads):
+            rec[f"{tag}/solve_vjp_{nm}"] = gr.numpy()
+        rec[f"{tag}/solve_w"] = w.numpy()
+        tans = [r(*t.shape) for t in (a, al, ga, rhs)]
+        with fw.dual_level():
+            duals = [fw.make_dual(p, t) for p, t in zip((a, al, ga, rhs), tans)]
+            _, tout = fw.unpack_dual(TridiagonalSolve.apply(*duals))
+        for nm, t in zip(("a", "alpha", "gamma", "rhs"), tans):
+            rec[f"{tag}/solve_tan_{nm}"] = t.numpy()
+        rec[f"{tag}/solve_jvp"] = tout.numpy()
+        fins = [t.clone().requires_grad_(True) for t in (a, b, c)]
+        fal, fga = TridiagonalFactorize.apply(*fins)
+        fgrads = torch.autograd.grad((fal * wa).sum() + (fga * wg).sum(), fins)
+        rec[f"{tag}/factor_wa"], rec[f"{tag}/factor_wg"] = wa.numpy(), wg.numpy()
+        for nm, gr in zip(("a", "b", "c"), fgrads):
+            rec[f"{tag}/factor_vjp_{nm}"] = gr.numpy()
+        ftans = [r(n, L) for _ in range(3)]
+        with fw.dual_level():
+            duals = [fw.make_dual(p, t) for p, t in zip((a, b, c), ftans)]
+            o1, o2 = TridiagonalFactorize.apply(*duals)
+            rec[f"{tag}/factor_jvp_alpha"] = fw.unpack_dual(o1)[1].numpy()
+            rec[f"{tag}/factor_jvp_gamma"] = fw.unpack_dual(o2)[1].numpy()
+        for nm, t in zip(("a", "b", "c"), ftans):
+            rec[f"{tag}/factor_tan_{nm}"] = t.numpy()
+    np.savez_compressed(HERE / "tridiag_ref.npz", **rec)
+    print("wrote", HERE / "tridiag_ref.npz", len(rec))
 
 
 if __name__ == "__main__":
