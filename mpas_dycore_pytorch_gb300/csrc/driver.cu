@@ -247,7 +247,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
       CHECK_RC(mpasg_smlstep_pert(m, c, &f, stream));
       MARK(MPASG_STAGE_SMLSTEP);
       for (int small = 1; small <= nsub[rk - 1]; ++small) {
-        CHECK_RC(mpasg_acoustic_step(m, c, &f, small, dts, stream));
+        CHECK_RC(mpasgi_acoustic_step(m, c, &f, small, dts, s, true));
         MARK(MPASG_STAGE_ACOUSTIC);
         CHECK_RC(mpasg_divergence_damping(m, c, &f, dts, stream));
         MARK(MPASG_STAGE_DIVDAMP);

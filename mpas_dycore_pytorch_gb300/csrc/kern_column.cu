@@ -284,6 +284,142 @@ __global__ void k_ac_thomas(mpasg_mesh m, mpasg_fields f) {
   }
 }
 
+// ---------------------------------------------------------------- acoustic columns, mixed form
+// The acoustic perturbations (rho_pp, rtheta_pp, rw_p, ru_p) are within-stage increments
+// without a large mean; the mixed form forms their right-hand sides and post-solve
+// increments in float32 and accumulates them in float64 (ac_rs, ac_ts, ac_x, rho_pp,
+// rtheta_pp, wwAvg); the tridiagonal solve stays float64.  theta at the edges is split
+// into the reference profile and the float32 deviation (theta_save_dev).
+struct AcLevelF {
+  float drs, dts, rho_in, rt_in;  // float32 increments of rs / ts, and the inputs
+};
+
+MPASG_D AcLevelF ac_level_mixed(const mpasg_mesh& m, const mpasg_fields& f, int c, int k, bool first, float dts,
+                                float resm, double* rs64, double* ts64) {
+  const int L = m.nVertLevels;
+  const int me = m.maxEdges;
+  const int n = m.nEdgesOnCell[c];
+  const float ia = m.invAreaCell_f32[c];
+  float rs = 0.0f, tsd = 0.0f;
+  for (int j = 0; j < n; ++j) {
+    int e = m.edgesOnCell[c * me + j];
+    const float wgt = m.edgesOnCell_sign_f32[c * me + j] * m.dvEdge_f32[e];
+    const float flux = dts * wgt * cv<float>(f.ru_p[(size_t)e * L + k]) * ia;
+    int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
+    const float th_e = 0.5f * (f.theta_save_dev[(size_t)c2 * L + k] + f.theta_save_dev[(size_t)c1 * L + k]);
+    rs = rs - flux;
+    tsd = tsd - flux * th_e;
+  }
+  const float ts = cv<float>(m.ref_theta[k]) * rs + tsd;  // sum_j -flux_j (ref + theta'_j)
+  const size_t o = (size_t)c * L + k;
+  const size_t ow = (size_t)c * (L + 1) + k;
+  AcLevelF a;
+  const double rho_in = first ? 0.0 : f.rho_pp[o];
+  const double rt_in = first ? 0.0 : f.rtheta_pp[o];
+  a.rho_in = cv<float>(rho_in);
+  a.rt_in = cv<float>(rt_in);
+  const float rwp_k = first ? 0.0f : cv<float>(f.rw_p[ow]);
+  const float rwp_k1 = first ? 0.0f : cv<float>(f.rw_p[ow + 1]);
+  a.drs = dts * cv<float>(f.tend_rho[o]) + rs - cv<float>(f.cofrz[k]) * resm * (rwp_k1 - rwp_k);
+  a.dts = dts * cv<float>(f.tend_theta[o]) + ts -
+          resm * m.rdzw_f32[k] * (cv<float>(f.coftz[ow + 1]) * rwp_k1 - cv<float>(f.coftz[ow]) * rwp_k);
+  if (rs64) *rs64 = rho_in + f64(a.drs);
+  if (ts64) *ts64 = rt_in + f64(a.dts);
+  return a;
+}
+
+__global__ void __launch_bounds__(kBlock) k_ac_prep_mixed(mpasg_mesh m, mpasg_fields f, FastDiv fl1,
+                                                          int small_step, float dts, float epssm, float resm) {
+  __shared__ AcLevelF s_lv[kBlock];
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < (uint32_t)m.nCells * (L + 1);
+  const bool first = (small_step == 1);
+  uint32_t c = 0, k = 0;
+  AcLevelF lv{0.0f, 0.0f, 0.0f, 0.0f};
+  double rs64 = 0.0, ts64 = 0.0;
+  if (active) {
+    c = fl1.div(i);
+    k = i - c * (L + 1);
+    if (k < (uint32_t)L) lv = ac_level_mixed(m, f, c, k, first, dts, resm, &rs64, &ts64);
+  }
+  s_lv[threadIdx.x] = lv;
+  __syncthreads();
+  if (!active) return;
+  const size_t o = (size_t)c * L;
+  const size_t ow = (size_t)c * (L + 1);
+  if (k < (uint32_t)L) {
+    f.ac_rs[o + k] = rs64;
+    f.ac_ts[o + k] = ts64;
+    f.rtheta_pp_old[o + k] = first ? 0.0 : f.rtheta_pp[o + k];
+  }
+  const double rwp_k = first ? 0.0 : f.rw_p[ow + k];
+  if (k == 0 || k == (uint32_t)L) {  // boundary values pass through the solve unchanged
+    f.ac_x[ow + k] = rwp_k;
+    if (first) f.wwAvg[ow + k] = 0.0;
+    return;
+  }
+  const AcLevelF lo = (threadIdx.x >= 1) ? s_lv[threadIdx.x - 1]
+                                         : ac_level_mixed(m, f, c, k - 1, first, dts, resm, nullptr, nullptr);
+  const double ww_in = first ? 0.0 : f.wwAvg[ow + k];
+  const float rwp = cv<float>(rwp_k);
+  f.wwAvg[ow + k] = ww_in + f64(0.5f * (1.0f - epssm) * rwp);
+  const float zz_k = m.zz_f32[o + k], zz_km1 = m.zz_f32[o + k - 1];
+  const float cw_k = cv<float>(f.cofwt[o + k]), cw_km1 = cv<float>(f.cofwt[o + k - 1]);
+  const float ts_k = lv.rt_in + lv.dts, ts_km1 = lo.rt_in + lo.dts;
+  const float rs_k = lv.rho_in + lv.drs, rs_km1 = lo.rho_in + lo.drs;
+  const float inc = dts * cv<float>(f.tend_rw[ow + k]) -
+                    cv<float>(f.cofwz[o + k]) *
+                        ((zz_k * ts_k - zz_km1 * ts_km1) + resm * (zz_k * lv.rt_in - zz_km1 * lo.rt_in)) -
+                    cv<float>(f.cofwr[o + k]) * ((rs_k + rs_km1) + resm * (lv.rho_in + lo.rho_in)) +
+                    cw_k * (ts_k + resm * lv.rt_in) + cw_km1 * (ts_km1 + resm * lo.rt_in);
+  f.ac_x[ow + k] = rwp_k + f64(inc);
+}
+
+// Rayleigh damping of the solution (float64); levels without damping pass through
+MPASG_D double ac_damped_mixed(const mpasg_mesh& m, const mpasg_fields& f, size_t o, size_t ow, int k, int L,
+                               double x, double dts) {
+  if (k == 0 || k == L) return x;
+  const double dss = m.dss[o + k];
+  if (dss == 0.0) return x;
+  double fzm = m.fzm[k], fzp = m.fzp[k];
+  double zz_i = fzm * m.zz[o + k] + fzp * m.zz[o + k - 1];
+  double rho_i = fzm * f.rho_zz[o + k] + fzp * f.rho_zz[o + k - 1];
+  double rw_delta = f.rw_save[ow + k] - f.rw[ow + k];
+  double num = x + rw_delta - dts * dss * zz_i * rho_i * f.w[ow + k];
+  return fdiv<float>(num, 1.0 + dts * dss) - rw_delta;
+}
+
+__global__ void __launch_bounds__(kBlock) k_ac_post_mixed(mpasg_mesh m, mpasg_fields f, FastDiv fl1, double dts,
+                                                          float epssm) {
+  __shared__ double s_xr[kBlock];
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < (uint32_t)m.nCells * (L + 1);
+  uint32_t c = 0, k = 0;
+  size_t o = 0, ow = 0;
+  double xr = 0.0;
+  if (active) {
+    c = fl1.div(i);
+    k = i - c * (L + 1);
+    o = (size_t)c * L;
+    ow = (size_t)c * (L + 1);
+    xr = ac_damped_mixed(m, f, o, ow, k, L, f.ac_x[ow + k], dts);
+  }
+  s_xr[threadIdx.x] = xr;
+  __syncthreads();
+  if (!active) return;
+  f.rw_p[ow + k] = xr;
+  if (k >= 1 && k < (uint32_t)L) f.wwAvg[ow + k] = f.wwAvg[ow + k] + f64(0.5f * (1.0f + epssm) * cv<float>(xr));
+  if (k == (uint32_t)L) return;
+  const double xr1 = (threadIdx.x + 1 < blockDim.x) ? s_xr[threadIdx.x + 1]
+                                                    : ac_damped_mixed(m, f, o, ow, k + 1, L, f.ac_x[ow + k + 1], dts);
+  const float x0 = cv<float>(xr), x1 = cv<float>(xr1);
+  f.rho_pp[o + k] = f.ac_rs[o + k] - f64(cv<float>(f.cofrz[k]) * dif<float>(xr1, xr));
+  f.rtheta_pp[o + k] = f.ac_ts[o + k] - f64(m.rdzw_f32[k] * (cv<float>(f.coftz[ow + k + 1]) * x1 -
+                                                             cv<float>(f.coftz[ow + k]) * x0));
+}
+
 // The same sweeps with the columns staged through shared memory: one warp solves 32
 // columns; the block's x, a, alpha and gamma are loaded and stored with coalesced
 // accesses (consecutive threads read consecutive levels of a column) into a [level][33]
@@ -626,18 +762,28 @@ extern "C" int mpasg_vert_imp_coefs(const mpasg_mesh* m, const mpasg_config* c, 
 
 extern "C" int mpasg_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
                                    int small_step, double dts, void* stream) {
+  return mpasgi_acoustic_step(m, c, f, small_step, dts, (cudaStream_t)stream, false);
+}
+
+int mpasgi_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int small_step, double dts,
+                         cudaStream_t s, bool copies_current) {
   if (!m || !c || !f || small_step < 1) return MPASG_E_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
+  if (c->precision == MPASG_PRECISION_MIXED && !copies_current) {
+    const int rc = mpasgi_theta_dev(m, f, s);  // the float32 theta deviations read below
+    if (rc != MPASG_OK) return rc;
+  }
   const int L = m->nVertLevels;
   const double rcv = kRgas / (kCp - kRgas);
   const double c2 = kCp * rcv;
   const double resm = (1.0 - c->epssm) / (1.0 + c->epssm);
   const long long ncw = (long long)m->nCells * (L + 1);
-  if (c->precision == MPASG_PRECISION_MIXED) {
+  const bool mixed = c->precision == MPASG_PRECISION_MIXED;
+  if (mixed) {
     k_acoustic_edges<float><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), small_step,
                                                                                 dts, c2);
     MPASG_LAUNCH_CHECK();
-    k_ac_prep<float><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, dts, c->epssm, resm);
+    k_ac_prep_mixed<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, (float)dts,
+                                                    (float)c->epssm, (float)resm);
     MPASG_LAUNCH_CHECK();
   } else {
     k_acoustic_edges<double><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), small_step,
@@ -661,7 +807,10 @@ extern "C" int mpasg_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, m
   else
     k_ac_thomas<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
   MPASG_LAUNCH_CHECK();
-  k_ac_post<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), dts, c->epssm);
+  if (mixed)
+    k_ac_post_mixed<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), dts, (float)c->epssm);
+  else
+    k_ac_post<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), dts, c->epssm);
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }

@@ -634,6 +634,13 @@ int launch_dyn_tend(const mpasg_mesh* m, mpasg_fields* f, const TendScalars& p, 
 
 }  // namespace
 
+int mpasgi_theta_dev(const mpasg_mesh* m, mpasg_fields* f, cudaStream_t s) {
+  const int L = m->nVertLevels;
+  k_theta_dev<<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, FastDiv(L));
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
 extern "C" int mpasg_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step,
                               void* stream) {
   return mpasgi_dyn_tend(m, c, f, rk_step, (cudaStream_t)stream, false);
