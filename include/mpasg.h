@@ -189,6 +189,7 @@ typedef struct mpasg_fields {
   double *ac_rs, *ac_ts;                                            /* (C+1, L) */
   double *ac_x;                                                     /* (C+1, L+1) */
   double *b_tri, *c_tri;                                            /* (C+1, L) */
+  double *tri_m;        /* (C+1, L) mixed form: -alpha_tri * a_tri, the forward-sweep factor */
   /* mixed form (float32): copies of u, pv_edge, w, rw kept current by the step, the
    * deviations theta_m - ref_theta and theta_m_save - ref_theta, and the stencils'
    * intermediate edge fluxes, edge / vertex kinetic energy and vertex PV */

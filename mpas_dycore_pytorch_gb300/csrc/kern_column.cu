@@ -140,6 +140,7 @@ __global__ void k_vimp_factor(mpasg_mesh m, mpasg_fields f) {
     gam = f.c_tri[o + k] * alpha;
     f.alpha_tri[o + k] = alpha;
     f.gamma_tri[o + k] = gam;
+    if (sizeof(T) != sizeof(double)) f.tri_m[o + k] = -(alpha * f.a_tri[o + k]);
   }
 }
 
@@ -473,6 +474,61 @@ __global__ void __launch_bounds__(kThomasCols) k_ac_thomas_staged(mpasg_mesh m, 
   }
 }
 
+// Mixed form (still float64): u_k = alpha_k x_k + m_k u_(k-1) with m_k = -alpha_k a_k
+// precomputed by the factorisation, so the serial dependence is one FMA per level
+// (alpha_k x_k does not depend on the chain and issues ahead).
+__global__ void __launch_bounds__(kThomasCols) k_ac_thomas_staged_mixed(mpasg_mesh m, mpasg_fields f, FastDiv fl,
+                                                                        FastDiv fl1) {
+  extern __shared__ double s_col[];
+  const int L = m.nVertLevels;
+  double* sx = s_col;
+  double* sm = sx + (size_t)(L + 1) * kThomasPitch;
+  double* sal = sm + (size_t)L * kThomasPitch;
+  double* sg = sal + (size_t)L * kThomasPitch;
+  const int c0 = blockIdx.x * kThomasCols;
+  const int ncol = min(kThomasCols, m.nCells - c0);
+  const int t = threadIdx.x;
+  const uint32_t nw = (uint32_t)ncol * (L + 1), nl = (uint32_t)ncol * L;
+  const double* gx = f.ac_x + (size_t)c0 * (L + 1);
+  const size_t o0 = (size_t)c0 * L;
+  for (uint32_t idx = t; idx < nw; idx += kThomasCols) {
+    uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
+    sx[k * kThomasPitch + col] = gx[idx];
+  }
+  for (uint32_t idx = t; idx < nl; idx += kThomasCols) {
+    uint32_t col = fl.div(idx), k = idx - col * L;
+    sm[k * kThomasPitch + col] = f.tri_m[o0 + idx];
+    sal[k * kThomasPitch + col] = f.alpha_tri[o0 + idx];
+    sg[k * kThomasPitch + col] = f.gamma_tri[o0 + idx];
+  }
+  __syncwarp();
+  if (t < ncol) {
+    double xp = sx[t];
+    for (int k = 1; k < L; ++k) {
+      xp = fma(sm[k * kThomasPitch + t], xp, sal[k * kThomasPitch + t] * sx[k * kThomasPitch + t]);
+      sx[k * kThomasPitch + t] = xp;
+    }
+    double xn = sx[L * kThomasPitch + t];
+    for (int k = L - 1; k >= 0; --k) {
+      xn = fma(-sg[k * kThomasPitch + t], xn, sx[k * kThomasPitch + t]);
+      sx[k * kThomasPitch + t] = xn;
+    }
+  }
+  __syncwarp();
+  double* gxo = f.ac_x + (size_t)c0 * (L + 1);
+  for (uint32_t idx = t; idx < nw; idx += kThomasCols) {
+    uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
+    gxo[idx] = sx[k * kThomasPitch + col];
+  }
+}
+
+// tri_m = -alpha_tri * a_tri (the mixed forward-sweep factor) from the stored factors
+__global__ void k_tri_m(long long n, const double* __restrict__ a, const double* __restrict__ al,
+                        double* __restrict__ tm) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) tm[i] = -(al[i] * a[i]);
+}
+
 size_t thomas_smem_bytes(int L) { return (size_t)(4 * L + 1) * kThomasPitch * sizeof(double); }
 
 MPASG_D double ac_damped(const mpasg_mesh& m, const mpasg_fields& f, size_t o, size_t ow, int k, int L, double x,
@@ -771,6 +827,9 @@ int mpasgi_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_field
   if (c->precision == MPASG_PRECISION_MIXED && !copies_current) {
     const int rc = mpasgi_theta_dev(m, f, s);  // the float32 theta deviations read below
     if (rc != MPASG_OK) return rc;
+    const long long n = (long long)m->nCells * m->nVertLevels;
+    k_tri_m<<<nblocks(n), kBlock, 0, s>>>(n, f->a_tri, f->alpha_tri, f->tri_m);  // forward-sweep factor
+    MPASG_LAUNCH_CHECK();
   }
   const int L = m->nVertLevels;
   const double rcv = kRgas / (kCp - kRgas);
@@ -799,11 +858,19 @@ int mpasgi_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_field
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MPASG_E_CUDA;
   if (!smem_opt_in[dev])
-    smem_opt_in[dev] = cudaFuncSetAttribute(k_ac_thomas_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            200 * 1024) == cudaSuccess;
-  if (smem_opt_in[dev] && smem <= 200 * 1024)
+    smem_opt_in[dev] =
+        cudaFuncSetAttribute(k_ac_thomas_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+            cudaSuccess &&
+        cudaFuncSetAttribute(k_ac_thomas_staged_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+            cudaSuccess;
+  if (smem_opt_in[dev] && smem <= 200 * 1024 && mixed)
+    k_ac_thomas_staged_mixed<<<nblocks(m->nCells, kThomasCols), kThomasCols, smem, s>>>(*m, *f, FastDiv(L),
+                                                                                        FastDiv(L + 1));
+  else if (smem_opt_in[dev] && smem <= 200 * 1024)
     k_ac_thomas_staged<<<nblocks(m->nCells, kThomasCols), kThomasCols, smem, s>>>(*m, *f, FastDiv(L),
                                                                                   FastDiv(L + 1));
+  else if (mixed)
+    return MPASG_E_ARG;  // the mixed sweep needs the staged kernel (L <= 200)
   else
     k_ac_thomas<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
   MPASG_LAUNCH_CHECK();
