@@ -60,7 +60,12 @@ MPASG_D VimpLevel vimp_level(const mpasg_mesh& m, const mpasg_fields& f, size_t 
   double zz = m.zz[o + k], p = f.exner[o + k];
   double rb = m.rho_base[o + k], rtb = f.rtheta_base[o + k], pb = f.exner_base[o + k];
   double rt = f.rtheta_p[o + k], q = f.qtot[o + k];
-  v.cofwt = fdiv<T>(fdiv<T>(0.5 * dtseps * rcv * zz * kGravity * rb, 1.0 + q) * p, (rtb + rt) * pb);
+  if (sizeof(T) == sizeof(double))
+    v.cofwt = fdiv<T>(fdiv<T>(0.5 * dtseps * rcv * zz * kGravity * rb, 1.0 + q) * p, (rtb + rt) * pb);
+  else  // mixed form: the dry case needs no 1 / (1 + q)
+    v.cofwt = (q == 0.0 ? 0.5 * dtseps * rcv * zz * kGravity * rb
+                        : fdiv<T>(0.5 * dtseps * rcv * zz * kGravity * rb, 1.0 + q)) *
+              p * rcp_nr((rtb + rt) * pb);
   v.coftz = (k == 0) ? 0.0 : dtseps * (m.fzm[k] * f.theta_m[o + k] + m.fzp[k] * f.theta_m[o + k - 1]);
   return v;
 }
@@ -670,7 +675,7 @@ __global__ void k_recover_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int r
     f.rho_p[o] = rho_p;
     f.rho_zz[o] = rho_zz;
     f.rtheta_p[o] = rtheta_p;
-    f.theta_m[o] = fdiv<T>(rtheta_p + rtb, rho_zz);
+    f.theta_m[o] = sizeof(T) == sizeof(double) ? (rtheta_p + rtb) / rho_zz : (rtheta_p + rtb) * rcp_nr1(rho_zz);
     if (rk_step == 3) {
       const double rcv = kRgas / (kCp - kRgas);
       double zz = m.zz[o];
@@ -718,7 +723,8 @@ __global__ void k_recover_edges(mpasg_mesh m, mpasg_fields f, FastDiv fl, double
   f.ruAvg[i] = rus + f.ruAvg[i] * inv_ns;
   double ru = rus + f.ru_p[i];
   f.ru[i] = ru;
-  const double u = fdiv<T>(2.0 * ru, f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k]);
+  const double rho2 = f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k];
+  const double u = sizeof(T) == sizeof(double) ? 2.0 * ru / rho2 : 2.0 * ru * rcp_nr1(rho2);
   f.u[i] = u;
   if (sizeof(T) != sizeof(double)) f.u_f32[i] = d2f_bits(u);
 }

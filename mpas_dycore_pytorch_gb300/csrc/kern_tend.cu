@@ -585,7 +585,9 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
     tmean = tmean - m.rdzw[k] * (wr_k1 - wr_k);
     const double ttot = f64(tt) + tmean;
     const double rz = f.rho_zz[o];
-    f.rthdynten[o] = (ttot - f.tend_rho[o] * f.theta_m[o]) * rcp_nr(rz);
+    // (a diagnostic for physics coupling: the cancelling difference in float64, the
+    // quotient in float32)
+    f.rthdynten[o] = f64(cv<T>(ttot - f.tend_rho[o] * f.theta_m[o]) / cv<T>(rz));
     f.tend_theta[o] = ttot + rz * f.rt_diabatic_tend[o] + f.tend_theta_euler[o];
   }
 }
