@@ -156,6 +156,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_throughput(ms_local: float, cell_levels_per_step: int, K: int, world: int, device=None):
+    """Whole-job throughput of ``world`` independent replicas: the slowest rank's time
+    (all-reduce MAX; no exchange otherwise) and the cell-level-steps of all ranks over it."""
+    import torch
+    ms = float(ms_local)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * cell_levels_per_step * K / (ms / 1e3)
+
+
 def _time_steps(step, K, W):
     """ms per step of ``step()`` over K calls after W warm-up calls (CUDA events)."""
     import torch
@@ -350,14 +363,11 @@ def run_gb300(args, rank, world):
         end.record()
         torch.cuda.synchronize()
     ms = start.elapsed_time(end)
+    ms, value = replica_throughput(ms, C_ * L_, K, world, dev)
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
     bad = model.check_finite()
-    value = world * C_ * L_ * K / (ms / 1e3)
 
     if timed_graph is not None:
         stage_ms = {}
@@ -414,8 +424,8 @@ def run_gb300(args, rank, world):
             host[k].copy_(ex[k], non_blocking=True)
     e_end.record()
     torch.cuda.synchronize()
-    e_ms = e_start.elapsed_time(e_end)
-    e2e = {"value": world * C_ * L_ * K / (e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+    e_ms, e_value = replica_throughput(e_start.elapsed_time(e_end), C_ * L_, K, world, dev)
+    e2e = {"value": e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": h2d}
 
     state_bytes = model.state.bytes
