@@ -210,6 +210,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
     for prec in ("float64", "mixed"):
         m = Model(st, cfg, w["dt"], num_scalars=S, device=dev, precision=prec, order=args.order)
         m.prepare(st)
+        tune = m.autotune()
         _graph_model(m)
         for _ in range(nerr - 1):
             m.step()
@@ -229,7 +230,8 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
     forms["mixed"] = {"value": cl / (ms_mixed / 1e3), "ms_per_step": ms_mixed,
                       "speedup_vs_float64": ms_plain / ms_mixed,
                       "max_rel_l2_vs_float64_after_24_steps": max(err.values()),
-                      "worst_field": max(err, key=err.get), "dtype": "f32 stencils / f64 state"}
+                      "worst_field": max(err, key=err.get), "dtype": "f32 stencils / f64 state",
+                      "autotune": tune}
     if args.ensemble > 0:
         ew = WORKLOADS["c2"]
         ecfg = _cfg(ew)
@@ -238,6 +240,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
             spec, ecfg, as_torch=False)
         m = Model(single, ecfg, ew["dt"], num_scalars=S, device=dev, order=args.order)
         m.prepare(single)
+        m.autotune()
         ms_single = _time_steps(_graph_model(m).step, K, W)
         cl1 = st_cells_levels(single)
         del m
@@ -245,6 +248,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
         members = member_cases(spec, seeds=list(range(100, 100 + args.ensemble)), config=ecfg, u_noise=0.5)
         for prec in ("float64", "mixed"):
             ens = Ensemble(members, ecfg, ew["dt"], precision=prec, device=dev, order=args.order)
+            etune = ens.model.autotune()
             _graph_model(ens.model)
             ms_e = _time_steps(ens.step, K, W)
             bad = ens.model.check_finite()
@@ -253,7 +257,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
                 "value": ens.cell_levels / (ms_e / 1e3), "ms_per_step": ms_e,
                 "aggregate_vs_single_member_float64": (ens.cell_levels / ms_e) / (cl1 / ms_single),
                 "single_member_float64_value": cl1 / (ms_single / 1e3), "nonfinite": bad,
-                "state_bytes": ens.model.state.bytes}
+                "state_bytes": ens.model.state.bytes, "autotune": etune}
             del ens
             torch.cuda.empty_cache()
     return forms
@@ -301,6 +305,7 @@ def run_gb300(args, rank, world):
     S = int(st["scalars"].shape[-1])
     model = Model(st, cfg, w["dt"], num_scalars=S, device=dev, precision=args.precision, order=args.order)
     model.prepare(st)
+    tuning = model.autotune()
     C_, L_ = model.dmesh.nCells, model.dmesh.nVertLevels
     lib = model.lib
     # launches per step (eager step, counted by the library)
@@ -444,7 +449,8 @@ def run_gb300(args, rank, world):
                    "state_bytes": state_bytes,
                    "l2": "inputs larger than L2 (device state %.1f GB)" % (state_bytes / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "cuda_graph": True, "bytes_per_cell_level_step": bytes_per_cell_level_step(S, True)},
+                   "cuda_graph": True, "bytes_per_cell_level_step": bytes_per_cell_level_step(S, True),
+                   "autotune": tuning},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * K,
         "clocks": clocks.summary(), "stage_ms_per_step": stage_ms, "nonfinite": bad,
         "forms": forms,

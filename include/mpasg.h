@@ -124,7 +124,8 @@ typedef struct mpasg_config {
   int32_t horiz_mixing_smagorinsky; /* 1: 2d_smagorinsky */
   int32_t num_scalars, moist_start, moist_end;
   int32_t precision;                /* MPASG_PRECISION_FLOAT64 or MPASG_PRECISION_MIXED */
-  int32_t reserved1;
+  int32_t tile_tend_u;              /* levels per thread of the u tendency: 1 (0), 2 or 4
+                                       (autotuned; tiles agree to one FMA rounding) */
 } mpasg_config;
 
 /* Arithmetic of the step.  FLOAT64: every stage in float64 (the reference's arithmetic).
@@ -230,6 +231,12 @@ int mpasg_step(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, void
  * boundaries (>= 0) or a negative status. */
 int mpasg_step_timed(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
                      void *const *events, int32_t *stage_kinds, int n_events, void *stream);
+/* Autotuner: times the tile shapes of the tuned kernels on the current state (the u
+ * tendency with 1, 2 and 4 levels per thread) and stores the fastest in c (tile_tend_u);
+ * times_ms (optional, 3 floats) receives the measured times.  Synchronises the stream;
+ * call it outside stream capture, after the state is loaded.  Leaves the state unchanged. */
+int mpasg_autotune(const mpasg_mesh *m, mpasg_config *c, mpasg_fields *f, float *times_ms,
+                   void *stream);
 /* Applies a helper of the mixed form to n device float64 values (in -> out), for testing
  * the helpers against CUDA's own conversions and division: which = 0 float64 -> float32 ->
  * float64 through the integer repacking; which = 1 the Newton-Raphson reciprocal. */

@@ -34,7 +34,7 @@ CONFIG_DOUBLES = ("dt", "epssm", "smdiv", "len_disp", "coef_3rd_order", "c_s", "
                   "del4u_div_factor", "apvm_upwinding", "h_mom_eddy_visc4", "h_theta_eddy_visc4")
 CONFIG_INTS = ("time_integration_order", "number_of_sub_steps", "dynamics_split_steps",
                "monotonic", "horiz_mixing_smagorinsky", "num_scalars", "moist_start", "moist_end",
-               "precision", "reserved1")
+               "precision", "tile_tend_u")
 PRECISIONS = {"float64": 0, "mixed": 1}
 
 # (name, kind) in header order; kind names the row space: e/c/cw/v/cs/es/cws/L/cL/cLw/...
@@ -123,7 +123,7 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_advance_scalars_static", "mpasg_numerics_check", "mpasg_surface_pressure",
            "mpasg_weighted_sq_sum", "mpasg_sfc_order", "mpasg_edge_order", "mpasg_permute_rows",
            "mpasg_tridiag_solve", "mpasg_tridiag_solve_vjp", "mpasg_tridiag_solve_jvp", "mpasg_tridiag_factor",
-           "mpasg_tridiag_factor_vjp", "mpasg_tridiag_factor_jvp")
+           "mpasg_tridiag_factor_vjp", "mpasg_tridiag_factor_jvp", "mpasg_autotune")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -171,6 +171,7 @@ def load() -> C.CDLL:
         "mpasg_sfc_order": ([C.c_longlong, vp, vp, vp, vp], C.c_int),
         "mpasg_edge_order": ([C.c_longlong, C.c_longlong, vp, vp, vp], C.c_int),
         "mpasg_permute_rows": ([vp, vp, vp, C.c_longlong, C.c_longlong, vp], C.c_int),
+        "mpasg_autotune": ([m, c, f, vp, vp], C.c_int),
         "mpasg_tridiag_solve": ([C.c_longlong, C.c_int] + [vp] * 6, C.c_int),
         "mpasg_tridiag_solve_vjp": ([C.c_longlong, C.c_int] + [vp] * 11, C.c_int),
         "mpasg_tridiag_solve_jvp": ([C.c_longlong, C.c_int] + [vp] * 11, C.c_int),

@@ -230,6 +230,18 @@ class Model:
         _lib.check(rc, "mpasg_step (capture)")
         self._graph = g
 
+    def autotune(self) -> dict:
+        """Pick the tile shapes of the tuned kernels on this mesh and state
+        (``mpasg_autotune``); returns the measured times per candidate (ms)."""
+        times = (C.c_float * 3)()
+        torch.cuda.synchronize()
+        rc = self.lib.mpasg_autotune(C.byref(self.dmesh.struct), C.byref(self.cstruct), C.byref(self.state.struct),
+                                     times, _stream_ptr())
+        _lib.check(rc, "mpasg_autotune")
+        self._graph = None  # a captured graph holds the old tile
+        return {"tend_u_levels_per_thread": int(self.cstruct.tile_tend_u),
+                "tend_u_ms": {1: times[0], 2: times[1], 4: times[2]}}
+
     def check_finite(self) -> int:
         self.call("mpasg_check_finite")
         return int(self.state.status[0].item())

@@ -152,6 +152,90 @@ __global__ void __launch_bounds__(kBlock) k_tend_u(mpasg_mesh m, mpasg_fields f,
   }
 }
 
+// k_tend_u with V consecutive levels per thread (a tile of the autotuner): the edge's
+// connectivity and TRiSK weights are loaded once for V levels, the V neighbour gathers
+// are independent, and the interface fluxes at k0 .. k0+V are computed in-thread (the
+// top one again by the next chunk).  Per level, the same expressions in the same order as
+// k_tend_u; the compiler may fuse multiply-adds differently in the two kernels, so the
+// tiles agree to the rounding of one FMA (last bit).
+template <typename T, int V>
+__global__ void __launch_bounds__(kBlock) k_tend_u_chunk(mpasg_mesh m, mpasg_fields f, FastDiv flc, int nchunk,
+                                                         TendScalars p) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * (uint32_t)nchunk) return;
+  const uint32_t e = flc.div(i);
+  const int k0 = (int)(i - e * (uint32_t)nchunk) * V;
+  const T* u = fp<T>(f.u, f.u_f32);
+  const T* rw = fp<T>(f.rw, f.rw_f32);
+  const T* fzm = G(fzm);
+  const T* fzp = G(fzp);
+  const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
+  const T* ue = u + (size_t)e * L;
+  T wd[V + 1];
+#pragma unroll
+  for (int v = 0; v <= V; ++v) {
+    const int kk = k0 + v;
+    wd[v] = T(0);
+    if (kk < L) {
+      T rwe = T(0.5) * (rw[(size_t)c1 * (L + 1) + kk] + rw[(size_t)c2 * (L + 1) + kk]);
+      wd[v] = wduz_at<T>(ue, rwe, kk, L, fzm, fzp);
+    }
+  }
+  const int n2 = m.nEdgesOnEdge[e];
+  const int me2 = m.maxEdges2;
+  const T* pv = fp<T>(f.pv_edge, f.pv_edge_f32);
+  const T* woe = G(weightsOnEdge);
+  T pv_self[V], q[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    pv_self[v] = (k0 + v < L) ? pv[(size_t)e * L + k0 + v] : T(0);
+    q[v] = T(0);
+  }
+  for (int j = 0; j < n2; ++j) {
+    const int eo = m.edgesOnEdge[e * me2 + j];
+    const T w = woe[e * me2 + j];
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      if (k0 + v < L) {
+        const size_t oo = (size_t)eo * L + k0 + v;
+        T t = (w * u[oo]) * (pv_self[v] + pv[oo]);
+        q[v] = (j == 0) ? t : q[v] + t;
+      }
+    }
+  }
+  const T inv_dc = G(invDcEdge)[e];
+#pragma unroll
+  for (int v = 0; v < V; ++v) {
+    const int k = k0 + v;
+    if (k >= L) break;
+    const size_t ie = (size_t)e * L + k;
+    T tu = -G(rdzw)[k] * ((k + 1 >= L ? T(0) : wd[v + 1]) - wd[v]);
+    const T qv = T(0.5) * q[v];
+    const size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
+    const T rho_e = cv<T>(f.h_edge[ie]);
+    tu = tu + rho_e * (qv - dif<T>(f.ke[i2], f.ke[i1]) * inv_dc) -
+         ue[k] * T(0.5) * (cv<T>(f.h_divergence[i1]) + cv<T>(f.h_divergence[i2]));
+    if (p.rk_step == 1) {
+      const T* zz = G(zz);
+      T teu = -cv<T>(f.cqu_e[ie]) * (div_or_one<T>(dif<T>(f.pressure_p[i2], f.pressure_p[i1]) * inv_dc,
+                                                   T(0.5) * (zz[i2] + zz[i1])) -
+                                     T(0.5) * G(zxu)[ie] * (cv<T>(f.dpdz[i1]) + cv<T>(f.dpdz[i2])));
+      int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
+      T r_dv = vmin(G(invDvEdge)[e], T(4) * inv_dc);
+      T u_diff = (cv<T>(f.divergence[i2]) - cv<T>(f.divergence[i1])) * inv_dc -
+                 (cv<T>(f.vorticity[(size_t)v2 * L + k]) - cv<T>(f.vorticity[(size_t)v1 * L + k])) * r_dv;
+      f.delsq_u[ie] = f64(u_diff);
+      T kdiffu = T(0.5) * (cv<T>(f.kdiff[i1]) + cv<T>(f.kdiff[i2]));
+      teu = teu + rho_e * kdiffu * u_diff * G(meshScalingDel2)[e];
+      f.tend_u_euler[ie] = f64(teu);
+      f.tend_u[ie] = f64(p.del4 ? tu : tu + teu);
+    } else {
+      f.tend_u[ie] = f64(tu + cv<T>(f.tend_u_euler[ie]));
+    }
+  }
+}
+
 template <typename T>
 __global__ void k_del4_vertex(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   const int L = m.nVertLevels;
@@ -592,8 +676,11 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
   }
 }
 
+MPASG_HD int tile_levels(int code) { return code == 2 ? 2 : code == 4 ? 4 : 1; }
+
 template <typename T>
-int launch_dyn_tend(const mpasg_mesh* m, mpasg_fields* f, const TendScalars& p, int rk_step, cudaStream_t s) {
+int launch_dyn_tend(const mpasg_mesh* m, mpasg_fields* f, const TendScalars& p, int rk_step, cudaStream_t s,
+                    int c_tile) {
   const int L = m->nVertLevels;
   const long long ncl = (long long)m->nCells * L, nel = (long long)m->nEdges * L;
   const long long ncw = (long long)m->nCells * (L + 1), nvl = (long long)m->nVertices * L;
@@ -604,7 +691,17 @@ int launch_dyn_tend(const mpasg_mesh* m, mpasg_fields* f, const TendScalars& p, 
   }
   k_tend_cells_a<T><<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, p);
   MPASG_LAUNCH_CHECK();
-  k_tend_u<T><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, p);
+  const int vt = tile_levels(c_tile);  // levels per thread of k_tend_u (autotuner choice)
+  if (vt == 1) {
+    k_tend_u<T><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, p);
+  } else {
+    const int nchunk = (L + vt - 1) / vt;
+    const long long nth = (long long)m->nEdges * nchunk;
+    if (vt == 2)
+      k_tend_u_chunk<T, 2><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+    else
+      k_tend_u_chunk<T, 4><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+  }
   MPASG_LAUNCH_CHECK();
   if (rk_step == 1) {
     if (p.del4) {
@@ -676,7 +773,66 @@ int mpasgi_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
       const int rc = mpasgi_pack_f32(m, f, s);
       if (rc != MPASG_OK) return rc;
     }
-    return launch_dyn_tend<float>(m, f, p, rk_step, s);
+    return launch_dyn_tend<float>(m, f, p, rk_step, s, c->tile_tend_u);
   }
-  return launch_dyn_tend<double>(m, f, p, rk_step, s);
+  return launch_dyn_tend<double>(m, f, p, rk_step, s, c->tile_tend_u);
+}
+
+// Autotuner: times the u-tendency kernel with 1, 2 and 4 levels per thread on the current
+// state (rk-2 form, 3 launches each after one warm-up) and keeps the fastest in
+// c->tile_tend_u.  Host-synchronising: call it outside stream capture.  The kernel only
+// writes its outputs (tend_u, ...), so the state is unchanged.
+extern "C" int mpasg_autotune(const mpasg_mesh* m, mpasg_config* c, mpasg_fields* f, float* times_ms,
+                              void* stream) {
+  if (!m || !c || !f) return MPASG_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool mixed = c->precision == MPASG_PRECISION_MIXED;
+  if (mixed) {
+    const int rc = mpasgi_pack_f32(m, f, s);
+    if (rc != MPASG_OK) return rc;
+  }
+  TendScalars p{};
+  p.rk_step = 2;
+  p.coef3 = c->coef_3rd_order;
+  const int L = m->nVertLevels;
+  const long long nel = (long long)m->nEdges * L;
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return MPASG_E_CUDA;
+  const int tiles[3] = {1, 2, 4};
+  float best = 1e30f;
+  int best_tile = 1;
+  int rc = MPASG_OK;
+  for (int t = 0; t < 3 && rc == MPASG_OK; ++t) {
+    const int vt = tiles[t];
+    const int nchunk = (L + vt - 1) / vt;
+    const long long nth = (long long)m->nEdges * nchunk;
+    float ms = 0.0f;
+    for (int rep = 0; rep < 4; ++rep) {
+      if (rep == 1) cudaEventRecord(a, s);
+      if (vt == 1) {
+        if (mixed) k_tend_u<float><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, FastDiv(L), p);
+        else k_tend_u<double><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, FastDiv(L), p);
+      } else if (vt == 2) {
+        if (mixed) k_tend_u_chunk<float, 2><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+        else k_tend_u_chunk<double, 2><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+      } else {
+        if (mixed) k_tend_u_chunk<float, 4><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+        else k_tend_u_chunk<double, 4><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+      }
+      mpasg_count_launch();
+      if (cudaGetLastError() != cudaSuccess) rc = MPASG_E_LAUNCH;
+    }
+    cudaEventRecord(b, s);
+    if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) rc = MPASG_E_CUDA;
+    ms /= 3.0f;
+    if (times_ms) times_ms[t] = ms;
+    if (rc == MPASG_OK && ms < best) {
+      best = ms;
+      best_tile = vt;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc == MPASG_OK) c->tile_tend_u = best_tile;
+  return rc;
 }
