@@ -371,6 +371,7 @@ class CaseSpec:
     u_noise: float = 0.0
     w_sine: float = 0.0
     round_wind_bits: int = 0
+    qv_surface: float = 0.0  # > 0: moist case, water vapour as scalar 0 (moist_end = 1)
 
 
 def _vertical_metrics(zw: np.ndarray) -> dict:
@@ -476,6 +477,10 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
         else:  # smooth product field
             h = 0.5 + 0.5 * np.cos(latc) ** 2 * np.cos(2.0 * lonc)
         tracers.append(np.repeat(h[:, None], nlev, 1))
+    qv = np.zeros((nc, nlev))
+    if spec.qv_surface > 0.0:  # vapour decaying with a 2.5 km scale height, wetter at the equator
+        qv = spec.qv_surface * np.exp(-zmid / 2500.0)[None, :] * (0.25 + 0.75 * np.cos(latc) ** 2)[:, None]
+        tracers = [qv] + tracers
     scalars = np.stack(tracers, -1) if tracers else np.zeros((nc, nlev, 0))
 
     zgrid = np.repeat(zw[None, :], nc, 0)
@@ -485,8 +490,8 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
         "zz": np.ones((nc, nlev)), "zgrid": zgrid,
         "zb": np.zeros((ne, 2, nlev + 1)), "zb3": np.zeros((ne, 2, nlev + 1)),
         "zxu": np.zeros((ne, nlev)),
-        "scalars": scalars, "num_scalars": spec.n_tracers, "qv": np.zeros((nc, nlev)),
-        "moist_start": 1, "moist_end": 0,
+        "scalars": scalars, "num_scalars": scalars.shape[-1], "qv": qv,
+        "moist_start": 1, "moist_end": 1 if spec.qv_surface > 0.0 else 0,
         "u_init": np.full(nlev, 0.0), "v_init": np.zeros(nlev),
         "t_init": theta_b.copy(), "qv_init": np.zeros(nlev),
     }

@@ -287,7 +287,8 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   // ---- split transport RK3 with the substep-averaged mass fluxes
   if (S > 0) {
     CHECK_RC(copy(f.scalars_a, f.scalars_init, ncs, s));
-    const double dts_t[3] = {dt / 3.0, dt / 2.0, dt};
+    // transport stage dts; the first is dt/2 for RK2 (time_integration.py:3366-3370)
+    const double dts_t[3] = {c->time_integration_order == 2 ? dt / 2.0 : dt / 3.0, dt / 2.0, dt};
     MARK(MPASG_STAGE_SPLIT);
     for (int rk = 1; rk <= 3; ++rk) {
       if (rk == 3 && c->monotonic) {

@@ -282,7 +282,8 @@ class Stepper:
         hfa = np.zeros((ne + 1, nl, scalars_init.shape[2]))
         tsave = np.zeros_like(scalars_init)
         for rk in range(1, 4):
-            dt_t = [dt / 3.0, dt / 2.0, dt][rk - 1]
+            # transport stage dts; the first is dt/2 for RK2 (time_integration.py:3366-3370)
+            dt_t = [dt / 2.0 if self.order == 2 else dt / 3.0, dt / 2.0, dt][rk - 1]
             if rk == 3 and self.monotonic:
                 out = self._call("scalars_mono", S.advance_scalars_mono, {
                     "dt": dt_t, "coef_3rd_order": self.coef3, "uhAvg": ru_avg, "wwAvg": ww_avg,

@@ -67,6 +67,14 @@ CASES = {
     # configs[1]-style: stretched levels, three tracers, monotone transport
     "g2_mono": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=1, n_bumps=8, n_tracers=3),
                     config=dict(config_monotonic=True), dt=1800.0, nsteps=2),
+    # moist: water vapour as scalar 0 (moist coefficients cqw / cqu != 1, theta_m != theta)
+    "g2_moist": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=2, n_bumps=6, n_tracers=1,
+                               qv_surface=0.012),
+                     config=dict(config_monotonic=True), dt=1200.0, nsteps=2),
+    # second-order Runge-Kutta (config_time_integration_order = 2), three acoustic substeps
+    "g2_rk2": dict(spec=dict(level=2, nlev=12, seed=3, n_bumps=6, n_tracers=2),
+                   config=dict(config_monotonic=False, config_time_integration_order=2,
+                               config_number_of_sub_steps=4), dt=900.0, nsteps=2),
 }
 
 BASE_CONFIG = {

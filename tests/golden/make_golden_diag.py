@@ -26,7 +26,7 @@ sys.path.insert(0, str(HERE))
 sys.path.insert(0, str(HERE.parent))
 
 import make_golden  # noqa: E402
-from fixtures import group, load_case  # noqa: E402
+from fixtures import CASES, group, load_case  # noqa: E402
 
 
 def main() -> None:
@@ -35,7 +35,7 @@ def main() -> None:
     from mpas_pytorch.diagnostics import physics_interface_surface_pressure
 
     out = {}
-    for case in ("g2_explicit", "g2_mono"):
+    for case in CASES:
         meta, st, _ = load_case(case)
         loaded, prepared = group(st, "loaded"), group(st, "prepared")
         nc = int(np.asarray(loaded["nCells"]).reshape(-1)[0])

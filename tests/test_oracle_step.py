@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from oracle.step import Stepper
-from fixtures import CASES, group, load_case, rel_l2
+from fixtures import CASES, group, load_case, rel_l2, step_tol
 
 FIELDS = ("u", "w", "theta_m", "rho_zz", "scalars", "rho_p", "rtheta_p", "exner", "pressure_p",
           "ru", "rw", "v", "divergence", "vorticity", "ke", "pv_edge", "rho_edge",
@@ -41,4 +41,4 @@ def test_two_steps_match_reference(case):
         state = stepper.srk3_step(state, meta["dt"])
         ref = group(st, f"step{step}")
         for k in FIELDS:
-            assert rel_l2(state[k][:-1], ref[k][:-1]) <= 1e-12, (step, k)
+            assert rel_l2(state[k][:-1], ref[k][:-1]) <= step_tol(case, k), (step, k)
