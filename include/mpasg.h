@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define MPASG_ABI_VERSION 2
+#define MPASG_ABI_VERSION 3
 
 enum {
   MPASG_OK = 0,
@@ -109,6 +109,8 @@ typedef struct mpasg_mesh {
       *defc_a_f32, *defc_b_f32, *meshScalingDel2_f32, *meshScalingDel4_f32,
       *coeffs_reconstruct_f32, *zxu_f32, *zz_f32, *rdzw_f32, *rdzu_f32, *fzm_f32, *fzp_f32,
       *fnm_f32, *fnp_f32, *rdnw_f32;
+  /* interface heights (C+1, L+1): the vertical mixing options of the tendencies */
+  const double *zgrid;
 } mpasg_mesh;
 
 /* Namelist options the step consumes (validated on the host). */
@@ -126,6 +128,12 @@ typedef struct mpasg_config {
   int32_t precision;                /* MPASG_PRECISION_FLOAT64 or MPASG_PRECISION_MIXED */
   int32_t tile_tend_u;              /* levels per thread of the u tendency: 1 (0), 2 or 4
                                        (autotuned; tiles agree to one FMA rounding) */
+  /* mixing options of the large-step tendencies (dyn_tend.py:3367-3456, 2730-2780,
+   * 4612-4650, 5064-5100): 2d_fixed del2 coefficient (kdiff everywhere), vertical mixing
+   * of u and w / of theta (full state; 0 = off), CAM-style top-level damping (0 = off) */
+  double h_theta_eddy_visc2, v_mom_eddy_visc2, v_theta_eddy_visc2, mpas_cam_coef;
+  int32_t number_cam_damping_levels;
+  int32_t reserved0;
 } mpasg_config;
 
 /* Arithmetic of the step.  FLOAT64: every stage in float64 (the reference's arithmetic).

@@ -13,7 +13,7 @@ import pathlib
 from .errors import MpasConfigError, MpasDeviceError, MpasExtensionMissingError, MpasNumericalError
 
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "libmpasg.so"
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 MESH_INT_DIMS = ("nCells", "nEdges", "nVertices", "nVertLevels", "maxEdges", "maxEdges2",
                  "vertexDegree", "nAdvMax", "flatTerrain", "reserved0")
@@ -93,6 +93,9 @@ MESH_F32_PTRS = tuple(n + "_f32" for n in (
     "meshScalingDel2", "meshScalingDel4", "coeffs_reconstruct", "zxu", "zz", "rdzw", "rdzu", "fzm", "fzp", "fnm",
     "fnp", "rdnw"))
 
+# float64 arrays appended after the float32 copies
+MESH_TAIL_PTRS = ("zgrid",)
+
 
 STAGE_NAMES = ("begin", "setup", "moist", "vert_imp_coefs", "dyn_tend_rk1", "dyn_tend",
                "smlstep_pert", "acoustic_step", "divergence_damping", "recover", "diagnostics",
@@ -102,11 +105,16 @@ STAGE_NAMES = ("begin", "setup", "moist", "vert_imp_coefs", "dyn_tend_rk1", "dyn
 class MeshStruct(C.Structure):
     _fields_ = ([(n, C.c_int32) for n in MESH_INT_DIMS] + [(n, C.c_double) for n in MESH_DOUBLES]
                 + [(n, C.c_void_p) for n in MESH_INT_PTRS] + [(n, C.c_void_p) for n in MESH_DBL_PTRS]
-                + [(n, C.c_void_p) for n in MESH_F32_PTRS])
+                + [(n, C.c_void_p) for n in MESH_F32_PTRS] + [(n, C.c_void_p) for n in MESH_TAIL_PTRS])
+
+
+CONFIG_MIXING_DOUBLES = ("h_theta_eddy_visc2", "v_mom_eddy_visc2", "v_theta_eddy_visc2", "mpas_cam_coef")
+CONFIG_MIXING_INTS = ("number_cam_damping_levels", "reserved0")
 
 
 class ConfigStruct(C.Structure):
-    _fields_ = [(n, C.c_double) for n in CONFIG_DOUBLES] + [(n, C.c_int32) for n in CONFIG_INTS]
+    _fields_ = ([(n, C.c_double) for n in CONFIG_DOUBLES] + [(n, C.c_int32) for n in CONFIG_INTS]
+                + [(n, C.c_double) for n in CONFIG_MIXING_DOUBLES] + [(n, C.c_int32) for n in CONFIG_MIXING_INTS])
 
 
 class FieldsStruct(C.Structure):

@@ -32,7 +32,7 @@ DEFAULTS = {
     "config_h_mom_eddy_visc2": 0.0, "config_h_mom_eddy_visc4": 0.0,
     "config_v_mom_eddy_visc2": 0.0, "config_h_theta_eddy_visc2": 0.0,
     "config_h_theta_eddy_visc4": 0.0, "config_v_theta_eddy_visc2": 0.0,
-    "config_rayleigh_damp_u": False, "config_mpas_cam_coef": 0.0,
+    "config_rayleigh_damp_u": False, "config_mpas_cam_coef": 0.0, "config_number_cam_damping_levels": 4,
     "config_curvature_u": False, "config_mix_full": True, "config_IAU_option": "off",
     "config_apply_lbcs": False, "config_dt": 720.0,
     # GB300 extension (no reference counterpart): "float64" (the reference's arithmetic)
@@ -57,9 +57,6 @@ def validate_supported(cfg: Mapping[str, Any]) -> None:
         bad.append("config_split_dynamics_transport=False (coupled transport)")
     if int(cfg["config_time_integration_order"]) not in (2, 3):
         bad.append("config_time_integration_order")
-    for key in ("config_v_mom_eddy_visc2", "config_v_theta_eddy_visc2", "config_mpas_cam_coef"):
-        if float(cfg[key]) != 0.0:
-            bad.append(key)
     for key in ("config_rayleigh_damp_u", "config_curvature_u", "config_positive_definite",
                 "config_apply_lbcs"):
         if bool(cfg[key]):
@@ -68,7 +65,7 @@ def validate_supported(cfg: Mapping[str, Any]) -> None:
         bad.append("config_mix_full=False")
     if str(cfg["config_IAU_option"]) != "off":
         bad.append("config_IAU_option")
-    if str(cfg["config_horiz_mixing"]) not in ("2d_smagorinsky",):
+    if str(cfg["config_horiz_mixing"]) not in ("2d_smagorinsky", "2d_fixed"):
         bad.append("config_horiz_mixing")
     if str(cfg["config_precision"]) not in _lib.PRECISIONS:
         bad.append("config_precision")
@@ -110,6 +107,11 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
     c.moist_start = int(moist_start)
     c.moist_end = int(moist_end)
     c.precision = _lib.PRECISIONS[str(cfg["config_precision"])]
+    c.h_theta_eddy_visc2 = float(cfg["config_h_theta_eddy_visc2"])
+    c.v_mom_eddy_visc2 = float(cfg["config_v_mom_eddy_visc2"])
+    c.v_theta_eddy_visc2 = float(cfg["config_v_theta_eddy_visc2"])
+    c.mpas_cam_coef = float(cfg["config_mpas_cam_coef"])
+    c.number_cam_damping_levels = int(cfg["config_number_cam_damping_levels"])
     return c
 
 

@@ -4,7 +4,8 @@
 //   k_tend_cells_a   h_divergence (+ rk 1: Smagorinsky kdiff, tend_rho, dpdz)   sections :9925-9992
 //   k_tend_u         u tendency: vertical transport, PV flux, KE gradient, divergence
 //                    coupling (+ rk 1: pressure gradient and del2 mixing)        :9993-10315
-//   k_del4_vertex / k_del4_cell / k_tend_u_del4   del4 filter of u (rk 1)        :10075-10315
+//   k_del4_vertex / k_del4_cell / k_tend_u_finish   del4 filter and vertical mixing of u
+//                    (rk 1)                                                      :10075-10315
 //   k_mix_cells_a / k_mix_cells_b   w and theta del2 / del4 mixing (rk 1)       :10355, :10544
 //   k_adv_edges      horizontal advective fluxes of w and theta, once per edge    :10316, :10442
 //   k_tend_w_theta   w and theta flux divergence, vertical fluxes, buoyancy,
@@ -22,8 +23,18 @@ namespace {
 
 struct TendScalars {
   double inv_dt, c_s_len2, kdiff_cap, h_mom_visc4, h_theta_visc4, del4u_div, coef3, visc2;
+  double cam_base, v_mom, v_theta;  // CAM damping base, vertical mixing coefficients (0: off)
   int rk_step, smag, del4;
+  int ncam;   // CAM damping levels (0: off)
+  int defer;  // k_tend_u leaves tend_u_euler to k_tend_u_finish (del4 and / or vertical mixing)
 };
+
+// CAM-style damping of the top ncam levels (dyn_tend.py:3434-3456): kdiff raised to
+// base * (1 - (L - (k + 1)) / ncam), base = 4 * 2.0833 * len_disp * mpas_cam_coef
+MPASG_D double cam_kdiff(double kd, const TendScalars& p, uint32_t k, int L) {
+  const double factor = 1.0 - (double)(L - (int)(k + 1)) / (double)p.ncam;
+  return fmax(kd, p.cam_base * factor);
+}
 
 template <typename T>
 __global__ void k_tend_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendScalars p) {
@@ -63,9 +74,11 @@ __global__ void k_tend_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendSca
       dd = ndd;
       dof = ndo;
     }
-    f.kdiff[i] = f64(vmin(cv<T>(p.c_s_len2) * vsqrt(dd * dd + dof * dof), cv<T>(p.kdiff_cap)));
-  } else {
-    f.kdiff[i] = p.visc2;
+    double kd = f64(vmin(cv<T>(p.c_s_len2) * vsqrt(dd * dd + dof * dof), cv<T>(p.kdiff_cap)));
+    if (p.ncam > 0 && (int)k >= L - p.ncam) kd = cam_kdiff(kd, p, k, L);
+    f.kdiff[i] = kd;
+  } else {  // 2d_fixed: the theta del2 coefficient everywhere
+    f.kdiff[i] = (p.ncam > 0 && (int)k >= L - p.ncam) ? cam_kdiff(p.visc2, p, k, L) : p.visc2;
   }
 }
 
@@ -146,7 +159,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_u(mpasg_mesh m, mpasg_fields f,
     T kdiffu = T(0.5) * (cv<T>(f.kdiff[i1]) + cv<T>(f.kdiff[i2]));
     teu = teu + rho_e * kdiffu * u_diff * G(meshScalingDel2)[e];
     f.tend_u_euler[i] = f64(teu);
-    f.tend_u[i] = f64(p.del4 ? tu : tu + teu);
+    f.tend_u[i] = f64(p.defer ? tu : tu + teu);
   } else {
     f.tend_u[i] = f64(tu + cv<T>(f.tend_u_euler[i]));
   }
@@ -229,7 +242,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_u_chunk(mpasg_mesh m, mpasg_fie
       T kdiffu = T(0.5) * (cv<T>(f.kdiff[i1]) + cv<T>(f.kdiff[i2]));
       teu = teu + rho_e * kdiffu * u_diff * G(meshScalingDel2)[e];
       f.tend_u_euler[ie] = f64(teu);
-      f.tend_u[ie] = f64(p.del4 ? tu : tu + teu);
+      f.tend_u[ie] = f64(p.defer ? tu : tu + teu);
     } else {
       f.tend_u[ie] = f64(tu + cv<T>(f.tend_u_euler[ie]));
     }
@@ -277,23 +290,58 @@ __global__ void k_del4_cell(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   f.delsq_div[i] = f64(acc);
 }
 
+// rk 1 completion of the u tendency when k_tend_u deferred it: del4 filter (if enabled),
+// then vertical mixing of u (dyn_tend.py:2730-2780; full state, interior levels, heights
+// of the edge's interfaces as the mean of its two cells), then tend_u += tend_u_euler
 template <typename T>
-__global__ void k_tend_u_del4(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendScalars p) {
+__global__ void k_tend_u_finish(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendScalars p) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)m.nEdges * L) return;
   uint32_t e = fl.div(i), k = i - e * L;
   const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-  const int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
-  const T inv_dc = G(invDcEdge)[e];
-  T u_mix = G(meshScalingDel4)[e] * cv<T>(p.h_mom_visc4);
-  T r_dc4 = u_mix * cv<T>(p.del4u_div) * inv_dc;
-  T r_dv4 = u_mix * vmin(G(invDvEdge)[e], T(4) * inv_dc);
-  T u_diff4 = (cv<T>(f.delsq_div[(size_t)c2 * L + k]) - cv<T>(f.delsq_div[(size_t)c1 * L + k])) * r_dc4 -
-              (cv<T>(f.delsq_vort[(size_t)v2 * L + k]) - cv<T>(f.delsq_vort[(size_t)v1 * L + k])) * r_dv4;
-  T teu = cv<T>(f.tend_u_euler[i]) - cv<T>(f.h_edge[i]) * u_diff4;
+  T teu = cv<T>(f.tend_u_euler[i]);
+  if (p.del4) {
+    const int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
+    const T inv_dc = G(invDcEdge)[e];
+    T u_mix = G(meshScalingDel4)[e] * cv<T>(p.h_mom_visc4);
+    T r_dc4 = u_mix * cv<T>(p.del4u_div) * inv_dc;
+    T r_dv4 = u_mix * vmin(G(invDvEdge)[e], T(4) * inv_dc);
+    T u_diff4 = (cv<T>(f.delsq_div[(size_t)c2 * L + k]) - cv<T>(f.delsq_div[(size_t)c1 * L + k])) * r_dc4 -
+                (cv<T>(f.delsq_vort[(size_t)v2 * L + k]) - cv<T>(f.delsq_vort[(size_t)v1 * L + k])) * r_dv4;
+    teu = teu - cv<T>(f.h_edge[i]) * u_diff4;
+  }
+  if (p.v_mom > 0.0 && k >= 1 && k + 1 < (uint32_t)L) {
+    const double* z1p = m.zgrid + (size_t)c1 * (L + 1);
+    const double* z2p = m.zgrid + (size_t)c2 * (L + 1);
+    const double za = 0.5 * (z1p[k - 1] + z2p[k - 1]), zb = 0.5 * (z1p[k] + z2p[k]);
+    const double zc = 0.5 * (z1p[k + 1] + z2p[k + 1]), zd = 0.5 * (z1p[k + 2] + z2p[k + 2]);
+    const double zm = 0.5 * (za + zb), z0 = 0.5 * (zb + zc), zp = 0.5 * (zc + zd);
+    const double* u = f.u + (size_t)e * L;
+    const T d_up = dif<T>(u[k + 1], u[k]) / cv<T>(zp - z0);
+    const T d_dn = dif<T>(u[k], u[k - 1]) / cv<T>(z0 - zm);
+    teu = teu + cv<T>(f.h_edge[i]) * cv<T>(p.v_mom) * (d_up - d_dn) / cv<T>(0.5 * (zp - zm));
+  }
   f.tend_u_euler[i] = f64(teu);
   f.tend_u[i] = f64(cv<T>(f.tend_u[i]) + teu);
+}
+
+// vertical mixing of w at interface k, 1 <= k <= L-1 (dyn_tend.py:4636-4648, rk 1)
+MPASG_D double w_vmix(const mpasg_mesh& m, const mpasg_fields& f, size_t oc, size_t ow, uint32_t k, double v) {
+  const double rho_half = 0.5 * (f.rho_zz[oc + k] + f.rho_zz[oc + k - 1]);
+  const double w_up = (f.w[ow + k + 1] - f.w[ow + k]) * m.rdzw[k];
+  const double w_down = (f.w[ow + k] - f.w[ow + k - 1]) * m.rdzw[k - 1];
+  return v * rho_half * (w_up - w_down) * m.rdzu[k];
+}
+
+// vertical mixing of theta at level k, 1 <= k <= L-2 (dyn_tend.py:5064-5100, rk 1;
+// Prandtl factor 1)
+MPASG_D double theta_vmix(const mpasg_mesh& m, const mpasg_fields& f, uint32_t c, uint32_t k, int L, double v) {
+  const double* zg = m.zgrid + (size_t)c * (L + 1);
+  const double zm = 0.5 * (zg[k - 1] + zg[k]), z0 = 0.5 * (zg[k] + zg[k + 1]), zp = 0.5 * (zg[k + 1] + zg[k + 2]);
+  const double* th = f.theta_m + (size_t)c * L;
+  const double diff = (th[k + 1] - th[k]) / (zp - z0) - (th[k] - th[k - 1]) / (z0 - zm);
+  return v * 1.0 * f.rho_zz[(size_t)c * L + k] * diff / (0.5 * (zp - zm));
 }
 
 // w / theta del2 mixing and the del2 fields for del4 (rk 1); index space (C, L+1)
@@ -508,6 +556,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta(mpasg_mesh m, mpasg_fie
       const double res = m.rdzu[k] * (f.pressure_p[oc + k] - f.pressure_p[oc + k - 1]) -
                          (m.fzm[k] * f.dpdz[oc + k] + m.fzp[k] * f.dpdz[oc + k - 1]);
       teu = teu - f.cqw[ow + k] * res;
+      if (p.v_mom > 0.0) teu = teu + w_vmix(m, f, oc, ow, k, p.v_mom);
       f.tend_w_euler[i] = teu;
     }
     f.tend_w[i] = tw + teu;
@@ -538,7 +587,12 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta(mpasg_mesh m, mpasg_fie
     // unfused: the difference cancels strongly (as rounded by the reference)
     f.rthdynten[o] = sub_rn(tt, mul_rn(f.tend_rho[o], f.theta_m[o])) / rz;
     tt = tt + rz * rtd;
-    tt = tt + f.tend_theta_euler[o];
+    double tte = f.tend_theta_euler[o];
+    if (p.rk_step == 1 && p.v_theta > 0.0 && k >= 1 && k + 1 < (uint32_t)L) {
+      tte = tte + theta_vmix(m, f, c, k, L, p.v_theta);
+      f.tend_theta_euler[o] = tte;
+    }
+    tt = tt + tte;
     f.tend_theta[o] = tt;
   }
 }
@@ -633,6 +687,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
       const double res = m.rdzu[k] * (f.pressure_p[oc + k] - f.pressure_p[oc + k - 1]) -
                          (m.fzm[k] * f.dpdz[oc + k] + m.fzp[k] * f.dpdz[oc + k - 1]);
       teu = teu - cv<T>(f.cqw[ow + k]) * cv<T>(res);
+      if (p.v_mom > 0.0) teu = teu + cv<T>(w_vmix(m, f, oc, ow, k, p.v_mom));
       f.tend_w_euler[i] = f64(teu);
     }
     f.tend_w[i] = f64(tw + teu);
@@ -672,7 +727,12 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
     // (a diagnostic for physics coupling: the cancelling difference in float64, the
     // quotient in float32)
     f.rthdynten[o] = f64(cv<T>(ttot - f.tend_rho[o] * f.theta_m[o]) / cv<T>(rz));
-    f.tend_theta[o] = ttot + rz * f.rt_diabatic_tend[o] + f.tend_theta_euler[o];
+    double tte = f.tend_theta_euler[o];
+    if (p.rk_step == 1 && p.v_theta > 0.0 && k >= 1 && k + 1 < (uint32_t)L) {
+      tte = tte + theta_vmix(m, f, c, k, L, p.v_theta);
+      f.tend_theta_euler[o] = tte;
+    }
+    f.tend_theta[o] = ttot + rz * f.rt_diabatic_tend[o] + tte;
   }
 }
 
@@ -709,7 +769,9 @@ int launch_dyn_tend(const mpasg_mesh* m, mpasg_fields* f, const TendScalars& p, 
       MPASG_LAUNCH_CHECK();
       k_del4_cell<T><<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl);
       MPASG_LAUNCH_CHECK();
-      k_tend_u_del4<T><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, p);
+    }
+    if (p.defer) {
+      k_tend_u_finish<T><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, p);
       MPASG_LAUNCH_CHECK();
     }
     k_mix_cells_a<T><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, fl1);
@@ -763,11 +825,20 @@ int mpasgi_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
     p.h_mom_visc4 = c->h_mom_eddy_visc4;
     p.h_theta_visc4 = c->h_theta_eddy_visc4;
   }
-  p.visc2 = 0.0;
+  p.visc2 = p.smag ? 0.0 : c->h_theta_eddy_visc2;
   p.del4u_div = c->del4u_div_factor;
   p.coef3 = c->coef_3rd_order;
   p.rk_step = rk_step;
   p.del4 = (p.h_mom_visc4 > 0.0) ? 1 : 0;
+  if (c->number_cam_damping_levels > m->nVertLevels) return MPASG_E_ARG;
+  p.ncam = (c->mpas_cam_coef > 0.0 && c->number_cam_damping_levels > 0) ? c->number_cam_damping_levels : 0;
+  p.cam_base = 4.0 * 2.0833 * c->len_disp * c->mpas_cam_coef;
+  p.v_mom = c->v_mom_eddy_visc2 > 0.0 ? c->v_mom_eddy_visc2 : 0.0;
+  p.v_theta = c->v_theta_eddy_visc2 > 0.0 ? c->v_theta_eddy_visc2 : 0.0;
+  p.defer = (p.del4 || p.v_mom > 0.0) ? 1 : 0;
+  if (p.v_mom > 0.0 || p.v_theta > 0.0) {
+    if (!m->zgrid) return MPASG_E_ARG;
+  }
   if (c->precision == MPASG_PRECISION_MIXED) {
     if (!copies_current) {
       const int rc = mpasgi_pack_f32(m, f, s);

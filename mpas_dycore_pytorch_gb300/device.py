@@ -113,6 +113,10 @@ class DeviceMesh:
             t = torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
             self._keep[n] = t
             setattr(st, n, t.data_ptr())
+        for n in _lib.MESH_TAIL_PTRS:
+            if n not in ref:
+                raise MpasConfigError(f"mesh is missing {n}")
+            dbls[n] = np.ascontiguousarray(_np(ref[n])[:, :nl + 1], dtype=np.float64)
         for n, a in dbls.items():
             t = torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
             self._keep[n] = t

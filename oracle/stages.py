@@ -592,6 +592,13 @@ def dyn_tend(a):
                 d_off = np.where(valid[:, None], do, d_off)
             kdiff[:nc] = np.minimum((c_s * len_disp) ** 2 * np.sqrt(d_diag ** 2 + d_off ** 2),
                                     (0.01 * len_disp ** 2) * inv_dt)
+        else:  # 2d_fixed: the theta coefficient everywhere (dyn_tend.py:3420-3427)
+            kdiff[:nc] = _f(a, "config_h_theta_eddy_visc2")
+        cam, ncam = _f(a, "config_mpas_cam_coef"), _i(a, "config_number_cam_damping_levels")
+        if cam > 0.0 and ncam > 0:  # CAM-style top-level damping (dyn_tend.py:3434-3456)
+            base = 4.0 * 2.0833 * len_disp * cam
+            for k in range(nl - ncam, nl):
+                kdiff[:nc, k] = np.maximum(kdiff[:nc, k], base * (1.0 - float(nl - (k + 1)) / float(ncam)))
     else:
         kdiff = kdiff_in
 
@@ -674,6 +681,16 @@ def dyn_tend(a):
             r_dv4 = (u_mix * np.minimum(inv_dv[:ne], 4.0 * inv_dc[:ne]))[:, None]
             u_diff4 = (dsd[e2] - dsd[e1]) * r_dc4 - (dsv[v2] - dsv[v1]) * r_dv4
             tend_u_euler[:ne] = tend_u_euler[:ne] - rho_edge[:ne] * u_diff4
+        v_mom = _f(a, "config_v_mom_eddy_visc2")
+        if v_mom > 0.0 and nl > 2:  # vertical mixing of u (dyn_tend.py:2730-2780), full state
+            zg = a["zgrid"]
+            zi = lambda k0, k1: 0.5 * (zg[e1, k0:k1] + zg[e2, k0:k1])
+            z1, z2, z3, z4 = zi(0, nl - 2), zi(1, nl - 1), zi(2, nl), zi(3, nl + 1)
+            zm, z0, zp = 0.5 * (z1 + z2), 0.5 * (z2 + z3), 0.5 * (z3 + z4)
+            uu = u[:ne]
+            tend_u_euler[:ne, 1:nl - 1] = tend_u_euler[:ne, 1:nl - 1] + rho_edge[:ne, 1:nl - 1] * v_mom * (
+                (uu[:, 2:nl] - uu[:, 1:nl - 1]) / (zp - z0) - (uu[:, 1:nl - 1] - uu[:, :nl - 2]) / (z0 - zm)
+            ) / (0.5 * (zp - zm))
     tend_u = zpad(tend_u + tend_u_euler[:ne])
 
     # ---- w tendency ----
@@ -724,6 +741,13 @@ def dyn_tend(a):
         tend_w_euler[:nc, 1:nl] = tend_w_euler[:nc, 1:nl] - cqw[:nc, 1:nl] * (
             rdzu[None, 1:] * (pp[:nc, 1:] - pp[:nc, :nl - 1])
             - (fzm[None, 1:] * dpdz[:nc, 1:] + fzp[None, 1:] * dpdz[:nc, :nl - 1]))
+        v_mom = _f(a, "config_v_mom_eddy_visc2")
+        if v_mom > 0.0:  # vertical mixing of w (dyn_tend.py:4636-4648)
+            rz = a["rho_zz"][:nc]
+            rho_half = 0.5 * (rz[:, 1:nl] + rz[:, :nl - 1])
+            w_up = (wc[:, 2:nl + 1] - wc[:, 1:nl]) * rdzw[1:nl]
+            w_down = (wc[:, 1:nl] - wc[:, :nl - 1]) * rdzw[:nl - 1]
+            tend_w_euler[:nc, 1:nl] = tend_w_euler[:nc, 1:nl] + v_mom * rho_half * (w_up - w_down) * rdzu[1:nl]
     tw[:, 1:nl] = tw[:, 1:nl] + tend_w_euler[:nc, 1:nl]
     tend_w = zpad(tw)
 
@@ -763,6 +787,15 @@ def dyn_tend(a):
                               * dv[e] * sign[:, j] * inv_dc[e], 0.0)[:, None]
                 c1, c2 = e1[e], e2[e]
                 tend_theta_euler[:nc] = tend_theta_euler[:nc] - es * (delsq_t[c2] - delsq_t[c1])
+        v_th = _f(a, "config_v_theta_eddy_visc2")
+        if v_th > 0.0 and nl > 2:  # vertical mixing of theta (dyn_tend.py:5064-5100), full state
+            zg = a["zgrid"][:nc]
+            z1, z2, z3, z4 = zg[:, 0:nl - 2], zg[:, 1:nl - 1], zg[:, 2:nl], zg[:, 3:nl + 1]
+            zm, z0, zp = 0.5 * (z1 + z2), 0.5 * (z2 + z3), 0.5 * (z3 + z4)
+            th = theta_m[:nc]
+            diff = (th[:, 2:nl] - th[:, 1:nl - 1]) / (zp - z0) - (th[:, 1:nl - 1] - th[:, :nl - 2]) / (z0 - zm)
+            tend_theta_euler[:nc, 1:nl - 1] = tend_theta_euler[:nc, 1:nl - 1] + \
+                v_th * prandtl_inv * a["rho_zz"][:nc, 1:nl - 1] * diff / (0.5 * (zp - zm))
     else:
         tend_theta_euler = a["tend_theta_euler_in"].copy()
     th = theta_m[:nc]

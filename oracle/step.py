@@ -204,6 +204,11 @@ class Stepper:
                     "config_h_mom_eddy_visc4": float(self.cfg.get("config_h_mom_eddy_visc4", 0.0)),
                     "config_h_theta_eddy_visc4": float(self.cfg.get("config_h_theta_eddy_visc4", 0.0)),
                     "config_visc4_2dsmag": float(self.cfg.get("config_visc4_2dsmag", 0.05)),
+                    "config_h_theta_eddy_visc2": float(self.cfg.get("config_h_theta_eddy_visc2", 0.0)),
+                    "config_v_mom_eddy_visc2": float(self.cfg.get("config_v_mom_eddy_visc2", 0.0)),
+                    "config_v_theta_eddy_visc2": float(self.cfg.get("config_v_theta_eddy_visc2", 0.0)),
+                    "config_mpas_cam_coef": float(self.cfg.get("config_mpas_cam_coef", 0.0)),
+                    "config_number_cam_damping_levels": int(self.cfg.get("config_number_cam_damping_levels", 4)),
                     "config_len_disp": self.len_disp,
                     "u": st["u"], "v": st["v"], "w": st["w"], "ru": st["ru"], "rw": st["rw"],
                     "ru_save": save["ru_save"], "rw_save": save["rw_save"],

@@ -71,10 +71,22 @@ CASES = {
     "g2_moist": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=2, n_bumps=6, n_tracers=1,
                                qv_surface=0.012),
                      config=dict(config_monotonic=True), dt=1200.0, nsteps=2),
-    # second-order Runge-Kutta (config_time_integration_order = 2), three acoustic substeps
+    # second-order Runge-Kutta (config_time_integration_order = 2), four acoustic substeps
     "g2_rk2": dict(spec=dict(level=2, nlev=12, seed=3, n_bumps=6, n_tracers=2),
                    config=dict(config_monotonic=False, config_time_integration_order=2,
                                config_number_of_sub_steps=4), dt=900.0, nsteps=2),
+    # fixed-coefficient horizontal mixing (del2 and del4) with vertical mixing of u, w, theta
+    "g2_fixed": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=4, n_bumps=6, n_tracers=1,
+                               w_sine=0.05),
+                     config=dict(config_monotonic=True, config_horiz_mixing="2d_fixed",
+                                 config_h_mom_eddy_visc4=1.0e10, config_h_theta_eddy_visc4=5.0e9,
+                                 config_h_theta_eddy_visc2=2.0e4, config_v_mom_eddy_visc2=1.0,
+                                 config_v_theta_eddy_visc2=1.0), dt=1200.0, nsteps=2),
+    # CAM-style second-order damping in the top levels with full APVM upwinding
+    "g2_cam": dict(spec=dict(level=2, nlev=12, seed=5, n_bumps=6, n_tracers=1),
+                   config=dict(config_monotonic=False, config_mpas_cam_coef=1.0,
+                               config_number_cam_damping_levels=4,
+                               config_apvm_upwinding=1.0), dt=1200.0, nsteps=2),
 }
 
 BASE_CONFIG = {

@@ -93,3 +93,29 @@ def test_mixed_form_within_stated_error_after_24_steps():
     assert not bad, bad
     # the mixed form really differs from the float64 form (float32 arithmetic ran)
     assert max(worst.values()) > 1e-12
+
+
+@pytest.mark.parametrize("options", [
+    {"config_horiz_mixing": "2d_fixed", "config_h_mom_eddy_visc4": 1.0e10, "config_h_theta_eddy_visc4": 5.0e9,
+     "config_h_theta_eddy_visc2": 2.0e4, "config_v_mom_eddy_visc2": 1.0, "config_v_theta_eddy_visc2": 1.0},
+    {"config_mpas_cam_coef": 1.0, "config_number_cam_damping_levels": 4, "config_apvm_upwinding": 1.0},
+], ids=["fixed_vertical_mixing", "cam_damping"])
+def test_mixed_form_with_mixing_options(options):
+    """The mixing options (2d_fixed, vertical mixing, CAM damping) in the mixed form stay
+    within the stated error of the float64 form (6 steps on the level-4 mesh)."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    spec = CaseSpec(level=4, nlev=26, seed=4, n_bumps=8, n_tracers=1, w_sine=0.05)
+    cfg = {"config_time_integration_order": 3, "config_len_disp": 240000.0, "config_number_of_sub_steps": 2,
+           "config_dynamics_split_steps": 3, "config_monotonic": True, "config_dt": 1200.0}
+    cfg.update(options)
+    ref = _run(spec, cfg, 1200.0, "float64", 6)
+    got = _run(spec, cfg, 1200.0, "mixed", 6)
+    worst = {}
+    for k, r in ref.items():
+        den = np.linalg.norm(r.ravel())
+        if den > 0.0:
+            worst[k] = float(np.linalg.norm((got[k] - r).ravel()) / den)
+    bad = {k: v for k, v in worst.items() if v > MIXED_TOL}
+    assert not bad, bad
+    assert max(worst.values()) > 1e-12

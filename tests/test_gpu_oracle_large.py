@@ -14,22 +14,30 @@ CFG0 = {"config_time_integration_order": 3, "config_len_disp": 120000.0, "config
         "config_dt": 1800.0}
 
 
-def _case(level, nlev, ntr, mono, seed=0, dz=None):
+OPTIONS = {"config_horiz_mixing": "2d_fixed", "config_h_mom_eddy_visc4": 1.0e10,
+           "config_h_theta_eddy_visc4": 5.0e9, "config_h_theta_eddy_visc2": 2.0e4,
+           "config_v_mom_eddy_visc2": 1.0, "config_v_theta_eddy_visc2": 1.0,
+           "config_mpas_cam_coef": 1.0, "config_apvm_upwinding": 1.0}
+
+
+def _case(level, nlev, ntr, mono, seed=0, dz=None, options=None):
     from mpas_dycore_pytorch_gb300.cases import CaseSpec
     from mpas_dycore_pytorch_gb300.loader import load_case
     cfg = dict(CFG0)
     cfg["config_monotonic"] = mono
+    cfg.update(options or {})
     spec = CaseSpec(level=level, nlev=nlev, seed=seed, n_bumps=8, n_tracers=ntr, dz_bottom=dz)
     st, _ = load_case(spec, cfg, as_torch=False)
     return st, cfg
 
 
-@pytest.mark.parametrize("mono", [False, True])
-def test_level4_two_steps_vs_oracle(mono):
+@pytest.mark.parametrize("mono,options", [(False, None), (True, None), (True, OPTIONS)],
+                         ids=["explicit", "monotone", "monotone_mixing_options"])
+def test_level4_two_steps_vs_oracle(mono, options):
     need_gpu()
     from mpas_dycore_pytorch_gb300.api import Model
     from oracle.step import Stepper
-    st, cfg = _case(4, 26, 3 if mono else 1, mono)
+    st, cfg = _case(4, 26, 3 if mono else 1, mono, options=options)
     model = Model(st, cfg, 1800.0, num_scalars=st["scalars"].shape[-1])
     model.prepare(st)
     ref = Stepper(st, cfg)
