@@ -53,8 +53,8 @@ def validate_supported(cfg: Mapping[str, Any]) -> None:
     """Reject options outside the implemented path before any device work (mirrors the
     reference's capability rejection, tests/test_configuration_contracts.py:48-79)."""
     bad = []
-    if not bool(cfg["config_split_dynamics_transport"]):
-        bad.append("config_split_dynamics_transport=False (coupled transport)")
+    if int(cfg["config_dynamics_split_steps"]) < 1:
+        bad.append("config_dynamics_split_steps < 1")
     if int(cfg["config_time_integration_order"]) not in (2, 3):
         bad.append("config_time_integration_order")
     for key in ("config_rayleigh_damp_u", "config_curvature_u", "config_positive_definite",
@@ -100,7 +100,9 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
     c.h_theta_eddy_visc4 = float(cfg["config_h_theta_eddy_visc4"])
     c.time_integration_order = int(cfg["config_time_integration_order"])
     c.number_of_sub_steps = int(cfg["config_number_of_sub_steps"])
-    c.dynamics_split_steps = int(cfg["config_dynamics_split_steps"])
+    # split transport off is one dynamics substep with the scalars inside the RK stages
+    # (the reference's _resolve_dynamics_split, time_integration.py:1809-1878)
+    c.dynamics_split_steps = int(cfg["config_dynamics_split_steps"]) if bool(cfg["config_split_dynamics_transport"]) else 1
     c.monotonic = 1 if bool(cfg["config_monotonic"]) else 0
     c.horiz_mixing_smagorinsky = 1 if str(cfg["config_horiz_mixing"]) == "2d_smagorinsky" else 0
     c.num_scalars = int(num_scalars)

@@ -189,6 +189,19 @@ extern "C" int mpasg_step_timed(const mpasg_mesh* m, const mpasg_config* c, mpas
 }
 
 namespace {
+// One transport RK stage, scalars_init and scalars_a -> scalars_b, then a and b swap:
+// monotone at the last stage when config_monotonic, else explicit.
+int transport_stage(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk, double dt_stage,
+                    cudaStream_t s) {
+  const int rc = (rk == 3 && c->monotonic) ? mpasg_advance_scalars_mono(m, c, f, dt_stage, (void*)s)
+                                           : mpasg_advance_scalars(m, c, f, rk, dt_stage, (void*)s);
+  if (rc != MPASG_OK) return rc;
+  double* t = f->scalars_a;
+  f->scalars_a = f->scalars_b;
+  f->scalars_b = t;
+  return MPASG_OK;
+}
+
 int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec) {
   void* stream = (void*)s;
 #define MARK(kind)                                  \
@@ -203,6 +216,9 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   const long long ncl = (nc + 1) * L, nel = (ne + 1) * L, ncw = (nc + 1) * (L + 1);
   const long long ncs = (nc + 1) * L * S;
   const int split = c->dynamics_split_steps;
+  // one dynamics substep is the coupled mode: the scalars advance inside every RK stage
+  // (after recovery, before the diagnostics), not in a transport loop after the substeps
+  const bool coupled = split == 1;
   const int ns = c->number_of_sub_steps;
   const double dt = c->dt;
   const double dt_dyn = dt / split;
@@ -229,6 +245,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   CHECK_RC(copy(f.rr_save, f.rho_p, ncl, s));
   CHECK_RC(copy(f.rho_zz_old_split, f.rho_zz, ncl, s));
   if (S > 0) CHECK_RC(copy(f.scalars_init, f.scalars, ncs, s));
+  if (S > 0 && coupled) CHECK_RC(copy(f.scalars_a, f.scalars_init, ncs, s));
   if (c->precision == MPASG_PRECISION_MIXED) CHECK_RC(mpasgi_pack_f32(m, &f, s));
   MARK(MPASG_STAGE_SETUP);
   CHECK_RC(mpasg_moist_coefficients(m, c, &f, stream));
@@ -254,6 +271,10 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
       }
       CHECK_RC(mpasg_recover_large_step(m, c, &f, rk, nsub[rk - 1], rk_ts[rk - 1], stream));
       MARK(MPASG_STAGE_RECOVER);
+      if (coupled && S > 0) {  // time_integration.py:7890-8200: stage dt, this stage's mass fluxes
+        CHECK_RC(transport_stage(m, c, &f, rk, rk_ts[rk - 1], s));
+        MARK(rk == 3 && c->monotonic ? MPASG_STAGE_SCALARS_MONO : MPASG_STAGE_SCALARS);
+      }
       CHECK_RC(mpasgi_solve_diagnostics(m, c, &f, rk, s, true));
       MARK(MPASG_STAGE_DIAG);
     }
@@ -285,25 +306,17 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   MPASG_LAUNCH_CHECK();
 
   // ---- split transport RK3 with the substep-averaged mass fluxes
-  if (S > 0) {
+  if (S > 0 && !coupled) {
     CHECK_RC(copy(f.scalars_a, f.scalars_init, ncs, s));
     // transport stage dts; the first is dt/2 for RK2 (time_integration.py:3366-3370)
     const double dts_t[3] = {c->time_integration_order == 2 ? dt / 2.0 : dt / 3.0, dt / 2.0, dt};
     MARK(MPASG_STAGE_SPLIT);
     for (int rk = 1; rk <= 3; ++rk) {
-      if (rk == 3 && c->monotonic) {
-        CHECK_RC(mpasg_advance_scalars_mono(m, c, &f, dts_t[rk - 1], stream));
-        MARK(MPASG_STAGE_SCALARS_MONO);
-      } else {
-        CHECK_RC(mpasg_advance_scalars(m, c, &f, rk, dts_t[rk - 1], stream));
-        MARK(MPASG_STAGE_SCALARS);
-      }
-      double* t = f.scalars_a;
-      f.scalars_a = f.scalars_b;
-      f.scalars_b = t;
+      CHECK_RC(transport_stage(m, c, &f, rk, dts_t[rk - 1], s));
+      MARK(rk == 3 && c->monotonic ? MPASG_STAGE_SCALARS_MONO : MPASG_STAGE_SCALARS);
     }
-    CHECK_RC(copy(f.scalars, f.scalars_a, ncs, s));
   }
+  if (S > 0) CHECK_RC(copy(f.scalars, f.scalars_a, ncs, s));
   MARK(MPASG_STAGE_SPLIT);
   CHECK_RC(mpasgi_reconstruct(m, c, &f, s, true));
   MARK(MPASG_STAGE_RECONSTRUCT);

@@ -373,8 +373,10 @@ int launch_scalars(const mpasg_mesh* m, const mpasg_config* c, const mpasg_field
   g.hflux = hflux;
   k_pattern_c<T><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, fl, S, g.ruAvg, g.scalars_a, hflux, 0);
   MPASG_LAUNCH_CHECK();
+  // density weights: advanced with the stage in the split transport loop; the stage's
+  // new density in the coupled mode (one dynamics substep, time_integration.py:7930-8200)
   double w_old, w_new;
-  time_weights(1, rk_step, c->time_integration_order, &w_old, &w_new);
+  time_weights(c->dynamics_split_steps > 1 ? 1 : 0, rk_step, c->time_integration_order, &w_old, &w_new);
   k_scalars_update<T><<<nblocks((long long)m->nCells * L), kBlock, kBlock * S * sizeof(T), s>>>(
       *m, g, fl, S, dt_stage, w_old, w_new, c->coef_3rd_order, g.scalars_init, g.scalars_a, g.scalars_b);
   MPASG_LAUNCH_CHECK();

@@ -18,7 +18,7 @@ import numpy as np
 
 from . import stages as S
 
-__all__ = ["Stepper", "rk_weights", "STAGE_NAMES"]
+__all__ = ["Stepper", "rk_weights", "STAGE_NAMES", "COUPLED_STAGE_NAMES", "stage_names"]
 
 RVORD = 461.6 / 287.0
 
@@ -35,6 +35,16 @@ STAGE_NAMES = {
     "scalars_mono": "mpas.monotonic_scalar_transport_advance_scalars_mono_transport",
     "reconstruct": "mpas.vector_reconstruction",
 }
+# the transport stages as the coupled mode calls them (inside the RK stages)
+COUPLED_STAGE_NAMES = {
+    "scalars": "mpas.explicit_scalar_transport_advance_scalars",
+    "scalars_mono": "mpas.monotonic_scalar_transport_advance_scalars_mono",
+}
+
+
+def stage_names(key):
+    """Every reference stage name under which ``key`` is called (split and coupled modes)."""
+    return [STAGE_NAMES[key]] + ([COUPLED_STAGE_NAMES[key]] if key in COUPLED_STAGE_NAMES else [])
 
 
 def rk_weights(dt, ns, order):
@@ -72,7 +82,12 @@ class Stepper:
                      "maxEdges2": int(m["maxEdges2"]), "vertexDegree": int(m["vertexDegree"])}
         self.order = int(self.cfg.get("config_time_integration_order", 3))
         self.ns = int(self.cfg.get("config_number_of_sub_steps", 2))
+        # dynamics substeps per step; split transport off (or one substep) is the coupled
+        # mode: scalars advance inside every RK stage (time_integration.py:1809-1878, 7890-7960)
         self.split = int(self.cfg.get("config_dynamics_split_steps", 3))
+        if not bool(self.cfg.get("config_split_dynamics_transport", True)):
+            self.split = 1
+        self.coupled = self.split == 1
         self.epssm = float(self.cfg.get("config_epssm", 0.1))
         self.smdiv = float(self.cfg.get("config_smdiv", 0.1))
         self.len_disp = float(self.cfg.get("config_len_disp", 0.0))
@@ -92,7 +107,8 @@ class Stepper:
         a.update(args)
         out = fn(a)
         if self.on_stage is not None:
-            self.on_stage(STAGE_NAMES[key], a, out)
+            name = COUPLED_STAGE_NAMES[key] if self.coupled and key in COUPLED_STAGE_NAMES else STAGE_NAMES[key]
+            self.on_stage(name, a, out)
         return out
 
     # ------------------------------------------------------------------ prepare
@@ -262,6 +278,10 @@ class Stepper:
                 if rk == 3:
                     st["exner"] = rec["exner"]
                     st["pressure_p"] = rec["pressure_p"]
+                if self.coupled and scalars_init.shape[2] > 0:
+                    st["scalars"] = self._transport_stage(rk, rk_ts[rk - 1], work["ruAvg"], work["wwAvg"],
+                                                          scalars_init, st["scalars"], rho_zz_old_split,
+                                                          st["rho_zz"], advance_density=0)
                 d = self._call("diag", S.solve_diagnostics, {
                     "u": st["u"], "h": st["rho_zz"], "v_in": st["v"], "rk_step": rk, "dt": dt,
                     "config_apvm_upwinding": self.apvm})
@@ -282,30 +302,33 @@ class Stepper:
         st["ruAvg"] = ru_avg
         st["wwAvg"] = ww_avg
 
-        # split transport RK3 with the substep-averaged mass fluxes
-        scalars_new = scalars_init.copy()
-        hfa = np.zeros((ne + 1, nl, scalars_init.shape[2]))
-        tsave = np.zeros_like(scalars_init)
-        for rk in range(1, 4):
-            # transport stage dts; the first is dt/2 for RK2 (time_integration.py:3366-3370)
-            dt_t = [dt / 2.0 if self.order == 2 else dt / 3.0, dt / 2.0, dt][rk - 1]
-            if rk == 3 and self.monotonic:
-                out = self._call("scalars_mono", S.advance_scalars_mono, {
-                    "dt": dt_t, "coef_3rd_order": self.coef3, "uhAvg": ru_avg, "wwAvg": ww_avg,
-                    "rho_zz_old": rho_zz_old_split, "rho_zz_new": st["rho_zz"],
-                    "scalars_old": scalars_init, "scalars_new": scalars_new,
-                    "scalar_tend": np.zeros_like(scalars_init)})
-                scalars_new = out["scalars_new"]
-            else:
-                out = self._call("scalars", S.advance_scalars, {
-                    "rk_step": rk, "dt": dt_t, "coef_3rd_order": self.coef3,
-                    "config_time_integration_order": self.order, "advance_density": 1,
-                    "do_physics": False, "scalar_old": scalars_init, "scalar_new": scalars_new,
-                    "scalar_tend_save": tsave, "rho_zz_old": rho_zz_old_split,
-                    "rho_zz_new": st["rho_zz"], "uhAvg": ru_avg, "wwAvg": ww_avg,
-                    "horiz_flux_arr": hfa})
-                scalars_new = out["scalar_new"]
-                hfa = out["horiz_flux_arr"]
-        st["scalars"] = scalars_new
+        if not self.coupled:
+            # split transport RK3 with the substep-averaged mass fluxes
+            scalars_new = scalars_init.copy()
+            for rk in range(1, 4):
+                # transport stage dts; the first is dt/2 for RK2 (time_integration.py:3366-3370)
+                dt_t = [dt / 2.0 if self.order == 2 else dt / 3.0, dt / 2.0, dt][rk - 1]
+                scalars_new = self._transport_stage(rk, dt_t, ru_avg, ww_avg, scalars_init, scalars_new,
+                                                    rho_zz_old_split, st["rho_zz"], advance_density=1)
+            st["scalars"] = scalars_new
         st.update(self._call("reconstruct", S.reconstruct_2d, {"u": st["u"]}))
         return st
+
+    def _transport_stage(self, rk, dt_t, uh, ww, scalars_old, scalars_new, rho_old, rho_new, advance_density):
+        """One transport RK stage: monotone at the last stage when config_monotonic, else
+        explicit (time_integration.py:3954-4700 split, :7930-8200 coupled)."""
+        if rk == 3 and self.monotonic:
+            out = self._call("scalars_mono", S.advance_scalars_mono, {
+                "dt": dt_t, "coef_3rd_order": self.coef3, "uhAvg": uh, "wwAvg": ww,
+                "rho_zz_old": rho_old, "rho_zz_new": rho_new,
+                "scalars_old": scalars_old, "scalars_new": scalars_new,
+                "scalar_tend": np.zeros_like(scalars_old)})
+            return out["scalars_new"]
+        out = self._call("scalars", S.advance_scalars, {
+            "rk_step": rk, "dt": dt_t, "coef_3rd_order": self.coef3,
+            "config_time_integration_order": self.order, "advance_density": advance_density,
+            "do_physics": False, "scalar_old": scalars_old, "scalar_new": scalars_new,
+            "scalar_tend_save": np.zeros_like(scalars_old), "rho_zz_old": rho_old,
+            "rho_zz_new": rho_new, "uhAvg": uh, "wwAvg": ww,
+            "horiz_flux_arr": np.zeros((self.ne + 1, self.nl, scalars_old.shape[2]))})
+        return out["scalar_new"]

@@ -87,6 +87,13 @@ CASES = {
                    config=dict(config_monotonic=False, config_mpas_cam_coef=1.0,
                                config_number_cam_damping_levels=4,
                                config_apvm_upwinding=1.0), dt=1200.0, nsteps=2),
+    # two dynamics substeps per transport step
+    "g2_split2": dict(spec=dict(level=2, nlev=12, seed=6, n_bumps=6, n_tracers=2),
+                      config=dict(config_monotonic=True, config_dynamics_split_steps=2), dt=1200.0, nsteps=2),
+    # coupled transport: scalars advanced inside every RK stage of the single dynamics step
+    "g2_coupled": dict(spec=dict(level=2, nlev=12, seed=7, n_bumps=6, n_tracers=2),
+                       config=dict(config_monotonic=True, config_split_dynamics_transport=False),
+                       dt=600.0, nsteps=2),
 }
 
 BASE_CONFIG = {

@@ -14,7 +14,7 @@ import torch
 
 from fixtures import CASES, tap_calls
 from gpu_helpers import model_for_case, need_gpu
-from oracle.step import STAGE_NAMES
+from oracle.step import stage_names
 
 
 def test_oversize_problem_is_refused_before_any_device_work():
@@ -58,7 +58,7 @@ def _two_stage_calls(model, entry, inp, fields):
 def test_static_scratch_matches_caller_scratch_entry(case):
     need_gpu()
     from mpas_dycore_pytorch_gb300 import _lib
-    calls = list(tap_calls(case, STAGE_NAMES["scalars"]))
+    calls = [call for name in stage_names("scalars") for call in tap_calls(case, name)]
     if not calls:
         pytest.skip("no explicit transport stage in this case")
     inp = calls[0][0]
