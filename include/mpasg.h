@@ -133,7 +133,7 @@ typedef struct mpasg_config {
    * of u and w / of theta (full state; 0 = off), CAM-style top-level damping (0 = off) */
   double h_theta_eddy_visc2, v_mom_eddy_visc2, v_theta_eddy_visc2, mpas_cam_coef;
   int32_t number_cam_damping_levels;
-  int32_t reserved0;
+  int32_t scalar_advection_off;     /* 1: config_scalar_advection = false (scalars not transported) */
 } mpasg_config;
 
 /* Arithmetic of the step.  FLOAT64: every stage in float64 (the reference's arithmetic).

@@ -109,7 +109,7 @@ class MeshStruct(C.Structure):
 
 
 CONFIG_MIXING_DOUBLES = ("h_theta_eddy_visc2", "v_mom_eddy_visc2", "v_theta_eddy_visc2", "mpas_cam_coef")
-CONFIG_MIXING_INTS = ("number_cam_damping_levels", "reserved0")
+CONFIG_MIXING_INTS = ("number_cam_damping_levels", "scalar_advection_off")
 
 
 class ConfigStruct(C.Structure):

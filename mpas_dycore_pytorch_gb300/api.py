@@ -28,7 +28,7 @@ DEFAULTS = {
     "config_epssm": 0.1, "config_smdiv": 0.1, "config_len_disp": 0.0,
     "config_visc4_2dsmag": 0.05, "config_del4u_div_factor": 10.0,
     "config_apvm_upwinding": 0.5, "config_horiz_mixing": "2d_smagorinsky",
-    "config_monotonic": True, "config_positive_definite": False,
+    "config_monotonic": True, "config_positive_definite": False, "config_scalar_advection": True,
     "config_h_mom_eddy_visc2": 0.0, "config_h_mom_eddy_visc4": 0.0,
     "config_v_mom_eddy_visc2": 0.0, "config_h_theta_eddy_visc2": 0.0,
     "config_h_theta_eddy_visc4": 0.0, "config_v_theta_eddy_visc2": 0.0,
@@ -57,8 +57,7 @@ def validate_supported(cfg: Mapping[str, Any]) -> None:
         bad.append("config_dynamics_split_steps < 1")
     if int(cfg["config_time_integration_order"]) not in (2, 3):
         bad.append("config_time_integration_order")
-    for key in ("config_rayleigh_damp_u", "config_curvature_u", "config_positive_definite",
-                "config_apply_lbcs"):
+    for key in ("config_rayleigh_damp_u", "config_curvature_u", "config_apply_lbcs"):
         if bool(cfg[key]):
             bad.append(key)
     if not bool(cfg["config_mix_full"]):
@@ -103,7 +102,9 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
     # split transport off is one dynamics substep with the scalars inside the RK stages
     # (the reference's _resolve_dynamics_split, time_integration.py:1809-1878)
     c.dynamics_split_steps = int(cfg["config_dynamics_split_steps"]) if bool(cfg["config_split_dynamics_transport"]) else 1
-    c.monotonic = 1 if bool(cfg["config_monotonic"]) else 0
+    # the positive-definite option selects the same limited final transport stage
+    # (time_integration.py:3979-3987)
+    c.monotonic = 1 if (bool(cfg["config_monotonic"]) or bool(cfg["config_positive_definite"])) else 0
     c.horiz_mixing_smagorinsky = 1 if str(cfg["config_horiz_mixing"]) == "2d_smagorinsky" else 0
     c.num_scalars = int(num_scalars)
     c.moist_start = int(moist_start)
@@ -114,6 +115,7 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
     c.v_theta_eddy_visc2 = float(cfg["config_v_theta_eddy_visc2"])
     c.mpas_cam_coef = float(cfg["config_mpas_cam_coef"])
     c.number_cam_damping_levels = int(cfg["config_number_cam_damping_levels"])
+    c.scalar_advection_off = 0 if bool(cfg["config_scalar_advection"]) else 1
     return c
 
 

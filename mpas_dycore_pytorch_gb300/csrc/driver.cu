@@ -213,6 +213,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   mpasg_fields f = *fin;  // local copy: transport ping-pongs its scalar buffers
   const long long L = m->nVertLevels, nc = m->nCells, ne = m->nEdges;
   const long long S = c->num_scalars;
+  const bool advect = S > 0 && !c->scalar_advection_off;  // config_scalar_advection
   const long long ncl = (nc + 1) * L, nel = (ne + 1) * L, ncw = (nc + 1) * (L + 1);
   const long long ncs = (nc + 1) * L * S;
   const int split = c->dynamics_split_steps;
@@ -245,7 +246,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   CHECK_RC(copy(f.rr_save, f.rho_p, ncl, s));
   CHECK_RC(copy(f.rho_zz_old_split, f.rho_zz, ncl, s));
   if (S > 0) CHECK_RC(copy(f.scalars_init, f.scalars, ncs, s));
-  if (S > 0 && coupled) CHECK_RC(copy(f.scalars_a, f.scalars_init, ncs, s));
+  if (advect && coupled) CHECK_RC(copy(f.scalars_a, f.scalars_init, ncs, s));
   if (c->precision == MPASG_PRECISION_MIXED) CHECK_RC(mpasgi_pack_f32(m, &f, s));
   MARK(MPASG_STAGE_SETUP);
   CHECK_RC(mpasg_moist_coefficients(m, c, &f, stream));
@@ -271,7 +272,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
       }
       CHECK_RC(mpasg_recover_large_step(m, c, &f, rk, nsub[rk - 1], rk_ts[rk - 1], stream));
       MARK(MPASG_STAGE_RECOVER);
-      if (coupled && S > 0) {  // time_integration.py:7890-8200: stage dt, this stage's mass fluxes
+      if (coupled && advect) {  // time_integration.py:7890-8200: stage dt, this stage's mass fluxes
         CHECK_RC(transport_stage(m, c, &f, rk, rk_ts[rk - 1], s));
         MARK(rk == 3 && c->monotonic ? MPASG_STAGE_SCALARS_MONO : MPASG_STAGE_SCALARS);
       }
@@ -306,7 +307,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   MPASG_LAUNCH_CHECK();
 
   // ---- split transport RK3 with the substep-averaged mass fluxes
-  if (S > 0 && !coupled) {
+  if (advect && !coupled) {
     CHECK_RC(copy(f.scalars_a, f.scalars_init, ncs, s));
     // transport stage dts; the first is dt/2 for RK2 (time_integration.py:3366-3370)
     const double dts_t[3] = {c->time_integration_order == 2 ? dt / 2.0 : dt / 3.0, dt / 2.0, dt};
@@ -316,7 +317,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
       MARK(rk == 3 && c->monotonic ? MPASG_STAGE_SCALARS_MONO : MPASG_STAGE_SCALARS);
     }
   }
-  if (S > 0) CHECK_RC(copy(f.scalars, f.scalars_a, ncs, s));
+  if (advect) CHECK_RC(copy(f.scalars, f.scalars_a, ncs, s));
   MARK(MPASG_STAGE_SPLIT);
   CHECK_RC(mpasgi_reconstruct(m, c, &f, s, true));
   MARK(MPASG_STAGE_RECONSTRUCT);

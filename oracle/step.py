@@ -93,7 +93,11 @@ class Stepper:
         self.len_disp = float(self.cfg.get("config_len_disp", 0.0))
         if self.len_disp <= 0.0:
             self.len_disp = float(np.min(m["dcEdge"][:self.ne]))
-        self.monotonic = bool(self.cfg.get("config_monotonic", True))
+        # positive-definite selects the same limited last transport stage as monotonic
+        # (time_integration.py:3979-3987); config_scalar_advection = false skips transport
+        self.monotonic = bool(self.cfg.get("config_monotonic", True)) or \
+            bool(self.cfg.get("config_positive_definite", False))
+        self.advect = bool(self.cfg.get("config_scalar_advection", True))
         self.apvm = float(self.cfg.get("config_apvm_upwinding", 0.5))
         self.coef3 = float(m.get("coef_3rd_order", 0.25))
         self.c_s = float(m.get("c_s", 0.125))
@@ -278,7 +282,7 @@ class Stepper:
                 if rk == 3:
                     st["exner"] = rec["exner"]
                     st["pressure_p"] = rec["pressure_p"]
-                if self.coupled and scalars_init.shape[2] > 0:
+                if self.coupled and self.advect and scalars_init.shape[2] > 0:
                     st["scalars"] = self._transport_stage(rk, rk_ts[rk - 1], work["ruAvg"], work["wwAvg"],
                                                           scalars_init, st["scalars"], rho_zz_old_split,
                                                           st["rho_zz"], advance_density=0)
@@ -302,7 +306,7 @@ class Stepper:
         st["ruAvg"] = ru_avg
         st["wwAvg"] = ww_avg
 
-        if not self.coupled:
+        if not self.coupled and self.advect:
             # split transport RK3 with the substep-averaged mass fluxes
             scalars_new = scalars_init.copy()
             for rk in range(1, 4):

@@ -94,6 +94,14 @@ CASES = {
     "g2_coupled": dict(spec=dict(level=2, nlev=12, seed=7, n_bumps=6, n_tracers=2),
                        config=dict(config_monotonic=True, config_split_dynamics_transport=False),
                        dt=600.0, nsteps=2),
+    # positive-definite limiter instead of monotonic (same limited last stage); boundaries only
+    "g2_posdef": dict(spec=dict(level=2, nlev=12, seed=8, n_bumps=6, n_tracers=2),
+                      config=dict(config_monotonic=False, config_positive_definite=True),
+                      dt=1200.0, nsteps=2, taps=False),
+    # scalar transport switched off (config_scalar_advection = false); boundaries only
+    "g2_noadv": dict(spec=dict(level=2, nlev=12, seed=9, n_bumps=6, n_tracers=2),
+                     config=dict(config_monotonic=True, config_scalar_advection=False),
+                     dt=1200.0, nsteps=2, taps=False),
 }
 
 BASE_CONFIG = {
@@ -166,7 +174,7 @@ def run_case(mp, name: str, case: dict) -> None:
             meta.setdefault("loaded_scalars", {})[key] = _scalar(value)
 
     taps: dict[str, np.ndarray] = {}
-    recording = {"on": True}
+    recording = {"on": case.get("taps", True)}
     counts: dict[str, int] = {}
     keep_per_stage = {"mpas.acoustic_step_acoustic_step": 3, "mpas.divergence_damping": 2,
                       "mpas.large_step_recovery_recover_large_step": 3,
