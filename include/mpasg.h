@@ -111,6 +111,9 @@ typedef struct mpasg_mesh {
       *fnm_f32, *fnp_f32, *rdnw_f32;
   /* interface heights (C+1, L+1): the vertical mixing options of the tendencies */
   const double *zgrid;
+  /* initial profiles read by config_mix_full = false: u_init, v_init (L), angleEdge (E+1),
+   * t_init (C+1, L) */
+  const double *u_init, *v_init, *angleEdge, *t_init;
 } mpasg_mesh;
 
 /* Namelist options the step consumes (validated on the host). */
@@ -134,6 +137,11 @@ typedef struct mpasg_config {
   double h_theta_eddy_visc2, v_mom_eddy_visc2, v_theta_eddy_visc2, mpas_cam_coef;
   int32_t number_cam_damping_levels;
   int32_t scalar_advection_off;     /* 1: config_scalar_advection = false (scalars not transported) */
+  /* Rayleigh damping of u on the top levels (every RK stage; dyn_tend.py:10066-10072,
+   * 2956-2990) and vertical mixing of the perturbation from the initial profiles */
+  double rayleigh_damp_u_timescale_days;
+  int32_t rayleigh_damp_u_levels;   /* 0: off */
+  int32_t mix_perturbation;         /* 1: config_mix_full = false */
 } mpasg_config;
 
 /* Arithmetic of the step.  FLOAT64: every stage in float64 (the reference's arithmetic).

@@ -94,7 +94,7 @@ MESH_F32_PTRS = tuple(n + "_f32" for n in (
     "fnp", "rdnw"))
 
 # float64 arrays appended after the float32 copies
-MESH_TAIL_PTRS = ("zgrid",)
+MESH_TAIL_PTRS = ("zgrid", "u_init", "v_init", "angleEdge", "t_init")
 
 
 STAGE_NAMES = ("begin", "setup", "moist", "vert_imp_coefs", "dyn_tend_rk1", "dyn_tend",
@@ -112,9 +112,14 @@ CONFIG_MIXING_DOUBLES = ("h_theta_eddy_visc2", "v_mom_eddy_visc2", "v_theta_eddy
 CONFIG_MIXING_INTS = ("number_cam_damping_levels", "scalar_advection_off")
 
 
+CONFIG_DAMPING = (("rayleigh_damp_u_timescale_days", C.c_double), ("rayleigh_damp_u_levels", C.c_int32),
+                  ("mix_perturbation", C.c_int32))
+
+
 class ConfigStruct(C.Structure):
     _fields_ = ([(n, C.c_double) for n in CONFIG_DOUBLES] + [(n, C.c_int32) for n in CONFIG_INTS]
-                + [(n, C.c_double) for n in CONFIG_MIXING_DOUBLES] + [(n, C.c_int32) for n in CONFIG_MIXING_INTS])
+                + [(n, C.c_double) for n in CONFIG_MIXING_DOUBLES] + [(n, C.c_int32) for n in CONFIG_MIXING_INTS]
+                + list(CONFIG_DAMPING))
 
 
 class FieldsStruct(C.Structure):

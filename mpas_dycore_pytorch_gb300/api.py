@@ -32,7 +32,9 @@ DEFAULTS = {
     "config_h_mom_eddy_visc2": 0.0, "config_h_mom_eddy_visc4": 0.0,
     "config_v_mom_eddy_visc2": 0.0, "config_h_theta_eddy_visc2": 0.0,
     "config_h_theta_eddy_visc4": 0.0, "config_v_theta_eddy_visc2": 0.0,
-    "config_rayleigh_damp_u": False, "config_mpas_cam_coef": 0.0, "config_number_cam_damping_levels": 4,
+    "config_rayleigh_damp_u": False, "config_rayleigh_damp_u_timescale_days": 5.0,
+    "config_number_rayleigh_damp_u_levels": 6,
+    "config_mpas_cam_coef": 0.0, "config_number_cam_damping_levels": 4,
     "config_curvature_u": False, "config_mix_full": True, "config_IAU_option": "off",
     "config_apply_lbcs": False, "config_dt": 720.0,
     # GB300 extension (no reference counterpart): "float64" (the reference's arithmetic)
@@ -57,11 +59,9 @@ def validate_supported(cfg: Mapping[str, Any]) -> None:
         bad.append("config_dynamics_split_steps < 1")
     if int(cfg["config_time_integration_order"]) not in (2, 3):
         bad.append("config_time_integration_order")
-    for key in ("config_rayleigh_damp_u", "config_curvature_u", "config_apply_lbcs"):
+    for key in ("config_curvature_u", "config_apply_lbcs"):
         if bool(cfg[key]):
             bad.append(key)
-    if not bool(cfg["config_mix_full"]):
-        bad.append("config_mix_full=False")
     if str(cfg["config_IAU_option"]) != "off":
         bad.append("config_IAU_option")
     if str(cfg["config_horiz_mixing"]) not in ("2d_smagorinsky", "2d_fixed"):
@@ -116,6 +116,9 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
     c.mpas_cam_coef = float(cfg["config_mpas_cam_coef"])
     c.number_cam_damping_levels = int(cfg["config_number_cam_damping_levels"])
     c.scalar_advection_off = 0 if bool(cfg["config_scalar_advection"]) else 1
+    c.rayleigh_damp_u_timescale_days = float(cfg["config_rayleigh_damp_u_timescale_days"])
+    c.rayleigh_damp_u_levels = int(cfg["config_number_rayleigh_damp_u_levels"]) if bool(cfg["config_rayleigh_damp_u"]) else 0
+    c.mix_perturbation = 0 if bool(cfg["config_mix_full"]) else 1
     return c
 
 

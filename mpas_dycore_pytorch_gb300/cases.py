@@ -372,6 +372,7 @@ class CaseSpec:
     w_sine: float = 0.0
     round_wind_bits: int = 0
     qv_surface: float = 0.0  # > 0: moist case, water vapour as scalar 0 (moist_end = 1)
+    uv_init: tuple = (0.0, 0.0)  # initial (u, v) profile values (read by config_mix_full = false)
 
 
 def _vertical_metrics(zw: np.ndarray) -> dict:
@@ -492,7 +493,7 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
         "zxu": np.zeros((ne, nlev)),
         "scalars": scalars, "num_scalars": scalars.shape[-1], "qv": qv,
         "moist_start": 1, "moist_end": 1 if spec.qv_surface > 0.0 else 0,
-        "u_init": np.full(nlev, 0.0), "v_init": np.zeros(nlev),
+        "u_init": np.full(nlev, float(spec.uv_init[0])), "v_init": np.full(nlev, float(spec.uv_init[1])),
         "t_init": theta_b.copy(), "qv_init": np.zeros(nlev),
     }
     for k, v in vm.items():

@@ -24,8 +24,11 @@ namespace {
 struct TendScalars {
   double inv_dt, c_s_len2, kdiff_cap, h_mom_visc4, h_theta_visc4, del4u_div, coef3, visc2;
   double cam_base, v_mom, v_theta;  // CAM damping base, vertical mixing coefficients (0: off)
+  double ray_coef;                  // 1 / (levels * timescale): Rayleigh damping of u
   int rk_step, smag, del4;
   int ncam;   // CAM damping levels (0: off)
+  int ray_n;  // Rayleigh-damped top levels of u (0: off)
+  int mix_pert;  // vertical mixing of the perturbation from the initial profiles
   int defer;  // k_tend_u leaves tend_u_euler to k_tend_u_finish (del4 and / or vertical mixing)
 };
 
@@ -80,6 +83,16 @@ __global__ void k_tend_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendSca
   } else {  // 2d_fixed: the theta del2 coefficient everywhere
     f.kdiff[i] = (p.ncam > 0 && (int)k >= L - p.ncam) ? cam_kdiff(p.visc2, p, k, L) : p.visc2;
   }
+}
+
+// Rayleigh damping of u on the top ray_n levels (dyn_tend.py:2956-2990), every RK stage:
+// tend_u - rho_edge u ((k + 1) - k0) / (ray_n timescale), k0 = L - ray_n
+template <typename T>
+MPASG_D T rayleigh_u(T tu, T rho_e, T u_k, int k, int L, const TendScalars& p) {
+  const int k0 = L - p.ray_n;
+  if (p.ray_n <= 0 || k < k0) return tu;
+  const double damp = (((double)k + 1.0) - (double)k0) * p.ray_coef;
+  return tu - rho_e * u_k * cv<T>(damp);
 }
 
 template <typename T>
@@ -146,6 +159,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_u(mpasg_mesh m, mpasg_fields f,
   const T rho_e = cv<T>(f.h_edge[i]);
   tu = tu + rho_e * (q - dif<T>(f.ke[i2], f.ke[i1]) * inv_dc) -
        ue[k] * T(0.5) * (cv<T>(f.h_divergence[i1]) + cv<T>(f.h_divergence[i2]));
+  tu = rayleigh_u<T>(tu, rho_e, ue[k], (int)k, L, p);
   if (p.rk_step == 1) {
     const T* zz = G(zz);
     T teu = -cv<T>(f.cqu_e[i]) * (div_or_one<T>(dif<T>(f.pressure_p[i2], f.pressure_p[i1]) * inv_dc,
@@ -229,6 +243,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_u_chunk(mpasg_mesh m, mpasg_fie
     const T rho_e = cv<T>(f.h_edge[ie]);
     tu = tu + rho_e * (qv - dif<T>(f.ke[i2], f.ke[i1]) * inv_dc) -
          ue[k] * T(0.5) * (cv<T>(f.h_divergence[i1]) + cv<T>(f.h_divergence[i2]));
+    tu = rayleigh_u<T>(tu, rho_e, ue[k], k, L, p);
     if (p.rk_step == 1) {
       const T* zz = G(zz);
       T teu = -cv<T>(f.cqu_e[ie]) * (div_or_one<T>(dif<T>(f.pressure_p[i2], f.pressure_p[i1]) * inv_dc,
@@ -318,8 +333,15 @@ __global__ void k_tend_u_finish(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendSc
     const double zc = 0.5 * (z1p[k + 1] + z2p[k + 1]), zd = 0.5 * (z1p[k + 2] + z2p[k + 2]);
     const double zm = 0.5 * (za + zb), z0 = 0.5 * (zb + zc), zp = 0.5 * (zc + zd);
     const double* u = f.u + (size_t)e * L;
-    const T d_up = dif<T>(u[k + 1], u[k]) / cv<T>(zp - z0);
-    const T d_dn = dif<T>(u[k], u[k - 1]) / cv<T>(z0 - zm);
+    double um = u[k - 1], u0 = u[k], up = u[k + 1];
+    if (p.mix_pert) {  // perturbation from the initial profile along the edge normal
+      const double ca = cos(m.angleEdge[e]), sa = sin(m.angleEdge[e]);
+      um = um - m.u_init[k - 1] * ca - m.v_init[k - 1] * sa;
+      u0 = u0 - m.u_init[k] * ca - m.v_init[k] * sa;
+      up = up - m.u_init[k + 1] * ca - m.v_init[k + 1] * sa;
+    }
+    const T d_up = dif<T>(up, u0) / cv<T>(zp - z0);
+    const T d_dn = dif<T>(u0, um) / cv<T>(z0 - zm);
     teu = teu + cv<T>(f.h_edge[i]) * cv<T>(p.v_mom) * (d_up - d_dn) / cv<T>(0.5 * (zp - zm));
   }
   f.tend_u_euler[i] = f64(teu);
@@ -336,11 +358,19 @@ MPASG_D double w_vmix(const mpasg_mesh& m, const mpasg_fields& f, size_t oc, siz
 
 // vertical mixing of theta at level k, 1 <= k <= L-2 (dyn_tend.py:5064-5100, rk 1;
 // Prandtl factor 1)
-MPASG_D double theta_vmix(const mpasg_mesh& m, const mpasg_fields& f, uint32_t c, uint32_t k, int L, double v) {
+MPASG_D double theta_vmix(const mpasg_mesh& m, const mpasg_fields& f, uint32_t c, uint32_t k, int L, double v,
+                          int mix_pert) {
   const double* zg = m.zgrid + (size_t)c * (L + 1);
   const double zm = 0.5 * (zg[k - 1] + zg[k]), z0 = 0.5 * (zg[k] + zg[k + 1]), zp = 0.5 * (zg[k + 1] + zg[k + 2]);
   const double* th = f.theta_m + (size_t)c * L;
-  const double diff = (th[k + 1] - th[k]) / (zp - z0) - (th[k] - th[k - 1]) / (z0 - zm);
+  double tm = th[k - 1], t0 = th[k], tp = th[k + 1];
+  if (mix_pert) {  // perturbation from the initial profile
+    const double* ti = m.t_init + (size_t)c * L;
+    tm = tm - ti[k - 1];
+    t0 = t0 - ti[k];
+    tp = tp - ti[k + 1];
+  }
+  const double diff = (tp - t0) / (zp - z0) - (t0 - tm) / (z0 - zm);
   return v * 1.0 * f.rho_zz[(size_t)c * L + k] * diff / (0.5 * (zp - zm));
 }
 
@@ -589,7 +619,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta(mpasg_mesh m, mpasg_fie
     tt = tt + rz * rtd;
     double tte = f.tend_theta_euler[o];
     if (p.rk_step == 1 && p.v_theta > 0.0 && k >= 1 && k + 1 < (uint32_t)L) {
-      tte = tte + theta_vmix(m, f, c, k, L, p.v_theta);
+      tte = tte + theta_vmix(m, f, c, k, L, p.v_theta, p.mix_pert);
       f.tend_theta_euler[o] = tte;
     }
     tt = tt + tte;
@@ -729,7 +759,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
     f.rthdynten[o] = f64(cv<T>(ttot - f.tend_rho[o] * f.theta_m[o]) / cv<T>(rz));
     double tte = f.tend_theta_euler[o];
     if (p.rk_step == 1 && p.v_theta > 0.0 && k >= 1 && k + 1 < (uint32_t)L) {
-      tte = tte + theta_vmix(m, f, c, k, L, p.v_theta);
+      tte = tte + theta_vmix(m, f, c, k, L, p.v_theta, p.mix_pert);
       f.tend_theta_euler[o] = tte;
     }
     f.tend_theta[o] = ttot + rz * f.rt_diabatic_tend[o] + tte;
@@ -839,6 +869,12 @@ int mpasgi_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
   if (p.v_mom > 0.0 || p.v_theta > 0.0) {
     if (!m->zgrid) return MPASG_E_ARG;
   }
+  p.mix_pert = c->mix_perturbation ? 1 : 0;
+  if (p.mix_pert && (p.v_mom > 0.0 || p.v_theta > 0.0) && (!m->u_init || !m->v_init || !m->angleEdge || !m->t_init))
+    return MPASG_E_ARG;
+  p.ray_n = c->rayleigh_damp_u_levels;
+  if (p.ray_n > m->nVertLevels || p.ray_n < 0) return MPASG_E_ARG;
+  p.ray_coef = p.ray_n > 0 ? 1.0 / ((double)p.ray_n * (c->rayleigh_damp_u_timescale_days * 86400.0)) : 0.0;
   if (c->precision == MPASG_PRECISION_MIXED) {
     if (!copies_current) {
       const int rc = mpasgi_pack_f32(m, f, s);

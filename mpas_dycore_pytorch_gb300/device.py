@@ -116,7 +116,9 @@ class DeviceMesh:
         for n in _lib.MESH_TAIL_PTRS:
             if n not in ref:
                 raise MpasConfigError(f"mesh is missing {n}")
-            dbls[n] = np.ascontiguousarray(_np(ref[n])[:, :nl + 1], dtype=np.float64)
+            a = _np(ref[n])
+            a = a[:, :nl + 1] if n == "zgrid" else a[:nl] if a.ndim == 1 and n != "angleEdge" else a
+            dbls[n] = np.ascontiguousarray(a, dtype=np.float64)
         for n, a in dbls.items():
             t = torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
             self._keep[n] = t

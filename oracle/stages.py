@@ -688,9 +688,18 @@ def dyn_tend(a):
             z1, z2, z3, z4 = zi(0, nl - 2), zi(1, nl - 1), zi(2, nl), zi(3, nl + 1)
             zm, z0, zp = 0.5 * (z1 + z2), 0.5 * (z2 + z3), 0.5 * (z3 + z4)
             uu = u[:ne]
+            if not bool(a.get("config_mix_full", True)):  # perturbation from the initial profile
+                ang = a["angleEdge"][:ne, None]
+                uu = uu - a["u_init"][None, :nl] * np.cos(ang) - a["v_init"][None, :nl] * np.sin(ang)
             tend_u_euler[:ne, 1:nl - 1] = tend_u_euler[:ne, 1:nl - 1] + rho_edge[:ne, 1:nl - 1] * v_mom * (
                 (uu[:, 2:nl] - uu[:, 1:nl - 1]) / (zp - z0) - (uu[:, 1:nl - 1] - uu[:, :nl - 2]) / (z0 - zm)
             ) / (0.5 * (zp - zm))
+    if bool(a.get("config_rayleigh_damp_u", False)):  # top-level damping of u, every RK stage
+        nray = _i(a, "config_number_rayleigh_damp_u_levels")  # (dyn_tend.py:10066-10072, 2956-2990)
+        coef = 1.0 / (float(nray) * (_f(a, "config_rayleigh_damp_u_timescale_days") * 86400.0))
+        k0 = nl - nray
+        damp = ((np.arange(k0, nl, dtype=np.float64) + 1.0) - float(k0)) * coef
+        tend_u[:, k0:] = tend_u[:, k0:] - rho_edge[:ne, k0:] * u[:ne, k0:] * damp[None, :]
     tend_u = zpad(tend_u + tend_u_euler[:ne])
 
     # ---- w tendency ----
@@ -793,6 +802,8 @@ def dyn_tend(a):
             z1, z2, z3, z4 = zg[:, 0:nl - 2], zg[:, 1:nl - 1], zg[:, 2:nl], zg[:, 3:nl + 1]
             zm, z0, zp = 0.5 * (z1 + z2), 0.5 * (z2 + z3), 0.5 * (z3 + z4)
             th = theta_m[:nc]
+            if not bool(a.get("config_mix_full", True)):
+                th = th - a["t_init"][:nc]
             diff = (th[:, 2:nl] - th[:, 1:nl - 1]) / (zp - z0) - (th[:, 1:nl - 1] - th[:, :nl - 2]) / (z0 - zm)
             tend_theta_euler[:nc, 1:nl - 1] = tend_theta_euler[:nc, 1:nl - 1] + \
                 v_th * prandtl_inv * a["rho_zz"][:nc, 1:nl - 1] * diff / (0.5 * (zp - zm))

@@ -229,6 +229,12 @@ class Stepper:
                     "config_v_theta_eddy_visc2": float(self.cfg.get("config_v_theta_eddy_visc2", 0.0)),
                     "config_mpas_cam_coef": float(self.cfg.get("config_mpas_cam_coef", 0.0)),
                     "config_number_cam_damping_levels": int(self.cfg.get("config_number_cam_damping_levels", 4)),
+                    "config_mix_full": bool(self.cfg.get("config_mix_full", True)),
+                    "config_rayleigh_damp_u": bool(self.cfg.get("config_rayleigh_damp_u", False)),
+                    "config_rayleigh_damp_u_timescale_days":
+                        float(self.cfg.get("config_rayleigh_damp_u_timescale_days", 5.0)),
+                    "config_number_rayleigh_damp_u_levels":
+                        int(self.cfg.get("config_number_rayleigh_damp_u_levels", 6)),
                     "config_len_disp": self.len_disp,
                     "u": st["u"], "v": st["v"], "w": st["w"], "ru": st["ru"], "rw": st["rw"],
                     "ru_save": save["ru_save"], "rw_save": save["rw_save"],

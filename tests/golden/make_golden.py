@@ -94,6 +94,15 @@ CASES = {
     "g2_coupled": dict(spec=dict(level=2, nlev=12, seed=7, n_bumps=6, n_tracers=2),
                        config=dict(config_monotonic=True, config_split_dynamics_transport=False),
                        dt=600.0, nsteps=2),
+    # Rayleigh damping of u on the top levels, vertical mixing of the perturbation from the
+    # initial profiles (config_mix_full = false)
+    "g2_rayleigh": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=10, n_bumps=6, n_tracers=1,
+                                  w_sine=0.05, uv_init=(15.0, 2.0)),
+                        config=dict(config_monotonic=False, config_rayleigh_damp_u=True,
+                                    config_rayleigh_damp_u_timescale_days=0.5,
+                                    config_number_rayleigh_damp_u_levels=4, config_mix_full=False,
+                                    config_v_mom_eddy_visc2=2.0, config_v_theta_eddy_visc2=2.0),
+                        dt=1200.0, nsteps=2),
     # positive-definite limiter instead of monotonic (same limited last stage); boundaries only
     "g2_posdef": dict(spec=dict(level=2, nlev=12, seed=8, n_bumps=6, n_tracers=2),
                       config=dict(config_monotonic=False, config_positive_definite=True),

@@ -99,7 +99,10 @@ def test_mixed_form_within_stated_error_after_24_steps():
     {"config_horiz_mixing": "2d_fixed", "config_h_mom_eddy_visc4": 1.0e10, "config_h_theta_eddy_visc4": 5.0e9,
      "config_h_theta_eddy_visc2": 2.0e4, "config_v_mom_eddy_visc2": 1.0, "config_v_theta_eddy_visc2": 1.0},
     {"config_mpas_cam_coef": 1.0, "config_number_cam_damping_levels": 4, "config_apvm_upwinding": 1.0},
-], ids=["fixed_vertical_mixing", "cam_damping"])
+    {"config_rayleigh_damp_u": True, "config_rayleigh_damp_u_timescale_days": 0.5,
+     "config_number_rayleigh_damp_u_levels": 6, "config_mix_full": False, "config_v_mom_eddy_visc2": 2.0,
+     "config_v_theta_eddy_visc2": 2.0},
+], ids=["fixed_vertical_mixing", "cam_damping", "rayleigh_perturbation_mixing"])
 def test_mixed_form_with_mixing_options(options):
     """The mixing options (2d_fixed, vertical mixing, CAM damping) in the mixed form stay
     within the stated error of the float64 form (6 steps on the level-4 mesh)."""
