@@ -263,6 +263,72 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
     return forms
 
 
+def measure_ensemble_groups(args, dev):
+    """The two-grid mixed-precision ensemble: 96 members of 10242 cells x 41 levels (dt
+    900 s) and 32 members of 40962 cells x 55 stretched levels (dt 720 s), 2 monotone
+    tracers, seeds 100-227 with u noise 0.5 m/s, all replayed from one CUDA graph.  Also
+    times each member shape alone in float64 (the sequential baseline) and checks the
+    first member of each group against its float64 solo run after 24 steps."""
+    import torch
+
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.device import STATE_KEYS
+    from mpas_dycore_pytorch_gb300.ensemble import EnsembleGroups, member_cases
+
+    K, W, nerr = args.steps, args.warmup, 24
+    shapes = [("c2", 96, list(range(100, 196))), ("c1", 32, list(range(196, 228)))]
+    groups, solo_ms, firsts = [], [], []
+    for key, n, seeds in shapes:
+        w = WORKLOADS[key]
+        spec = CaseSpec(**dict(w["spec"], n_tracers=2))
+        cfg = _cfg(w)
+        mem = member_cases(spec, seeds=seeds[:n], config=cfg, u_noise=0.5)
+        groups.append((mem, cfg, w["dt"]))
+        firsts.append((mem[0], cfg, w["dt"]))
+    # float64 solo runs of each group's first member: sequential baseline and error reference
+    ref_end = []
+    for m0, cfg, dt in firsts:
+        solo = Model(m0, cfg, dt, num_scalars=2, device=dev, order=args.order)
+        solo.prepare(m0)
+        solo.autotune()
+        solo.capture_graph()
+        for _ in range(nerr):
+            solo.step()
+        torch.cuda.synchronize()
+        exp = solo.export()  # the member's own order (the solo run may be in curve order)
+        ref_end.append({k: exp[k][:-1] for k in STATE_KEYS})
+        solo_ms.append(_time_steps(solo.step, K, W))
+        del solo
+        torch.cuda.empty_cache()
+    ens = EnsembleGroups(groups, precision="mixed", device=dev, order=args.order)
+    tune = ens.autotune()
+    ens.capture_graph()
+    for _ in range(nerr):
+        ens.step()
+    torch.cuda.synchronize()
+    err = {}
+    for gi, ref in enumerate(ref_end):
+        got = ens.member_state(gi, 0)
+        for k, r in ref.items():
+            den = torch.linalg.vector_norm(r).item()
+            if den > 0:
+                e = torch.linalg.vector_norm(got[k][:-1] - r).item() / den
+                err[f"{shapes[gi][0]}:{k}"] = e
+    ms = _time_steps(ens.step, K, W)
+    seq_ms = sum(n * t for (_, n, _), t in zip(shapes, solo_ms))
+    out = {"members": [n for _, n, _ in shapes],
+           "member_workloads": ["10242 cells x 41 levels, dt 900 s", "40962 cells x 55 levels, dt 720 s"],
+           "value": ens.cell_levels / (ms / 1e3), "ms_per_step": ms,
+           "sequential_float64_ms_per_step": seq_ms, "speedup_vs_sequential_float64": seq_ms / ms,
+           "max_rel_l2_first_members_vs_float64_after_24_steps": max(err.values()),
+           "worst_field": max(err, key=err.get), "nonfinite": ens.check_finite(),
+           "state_bytes": ens.state_bytes, "autotune": tune, "graph": "one graph, one stream per group"}
+    del ens
+    torch.cuda.empty_cache()
+    return out
+
+
 def st_cells_levels(st):
     import numpy as np
     return int(np.asarray(st["nCells"]).reshape(-1)[0]) * int(np.asarray(st["nVertLevels"]).reshape(-1)[0])
@@ -439,6 +505,8 @@ def run_gb300(args, rank, world):
         del model, host
         torch.cuda.empty_cache()
         forms = measure_forms(args, dev, st, cfg, w, ms / K)
+        if args.ensemble_groups:
+            forms["batched_two_grids"] = measure_ensemble_groups(args, dev)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -496,6 +564,8 @@ def main():
     ap.add_argument("--order", default="sfc", choices=("native", "sfc"),
                     help="mesh order on the device: generator order or Hilbert curve")
     ap.add_argument("--ensemble", type=int, default=96, help="members of the batched level-5 ensemble (0: skip)")
+    ap.add_argument("--ensemble-groups", action="store_true",
+                    help="also run the two-grid mixed ensemble (96 x 10242x41 + 32 x 40962x55, ~200 GB)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -204,3 +204,73 @@ class Ensemble:
             perm, dims = self._perms[b]
             out = restore_order(out, perm, dims)
         return out
+
+
+class EnsembleGroups:
+    """Members on several vertical grids (or with different timesteps / options), e.g. 96
+    members of 10242 cells x 41 levels beside 32 members of 40962 cells x 55 levels.
+
+    The level count is a dimension of every kernel's index space, so members sharing a
+    vertical grid and options form one union (``Ensemble``) and the groups step side by
+    side: ``capture_graph`` records every group's large step into ONE CUDA graph, each
+    group on its own stream forked from and joined back to the capturing stream, so a
+    replay launches the whole ensemble at once and the groups' kernels overlap.  Each
+    member's result is the same as in its group alone (bit-identical in float64: the
+    groups share no memory).
+    """
+
+    def __init__(self, groups: Sequence[tuple[Sequence[Mapping[str, Any]], Mapping[str, Any] | None, float]],
+                 precision: str | None = None, device: str | torch.device = "cuda", order: str = "native"):
+        if not groups:
+            raise MpasConfigError("an ensemble needs at least one group")
+        self.groups = [Ensemble(members, config, dt, precision=precision, device=device, order=order)
+                       for members, config, dt in groups]
+        self.cell_levels = sum(g.cell_levels for g in self.groups)
+        self._graph = None
+        self._streams = None
+
+    def autotune(self) -> list[dict]:
+        return [g.model.autotune() for g in self.groups]
+
+    def step(self) -> None:
+        if self._graph is not None:
+            self._graph.replay()
+        else:
+            for g in self.groups:
+                g.model.step()
+
+    def capture_graph(self) -> None:
+        """One graph for all groups (fork / join over one stream per group)."""
+        import ctypes as C
+
+        from . import _lib
+
+        torch.cuda.synchronize()
+        main = torch.cuda.Stream()
+        side = [torch.cuda.Stream() for _ in self.groups]
+        main.wait_stream(torch.cuda.current_stream())
+        graph = torch.cuda.CUDAGraph()
+        rcs = []
+        with torch.cuda.stream(main):
+            with torch.cuda.graph(graph, stream=main):
+                for g, s in zip(self.groups, side):
+                    s.wait_stream(main)
+                    m = g.model
+                    rcs.append(m.lib.mpasg_step(C.byref(m.dmesh.struct), C.byref(m.cstruct),
+                                                C.byref(m.state.struct), C.c_void_p(s.cuda_stream)))
+                    main.wait_stream(s)
+        torch.cuda.current_stream().wait_stream(main)
+        for rc in rcs:
+            _lib.check(rc, "mpasg_step (ensemble capture)")
+        self._graph = graph
+        self._streams = (main, side)
+
+    def check_finite(self) -> int:
+        return sum(g.model.check_finite() for g in self.groups)
+
+    def member_state(self, group: int, b: int) -> dict:
+        return self.groups[group].member_state(b)
+
+    @property
+    def state_bytes(self) -> int:
+        return sum(g.model.state.bytes for g in self.groups)

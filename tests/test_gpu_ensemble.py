@@ -41,3 +41,33 @@ def test_members_match_individual_runs(members, precision):
         for k in STATE_KEYS:
             want = solo.state.f[k][:-1]
             assert torch.equal(got[k][:-1], want), (precision, b, k)
+
+
+@pytest.mark.parametrize("precision", ("float64", "mixed"))
+def test_groups_on_different_vertical_grids_in_one_graph(members, precision):
+    """Members on two vertical grids (16 and 12 levels) with different timesteps: one CUDA
+    graph replays both groups' steps, and every member matches its solo run bit for bit."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.device import STATE_KEYS
+    from mpas_dycore_pytorch_gb300.ensemble import EnsembleGroups, member_cases
+    cfg12 = dict(CFG, config_dt=900.0, config_monotonic=False)
+    other = member_cases(CaseSpec(level=3, nlev=12, n_bumps=2, n_tracers=2, dz_bottom=300.0), seeds=[20, 21, 22],
+                         config=cfg12, u_noise=0.5)
+    groups = [(members, CFG, 600.0), (other, cfg12, 900.0)]
+    ens = EnsembleGroups(groups, precision=precision)
+    ens.capture_graph()
+    for _ in range(2):
+        ens.step()
+    torch.cuda.synchronize()
+    assert ens.check_finite() == 0
+    for gi, (mems, cfg, dt) in enumerate(groups):
+        for b, m in enumerate(mems):
+            solo = Model(m, cfg, dt, num_scalars=2, precision=precision)
+            solo.prepare(m)
+            for _ in range(2):
+                solo.step()
+            got = ens.member_state(gi, b)
+            for k in STATE_KEYS:
+                assert torch.equal(got[k][:-1], solo.state.f[k][:-1]), (precision, gi, b, k)
