@@ -55,6 +55,11 @@ WORKLOADS = {
 # of the level-5 x 41 case (profiles/dyn_tend_dram_traffic_level5_10242x41_fp64.md), scaled
 # to the workload by its cell-levels
 TRAFFIC_B_PER_CELL_LEVEL = {"dyn_tend": 542.7}
+# executed float64 flops (2 per FMA) per call and cell-level of a float64 stage, averaged
+# over a large step's calls, from an ncu count on the same level-5 x 41 case
+# (profiles/dyn_tend_fp64_flops_level5_10242x41.md)
+FP64_FLOP_PER_CELL_LEVEL = {"dyn_tend": 637.5}
+FP64_INST_PER_CELL_LEVEL = {"dyn_tend": 476.4}  # DFMA + DMUL + DADD issued
 BASE_CFG = {"config_time_integration_order": 3, "config_len_disp": 120000.0,
             "config_number_of_sub_steps": 2, "config_dynamics_split_steps": 3}
 
@@ -329,6 +334,32 @@ def measure_ensemble_groups(args, dev):
     return out
 
 
+def fp64_roofline(flops_per_launch, inst_per_launch, launch_ms, dev):
+    """{"achieved", "peak", "unit": "TFLOP/s", "frac"} for a float64-bound stage; the peak
+    from mpasg_fp64_peak (1216 blocks x 256 threads x 4096 rounds of 8 FMAs).  A DMUL or
+    DADD occupies the pipe like a DFMA but counts one flop, so "pipe_frac" (issued float64
+    instructions against peak / 2 per second) is the utilisation of the bounding unit."""
+    import ctypes as C
+
+    import torch
+
+    from mpas_dycore_pytorch_gb300 import _lib
+    blocks = 152 * 8
+    buf = torch.rand(blocks * 256, dtype=torch.float64, device=dev) * 0.5
+    peak = C.c_double(0.0)
+    rc = _lib.load().mpasg_fp64_peak(C.c_void_p(buf.data_ptr()), blocks, 4096, C.byref(peak),
+                                     C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(rc, "mpasg_fp64_peak")
+    achieved = flops_per_launch / (launch_ms / 1e3) / 1e12
+    pk = peak.value / 1e12
+    pipe = inst_per_launch / (launch_ms / 1e3) / (peak.value / 2.0)
+    return {"achieved": round(achieved, 4), "peak": round(pk, 4), "unit": "TFLOP/s", "frac": round(achieved / pk, 4),
+            "pipe_frac": round(pipe, 4), "flops_per_launch": round(flops_per_launch),
+            "fp64_instructions_per_launch": round(inst_per_launch),
+            "peak_source": "measured in this run (mpasg_fp64_peak)",
+            "flops_source": "ncu executed float64 instructions (2 flops per FMA), level-5 count scaled by cell-levels"}
+
+
 def st_cells_levels(st):
     import numpy as np
     return int(np.asarray(st["nCells"]).reshape(-1)[0]) * int(np.asarray(st["nVertLevels"]).reshape(-1)[0])
@@ -475,6 +506,12 @@ def run_gb300(args, rank, world):
                 "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"stage:{dom}",
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_call,
                 "launch_ms": round(per_call_ms, 4)}
+        # the float64 form's real bound: the float64 pipe (GB300 runs float64 at 1/64 of
+        # float32).  Executed float64 flops of the stage from an ncu count, against the
+        # float64 peak measured here with the library's own multiply-add kernel.
+        if dom in FP64_FLOP_PER_CELL_LEVEL and args.precision == "float64":
+            roof["fp64_pipe"] = fp64_roofline(FP64_FLOP_PER_CELL_LEVEL[dom] * C_ * L_,
+                                              FP64_INST_PER_CELL_LEVEL[dom] * C_ * L_, per_call_ms, dev)
 
     # end to end through the public API with pinned host buffers
     keys = [k for k in STATE_KEYS]

@@ -257,6 +257,11 @@ int mpasg_autotune(const mpasg_mesh *m, mpasg_config *c, mpasg_fields *f, float 
  * the helpers against CUDA's own conversions and division: which = 0 float64 -> float32 ->
  * float64 through the integer repacking; which = 1 the Newton-Raphson reciprocal. */
 int mpasg_numerics_check(int which, const double *in, double *out, long long n, void *stream);
+/* Float64 arithmetic peak of this GPU, measured: `blocks` x 256 threads each run `iters`
+ * rounds of 8 independent fused multiply-adds on values read from buf (blocks * 256
+ * doubles, written back so nothing is optimised away); *flops_per_s receives
+ * 2 * 8 * iters * threads / time of the second of two launches.  Synchronises the stream. */
+int mpasg_fp64_peak(double *buf, int blocks, int iters, double *flops_per_s, void *stream);
 /* Count non-finite values of the prognostic fields into f->status[0] (async). */
 int mpasg_check_finite(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, void *stream);
 

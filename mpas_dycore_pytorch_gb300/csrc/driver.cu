@@ -130,6 +130,47 @@ extern "C" int mpasg_numerics_check(int which, const double* in, double* out, lo
   return MPASG_OK;
 }
 
+namespace {
+// 8 independent multiply-add chains per thread: the float64 pipe, not latency, bounds it
+__global__ void __launch_bounds__(256) k_fp64_peak(double* buf, int iters) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const double x = buf[t], y = 1.0 - x;
+  double a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = x + (double)j;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = fma(a[j], x, y);
+  }
+  double sum = 0.0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) sum += a[j];
+  buf[t] = sum;
+}
+}  // namespace
+
+extern "C" int mpasg_fp64_peak(double* buf, int blocks, int iters, double* flops_per_s, void* stream) {
+  if (!buf || !flops_per_s || blocks < 1 || iters < 1) return MPASG_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return MPASG_E_CUDA;
+  int rc = MPASG_OK;
+  float ms = 0.0f;
+  for (int rep = 0; rep < 2 && rc == MPASG_OK; ++rep) {
+    if (rep == 1 && cudaEventRecord(a, s) != cudaSuccess) rc = MPASG_E_CUDA;
+    k_fp64_peak<<<blocks, 256, 0, s>>>(buf, iters);
+    mpasg_count_launch();
+    if (cudaGetLastError() != cudaSuccess) rc = MPASG_E_LAUNCH;
+  }
+  if (rc == MPASG_OK && (cudaEventRecord(b, s) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+                         cudaEventElapsedTime(&ms, a, b) != cudaSuccess))
+    rc = MPASG_E_CUDA;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc == MPASG_OK) *flops_per_s = 2.0 * 8.0 * (double)iters * (double)blocks * 256.0 / ((double)ms * 1e-3);
+  return rc;
+}
+
 extern "C" int mpasg_check_finite(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, void* stream) {
   if (!m || !c || !f || !f->status) return MPASG_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
