@@ -257,6 +257,21 @@ int mpasg_autotune(const mpasg_mesh *m, mpasg_config *c, mpasg_fields *f, float 
  * the helpers against CUDA's own conversions and division: which = 0 float64 -> float32 ->
  * float64 through the integer repacking; which = 1 the Newton-Raphson reciprocal. */
 int mpasg_numerics_check(int which, const double *in, double *out, long long n, void *stream);
+/* Vector-Jacobian product of one large step's split scalar transport with explicit
+ * stages (config_monotonic off, dynamics_split_steps >= 2, scalar advection on;
+ * mpas_pytorch/dynamics/advance_scalars.py:1272 composed as time_integration.py:3954-4700):
+ * the step's end scalars are linear in its start scalars given the step's averaged mass
+ * fluxes ruavg (E+1, L) and wwavg (C+1, L+1) and the densities rho_old (at the step's
+ * start) and rho_new (at its end), (C+1, L).  g_out (C+1, L, S) -> g_in (C+1, L, S).
+ * adj_ptr (C+1) / adj_es: the advection stencils transposed -- for cell c, entries
+ * adj_ptr[c] .. adj_ptr[c+1]-1 hold e * nAdvMax + slot of every stencil slot reading c;
+ * edge_cell_w (E, 2): -edgesOnCell_sign * invAreaCell of each edge's two cells (0 for
+ * the padding cell).  work: 3 (C+1) L S + (E+1) L S doubles.  The padding row of g_out passes
+ * through to g_in (the step copies it unchanged).  Deterministic (gathers). */
+int mpasg_transport_vjp(const mpasg_mesh *m, const mpasg_config *c, const double *ruavg,
+                        const double *wwavg, const double *rho_old, const double *rho_new,
+                        const int32_t *adj_ptr, const int32_t *adj_es, const double *edge_cell_w,
+                        const double *g_out, double *g_in, double *work, void *stream);
 /* Float64 arithmetic peak of this GPU, measured: `blocks` x 256 threads each run `iters`
  * rounds of 8 independent fused multiply-adds on values read from buf (blocks * 256
  * doubles, written back so nothing is optimised away); *flops_per_s receives

@@ -136,7 +136,8 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_advance_scalars_static", "mpasg_numerics_check", "mpasg_surface_pressure",
            "mpasg_weighted_sq_sum", "mpasg_sfc_order", "mpasg_edge_order", "mpasg_permute_rows",
            "mpasg_tridiag_solve", "mpasg_tridiag_solve_vjp", "mpasg_tridiag_solve_jvp", "mpasg_tridiag_factor",
-           "mpasg_tridiag_factor_vjp", "mpasg_tridiag_factor_jvp", "mpasg_autotune", "mpasg_fp64_peak")
+           "mpasg_tridiag_factor_vjp", "mpasg_tridiag_factor_jvp", "mpasg_autotune", "mpasg_fp64_peak",
+           "mpasg_transport_vjp")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -179,6 +180,7 @@ def load() -> C.CDLL:
         "mpasg_advance_scalars_static": ([m, c, f, C.c_int, C.c_double, vp], C.c_int),
         "mpasg_numerics_check": ([C.c_int, vp, vp, C.c_longlong, vp], C.c_int),
         "mpasg_fp64_peak": ([vp, C.c_int, C.c_int, vp, vp], C.c_int),
+        "mpasg_transport_vjp": ([m, c] + [vp] * 11, C.c_int),
         "mpasg_surface_pressure": ([C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, vp, vp],
                                    C.c_int),
         "mpasg_weighted_sq_sum": ([C.c_longlong, vp, vp, vp, vp, vp], C.c_int),

@@ -345,6 +345,101 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
     return _merge(initial_state, model.export())
 
 
+def _scalar_derivative_forward(state: Mapping[str, Any], mesh: Mapping[str, Any] | None, kwargs: dict):
+    """Forward run for run_simulation.vjp / .jvp with each step's transport inputs taped."""
+    from .tracer_adjoint import ScalarTape, check_supported
+    unknown = set(kwargs) - {"config", "dt", "nsteps", "device", "differentiable", "checkpoint_timesteps",
+                             "checkpoint_use_reentrant", "checkpoint_materialize_final"}
+    if unknown:
+        raise MpasConfigError(f"unsupported keyword arguments for the derivative runs: {sorted(unknown)}")
+    mesh = mesh if mesh is not None else state
+    merged = dict(mesh)
+    merged.update(state)
+    cfg = resolved_config(kwargs.get("config"))
+    dt = float(cfg["config_dt"] if kwargs.get("dt") is None else kwargs["dt"])
+    nsteps = int(kwargs.get("nsteps", 1))
+    ns = _int(merged.get("num_scalars", _np(merged["scalars"]).shape[-1]))
+    # the Model's defaults: every scalar is a moist species unless moist_end says otherwise
+    ms, me = _int(merged.get("moist_start", 1)), _int(merged.get("moist_end", ns))
+    check_supported(cfg, ms, me)
+    model = Model(merged, cfg, dt, num_scalars=ns, device=kwargs.get("device", "cuda"))
+    if _is_prepared(state):
+        model.load_boundary(state)
+    else:
+        model.prepare(merged)
+    tape = ScalarTape()
+    for _ in range(nsteps):
+        model.step()
+        tape.record(model)
+    bad = model.check_finite()
+    if bad:
+        raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")
+    return model, tape, _merge(state, model.export())
+
+
+def run_simulation_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any], objective: Callable,
+                       track_keys=None, **kwargs) -> dict:
+    """Adjoint of ``run_simulation`` for the transported scalars (the reference's
+    ``run_simulation.vjp``, atmosphere_model.py:2101): d objective(out) / d state["scalars"]
+    through ``nsteps`` steps, computed by the hand-written transposed transport
+    (``mpasg_transport_vjp``).  ``track_keys`` must be ``("scalars",)``; passive scalars
+    with the explicit split transport only (the dynamics do not depend on them)."""
+    from .tracer_adjoint import scalars_vjp
+    keys = tuple(track_keys) if track_keys is not None else None
+    if keys != ("scalars",):
+        raise MpasUnsupportedCapabilityError(
+            "run_simulation.vjp on the GB300 path differentiates with respect to 'scalars' only; "
+            f"pass track_keys=('scalars',) (got {keys})")
+    if "scalars" not in state or not hasattr(state["scalars"], "shape"):
+        raise KeyError("Tracked VJP key 'scalars' is missing from state")
+    model, tape, out = _scalar_derivative_forward(state, mesh, dict(kwargs))
+    leaf = out["scalars"].detach().clone().requires_grad_(True)
+    out = dict(out)
+    out["scalars"] = leaf
+    loss = objective(out)
+    if not isinstance(loss, torch.Tensor):
+        raise TypeError(f"objective must return a tensor, got {type(loss).__name__}")
+    if loss.ndim != 0:
+        raise MpasConfigError("objective must return a scalar tensor")
+    (g_end,) = torch.autograd.grad(loss, [leaf], allow_unused=True)
+    if g_end is None:
+        return {}
+    g0 = scalars_vjp(model, tape, g_end.detach())
+    ref = state["scalars"]
+    g0 = g0[:ref.shape[0]]
+    return {"scalars": g0 if isinstance(ref, torch.Tensor) and ref.device == g0.device else
+            (g0.to(ref.device) if isinstance(ref, torch.Tensor) else g0.cpu())}
+
+
+def run_simulation_jvp(state: Mapping[str, Any], mesh: Mapping[str, Any], perturbation: Mapping[str, Any],
+                       **kwargs) -> dict:
+    """Tangent-linear ``run_simulation`` for the transported scalars (the reference's
+    ``run_simulation.jvp``, atmosphere_model.py:2041): the tangent of the end scalars
+    along ``perturbation["scalars"]``, replayed through each step's recorded transport.
+    Outputs that do not depend on the scalars get no tangent, as in the reference."""
+    from .tracer_adjoint import scalars_jvp
+    if set(perturbation) != {"scalars"}:
+        raise MpasUnsupportedCapabilityError(
+            "run_simulation.jvp on the GB300 path takes a 'scalars' perturbation only "
+            f"(got {sorted(perturbation)})")
+    v = perturbation["scalars"]
+    if not isinstance(v, torch.Tensor):
+        raise TypeError(f"Perturbation 'scalars' must be a tensor, got {type(v).__name__}")
+    ref = state["scalars"]
+    if tuple(v.shape) != tuple(ref.shape):
+        raise MpasConfigError(f"Perturbation 'scalars' has shape {tuple(v.shape)}; expected {tuple(ref.shape)}")
+    model, tape, _ = _scalar_derivative_forward(state, mesh, dict(kwargs))
+    dev = model.dmesh.device
+    full = torch.zeros(model.state.f["scalars"].shape, dtype=torch.float64, device=dev)
+    full[:v.shape[0]] = v.to(device=dev, dtype=torch.float64)
+    t = scalars_jvp(model, tape, full)[:v.shape[0]]
+    return {"scalars": t.to(v.device)}
+
+
+run_simulation.vjp = run_simulation_vjp  # type: ignore[attr-defined]
+run_simulation.jvp = run_simulation_jvp  # type: ignore[attr-defined]
+
+
 def run_timestep(state: Mapping[str, Any], mesh: Mapping[str, Any] | None = None,
                  config: Mapping[str, Any] | None = None, dt: float | None = None,
                  device: str | torch.device = "cuda", differentiable: bool = False) -> dict:

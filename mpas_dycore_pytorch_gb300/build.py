@@ -19,7 +19,8 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libmpasg.so"
-SOURCES = ("kern_column.cu", "kern_tend.cu", "kern_diag.cu", "kern_transport.cu", "driver.cu", "reorder.cu", "kern_adjoint.cu")
+SOURCES = ("kern_column.cu", "kern_tend.cu", "kern_diag.cu", "kern_transport.cu", "driver.cu", "reorder.cu",
+           "kern_adjoint.cu", "kern_transport_adj.cu")
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
 
 

@@ -358,7 +358,9 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
       MARK(rk == 3 && c->monotonic ? MPASG_STAGE_SCALARS_MONO : MPASG_STAGE_SCALARS);
     }
   }
-  if (advect) CHECK_RC(copy(f.scalars, f.scalars_a, ncs, s));
+  // active rows only: the padding row of the scalars passes through the step unchanged,
+  // as in the reference
+  if (advect) CHECK_RC(copy(f.scalars, f.scalars_a, nc * L * S, s));
   MARK(MPASG_STAGE_SPLIT);
   CHECK_RC(mpasgi_reconstruct(m, c, &f, s, true));
   MARK(MPASG_STAGE_RECONSTRUCT);

@@ -138,12 +138,11 @@ def _scalar(v):
     return Ellipsis
 
 
-def run_case(mp, name: str, case: dict) -> None:
+def load_reference_case(mp, case: dict):
+    """The case's raw arrays through the reference's own loader: (state, mesh, config)."""
     import numpy as np
     import torch
 
-    import mpas_pytorch.dynamics.dyn_tend as dyn_tend_mod
-    import mpas_pytorch.dynamics.time_integration as ti
     import mpas_pytorch.ic_loader as icl
     from mpas_dycore_pytorch_gb300.cases import CaseSpec, make_case
 
@@ -172,6 +171,17 @@ def run_case(mp, name: str, case: dict) -> None:
     cfg.update(case["config"])
     cfg["config_dt"] = case["dt"]
     state, meshd = mp.load_initial_state(tmp / "init.nc", tmp / "grid.nc", config=cfg)
+    return state, meshd, cfg
+
+
+def run_case(mp, name: str, case: dict) -> None:
+    import numpy as np
+    import torch
+
+    import mpas_pytorch.dynamics.dyn_tend as dyn_tend_mod
+    import mpas_pytorch.dynamics.time_integration as ti
+
+    state, meshd, cfg = load_reference_case(mp, case)
 
     arrays: dict[str, np.ndarray] = {}
     meta: dict = {"spec": case["spec"], "config": cfg, "dt": case["dt"],

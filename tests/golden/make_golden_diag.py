@@ -11,6 +11,10 @@ through ``torch.autograd.grad``, forward mode through ``torch.autograd.forward_a
 seeded diagonally dominant column systems and writes ``tridiag_ref.npz``.  Imports the
 reference the same way as ``make_golden.py`` (netCDF4 stub).
 
+Also runs the reference's ``run_simulation.vjp`` / ``.jvp`` with respect to the scalars on
+the g2_explicit case (two steps) and writes the weights, tangent and results to
+``scalars_ad_g2.npz``.
+
 Run:  python tests/golden/make_golden_diag.py
 """
 
@@ -30,7 +34,7 @@ from fixtures import CASES, group, load_case  # noqa: E402
 
 
 def main() -> None:
-    make_golden._import_reference()
+    mp = make_golden._import_reference()
     import torch
     from mpas_pytorch.diagnostics import physics_interface_surface_pressure
 
@@ -48,6 +52,24 @@ def main() -> None:
                 zgrid=t(loaded["zgrid"]))
             out[f"{case}/{step}"] = sp.numpy()
     np.savez_compressed(HERE / "sp_g2.npz", **out)
+
+    # the reference's own JVP / VJP of run_simulation with respect to the scalars
+    # (atmosphere_model.py:2041, :2101) on g2_explicit (explicit transport, passive tracer),
+    # two steps: objective = sum(weights * final scalars), seeded weights and tangent
+    ad = {}
+    state, meshd, cfg = make_golden.load_reference_case(mp, make_golden.CASES["g2_explicit"])
+    g = torch.Generator().manual_seed(20261203)
+    sc = state["scalars"]
+    wts = torch.rand(sc.shape, generator=g, dtype=torch.float64)
+    tan = torch.randn(sc.shape, generator=g, dtype=torch.float64)
+    kw = dict(config=cfg, dt=make_golden.CASES["g2_explicit"]["dt"], nsteps=2)
+    grads = mp.run_simulation.vjp(state, meshd, lambda o: (o["scalars"] * wts).sum(), track_keys=("scalars",), **kw)
+    tangents = mp.run_simulation.jvp(state, meshd, {"scalars": tan}, **kw)
+    ad.update({"weights": wts.numpy(), "vjp_scalars": grads["scalars"].detach().numpy(),
+               "tangent": tan.numpy(), "jvp_scalars": tangents["scalars"].detach().numpy(),
+               "jvp_keys": np.array(sorted(tangents))})
+    np.savez_compressed(HERE / "scalars_ad_g2.npz", **ad)
+    print("wrote", HERE / "scalars_ad_g2.npz", sorted(ad))
     print("wrote", HERE / "sp_g2.npz", sorted(out))
 
     from mpas_pytorch.mesh_reordering import apply_rcm_reordering

@@ -40,6 +40,8 @@ def test_two_steps_match_reference(case):
         for k in FIELDS:
             err = rel_l2(to_np(got[k])[:-1], ref[k][:-1])
             assert err <= step_tol(case, k), (step, k, err)
+        # the scalars' padding row passes through the step unchanged, as in the reference
+        assert np.array_equal(to_np(got["scalars"])[-1], ref["scalars"][-1])
 
 
 @pytest.mark.parametrize("case", CASES)

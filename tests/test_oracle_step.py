@@ -42,3 +42,4 @@ def test_two_steps_match_reference(case):
         ref = group(st, f"step{step}")
         for k in FIELDS:
             assert rel_l2(state[k][:-1], ref[k][:-1]) <= step_tol(case, k), (step, k)
+        assert np.array_equal(state["scalars"][-1], ref["scalars"][-1])

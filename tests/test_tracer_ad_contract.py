@@ -1,0 +1,53 @@
+"""Argument contract of run_simulation.vjp / .jvp on the GB300 path (CPU: everything
+here is rejected before any device work)."""
+
+import numpy as np
+import pytest
+import torch
+
+from mpas_dycore_pytorch_gb300.api import run_simulation
+from mpas_dycore_pytorch_gb300.errors import MpasConfigError, MpasUnsupportedCapabilityError
+from fixtures import group, load_case
+
+
+def _case():
+    meta, st, _ = load_case("g2_explicit")
+    state = {k: torch.as_tensor(v) for k, v in group(st, "loaded").items()}
+    state.update(meta["loaded_scalars"])
+    return state, meta
+
+
+def test_vjp_tracks_scalars_only():
+    state, meta = _case()
+    for keys in (None, ("u",), ("scalars", "theta")):
+        with pytest.raises(MpasUnsupportedCapabilityError):
+            run_simulation.vjp(state, state, lambda o: o["scalars"].sum(), track_keys=keys, config=meta["config"])
+
+
+@pytest.mark.parametrize("extra", [{"config_monotonic": True}, {"config_positive_definite": True},
+                                   {"config_split_dynamics_transport": False}, {"config_dynamics_split_steps": 1},
+                                   {"config_scalar_advection": False}])
+def test_unsupported_transport_rejected(extra):
+    state, meta = _case()
+    cfg = dict(meta["config"], **extra)
+    with pytest.raises(MpasUnsupportedCapabilityError):
+        run_simulation.vjp(state, state, lambda o: o["scalars"].sum(), track_keys=("scalars",), config=cfg)
+    with pytest.raises(MpasUnsupportedCapabilityError):
+        run_simulation.jvp(state, state, {"scalars": torch.zeros_like(state["scalars"])}, config=cfg)
+
+
+def test_moist_scalars_rejected():
+    state, meta = _case()
+    state = dict(state, moist_end=1)
+    with pytest.raises(MpasUnsupportedCapabilityError):
+        run_simulation.vjp(state, state, lambda o: o["scalars"].sum(), track_keys=("scalars",), config=meta["config"])
+
+
+def test_jvp_perturbation_contract():
+    state, meta = _case()
+    with pytest.raises(MpasUnsupportedCapabilityError):
+        run_simulation.jvp(state, state, {"u": torch.zeros_like(state["u"])}, config=meta["config"])
+    with pytest.raises(MpasConfigError):
+        run_simulation.jvp(state, state, {"scalars": torch.zeros(3, 2)}, config=meta["config"])
+    with pytest.raises(TypeError):
+        run_simulation.jvp(state, state, {"scalars": np.zeros(3)}, config=meta["config"])
