@@ -274,6 +274,55 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
     return forms
 
 
+def measure_scalar_vjp(args, dev):
+    """The scalar VJP (tracer_adjoint: taped forward + transposed transport, what
+    run_simulation.vjp with track_keys=("scalars",) runs after its setup) on the level-5 x
+    41 mesh (explicit transport, 3 passive tracers, 24 steps at dt 900 s), against the plain
+    forward of the same 24 steps replayed from a CUDA graph; CUDA events on the stream."""
+    import torch
+
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.loader import load_case
+    from mpas_dycore_pytorch_gb300.tracer_adjoint import ScalarTape, scalars_vjp, transport_adjacency
+
+    w = WORKLOADS["c2"]
+    cfg = dict(_cfg(w), config_monotonic=False)
+    st, _ = load_case(CaseSpec(**w["spec"]), cfg, as_torch=False)
+    nsteps = 24
+    S = int(st["scalars"].shape[-1])
+    m = Model(st, cfg, w["dt"], num_scalars=S, device=dev)
+    m.prepare(st)
+    m.step()
+    m.capture_graph()
+    ms_fwd = _time_steps(m.step, nsteps, args.warmup)
+    del m
+    torch.cuda.empty_cache()
+    m = Model(st, cfg, w["dt"], num_scalars=S, device=dev)
+    transport_adjacency(m.dmesh)  # host-built once per mesh
+    g_end = torch.rand(m.state.f["scalars"].shape, dtype=torch.float64, device=dev)
+    ms = []
+    for rep in range(2):  # the second repetition is timed
+        m.prepare(st)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        tape = ScalarTape()
+        for _ in range(nsteps):
+            m.step()
+            tape.record(m)
+        g0 = scalars_vjp(m, tape, g_end)
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    cl = st_cells_levels(st)
+    return {"workload": "level-5 mesh 10242 cells x 41 levels, 3 passive tracers, explicit transport, 24 steps",
+            "value": cl * nsteps / (ms[-1] / 1e3), "unit": UNIT, "ms": ms[-1],
+            "forward_graph_ms": ms_fwd * nsteps, "vjp_over_forward": ms[-1] / (ms_fwd * nsteps),
+            "includes": "24 eager forward steps with the transport tape, then the transposed transport of each step",
+            "gradient_finite": bool(torch.isfinite(g0).all())}
+
+
 def measure_ensemble_groups(args, dev):
     """The two-grid mixed-precision ensemble: 96 members of 10242 cells x 41 levels (dt
     900 s) and 32 members of 40962 cells x 55 stretched levels (dt 720 s), 2 monotone
@@ -548,6 +597,7 @@ def run_gb300(args, rank, world):
         del model, host
         torch.cuda.empty_cache()
         forms = measure_forms(args, dev, st, cfg, w, ms / K)
+        forms["vjp_scalars"] = measure_scalar_vjp(args, dev)
         if args.ensemble_groups:
             forms["batched_two_grids"] = measure_ensemble_groups(args, dev)
 
