@@ -195,6 +195,16 @@ def _time_steps(step, K, W):
     return a.elapsed_time(b) / K
 
 
+def _tune(model, args):
+    """The autotuner, or a fixed tile (--tile 1/2/4: profiling runs, where ncu's serialised
+    replay would distort the tuner's own timings)."""
+    if args.tile == "auto":
+        return model.autotune()
+    model.cstruct.tile_tend_u = int(args.tile)
+    model._graph = None
+    return {"tend_u_levels_per_thread": int(args.tile), "tend_u_ms": None, "fixed": True}
+
+
 def _graph_model(model):
     model.step()  # eager first step (shared-memory opt-ins happen before capture)
     model.capture_graph()
@@ -221,7 +231,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
     for prec in ("float64", "mixed"):
         m = Model(st, cfg, w["dt"], num_scalars=S, device=dev, precision=prec, order=args.order)
         m.prepare(st)
-        tune = m.autotune()
+        tune = _tune(m, args)
         _graph_model(m)
         for _ in range(nerr - 1):
             m.step()
@@ -251,7 +261,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
             spec, ecfg, as_torch=False)
         m = Model(single, ecfg, ew["dt"], num_scalars=S, device=dev, order=args.order)
         m.prepare(single)
-        m.autotune()
+        _tune(m, args)
         ms_single = _time_steps(_graph_model(m).step, K, W)
         cl1 = st_cells_levels(single)
         del m
@@ -259,7 +269,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
         members = member_cases(spec, seeds=list(range(100, 100 + args.ensemble)), config=ecfg, u_noise=0.5)
         for prec in ("float64", "mixed"):
             ens = Ensemble(members, ecfg, ew["dt"], precision=prec, device=dev, order=args.order)
-            etune = ens.model.autotune()
+            etune = _tune(ens.model, args)
             _graph_model(ens.model)
             ms_e = _time_steps(ens.step, K, W)
             bad = ens.model.check_finite()
@@ -351,7 +361,7 @@ def measure_ensemble_groups(args, dev):
     for m0, cfg, dt in firsts:
         solo = Model(m0, cfg, dt, num_scalars=2, device=dev, order=args.order)
         solo.prepare(m0)
-        solo.autotune()
+        _tune(solo, args)
         solo.capture_graph()
         for _ in range(nerr):
             solo.step()
@@ -362,7 +372,7 @@ def measure_ensemble_groups(args, dev):
         del solo
         torch.cuda.empty_cache()
     ens = EnsembleGroups(groups, precision="mixed", device=dev, order=args.order)
-    tune = ens.autotune()
+    tune = [_tune(g.model, args) for g in ens.groups]
     ens.capture_graph()
     for _ in range(nerr):
         ens.step()
@@ -457,7 +467,7 @@ def run_gb300(args, rank, world):
     S = int(st["scalars"].shape[-1])
     model = Model(st, cfg, w["dt"], num_scalars=S, device=dev, precision=args.precision, order=args.order)
     model.prepare(st)
-    tuning = model.autotune()
+    tuning = _tune(model, args)
     C_, L_ = model.dmesh.nCells, model.dmesh.nVertLevels
     lib = model.lib
     # launches per step (eager step, counted by the library)
@@ -657,6 +667,8 @@ def main():
     ap.add_argument("--order", default="sfc", choices=("native", "sfc"),
                     help="mesh order on the device: generator order or Hilbert curve")
     ap.add_argument("--ensemble", type=int, default=96, help="members of the batched level-5 ensemble (0: skip)")
+    ap.add_argument("--tile", default="auto", choices=("auto", "1", "2", "4"),
+                    help="levels per thread of the u tendency: autotuned, or fixed (profiling)")
     ap.add_argument("--ensemble-groups", action="store_true",
                     help="also run the two-grid mixed ensemble (96 x 10242x41 + 32 x 40962x55, ~200 GB)")
     args = ap.parse_args()

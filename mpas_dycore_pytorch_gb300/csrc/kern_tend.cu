@@ -39,7 +39,7 @@ MPASG_D double cam_kdiff(double kd, const TendScalars& p, uint32_t k, int L) {
   return fmax(kd, p.cam_base * factor);
 }
 
-template <typename T>
+template <typename T, bool CAM = false>
 __global__ void k_tend_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendScalars p) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -78,10 +78,10 @@ __global__ void k_tend_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendSca
       dof = ndo;
     }
     double kd = f64(vmin(cv<T>(p.c_s_len2) * vsqrt(dd * dd + dof * dof), cv<T>(p.kdiff_cap)));
-    if (p.ncam > 0 && (int)k >= L - p.ncam) kd = cam_kdiff(kd, p, k, L);
+    if (CAM && (int)k >= L - p.ncam) kd = cam_kdiff(kd, p, k, L);
     f.kdiff[i] = kd;
   } else {  // 2d_fixed: the theta del2 coefficient everywhere
-    f.kdiff[i] = (p.ncam > 0 && (int)k >= L - p.ncam) ? cam_kdiff(p.visc2, p, k, L) : p.visc2;
+    f.kdiff[i] = (CAM && (int)k >= L - p.ncam) ? cam_kdiff(p.visc2, p, k, L) : p.visc2;
   }
 }
 
@@ -102,7 +102,9 @@ MPASG_D T wduz_at(const T* __restrict__ u, T rwe, int kk, int L, const T* fzm, c
   return flux3<T>(u[kk - 2], u[kk - 1], u[kk], u[kk + 1], rwe, T(1));
 }
 
-template <typename T>
+// RAY: Rayleigh damping of u compiled in (a run-time test would cost float64 work in
+// every thread of the hot kernel once the compiler predicates it)
+template <typename T, bool RAY = false>
 __global__ void __launch_bounds__(kBlock) k_tend_u(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendScalars p) {
   __shared__ T s_wd[kBlock];
   const int L = m.nVertLevels;
@@ -159,7 +161,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_u(mpasg_mesh m, mpasg_fields f,
   const T rho_e = cv<T>(f.h_edge[i]);
   tu = tu + rho_e * (q - dif<T>(f.ke[i2], f.ke[i1]) * inv_dc) -
        ue[k] * T(0.5) * (cv<T>(f.h_divergence[i1]) + cv<T>(f.h_divergence[i2]));
-  tu = rayleigh_u<T>(tu, rho_e, ue[k], (int)k, L, p);
+  if (RAY) tu = rayleigh_u<T>(tu, rho_e, ue[k], (int)k, L, p);
   if (p.rk_step == 1) {
     const T* zz = G(zz);
     T teu = -cv<T>(f.cqu_e[i]) * (div_or_one<T>(dif<T>(f.pressure_p[i2], f.pressure_p[i1]) * inv_dc,
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_u(mpasg_mesh m, mpasg_fields f,
 // top one again by the next chunk).  Per level, the same expressions in the same order as
 // k_tend_u; the compiler may fuse multiply-adds differently in the two kernels, so the
 // tiles agree to the rounding of one FMA (last bit).
-template <typename T, int V>
+template <typename T, int V, bool RAY = false>
 __global__ void __launch_bounds__(kBlock) k_tend_u_chunk(mpasg_mesh m, mpasg_fields f, FastDiv flc, int nchunk,
                                                          TendScalars p) {
   const int L = m.nVertLevels;
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_u_chunk(mpasg_mesh m, mpasg_fie
     const T rho_e = cv<T>(f.h_edge[ie]);
     tu = tu + rho_e * (qv - dif<T>(f.ke[i2], f.ke[i1]) * inv_dc) -
          ue[k] * T(0.5) * (cv<T>(f.h_divergence[i1]) + cv<T>(f.h_divergence[i2]));
-    tu = rayleigh_u<T>(tu, rho_e, ue[k], k, L, p);
+    if (RAY) tu = rayleigh_u<T>(tu, rho_e, ue[k], k, L, p);
     if (p.rk_step == 1) {
       const T* zz = G(zz);
       T teu = -cv<T>(f.cqu_e[ie]) * (div_or_one<T>(dif<T>(f.pressure_p[i2], f.pressure_p[i1]) * inv_dc,
@@ -779,18 +781,26 @@ int launch_dyn_tend(const mpasg_mesh* m, mpasg_fields* f, const TendScalars& p, 
     k_theta_dev<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl);
     MPASG_LAUNCH_CHECK();
   }
-  k_tend_cells_a<T><<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, p);
+  if (p.ncam > 0 && rk_step == 1)
+    k_tend_cells_a<T, true><<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, p);
+  else
+    k_tend_cells_a<T><<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, p);
   MPASG_LAUNCH_CHECK();
   const int vt = tile_levels(c_tile);  // levels per thread of k_tend_u (autotuner choice)
+  const bool ray = p.ray_n > 0;
   if (vt == 1) {
-    k_tend_u<T><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, p);
+    if (ray) k_tend_u<T, true><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, p);
+    else k_tend_u<T><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, p);
   } else {
     const int nchunk = (L + vt - 1) / vt;
     const long long nth = (long long)m->nEdges * nchunk;
-    if (vt == 2)
-      k_tend_u_chunk<T, 2><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
-    else
-      k_tend_u_chunk<T, 4><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+    if (vt == 2) {
+      if (ray) k_tend_u_chunk<T, 2, true><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+      else k_tend_u_chunk<T, 2><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+    } else {
+      if (ray) k_tend_u_chunk<T, 4, true><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+      else k_tend_u_chunk<T, 4><<<nblocks(nth), kBlock, 0, s>>>(*m, *f, FastDiv(nchunk), nchunk, p);
+    }
   }
   MPASG_LAUNCH_CHECK();
   if (rk_step == 1) {
