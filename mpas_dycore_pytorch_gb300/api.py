@@ -51,19 +51,87 @@ def resolved_config(config: Mapping[str, Any] | None) -> dict:
     return cfg
 
 
+_TRUE = {"1", "true", "t", "yes", "y", "on", ".true.", ".t."}
+_FALSE = {"0", "false", "f", "no", "n", "off", "", ".false.", ".f."}
+# logical namelist switches whose true value asks for a mode outside the dycore
+# (restart, data assimilation, surface updates, decomposition, regional boundaries)
+_UNSUPPORTED_SWITCHES = ("config_do_restart", "config_do_DAcycling", "config_jedi_da", "config_sst_update",
+                         "config_sstdiurn_update", "config_deepsoiltemp_update", "config_explicit_proc_decomp",
+                         "config_apply_lbcs", "config_enable_sharding")
+
+
+def _logical(value: Any, key: str) -> bool:
+    """A namelist logical: Python / numpy / torch booleans and numbers, or Fortran-style
+    strings ("true", ".true.", "t", "off", ...); anything else is a configuration error."""
+    if hasattr(value, "item") and callable(value.item):
+        value = value.item()
+    if isinstance(value, str):
+        v = value.strip().lower()
+        if v in _TRUE:
+            return True
+        if v in _FALSE:
+            return False
+        raise MpasConfigError(f"{key}: expected a logical value, got {value!r}")
+    return bool(value)
+
+
+def _flag(cfg: Mapping[str, Any], key: str) -> bool:
+    return _logical(cfg[key], key)
+
+
+def active_unsupported_settings(cfg: Mapping[str, Any]) -> list[str]:
+    """Keys of ``cfg`` that request a mode this path does not run (a physics suite, a
+    physics scheme, IAU, restart / assimilation / surface-update switches, sharding,
+    regional boundaries), with the reference's reading of their values
+    (namelist_metadata.py:76-106)."""
+    bad = []
+    norm = lambda v: str(v).strip().lower()
+    if norm(cfg.get("config_physics_suite", "none")) not in ("", "none", "off"):
+        bad.append("config_physics_suite")
+    if norm(cfg.get("config_IAU_option", "off")) not in ("", "off", "none"):
+        bad.append("config_IAU_option")
+    for key in _UNSUPPORTED_SWITCHES:
+        short = key[len("config_"):]
+        if key in cfg or short in cfg:
+            if _logical(cfg[key] if key in cfg else cfg[short], key):
+                bad.append(key)
+    for key in sorted(cfg):
+        if isinstance(key, str) and key.startswith("config_") and key.endswith("_scheme") and \
+                norm(cfg[key]) not in ("", "none", "off"):
+            bad.append(key)
+    return bad
+
+
+def reject_unsupported_request(state: Mapping[str, Any] | None, mesh: Mapping[str, Any] | None,
+                               config: Mapping[str, Any] | None) -> None:
+    """The public routes' first check, before any preparation or device work: unsupported
+    modes and reduced-precision float storage (the reference's
+    tests/test_configuration_contracts.py:48-80 contract)."""
+    bad = active_unsupported_settings(config or {})
+    if bad:
+        raise MpasUnsupportedCapabilityError(f"unsupported active MPAS settings on the GB300 path: {bad}")
+    for where, d in (("state", state), ("mesh", mesh)):
+        for key, v in (d or {}).items():
+            dt = getattr(v, "dtype", None)
+            if dt is None:
+                continue
+            if dt in (torch.float32, torch.float16, torch.bfloat16) or \
+                    (isinstance(dt, np.dtype) and dt.kind == "f" and dt.itemsize < 8):
+                raise MpasUnsupportedCapabilityError(
+                    f"{where}[{key!r}] has dtype {dt}; the GB300 path takes float64 storage "
+                    "(config_precision selects the arithmetic)")
+
+
 def validate_supported(cfg: Mapping[str, Any]) -> None:
     """Reject options outside the implemented path before any device work (mirrors the
     reference's capability rejection, tests/test_configuration_contracts.py:48-79)."""
-    bad = []
+    bad = active_unsupported_settings(cfg)
     if int(cfg["config_dynamics_split_steps"]) < 1:
         bad.append("config_dynamics_split_steps < 1")
     if int(cfg["config_time_integration_order"]) not in (2, 3):
         bad.append("config_time_integration_order")
-    for key in ("config_curvature_u", "config_apply_lbcs"):
-        if bool(cfg[key]):
-            bad.append(key)
-    if str(cfg["config_IAU_option"]) != "off":
-        bad.append("config_IAU_option")
+    if _flag(cfg, "config_curvature_u"):
+        bad.append("config_curvature_u")
     if str(cfg["config_horiz_mixing"]) not in ("2d_smagorinsky", "2d_fixed"):
         bad.append("config_horiz_mixing")
     if str(cfg["config_precision"]) not in _lib.PRECISIONS:
@@ -101,10 +169,10 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
     c.number_of_sub_steps = int(cfg["config_number_of_sub_steps"])
     # split transport off is one dynamics substep with the scalars inside the RK stages
     # (the reference's _resolve_dynamics_split, time_integration.py:1809-1878)
-    c.dynamics_split_steps = int(cfg["config_dynamics_split_steps"]) if bool(cfg["config_split_dynamics_transport"]) else 1
+    c.dynamics_split_steps = int(cfg["config_dynamics_split_steps"]) if _flag(cfg, "config_split_dynamics_transport") else 1
     # the positive-definite option selects the same limited final transport stage
     # (time_integration.py:3979-3987)
-    c.monotonic = 1 if (bool(cfg["config_monotonic"]) or bool(cfg["config_positive_definite"])) else 0
+    c.monotonic = 1 if (_flag(cfg, "config_monotonic") or _flag(cfg, "config_positive_definite")) else 0
     c.horiz_mixing_smagorinsky = 1 if str(cfg["config_horiz_mixing"]) == "2d_smagorinsky" else 0
     c.num_scalars = int(num_scalars)
     c.moist_start = int(moist_start)
@@ -115,10 +183,10 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
     c.v_theta_eddy_visc2 = float(cfg["config_v_theta_eddy_visc2"])
     c.mpas_cam_coef = float(cfg["config_mpas_cam_coef"])
     c.number_cam_damping_levels = int(cfg["config_number_cam_damping_levels"])
-    c.scalar_advection_off = 0 if bool(cfg["config_scalar_advection"]) else 1
+    c.scalar_advection_off = 0 if _flag(cfg, "config_scalar_advection") else 1
     c.rayleigh_damp_u_timescale_days = float(cfg["config_rayleigh_damp_u_timescale_days"])
-    c.rayleigh_damp_u_levels = int(cfg["config_number_rayleigh_damp_u_levels"]) if bool(cfg["config_rayleigh_damp_u"]) else 0
-    c.mix_perturbation = 0 if bool(cfg["config_mix_full"]) else 1
+    c.rayleigh_damp_u_levels = int(cfg["config_number_rayleigh_damp_u_levels"]) if _flag(cfg, "config_rayleigh_damp_u") else 0
+    c.mix_perturbation = 0 if _flag(cfg, "config_mix_full") else 1
     return c
 
 
@@ -292,8 +360,11 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
     complete step boundary returned by a previous call.  Returns the final boundary with
     the reference's keys; tensors stay on the CUDA device.
     """
+    reject_unsupported_request(initial_state, mesh, config)
     if differentiable:
-        raise MpasUnsupportedCapabilityError("differentiable runs are not implemented on the GB300 path")
+        raise MpasUnsupportedCapabilityError(
+            "differentiable=True runs are not implemented on the GB300 path; run_simulation.vjp / .jvp "
+            "differentiate with respect to the transported scalars")
     if int(nsteps) != nsteps or nsteps < 0:
         raise MpasConfigError("nsteps must be a non-negative integer")
     mesh = mesh if mesh is not None else initial_state
@@ -303,7 +374,7 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
     dt = float(cfg["config_dt"] if dt is None else dt)
     if nsteps == 0:
         return dict(initial_state)
-    if bool(cfg.get("config_mesh_reordering_rcm", False)) and not merged.get("_rcm_applied", False):
+    if _flag(cfg, "config_mesh_reordering_rcm") and not merged.get("_rcm_applied", False):
         # the reference reorders state and mesh and updates the caller's mesh in place
         # (atmosphere_model.py:810-827); results come back in the RCM order
         from .reorder import apply_rcm_reordering
@@ -385,6 +456,7 @@ def run_simulation_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any], object
     (``mpasg_transport_vjp``).  ``track_keys`` must be ``("scalars",)``; passive scalars
     with the explicit split transport only (the dynamics do not depend on them)."""
     from .tracer_adjoint import scalars_vjp
+    reject_unsupported_request(state, mesh, kwargs.get("config"))
     keys = tuple(track_keys) if track_keys is not None else None
     if keys != ("scalars",):
         raise MpasUnsupportedCapabilityError(
@@ -418,6 +490,7 @@ def run_simulation_jvp(state: Mapping[str, Any], mesh: Mapping[str, Any], pertur
     along ``perturbation["scalars"]``, replayed through each step's recorded transport.
     Outputs that do not depend on the scalars get no tangent, as in the reference."""
     from .tracer_adjoint import scalars_jvp
+    reject_unsupported_request(state, mesh, kwargs.get("config"))
     if set(perturbation) != {"scalars"}:
         raise MpasUnsupportedCapabilityError(
             "run_simulation.jvp on the GB300 path takes a 'scalars' perturbation only "

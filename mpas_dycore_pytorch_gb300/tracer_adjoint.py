@@ -36,12 +36,13 @@ def _p(t: torch.Tensor) -> C.c_void_p:
 
 
 def check_supported(cfg: Mapping[str, Any], moist_start: int, moist_end: int) -> None:
+    from .api import _flag
     bad = []
-    if bool(cfg["config_monotonic"]) or bool(cfg["config_positive_definite"]):
+    if _flag(cfg, "config_monotonic") or _flag(cfg, "config_positive_definite"):
         bad.append("the monotone limiter (config_monotonic / config_positive_definite)")
-    if not bool(cfg["config_split_dynamics_transport"]) or int(cfg["config_dynamics_split_steps"]) < 2:
+    if not _flag(cfg, "config_split_dynamics_transport") or int(cfg["config_dynamics_split_steps"]) < 2:
         bad.append("coupled transport")
-    if not bool(cfg["config_scalar_advection"]):
+    if not _flag(cfg, "config_scalar_advection"):
         bad.append("config_scalar_advection = false")
     if moist_end >= moist_start:
         bad.append("moist scalars (their derivatives run through the dynamics)")
