@@ -122,6 +122,22 @@ def reject_unsupported_request(state: Mapping[str, Any] | None, mesh: Mapping[st
                     "(config_precision selects the arithmetic)")
 
 
+FINITE_CHECK_KEYS = ("u", "w", "theta", "rho", "theta_m", "rho_zz", "scalars", "qv", "rho_base", "theta_base",
+                     "zz", "pressure_p", "pressure_base")
+
+
+def require_finite_inputs(state: Mapping[str, Any], context: str = "initial state") -> None:
+    """Reject non-finite model fields before any work (the reference's check,
+    atmosphere_model.py:77-94), as MpasNumericalError (an MpasConfigError)."""
+    for name in FINITE_CHECK_KEYS:
+        v = state.get(name)
+        if isinstance(v, torch.Tensor):
+            if v.is_floating_point() and not bool(torch.isfinite(v).all()):
+                raise MpasNumericalError(f"{context}: {name} contains nonfinite values")
+        elif isinstance(v, np.ndarray) and v.dtype.kind == "f" and not np.all(np.isfinite(v)):
+            raise MpasNumericalError(f"{context}: {name} contains nonfinite values")
+
+
 def validate_supported(cfg: Mapping[str, Any]) -> None:
     """Reject options outside the implemented path before any device work (mirrors the
     reference's capability rejection, tests/test_configuration_contracts.py:48-79)."""
@@ -361,6 +377,7 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
     the reference's keys; tensors stay on the CUDA device.
     """
     reject_unsupported_request(initial_state, mesh, config)
+    require_finite_inputs(initial_state)
     if differentiable:
         raise MpasUnsupportedCapabilityError(
             "differentiable=True runs are not implemented on the GB300 path; run_simulation.vjp / .jvp "

@@ -66,3 +66,12 @@ def test_inactive_values_pass():
 def test_ambiguous_logical_is_a_config_error():
     with pytest.raises(MpasConfigError):
         active_unsupported_settings({"config_jedi_da": "maybe"})
+
+
+@pytest.mark.parametrize("key", ["u", "theta", "scalars"])
+def test_nonfinite_inputs_rejected_first(key):
+    state = {"u": torch.ones((2, 1), dtype=torch.float64), "theta": torch.ones((2, 1), dtype=torch.float64),
+             "scalars": torch.ones((2, 1, 1), dtype=torch.float64)}
+    state[key][0] = float("nan")
+    with pytest.raises(MpasConfigError, match="nonfinite"):
+        gb.run_simulation(state, {}, config={}, nsteps=1)
