@@ -430,12 +430,15 @@ __global__ void __launch_bounds__(kBlock) k_ac_post_mixed(mpasg_mesh m, mpasg_fi
 // columns; the block's x, a, alpha and gamma are loaded and stored with coalesced
 // accesses (consecutive threads read consecutive levels of a column) into a [level][33]
 // layout, so the sequential sweeps read shared memory instead of waiting on one global
-// load per level.  Same arithmetic as k_ac_thomas.
+// load per level.  The staging runs on all kThomasThreads threads (4 warps, 4x the loads
+// in flight: the copy, not the sweep, bounded the one-warp version), the sweeps on the
+// first warp.  Same arithmetic as k_ac_thomas.
 constexpr int kThomasCols = 32;
 constexpr int kThomasPitch = kThomasCols + 1;
+constexpr int kThomasThreads = 128;
 
-__global__ void __launch_bounds__(kThomasCols) k_ac_thomas_staged(mpasg_mesh m, mpasg_fields f, FastDiv fl,
-                                                                  FastDiv fl1) {
+__global__ void __launch_bounds__(kThomasThreads) k_ac_thomas_staged(mpasg_mesh m, mpasg_fields f, FastDiv fl,
+                                                                     FastDiv fl1) {
   extern __shared__ double s_col[];
   const int L = m.nVertLevels;
   double* sx = s_col;                              // (L+1) x pitch
@@ -448,17 +451,17 @@ __global__ void __launch_bounds__(kThomasCols) k_ac_thomas_staged(mpasg_mesh m, 
   const uint32_t nw = (uint32_t)ncol * (L + 1), nl = (uint32_t)ncol * L;
   const double* gx = f.ac_x + (size_t)c0 * (L + 1);
   const size_t o0 = (size_t)c0 * L;
-  for (uint32_t idx = t; idx < nw; idx += kThomasCols) {
+  for (uint32_t idx = t; idx < nw; idx += kThomasThreads) {
     uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
     sx[k * kThomasPitch + col] = gx[idx];
   }
-  for (uint32_t idx = t; idx < nl; idx += kThomasCols) {
+  for (uint32_t idx = t; idx < nl; idx += kThomasThreads) {
     uint32_t col = fl.div(idx), k = idx - col * L;
     sa[k * kThomasPitch + col] = f.a_tri[o0 + idx];
     sal[k * kThomasPitch + col] = f.alpha_tri[o0 + idx];
     sg[k * kThomasPitch + col] = f.gamma_tri[o0 + idx];
   }
-  __syncwarp();
+  __syncthreads();
   if (t < ncol) {
     double xp = sx[t];
     for (int k = 1; k < L; ++k) {
@@ -471,9 +474,9 @@ __global__ void __launch_bounds__(kThomasCols) k_ac_thomas_staged(mpasg_mesh m, 
       sx[k * kThomasPitch + t] = xn;
     }
   }
-  __syncwarp();
+  __syncthreads();
   double* gxo = f.ac_x + (size_t)c0 * (L + 1);
-  for (uint32_t idx = t; idx < nw; idx += kThomasCols) {
+  for (uint32_t idx = t; idx < nw; idx += kThomasThreads) {
     uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
     gxo[idx] = sx[k * kThomasPitch + col];
   }
@@ -482,8 +485,8 @@ __global__ void __launch_bounds__(kThomasCols) k_ac_thomas_staged(mpasg_mesh m, 
 // Mixed form (still float64): u_k = alpha_k x_k + m_k u_(k-1) with m_k = -alpha_k a_k
 // precomputed by the factorisation, so the serial dependence is one FMA per level
 // (alpha_k x_k does not depend on the chain and issues ahead).
-__global__ void __launch_bounds__(kThomasCols) k_ac_thomas_staged_mixed(mpasg_mesh m, mpasg_fields f, FastDiv fl,
-                                                                        FastDiv fl1) {
+__global__ void __launch_bounds__(kThomasThreads) k_ac_thomas_staged_mixed(mpasg_mesh m, mpasg_fields f,
+                                                                           FastDiv fl, FastDiv fl1) {
   extern __shared__ double s_col[];
   const int L = m.nVertLevels;
   double* sx = s_col;
@@ -496,17 +499,17 @@ __global__ void __launch_bounds__(kThomasCols) k_ac_thomas_staged_mixed(mpasg_me
   const uint32_t nw = (uint32_t)ncol * (L + 1), nl = (uint32_t)ncol * L;
   const double* gx = f.ac_x + (size_t)c0 * (L + 1);
   const size_t o0 = (size_t)c0 * L;
-  for (uint32_t idx = t; idx < nw; idx += kThomasCols) {
+  for (uint32_t idx = t; idx < nw; idx += kThomasThreads) {
     uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
     sx[k * kThomasPitch + col] = gx[idx];
   }
-  for (uint32_t idx = t; idx < nl; idx += kThomasCols) {
+  for (uint32_t idx = t; idx < nl; idx += kThomasThreads) {
     uint32_t col = fl.div(idx), k = idx - col * L;
     sm[k * kThomasPitch + col] = f.tri_m[o0 + idx];
     sal[k * kThomasPitch + col] = f.alpha_tri[o0 + idx];
     sg[k * kThomasPitch + col] = f.gamma_tri[o0 + idx];
   }
-  __syncwarp();
+  __syncthreads();
   if (t < ncol) {
     double xp = sx[t];
     for (int k = 1; k < L; ++k) {
@@ -519,13 +522,61 @@ __global__ void __launch_bounds__(kThomasCols) k_ac_thomas_staged_mixed(mpasg_me
       sx[k * kThomasPitch + t] = xn;
     }
   }
-  __syncwarp();
+  __syncthreads();
   double* gxo = f.ac_x + (size_t)c0 * (L + 1);
-  for (uint32_t idx = t; idx < nw; idx += kThomasCols) {
+  for (uint32_t idx = t; idx < nw; idx += kThomasThreads) {
     uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
     gxo[idx] = sx[k * kThomasPitch + col];
   }
 }
+
+// Thomas factorisation (k_vimp_factor) with the columns staged the same way: a, b, c in
+// and alpha, gamma (and the mixed form's tri_m) out through a [level][33] layout with
+// coalesced copies by 4 warps; the division chain of each column runs on the first warp
+// from shared memory.  Same arithmetic as k_vimp_factor.
+template <typename T>
+__global__ void __launch_bounds__(kThomasThreads) k_vimp_factor_staged(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
+  extern __shared__ double s_col[];
+  const int L = m.nVertLevels;
+  double* sa = s_col;  // L x pitch each
+  double* sb = sa + (size_t)L * kThomasPitch;
+  double* sc = sb + (size_t)L * kThomasPitch;
+  double* sal = sc + (size_t)L * kThomasPitch;
+  double* sg = sal + (size_t)L * kThomasPitch;
+  const int c0 = blockIdx.x * kThomasCols;
+  const int ncol = min(kThomasCols, m.nCells - c0);
+  const int t = threadIdx.x;
+  const uint32_t nl = (uint32_t)ncol * L;
+  const size_t o0 = (size_t)c0 * L;
+  for (uint32_t idx = t; idx < nl; idx += kThomasThreads) {
+    uint32_t col = fl.div(idx), k = idx - col * L;
+    sa[k * kThomasPitch + col] = f.a_tri[o0 + idx];
+    sb[k * kThomasPitch + col] = f.b_tri[o0 + idx];
+    sc[k * kThomasPitch + col] = f.c_tri[o0 + idx];
+  }
+  __syncthreads();
+  if (t < ncol) {
+    double gam = 0.0;
+    sal[t] = 0.0;
+    sg[t] = 0.0;
+    for (int k = 1; k < L; ++k) {
+      const double alpha = fdiv<T>(1.0, sb[k * kThomasPitch + t] - sa[k * kThomasPitch + t] * gam);
+      gam = sc[k * kThomasPitch + t] * alpha;
+      sal[k * kThomasPitch + t] = alpha;
+      sg[k * kThomasPitch + t] = gam;
+    }
+  }
+  __syncthreads();
+  for (uint32_t idx = t; idx < nl; idx += kThomasThreads) {
+    uint32_t col = fl.div(idx), k = idx - col * L;
+    const double alpha = sal[k * kThomasPitch + col];
+    f.alpha_tri[o0 + idx] = alpha;
+    f.gamma_tri[o0 + idx] = sg[k * kThomasPitch + col];
+    if (sizeof(T) != sizeof(double) && k > 0) f.tri_m[o0 + idx] = -(alpha * sa[k * kThomasPitch + col]);
+  }
+}
+
+size_t vimp_factor_smem_bytes(int L) { return (size_t)5 * L * kThomasPitch * sizeof(double); }
 
 // tri_m = -alpha_tri * a_tri (the mixed forward-sweep factor) from the stored factors
 __global__ void k_tri_m(long long n, const double* __restrict__ a, const double* __restrict__ al,
@@ -809,14 +860,29 @@ extern "C" int mpasg_vert_imp_coefs(const mpasg_mesh* m, const mpasg_config* c, 
   if (!m || !c || !f) return MPASG_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const int L = m->nVertLevels;
+  // the staged factorisation needs more than 48 KB of dynamic shared memory: opt in once
+  // per device (the first call on a device should come before any stream capture)
+  const size_t smem = vimp_factor_smem_bytes(L);
+  static bool smem_opt_in[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MPASG_E_CUDA;
+  if (!smem_opt_in[dev])
+    smem_opt_in[dev] = cudaFuncSetAttribute(k_vimp_factor_staged<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            200 * 1024) == cudaSuccess &&
+                       cudaFuncSetAttribute(k_vimp_factor_staged<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            200 * 1024) == cudaSuccess;
+  const bool staged = smem_opt_in[dev] && smem <= 200 * 1024;
+  const int nblk = nblocks(m->nCells, kThomasCols);
   if (c->precision == MPASG_PRECISION_MIXED) {
     k_vimp_coefs<float><<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), dts, c->epssm);
     MPASG_LAUNCH_CHECK();
-    k_vimp_factor<float><<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
+    if (staged) k_vimp_factor_staged<float><<<nblk, kThomasThreads, smem, s>>>(*m, *f, FastDiv(L));
+    else k_vimp_factor<float><<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
   } else {
     k_vimp_coefs<double><<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), dts, c->epssm);
     MPASG_LAUNCH_CHECK();
-    k_vimp_factor<double><<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
+    if (staged) k_vimp_factor_staged<double><<<nblk, kThomasThreads, smem, s>>>(*m, *f, FastDiv(L));
+    else k_vimp_factor<double><<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f);
   }
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
@@ -870,10 +936,10 @@ int mpasgi_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_field
         cudaFuncSetAttribute(k_ac_thomas_staged_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
             cudaSuccess;
   if (smem_opt_in[dev] && smem <= 200 * 1024 && mixed)
-    k_ac_thomas_staged_mixed<<<nblocks(m->nCells, kThomasCols), kThomasCols, smem, s>>>(*m, *f, FastDiv(L),
+    k_ac_thomas_staged_mixed<<<nblocks(m->nCells, kThomasCols), kThomasThreads, smem, s>>>(*m, *f, FastDiv(L),
                                                                                         FastDiv(L + 1));
   else if (smem_opt_in[dev] && smem <= 200 * 1024)
-    k_ac_thomas_staged<<<nblocks(m->nCells, kThomasCols), kThomasCols, smem, s>>>(*m, *f, FastDiv(L),
+    k_ac_thomas_staged<<<nblocks(m->nCells, kThomasCols), kThomasThreads, smem, s>>>(*m, *f, FastDiv(L),
                                                                                   FastDiv(L + 1));
   else if (mixed)
     return MPASG_E_ARG;  // the mixed sweep needs the staged kernel (L <= 200)
