@@ -114,6 +114,9 @@ typedef struct mpasg_mesh {
   /* initial profiles read by config_mix_full = false: u_init, v_init (L), angleEdge (E+1),
    * t_init (C+1, L) */
   const double *u_init, *v_init, *angleEdge, *t_init;
+  /* (C+1, maxEdges): edgesOnCell_sign * dvEdge * invAreaCell of every cell's edge slots
+   * (the divergence weight of the acoustic flux sums) */
+  const double *cell_edge_geo;
 } mpasg_mesh;
 
 /* Namelist options the step consumes (validated on the host). */
@@ -207,6 +210,7 @@ typedef struct mpasg_fields {
   double *ac_x;                                                     /* (C+1, L+1) */
   double *b_tri, *c_tri;                                            /* (C+1, L) */
   double *tri_m;        /* (C+1, L) mixed form: -alpha_tri * a_tri, the forward-sweep factor */
+  double *theta_edge_save;  /* (E+1, L) edge mean of theta_m_save (acoustic right-hand side) */
   /* mixed form (float32): copies of u, pv_edge, w, rw kept current by the step, the
    * deviations theta_m - ref_theta and theta_m_save - ref_theta, and the stencils'
    * intermediate edge fluxes, edge / vertex kinetic energy and vertex PV */

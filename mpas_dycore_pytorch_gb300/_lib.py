@@ -77,7 +77,7 @@ FIELDS = (
     ("rho_int", "c"),
     ("flux_w_e", "e"), ("flux_th_e", "e"),
     ("ac_rs", "c"), ("ac_ts", "c"), ("ac_x", "cw"), ("b_tri", "c"), ("c_tri", "c"),
-    ("tri_m", "c"),
+    ("tri_m", "c"), ("theta_edge_save", "e"),
 )
 # float32 members of mpasg_fields (after FIELDS, before status)
 FIELDS32 = (
@@ -94,7 +94,7 @@ MESH_F32_PTRS = tuple(n + "_f32" for n in (
     "fnp", "rdnw"))
 
 # float64 arrays appended after the float32 copies
-MESH_TAIL_PTRS = ("zgrid", "u_init", "v_init", "angleEdge", "t_init")
+MESH_TAIL_PTRS = ("zgrid", "u_init", "v_init", "angleEdge", "t_init", "cell_edge_geo")
 
 
 STAGE_NAMES = ("begin", "setup", "moist", "vert_imp_coefs", "dyn_tend_rk1", "dyn_tend",

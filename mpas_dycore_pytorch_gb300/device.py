@@ -113,7 +113,15 @@ class DeviceMesh:
             t = torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
             self._keep[n] = t
             setattr(st, n, t.data_ptr())
+        # the acoustic flux sums' divergence weight, formed once: sign * dvEdge * invAreaCell
+        eoc0 = ints["edgesOnCell"].astype(np.int64)
+        geo = np.zeros((nc + 1, me))
+        geo[:nc] = (dbls["edgesOnCell_sign"][:nc] * dbls["dvEdge"][np.minimum(eoc0, ne)]) * \
+            dbls["invAreaCell"][:nc, None]
+        dbls["cell_edge_geo"] = np.ascontiguousarray(geo)
         for n in _lib.MESH_TAIL_PTRS:
+            if n == "cell_edge_geo":
+                continue
             if n not in ref:
                 raise MpasConfigError(f"mesh is missing {n}")
             a = _np(ref[n])
