@@ -211,6 +211,7 @@ typedef struct mpasg_fields {
   double *b_tri, *c_tri;                                            /* (C+1, L) */
   double *tri_m;        /* (C+1, L) mixed form: -alpha_tri * a_tri, the forward-sweep factor */
   double *theta_edge_save;  /* (E+1, L) edge mean of theta_m_save (acoustic right-hand side) */
+  double *theta_edge_rsum;  /* (E+1, L) 1 / (theta_m_save_1 + theta_m_save_2) (divergence damping) */
   /* mixed form (float32): copies of u, pv_edge, w, rw kept current by the step, the
    * deviations theta_m - ref_theta and theta_m_save - ref_theta, and the stencils'
    * intermediate edge fluxes, edge / vertex kinetic energy and vertex PV */

@@ -77,7 +77,7 @@ FIELDS = (
     ("rho_int", "c"),
     ("flux_w_e", "e"), ("flux_th_e", "e"),
     ("ac_rs", "c"), ("ac_ts", "c"), ("ac_x", "cw"), ("b_tri", "c"), ("c_tri", "c"),
-    ("tri_m", "c"), ("theta_edge_save", "e"),
+    ("tri_m", "c"), ("theta_edge_save", "e"), ("theta_edge_rsum", "e"),
 )
 # float32 members of mpasg_fields (after FIELDS, before status)
 FIELDS32 = (

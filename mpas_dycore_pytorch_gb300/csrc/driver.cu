@@ -289,7 +289,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   if (S > 0) CHECK_RC(copy(f.scalars_init, f.scalars, ncs, s));
   if (advect && coupled) CHECK_RC(copy(f.scalars_a, f.scalars_init, ncs, s));
   if (c->precision == MPASG_PRECISION_MIXED) CHECK_RC(mpasgi_pack_f32(m, &f, s));
-  else CHECK_RC(mpasgi_theta_edge(m, &f, s));  // edge mean of theta_m_save
+  CHECK_RC(mpasgi_theta_edge(m, &f, s));  // edge mean of theta_m_save and its reciprocal sum
   MARK(MPASG_STAGE_SETUP);
   CHECK_RC(mpasg_moist_coefficients(m, c, &f, stream));
   MARK(MPASG_STAGE_MOIST);
@@ -309,7 +309,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
       for (int small = 1; small <= nsub[rk - 1]; ++small) {
         CHECK_RC(mpasgi_acoustic_step(m, c, &f, small, dts, s, true));
         MARK(MPASG_STAGE_ACOUSTIC);
-        CHECK_RC(mpasg_divergence_damping(m, c, &f, dts, stream));
+        CHECK_RC(mpasgi_divergence_damping(m, c, &f, dts, s, true));
         MARK(MPASG_STAGE_DIVDAMP);
       }
       CHECK_RC(mpasg_recover_large_step(m, c, &f, rk, nsub[rk - 1], rk_ts[rk - 1], stream));
@@ -339,7 +339,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
       CHECK_RC(copy(f.rho_p_save, f.rho_p, ncl, s));
       CHECK_RC(copy(f.theta_m_save, f.theta_m, ncl, s));
       CHECK_RC(copy(f.rr_save, f.rho_p, ncl, s));
-      if (c->precision != MPASG_PRECISION_MIXED) CHECK_RC(mpasgi_theta_edge(m, &f, s));
+      CHECK_RC(mpasgi_theta_edge(m, &f, s));
     }
   }
   MARK(MPASG_STAGE_SPLIT);

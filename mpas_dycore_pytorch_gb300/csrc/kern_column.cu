@@ -230,14 +230,17 @@ MPASG_D AcLevel ac_level(const mpasg_mesh& m, const mpasg_fields& f, int c, int 
 }
 
 // edge mean of theta_m_save, 0.5 (theta_2 + theta_1), the value the acoustic right-hand
-// side takes per edge (theta_m_save only changes at the dynamics substep boundaries)
+// side takes per edge, and the reciprocal of the sum that divergence damping divides by
+// (theta_m_save only changes at the dynamics substep boundaries)
 __global__ void k_theta_edge(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)m.nEdges * L) return;
   uint32_t e = fl.div(i), k = i - e * L;
   const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-  f.theta_edge_save[i] = 0.5 * (f.theta_m_save[(size_t)c2 * L + k] + f.theta_m_save[(size_t)c1 * L + k]);
+  const double sum = f.theta_m_save[(size_t)c2 * L + k] + f.theta_m_save[(size_t)c1 * L + k];
+  f.theta_edge_save[i] = 0.5 * sum;
+  f.theta_edge_rsum[i] = 1.0 / sum;  // divergence damping multiplies instead of dividing
 }
 
 template <typename T>
@@ -652,7 +655,9 @@ __global__ void k_divergence_damping(mpasg_mesh m, mpasg_fields f, FastDiv fl, d
   size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
   T d1 = -dif<T>(f.rtheta_pp[i1], f.rtheta_pp_old[i1]);  // substep change: float64 difference
   T d2 = -dif<T>(f.rtheta_pp[i2], f.rtheta_pp_old[i2]);
-  f.ru_p[i] = f.ru_p[i] + f64(cv<T>(coef) * (d2 - d1) / (cv<T>(f.theta_m_save[i1]) + cv<T>(f.theta_m_save[i2])));
+  // / (theta_m_save_1 + theta_m_save_2) as a product with the reciprocal formed once per
+  // dynamics substep (k_theta_edge); within one rounding of the quotient
+  f.ru_p[i] = f.ru_p[i] + f64(cv<T>(coef) * (d2 - d1) * cv<T>(f.theta_edge_rsum[i]));
 }
 
 // ---------------------------------------------------------------- small-step perturbation
@@ -914,7 +919,7 @@ int mpasgi_theta_edge(const mpasg_mesh* m, mpasg_fields* f, cudaStream_t s) {
 int mpasgi_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int small_step, double dts,
                          cudaStream_t s, bool copies_current) {
   if (!m || !c || !f || small_step < 1) return MPASG_E_ARG;
-  if (c->precision != MPASG_PRECISION_MIXED && !copies_current) {
+  if (!copies_current) {
     const int rc = mpasgi_theta_edge(m, f, s);  // the edge theta the right-hand side reads
     if (rc != MPASG_OK) return rc;
   }
@@ -978,8 +983,17 @@ int mpasgi_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_field
 
 extern "C" int mpasg_divergence_damping(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
                                         double dts, void* stream) {
+  return mpasgi_divergence_damping(m, c, f, dts, (cudaStream_t)stream, false);
+}
+
+int mpasgi_divergence_damping(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, double dts,
+                              cudaStream_t stream, bool copies_current) {
   if (!m || !c || !f) return MPASG_E_ARG;
   const int L = m->nVertLevels;
+  if (!copies_current) {
+    const int rc = mpasgi_theta_edge(m, f, stream);  // the reciprocal edge sums read below
+    if (rc != MPASG_OK) return rc;
+  }
   double coef = 2.0 * c->smdiv * c->len_disp / dts;
   if (c->precision == MPASG_PRECISION_MIXED)
     k_divergence_damping<float><<<nblocks((long long)m->nEdges * L), kBlock, 0, (cudaStream_t)stream>>>(
