@@ -117,6 +117,11 @@ typedef struct mpasg_mesh {
   /* (C+1, maxEdges): edgesOnCell_sign * dvEdge * invAreaCell of every cell's edge slots
    * (the divergence weight of the acoustic flux sums) */
   const double *cell_edge_geo;
+  /* (C+1, maxEdges) products the stencils would otherwise form at every level, each in the
+   * association the kernels use: edgesOnCell_sign * dvEdge; the del2 mixing weights
+   * 0.5 * invAreaCell * sign * dvEdge * invDcEdge (w) and invAreaCell * sign * dvEdge *
+   * invDcEdge (theta) */
+  const double *cell_edge_sdv, *cell_edge_es_w, *cell_edge_es_t;
 } mpasg_mesh;
 
 /* Namelist options the step consumes (validated on the host). */

@@ -63,8 +63,7 @@ __global__ void k_diag_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, int apvm)
   T ke = T(0);
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
-    double wgt = m.edgesOnCell_sign[c * me + j] * m.dvEdge[e];
-    double t = wgt * f.u[(size_t)e * L + k];
+    double t = m.cell_edge_sdv[c * me + j] * f.u[(size_t)e * L + k];  // (sign * dvEdge) * u
     T kt = T(0.25) * fp<T>(f.ke_edge, f.ke_edge_f32)[(size_t)e * L + k];
     div = (j == 0) ? t : div + t;
     ke = (j == 0) ? kt : ke + kt;

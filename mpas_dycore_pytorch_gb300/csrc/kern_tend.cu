@@ -51,8 +51,7 @@ __global__ void k_tend_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl, TendSca
   double hdiv = 0.0;
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
-    double wgt = m.edgesOnCell_sign[c * me + j] * m.dvEdge[e];
-    double t = wgt * f.ru[(size_t)e * L + k];
+    double t = m.cell_edge_sdv[c * me + j] * f.ru[(size_t)e * L + k];  // (sign * dvEdge) * ru
     hdiv = (j == 0) ? t : hdiv + t;
   }
   hdiv = hdiv * m.invAreaCell[c];
@@ -396,7 +395,8 @@ __global__ void k_mix_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
       int ec1 = m.cellsOnEdge[2 * e], ec2 = m.cellsOnEdge[2 * e + 1];
-      T es = T(0.5) * ia * sg[c * me + j] * dv[e] * idc[e];
+      T es = sizeof(T) == sizeof(double) ? cv<T>(m.cell_edge_es_w[c * me + j])  // same product, formed once
+                                         : T(0.5) * ia * sg[c * me + j] * dv[e] * idc[e];
       T flux = es * (cv<T>(f.h_edge[(size_t)e * L + k]) + cv<T>(f.h_edge[(size_t)e * L + k - 1])) *
                (w[(size_t)ec2 * (L + 1) + k] - w[(size_t)ec1 * (L + 1) + k]);
       dw = dw + flux;
@@ -417,7 +417,7 @@ __global__ void k_mix_cells_a(mpasg_mesh m, mpasg_fields f, FastDiv fl1) {
     for (int j = 0; j < n; ++j) {
       int e = m.edgesOnCell[c * me + j];
       int ec1 = m.cellsOnEdge[2 * e], ec2 = m.cellsOnEdge[2 * e + 1];
-      T es = ia * sg[c * me + j] * dv[e] * idc[e];
+      T es = sizeof(T) == sizeof(double) ? cv<T>(m.cell_edge_es_t[c * me + j]) : ia * sg[c * me + j] * dv[e] * idc[e];
       T pr = T(1) * msd2[e];
       T flux = es * dif<T>(f.theta_m[(size_t)ec2 * L + k], f.theta_m[(size_t)ec1 * L + k]) *
                cv<T>(f.h_edge[(size_t)e * L + k]);
@@ -606,10 +606,10 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta(mpasg_mesh m, mpasg_fie
     if (p.rk_step > 1) {
       for (int j = 0; j < n; ++j) {
         int e = m.edgesOnCell[c * me + j];
-        int ec1 = m.cellsOnEdge[2 * e], ec2 = m.cellsOnEdge[2 * e + 1];
-        T wgt = m.edgesOnCell_sign[c * me + j] * m.dvEdge[e];
-        T flux = wgt * (f.ru_save[(size_t)e * L + k] - f.ru[(size_t)e * L + k]) * T(0.5) *
-                 (f.theta_m_save[(size_t)ec2 * L + k] + f.theta_m_save[(size_t)ec1 * L + k]);
+        // (sign dvEdge) (ru_save - ru) 0.5 (theta_2 + theta_1), with the slot product and the
+        // edge mean formed once (scaling by 0.5 is exact, so the rounding is unchanged)
+        T flux = m.cell_edge_sdv[c * me + j] * (f.ru_save[(size_t)e * L + k] - f.ru[(size_t)e * L + k]) *
+                 f.theta_edge_save[(size_t)e * L + k];
         tt = tt - flux;
       }
     }
@@ -850,6 +850,10 @@ extern "C" int mpasg_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_
 int mpasgi_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int rk_step, cudaStream_t s,
                     bool copies_current) {
   if (!m || !c || !f || rk_step < 1 || rk_step > 3) return MPASG_E_ARG;
+  if (!copies_current && rk_step > 1 && c->precision != MPASG_PRECISION_MIXED) {
+    const int rc = mpasgi_theta_edge(m, f, s);  // the edge mean of theta_m_save read below
+    if (rc != MPASG_OK) return rc;
+  }
   if (m->nVertLevels < 4) return MPASG_E_ARG;
   if (c->precision != MPASG_PRECISION_FLOAT64 && c->precision != MPASG_PRECISION_MIXED) return MPASG_E_ARG;
   TendScalars p;

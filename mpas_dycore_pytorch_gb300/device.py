@@ -119,8 +119,18 @@ class DeviceMesh:
         geo[:nc] = (dbls["edgesOnCell_sign"][:nc] * dbls["dvEdge"][np.minimum(eoc0, ne)]) * \
             dbls["invAreaCell"][:nc, None]
         dbls["cell_edge_geo"] = np.ascontiguousarray(geo)
+        # per-slot products formed in the kernels' own association (bit-identical)
+        ec = np.minimum(eoc0, ne)
+        sg, dv, idc, ia = dbls["edgesOnCell_sign"][:nc], dbls["dvEdge"][ec], dbls["invDcEdge"][ec], \
+            dbls["invAreaCell"][:nc, None]
+        derived_slots = {"cell_edge_sdv": sg * dv, "cell_edge_es_w": (((0.5 * ia) * sg) * dv) * idc,
+                         "cell_edge_es_t": ((ia * sg) * dv) * idc}
+        for n, v in derived_slots.items():
+            a = np.zeros((nc + 1, me))
+            a[:nc] = v
+            dbls[n] = a
         for n in _lib.MESH_TAIL_PTRS:
-            if n == "cell_edge_geo":
+            if n == "cell_edge_geo" or n in derived_slots:
                 continue
             if n not in ref:
                 raise MpasConfigError(f"mesh is missing {n}")
