@@ -64,8 +64,8 @@ TRAFFIC_B_PER_CELL_LEVEL = {"dyn_tend": 542.7}
 # executed float64 flops (2 per FMA) per call and cell-level of a float64 stage, averaged
 # over a large step's calls, from an ncu count on the same level-5 x 41 case
 # (profiles/dyn_tend_fp64_flops_level5_10242x41.md)
-FP64_FLOP_PER_CELL_LEVEL = {"dyn_tend": 637.5}
-FP64_INST_PER_CELL_LEVEL = {"dyn_tend": 476.4}  # DFMA + DMUL + DADD issued
+FP64_FLOP_PER_CELL_LEVEL = {"dyn_tend": 607.3}
+FP64_INST_PER_CELL_LEVEL = {"dyn_tend": 446.3}  # DFMA + DMUL + DADD issued
 BASE_CFG = {"config_time_integration_order": 3, "config_len_disp": 120000.0,
             "config_number_of_sub_steps": 2, "config_dynamics_split_steps": 3}
 
