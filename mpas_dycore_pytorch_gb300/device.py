@@ -178,8 +178,8 @@ class DeviceState:
     def __init__(self, mesh: DeviceMesh, num_scalars: int):
         self.mesh = mesh
         self.num_scalars = int(num_scalars)
-        if not 1 <= self.num_scalars <= 8:
-            raise MpasUnsupportedCapabilityError("1 to 8 scalars are supported")
+        if not 0 <= self.num_scalars <= 8:
+            raise MpasUnsupportedCapabilityError("0 to 8 scalars are supported")
         S = self.num_scalars
         shapes = dict((k, f(mesh)) for k, f in ROWS.items())
         shapes["cs"] = (mesh.nCells + 1, mesh.nVertLevels, S)

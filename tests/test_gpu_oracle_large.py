@@ -66,3 +66,24 @@ def test_monotone_tracers_stay_bounded_level5():
     assert q.min() >= -1e-14
     assert q.max() <= q0.max() * (1 + 1e-10) + 1e-12
     assert model.check_finite() == 0
+
+
+def test_no_scalars_two_steps_vs_oracle():
+    """An empty scalar set (num_scalars = 0): the dynamics alone, against the oracle."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import Model
+    from oracle.step import Stepper
+    st, cfg = _case(3, 16, 0, False)
+    assert st["scalars"].shape[-1] == 0
+    model = Model(st, cfg, 1800.0, num_scalars=0)
+    model.prepare(st)
+    ref = Stepper(st, cfg)
+    rs = ref.prepare(st, 1800.0)
+    for _ in range(2):
+        model.step()
+        rs = ref.srk3_step(rs, 1800.0)
+    got = model.export()
+    for k in ("u", "w", "theta_m", "rho_zz", "exner", "v", "divergence", "uReconstructZonal"):
+        err = rel_l2(to_np(got[k])[:-1], rs[k][:-1])
+        assert err <= 1e-11, (k, err)
+    assert model.check_finite() == 0

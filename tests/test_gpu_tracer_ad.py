@@ -105,3 +105,21 @@ def test_central_difference_matches_vjp():
         fd = (objective(st["scalars"] + h * v) - objective(st["scalars"] - h * v)) / (2 * h)
         errs.append(abs(fd - dd) / abs(dd))
     assert min(errs) <= 1e-6, errs
+
+
+def test_mixed_precision_derivatives_within_stated_error():
+    """The mixed form's scalar VJP / JVP (float32 stencils in the taped forward and the
+    tangent replay, float64 transposed transport) against the reference's float64 VJP /
+    JVP: the stated bound for mixed-precision gradients is 1e-4."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import run_simulation
+    state, meta = _case()
+    cfg = dict(meta["config"], config_precision="mixed")
+    w = torch.as_tensor(GOLDEN["weights"]).cuda()
+    g = run_simulation.vjp(state, state, lambda o: (o["scalars"] * w).sum(), track_keys=("scalars",), config=cfg,
+                           dt=meta["dt"], nsteps=2)["scalars"].cpu().numpy()
+    t = run_simulation.jvp(state, state, {"scalars": torch.as_tensor(GOLDEN["tangent"])}, config=cfg, dt=meta["dt"],
+                           nsteps=2)["scalars"].cpu().numpy()
+    eg, et = rel_l2(g, GOLDEN["vjp_scalars"]), rel_l2(t, GOLDEN["jvp_scalars"])
+    assert eg <= 1e-4 and et <= 1e-4, (eg, et)
+    assert max(eg, et) > 1e-12  # float32 arithmetic really ran
