@@ -60,8 +60,11 @@ MPASG_D VimpLevel vimp_level(const mpasg_mesh& m, const mpasg_fields& f, size_t 
   double zz = m.zz[o + k], p = f.exner[o + k];
   double rb = m.rho_base[o + k], rtb = f.rtheta_base[o + k], pb = f.exner_base[o + k];
   double rt = f.rtheta_p[o + k], q = f.qtot[o + k];
-  if (sizeof(T) == sizeof(double))
-    v.cofwt = fdiv<T>(fdiv<T>(0.5 * dtseps * rcv * zz * kGravity * rb, 1.0 + q) * p, (rtb + rt) * pb);
+  if (sizeof(T) == sizeof(double)) {
+    // x / (1 + q) is x itself when q == 0 (dry columns): the division is skipped, not changed
+    const double x = 0.5 * dtseps * rcv * zz * kGravity * rb;
+    v.cofwt = fdiv<T>((q == 0.0 ? x : fdiv<T>(x, 1.0 + q)) * p, (rtb + rt) * pb);
+  }
   else  // mixed form: the dry case needs no 1 / (1 + q)
     v.cofwt = (q == 0.0 ? 0.5 * dtseps * rcv * zz * kGravity * rb
                         : fdiv<T>(0.5 * dtseps * rcv * zz * kGravity * rb, 1.0 + q)) *
