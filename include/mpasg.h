@@ -122,6 +122,8 @@ typedef struct mpasg_mesh {
    * 0.5 * invAreaCell * sign * dvEdge * invDcEdge (w) and invAreaCell * sign * dvEdge *
    * invDcEdge (theta) */
   const double *cell_edge_sdv, *cell_edge_es_w, *cell_edge_es_t;
+  /* dcEdge * dvEdge (E+1) and edgesOnVertex_sign * dcEdge (V+1, vertexDegree), formed once */
+  const double *edge_dcdv, *vertex_edge_sdc;
 } mpasg_mesh;
 
 /* Namelist options the step consumes (validated on the host). */

@@ -18,7 +18,8 @@ __global__ void k_diag_edges_a(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
   f.h_edge[i] = f64(T(0.5) * (cv<T>(f.rho_zz[(size_t)c1 * L + k]) + cv<T>(f.rho_zz[(size_t)c2 * L + k])));
   const T u = fp<T>(f.u, f.u_f32)[i];
-  fpw<T>(f.ke_edge, f.ke_edge_f32)[i] = (G(dcEdge)[e] * G(dvEdge)[e]) * (u * u);
+  const T dcdv = sizeof(T) == sizeof(double) ? cv<T>(m.edge_dcdv[e]) : G(dcEdge)[e] * G(dvEdge)[e];
+  fpw<T>(f.ke_edge, f.ke_edge_f32)[i] = dcdv * (u * u);
 }
 
 // vorticity, vertex kinetic energy and potential vorticity
@@ -34,8 +35,7 @@ __global__ void k_diag_vertices(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   T kev = T(0);
   for (int j = 0; j < vd; ++j) {
     int e = m.edgesOnVertex[v * vd + j];
-    double wgt = m.edgesOnVertex_sign[v * vd + j] * m.dcEdge[e];
-    double t = wgt * f.u[(size_t)e * L + k];
+    double t = m.vertex_edge_sdc[v * vd + j] * f.u[(size_t)e * L + k];  // (sign * dcEdge) * u
     T ke = fp<T>(f.ke_edge, f.ke_edge_f32)[(size_t)e * L + k];
     vort = (j == 0) ? t : vort + t;
     kev = (j == 0) ? ke : kev + ke;

@@ -129,6 +129,16 @@ class DeviceMesh:
             a = np.zeros((nc + 1, me))
             a[:nc] = v
             dbls[n] = a
+        vd = self.vertexDegree
+        eov0 = np.minimum(ints["edgesOnVertex"].astype(np.int64), ne)
+        sdc = np.zeros((nv + 1, vd))
+        sdc[:nv] = dbls["edgesOnVertex_sign"][:nv, :vd] * dbls["dcEdge"][eov0]
+        derived_slots["vertex_edge_sdc"] = sdc
+        dbls["vertex_edge_sdc"] = sdc
+        dcdv = np.zeros(ne + 1)
+        dcdv[:ne] = dbls["dcEdge"][:ne] * dbls["dvEdge"][:ne]
+        derived_slots["edge_dcdv"] = dcdv
+        dbls["edge_dcdv"] = dcdv
         for n in _lib.MESH_TAIL_PTRS:
             if n == "cell_edge_geo" or n in derived_slots:
                 continue
