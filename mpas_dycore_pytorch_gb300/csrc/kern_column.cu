@@ -725,14 +725,28 @@ MPASG_D double pow1p_rcv_m1(double x) {
 // exner = exner_base (1 + x)^(R/cv), x = rtheta_p / rtheta_base, with the increment
 // exner - exner_base = exner_base pow1p_rcv_m1(x) (pow when |x| >= 0.02), so the
 // pressure perturbation needs no difference of nearly equal Exner values.
-template <typename T>
-__global__ void k_recover_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int rk_step, double inv_ns,
-                                double rk_dt) {
+// FLAT (flat terrain, no slope terms): w itself is finished here as well, omega-derived
+// part over the interface density, with the level below's density from the neighbouring
+// thread (shared memory) -- the same expressions k_recover_w evaluates, one launch fewer.
+template <typename T, bool FLAT = false>
+__global__ void __launch_bounds__(kBlock) k_recover_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int rk_step,
+                                                          double inv_ns, double rk_dt) {
+  __shared__ double s_rho[FLAT ? kBlock : 1];
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint32_t)m.nCells * (L + 1)) return;
-  uint32_t c = fl1.div(i), k = i - c * (L + 1);
+  const bool active = i < (uint32_t)m.nCells * (L + 1);
+  if (!FLAT && !active) return;
+  uint32_t c = 0, k = 0;
+  if (active) {
+    c = fl1.div(i);
+    k = i - c * (L + 1);
+  }
   const size_t o = (size_t)c * L + k;
+  if (FLAT) {
+    s_rho[threadIdx.x] = (active && k < (uint32_t)L) ? f.rho_p_save[o] + f.rho_pp[o] + m.rho_base[o] : 0.0;
+    __syncthreads();
+    if (!active) return;
+  }
   if (k < (uint32_t)L) {
     double rho_p = f.rho_p_save[o] + f.rho_pp[o];
     double rho_zz = rho_p + m.rho_base[o];
@@ -778,7 +792,21 @@ __global__ void k_recover_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl1, int r
     if (sizeof(T) != sizeof(double)) f.rw_f32[ow] = d2f_bits(rw);
     size_t oc = (size_t)c * L;
     const double den = m.fzm[k] * m.zz[oc + k] + m.fzp[k] * m.zz[oc + k - 1];
-    f.w[ow] = den == 1.0 ? rw : fdiv<T>(rw, den);
+    const double wo = den == 1.0 ? rw : fdiv<T>(rw, den);
+    if (!FLAT) {
+      f.w[ow] = wo;
+    } else {
+      const double rho_k = s_rho[threadIdx.x];
+      const double rho_km1 = threadIdx.x >= 1 ? s_rho[threadIdx.x - 1]
+                                              : f.rho_p_save[oc + k - 1] + f.rho_pp[oc + k - 1] + m.rho_base[oc + k - 1];
+      const double wk = fdiv<T>(wo, m.fzm[k] * rho_k + m.fzp[k] * rho_km1);
+      f.w[ow] = wk;
+      if (sizeof(T) != sizeof(double)) f.w_f32[ow] = d2f_bits(wk);
+    }
+  } else if (FLAT) {  // bottom and top interfaces: no slope flux, w = 0
+    const size_t ow = (size_t)c * (L + 1) + k;
+    f.w[ow] = 0.0;
+    if (sizeof(T) != sizeof(double)) f.w_f32[ow] = 0.0f;
   }
 }
 
@@ -848,12 +876,17 @@ template <typename T>
 int launch_recover(const mpasg_mesh* m, mpasg_fields* f, int rk_step, double inv_ns, double rk_dt, cudaStream_t s) {
   const int L = m->nVertLevels;
   const long long ncw = (long long)m->nCells * (L + 1);
-  k_recover_cells<T><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), rk_step, inv_ns, rk_dt);
+  if (m->flatTerrain)
+    k_recover_cells<T, true><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), rk_step, inv_ns, rk_dt);
+  else
+    k_recover_cells<T><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), rk_step, inv_ns, rk_dt);
   MPASG_LAUNCH_CHECK();
   k_recover_edges<T><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), inv_ns);
   MPASG_LAUNCH_CHECK();
-  k_recover_w<T><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1));
-  MPASG_LAUNCH_CHECK();
+  if (!m->flatTerrain) {  // slope fluxes need the new ru of k_recover_edges
+    k_recover_w<T><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1));
+    MPASG_LAUNCH_CHECK();
+  }
   return MPASG_OK;
 }
 
