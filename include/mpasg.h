@@ -124,6 +124,8 @@ typedef struct mpasg_mesh {
   const double *cell_edge_sdv, *cell_edge_es_w, *cell_edge_es_t;
   /* dcEdge * dvEdge (E+1) and edgesOnVertex_sign * dcEdge (V+1, vertexDegree), formed once */
   const double *edge_dcdv, *vertex_edge_sdc;
+  /* (C+1, 4): cos latCell, sin latCell, cos lonCell, sin lonCell (reconstruction) */
+  const double *cell_trig;
 } mpasg_mesh;
 
 /* Namelist options the step consumes (validated on the host). */

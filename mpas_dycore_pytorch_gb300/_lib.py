@@ -95,7 +95,8 @@ MESH_F32_PTRS = tuple(n + "_f32" for n in (
 
 # float64 arrays appended after the float32 copies
 MESH_TAIL_PTRS = ("zgrid", "u_init", "v_init", "angleEdge", "t_init", "cell_edge_geo", "cell_edge_sdv",
-                  "cell_edge_es_w", "cell_edge_es_t", "edge_dcdv", "vertex_edge_sdc")
+                  "cell_edge_es_w", "cell_edge_es_t", "edge_dcdv", "vertex_edge_sdc",
+                  "cell_trig")
 
 
 STAGE_NAMES = ("begin", "setup", "moist", "vert_imp_coefs", "dyn_tend_rk1", "dyn_tend",

@@ -133,11 +133,6 @@ __global__ void k_diag_edges_b(mpasg_mesh m, mpasg_fields f, FastDiv fl, int rec
   if (sizeof(T) != sizeof(double)) f.pv_edge_f32[i] = pve;
 }
 
-MPASG_D double vcos(double x) { return cos(x); }
-MPASG_D float vcos(float x) { return cosf(x); }
-MPASG_D double vsin(double x) { return sin(x); }
-MPASG_D float vsin(float x) { return sinf(x); }
-
 // mpas_reconstruct_2d: RBF reconstruction of the cell-centre wind
 template <typename T>
 __global__ void k_reconstruct(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
@@ -159,8 +154,8 @@ __global__ void k_reconstruct(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
       x = x + tx; y = y + ty; z = z + tz;
     }
   }
-  const T lat = cv<T>(m.latCell[c]), lon = cv<T>(m.lonCell[c]);
-  const T clat = vcos(lat), slat = vsin(lat), clon = vcos(lon), slon = vsin(lon);
+  const double* tr = m.cell_trig + (size_t)c * 4;  // cos / sin of the cell's latitude and longitude
+  const T clat = cv<T>(tr[0]), slat = cv<T>(tr[1]), clon = cv<T>(tr[2]), slon = cv<T>(tr[3]);
   f.uReconstructX[i] = f64(x);
   f.uReconstructY[i] = f64(y);
   f.uReconstructZ[i] = f64(z);

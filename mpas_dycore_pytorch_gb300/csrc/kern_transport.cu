@@ -315,6 +315,7 @@ __global__ void k_mono_cells_c(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S, 
   const int n = m.nEdgesOnCell[c];
   const T ia = cv<T>(m.invAreaCell[c]);
   const double rint = f.rho_int[i];
+  const double inv_rint = fdiv<T>(1.0, rint);  // one reciprocal for every scalar of the cell-level
   const size_t oc = (size_t)c * L;
   for (int s = 0; s < S; ++s) {
     size_t o = (size_t)i * S + s;
@@ -343,7 +344,7 @@ __global__ void k_mono_cells_c(mpasg_mesh m, mpasg_fields f, FastDiv fl, int S, 
         hsum = hsum - cv<T>(f.hflux[((size_t)e * L + k) * S + s]) * sw;
     }
     if (sizeof(T) != sizeof(double)) rows = rows + f64(hsum);
-    double st2 = fdiv<T>(rows - f64(cv<T>(m.rdnw[k]) * (wl_hi - wl_lo)), rint);
+    double st2 = (rows - f64(cv<T>(m.rdnw[k]) * (wl_hi - wl_lo))) * inv_rint;
     s_out[o] = st2 > 0.0 ? st2 : 0.0;
   }
 }

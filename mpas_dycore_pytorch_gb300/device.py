@@ -139,6 +139,11 @@ class DeviceMesh:
         dcdv[:ne] = dbls["dcEdge"][:ne] * dbls["dvEdge"][:ne]
         derived_slots["edge_dcdv"] = dcdv
         dbls["edge_dcdv"] = dcdv
+        lat, lon = _np(ref["latCell"]).astype(np.float64)[:nc], _np(ref["lonCell"]).astype(np.float64)[:nc]
+        trig = np.zeros((nc + 1, 4))
+        trig[:nc] = np.stack([np.cos(lat), np.sin(lat), np.cos(lon), np.sin(lon)], -1)
+        derived_slots["cell_trig"] = trig
+        dbls["cell_trig"] = trig
         for n in _lib.MESH_TAIL_PTRS:
             if n == "cell_edge_geo" or n in derived_slots:
                 continue
