@@ -37,22 +37,23 @@ METRIC = "cell-level-steps/s fwd & VJP, mixed/batched vs plain FP64 on GB300 at 
 UNIT = "cell-level-steps/s"
 
 WORKLOADS = {
-    # configs[1]: level-6 mesh, 55 stretched levels, 32 bumps, 3 monotone tracers, dt 720 s
+    # headline: level-6 mesh, 55 stretched levels, 32 bumps, 3 monotone tracers, dt 720 s
     "c1": dict(spec=dict(level=6, nlev=55, dz_bottom=50.0, seed=1, n_bumps=32, n_tracers=3),
                config=dict(config_monotonic=True), dt=720.0,
                name="plain float64 forward, level-6 icosahedral mesh 40962 cells x 55 levels, "
                     "3 monotone tracers, dt 720 s, split 3 x RK3 x ns 2"),
-    # configs[2] mesh: level-5 mesh, 41 levels (profiling size: state > L2, a few GB at most)
+    # level-5 mesh, 41 levels (the differentiation workload's mesh; profiling size: state > L2,
+    # a few GB at most)
     "c2": dict(spec=dict(level=5, nlev=41, seed=2, n_bumps=8, n_tracers=3),
                config=dict(config_monotonic=True), dt=900.0,
                name="plain float64 forward, level-5 mesh 10242 cells x 41 levels, 3 monotone tracers, dt 900 s"),
-    # configs[4] forward: level-8 mesh, 55 stretched levels, 128 bumps, 3 monotone tracers, dt 180 s;
+    # large forward: level-8 mesh, 55 stretched levels, 128 bumps, 3 monotone tracers, dt 180 s;
     # the dissipation length is the mesh's own spacing (30 km), as MPAS sets it per mesh
     "c4": dict(spec=dict(level=8, nlev=55, dz_bottom=50.0, seed=3, n_bumps=128, n_tracers=3),
                config=dict(config_monotonic=True, config_len_disp=30000.0), dt=180.0,
                name="plain float64 forward, level-8 icosahedral mesh 655362 cells x 55 levels, "
                     "3 monotone tracers, dt 180 s, split 3 x RK3 x ns 2"),
-    # configs[0]: level-4 mesh, 26 uniform levels, 8 bumps, 1 non-monotone tracer, dt 1800 s
+    # CPU-runnable case: level-4 mesh, 26 uniform levels, 8 bumps, 1 non-monotone tracer, dt 1800 s
     "c0": dict(spec=dict(level=4, nlev=26, seed=0, n_bumps=8, n_tracers=1),
                config=dict(config_monotonic=False), dt=1800.0,
                name="plain float64 forward, level-4 mesh 2562 cells x 26 levels, 1 tracer, dt 1800 s"),
