@@ -593,9 +593,8 @@ def run_gb300(args, rank, world):
     for _ in range(K):
         model.load_boundary(host)
         model.step()
-        ex = model.export(clone=False)
-        for k in keys:
-            host[k].copy_(ex[k], non_blocking=True)
+        model.export_to(host)
+    model.wait_exports()
     e_end.record()
     torch.cuda.synchronize()
     e_ms, e_value = replica_throughput(e_start.elapsed_time(e_end), C_ * L_, K, world, dev)

@@ -252,6 +252,8 @@ class Model:
         # static fields the step reads from the state side
         self.state.load(mesh, keys=("rt_diabatic_tend",))
         self._graph = None
+        self._d2h_stream = None
+        self._pending_d2h: dict[int, torch.cuda.Event] = {}
         self._rows_in = self._rows_out = None
         if self._perm is not None:  # device row maps, padding row last
             dev = self.dmesh.device
@@ -298,8 +300,42 @@ class Model:
 
     def load_boundary(self, state: Mapping[str, Any]) -> None:
         """Load a prepared (complete) step boundary (caller's order)."""
-        self.state.load(state, keys=STATE_KEYS + ("rho_edge",), rows=self._rows_in)
+        self.state.load(state, keys=STATE_KEYS + ("rho_edge",), rows=self._rows_in, pending=self._pending_d2h)
         self.state.f["rho_zz"][self.dmesh.nCells].fill_(1.0)
+
+    def export_to(self, host: Mapping[str, torch.Tensor]) -> None:
+        """Copy the step boundary (caller's order) into the caller's host tensors, one
+        field after another on a copy stream of its own.  The copies run while the
+        compute stream goes on: a later ``load_boundary`` from the same host tensors waits
+        for each field's copy just before it reads that field, so the copies in and out
+        of a chain of steps overlap field by field.  Call ``wait_exports`` (or
+        synchronise the device) before reading the host tensors."""
+        cur = torch.cuda.current_stream()
+        if self._d2h_stream is None:
+            self._d2h_stream = torch.cuda.Stream(device=self.dmesh.device)
+        side = self._d2h_stream
+        ex = self.state.export()
+        for k, dst in host.items():
+            if k not in ex:
+                raise MpasConfigError(f"export_to: {k!r} is not a field of the step boundary")
+            src = self._export_field(k, ex[k]) if self._perm is not None else ex[k].clone()  # a snapshot
+            if tuple(dst.shape) != tuple(src.shape):
+                raise MpasConfigError(f"export_to: {k}: shape {tuple(dst.shape)} != {tuple(src.shape)}")
+            ready = torch.cuda.Event()
+            ready.record(cur)
+            side.wait_event(ready)
+            with torch.cuda.stream(side):
+                dst.copy_(src, non_blocking=True)
+            src.record_stream(side)
+            done = torch.cuda.Event()
+            done.record(side)
+            self._pending_d2h[dst.data_ptr()] = done
+
+    def wait_exports(self) -> None:
+        """Make the current stream wait for every ``export_to`` copy issued so far."""
+        if self._d2h_stream is not None:
+            torch.cuda.current_stream().wait_stream(self._d2h_stream)
+        self._pending_d2h.clear()
 
     def step(self) -> None:
         if self._graph is not None:
@@ -345,12 +381,12 @@ class Model:
         if self._perm is None:
             ex = self.state.export()
             return {k: v.clone() for k, v in ex.items()} if clone else dict(ex)
-        from .device import ENTITY, FIELD_KIND
-        out = {}
-        for k, v in self.state.export().items():
-            name = {"rho_edge": "h_edge", "ur_cell": "uReconstructZonal", "vr_cell": "uReconstructMeridional"}.get(k, k)
-            out[k] = self.state.gather_rows(v, self._rows_out[ENTITY[FIELD_KIND[name]]])
-        return out
+        return {k: self._export_field(k, v) for k, v in self.state.export().items()}
+
+    def _export_field(self, key: str, v: torch.Tensor) -> torch.Tensor:
+        """One device field gathered into the caller's row order."""
+        from .device import ALIASES, ENTITY, FIELD_KIND
+        return self.state.gather_rows(v, self._rows_out[ENTITY[FIELD_KIND[ALIASES.get(key, key)]]])
 
 
 def _is_prepared(state: Mapping[str, Any]) -> bool:

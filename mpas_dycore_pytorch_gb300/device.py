@@ -233,6 +233,9 @@ class DeviceState:
         self.bytes = total * 8 + pos32 * 4
         # rho_zz padding row holds 1.0 (the reference's sentinel)
         self.f["rho_zz"][mesh.nCells].fill_(1.0)
+        # staging of loads that are gathered into the device order; reused field after
+        # field (all on one stream), grown to the largest field
+        self._stage = torch.empty(0, dtype=torch.float64, device=mesh.device)
 
     def field(self, name: str) -> torch.Tensor:
         return self.f[ALIASES.get(name, name)]
@@ -248,10 +251,14 @@ class DeviceState:
         _lib.check(rc, "mpasg_permute_rows")
         return out
 
-    def load(self, state: Mapping[str, Any], keys=None, rows: Mapping[str, torch.Tensor] | None = None) -> None:
+    def load(self, state: Mapping[str, Any], keys=None, rows: Mapping[str, torch.Tensor] | None = None,
+             pending: dict | None = None) -> None:
         """Copy reference-layout arrays (numpy or torch) into the named fields; with
         ``rows`` (entity -> device row index, N+1 entries) the rows are gathered into the
-        device order on the device."""
+        device order on the device, through one staging buffer kept across fields and
+        calls.  ``pending`` maps a host tensor's address to the event of a device-to-host
+        copy still writing it: the copy out of that tensor waits for that event only."""
+        cur = torch.cuda.current_stream(self.mesh.device)
         for key in keys if keys is not None else state.keys():
             if key not in state:
                 continue
@@ -263,12 +270,20 @@ class DeviceState:
                 continue
             dst = self.f[name]
             t = torch.as_tensor(src, dtype=torch.float64)
+            if pending and isinstance(src, torch.Tensor):
+                ev = pending.pop(src.data_ptr(), None)
+                if ev is not None:
+                    cur.wait_event(ev)
             ent = ENTITY.get(FIELD_KIND.get(name)) if rows is not None else None
             if ent is not None:
                 if t.dim() != dst.dim() or tuple(t.shape[1:]) != tuple(dst.shape[1:]) or \
                         t.shape[0] not in (dst.shape[0], dst.shape[0] - 1):
                     raise MpasConfigError(f"{key}: shape {tuple(t.shape)} != {tuple(dst.shape)}")
-                stage = torch.zeros(dst.shape, dtype=torch.float64, device=dst.device)
+                if self._stage.numel() < dst.numel():
+                    self._stage = torch.empty(dst.numel(), dtype=torch.float64, device=dst.device)
+                stage = self._stage[: dst.numel()].view(dst.shape)
+                if t.shape[0] < stage.shape[0]:
+                    stage[t.shape[0]:].zero_()
                 stage[: t.shape[0]].copy_(t, non_blocking=True)
                 self.gather_rows(stage, rows[ent], out=dst)
                 continue

@@ -142,3 +142,39 @@ def test_model_sfc_order_is_transparent():
     a, b = native.export(), sfc.export()
     for k in STATE_KEYS:
         assert torch.equal(a[k][:-1], b[k][:-1]), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", ["native", "sfc"])
+def test_host_chain_through_export_to_matches_resident_steps(order):
+    """Steps chained through pinned host buffers (load_boundary -> step -> export_to,
+    the copies out overlapping the next copies in) equal the same steps kept on the
+    device, bit for bit; the padding rows come back too."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.device import STATE_KEYS
+    from mpas_dycore_pytorch_gb300.loader import load_case as synth
+    cfg = {"config_time_integration_order": 3, "config_len_disp": 120000.0, "config_monotonic": True,
+           "config_dt": 600.0}
+    st, _ = synth(CaseSpec(level=3, nlev=14, seed=9, n_bumps=3, n_tracers=2), cfg, as_torch=False)
+    resident = Model(st, cfg, 600.0, num_scalars=2, order=order)
+    chained = Model(st, cfg, 600.0, num_scalars=2, order=order)
+    resident.prepare(st)
+    chained.prepare(st)
+    start = resident.export()
+    host = {k: torch.empty(start[k].shape, dtype=torch.float64, pin_memory=True) for k in STATE_KEYS}
+    for k in STATE_KEYS:
+        host[k].copy_(start[k])
+    for _ in range(3):
+        resident.step()
+        chained.load_boundary(host)
+        chained.step()
+        chained.export_to(host)
+    chained.wait_exports()
+    torch.cuda.synchronize()
+    want = resident.export()
+    for k in STATE_KEYS:
+        assert torch.equal(host[k], want[k].cpu()), k
+    with pytest.raises(Exception):
+        chained.export_to({"not_a_field": host["u"]})
