@@ -512,3 +512,22 @@ def make_case(spec: CaseSpec, radius: float = EARTH_RADIUS):
     for k in ("deriv_two", "defc_a", "defc_b"):
         init[k] = mesh.pop(k)
     return init, mesh
+
+
+def write_case_files(spec: CaseSpec, directory, radius: float = EARTH_RADIUS, clobber: bool = False):
+    """Write the synthetic case as an MPAS grid file and an initial-condition file
+    (NetCDF-3, MPAS dimension and field names; ``netcdf_io.write_mpas_fields``), the pair
+    ``load_initial_state(init_path, grid_path)`` reads.  Returns ``(init_path, grid_path)``."""
+    import pathlib
+
+    from .netcdf_io import write_mpas_fields
+    d = pathlib.Path(directory)
+    d.mkdir(parents=True, exist_ok=True)
+    init, grid = make_case(spec, radius)
+    init = dict(init, nCells=grid["nCells"], nEdges=grid["nEdges"], nVertices=grid["nVertices"],
+                maxEdges=grid["maxEdges"], nVertLevels=int(spec.nlev))
+    tag = f"x1.{grid['nCells']}"
+    grid_path, init_path = d / f"{tag}.grid.nc", d / f"{tag}.init.nc"
+    write_mpas_fields(grid_path, grid, attrs={"sphere_radius": float(radius)}, clobber=clobber)
+    write_mpas_fields(init_path, init, attrs={"sphere_radius": float(radius)}, clobber=clobber)
+    return init_path, grid_path

@@ -8,9 +8,8 @@
   dictionaries (derived metrics, advection stencils, reconstruction coefficients, padding
   rows) from raw initial-condition and grid fields.  The fields are given as mappings of
   arrays; reading them from netCDF files needs the ``netCDF4`` package.
-* ``read_history`` / ``write_history`` / ``read_restart`` / ``write_restart`` are netCDF
-  formats; this build does not implement them and raises
-  ``MpasUnsupportedCapabilityError`` (netCDF4 is not available on the machines it targets).
+* ``read_history`` / ``write_history`` / ``read_restart`` / ``write_restart`` are in
+  ``netcdf_io.py`` (NetCDF-3 files with the reference's schema).
 """
 
 from __future__ import annotations
@@ -102,6 +101,14 @@ def load_config_from_namelist(namelist_path: str | pathlib.Path, *, strict: bool
 
 
 def _read_netcdf(path: pathlib.Path) -> dict[str, Any]:
+    """Fields of a grid or initial-condition file: NetCDF-3 through scipy, NetCDF-4 through
+    the netCDF4 package when it is installed."""
+    if not path.exists():
+        raise FileNotFoundError(f"file not found: {path}")
+    with open(path, "rb") as fh:
+        if fh.read(3) == b"CDF":
+            from .netcdf_io import read_mpas_fields
+            return read_mpas_fields(path)
     try:
         import netCDF4  # noqa: F401
     except ImportError as exc:
@@ -159,17 +166,4 @@ def load_initial_state(init_path, grid_path, mesh_support_path=None, *, device: 
     return state, mesh
 
 
-def _netcdf_io(name: str):
-    def fn(*args, **kwargs):
-        raise MpasUnsupportedCapabilityError(
-            f"{name}: the netCDF history / restart formats are not implemented on the GB300 path "
-            "(netCDF4 is not available where it runs); keep the state dictionaries of run_simulation instead")
-    fn.__name__ = name
-    fn.__doc__ = f"The reference's ``{name}`` (netCDF); raises MpasUnsupportedCapabilityError here."
-    return fn
-
-
-read_history = _netcdf_io("read_history")
-write_history = _netcdf_io("write_history")
-read_restart = _netcdf_io("read_restart")
-write_restart = _netcdf_io("write_restart")
+from .netcdf_io import read_history, read_restart, write_history, write_restart  # noqa: E402,F401

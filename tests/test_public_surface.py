@@ -84,11 +84,11 @@ def test_load_initial_state_matches_reference_loader():
         assert np.abs(g - ref[k]).max() <= 1e-14 * max(np.abs(ref[k]).max(), 1e-300), k
     with pytest.raises(gb.MpasMissingFieldError):
         gb.load_initial_state({"u": np.zeros(3)}, grid, config=meta["config"])
-    with pytest.raises(gb.MpasUnsupportedCapabilityError):
-        gb.load_initial_state("init.nc", "grid.nc")
+    with pytest.raises(FileNotFoundError):
+        gb.load_initial_state("no-such-init.nc", "no-such-grid.nc")
 
 
-@pytest.mark.parametrize("name", ["read_history", "write_history", "read_restart", "write_restart"])
-def test_netcdf_io_is_a_typed_rejection(name):
-    with pytest.raises(gb.MpasUnsupportedCapabilityError):
-        getattr(gb, name)("x.nc")
+@pytest.mark.parametrize("name", ["read_history", "read_restart"])
+def test_netcdf_readers_report_missing_files(name, tmp_path):
+    with pytest.raises(FileNotFoundError):
+        getattr(gb, name)(tmp_path / "x.nc")
