@@ -65,10 +65,10 @@ MPASG_D VimpLevel vimp_level(const mpasg_mesh& m, const mpasg_fields& f, size_t 
     const double x = 0.5 * dtseps * rcv * zz * kGravity * rb;
     v.cofwt = fdiv<T>((q == 0.0 ? x : fdiv<T>(x, 1.0 + q)) * p, (rtb + rt) * pb);
   }
-  else  // mixed form: the dry case needs no 1 / (1 + q)
-    v.cofwt = (q == 0.0 ? 0.5 * dtseps * rcv * zz * kGravity * rb
-                        : fdiv<T>(0.5 * dtseps * rcv * zz * kGravity * rb, 1.0 + q)) *
-              p * rcp_nr((rtb + rt) * pb);
+  else {  // mixed form: the dry case needs no 1 / (1 + q); constants folded into one factor
+    const double x = (dtseps * (0.5 * rcv * kGravity)) * zz * rb;
+    v.cofwt = (q == 0.0 ? x : fdiv<T>(x, 1.0 + q)) * p * rcp_nr((rtb + rt) * pb);
+  }
   v.coftz = (k == 0) ? 0.0 : dtseps * (m.fzm[k] * f.theta_m[o + k] + m.fzp[k] * f.theta_m[o + k - 1]);
   return v;
 }
@@ -128,10 +128,18 @@ __global__ void __launch_bounds__(kBlock) k_vimp_coefs(mpasg_mesh m, mpasg_field
   const double cw_k = me_.cofwt, cw_km1 = lo.cofwt;
   const double rdzw_k = m.rdzw[k], rdzw_km1 = m.rdzw[k - 1];
   const double cofrz_k = dtseps * rdzw_k, cofrz_km1 = dtseps * rdzw_km1;
-  f.a_tri[o + k] = -cofwz * ct_km1 * rdzw_km1 * zzm + cofwr * cofrz_km1 - cw_km1 * ct_km1 * rdzw_km1;
-  f.b_tri[o + k] = 1.0 + cofwz * (ct_k * rdzw_k * zz + ct_k * rdzw_km1 * zzm) -
-                   ct_k * (cw_k * rdzw_k - cw_km1 * rdzw_km1) + cofwr * (cofrz_k - cofrz_km1);
-  f.c_tri[o + k] = -cofwz * ct_kp1 * rdzw_k * zz - cofwr * cofrz_k + cw_k * ct_kp1 * rdzw_k;
+  if (sizeof(T) == sizeof(double)) {  // the reference's expressions (vert_imp_coefs.py:388-428)
+    f.a_tri[o + k] = -cofwz * ct_km1 * rdzw_km1 * zzm + cofwr * cofrz_km1 - cw_km1 * ct_km1 * rdzw_km1;
+    f.b_tri[o + k] = 1.0 + cofwz * (ct_k * rdzw_k * zz + ct_k * rdzw_km1 * zzm) -
+                     ct_k * (cw_k * rdzw_k - cw_km1 * rdzw_km1) + cofwr * (cofrz_k - cofrz_km1);
+    f.c_tri[o + k] = -cofwz * ct_kp1 * rdzw_k * zz - cofwr * cofrz_k + cw_k * ct_kp1 * rdzw_k;
+  } else {  // mixed form: the same float64 coefficients with the common factors taken out
+    const double tm = ct_km1 * rdzw_km1, tp = ct_kp1 * rdzw_k;
+    f.a_tri[o + k] = cofwr * cofrz_km1 - tm * (cofwz * zzm + cw_km1);
+    f.b_tri[o + k] = 1.0 + ct_k * (cofwz * (rdzw_k * zz + rdzw_km1 * zzm) - (cw_k * rdzw_k - cw_km1 * rdzw_km1)) +
+                     cofwr * (cofrz_k - cofrz_km1);
+    f.c_tri[o + k] = tp * (cw_k - cofwz * zz) - cofwr * cofrz_k;
+  }
 }
 
 template <typename T>

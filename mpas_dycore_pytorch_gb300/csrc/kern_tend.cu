@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_w_theta_mixed(mpasg_mesh m, mpa
       for (int j = 0; j < n; ++j) {
         int e = m.edgesOnCell[c * me + j];
         int ec1 = m.cellsOnEdge[2 * e], ec2 = m.cellsOnEdge[2 * e + 1];
-        const double wgt = m.edgesOnCell_sign[c * me + j] * m.dvEdge[e];
+        const double wgt = m.cell_edge_sdv[c * me + j];  // sign * dvEdge (mesh table)
         const double dru = f.ru_save[(size_t)e * L + k] - f.ru[(size_t)e * L + k];
         dsum = dsum + wgt * dru;
         T flux = cv<T>(wgt) * cv<T>(dru) * T(0.5) *
