@@ -410,16 +410,18 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
 
     ``initial_state`` is either a loaded raw state (prepared here, on the device) or a
     complete step boundary returned by a previous call.  Returns the final boundary with
-    the reference's keys; tensors stay on the CUDA device.
+    the reference's keys; tensors stay on the CUDA device.  With ``differentiable=True``
+    and ``initial_state["scalars"]`` requiring grad, the returned ``scalars`` carry the
+    hand-written adjoint of the scalar transport into autograd (passive scalars, explicit
+    split transport); other inputs requiring grad are rejected before any device work.
     """
     reject_unsupported_request(initial_state, mesh, config)
     require_finite_inputs(initial_state)
-    if differentiable:
-        raise MpasUnsupportedCapabilityError(
-            "differentiable=True runs are not implemented on the GB300 path; run_simulation.vjp / .jvp "
-            "differentiate with respect to the transported scalars")
     if int(nsteps) != nsteps or nsteps < 0:
         raise MpasConfigError("nsteps must be a non-negative integer")
+    if differentiable and _grad_keys(initial_state, mesh) and nsteps > 0:
+        return _run_differentiable(initial_state, mesh, config, dt, int(nsteps), device, on_step, on_phase,
+                                   on_initial)
     mesh = mesh if mesh is not None else initial_state
     merged = dict(mesh)
     merged.update(initial_state)
@@ -499,6 +501,55 @@ def _scalar_derivative_forward(state: Mapping[str, Any], mesh: Mapping[str, Any]
     if bad:
         raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")
     return model, tape, _merge(state, model.export())
+
+
+def _grad_keys(state: Mapping[str, Any], mesh: Mapping[str, Any] | None) -> list[str]:
+    """The inputs that require gradients; only ``scalars`` can (checked before any
+    device work)."""
+    keys = sorted({k for d in (state, mesh or {}) for k, v in d.items()
+                   if isinstance(v, torch.Tensor) and v.requires_grad})
+    other = [k for k in keys if k != "scalars"]
+    if other:
+        raise MpasUnsupportedCapabilityError(
+            "differentiable runs on the GB300 path carry gradients for 'scalars' only (hand-written adjoint of "
+            f"the scalar transport); inputs requiring grad: {other}")
+    return keys
+
+
+class _ScalarsThroughSteps(torch.autograd.Function):
+    """The end scalars of a taped forward as a function of the start scalars: forward
+    returns the already computed result, backward runs the hand-written transposed
+    transport of every taped step (``mpasg_transport_vjp``)."""
+
+    @staticmethod
+    def forward(ctx, scalars_in, scalars_end, model, tape):  # noqa: D401
+        ctx.model, ctx.tape = model, tape
+        ctx.in_rows, ctx.in_device = scalars_in.shape[0], scalars_in.device
+        return scalars_end.detach().clone()
+
+    @staticmethod
+    def backward(ctx, g_end):
+        from .tracer_adjoint import scalars_vjp
+        g0 = scalars_vjp(ctx.model, ctx.tape, g_end.detach())[:ctx.in_rows]
+        return g0.to(ctx.in_device), None, None, None
+
+
+def _run_differentiable(state, mesh, config, dt, nsteps, device, on_step, on_phase, on_initial) -> dict:
+    """run_simulation(differentiable=True) with ``scalars`` requiring grad: the taped
+    forward, and the end scalars attached to the autograd graph through
+    ``_ScalarsThroughSteps`` (passive scalars, explicit split transport)."""
+    if on_step is not None or on_initial is not None:
+        raise MpasUnsupportedCapabilityError("on_step / on_initial are not available in differentiable runs")
+    plain = {k: (v.detach() if isinstance(v, torch.Tensor) else v) for k, v in state.items()}
+    if on_phase is not None:
+        on_phase("forecast_integration_begin")
+    model, tape, out = _scalar_derivative_forward(plain, mesh, {"config": config, "dt": dt, "nsteps": nsteps,
+                                                                "device": device})
+    if on_phase is not None:
+        on_phase("forecast_integration_end")
+    out = dict(out)
+    out["scalars"] = _ScalarsThroughSteps.apply(state["scalars"], out["scalars"], model, tape)
+    return out
 
 
 def run_simulation_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any], objective: Callable,

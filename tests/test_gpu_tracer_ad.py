@@ -123,3 +123,25 @@ def test_mixed_precision_derivatives_within_stated_error():
     eg, et = rel_l2(g, GOLDEN["vjp_scalars"]), rel_l2(t, GOLDEN["jvp_scalars"])
     assert eg <= 1e-4 and et <= 1e-4, (eg, et)
     assert max(eg, et) > 1e-12  # float32 arithmetic really ran
+
+
+def test_autograd_through_a_differentiable_run():
+    """run_simulation(differentiable=True) with the start scalars requiring grad: the
+    end scalars equal the plain run's, and backward() gives the reference's VJP (the same
+    numbers as run_simulation.vjp)."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import run_simulation
+    state, meta = _case()
+    w = torch.as_tensor(GOLDEN["weights"]).cuda()
+    x = state["scalars"].clone().requires_grad_(True)
+    st = dict(state)
+    st["scalars"] = x
+    out = run_simulation(st, state, meta["config"], meta["dt"], nsteps=2, differentiable=True)
+    assert out["scalars"].requires_grad
+    plain = run_simulation(state, state, meta["config"], meta["dt"], nsteps=2)
+    assert torch.equal(out["scalars"].detach(), plain["scalars"])
+    (out["scalars"] * w).sum().backward()
+    assert rel_l2(x.grad.numpy(), GOLDEN["vjp_scalars"]) <= GRAD_TOL
+    via_vjp = run_simulation.vjp(state, state, lambda o: (o["scalars"] * w).sum(), track_keys=("scalars",),
+                                 config=meta["config"], dt=meta["dt"], nsteps=2)["scalars"]
+    assert torch.equal(x.grad, via_vjp.to(x.grad.device))

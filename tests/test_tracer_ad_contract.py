@@ -51,3 +51,15 @@ def test_jvp_perturbation_contract():
         run_simulation.jvp(state, state, {"scalars": torch.zeros(3, 2)}, config=meta["config"])
     with pytest.raises(TypeError):
         run_simulation.jvp(state, state, {"scalars": np.zeros(3)}, config=meta["config"])
+
+
+def test_differentiable_runs_carry_scalar_gradients_only():
+    """differentiable=True with a non-scalar input requiring grad is rejected before any
+    device work (the GB300 adjoint covers the scalar transport)."""
+    import mpas_dycore_pytorch_gb300 as gb
+    from fixtures import group, load_case
+    meta, st, _ = load_case("g2_explicit")
+    state = {k: torch.as_tensor(v) for k, v in group(st, "loaded").items()}
+    state["u"] = state["u"].clone().requires_grad_(True)
+    with pytest.raises(gb.MpasUnsupportedCapabilityError, match="scalars"):
+        gb.run_simulation(state, state, meta["config"], meta["dt"], nsteps=1, differentiable=True)
