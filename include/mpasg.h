@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define MPASG_ABI_VERSION 3
+#define MPASG_ABI_VERSION 4
 
 enum {
   MPASG_OK = 0,
@@ -286,6 +286,24 @@ int mpasg_transport_vjp(const mpasg_mesh *m, const mpasg_config *c, const double
                         const double *wwavg, const double *rho_old, const double *rho_new,
                         const int32_t *adj_ptr, const int32_t *adj_es, const double *edge_cell_w,
                         const double *g_out, double *g_in, double *work, void *stream);
+/* One explicit transport stage's vector-Jacobian product (the stage of
+ * mpas_pytorch/dynamics/advance_scalars.py:1272: s_out = (s_old rho_old + dt_stage (H(s_in)
+ * - V(s_in))) / (w_old rho_old + w_new rho_new), fluxes ruavg / wwavg fixed): from the
+ * cotangent g_out (C+1, L, S) of the stage output, writes the cotangent of s_in into the
+ * active rows of g_sin and adds the cotangent of s_old into g_sold.  work_edges:
+ * (E+1) L S doubles.  Used for the coupled transport mode, where every RK stage has its
+ * own fluxes and density (w_old = 0, w_new = 1); adjacency arrays as for
+ * mpasg_transport_vjp. */
+int mpasg_transport_vjp_stage(const mpasg_mesh *m, const mpasg_config *c, double dt_stage, double w_old,
+                              double w_new, const double *ruavg, const double *wwavg, const double *rho_old,
+                              const double *rho_new, const int32_t *adj_ptr, const int32_t *adj_es,
+                              const double *edge_cell_w, const double *g_out, double *g_sin, double *g_sold,
+                              double *work_edges, void *stream);
+/* One large step in the coupled transport mode (dynamics_split_steps == 1) that also
+ * writes every RK stage's transport inputs into tape: for stage rk (1..3), at offset
+ * (rk-1) ((E+1) L + (C+1)(L+1) + (C+1) L), ruAvg (E+1, L), wwAvg (C+1, L+1) and rho_zz
+ * (C+1, L) after the stage's recovery (time_integration.py:7890-8200). */
+int mpasg_step_taped(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, double *tape, void *stream);
 /* Float64 arithmetic peak of this GPU, measured: `blocks` x 256 threads each run `iters`
  * rounds of 8 independent fused multiply-adds on values read from buf (blocks * 256
  * doubles, written back so nothing is optimised away); *flops_per_s receives

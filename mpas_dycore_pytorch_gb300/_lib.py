@@ -13,7 +13,7 @@ import pathlib
 from .errors import MpasConfigError, MpasDeviceError, MpasExtensionMissingError, MpasNumericalError
 
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "libmpasg.so"
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 MESH_INT_DIMS = ("nCells", "nEdges", "nVertices", "nVertLevels", "maxEdges", "maxEdges2",
                  "vertexDegree", "nAdvMax", "flatTerrain", "reserved0")
@@ -139,7 +139,7 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_weighted_sq_sum", "mpasg_sfc_order", "mpasg_edge_order", "mpasg_permute_rows",
            "mpasg_tridiag_solve", "mpasg_tridiag_solve_vjp", "mpasg_tridiag_solve_jvp", "mpasg_tridiag_factor",
            "mpasg_tridiag_factor_vjp", "mpasg_tridiag_factor_jvp", "mpasg_autotune", "mpasg_fp64_peak",
-           "mpasg_transport_vjp")
+           "mpasg_transport_vjp", "mpasg_transport_vjp_stage", "mpasg_step_taped")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -183,6 +183,8 @@ def load() -> C.CDLL:
         "mpasg_numerics_check": ([C.c_int, vp, vp, C.c_longlong, vp], C.c_int),
         "mpasg_fp64_peak": ([vp, C.c_int, C.c_int, vp, vp], C.c_int),
         "mpasg_transport_vjp": ([m, c] + [vp] * 11, C.c_int),
+        "mpasg_transport_vjp_stage": ([m, c, C.c_double, C.c_double, C.c_double] + [vp] * 12, C.c_int),
+        "mpasg_step_taped": ([m, c, f, vp, vp], C.c_int),
         "mpasg_surface_pressure": ([C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, vp, vp],
                                    C.c_int),
         "mpasg_weighted_sq_sum": ([C.c_longlong, vp, vp, vp, vp, vp], C.c_int),

@@ -493,10 +493,9 @@ def _scalar_derivative_forward(state: Mapping[str, Any], mesh: Mapping[str, Any]
         model.load_boundary(state)
     else:
         model.prepare(merged)
-    tape = ScalarTape()
+    tape = ScalarTape(model)
     for _ in range(nsteps):
-        model.step()
-        tape.record(model)
+        tape.step(model)
     bad = model.check_finite()
     if bad:
         raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")

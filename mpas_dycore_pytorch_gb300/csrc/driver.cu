@@ -209,12 +209,19 @@ struct StageRecorder {
   }
 };
 
-int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec);
+int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec,
+              double* tape = nullptr);
 }  // namespace
 
 extern "C" int mpasg_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, void* stream) {
   if (!m || !c || !fin) return MPASG_E_ARG;
   return step_impl(m, c, fin, (cudaStream_t)stream, nullptr);
+}
+
+extern "C" int mpasg_step_taped(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, double* tape,
+                                void* stream) {
+  if (!m || !c || !fin || !tape || c->dynamics_split_steps != 1 || c->num_scalars < 1) return MPASG_E_ARG;
+  return step_impl(m, c, fin, (cudaStream_t)stream, nullptr, tape);
 }
 
 extern "C" int mpasg_step_timed(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, void* const* events,
@@ -243,7 +250,8 @@ int transport_stage(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
   return MPASG_OK;
 }
 
-int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec) {
+int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec,
+              double* tape) {
   void* stream = (void*)s;
 #define MARK(kind)                                  \
   do {                                              \
@@ -317,6 +325,12 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
       if (coupled && advect) {  // time_integration.py:7890-8200: stage dt, this stage's mass fluxes
         CHECK_RC(transport_stage(m, c, &f, rk, rk_ts[rk - 1], s));
         MARK(rk == 3 && c->monotonic ? MPASG_STAGE_SCALARS_MONO : MPASG_STAGE_SCALARS);
+        if (tape) {  // the stage's transport inputs, for the scalar derivatives
+          double* t = tape + (rk - 1) * (nel + ncw + ncl);
+          CHECK_RC(copy(t, f.ruAvg, nel, s));
+          CHECK_RC(copy(t + nel, f.wwAvg, ncw, s));
+          CHECK_RC(copy(t + nel + ncw, f.rho_zz, ncl, s));
+        }
       }
       CHECK_RC(mpasgi_solve_diagnostics(m, c, &f, rk, s, true));
       MARK(MPASG_STAGE_DIAG);

@@ -119,6 +119,32 @@ __global__ void k_tadj_finish(long long n, const double* __restrict__ a, const d
 
 }  // namespace
 
+namespace {
+// One explicit stage's adjoint: g (cotangent of the stage output) -> sbar (cotangent of
+// the stage input, active rows) and gold += (cotangent of s_old); hb: edge scratch.
+int tadj_stage(const mpasg_mesh* m, int S, double dt, double w_old, double w_new, double coef3, const double* ruavg,
+               const double* wwavg, const double* rho_old, const double* rho_new, const int32_t* adj_ptr,
+               const int32_t* adj_es, const double* edge_cell_w, const double* g, double* gold, double* sbar,
+               double* hb, cudaStream_t s) {
+  const int L = m->nVertLevels;
+  FastDiv fl(L);
+  const long long ncl = (long long)m->nCells * L, nel = (long long)m->nEdges * L;
+  k_tadj_cells_v<<<nblocks(ncl), kBlock, 0, s>>>(*m, fl, S, dt, w_old, w_new, coef3, wwavg, rho_old, rho_new, g,
+                                                 gold, sbar);
+  MPASG_LAUNCH_CHECK();
+  k_tadj_edges<<<nblocks(nel), kBlock, 0, s>>>(*m, fl, S, dt, w_old, w_new, ruavg, edge_cell_w, rho_old, rho_new, g,
+                                               hb);
+  MPASG_LAUNCH_CHECK();
+  k_tadj_cells_h<<<nblocks(ncl), kBlock, 0, s>>>(*m, fl, S, ruavg, adj_ptr, adj_es, hb, sbar);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
+bool tadj_supported(const mpasg_config* c) {
+  return c->num_scalars >= 1 && c->num_scalars <= 8 && !c->monotonic && !c->scalar_advection_off;
+}
+}  // namespace
+
 extern "C" int mpasg_transport_vjp(const mpasg_mesh* m, const mpasg_config* c, const double* ruavg,
                                    const double* wwavg, const double* rho_old, const double* rho_new,
                                    const int32_t* adj_ptr, const int32_t* adj_es, const double* edge_cell_w,
@@ -126,8 +152,8 @@ extern "C" int mpasg_transport_vjp(const mpasg_mesh* m, const mpasg_config* c, c
   if (!m || !c || !ruavg || !wwavg || !rho_old || !rho_new || !adj_ptr || !adj_es || !edge_cell_w || !g_out ||
       !g_in || !work)
     return MPASG_E_ARG;
+  if (!tadj_supported(c) || c->dynamics_split_steps < 2) return MPASG_E_ARG;
   const int S = c->num_scalars;
-  if (S < 1 || S > 8 || c->monotonic || c->dynamics_split_steps < 2 || c->scalar_advection_off) return MPASG_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const int L = m->nVertLevels;
   // work: three cell cotangent buffers, then the edge cotangents ((E+1) L S)
@@ -141,8 +167,7 @@ extern "C" int mpasg_transport_vjp(const mpasg_mesh* m, const mpasg_config* c, c
   if (cudaMemsetAsync(gb, 0, ncs * sizeof(double), s) != cudaSuccess) return MPASG_E_CUDA;
   const double dt = c->dt;
   const double dts[3] = {c->time_integration_order == 2 ? dt / 2.0 : dt / 3.0, dt / 2.0, dt};
-  FastDiv fl(L);
-  const long long ncl = (long long)m->nCells * L, nel = (long long)m->nEdges * L;
+  const long long ncl = (long long)m->nCells * L;
   const double* g = g_out;
   double* outs[3] = {ga, gb, ga};  // stage 3 -> ga, stage 2 -> gb, stage 1 -> ga
   for (int rk = 3; rk >= 1; --rk) {
@@ -150,16 +175,10 @@ extern "C" int mpasg_transport_vjp(const mpasg_mesh* m, const mpasg_config* c, c
     if (rk == 1 && c->time_integration_order == 3) w_new = 1.0 / 3.0;
     else if ((rk == 1 && c->time_integration_order == 2) || rk == 2) w_new = 1.0 / 2.0;
     else w_new = 1.0;
-    const double w_old = 1.0 - w_new;
     double* sbar = outs[3 - rk];
-    k_tadj_cells_v<<<nblocks(ncl), kBlock, 0, s>>>(*m, fl, S, dts[rk - 1], w_old, w_new, c->coef_3rd_order, wwavg,
-                                                   rho_old, rho_new, g, gacc, sbar);
-    MPASG_LAUNCH_CHECK();
-    k_tadj_edges<<<nblocks(nel), kBlock, 0, s>>>(*m, fl, S, dts[rk - 1], w_old, w_new, ruavg, edge_cell_w, rho_old,
-                                                 rho_new, g, hb);
-    MPASG_LAUNCH_CHECK();
-    k_tadj_cells_h<<<nblocks(ncl), kBlock, 0, s>>>(*m, fl, S, ruavg, adj_ptr, adj_es, hb, sbar);
-    MPASG_LAUNCH_CHECK();
+    const int rc = tadj_stage(m, S, dts[rk - 1], 1.0 - w_new, w_new, c->coef_3rd_order, ruavg, wwavg, rho_old,
+                              rho_new, adj_ptr, adj_es, edge_cell_w, g, gacc, sbar, hb, s);
+    if (rc != MPASG_OK) return rc;
     g = sbar;  // the previous stage's output cotangent
   }
   // s_in of stage 1 is the step's start: its cotangent joins the s_old cotangents; the
@@ -170,4 +189,17 @@ extern "C" int mpasg_transport_vjp(const mpasg_mesh* m, const mpasg_config* c, c
                       s) != cudaSuccess)
     return MPASG_E_CUDA;
   return MPASG_OK;
+}
+
+extern "C" int mpasg_transport_vjp_stage(const mpasg_mesh* m, const mpasg_config* c, double dt_stage, double w_old,
+                                         double w_new, const double* ruavg, const double* wwavg,
+                                         const double* rho_old, const double* rho_new, const int32_t* adj_ptr,
+                                         const int32_t* adj_es, const double* edge_cell_w, const double* g_out,
+                                         double* g_sin, double* g_sold, double* work_edges, void* stream) {
+  if (!m || !c || !ruavg || !wwavg || !rho_old || !rho_new || !adj_ptr || !adj_es || !edge_cell_w || !g_out ||
+      !g_sin || !g_sold || !work_edges || g_sin == g_out)
+    return MPASG_E_ARG;
+  if (!tadj_supported(c)) return MPASG_E_ARG;
+  return tadj_stage(m, c->num_scalars, dt_stage, w_old, w_new, c->coef_3rd_order, ruavg, wwavg, rho_old, rho_new,
+                    adj_ptr, adj_es, edge_cell_w, g_out, g_sold, g_sin, work_edges, (cudaStream_t)stream);
 }

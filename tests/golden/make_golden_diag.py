@@ -13,7 +13,8 @@ reference the same way as ``make_golden.py`` (netCDF4 stub).
 
 Also runs the reference's ``run_simulation.vjp`` / ``.jvp`` with respect to the scalars on
 the g2_explicit case (two steps) and writes the weights, tangent and results to
-``scalars_ad_g2.npz``.
+``scalars_ad_g2.npz``; the same in the coupled transport mode (g2_coupled mesh, explicit
+stages) to ``scalars_ad_g2_coupled.npz``.
 
 Run:  python tests/golden/make_golden_diag.py
 """
@@ -70,6 +71,25 @@ def main() -> None:
                "jvp_keys": np.array(sorted(tangents))})
     np.savez_compressed(HERE / "scalars_ad_g2.npz", **ad)
     print("wrote", HERE / "scalars_ad_g2.npz", sorted(ad))
+
+    # the same in the coupled transport mode (config_split_dynamics_transport = false: the
+    # scalars advance inside every RK stage with that stage's fluxes), explicit stages,
+    # on the g2_coupled mesh and tracers, two steps
+    case = dict(make_golden.CASES["g2_coupled"], config=dict(config_monotonic=False,
+                                                             config_split_dynamics_transport=False))
+    state, meshd, cfg = make_golden.load_reference_case(mp, case)
+    g = torch.Generator().manual_seed(20261204)
+    sc = state["scalars"]
+    wts = torch.rand(sc.shape, generator=g, dtype=torch.float64)
+    tan = torch.randn(sc.shape, generator=g, dtype=torch.float64)
+    kw = dict(config=cfg, dt=case["dt"], nsteps=2)
+    grads = mp.run_simulation.vjp(state, meshd, lambda o: (o["scalars"] * wts).sum(), track_keys=("scalars",), **kw)
+    tangents = mp.run_simulation.jvp(state, meshd, {"scalars": tan}, **kw)
+    adc = {"weights": wts.numpy(), "vjp_scalars": grads["scalars"].detach().numpy(), "tangent": tan.numpy(),
+           "jvp_scalars": tangents["scalars"].detach().numpy(), "config": np.array(repr(cfg)),
+           "dt": np.array(case["dt"])}
+    np.savez_compressed(HERE / "scalars_ad_g2_coupled.npz", **adc)
+    print("wrote", HERE / "scalars_ad_g2_coupled.npz", sorted(adc))
     print("wrote", HERE / "sp_g2.npz", sorted(out))
 
     from mpas_pytorch.mesh_reordering import apply_rcm_reordering

@@ -145,3 +145,45 @@ def test_autograd_through_a_differentiable_run():
     via_vjp = run_simulation.vjp(state, state, lambda o: (o["scalars"] * w).sum(), track_keys=("scalars",),
                                  config=meta["config"], dt=meta["dt"], nsteps=2)["scalars"]
     assert torch.equal(x.grad, via_vjp.to(x.grad.device))
+
+
+GOLDEN_C = np.load(pathlib.Path(__file__).resolve().parent / "golden" / "scalars_ad_g2_coupled.npz")
+
+
+def _coupled_case():
+    meta, st, _ = load_case("g2_coupled")
+    state = {k: torch.as_tensor(v) for k, v in group(st, "loaded").items()}
+    state.update(meta["loaded_scalars"])
+    return state, dict(meta["config"], config_monotonic=False), float(meta["dt"])
+
+
+def test_coupled_mode_vjp_and_jvp_match_reference():
+    """Coupled transport (the scalars advance inside every RK stage with that stage's
+    fluxes): the stage-by-stage adjoint and the replayed tangent against the reference's
+    run_simulation.vjp / .jvp (golden scalars_ad_g2_coupled.npz, two steps)."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import run_simulation
+    state, cfg, dt = _coupled_case()
+    w = torch.as_tensor(GOLDEN_C["weights"]).cuda()
+    g = run_simulation.vjp(state, state, lambda o: (o["scalars"] * w).sum(), track_keys=("scalars",), config=cfg,
+                           dt=dt, nsteps=2)["scalars"].cpu().numpy()
+    assert rel_l2(g, GOLDEN_C["vjp_scalars"]) <= GRAD_TOL
+    t = run_simulation.jvp(state, state, {"scalars": torch.as_tensor(GOLDEN_C["tangent"])}, config=cfg, dt=dt,
+                           nsteps=2)["scalars"].cpu().numpy()
+    assert rel_l2(t, GOLDEN_C["jvp_scalars"]) <= GRAD_TOL
+
+
+def test_coupled_mode_dot_product_identity():
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import run_simulation
+    st, cfg = _level3()
+    cfg = dict(cfg, config_split_dynamics_transport=False)
+    g = torch.Generator().manual_seed(17)
+    v = torch.randn(st["scalars"].shape, generator=g, dtype=torch.float64)
+    w = torch.randn(st["scalars"].shape, generator=g, dtype=torch.float64).cuda()
+    jv = run_simulation.jvp(st, st, {"scalars": v}, config=cfg, nsteps=3)["scalars"].cuda()
+    jtw = run_simulation.vjp(st, st, lambda o: (o["scalars"] * w).sum(), track_keys=("scalars",), config=cfg,
+                             nsteps=3)["scalars"].cuda()
+    lhs = float((jv * w).sum())
+    rhs = float((v.cuda() * jtw).sum())
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs))

@@ -25,7 +25,7 @@ def test_vjp_tracks_scalars_only():
 
 
 @pytest.mark.parametrize("extra", [{"config_monotonic": True}, {"config_positive_definite": True},
-                                   {"config_split_dynamics_transport": False}, {"config_dynamics_split_steps": 1},
+                                   {"config_monotonic": True, "config_split_dynamics_transport": False},
                                    {"config_scalar_advection": False}])
 def test_unsupported_transport_rejected(extra):
     state, meta = _case()
