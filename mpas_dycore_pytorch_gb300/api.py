@@ -206,6 +206,11 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
     return c
 
 
+# boundary fields written by the second part of a step (mpasg_step_part 1)
+LATE_KEYS = ("scalars", "uReconstructX", "uReconstructY", "uReconstructZ", "uReconstructZonal",
+             "uReconstructMeridional", "ur_cell", "vr_cell")
+
+
 def _stream_ptr(stream: torch.cuda.Stream | None = None) -> C.c_void_p:
     s = stream if stream is not None else torch.cuda.current_stream()
     return C.c_void_p(s.cuda_stream)
@@ -252,6 +257,7 @@ class Model:
         # static fields the step reads from the state side
         self.state.load(mesh, keys=("rt_diabatic_tend",))
         self._graph = None
+        self._graph_parts = None
         self._d2h_stream = None
         self._pending_d2h: dict[int, torch.cuda.Event] = {}
         self._rows_in = self._rows_out = None
@@ -343,6 +349,44 @@ class Model:
         else:
             self.call("mpasg_step")
 
+    def capture_graph_parts(self) -> None:
+        """Capture the two parts of a large step (``mpasg_step_part``) as two CUDA graphs,
+        replayed by ``step_host``."""
+        torch.cuda.synchronize()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        graphs = []
+        for part in (0, 1):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(s):
+                with torch.cuda.graph(g, stream=s):
+                    rc = self.lib.mpasg_step_part(C.byref(self.dmesh.struct), C.byref(self.cstruct),
+                                                  C.byref(self.state.struct), part, C.c_void_p(s.cuda_stream))
+            _lib.check(rc, f"mpasg_step_part {part} (capture)")
+            graphs.append(g)
+        torch.cuda.current_stream().wait_stream(s)
+        self._graph_parts = graphs
+
+    def _step_part(self, part: int) -> None:
+        if self._graph_parts is not None:
+            self._graph_parts[part].replay()
+        else:
+            self.call("mpasg_step_part", part)
+
+    def step_host(self, host: Mapping[str, torch.Tensor]) -> None:
+        """Advance a step boundary held in (pinned) host tensors by one large step, in
+        place: ``load_boundary(host)``, the first part of the step, ``export_to`` of every
+        field that is final by then (all but the scalars and the reconstructed winds), which
+        copies out while the second part (the scalar transport and reconstruction) runs,
+        then ``export_to`` of the rest.  Call ``wait_exports`` before reading ``host``."""
+        self.load_boundary(host)
+        late = {k: v for k, v in host.items() if k in LATE_KEYS}
+        early = {k: v for k, v in host.items() if k not in LATE_KEYS}
+        self._step_part(0)
+        self.export_to(early)
+        self._step_part(1)
+        self.export_to(late)
+
     def capture_graph(self) -> None:
         """Capture one large step as a CUDA graph (replayed by ``step``)."""
         torch.cuda.synchronize()
@@ -367,7 +411,7 @@ class Model:
         rc = self.lib.mpasg_autotune(C.byref(self.dmesh.struct), C.byref(self.cstruct), C.byref(self.state.struct),
                                      times, _stream_ptr())
         _lib.check(rc, "mpasg_autotune")
-        self._graph = None  # a captured graph holds the old tile
+        self._graph = self._graph_parts = None  # captured graphs hold the old tile
         return {"tend_u_levels_per_thread": int(self.cstruct.tile_tend_u),
                 "tend_u_ms": {1: times[0], 2: times[1], 4: times[2]}}
 

@@ -210,12 +210,18 @@ struct StageRecorder {
 };
 
 int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec,
-              double* tape = nullptr);
+              double* tape = nullptr, int part = -1);
 }  // namespace
 
 extern "C" int mpasg_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, void* stream) {
   if (!m || !c || !fin) return MPASG_E_ARG;
   return step_impl(m, c, fin, (cudaStream_t)stream, nullptr);
+}
+
+extern "C" int mpasg_step_part(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, int part,
+                               void* stream) {
+  if (!m || !c || !fin || (part != 0 && part != 1)) return MPASG_E_ARG;
+  return step_impl(m, c, fin, (cudaStream_t)stream, nullptr, nullptr, part);
 }
 
 extern "C" int mpasg_step_taped(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, double* tape,
@@ -250,16 +256,49 @@ int transport_stage(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
   return MPASG_OK;
 }
 
-int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec,
-              double* tape) {
-  void* stream = (void*)s;
 #define MARK(kind)                                  \
   do {                                              \
     if (rec) CHECK_RC(rec->mark((kind), s));        \
   } while (0)
+
+// The end of a large step: the split transport RK3 with the substep-averaged mass fluxes
+// (the coupled mode advanced the scalars inside the RK stages already), the final scalars
+// and the reconstruction.  Writes only the scalars and the reconstructed winds.
+int step_tail(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, cudaStream_t s, StageRecorder* rec) {
+  const long long L = m->nVertLevels, nc = m->nCells;
+  const long long S = c->num_scalars;
+  const bool advect = S > 0 && !c->scalar_advection_off;
+  const bool coupled = c->dynamics_split_steps == 1;
+  const double dt = c->dt;
+  if (advect && !coupled) {
+    CHECK_RC(copy(f.scalars_a, f.scalars_init, (nc + 1) * L * S, s));
+    // transport stage dts; the first is dt/2 for RK2 (time_integration.py:3366-3370)
+    const double dts_t[3] = {c->time_integration_order == 2 ? dt / 2.0 : dt / 3.0, dt / 2.0, dt};
+    MARK(MPASG_STAGE_SPLIT);
+    for (int rk = 1; rk <= 3; ++rk) {
+      CHECK_RC(transport_stage(m, c, &f, rk, dts_t[rk - 1], s));
+      MARK(rk == 3 && c->monotonic ? MPASG_STAGE_SCALARS_MONO : MPASG_STAGE_SCALARS);
+    }
+    // active rows only: the padding row of the scalars passes through the step unchanged,
+    // as in the reference
+    CHECK_RC(copy(f.scalars, f.scalars_a, nc * L * S, s));
+  }
+  MARK(MPASG_STAGE_SPLIT);
+  CHECK_RC(mpasgi_reconstruct(m, c, &f, s, true));
+  MARK(MPASG_STAGE_RECONSTRUCT);
+  return MPASG_OK;
+}
+
+// part -1: the whole step; 0: everything before the split transport (the prognostic and
+// diagnostic fields other than the scalars and reconstructed winds are final after it);
+// 1: step_tail
+int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec,
+              double* tape, int part) {
+  void* stream = (void*)s;
   if (c->time_integration_order != 2 && c->time_integration_order != 3) return MPASG_E_ARG;
   if (c->number_of_sub_steps < 1 || c->dynamics_split_steps < 1) return MPASG_E_ARG;
   mpasg_fields f = *fin;  // local copy: transport ping-pongs its scalar buffers
+  if (part == 1) return step_tail(m, c, f, s, rec);
   const long long L = m->nVertLevels, nc = m->nCells, ne = m->nEdges;
   const long long S = c->num_scalars;
   const bool advect = S > 0 && !c->scalar_advection_off;  // config_scalar_advection
@@ -362,25 +401,10 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   MPASG_LAUNCH_CHECK();
   k_scale_d<<<nblocks(ncw), kBlock, 0, s>>>(f.wwAvg, f.wwAvg_split, inv, ncw);
   MPASG_LAUNCH_CHECK();
-
-  // ---- split transport RK3 with the substep-averaged mass fluxes
-  if (advect && !coupled) {
-    CHECK_RC(copy(f.scalars_a, f.scalars_init, ncs, s));
-    // transport stage dts; the first is dt/2 for RK2 (time_integration.py:3366-3370)
-    const double dts_t[3] = {c->time_integration_order == 2 ? dt / 2.0 : dt / 3.0, dt / 2.0, dt};
-    MARK(MPASG_STAGE_SPLIT);
-    for (int rk = 1; rk <= 3; ++rk) {
-      CHECK_RC(transport_stage(m, c, &f, rk, dts_t[rk - 1], s));
-      MARK(rk == 3 && c->monotonic ? MPASG_STAGE_SCALARS_MONO : MPASG_STAGE_SCALARS);
-    }
-  }
-  // active rows only: the padding row of the scalars passes through the step unchanged,
-  // as in the reference
-  if (advect) CHECK_RC(copy(f.scalars, f.scalars_a, nc * L * S, s));
-  MARK(MPASG_STAGE_SPLIT);
-  CHECK_RC(mpasgi_reconstruct(m, c, &f, s, true));
-  MARK(MPASG_STAGE_RECONSTRUCT);
-  return MPASG_OK;
-#undef MARK
+  // coupled mode: the scalars of the last RK stage are the step's (active rows only)
+  if (advect && coupled) CHECK_RC(copy(f.scalars, f.scalars_a, nc * L * S, s));
+  if (part == 0) return MPASG_OK;
+  return step_tail(m, c, *fin, s, rec);
 }
+#undef MARK
 }  // namespace

@@ -178,3 +178,37 @@ def test_host_chain_through_export_to_matches_resident_steps(order):
         assert torch.equal(host[k], want[k].cpu()), k
     with pytest.raises(Exception):
         chained.export_to({"not_a_field": host["u"]})
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order,coupled", [("native", False), ("sfc", False), ("sfc", True)])
+def test_step_host_in_two_parts_matches_resident_steps(order, coupled):
+    """Model.step_host (the step's two parts as graphs, the final fields copied out while
+    the transport runs) equals whole steps kept on the device, bit for bit."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.device import STATE_KEYS
+    from mpas_dycore_pytorch_gb300.loader import load_case as synth
+    cfg = {"config_time_integration_order": 3, "config_len_disp": 120000.0, "config_monotonic": True,
+           "config_dt": 600.0, "config_split_dynamics_transport": not coupled}
+    st, _ = synth(CaseSpec(level=3, nlev=14, seed=5, n_bumps=3, n_tracers=2), cfg, as_torch=False)
+    resident = Model(st, cfg, 600.0, num_scalars=2, order=order)
+    hosted = Model(st, cfg, 600.0, num_scalars=2, order=order)
+    resident.prepare(st)
+    hosted.prepare(st)
+    start = resident.export()
+    host = {k: torch.empty(start[k].shape, dtype=torch.float64, pin_memory=True) for k in STATE_KEYS}
+    for k in STATE_KEYS:
+        host[k].copy_(start[k])
+    hosted.step_host(host)  # eager parts
+    resident.step()
+    hosted.capture_graph_parts()
+    for _ in range(2):  # graph-replayed parts
+        hosted.step_host(host)
+        resident.step()
+    hosted.wait_exports()
+    torch.cuda.synchronize()
+    want = resident.export()
+    for k in STATE_KEYS:
+        assert torch.equal(host[k], want[k].cpu()), k
