@@ -586,18 +586,14 @@ def run_gb300(args, rank, world):
     for k in keys:
         host[k].copy_(ex0[k])
     h2d = sum(t.numel() * 8 for t in host.values())
-    # the two parts of a step as graphs; warm the host path (staging buffer, copy stream)
+    # the two parts of a step as graphs; warm the host path (staging buffers, copy streams)
     model.capture_graph_parts()
-    for _ in range(W):
-        model.step_host(host)
-    model.wait_exports()
+    model.run_host(host, W)
     torch.cuda.synchronize()
     e_start = torch.cuda.Event(enable_timing=True)
     e_end = torch.cuda.Event(enable_timing=True)
     e_start.record()
-    for _ in range(K):
-        model.step_host(host)
-    model.wait_exports()
+    model.run_host(host, K)
     e_end.record()
     torch.cuda.synchronize()
     e_ms, e_value = replica_throughput(e_start.elapsed_time(e_end), C_ * L_, K, world, dev)

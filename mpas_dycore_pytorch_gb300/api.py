@@ -258,7 +258,7 @@ class Model:
         self.state.load(mesh, keys=("rt_diabatic_tend",))
         self._graph = None
         self._graph_parts = None
-        self._d2h_stream = None
+        self._d2h_stream = self._h2d_stream = None
         self._pending_d2h: dict[int, torch.cuda.Event] = {}
         self._rows_in = self._rows_out = None
         if self._perm is not None:  # device row maps, padding row last
@@ -339,8 +339,9 @@ class Model:
 
     def wait_exports(self) -> None:
         """Make the current stream wait for every ``export_to`` copy issued so far."""
-        if self._d2h_stream is not None:
-            torch.cuda.current_stream().wait_stream(self._d2h_stream)
+        for side in (self._d2h_stream, self._h2d_stream):
+            if side is not None:
+                torch.cuda.current_stream().wait_stream(side)
         self._pending_d2h.clear()
 
     def step(self) -> None:
@@ -386,6 +387,80 @@ class Model:
         self.export_to(early)
         self._step_part(1)
         self.export_to(late)
+
+    def run_host(self, host: Mapping[str, torch.Tensor], nsteps: int) -> None:
+        """Advance a step boundary held in pinned host tensors by ``nsteps`` large steps,
+        in place, copying every step's boundary in from ``host`` and its result back out to
+        ``host`` (the same fields as ``step_host``).  The copies are pipelined on two copy
+        streams: each field of a step's result is copied out as soon as it is final (most
+        of them while the scalar transport runs), and copied back in, for the next step,
+        into a device staging buffer as soon as its copy out has finished; a step starts
+        once all of its inputs are staged.  Returns with the current stream ordered after
+        every copy (``host`` is complete once the current stream reaches that point)."""
+        from .device import ALIASES, ENTITY, FIELD_KIND
+        if self._graph_parts is None:
+            self.capture_graph_parts()
+        dev = self.dmesh.device
+        cur = torch.cuda.current_stream(dev)
+        if self._d2h_stream is None:
+            self._d2h_stream = torch.cuda.Stream(device=dev)
+        if self._h2d_stream is None:
+            self._h2d_stream = torch.cuda.Stream(device=dev)
+        down, up = self._d2h_stream, self._h2d_stream
+        # the copy streams start after everything issued so far (an earlier call's copies
+        # out into these host tensors, loads, steps)
+        up.wait_stream(cur)
+        down.wait_stream(cur)
+        names = {k: ALIASES.get(k, k) for k in host}
+        for k, n in names.items():
+            if n not in self.state.f or tuple(host[k].shape) != tuple(self.state.f[n].shape):
+                raise MpasConfigError(f"run_host: {k!r} is not a field of the step boundary with its shape")
+        staging = {k: torch.empty_like(self.state.f[n]) for k, n in names.items()}
+        rows = {k: (self._rows_in[ENTITY[FIELD_KIND[n]]] if self._perm is not None else None) for k, n in names.items()}
+        ready = {}
+        for k in host:  # the first step's inputs
+            ev = self._pending_d2h.pop(host[k].data_ptr(), None)
+            if ev is not None:
+                up.wait_event(ev)
+            with torch.cuda.stream(up):
+                staging[k].copy_(host[k], non_blocking=True)
+            ready[k] = torch.cuda.Event()
+            ready[k].record(up)
+        late = [k for k in host if k in LATE_KEYS]
+        early = [k for k in host if k not in LATE_KEYS]
+        for step in range(int(nsteps)):
+            for k, n in names.items():  # load the staged inputs into the state
+                cur.wait_event(ready[k])
+                if rows[k] is not None:
+                    self.state.gather_rows(staging[k], rows[k], out=self.state.f[n])
+                else:
+                    self.state.f[n].copy_(staging[k])
+            self.state.f["rho_zz"][self.dmesh.nCells].fill_(1.0)
+            last = step == int(nsteps) - 1
+            for part, keys in ((0, early), (1, late)):
+                self._step_part(part)
+                final = torch.cuda.Event()
+                final.record(cur)
+                down.wait_event(final)
+                for k in keys:
+                    with torch.cuda.stream(down):
+                        src = self._export_field(k, self.state.f[names[k]]) if self._perm is not None \
+                            else self.state.f[names[k]]
+                        host[k].copy_(src, non_blocking=True)
+                    if last:
+                        continue
+                    done = torch.cuda.Event()
+                    done.record(down)
+                    up.wait_event(done)  # the next step's input is this step's output
+                    with torch.cuda.stream(up):
+                        staging[k].copy_(host[k], non_blocking=True)
+                    ready[k] = torch.cuda.Event()
+                    ready[k].record(up)
+        for k in staging:
+            staging[k].record_stream(up)
+        # the state is not touched again before the last copies out have read it
+        cur.wait_stream(down)
+        cur.wait_stream(up)
 
     def capture_graph(self) -> None:
         """Capture one large step as a CUDA graph (replayed by ``step``)."""

@@ -212,3 +212,35 @@ def test_step_host_in_two_parts_matches_resident_steps(order, coupled):
     want = resident.export()
     for k in STATE_KEYS:
         assert torch.equal(host[k], want[k].cpu()), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", ["native", "sfc"])
+def test_run_host_pipeline_matches_resident_steps(order):
+    """Model.run_host (every step's boundary copied in from and out to pinned host
+    tensors, the copies pipelined with the steps on two copy streams) equals the same
+    steps kept on the device, bit for bit."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.device import STATE_KEYS
+    from mpas_dycore_pytorch_gb300.loader import load_case as synth
+    cfg = {"config_time_integration_order": 3, "config_len_disp": 120000.0, "config_monotonic": True,
+           "config_dt": 600.0}
+    st, _ = synth(CaseSpec(level=3, nlev=14, seed=6, n_bumps=3, n_tracers=2), cfg, as_torch=False)
+    resident = Model(st, cfg, 600.0, num_scalars=2, order=order)
+    hosted = Model(st, cfg, 600.0, num_scalars=2, order=order)
+    resident.prepare(st)
+    hosted.prepare(st)
+    start = resident.export()
+    host = {k: torch.empty(start[k].shape, dtype=torch.float64, pin_memory=True) for k in STATE_KEYS}
+    for k in STATE_KEYS:
+        host[k].copy_(start[k])
+    hosted.run_host(host, 1)
+    hosted.run_host(host, 3)
+    for _ in range(4):
+        resident.step()
+    torch.cuda.synchronize()
+    want = resident.export()
+    for k in STATE_KEYS:
+        assert torch.equal(host[k], want[k].cpu()), k
