@@ -299,10 +299,10 @@ int mpasg_transport_vjp_stage(const mpasg_mesh *m, const mpasg_config *c, double
                               const double *rho_new, const int32_t *adj_ptr, const int32_t *adj_es,
                               const double *edge_cell_w, const double *g_out, double *g_sin, double *g_sold,
                               double *work_edges, void *stream);
-/* One large step in two parts: part 0 runs everything before the split scalar transport,
- * after which every field of the step boundary but the scalars and the reconstructed
- * winds (uReconstruct*) is final; part 1 runs the split transport, the final scalars and
- * the reconstruction, and writes nothing else.  Part 0 then part 1 equals mpasg_step bit
+/* One large step in two parts: part 0 runs everything but the split scalar transport
+ * (the reconstruction, which reads u only, included), after which every field of the
+ * step boundary but the scalars is final; part 1 runs the split transport and writes the
+ * final scalars, nothing else of the boundary.  Part 0 then part 1 equals mpasg_step bit
  * for bit; the split lets a caller copy the final fields out while part 1 runs. */
 int mpasg_step_part(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, int part, void *stream);
 /* One large step in the coupled transport mode (dynamics_split_steps == 1) that also

@@ -207,8 +207,7 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
 
 
 # boundary fields written by the second part of a step (mpasg_step_part 1)
-LATE_KEYS = ("scalars", "uReconstructX", "uReconstructY", "uReconstructZ", "uReconstructZonal",
-             "uReconstructMeridional", "ur_cell", "vr_cell")
+LATE_KEYS = ("scalars",)
 
 
 def _stream_ptr(stream: torch.cuda.Stream | None = None) -> C.c_void_p:
@@ -377,9 +376,8 @@ class Model:
     def step_host(self, host: Mapping[str, torch.Tensor]) -> None:
         """Advance a step boundary held in (pinned) host tensors by one large step, in
         place: ``load_boundary(host)``, the first part of the step, ``export_to`` of every
-        field that is final by then (all but the scalars and the reconstructed winds), which
-        copies out while the second part (the scalar transport and reconstruction) runs,
-        then ``export_to`` of the rest.  Call ``wait_exports`` before reading ``host``."""
+        field that is final by then (all but the scalars), which copies out while the
+        second part (the scalar transport) runs, then ``export_to`` of the scalars.  Call ``wait_exports`` before reading ``host``."""
         self.load_boundary(host)
         late = {k: v for k, v in host.items() if k in LATE_KEYS}
         early = {k: v for k, v in host.items() if k not in LATE_KEYS}

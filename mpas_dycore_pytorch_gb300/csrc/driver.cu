@@ -262,8 +262,8 @@ int transport_stage(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
   } while (0)
 
 // The end of a large step: the split transport RK3 with the substep-averaged mass fluxes
-// (the coupled mode advanced the scalars inside the RK stages already), the final scalars
-// and the reconstruction.  Writes only the scalars and the reconstructed winds.
+// (the coupled mode advanced the scalars inside the RK stages already) and the final
+// scalars.  Of the step boundary it writes only the scalars.
 int step_tail(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, cudaStream_t s, StageRecorder* rec) {
   const long long L = m->nVertLevels, nc = m->nCells;
   const long long S = c->num_scalars;
@@ -282,16 +282,14 @@ int step_tail(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, cudaSt
     // active rows only: the padding row of the scalars passes through the step unchanged,
     // as in the reference
     CHECK_RC(copy(f.scalars, f.scalars_a, nc * L * S, s));
+    MARK(MPASG_STAGE_SPLIT);
   }
-  MARK(MPASG_STAGE_SPLIT);
-  CHECK_RC(mpasgi_reconstruct(m, c, &f, s, true));
-  MARK(MPASG_STAGE_RECONSTRUCT);
   return MPASG_OK;
 }
 
-// part -1: the whole step; 0: everything before the split transport (the prognostic and
-// diagnostic fields other than the scalars and reconstructed winds are final after it);
-// 1: step_tail
+// part -1: the whole step; 0: everything but the split transport (every field of the
+// step boundary but the scalars is final after it; the reconstruction reads u only, so
+// it runs before the transport); 1: step_tail
 int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cudaStream_t s, StageRecorder* rec,
               double* tape, int part) {
   void* stream = (void*)s;
@@ -403,6 +401,9 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   MPASG_LAUNCH_CHECK();
   // coupled mode: the scalars of the last RK stage are the step's (active rows only)
   if (advect && coupled) CHECK_RC(copy(f.scalars, f.scalars_a, nc * L * S, s));
+  MARK(MPASG_STAGE_SPLIT);
+  CHECK_RC(mpasgi_reconstruct(m, c, &f, s, true));
+  MARK(MPASG_STAGE_RECONSTRUCT);
   if (part == 0) return MPASG_OK;
   return step_tail(m, c, *fin, s, rec);
 }
