@@ -312,16 +312,18 @@ def measure_scalar_vjp(args, dev):
     m = Model(st, cfg, w["dt"], num_scalars=S, device=dev)
     transport_adjacency(m.dmesh)  # host-built once per mesh
     g_end = torch.rand(m.state.f["scalars"].shape, dtype=torch.float64, device=dev)
+    m.prepare(st)
+    m.step()
+    m.capture_graph()  # the taped forward replays the step graph (bitwise the eager step)
     ms = []
     for rep in range(2):  # the second repetition is timed
         m.prepare(st)
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        tape = ScalarTape()
+        tape = ScalarTape(m)
         for _ in range(nsteps):
-            m.step()
-            tape.record(m)
+            tape.step(m)
         g0 = scalars_vjp(m, tape, g_end)
         b.record()
         torch.cuda.synchronize()
@@ -330,7 +332,8 @@ def measure_scalar_vjp(args, dev):
     return {"workload": "level-5 mesh 10242 cells x 41 levels, 3 passive tracers, explicit transport, 24 steps",
             "value": cl * nsteps / (ms[-1] / 1e3), "unit": UNIT, "ms": ms[-1],
             "forward_graph_ms": ms_fwd * nsteps, "vjp_over_forward": ms[-1] / (ms_fwd * nsteps),
-            "includes": "24 eager forward steps with the transport tape, then the transposed transport of each step",
+            "includes": "24 graph-replayed forward steps with the transport tape, then the transposed transport of "
+                        "each step",
             "gradient_finite": bool(torch.isfinite(g0).all())}
 
 

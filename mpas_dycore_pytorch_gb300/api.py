@@ -611,8 +611,10 @@ def _scalar_derivative_forward(state: Mapping[str, Any], mesh: Mapping[str, Any]
     else:
         model.prepare(merged)
     tape = ScalarTape(model)
-    for _ in range(nsteps):
+    for i in range(nsteps):
         tape.step(model)
+        if i == 0 and nsteps > 1 and not tape.coupled:
+            model.capture_graph()  # later steps replay the step graph (bitwise the eager step)
     bad = model.check_finite()
     if bad:
         raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")
