@@ -157,7 +157,7 @@ int mpasgi_reconstruct(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields*
                        bool copies_current);
 // theta_m - ref_theta and theta_m_save - ref_theta (float32) for the mixed form
 int mpasgi_theta_dev(const mpasg_mesh* m, mpasg_fields* f, cudaStream_t s);
-int mpasgi_theta_edge(const mpasg_mesh* m, mpasg_fields* f, cudaStream_t s);
+int mpasgi_theta_edge(const mpasg_mesh* m, mpasg_fields* f, bool mixed, cudaStream_t s);
 int mpasgi_divergence_damping(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, double dts,
                               cudaStream_t s, bool copies_current);
 int mpasgi_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int small_step, double dts,

@@ -334,7 +334,8 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
   if (S > 0) CHECK_RC(copy(f.scalars_init, f.scalars, ncs, s));
   if (advect && coupled) CHECK_RC(copy(f.scalars_a, f.scalars_init, ncs, s));
   if (c->precision == MPASG_PRECISION_MIXED) CHECK_RC(mpasgi_pack_f32(m, &f, s));
-  CHECK_RC(mpasgi_theta_edge(m, &f, s));  // edge mean of theta_m_save and its reciprocal sum
+  // edge mean of theta_m_save and its reciprocal sum
+  CHECK_RC(mpasgi_theta_edge(m, &f, c->precision == MPASG_PRECISION_MIXED, s));
   MARK(MPASG_STAGE_SETUP);
   CHECK_RC(mpasg_moist_coefficients(m, c, &f, stream));
   MARK(MPASG_STAGE_MOIST);
@@ -390,7 +391,7 @@ int step_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, cud
       CHECK_RC(copy(f.rho_p_save, f.rho_p, ncl, s));
       CHECK_RC(copy(f.theta_m_save, f.theta_m, ncl, s));
       CHECK_RC(copy(f.rr_save, f.rho_p, ncl, s));
-      CHECK_RC(mpasgi_theta_edge(m, &f, s));
+      CHECK_RC(mpasgi_theta_edge(m, &f, c->precision == MPASG_PRECISION_MIXED, s));
     }
   }
   MARK(MPASG_STAGE_SPLIT);

@@ -243,6 +243,9 @@ MPASG_D AcLevel ac_level(const mpasg_mesh& m, const mpasg_fields& f, int c, int 
 // edge mean of theta_m_save, 0.5 (theta_2 + theta_1), the value the acoustic right-hand
 // side takes per edge, and the reciprocal of the sum that divergence damping divides by
 // (theta_m_save only changes at the dynamics substep boundaries)
+// MIXED: the mixed form's divergence damping reads the reciprocal as float32, so it is
+// the float32 reciprocal of the float32 sum (no float64 division)
+template <bool MIXED>
 __global__ void k_theta_edge(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -251,7 +254,8 @@ __global__ void k_theta_edge(mpasg_mesh m, mpasg_fields f, FastDiv fl) {
   const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
   const double sum = f.theta_m_save[(size_t)c2 * L + k] + f.theta_m_save[(size_t)c1 * L + k];
   f.theta_edge_save[i] = 0.5 * sum;
-  f.theta_edge_rsum[i] = 1.0 / sum;  // divergence damping multiplies instead of dividing
+  // divergence damping multiplies instead of dividing
+  f.theta_edge_rsum[i] = MIXED ? f2d_bits(1.0f / d2f_bits(sum)) : 1.0 / sum;
 }
 
 template <typename T>
@@ -953,9 +957,12 @@ extern "C" int mpasg_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, m
   return mpasgi_acoustic_step(m, c, f, small_step, dts, (cudaStream_t)stream, false);
 }
 
-int mpasgi_theta_edge(const mpasg_mesh* m, mpasg_fields* f, cudaStream_t s) {
+int mpasgi_theta_edge(const mpasg_mesh* m, mpasg_fields* f, bool mixed, cudaStream_t s) {
   const int L = m->nVertLevels;
-  k_theta_edge<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L));
+  if (mixed)
+    k_theta_edge<true><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L));
+  else
+    k_theta_edge<false><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L));
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }
@@ -964,7 +971,8 @@ int mpasgi_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_field
                          cudaStream_t s, bool copies_current) {
   if (!m || !c || !f || small_step < 1) return MPASG_E_ARG;
   if (!copies_current) {
-    const int rc = mpasgi_theta_edge(m, f, s);  // the edge theta the right-hand side reads
+    // the edge theta the right-hand side reads
+    const int rc = mpasgi_theta_edge(m, f, c->precision == MPASG_PRECISION_MIXED, s);
     if (rc != MPASG_OK) return rc;
   }
   if (c->precision == MPASG_PRECISION_MIXED && !copies_current) {
@@ -1035,7 +1043,8 @@ int mpasgi_divergence_damping(const mpasg_mesh* m, const mpasg_config* c, mpasg_
   if (!m || !c || !f) return MPASG_E_ARG;
   const int L = m->nVertLevels;
   if (!copies_current) {
-    const int rc = mpasgi_theta_edge(m, f, stream);  // the reciprocal edge sums read below
+    // the reciprocal edge sums read below
+    const int rc = mpasgi_theta_edge(m, f, c->precision == MPASG_PRECISION_MIXED, stream);
     if (rc != MPASG_OK) return rc;
   }
   double coef = 2.0 * c->smdiv * c->len_disp / dts;

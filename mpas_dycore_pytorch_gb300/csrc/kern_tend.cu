@@ -851,7 +851,7 @@ int mpasgi_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
                     bool copies_current) {
   if (!m || !c || !f || rk_step < 1 || rk_step > 3) return MPASG_E_ARG;
   if (!copies_current && rk_step > 1 && c->precision != MPASG_PRECISION_MIXED) {
-    const int rc = mpasgi_theta_edge(m, f, s);  // the edge mean of theta_m_save read below
+    const int rc = mpasgi_theta_edge(m, f, false, s);  // the edge mean of theta_m_save read below
     if (rc != MPASG_OK) return rc;
   }
   if (m->nVertLevels < 4) return MPASG_E_ARG;
