@@ -206,8 +206,10 @@ def make_config(cfg: Mapping[str, Any], mesh: Mapping[str, Any], dt: float, num_
     return c
 
 
-# boundary fields written by the second part of a step (mpasg_step_part 1)
+# boundary fields written by the second part of a step (mpasg_step_part 1), and those a
+# step never writes (base state and diabatic forcing, set by the preparation)
 LATE_KEYS = ("scalars",)
+STATIC_KEYS = ("rtheta_base", "exner_base", "pressure_base", "rt_diabatic_tend")
 
 
 def _stream_ptr(stream: torch.cuda.Stream | None = None) -> C.c_void_p:
@@ -424,8 +426,9 @@ class Model:
                 staging[k].copy_(host[k], non_blocking=True)
             ready[k] = torch.cuda.Event()
             ready[k].record(up)
+        static = [k for k in host if k in STATIC_KEYS]
         late = [k for k in host if k in LATE_KEYS]
-        early = [k for k in host if k not in LATE_KEYS]
+        early = [k for k in host if k not in LATE_KEYS and k not in STATIC_KEYS]
         for step in range(int(nsteps)):
             for k, n in names.items():  # load the staged inputs into the state
                 cur.wait_event(ready[k])
@@ -435,8 +438,11 @@ class Model:
                     self.state.f[n].copy_(staging[k])
             self.state.f["rho_zz"][self.dmesh.nCells].fill_(1.0)
             last = step == int(nsteps) - 1
-            for part, keys in ((0, early), (1, late)):
-                self._step_part(part)
+            # fields the step never writes are final once loaded; the others after the
+            # part of the step that writes them last
+            for part, keys in ((None, static), (0, early), (1, late)):
+                if part is not None:
+                    self._step_part(part)
                 final = torch.cuda.Event()
                 final.record(cur)
                 down.wait_event(final)
