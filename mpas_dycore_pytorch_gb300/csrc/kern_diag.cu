@@ -64,13 +64,15 @@ __global__ void k_diag_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, int apvm)
   for (int j = 0; j < n; ++j) {
     int e = m.edgesOnCell[c * me + j];
     double t = m.cell_edge_sdv[c * me + j] * f.u[(size_t)e * L + k];  // (sign * dvEdge) * u
-    T kt = T(0.25) * fp<T>(f.ke_edge, f.ke_edge_f32)[(size_t)e * L + k];
+    T kt = fp<T>(f.ke_edge, f.ke_edge_f32)[(size_t)e * L + k];
     div = (j == 0) ? t : div + t;
     ke = (j == 0) ? kt : ke + kt;
   }
   div = div * m.invAreaCell[c];
   const T ia = G(invAreaCell)[c];
-  ke = ke * ia;
+  // sum_j 0.25 ke_edge_j: the power-of-two factor applied once to the sum (scaling by
+  // 0.25 commutes with every rounding of the sum)
+  ke = (T(0.25) * ke) * ia;
   const T ke_fact = T(1.0 - 0.375);
   ke = ke_fact * ke;
   const int vd = m.vertexDegree;
