@@ -30,6 +30,8 @@
  *   mpasg_advance_scalars_mono  dynamics/advance_scalars_mono.py:2878
  *   mpasg_reconstruct_2d        dynamics/vector_reconstruction.py:311
  *   mpasg_surface_pressure      diagnostics.py:10  physics_interface_surface_pressure
+ *   mpasg_surface_pressure_vjp / _jvp, mpasg_weighted_sq_sum_vjp
+ *                               torch autograd through diagnostics.py:77-82 (reverse / forward mode)
  *   mpasg_sfc_order, mpasg_edge_order  mesh_reordering.py:106 compute_rcm_permutation (SFC orders)
  *   mpasg_tridiag_*             autodiff/tridiagonal_solve.py:177, autodiff/tridiagonal_factor.py:145
  *   mpasg_advance_scalars_static  (no counterpart: advance_scalars.py:1272 without caller scratch)
@@ -359,6 +361,31 @@ int mpasg_surface_pressure(int nCells, int rows, int nVertLevels, const double *
  * surface-pressure anomaly functional of the differentiation tests. */
 int mpasg_weighted_sq_sum(long long n, const double *x, const double *ref, const double *weight,
                           double *out, void *stream);
+
+/* Derivatives of mpasg_surface_pressure (the derivatives torch's autograd takes of
+ * mpas_pytorch/diagnostics.py:77-82 when the reference's physics_interface_surface_pressure
+ * is called on tensors that require grad), bit-identical to torch's reverse and forward
+ * modes on that expression.  Shapes as mpasg_surface_pressure; qv may be null (dry).
+ *   vjp: g_sp (rows) -> g_rho_zz, g_qv, g_pressure_p, g_pressure_base, each (rows, L) and
+ *        fully written (levels 0 and 1 of active cells carry the derivative; other entries
+ *        and the padding row are 0); any output may be null (not computed);
+ *   jvp: tangents (rows, L) of the same four inputs (null = zero) -> t_sp (rows, padding
+ *        row 0). */
+int mpasg_surface_pressure_vjp(int nCells, int rows, int nVertLevels, const double *rho_zz,
+                               const double *zz, const double *qv, const double *zgrid,
+                               double gravity, const double *g_sp, double *g_rho_zz, double *g_qv,
+                               double *g_pressure_p, double *g_pressure_base, void *stream);
+int mpasg_surface_pressure_jvp(int nCells, int rows, int nVertLevels, const double *rho_zz,
+                               const double *zz, const double *qv, const double *zgrid,
+                               double gravity, const double *t_rho_zz, const double *t_qv,
+                               const double *t_pressure_p, const double *t_pressure_base,
+                               double *t_sp, void *stream);
+/* Gradient of mpasg_weighted_sq_sum scaled by the device scalar *g_out (no host sync):
+ * g_x_i = 2 ((g_out weight_i)(x_i - ref_i)), g_ref = -g_x; g_x / g_ref may be null.
+ * Replaces torch's autograd through the reference-style objective
+ * sum(area * (sp - sp_ref)^2) of the differentiation checks. */
+int mpasg_weighted_sq_sum_vjp(long long n, const double *x, const double *ref, const double *weight,
+                              const double *g_out, double *g_x, double *g_ref, void *stream);
 
 /* ---- column tridiagonal operators and their derivatives --------------------------- */
 /* One column per row: a / b / c / alpha / gamma are (n, L), rhs / out (n, L+1), float64.

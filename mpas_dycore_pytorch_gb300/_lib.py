@@ -139,7 +139,8 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_weighted_sq_sum", "mpasg_sfc_order", "mpasg_edge_order", "mpasg_permute_rows",
            "mpasg_tridiag_solve", "mpasg_tridiag_solve_vjp", "mpasg_tridiag_solve_jvp", "mpasg_tridiag_factor",
            "mpasg_tridiag_factor_vjp", "mpasg_tridiag_factor_jvp", "mpasg_autotune", "mpasg_fp64_peak",
-           "mpasg_transport_vjp", "mpasg_transport_vjp_stage", "mpasg_step_taped", "mpasg_step_part")
+           "mpasg_transport_vjp", "mpasg_transport_vjp_stage", "mpasg_step_taped", "mpasg_step_part",
+           "mpasg_surface_pressure_vjp", "mpasg_surface_pressure_jvp", "mpasg_weighted_sq_sum_vjp")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -189,6 +190,11 @@ def load() -> C.CDLL:
         "mpasg_surface_pressure": ([C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, vp, vp],
                                    C.c_int),
         "mpasg_weighted_sq_sum": ([C.c_longlong, vp, vp, vp, vp, vp], C.c_int),
+        "mpasg_surface_pressure_vjp": ([C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_double] + [vp] * 6,
+                                       C.c_int),
+        "mpasg_surface_pressure_jvp": ([C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_double] + [vp] * 6,
+                                       C.c_int),
+        "mpasg_weighted_sq_sum_vjp": ([C.c_longlong] + [vp] * 7, C.c_int),
         "mpasg_sfc_order": ([C.c_longlong, vp, vp, vp, vp], C.c_int),
         "mpasg_edge_order": ([C.c_longlong, C.c_longlong, vp, vp, vp], C.c_int),
         "mpasg_permute_rows": ([vp, vp, vp, C.c_longlong, C.c_longlong, vp], C.c_int),

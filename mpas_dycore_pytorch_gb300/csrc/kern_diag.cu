@@ -210,6 +210,83 @@ __global__ void __launch_bounds__(1024) k_weighted_sq_sum(long long n, const dou
   if (threadIdx.x == 0) *out = part[0];
 }
 
+// Derivatives of the surface pressure (diagnostics.py:77-82) with respect to rho_zz, qv,
+// pressure_p and pressure_base.  hyd = A * B with A = (g/2) tem1 and
+// B = rho1 - ((0.5 (rho2 - rho1)) tem1) / s, s = tem1 + tem2; read backwards in the order
+// torch's reverse mode evaluates that expression, so the result is bit-identical to it.
+// One thread per cell-level of the (rows, L) cotangent arrays: levels 0 and 1 of the
+// active cells carry the derivative, every other entry is written 0.  Null outputs skip.
+__global__ void k_surface_pressure_vjp(int nc, int rows, int L, const double* __restrict__ rho_zz,
+                                       const double* __restrict__ zz, const double* __restrict__ qv,
+                                       const double* __restrict__ zgrid, double half_g,
+                                       const double* __restrict__ g_sp, double* __restrict__ g_rho,
+                                       double* __restrict__ g_qv, double* __restrict__ g_pp,
+                                       double* __restrict__ g_pb) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)rows * L) return;
+  const int c = (int)(i / L), k = (int)(i - (long long)c * L);
+  double gr = 0.0, gq = 0.0, gp = 0.0;
+  if (c < nc && k < 2) {
+    const size_t ow = (size_t)c * (L + 1);
+    const double tem1 = __dsub_rn(zgrid[ow + 1], zgrid[ow]);
+    const double s = __dadd_rn(tem1, __dsub_rn(zgrid[ow + 2], zgrid[ow + 1]));
+    const double g = g_sp[c];
+    const double gB = __dmul_rn(g, __dmul_rn(half_g, tem1));
+    const double gD = __dmul_rn(0.5, __dmul_rn(__ddiv_rn(-gB, s), tem1));
+    const double grho = k == 0 ? __dsub_rn(gB, gD) : gD;  // cotangent of rho1 / rho2
+    const double q = qv ? qv[i] : 0.0;
+    gr = __dmul_rn(__dmul_rn(grho, __dadd_rn(1.0, q)), zz[i]);
+    gq = __dmul_rn(grho, __dmul_rn(rho_zz[i], zz[i]));
+    gp = k == 0 ? g : 0.0;
+  }
+  if (g_rho) g_rho[i] = gr;
+  if (g_qv) g_qv[i] = gq;
+  if (g_pp) g_pp[i] = gp;
+  if (g_pb) g_pb[i] = gp;
+}
+
+// Tangent of the surface pressure for tangents of rho_zz, qv, pressure_p, pressure_base
+// (null tangent = zero), in the order torch's forward mode evaluates the expression.
+__global__ void k_surface_pressure_jvp(int nc, int rows, int L, const double* __restrict__ rho_zz,
+                                       const double* __restrict__ zz, const double* __restrict__ qv,
+                                       const double* __restrict__ zgrid, double half_g,
+                                       const double* __restrict__ t_rho, const double* __restrict__ t_qv,
+                                       const double* __restrict__ t_pp, const double* __restrict__ t_pb,
+                                       double* __restrict__ t_sp) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= rows) return;
+  if (c >= nc) {
+    t_sp[c] = 0.0;
+    return;
+  }
+  const size_t o = (size_t)c * L, ow = (size_t)c * (L + 1);
+  const double tem1 = __dsub_rn(zgrid[ow + 1], zgrid[ow]);
+  const double s = __dadd_rn(tem1, __dsub_rn(zgrid[ow + 2], zgrid[ow + 1]));
+  double d[2];
+  for (int k = 0; k < 2; ++k) {
+    const double q = qv ? qv[o + k] : 0.0;
+    const double a = t_rho ? __dmul_rn(__dmul_rn(t_rho[o + k], zz[o + k]), __dadd_rn(1.0, q)) : 0.0;
+    const double b = t_qv ? __dmul_rn(__dmul_rn(rho_zz[o + k], zz[o + k]), t_qv[o + k]) : 0.0;
+    d[k] = __dadd_rn(a, b);
+  }
+  const double dC = __ddiv_rn(__dmul_rn(__dmul_rn(0.5, __dsub_rn(d[1], d[0])), tem1), s);
+  const double hyd = __dmul_rn(__dmul_rn(half_g, tem1), __dsub_rn(d[0], dC));
+  t_sp[c] = __dadd_rn(__dadd_rn(hyd, t_pp ? t_pp[o] : 0.0), t_pb ? t_pb[o] : 0.0);
+}
+
+// gradient of sum_i w_i (x_i - r_i)^2 scaled by the device scalar *g_out:
+// g_x = 2 ((g_out w) (x - r)); g_r (optional) = -g_x
+__global__ void k_weighted_sq_sum_vjp(long long n, const double* __restrict__ x, const double* __restrict__ r,
+                                      const double* __restrict__ w, const double* __restrict__ g_out,
+                                      double* __restrict__ g_x, double* __restrict__ g_r) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double d = __dsub_rn(x[i], r ? r[i] : 0.0);
+  const double g = __dmul_rn(2.0, __dmul_rn(__dmul_rn(*g_out, w ? w[i] : 1.0), d));
+  if (g_x) g_x[i] = g;
+  if (g_r) g_r[i] = -g;
+}
+
 // ---------------------------------------------------------------- cold-start preparation
 __global__ void k_fill(double* p, int n, double v) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = v;
@@ -374,6 +451,48 @@ extern "C" int mpasg_weighted_sq_sum(long long n, const double* x, const double*
                                      double* out, void* stream) {
   if (!x || !out || n < 0) return MPASG_E_ARG;
   k_weighted_sq_sum<<<1, 1024, 0, (cudaStream_t)stream>>>(n, x, ref, weight, out);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
+extern "C" int mpasg_surface_pressure_vjp(int nCells, int rows, int nVertLevels, const double* rho_zz,
+                                          const double* zz, const double* qv, const double* zgrid,
+                                          double gravity, const double* g_sp, double* g_rho_zz, double* g_qv,
+                                          double* g_pressure_p, double* g_pressure_base, void* stream) {
+  if (!rho_zz || !zz || !zgrid || !g_sp || nVertLevels < 2 || nCells < 0 ||
+      (rows != nCells && rows != nCells + 1))
+    return MPASG_E_ARG;
+  const long long n = (long long)rows * nVertLevels;
+  if (n == 0) return MPASG_OK;
+  k_surface_pressure_vjp<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+      nCells, rows, nVertLevels, rho_zz, zz, qv, zgrid, 0.5 * gravity, g_sp, g_rho_zz, g_qv, g_pressure_p,
+      g_pressure_base);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
+extern "C" int mpasg_surface_pressure_jvp(int nCells, int rows, int nVertLevels, const double* rho_zz,
+                                          const double* zz, const double* qv, const double* zgrid,
+                                          double gravity, const double* t_rho_zz, const double* t_qv,
+                                          const double* t_pressure_p, const double* t_pressure_base,
+                                          double* t_sp, void* stream) {
+  if (!rho_zz || !zz || !zgrid || !t_sp || nVertLevels < 2 || nCells < 0 ||
+      (rows != nCells && rows != nCells + 1))
+    return MPASG_E_ARG;
+  if (rows == 0) return MPASG_OK;
+  k_surface_pressure_jvp<<<nblocks(rows), kBlock, 0, (cudaStream_t)stream>>>(
+      nCells, rows, nVertLevels, rho_zz, zz, qv, zgrid, 0.5 * gravity, t_rho_zz, t_qv, t_pressure_p,
+      t_pressure_base, t_sp);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
+extern "C" int mpasg_weighted_sq_sum_vjp(long long n, const double* x, const double* ref, const double* weight,
+                                         const double* g_out, double* g_x, double* g_ref, void* stream) {
+  if (!x || !g_out || n < 0) return MPASG_E_ARG;
+  if (n == 0) return MPASG_OK;
+  k_weighted_sq_sum_vjp<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, (cudaStream_t)stream>>>(
+      n, x, ref, weight, g_out, g_x, g_ref);
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }

@@ -6,6 +6,16 @@ messages; the arithmetic runs in ``mpasg_surface_pressure`` (bit-exact float64).
 ``surface_pressure_functional`` is the area-weighted squared surface-pressure anomaly
 used as the scalar objective of the differentiation checks (``mpasg_weighted_sq_sum``,
 fixed summation order).
+
+Both are differentiable like the reference's, whose autograd differentiates the torch
+expression: with ``rho_zz``, ``qv``, ``pressure_p`` or ``pressure_base`` requiring grad
+(or carrying forward-mode tangents) the surface pressure runs through a
+``torch.autograd.Function`` whose backward is ``mpasg_surface_pressure_vjp`` and whose
+forward-mode rule is ``mpasg_surface_pressure_jvp``, both bit-identical to torch's
+derivatives of the reference's expression; the objective's backward is
+``mpasg_weighted_sq_sum_vjp`` (with respect to ``sp`` and ``sp_ref``).  Derivatives with
+respect to the mesh inputs (``zz``, ``zgrid``) and the weights (``area``) are not built and
+are rejected before any device work.
 """
 
 from __future__ import annotations
@@ -13,8 +23,10 @@ from __future__ import annotations
 import ctypes as C
 
 import torch
+import torch.autograd.forward_ad as fwAD
 
 from . import _lib
+from .errors import MpasUnsupportedCapabilityError
 
 GRAVITY = 9.80616
 
@@ -47,28 +59,103 @@ def physics_interface_surface_pressure(*, nCells: int, rho_zz: torch.Tensor, zz:
         raise ValueError("surface pressure requires two mass levels and three W levels")
     if zgrid.shape[1] != rho_zz.shape[1] + 1:
         raise ValueError("zgrid must have one more level than rho_zz")
-    lib = _lib.load()
-    t = {k: _dev(v, k) for k, v in fields.items()}
-    rows = int(rho_zz.shape[0])
-    out = torch.empty(rows, dtype=torch.float64, device=t["rho_zz"].device)
-    p = lambda x: C.c_void_p(x.data_ptr())
-    rc = lib.mpasg_surface_pressure(int(nCells), rows, int(rho_zz.shape[1]), p(t["rho_zz"]), p(t["zz"]), p(t["qv"]),
-                                    p(t["pressure_p"]), p(t["pressure_base"]), p(t["zgrid"]), float(gravity), p(out),
-                                    C.c_void_p(torch.cuda.current_stream(out.device).cuda_stream))
-    _lib.check(rc, "mpasg_surface_pressure")
-    return out
+    for name in ("zz", "zgrid"):
+        if fields[name].requires_grad or _has_tangent(fields[name]):
+            raise MpasUnsupportedCapabilityError(
+                f"surface-pressure derivatives with respect to the mesh input {name} are not built")
+    return _SurfacePressure.apply(int(nCells), float(gravity), rho_zz, zz, qv, pressure_p, pressure_base, zgrid)
+
+
+def _has_tangent(x: torch.Tensor) -> bool:
+    """True when x carries a forward-mode tangent at the current dual level."""
+    return fwAD.unpack_dual(x).tangent is not None
+
+
+def _ptr(x: torch.Tensor | None) -> C.c_void_p:
+    return C.c_void_p(x.data_ptr()) if x is not None else C.c_void_p(0)
+
+
+def _stream(x: torch.Tensor) -> C.c_void_p:
+    return C.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
+
+
+class _SurfacePressure(torch.autograd.Function):
+    """Surface pressure with hand-written reverse and forward derivatives."""
+
+    @staticmethod
+    def forward(ctx, nCells, gravity, rho_zz, zz, qv, pressure_p, pressure_base, zgrid):
+        lib = _lib.load()
+        t = [_dev(v, k) for k, v in (("rho_zz", rho_zz), ("zz", zz), ("qv", qv), ("pressure_p", pressure_p),
+                                       ("pressure_base", pressure_base), ("zgrid", zgrid))]
+        rows, nlev = int(rho_zz.shape[0]), int(rho_zz.shape[1])
+        out = torch.empty(rows, dtype=torch.float64, device=t[0].device)
+        rc = lib.mpasg_surface_pressure(nCells, rows, nlev, *[_ptr(x) for x in t], gravity, _ptr(out), _stream(out))
+        _lib.check(rc, "mpasg_surface_pressure")
+        ctx.nCells, ctx.gravity = nCells, gravity
+        base = (t[0], t[1], t[2], t[5])  # rho_zz, zz, qv, zgrid as float64 contiguous
+        ctx.save_for_backward(*base)
+        ctx.save_for_forward(*base)
+        return out
+
+    @staticmethod
+    def backward(ctx, g_sp):
+        rho_zz, zz, qv, zgrid = ctx.saved_tensors
+        need = ctx.needs_input_grad
+        rows, nlev = int(rho_zz.shape[0]), int(rho_zz.shape[1])
+        g_sp = g_sp.to(torch.float64).contiguous()
+        outs = [torch.empty(rows, nlev, dtype=torch.float64, device=rho_zz.device) if need[i] else None
+                for i in (2, 4, 5, 6)]
+        rc = _lib.load().mpasg_surface_pressure_vjp(ctx.nCells, rows, nlev, _ptr(rho_zz), _ptr(zz), _ptr(qv),
+                                                    _ptr(zgrid), ctx.gravity, _ptr(g_sp), *[_ptr(o) for o in outs],
+                                                    _stream(rho_zz))
+        _lib.check(rc, "mpasg_surface_pressure_vjp")
+        return None, None, outs[0], None, outs[1], outs[2], outs[3], None
+
+    @staticmethod
+    def jvp(ctx, _n, _g, t_rho_zz, _t_zz, t_qv, t_pressure_p, t_pressure_base, _t_zgrid):
+        # zz / zgrid tangents are zeros torch materialises (dual mesh inputs are rejected
+        # before apply)
+        rho_zz, zz, qv, zgrid = ctx.saved_tensors
+        rows, nlev = int(rho_zz.shape[0]), int(rho_zz.shape[1])
+        tan = [None if x is None else _dev(x, "tangent") for x in (t_rho_zz, t_qv, t_pressure_p, t_pressure_base)]
+        out = torch.empty(rows, dtype=torch.float64, device=rho_zz.device)
+        rc = _lib.load().mpasg_surface_pressure_jvp(ctx.nCells, rows, nlev, _ptr(rho_zz), _ptr(zz), _ptr(qv),
+                                                    _ptr(zgrid), ctx.gravity, *[_ptr(x) for x in tan], _ptr(out),
+                                                    _stream(out))
+        _lib.check(rc, "mpasg_surface_pressure_jvp")
+        return out
+
+
+class _WeightedSqSum(torch.autograd.Function):
+    """sum_i w_i (x_i - r_i)^2 with a hand-written backward for x and r."""
+
+    @staticmethod
+    def forward(ctx, x, r, w):
+        out = torch.empty((), dtype=torch.float64, device=x.device)
+        rc = _lib.load().mpasg_weighted_sq_sum(int(x.numel()), _ptr(x), _ptr(r), _ptr(w), _ptr(out), _stream(x))
+        _lib.check(rc, "mpasg_weighted_sq_sum")
+        ctx.save_for_backward(x, r, w)
+        return out
+
+    @staticmethod
+    def backward(ctx, g_out):
+        x, r, w = ctx.saved_tensors
+        need = ctx.needs_input_grad
+        g_x = torch.empty_like(x) if need[0] else None
+        g_r = torch.empty_like(x) if need[1] else None
+        g_out = g_out.to(torch.float64).contiguous()
+        rc = _lib.load().mpasg_weighted_sq_sum_vjp(int(x.numel()), _ptr(x), _ptr(r), _ptr(w), _ptr(g_out),
+                                                   _ptr(g_x), _ptr(g_r), _stream(x))
+        _lib.check(rc, "mpasg_weighted_sq_sum_vjp")
+        return g_x, g_r, None
 
 
 def surface_pressure_functional(sp: torch.Tensor, sp_ref: torch.Tensor | None, area: torch.Tensor | None,
                                 nCells: int) -> torch.Tensor:
     """sum_c area_c (sp_c - sp_ref_c)^2 over the active cells (0-d float64 CUDA tensor)."""
-    lib = _lib.load()
+    if area is not None and area.requires_grad:
+        raise MpasUnsupportedCapabilityError("objective derivatives with respect to area are not built")
     x = _dev(sp, "sp")[:nCells].contiguous()
     r = _dev(sp_ref, "sp_ref")[:nCells].contiguous() if sp_ref is not None else None
     w = _dev(area, "area")[:nCells].contiguous() if area is not None else None
-    out = torch.empty((), dtype=torch.float64, device=x.device)
-    ptr = lambda v: C.c_void_p(v.data_ptr()) if v is not None else C.c_void_p(0)
-    rc = lib.mpasg_weighted_sq_sum(int(nCells), ptr(x), ptr(r), ptr(w), ptr(out),
-                                   C.c_void_p(torch.cuda.current_stream(x.device).cuda_stream))
-    _lib.check(rc, "mpasg_weighted_sq_sum")
-    return out
+    return _WeightedSqSum.apply(x, r, w)
