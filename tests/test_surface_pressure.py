@@ -207,3 +207,39 @@ def test_dual_mesh_inputs_are_rejected_before_device_work():
         with pytest.raises(MpasUnsupportedCapabilityError, match="zgrid"):
             physics_interface_surface_pressure(nCells=4, rho_zz=z, zz=z, qv=z, pressure_p=z, pressure_base=z,
                                                zgrid=zg)
+
+
+@pytest.mark.gpu
+def test_objective_gradient_against_central_differences():
+    """Central differences of the area-weighted squared-anomaly objective over
+    h = 2^-20 ... 2^-36 in a seeded direction of (rho_zz, qv, pressure_p): the best step
+    agrees with <grad, v> from the hand-written VJP chain to 1e-7, and the curve rises
+    again at the smallest steps (roundoff), as a central-difference curve does."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.diagnostics import physics_interface_surface_pressure, surface_pressure_functional
+    nc, t = _cuda_inputs("g2_moist")
+    ref = torch.as_tensor(AD["g2_moist/sp_ref"]).cuda()
+    area = torch.as_tensor(AD["g2_moist/area"]).cuda()
+    keys = ("rho_zz", "qv", "pressure_p")
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    # a direction large enough that truncation, not roundoff, limits the largest steps
+    scale = {"rho_zz": 1.0, "qv": 0.1, "pressure_p": 1.0e4}
+    v = {k: torch.randn(t[k].shape, generator=gen, dtype=torch.float64, device="cuda") * scale[k] for k in keys}
+
+    def objective(h):
+        x = dict(t)
+        for k in keys:
+            x[k] = t[k] + h * v[k]
+        return surface_pressure_functional(physics_interface_surface_pressure(nCells=nc, **x), ref, area, nc).item()
+
+    leaf = {k: (val.clone().requires_grad_(True) if k in keys else val) for k, val in t.items()}
+    obj = surface_pressure_functional(physics_interface_surface_pressure(nCells=nc, **leaf), ref, area, nc)
+    grads = torch.autograd.grad(obj, [leaf[k] for k in keys])
+    dot = float(sum((g * v[k]).sum() for k, g in zip(keys, grads)))
+    errs = []
+    for e in range(20, 37, 2):
+        h = 2.0 ** -e
+        fd = (objective(h) - objective(-h)) / (2 * h)
+        errs.append(abs(fd - dot) / abs(dot))
+    assert min(errs) <= 1e-7, errs
+    assert errs[-1] > min(errs), errs
