@@ -59,12 +59,11 @@ WORKLOADS = {
                name="plain float64 forward, level-4 mesh 2562 cells x 26 levels, 1 tracer, dt 1800 s"),
 }
 # DRAM bytes (read + write) per call and cell-level of a float64 stage, from an ncu capture
-# of the level-5 x 41 case (profiles/dyn_tend_dram_traffic_level5_10242x41_fp64.md), scaled
-# to the workload by its cell-levels
+# of the tendency stage on the level-5 mesh (10242 cells x 41 levels), scaled to the
+# workload by its cell-levels
 TRAFFIC_B_PER_CELL_LEVEL = {"dyn_tend": 542.7}
 # executed float64 flops (2 per FMA) per call and cell-level of a float64 stage, averaged
 # over a large step's calls, from an ncu count on the same level-5 x 41 case
-# (profiles/dyn_tend_fp64_flops_level5_10242x41.md)
 FP64_FLOP_PER_CELL_LEVEL = {"dyn_tend": 607.3}
 FP64_INST_PER_CELL_LEVEL = {"dyn_tend": 446.3}  # DFMA + DMUL + DADD issued
 BASE_CFG = {"config_time_integration_order": 3, "config_len_disp": 120000.0,

@@ -452,6 +452,9 @@ int mpasg_permute_rows(const double *src, double *dst, const long long *rows, lo
  *
  *  - The first call on each device looks up the scratch address (and may load the
  *    module); make that first call, with that device current, before any stream capture.
+ *    The address is cached for the life of the device's primary context: after a
+ *    cudaDeviceReset the cached address is stale, so do not call this entry point on that
+ *    device again in the same process.
  *  - Returns MPASG_E_SCRATCH, launching nothing, when nEdges * L * S exceeds
  *    MPASG_STATIC_SCRATCH_DOUBLES.
  *  - No scratch value needs to start at zero: each call writes every entry it reads.

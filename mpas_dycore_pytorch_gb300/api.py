@@ -359,6 +359,9 @@ class Model:
         s.wait_stream(torch.cuda.current_stream())
         graphs = []
         for part in (0, 1):
+            if part == 1 and not self._has_split_transport():
+                graphs.append(None)  # part 1 launches nothing: no graph to capture or replay
+                continue
             g = torch.cuda.CUDAGraph()
             with torch.cuda.stream(s):
                 with torch.cuda.graph(g, stream=s):
@@ -369,7 +372,16 @@ class Model:
         torch.cuda.current_stream().wait_stream(s)
         self._graph_parts = graphs
 
+    def _has_split_transport(self) -> bool:
+        """Whether the second part of a step (the split scalar transport) does any work:
+        scalars present, advection on and more than one dynamics substep (one substep is
+        the coupled mode, which transports inside the RK stages)."""
+        c = self.cstruct
+        return c.num_scalars > 0 and not c.scalar_advection_off and c.dynamics_split_steps > 1
+
     def _step_part(self, part: int) -> None:
+        if part == 1 and not self._has_split_transport():
+            return
         if self._graph_parts is not None:
             self._graph_parts[part].replay()
         else:

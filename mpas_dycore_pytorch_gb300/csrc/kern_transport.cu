@@ -435,13 +435,23 @@ std::mutex g_static_mutex;
 double* g_static_ptr[kMaxDevices] = {};
 
 // Device address of g_static_hflux on the current device, looked up once per device.
+// The cached address belongs to the device's primary context: it stays valid for the life
+// of the process unless that context is destroyed (cudaDeviceReset), after which a caller
+// must not use this entry point on that device again.  A failed lookup clears CUDA's
+// sticky last-error state, so it is not reported again by a later, unrelated launch check.
 int static_scratch(double** out) {
   int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return MPASG_E_CUDA;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return MPASG_E_CUDA;
+  }
   std::lock_guard<std::mutex> lock(g_static_mutex);
   if (!g_static_ptr[dev]) {
     void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_static_hflux) != cudaSuccess || !p) return MPASG_E_CUDA;
+    if (cudaGetSymbolAddress(&p, g_static_hflux) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return MPASG_E_CUDA;
+    }
     g_static_ptr[dev] = static_cast<double*>(p);
   }
   *out = g_static_ptr[dev];

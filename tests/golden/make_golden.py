@@ -1,8 +1,9 @@
 """Generate the golden fixtures under tests/golden/ by running the reference itself.
 
 This script is the only place that executes the reference (mpas_pytorch, pure
-Python + PyTorch, CPU float64).  It needs the reference source tree (default
-``/root/reference``, override with ``MPAS_REFERENCE``) and runs in a container
+Python + PyTorch, CPU float64).  It needs the reference source tree, named by the
+environment variable ``MPAS_REFERENCE`` (the directory that holds ``mpas_pytorch/``;
+there is no default), and runs in a container
 without netCDF4, so it puts a two-name stub module on ``sys.path`` first (the
 reference imports netCDF4 at package import, ``utils/checkpoint_reader.py:13``,
 but the dynamics never touch it).
@@ -21,7 +22,7 @@ For each case it
 Outputs: ``<case>_state.npz`` (prepared/step boundaries), ``<case>_taps.npz`` (stage
 arrays) and ``<case>.json`` (config, dims, scalar stage arguments, tap index).
 
-Run:  python tests/golden/make_golden.py
+Run:  MPAS_REFERENCE=<reference tree> python tests/golden/make_golden.py [case ...]
 """
 
 from __future__ import annotations
@@ -37,7 +38,17 @@ os.environ.setdefault("ATEN_CPU_CAPABILITY", "default")
 
 HERE = pathlib.Path(__file__).resolve().parent
 REPO = HERE.parent.parent
-REF = pathlib.Path(os.environ.get("MPAS_REFERENCE", "/root/reference"))
+
+
+def _reference_root() -> pathlib.Path:
+    """The reference source tree, from ``MPAS_REFERENCE`` (required)."""
+    root = os.environ.get("MPAS_REFERENCE")
+    if not root:
+        raise SystemExit("set MPAS_REFERENCE to the reference source tree (the directory holding mpas_pytorch/)")
+    path = pathlib.Path(root)
+    if not (path / "mpas_pytorch").is_dir():
+        raise SystemExit(f"MPAS_REFERENCE={root!r} does not hold mpas_pytorch/")
+    return path
 
 _STUB = '''
 class Dataset:
@@ -54,7 +65,7 @@ def _import_reference():
     (stub_dir / "netCDF4").mkdir()
     (stub_dir / "netCDF4" / "__init__.py").write_text(_STUB)
     sys.path.insert(0, str(stub_dir))
-    sys.path.insert(0, str(REF))
+    sys.path.insert(0, str(_reference_root()))
     sys.path.insert(0, str(REPO))
     import mpas_pytorch  # noqa: F401
     return mpas_pytorch

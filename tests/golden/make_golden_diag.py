@@ -16,7 +16,7 @@ the g2_explicit case (two steps) and writes the weights, tangent and results to
 ``scalars_ad_g2.npz``; the same in the coupled transport mode (g2_coupled mesh, explicit
 stages) to ``scalars_ad_g2_coupled.npz``.
 
-Run:  python tests/golden/make_golden_diag.py
+Run:  MPAS_REFERENCE=<reference tree> python tests/golden/make_golden_diag.py
 """
 
 from __future__ import annotations

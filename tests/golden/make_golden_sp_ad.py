@@ -15,7 +15,7 @@ fixtures (padded rows, qv = scalar 0, as ``make_golden_diag.py`` does) and recor
 Writes ``sp_ad_g2.npz``.  Imports the reference the same way as ``make_golden.py``
 (netCDF4 stub).
 
-Run:  python tests/golden/make_golden_sp_ad.py
+Run:  MPAS_REFERENCE=<reference tree> python tests/golden/make_golden_sp_ad.py
 """
 
 from __future__ import annotations

@@ -14,14 +14,14 @@ def need_gpu():
         pytest.skip("needs a CUDA device")
 
 
-def model_for_case(case: str, num_scalars=None):
+def model_for_case(case: str, num_scalars=None, precision=None):
     from mpas_dycore_pytorch_gb300.api import Model
     meta, st, _ = load_case(case)
     loaded = group(st, "loaded")
     mesh = dict(loaded)
     mesh.update(meta["loaded_scalars"])
     ns = num_scalars or int(loaded["scalars"].shape[-1])
-    return Model(mesh, meta["config"], meta["dt"], num_scalars=ns), meta, st, mesh
+    return Model(mesh, meta["config"], meta["dt"], num_scalars=ns, precision=precision), meta, st, mesh
 
 
 def to_np(x):

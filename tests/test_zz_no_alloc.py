@@ -21,7 +21,10 @@ def test_oversize_problem_is_refused_before_any_device_work():
     from mpas_dycore_pytorch_gb300 import _lib
     from mpas_dycore_pytorch_gb300.build import build
     from mpas_dycore_pytorch_gb300.errors import MpasConfigError
-    build()
+    try:
+        build()
+    except RuntimeError as exc:  # no nvcc on this machine
+        pytest.skip(str(exc))
     lib = _lib.load()
     m, c, f = _lib.MeshStruct(), _lib.ConfigStruct(), _lib.FieldsStruct()
     m.nCells, m.nEdges, m.nVertLevels = 40962, 122880, 55  # 120 km mesh, 55 levels
@@ -54,15 +57,18 @@ def _two_stage_calls(model, entry, inp, fields):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["float64", "mixed"])
 @pytest.mark.parametrize("case", CASES)
-def test_static_scratch_matches_caller_scratch_entry(case):
+def test_static_scratch_matches_caller_scratch_entry(case, precision):
+    """Both instantiations of the transport kernels (float64 and the mixed form's float32
+    stencils) write the library's scratch exactly as they write the caller's."""
     need_gpu()
     from mpas_dycore_pytorch_gb300 import _lib
     calls = [call for name in stage_names("scalars") for call in tap_calls(case, name)]
     if not calls:
         pytest.skip("no explicit transport stage in this case")
     inp = calls[0][0]
-    model, _, _, _ = model_for_case(case)
+    model, _, _, _ = model_for_case(case, precision=precision)
     st = model.state
     want = _two_stage_calls(model, "mpasg_advance_scalars", inp, st.struct)
     # the static entry point gets no hflux at all; the caller's hflux must stay untouched
