@@ -35,6 +35,9 @@
  *   mpasg_sfc_order, mpasg_edge_order  mesh_reordering.py:106 compute_rcm_permutation (SFC orders)
  *   mpasg_tridiag_*             autodiff/tridiagonal_solve.py:177, autodiff/tridiagonal_factor.py:145
  *   mpasg_advance_scalars_static  (no counterpart: advance_scalars.py:1272 without caller scratch)
+ *   mpasg_step_vjp, mpasg_prepare_vjp, mpasg_*_vjp (dynamics stages)
+ *                               torch autograd through atmosphere_model.py:2101 _run_simulation_vjp /
+ *                               dynamics/time_integration.py:4897 atm_srk3(differentiable=True)
  */
 #ifndef MPASG_H
 #define MPASG_H
@@ -415,6 +418,97 @@ int mpasg_tridiag_factor_jvp(long long n, int L, const double *a, const double *
                              const double *alpha, const double *gamma, const double *da,
                              const double *db, const double *dc, double *dalpha, double *dgamma,
                              void *stream);
+
+/* ---- dynamics derivatives (reverse mode) ------------------------------------------- */
+/*
+ * Hand-written vector-Jacobian products of the dry dynamics: the reverse mode the
+ * reference obtains from torch autograd through atm_srk3(differentiable=True)
+ * (dynamics/time_integration.py:4897-4948) and its custom Functions (dynamics/dyn_tend.py:
+ * 1194,1413,1568,3860; autodiff/tridiagonal_solve.py:232-291; autodiff/tridiagonal_factor.py:
+ * 183-231), with hard branches (third-order sign selectors, abs, min) frozen as taken, as in
+ * autodiff/soft_limiter.py:1-10.  Cotangents live in a second mpasg_fields `g` with the same
+ * layout as the forward fields: g->u is the cotangent of u, and so on.  Every transposed
+ * stencil is a deterministic gather (no atomics).  Scope: float64 arithmetic, dry columns
+ * (moist_end < moist_start), flat terrain, no vertical mixing, CAM or Rayleigh damping of u;
+ * anything else returns MPASG_E_ARG.  The mass-flux averages ruAvg / wwAvg carry no
+ * cotangent: they feed only the scalar transport, whose dependence on the dynamics is not
+ * differentiated here.
+ */
+/* Transposed connectivity of one mesh (0-based; -1 where a slot has no counterpart). */
+typedef struct mpasg_transpose {
+  const int32_t *edgeCellSlot;   /* (E, 2) slot of the edge in edgesOnCell of cellsOnEdge[e][s] */
+  const int32_t *edgeVertexSlot; /* (E, 2) slot of the edge in edgesOnVertex of verticesOnEdge[e][s] */
+  const int32_t *eoeTransSlot;   /* (E, maxEdges2) slot of e in edgesOnEdge of its j-th TRiSK neighbour */
+  const int32_t *cellsOnVertex;  /* (V, vertexDegree) missing -> nCells */
+  const int32_t *vertexKite;     /* (V, vertexDegree) kite index (into kiteAreasOnVertex[v]) that the cell
+                                    cellsOnVertex[v][s] weights this vertex with, -1 if none */
+  const int32_t *advPtr;         /* (C+1) CSR: the advection-stencil slots reading each cell */
+  const int32_t *advIdx;         /* e * nAdvMax + slot, in edge order */
+} mpasg_transpose;
+
+/* Doubles of the work buffer the dynamics derivatives use (any entry point below). */
+long long mpasg_dyn_vjp_work_doubles(const mpasg_mesh *m);
+/* Doubles of the per-step tape of mpasg_step_vjp (every RK stage's start state, the
+ * dynamics-substep saves, tendencies, implicit coefficients and acoustic-substep inputs). */
+long long mpasg_step_vjp_tape_doubles(const mpasg_mesh *m, const mpasg_config *c);
+
+/* Stage VJPs.  f holds the stage's forward inputs under the names the forward entry point
+ * reads; g holds the cotangents of the stage's outputs on entry and, on return, those of
+ * its inputs (outputs that overwrite an input field are consumed, inputs accumulate).
+ * Stages that need their forward outputs run the forward stage first, so f ends as the
+ * forward stage entry point leaves it. */
+/* vert_imp_coefs (vert_imp_coefs.py:188): cofwz, coftz, cofwt, a_tri, alpha_tri, gamma_tri
+ * -> exner, theta_m, rtheta_p (f holds the stage's coefficients, c_tri included). */
+int mpasg_vimp_vjp(const mpasg_mesh *m, const mpasg_config *c, const mpasg_fields *f, mpasg_fields *g,
+                   double dts, double *work, void *stream);
+/* atm_compute_dyn_tend_work (dyn_tend.py:10836): tend_u, tend_w, tend_theta, tend_rho and the
+ * Euler tendencies -> u, v, w, ru, rw, ru_save, rw_save, theta_m, theta_m_save, rho_zz,
+ * h_edge, divergence, vorticity, ke, pv_edge, pressure_p, rr_save (rk 1) or the rk-1
+ * tendencies passed through (rk 2, 3). */
+int mpasg_dyn_tend_vjp(const mpasg_mesh *m, const mpasg_config *c, const mpasg_fields *f, mpasg_fields *g,
+                       const mpasg_transpose *t, int rk_step, double *work, void *stream);
+/* atm_set_smlstep_pert_variables_work (smlstep_pert.py:373): tend_rw -> tend_w, tend_u. */
+int mpasg_smlstep_vjp(const mpasg_mesh *m, const mpasg_config *c, const mpasg_fields *f, mpasg_fields *g,
+                      void *stream);
+/* atm_advance_acoustic_step_work (acoustic_step.py:1297): ru_p, rho_pp, rtheta_pp, rw_p,
+ * rtheta_pp_old -> ru_p, rho_pp, rtheta_pp, rw_p (inputs), tend_u, tend_rho, tend_theta,
+ * tend_rw, exner, rho_zz, w, rw, rw_save, the implicit coefficients and theta_edge_save
+ * (the cotangent of the edge SUM theta_m_save_1 + theta_m_save_2).  Runs the forward
+ * substep first (f's acoustic fields end as mpasg_acoustic_step leaves them). */
+int mpasg_acoustic_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *g,
+                       const mpasg_transpose *t, int small_step, double dts, double *work, void *stream);
+/* atm_divergence_damping_3d (divergence_damping.py:299), ru_p -> rtheta_pp, rtheta_pp_old,
+ * theta_edge_save (edge-sum cotangent); f holds the stage's inputs. */
+int mpasg_divdamp_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *g,
+                      double dts, double *work, void *stream);
+/* atm_recover_large_step_variables_work (recover_large_step.py:1090): rho_p, rho_zz,
+ * rtheta_p, theta_m, u, ru, w, rw (+ exner, pressure_p at rk 3) -> the saves and the
+ * acoustic perturbations.  Runs the forward stage first. */
+int mpasg_recover_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *g,
+                      int rk_step, int ns, double rk_dt, double *work, void *stream);
+/* atm_compute_solve_diagnostics_work (solve_diagnostics.py:1052): h_edge, v, divergence,
+ * vorticity, ke, pv_edge -> u, rho_zz, v (rk < 3).  Runs the forward stage first. */
+int mpasg_diag_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *g,
+                   const mpasg_transpose *t, int rk_step, double *work, void *stream);
+
+/* One large step's reverse sweep (the reference's per-step checkpoint with recomputation,
+ * autodiff/checkpoint.py:106-254): f holds the step's start state (its 16 carried fields,
+ * as mpasg_step reads them) and is advanced by one step while every RK stage's inputs are
+ * written to `tape`; then the stages run backwards.  g holds the cotangents of the step's
+ * end state on entry and those of its start state on return (the carried fields u, v, w,
+ * ru, rw, theta_m, rho_zz, rho_p, rtheta_p, exner, pressure_p, h_edge, divergence,
+ * vorticity, ke, pv_edge); g's other fields are work.  No transport, no reconstruction:
+ * they do not feed the dynamics. */
+int mpasg_step_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *g,
+                   const mpasg_transpose *t, double *tape, double *work, void *stream);
+/* Reverse mode of the cold-start preparation (mpasg_prepare; init_coupled_diagnostics.py:147
+ * and the first diagnostics): f holds the prepared state, u and w the loaded wind (edges) and
+ * vertical wind (cells, L+1 levels); g the cotangents of the prepared state (consumed).
+ * Writes the cotangents of the loaded u, w, theta and rho (each fully written, padding rows
+ * zero). */
+int mpasg_prepare_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *g,
+                      const mpasg_transpose *t, const double *w_in, double *g_u, double *g_w,
+                      double *g_theta, double *g_rho, double *work, void *stream);
 
 /* ---- mesh reordering (host functions; no GPU needed) -------------------------------- */
 /* new_to_old[i] = the old index of the i-th point along the 3-D Hilbert curve through

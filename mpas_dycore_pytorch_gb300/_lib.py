@@ -129,6 +129,14 @@ class FieldsStruct(C.Structure):
                 + [("status", C.c_void_p)])
 
 
+TRANSPOSE_PTRS = ("edgeCellSlot", "edgeVertexSlot", "eoeTransSlot", "cellsOnVertex", "vertexKite", "advPtr",
+                  "advIdx")
+
+
+class TransposeStruct(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in TRANSPOSE_PTRS]
+
+
 EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg_prepare",
            "mpasg_step", "mpasg_step_timed",
            "mpasg_check_finite", "mpasg_moist_coefficients", "mpasg_vert_imp_coefs",
@@ -140,7 +148,10 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_tridiag_solve", "mpasg_tridiag_solve_vjp", "mpasg_tridiag_solve_jvp", "mpasg_tridiag_factor",
            "mpasg_tridiag_factor_vjp", "mpasg_tridiag_factor_jvp", "mpasg_autotune", "mpasg_fp64_peak",
            "mpasg_transport_vjp", "mpasg_transport_vjp_stage", "mpasg_step_taped", "mpasg_step_part",
-           "mpasg_surface_pressure_vjp", "mpasg_surface_pressure_jvp", "mpasg_weighted_sq_sum_vjp")
+           "mpasg_surface_pressure_vjp", "mpasg_surface_pressure_jvp", "mpasg_weighted_sq_sum_vjp",
+           "mpasg_dyn_vjp_work_doubles", "mpasg_step_vjp_tape_doubles", "mpasg_vimp_vjp", "mpasg_dyn_tend_vjp",
+           "mpasg_smlstep_vjp", "mpasg_acoustic_vjp", "mpasg_divdamp_vjp", "mpasg_recover_vjp", "mpasg_diag_vjp",
+           "mpasg_step_vjp", "mpasg_prepare_vjp")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -160,6 +171,7 @@ def load() -> C.CDLL:
     lib = C.CDLL(str(LIB_PATH))
     P = C.POINTER
     m, c, f = P(MeshStruct), P(ConfigStruct), P(FieldsStruct)
+    t = P(TransposeStruct)
     vp = C.c_void_p
     sig = {
         "mpasg_abi_version": ([], C.c_int),
@@ -205,6 +217,17 @@ def load() -> C.CDLL:
         "mpasg_tridiag_factor": ([C.c_longlong, C.c_int] + [vp] * 6, C.c_int),
         "mpasg_tridiag_factor_vjp": ([C.c_longlong, C.c_int] + [vp] * 10, C.c_int),
         "mpasg_tridiag_factor_jvp": ([C.c_longlong, C.c_int] + [vp] * 10, C.c_int),
+        "mpasg_dyn_vjp_work_doubles": ([m], C.c_longlong),
+        "mpasg_step_vjp_tape_doubles": ([m, c], C.c_longlong),
+        "mpasg_vimp_vjp": ([m, c, f, f, C.c_double, vp, vp], C.c_int),
+        "mpasg_dyn_tend_vjp": ([m, c, f, f, t, C.c_int, vp, vp], C.c_int),
+        "mpasg_smlstep_vjp": ([m, c, f, f, vp], C.c_int),
+        "mpasg_acoustic_vjp": ([m, c, f, f, t, C.c_int, C.c_double, vp, vp], C.c_int),
+        "mpasg_divdamp_vjp": ([m, c, f, f, C.c_double, vp, vp], C.c_int),
+        "mpasg_recover_vjp": ([m, c, f, f, C.c_int, C.c_int, C.c_double, vp, vp], C.c_int),
+        "mpasg_diag_vjp": ([m, c, f, f, t, C.c_int, vp, vp], C.c_int),
+        "mpasg_step_vjp": ([m, c, f, f, t, vp, vp, vp], C.c_int),
+        "mpasg_prepare_vjp": ([m, c, f, f, t] + [vp] * 7, C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

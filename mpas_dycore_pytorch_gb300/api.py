@@ -688,20 +688,94 @@ def _run_differentiable(state, mesh, config, dt, nsteps, device, on_step, on_pha
     return out
 
 
+def _objective_loss(objective: Callable, out: Mapping[str, Any]) -> torch.Tensor:
+    loss = objective(out)
+    if not isinstance(loss, torch.Tensor):
+        raise TypeError(f"objective must return a tensor, got {type(loss).__name__}")
+    if loss.ndim != 0:
+        raise MpasConfigError("objective must return a scalar tensor")
+    return loss
+
+
+def _dynamics_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any] | None, objective: Callable,
+                  keys: tuple, kwargs: dict) -> dict:
+    """run_simulation.vjp with respect to the loaded u, w, theta, rho: the hand-written
+    reverse mode of the dynamics (dyn_adjoint.py, ``mpasg_step_vjp``)."""
+    from .dyn_adjoint import DIFFERENTIABLE_OUT, DynamicsAdjoint, check_request, run_vjp
+    unknown = set(kwargs) - {"config", "dt", "nsteps", "device", "differentiable", "checkpoint_timesteps",
+                             "checkpoint_use_reentrant", "checkpoint_materialize_final"}
+    if unknown:
+        raise MpasConfigError(f"unsupported keyword arguments for the derivative runs: {sorted(unknown)}")
+    for k in keys:
+        if k not in state or not hasattr(state[k], "shape"):
+            raise KeyError(f"Tracked VJP key '{k}' is missing from state")
+    if _is_prepared(state):
+        raise MpasUnsupportedCapabilityError(
+            "dynamics derivatives start from a loaded (unprepared) state: track u, w, theta or rho")
+    mesh = mesh if mesh is not None else state
+    merged = dict(mesh)
+    merged.update(state)
+    cfg = resolved_config(kwargs.get("config"))
+    dt = float(cfg["config_dt"] if kwargs.get("dt") is None else kwargs["dt"])
+    nsteps = int(kwargs.get("nsteps", 1))
+    ns = _int(merged.get("num_scalars", _np(merged["scalars"]).shape[-1]))
+    check_request(cfg, merged, ns)
+    model = Model(merged, cfg, dt, num_scalars=ns, device=kwargs.get("device", "cuda"))
+    adj = DynamicsAdjoint(model)
+
+    def cotangents(final: dict) -> dict:
+        out = _merge(state, final)
+        leaves = {k: out[k].detach().clone().requires_grad_(True) for k in DIFFERENTIABLE_OUT
+                  if isinstance(out.get(k), torch.Tensor)}
+        # every other output the step computes is a leaf too: a derivative through it is
+        # refused (the base state and the diabatic forcing are constants of the run)
+        others = {k: v.detach().clone().requires_grad_(True) for k, v in final.items()
+                  if k not in leaves and k not in STATIC_KEYS and isinstance(v, torch.Tensor)
+                  and torch.is_floating_point(v)}
+        loss = _objective_loss(objective, {**out, **leaves, **others})
+        names = list(leaves) + list(others)
+        grads = torch.autograd.grad(loss, [leaves.get(k, others.get(k)) for k in names], allow_unused=True)
+        res = {}
+        for k, g in zip(names, grads):
+            if g is None:
+                continue
+            if k in others:
+                if bool(torch.any(g != 0)):
+                    raise MpasUnsupportedCapabilityError(f"the objective's derivative through {k!r} is not built")
+                continue
+            res[k] = g.detach()
+        return res
+
+    grads, _ = run_vjp(model, merged, nsteps, cotangents, adj)
+    res = {}
+    for k in keys:
+        ref = state[k]
+        g = grads[k][:ref.shape[0]]
+        res[k] = g if isinstance(ref, torch.Tensor) and ref.device == g.device else \
+            (g.to(ref.device) if isinstance(ref, torch.Tensor) else g.cpu())
+    return res
+
+
 def run_simulation_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any], objective: Callable,
                        track_keys=None, **kwargs) -> dict:
-    """Adjoint of ``run_simulation`` for the transported scalars (the reference's
-    ``run_simulation.vjp``, atmosphere_model.py:2101): d objective(out) / d state["scalars"]
-    through ``nsteps`` steps, computed by the hand-written transposed transport
-    (``mpasg_transport_vjp``).  ``track_keys`` must be ``("scalars",)``; passive scalars
-    with the explicit split transport only (the dynamics do not depend on them)."""
+    """Adjoint of ``run_simulation`` (the reference's ``run_simulation.vjp``,
+    atmosphere_model.py:2101): d objective(out) / d state[key] through ``nsteps`` steps.
+
+    * ``track_keys`` within ``("u", "w", "theta", "rho")``: the loaded wind, vertical wind,
+      potential temperature and density, through the preparation and the dynamics (the
+      hand-written reverse mode of dyn_adjoint.py: dry, flat terrain, float64; the
+      objective may read the step boundary's carried fields);
+    * ``track_keys=("scalars",)``: the transported scalars, by the hand-written transposed
+      transport (``mpasg_transport_vjp``; passive scalars, explicit split transport)."""
     from .tracer_adjoint import scalars_vjp
     reject_unsupported_request(state, mesh, kwargs.get("config"))
     keys = tuple(track_keys) if track_keys is not None else None
+    if keys and all(k in ("u", "w", "theta", "rho") for k in keys):
+        return _dynamics_vjp(state, mesh, objective, keys, dict(kwargs))
     if keys != ("scalars",):
         raise MpasUnsupportedCapabilityError(
-            "run_simulation.vjp on the GB300 path differentiates with respect to 'scalars' only; "
-            f"pass track_keys=('scalars',) (got {keys})")
+            "run_simulation.vjp on the GB300 path differentiates with respect to 'scalars', or to any of "
+            f"'u', 'w', 'theta', 'rho' (not both kinds at once); got {keys}")
     if "scalars" not in state or not hasattr(state["scalars"], "shape"):
         raise KeyError("Tracked VJP key 'scalars' is missing from state")
     model, tape, out = _scalar_derivative_forward(state, mesh, dict(kwargs))

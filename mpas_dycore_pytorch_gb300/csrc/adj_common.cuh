@@ -1,0 +1,87 @@
+// Shared pieces of the dynamics derivatives (reverse mode): the work-buffer layout and the
+// internal entry points the stage VJPs and the step driver share.
+#pragma once
+
+#include "common.cuh"
+
+// Work buffer of the dynamics VJPs: kAdjE edge arrays (E+1) x L, kAdjC cell arrays
+// (C+1) x (L+1) and kAdjV vertex arrays (V+1) x L, each 256-byte aligned.
+constexpr int kAdjE = 18, kAdjC = 16, kAdjV = 4;
+
+struct AdjWork {
+  double* e[kAdjE];
+  double* c[kAdjC];
+  double* v[kAdjV];
+};
+
+inline long long adj_round(long long n) { return (n + 31) / 32 * 32; }
+
+inline long long adj_work_doubles(const mpasg_mesh* m) {
+  const long long L = m->nVertLevels;
+  return kAdjE * adj_round((m->nEdges + 1LL) * L) + kAdjC * adj_round((m->nCells + 1LL) * (L + 1)) +
+         kAdjV * adj_round((m->nVertices + 1LL) * L);
+}
+
+inline AdjWork adj_work(const mpasg_mesh* m, double* w) {
+  AdjWork a;
+  const long long L = m->nVertLevels;
+  const long long ne = adj_round((m->nEdges + 1LL) * L), nc = adj_round((m->nCells + 1LL) * (L + 1)),
+                  nv = adj_round((m->nVertices + 1LL) * L);
+  for (int i = 0; i < kAdjE; ++i, w += ne) a.e[i] = w;
+  for (int i = 0; i < kAdjC; ++i, w += nc) a.c[i] = w;
+  for (int i = 0; i < kAdjV; ++i, w += nv) a.v[i] = w;
+  return a;
+}
+
+// Supported configurations of the dynamics derivatives (see mpasg.h).
+inline bool adj_supported(const mpasg_mesh* m, const mpasg_config* c) {
+  return m->flatTerrain && c->moist_end < c->moist_start && !(c->v_mom_eddy_visc2 > 0.0) &&
+         !(c->v_theta_eddy_visc2 > 0.0) && !(c->mpas_cam_coef > 0.0 && c->number_cam_damping_levels > 0) &&
+         c->rayleigh_damp_u_levels <= 0 && m->nVertLevels >= 4;
+}
+
+// 1 when cell c is the second cell (cellsOnEdge[e][1]) of edge e
+MPASG_D int cell_side(const mpasg_mesh& m, int e, int c) { return m.cellsOnEdge[2 * e] == c ? 0 : 1; }
+// 1 when vertex v is the second vertex (verticesOnEdge[e][1]) of edge e
+MPASG_D int vertex_side(const mpasg_mesh& m, int e, int v) { return m.verticesOnEdge[2 * e] == v ? 0 : 1; }
+
+// partial derivatives of flux3 (common.cuh; dyn_tend.py:839,853) with respect to its
+// arguments qm2, qm1, q0, qp1, ua; |ua| differentiated as sign(ua), 0 at 0 (torch's abs)
+struct Flux3Grad {
+  double qm2, qm1, q0, qp1, ua;
+};
+MPASG_D Flux3Grad flux3_grad(double qm2, double qm1, double q0, double qp1, double ua, double c3) {
+  const double au = fabs(ua);
+  const double s = ua > 0.0 ? 1.0 : (ua < 0.0 ? -1.0 : 0.0);
+  Flux3Grad d;
+  d.qm2 = (-ua - c3 * au) * kInv12;
+  d.qm1 = (7.0 * ua + 3.0 * c3 * au) * kInv12;
+  d.q0 = (7.0 * ua - 3.0 * c3 * au) * kInv12;
+  d.qp1 = (-ua + c3 * au) * kInv12;
+  d.ua = ((7.0 * (q0 + qm1) - (qp1 + qm2)) + c3 * s * ((qp1 - qm2) - 3.0 * (q0 - qm1))) * kInv12;
+  return d;
+}
+
+// internal entry points shared by the stage VJPs and the step driver
+int mpasgi_acoustic_parts(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int small_step, double dts,
+                          cudaStream_t s, int part);
+int mpasgi_recover_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
+                            int rk_step, double rk_dt, const AdjWork& w, cudaStream_t s);
+int mpasgi_diag_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
+                         const mpasg_transpose* t, int rk_step, const AdjWork& w, cudaStream_t s);
+int mpasgi_acoustic_vjp_core(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, mpasg_fields* g,
+                             const mpasg_transpose* t, int small_step, double dts, const AdjWork& w,
+                             cudaStream_t s);
+int mpasgi_acoustic_vjp_fwd(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int small_step, double dts,
+                            const AdjWork& w, cudaStream_t s);
+int mpasgi_acoustic_vjp_rev(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, mpasg_fields* g,
+                            const mpasg_transpose* t, int small_step, double dts, const AdjWork& w,
+                            cudaStream_t s);
+int mpasgi_vimp_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
+                         double dts, const AdjWork& w, cudaStream_t s);
+int mpasgi_smlstep_vjp_core(const mpasg_mesh* m, mpasg_fields* g, cudaStream_t s);
+int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
+                             const mpasg_transpose* t, int rk_step, const AdjWork& w, cudaStream_t s);
+int mpasgi_divdamp_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
+                            double dts, const AdjWork& w, cudaStream_t s);
+int mpasgi_zero(double* p, long long n, cudaStream_t s);

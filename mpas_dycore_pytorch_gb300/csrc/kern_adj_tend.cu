@@ -1,0 +1,1018 @@
+// Reverse mode of the large-step tendencies (the reference's atm_compute_dyn_tend_work,
+// mpas_pytorch/dynamics/dyn_tend.py:10836; the reference differentiates it through the
+// ordered-transpose custom Functions at :1194, :1413, :1568, :3860).
+//
+// The forward stage (kern_tend.cu) forms cell sums over edges, edge values from two cells,
+// the TRiSK sum over edgesOnEdge, the advection stencils and column fluxes.  Each is read
+// backwards as a gather over the outputs that read the thread's input: an edge collects its
+// two cells (slot of the edge in each cell from the transposed connectivity), a cell its
+// edges, a vertex its edges, an edge its TRiSK neighbours, a cell the advection-stencil
+// slots that read it (CSR), a level its neighbour levels.  Per-edge partial products that a
+// cell or vertex gather needs are written to the work buffer first.  No atomics: every
+// cotangent is a fixed-order sum, so results are bitwise reproducible.
+//
+// Values the derivatives need and the forward does not keep (the mass-flux divergence, the
+// Smagorinsky deformation and kdiff, the del2 field of u and its del4 divergence and curl)
+// are recomputed here from the stage's inputs, with the forward's expressions.
+#include "adj_common.cuh"
+
+namespace {
+
+struct AdjTendScalars {
+  double cs2, kdiff_cap, h_mom_visc4, h_theta_visc4, del4u_div, coef3, visc2;
+  int rk_step, smag, del4;
+};
+
+// ---- values: mass-flux divergence (every rk) and, at rk 1, Smagorinsky deformation and kdiff
+__global__ void k_tadj_values(mpasg_mesh m, mpasg_fields f, FastDiv fl, AdjTendScalars p, double* __restrict__ hd,
+                              double* __restrict__ kd, double* __restrict__ dd_out, double* __restrict__ do_out) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * L) return;
+  const uint32_t c = fl.div(i), k = i - c * L;
+  const int me = m.maxEdges;
+  const int n = m.nEdgesOnCell[c];
+  double h = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const int e = m.edgesOnCell[c * me + j];
+    const double t = m.cell_edge_sdv[c * me + j] * f.ru[(size_t)e * L + k];
+    h = (j == 0) ? t : h + t;
+  }
+  hd[i] = h * m.invAreaCell[c];
+  if (p.rk_step != 1) return;
+  if (p.smag) {
+    // Separately rounded products and sums in the reference's order: over a nearly rigid
+    // flow the deformation is a few roundings of its terms, and the direction of kdiff's
+    // derivative (dd, do) / |(dd, do)| follows those roundings exactly.
+    double dd = 0.0, dof = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const int e = m.edgesOnCell[c * me + j];
+      const double ca = m.defc_a[c * me + j], cb = m.defc_b[c * me + j];
+      const double ue = f.u[(size_t)e * L + k], ve = f.v[(size_t)e * L + k];
+      const double ndd = __dsub_rn(__dadd_rn(dd, __dmul_rn(ca, ue)), __dmul_rn(cb, ve));
+      const double ndo = __dadd_rn(__dadd_rn(dof, __dmul_rn(cb, ue)), __dmul_rn(ca, ve));
+      dd = ndd;
+      dof = ndo;
+    }
+    kd[i] = fmin(__dmul_rn(p.cs2, sqrt(__dadd_rn(__dmul_rn(dd, dd), __dmul_rn(dof, dof)))), p.kdiff_cap);
+    dd_out[i] = dd;
+    do_out[i] = dof;
+  } else {
+    kd[i] = p.visc2;
+  }
+}
+
+// ---- values (rk 1, del4): del2 of u on the edges (the forward's delsq_u = u_diff)
+__global__ void k_tadj_udiff(mpasg_mesh m, mpasg_fields f, FastDiv fl, double* __restrict__ ud) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i), k = i - e * L;
+  const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
+  const int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
+  const double inv_dc = m.invDcEdge[e];
+  const double r_dv = fmin(m.invDvEdge[e], 4.0 * inv_dc);
+  ud[i] = (f.divergence[(size_t)c2 * L + k] - f.divergence[(size_t)c1 * L + k]) * inv_dc -
+          (f.vorticity[(size_t)v2 * L + k] - f.vorticity[(size_t)v1 * L + k]) * r_dv;
+}
+
+// ---- values (rk 1, del4): its divergence (cells) and curl (vertices), as k_del4_cell / k_del4_vertex
+__global__ void k_tadj_del4_cells(mpasg_mesh m, FastDiv fl, const double* __restrict__ ud, double* __restrict__ dsd) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * L) return;
+  const uint32_t c = fl.div(i), k = i - c * L;
+  const int me = m.maxEdges;
+  const int n = m.nEdgesOnCell[c];
+  double acc = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const int e = m.edgesOnCell[c * me + j];
+    const double t = (m.invAreaCell[c] * m.dvEdge[e] * m.edgesOnCell_sign[c * me + j]) * ud[(size_t)e * L + k];
+    acc = (j == 0) ? t : acc + t;
+  }
+  dsd[i] = acc;
+}
+
+__global__ void k_tadj_del4_vertices(mpasg_mesh m, FastDiv fl, const double* __restrict__ ud,
+                                     double* __restrict__ dsv) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nVertices * L) return;
+  const uint32_t v = fl.div(i), k = i - v * L;
+  const int vd = m.vertexDegree;
+  double acc = 0.0;
+  for (int j = 0; j < vd; ++j) {
+    const int e = m.edgesOnVertex[v * vd + j];
+    const double t = (m.invAreaTriangle[v] * m.dcEdge[e] * m.edgesOnVertex_sign[v * vd + j]) * ud[(size_t)e * L + k];
+    acc = (j == 0) ? t : acc + t;
+  }
+  dsv[i] = acc;
+}
+
+// vertical theta flux at interface q (k_tend_w_theta's wdtz_at, float64 form) and its
+// partial derivatives with respect to theta_m[q-2..q+1], theta_m_save[q-1..q], rw[q], rw_save[q]
+struct WdtzGrad {
+  double th[4];  // q-2, q-1, q, q+1
+  double ths[2];  // q-1, q
+  double rw, rws;
+};
+MPASG_D WdtzGrad wdtz_grad(const mpasg_mesh& m, const double* th, const double* ths, const double* rw,
+                           const double* rws, int q, int L, double coef3) {
+  WdtzGrad d = {{0.0, 0.0, 0.0, 0.0}, {0.0, 0.0}, 0.0, 0.0};
+  const double fm = m.fzm[q], fp = m.fzp[q];
+  if (q == L - 1 && q != 1) {
+    d.th[2] = rws[q] * fm;
+    d.th[1] = rws[q] * fp;
+    d.rws = fm * th[q] + fp * th[q - 1];
+    return d;
+  }
+  if (q == 1) {
+    d.th[2] = rw[q] * fm;
+    d.th[1] = rw[q] * fp;
+    d.rw = fm * th[q] + fp * th[q - 1];
+  } else {
+    const Flux3Grad g = flux3_grad(th[q - 2], th[q - 1], th[q], th[q + 1], rw[q], coef3);
+    d.th[0] = g.qm2;
+    d.th[1] = g.qm1;
+    d.th[2] = g.q0;
+    d.th[3] = g.qp1;
+    d.rw = g.ua;
+  }
+  const double tse = fm * ths[q] + fp * ths[q - 1];
+  d.rw -= tse;
+  d.rws = tse;
+  d.ths[1] = (rws[q] - rw[q]) * fm;
+  d.ths[0] = (rws[q] - rw[q]) * fp;
+  return d;
+}
+
+// vertical w flux at interface q (wdwz_at) and its partials: w[q-2..q+1], rw[q-1], rw[q]
+struct WdwzGrad {
+  double w[4];
+  double rwm, rw;
+};
+MPASG_D WdwzGrad wdwz_grad(const double* w, const double* rw, int q, int L) {
+  WdwzGrad d = {{0.0, 0.0, 0.0, 0.0}, 0.0, 0.0};
+  if (q == 1 || q == L - 1) {
+    const double a = 0.25 * (w[q] + w[q - 1]), b = 0.25 * (rw[q] + rw[q - 1]);
+    d.rw = a;
+    d.rwm = a;
+    d.w[2] = b;
+    d.w[1] = b;
+    return d;
+  }
+  const Flux3Grad g = flux3_grad(w[q - 2], w[q - 1], w[q], w[q + 1], 0.5 * (rw[q] + rw[q - 1]), 1.0);
+  d.w[0] = g.qm2;
+  d.w[1] = g.qm1;
+  d.w[2] = g.q0;
+  d.w[3] = g.qp1;
+  d.rw = 0.5 * g.ua;
+  d.rwm = 0.5 * g.ua;
+  return d;
+}
+
+// ---- columns of the theta and w tendencies read backwards (index space C x (L+1)):
+// vertical fluxes of theta and w, the flux divergences' area factor, the buoyancy /
+// pressure-gradient residual (rk 1), the diabatic term, and the Euler tendencies
+// (collected for the mixing at rk 1, passed through at rk 2 and 3)
+__global__ void k_tadj_columns(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl1, AdjTendScalars p,
+                               double* __restrict__ tt1b, double* __restrict__ tw1b, double* __restrict__ tweb,
+                               double* __restrict__ tteb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * (L + 1)) return;
+  const uint32_t c = fl1.div(i);
+  const int k = (int)(i - c * (L + 1));
+  const size_t oc = (size_t)c * L, ow = (size_t)c * (L + 1);
+  const double ia = m.invAreaCell[c];
+  const double* th = f.theta_m + oc;
+  const double* ths = f.theta_m_save + oc;
+  const double* rw = f.rw + ow;
+  const double* rws = f.rw_save + ow;
+  const double* w = f.w + ow;
+  auto Gtt = [&](int q) { return (q >= 0 && q < L) ? g.tend_theta[oc + q] : 0.0; };
+  auto Gtw = [&](int q) { return (q >= 1 && q <= L - 1) ? g.tend_w[ow + q] : 0.0; };
+  auto wdtzb = [&](int q) { return Gtt(q) * (q < L ? m.rdzw[q] : 0.0) - Gtt(q - 1) * (q >= 1 ? m.rdzw[q - 1] : 0.0); };
+  auto wdwzb = [&](int q) { return Gtw(q) * m.rdzu[q < L ? q : 0] * (q <= L - 1 ? 1.0 : 0.0) -
+                                   Gtw(q - 1) * (q - 1 >= 1 ? m.rdzu[q - 1] : 0.0); };
+  // ---- mass level k: theta
+  if (k < L) {
+    const size_t o = oc + k;
+    const double G = g.tend_theta[o];
+    g.rho_zz[o] += G * f.rt_diabatic_tend[o];
+    tt1b[o] = G * ia;
+    double gth = 0.0, gths = 0.0;
+    for (int q = k - 1; q <= k + 2; ++q) {
+      if (q < 1 || q > L - 1) continue;
+      const double b = wdtzb(q);
+      if (b == 0.0) continue;
+      const WdtzGrad d = wdtz_grad(m, th, ths, rw, rws, q, L, p.coef3);
+      const int s = k - (q - 2);  // position of level k in q-2..q+1
+      gth += b * d.th[s];
+      if (k == q - 1) gths += b * d.ths[0];
+      if (k == q) gths += b * d.ths[1];
+    }
+    g.theta_m[o] += gth;
+    g.theta_m_save[o] += gths;
+    if (p.rk_step == 1) {
+      tteb[o] = G + g.tend_theta_euler[o];
+    } else {
+      g.tend_theta_euler[o] += G;
+    }
+  }
+  // ---- w level k: rw / rw_save from the theta flux, w / rw from the w flux
+  double grw = 0.0, grws = 0.0, gw = 0.0;
+  if (k >= 1 && k <= L - 1) {
+    const double b = wdtzb(k);
+    const WdtzGrad d = wdtz_grad(m, th, ths, rw, rws, k, L, p.coef3);
+    grw += b * d.rw;
+    grws += b * d.rws;
+  }
+  for (int q = k - 1; q <= k + 2; ++q) {
+    if (q < 1 || q > L - 1) continue;
+    const double b = wdwzb(q);
+    if (b == 0.0) continue;
+    const WdwzGrad d = wdwz_grad(w, rw, q, L);
+    gw += b * d.w[k - (q - 2)];
+    if (k == q) grw += b * d.rw;
+    if (k == q - 1) grw += b * d.rwm;
+  }
+  g.rw[ow + k] += grw;
+  g.rw_save[ow + k] += grws;
+  g.w[ow + k] += gw;
+  if (k >= 1 && k <= L - 1) {
+    const double G = g.tend_w[ow + k];
+    tw1b[ow + k] = G * ia;
+    if (p.rk_step == 1) {
+      tweb[ow + k] = G + g.tend_w_euler[ow + k];
+    } else {
+      g.tend_w_euler[ow + k] += G;
+    }
+  } else {
+    tw1b[ow + k] = 0.0;
+    tweb[ow + k] = 0.0;
+  }
+}
+
+// ---- rk 1: pressure gradient / buoyancy residual of tend_w_euler read backwards, per
+// mass level: -> pressure_p, rr_save (through dpdz)
+__global__ void k_tadj_wres(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl, const double* __restrict__ tweb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * L) return;
+  const uint32_t c = fl.div(i);
+  const int k = (int)(i - c * L);
+  const size_t ow = (size_t)c * (L + 1);
+  double gpp = 0.0, gdp = 0.0;
+  if (k >= 1) {
+    const double t = tweb[ow + k] * f.cqw[ow + k];
+    gpp += -t * m.rdzu[k];
+    gdp += t * m.fzm[k];
+  }
+  if (k + 1 <= L - 1) {
+    const double t = tweb[ow + k + 1] * f.cqw[ow + k + 1];
+    gpp += t * m.rdzu[k + 1];
+    gdp += t * m.fzp[k + 1];
+  }
+  g.pressure_p[i] += gpp;
+  g.rr_save[i] += gdp * (-kGravity) * (1.0 + f.qtot[i]);
+}
+
+// ---- edges: horizontal advective fluxes of theta and w read backwards (and, at rk > 1,
+// the theta flux of the change of ru within the dynamics substep).  Writes the cotangents
+// of the stencil sums (fltb, flwb) for the cell gather, adds to ru, ru_save and the
+// edge-sum cotangent of theta_m_save.
+__global__ void k_tadj_adv_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpasg_transpose t, FastDiv fl,
+                                 AdjTendScalars p, const double* __restrict__ tt1b, const double* __restrict__ tw1b,
+                                 double* __restrict__ fltb, double* __restrict__ flwb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  const int me = m.maxEdges, na = m.nAdvMax;
+  const int nadv = m.nAdvCellsForEdge[e];
+  const int32_t* cells = m.advCellsForEdge + (size_t)e * na;
+  // cotangents of the edge fluxes from the two cells' sums (x = -sign * flux)
+  auto edge_b = [&](const double* src, int kk, size_t pitch) {
+    double s = 0.0;
+    for (int q = 0; q < 2; ++q) {
+      const int j = t.edgeCellSlot[2 * e + q];
+      if (j < 0) continue;
+      const int c = m.cellsOnEdge[2 * e + q];
+      s += -src[(size_t)c * pitch + kk] * m.edgesOnCell_sign[c * me + j];
+    }
+    return s;
+  };
+  auto adv_sum = [&](const double* fld, int kk, size_t pitch, double sel) {
+    const double* cf = (sel >= 0.0 ? m.adv_coefs_p : m.adv_coefs_m) + (size_t)e * na;
+    double acc = 0.0;
+    for (int a = 0; a < nadv; ++a) {
+      const double tt = cf[a] * fld[(size_t)cells[a] * pitch + kk];
+      acc = (a == 0) ? tt : acc + tt;
+    }
+    return acc;
+  };
+  const double rue = f.ru[i];
+  // theta
+  const double fteb = edge_b(tt1b, k, L);
+  double gru = fteb * adv_sum(f.theta_m, k, L, rue);
+  fltb[i] = fteb * rue;
+  // w at level k (k >= 1) and k + 1: ru_w = fzm ru_k + fzp ru_(k-1)
+  auto ru_w = [&](int kk) { return m.fzm[kk] * f.ru[(size_t)e * L + kk] + m.fzp[kk] * f.ru[(size_t)e * L + kk - 1]; };
+  if (k >= 1) {
+    const double fweb = edge_b(tw1b, k, L + 1);
+    const double rw_k = ru_w(k);
+    gru += fweb * adv_sum(f.w, k, L + 1, rw_k) * m.fzm[k];
+    flwb[i] = fweb * rw_k;
+  } else {
+    flwb[i] = 0.0;
+  }
+  if (k + 1 <= L - 1) {
+    const double fweb = edge_b(tw1b, k + 1, L + 1);
+    gru += fweb * adv_sum(f.w, k + 1, L + 1, ru_w(k + 1)) * m.fzp[k + 1];
+  }
+  if (p.rk_step > 1) {  // - sum_j (sign dvEdge)_j (ru_save - ru) theta_edge_save
+    double s_sdv = 0.0;
+    for (int q = 0; q < 2; ++q) {
+      const int j = t.edgeCellSlot[2 * e + q];
+      if (j < 0) continue;
+      const int c = m.cellsOnEdge[2 * e + q];
+      s_sdv += -tt1b[(size_t)c * L + k] * m.cell_edge_sdv[c * me + j];
+    }
+    const double the = f.theta_edge_save[i];
+    g.ru_save[i] += s_sdv * the;
+    gru -= s_sdv * the;
+    g.theta_edge_save[i] += 0.5 * s_sdv * (f.ru_save[i] - rue);
+  }
+  g.ru[i] += gru;
+}
+
+// ---- cells: the advection stencils transposed (CSR of (edge, slot) readers): theta, w
+__global__ void k_tadj_adv_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpasg_transpose t, FastDiv fl1,
+                                 const double* __restrict__ fltb, const double* __restrict__ flwb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * (L + 1)) return;
+  const uint32_t c = fl1.div(i);
+  const int k = (int)(i - c * (L + 1));
+  const int na = m.nAdvMax;
+  double gth = 0.0, gw = 0.0;
+  const int p0 = t.advPtr[c], p1 = t.advPtr[c + 1];
+  for (int q = p0; q < p1; ++q) {
+    const int es = t.advIdx[q];
+    const int e = es / na;
+    const size_t ie = (size_t)e * L;
+    if (k < L) {
+      const double cf = f.ru[ie + k] >= 0.0 ? m.adv_coefs_p[es] : m.adv_coefs_m[es];
+      gth += cf * fltb[ie + k];
+    }
+    if (k >= 1 && k <= L - 1) {
+      const double rwk = m.fzm[k] * f.ru[ie + k] + m.fzp[k] * f.ru[ie + k - 1];
+      const double cf = rwk >= 0.0 ? m.adv_coefs_p[es] : m.adv_coefs_m[es];
+      gw += cf * flwb[ie + k];
+    }
+  }
+  if (k < L) g.theta_m[(size_t)c * L + k] += gth;
+  g.w[i] += gw;
+}
+
+// ---- edges: the u tendency read backwards (vertical transport, PV flux, kinetic-energy
+// gradient, divergence coupling; at rk 1 the pressure gradient and del2 / del4 mixing)
+__global__ void k_tadj_u(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl, AdjTendScalars p,
+                         const double* __restrict__ hd, const double* __restrict__ kd, const double* __restrict__ ud,
+                         const double* __restrict__ dsd, const double* __restrict__ dsv, double* __restrict__ qb_out,
+                         double* __restrict__ pke, double* __restrict__ phd, double* __restrict__ prwe,
+                         double* __restrict__ ppp, double* __restrict__ pkd, double* __restrict__ udb,
+                         double* __restrict__ pd4) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
+  const size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
+  const double* ue = f.u + (size_t)e * L;
+  const double* Gtu = g.tend_u + (size_t)e * L;
+  const double G = Gtu[k];
+  const double rho_e = f.h_edge[i];
+  const double inv_dc = m.invDcEdge[e];
+  // PV flux
+  const int n2 = m.nEdgesOnEdge[e], me2 = m.maxEdges2;
+  const double pv_self = f.pv_edge[i];
+  double q = 0.0;
+  for (int j = 0; j < n2; ++j) {
+    const int eo = m.edgesOnEdge[e * me2 + j];
+    const double tq = (m.weightsOnEdge[e * me2 + j] * f.u[(size_t)eo * L + k]) * (pv_self + f.pv_edge[(size_t)eo * L + k]);
+    q = (j == 0) ? tq : q + tq;
+  }
+  q = 0.5 * q;
+  double gh = G * (q - (f.ke[i2] - f.ke[i1]) * inv_dc);
+  qb_out[i] = G * rho_e;
+  pke[i] = G * rho_e * inv_dc;
+  double gu = -G * 0.5 * (hd[i1] + hd[i2]);
+  phd[i] = -G * ue[k] * 0.5;
+  // vertical transport: tu_k = -rdzw_k (wduz_(k+1) - wduz_k)
+  auto wduzb = [&](int qq) {
+    double b = 0.0;
+    if (qq <= L - 1) b += Gtu[qq] * m.rdzw[qq];
+    if (qq - 1 >= 0) b -= Gtu[qq - 1] * m.rdzw[qq - 1];
+    return b;
+  };
+  auto rwe = [&](int qq) {
+    return 0.5 * (f.rw[(size_t)c1 * (L + 1) + qq] + f.rw[(size_t)c2 * (L + 1) + qq]);
+  };
+  for (int qq = k - 1; qq <= k + 2; ++qq) {
+    if (qq < 1 || qq > L - 1) continue;
+    const double b = wduzb(qq);
+    if (b == 0.0) continue;
+    if (qq == 1 || qq == L - 1) {
+      if (k == qq) gu += b * rwe(qq) * m.fzm[qq];
+      if (k == qq - 1) gu += b * rwe(qq) * m.fzp[qq];
+    } else {
+      const Flux3Grad d = flux3_grad(ue[qq - 2], ue[qq - 1], ue[qq], ue[qq + 1], rwe(qq), 1.0);
+      const double dq[4] = {d.qm2, d.qm1, d.q0, d.qp1};
+      gu += b * dq[k - (qq - 2)];
+    }
+  }
+  // cotangent of the edge's interface rw (w level k, 1..L-1)
+  double pr = 0.0;
+  if (k >= 1 && k <= L - 1) {
+    const double b = wduzb(k);
+    if (k == 1 || k == L - 1)
+      pr = b * (m.fzm[k] * ue[k] + m.fzp[k] * ue[k - 1]);
+    else
+      pr = b * flux3_grad(ue[k - 2], ue[k - 1], ue[k], ue[k + 1], rwe(k), 1.0).ua;
+  }
+  prwe[i] = pr;
+  if (p.rk_step == 1) {
+    const double teub = G + g.tend_u_euler[i];
+    const double zzm = 0.5 * (m.zz[i2] + m.zz[i1]);
+    ppp[i] = -teub * f.cqu_e[i] * inv_dc / zzm;
+    const int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
+    const double r_dv = fmin(m.invDvEdge[e], 4.0 * inv_dc);
+    const double u_diff = (f.divergence[i2] - f.divergence[i1]) * inv_dc -
+                          (f.vorticity[(size_t)v2 * L + k] - f.vorticity[(size_t)v1 * L + k]) * r_dv;
+    const double kdiffu = 0.5 * (kd[i1] + kd[i2]);
+    const double msd2 = m.meshScalingDel2[e];
+    gh += teub * kdiffu * u_diff * msd2;
+    pkd[i] = 0.5 * teub * rho_e * u_diff * msd2;
+    udb[i] = teub * rho_e * kdiffu * msd2;
+    if (p.del4) {
+      const double u_mix = m.meshScalingDel4[e] * p.h_mom_visc4;
+      const double r_dc4 = u_mix * p.del4u_div * inv_dc;
+      const double r_dv4 = u_mix * r_dv;
+      const double u_diff4 = (dsd[i2] - dsd[i1]) * r_dc4 - (dsv[(size_t)v2 * L + k] - dsv[(size_t)v1 * L + k]) * r_dv4;
+      gh += -teub * u_diff4;
+      pd4[i] = -teub * rho_e;
+    }
+  } else {
+    g.tend_u_euler[i] += G;
+  }
+  (void)ud;
+  g.h_edge[i] += gh;
+  g.u[i] += gu;
+}
+
+// ---- cells: the u tendency's per-edge partials gathered (index space C x (L+1)):
+// ke, the mass-flux divergence, pressure_p, kdiff, the del4 divergence (mass levels);
+// rw through the edge-interface mean (w levels)
+__global__ void k_tadj_u_cells(mpasg_mesh m, mpasg_fields g, FastDiv fl1, AdjTendScalars p,
+                               const double* __restrict__ pke, const double* __restrict__ phd,
+                               const double* __restrict__ prwe, const double* __restrict__ ppp,
+                               const double* __restrict__ pkd, const double* __restrict__ pd4,
+                               double* __restrict__ hdb, double* __restrict__ kdb, double* __restrict__ dsdb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * (L + 1)) return;
+  const uint32_t c = fl1.div(i);
+  const int k = (int)(i - c * (L + 1));
+  const int me = m.maxEdges;
+  const int n = m.nEdgesOnCell[c];
+  double gke = 0.0, ghd = 0.0, gpp = 0.0, gkd = 0.0, gds = 0.0, grw = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const int e = m.edgesOnCell[c * me + j];
+    const int side = cell_side(m, e, (int)c);
+    if (k < L) {
+      const size_t ie = (size_t)e * L + k;
+      gke += side ? -pke[ie] : pke[ie];
+      ghd += phd[ie];
+      if (p.rk_step == 1) {
+        gpp += side ? ppp[ie] : -ppp[ie];
+        gkd += pkd[ie];
+        if (p.del4) {
+          const double inv_dc = m.invDcEdge[e];
+          const double r_dc4 = m.meshScalingDel4[e] * p.h_mom_visc4 * p.del4u_div * inv_dc;
+          gds += side ? pd4[ie] * r_dc4 : -pd4[ie] * r_dc4;
+        }
+      }
+    }
+    if (k >= 1 && k <= L - 1) grw += 0.5 * prwe[(size_t)e * L + k];
+  }
+  g.rw[i] += grw;
+  if (k == L) return;
+  const size_t o = (size_t)c * L + k;
+  g.ke[o] += gke;
+  hdb[o] = ghd;
+  if (p.rk_step == 1) {
+    g.pressure_p[o] += gpp;
+    kdb[o] = gkd;
+    dsdb[o] = gds;
+  }
+}
+
+// ---- vertices (rk 1, del4): the del4 curl's cotangent
+__global__ void k_tadj_dsv(mpasg_mesh m, FastDiv fl, AdjTendScalars p, const double* __restrict__ pd4,
+                           double* __restrict__ dsvb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nVertices * L) return;
+  const uint32_t v = fl.div(i);
+  const int k = (int)(i - v * L);
+  const int vd = m.vertexDegree;
+  double a = 0.0;
+  for (int j = 0; j < vd; ++j) {
+    const int e = m.edgesOnVertex[v * vd + j];
+    if (e >= m.nEdges) continue;
+    const double inv_dc = m.invDcEdge[e];
+    const double r_dv4 = m.meshScalingDel4[e] * p.h_mom_visc4 * fmin(m.invDvEdge[e], 4.0 * inv_dc);
+    const double pp = pd4[(size_t)e * L + k] * r_dv4;
+    a += vertex_side(m, e, (int)v) ? -pp : pp;
+  }
+  dsvb[i] = a;
+}
+
+// ---- edges (rk 1): total cotangent of u_diff (del2 + del4 through delsq_u)
+__global__ void k_tadj_udiff_b(mpasg_mesh m, mpasg_transpose t, FastDiv fl, AdjTendScalars p,
+                               const double* __restrict__ dsdb, const double* __restrict__ dsvb,
+                               double* __restrict__ udb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  if (!p.del4) return;
+  const int me = m.maxEdges, vd = m.vertexDegree;
+  double a = 0.0;
+  for (int s = 0; s < 2; ++s) {
+    const int jv = t.edgeVertexSlot[2 * e + s];
+    if (jv >= 0) {
+      const int v = m.verticesOnEdge[2 * e + s];
+      a += dsvb[(size_t)v * L + k] * (m.invAreaTriangle[v] * m.dcEdge[e] * m.edgesOnVertex_sign[v * vd + jv]);
+    }
+    const int jc = t.edgeCellSlot[2 * e + s];
+    if (jc >= 0) {
+      const int c = m.cellsOnEdge[2 * e + s];
+      a += dsdb[(size_t)c * L + k] * (m.invAreaCell[c] * m.dvEdge[e] * m.edgesOnCell_sign[c * me + jc]);
+    }
+  }
+  udb[i] += a;
+}
+
+// ---- cells / vertices (rk 1): u_diff's cotangent -> divergence, vorticity
+__global__ void k_tadj_div(mpasg_mesh m, mpasg_fields g, FastDiv fl, const double* __restrict__ udb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * L) return;
+  const uint32_t c = fl.div(i);
+  const int k = (int)(i - c * L);
+  const int me = m.maxEdges;
+  const int n = m.nEdgesOnCell[c];
+  double a = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const int e = m.edgesOnCell[c * me + j];
+    const double b = udb[(size_t)e * L + k] * m.invDcEdge[e];
+    a += cell_side(m, e, (int)c) ? b : -b;
+  }
+  g.divergence[i] += a;
+}
+
+__global__ void k_tadj_vort(mpasg_mesh m, mpasg_fields g, FastDiv fl, const double* __restrict__ udb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nVertices * L) return;
+  const uint32_t v = fl.div(i);
+  const int k = (int)(i - v * L);
+  const int vd = m.vertexDegree;
+  double a = 0.0;
+  for (int j = 0; j < vd; ++j) {
+    const int e = m.edgesOnVertex[v * vd + j];
+    if (e >= m.nEdges) continue;
+    const double r_dv = fmin(m.invDvEdge[e], 4.0 * m.invDcEdge[e]);
+    const double b = udb[(size_t)e * L + k] * r_dv;
+    a += vertex_side(m, e, (int)v) ? -b : b;
+  }
+  g.vorticity[i] += a;
+}
+
+// ---- edges: the PV flux q = 0.5 sum_j w_j u_j (pv_e + pv_j) transposed over edgesOnEdge
+__global__ void k_tadj_pv(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpasg_transpose t, FastDiv fl,
+                          const double* __restrict__ qb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  const int n2 = m.nEdgesOnEdge[e], me2 = m.maxEdges2;
+  const double pv = f.pv_edge[i], u = f.u[i], qbe = qb[i];
+  double gu = 0.0, gpv = 0.0;
+  for (int j = 0; j < n2; ++j) {
+    const int eo = m.edgesOnEdge[e * me2 + j];
+    const size_t io = (size_t)eo * L + k;
+    // own sum: d q_e / d pv_e
+    gpv += qbe * m.weightsOnEdge[e * me2 + j] * f.u[io] * 0.5;
+    // neighbour eo's sum reads u_e and pv_e at its slot jt
+    const int jt = t.eoeTransSlot[e * me2 + j];
+    if (jt < 0) continue;
+    const double wt = m.weightsOnEdge[(size_t)eo * me2 + jt];
+    const double qbo = qb[io];
+    gu += qbo * wt * 0.5 * (f.pv_edge[io] + pv);
+    gpv += qbo * wt * u * 0.5;
+  }
+  g.u[i] += gu;
+  g.pv_edge[i] += gpv;
+}
+
+// ---- rk 1 mixing: edges, the del4 parts' cotangents of delsq_theta / delsq_w per edge
+__global__ void k_tadj_mix_a(mpasg_mesh m, mpasg_transpose t, FastDiv fl, AdjTendScalars p,
+                             const double* __restrict__ tteb, const double* __restrict__ tweb, double* __restrict__ a4t,
+                             double* __restrict__ a4w) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  const int me = m.maxEdges;
+  double at = 0.0, aw = 0.0;
+  for (int s = 0; s < 2; ++s) {
+    const int j = t.edgeCellSlot[2 * e + s];
+    if (j < 0) continue;
+    const int c = m.cellsOnEdge[2 * e + s];
+    const double ia = m.invAreaCell[c];
+    const double base = m.meshScalingDel4[e];
+    const double sg = m.edgesOnCell_sign[c * me + j];
+    // es = msd4 * (visc4 * ia) * dv * sign * invDc, as k_mix_cells_b forms it
+    const double es_t = base * (p.h_theta_visc4 * 1.0 * ia) * m.dvEdge[e] * sg * m.invDcEdge[e];
+    const double es_w = base * (p.h_mom_visc4 * ia) * m.dvEdge[e] * sg * m.invDcEdge[e];
+    at += tteb[(size_t)c * L + k] * es_t;
+    if (k >= 1) aw += tweb[(size_t)c * (L + 1) + k] * es_w;
+  }
+  a4t[i] = p.h_theta_visc4 > 0.0 ? at : 0.0;
+  a4w[i] = p.h_mom_visc4 > 0.0 ? aw : 0.0;
+}
+
+// ---- rk 1 mixing: cells, delsq_theta / delsq_w cotangents (index space C x (L+1))
+__global__ void k_tadj_mix_b(mpasg_mesh m, FastDiv fl1, const double* __restrict__ a4t,
+                             const double* __restrict__ a4w, double* __restrict__ dstb, double* __restrict__ dswb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * (L + 1)) return;
+  const uint32_t c = fl1.div(i);
+  const int k = (int)(i - c * (L + 1));
+  const int me = m.maxEdges;
+  const int n = m.nEdgesOnCell[c];
+  double st = 0.0, sw = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const int e = m.edgesOnCell[c * me + j];
+    const int side = cell_side(m, e, (int)c);
+    if (k < L) st += side ? -a4t[(size_t)e * L + k] : a4t[(size_t)e * L + k];
+    if (k >= 1 && k <= L - 1) sw += side ? -a4w[(size_t)e * L + k] : a4w[(size_t)e * L + k];
+  }
+  if (k < L) dstb[(size_t)c * L + k] = st;
+  dswb[i] = sw;
+}
+
+// ---- rk 1 mixing: edges, the del2 fluxes read backwards: per-edge partials for the cell
+// gathers (theta, w, kdiff) and the cotangent of h_edge (rho_edge) from theta's flux; w's
+// flux reads rho_edge at two levels, its partial per w level goes to gre
+__global__ void k_tadj_mix_c(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpasg_transpose t, FastDiv fl,
+                             const double* __restrict__ kd, const double* __restrict__ tteb,
+                             const double* __restrict__ tweb, const double* __restrict__ dstb,
+                             const double* __restrict__ dswb, double* __restrict__ bt, double* __restrict__ kdt,
+                             double* __restrict__ bw, double* __restrict__ kdw, double* __restrict__ gre) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  const int me = m.maxEdges;
+  const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
+  const size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
+  const double msd2 = m.meshScalingDel2[e];
+  const double rho_e = f.h_edge[i];
+  // theta: flux_c = es_t(c) (theta_2 - theta_1) rho_e; tte_c += flux_c 0.5 (kd_1 + kd_2) msd2
+  const double dth = f.theta_m[i2] - f.theta_m[i1];
+  const double kdm = 0.5 * (kd[i1] + kd[i2]);
+  double b = 0.0, kt = 0.0;
+  for (int s = 0; s < 2; ++s) {
+    const int j = t.edgeCellSlot[2 * e + s];
+    if (j < 0) continue;
+    const int c = m.cellsOnEdge[2 * e + s];
+    const double es = m.cell_edge_es_t[c * me + j];
+    const size_t oc = (size_t)c * L + k;
+    const double flux = es * dth * rho_e;
+    b += (tteb[oc] * kdm * msd2 + dstb[oc]) * es;
+    kt += tteb[oc] * flux * 0.5 * msd2;
+  }
+  g.h_edge[i] += b * dth;
+  bt[i] = b * rho_e;
+  kdt[i] = kt;
+  // w (level k >= 1): flux_c = es_w(c) (rho_e_k + rho_e_(k-1)) (w_2 - w_1)
+  double bwk = 0.0, kw = 0.0, gr = 0.0;
+  if (k >= 1) {
+    const size_t w1 = (size_t)c1 * (L + 1) + k, w2 = (size_t)c2 * (L + 1) + k;
+    const double dw = f.w[w2] - f.w[w1];
+    const double rsum = rho_e + f.h_edge[i - 1];
+    const double kd4 = 0.25 * (kd[i1] + kd[i2] + kd[i1 - 1] + kd[i2 - 1]);
+    double bb = 0.0;
+    for (int s = 0; s < 2; ++s) {
+      const int j = t.edgeCellSlot[2 * e + s];
+      if (j < 0) continue;
+      const int c = m.cellsOnEdge[2 * e + s];
+      const double es = m.cell_edge_es_w[c * me + j];
+      const size_t ow = (size_t)c * (L + 1) + k;
+      const double flux = es * rsum * dw;
+      bb += (tweb[ow] * msd2 * kd4 + dswb[ow]) * es;
+      kw += tweb[ow] * flux * msd2 * 0.25;
+    }
+    gr = bb * dw;
+    bwk = bb * rsum;
+  }
+  bw[i] = bwk;
+  kdw[i] = kw;
+  gre[i] = gr;
+}
+
+// ---- rk 1 mixing: cells, theta / w / kdiff gathers (index space C x (L+1))
+__global__ void k_tadj_mix_d(mpasg_mesh m, mpasg_fields g, FastDiv fl1, const double* __restrict__ bt,
+                             const double* __restrict__ kdt, const double* __restrict__ bw,
+                             const double* __restrict__ kdw, double* __restrict__ kdb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * (L + 1)) return;
+  const uint32_t c = fl1.div(i);
+  const int k = (int)(i - c * (L + 1));
+  const int me = m.maxEdges;
+  const int n = m.nEdgesOnCell[c];
+  double gth = 0.0, gw = 0.0, gk = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const int e = m.edgesOnCell[c * me + j];
+    const int side = cell_side(m, e, (int)c);
+    const size_t ie = (size_t)e * L;
+    if (k < L) {
+      gth += side ? bt[ie + k] : -bt[ie + k];
+      gk += kdt[ie + k];
+      if (k >= 1) gk += kdw[ie + k];
+      if (k + 1 <= L - 1) gk += kdw[ie + k + 1];
+    }
+    if (k >= 1 && k <= L - 1) gw += side ? bw[ie + k] : -bw[ie + k];
+  }
+  if (k < L) {
+    const size_t o = (size_t)c * L + k;
+    g.theta_m[o] += gth;
+    kdb[o] += gk;
+  }
+  g.w[i] += gw;
+}
+
+// ---- rk 1 mixing: edges, rho_edge's cotangent from w's flux at its two w levels
+__global__ void k_tadj_mix_e(mpasg_mesh m, mpasg_fields g, FastDiv fl, const double* __restrict__ gre) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  double a = 0.0;
+  if (k >= 1) a += gre[i];
+  if (k + 1 <= L - 1) a += gre[i + 1];
+  g.h_edge[i] += a;
+}
+
+// ---- rk 1 Smagorinsky: kdiff = min(cs2 sqrt(dd^2 + do^2), cap) read backwards (min and
+// sqrt with the derivative of the branch taken; ties split as torch's minimum does)
+__global__ void k_tadj_kdiff(mpasg_mesh m, FastDiv fl, AdjTendScalars p, const double* __restrict__ kdb,
+                             double* __restrict__ ddb_io, double* __restrict__ dob_io) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * L) return;
+  const double dd = ddb_io[i], dof = dob_io[i];
+  const double sq = sqrt(__dadd_rn(__dmul_rn(dd, dd), __dmul_rn(dof, dof)));
+  const double A = __dmul_rn(p.cs2, sq);
+  const double gA = A < p.kdiff_cap ? kdb[i] : (A == p.kdiff_cap ? 0.5 * kdb[i] : 0.0);
+  const double gs = sq > 0.0 ? gA * p.cs2 * 0.5 / sq : 0.0;
+  ddb_io[i] = gs * 2.0 * dd;
+  dob_io[i] = gs * 2.0 * dof;
+}
+
+__global__ void k_tadj_deform(mpasg_mesh m, mpasg_fields g, mpasg_transpose t, FastDiv fl,
+                              const double* __restrict__ ddb, const double* __restrict__ dob) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  const int me = m.maxEdges;
+  double gu = 0.0, gv = 0.0;
+  for (int s = 0; s < 2; ++s) {
+    const int j = t.edgeCellSlot[2 * e + s];
+    if (j < 0) continue;
+    const int c = m.cellsOnEdge[2 * e + s];
+    const double ca = m.defc_a[c * me + j], cb = m.defc_b[c * me + j];
+    const double a = ddb[(size_t)c * L + k], b = dob[(size_t)c * L + k];
+    gu += a * ca + b * cb;
+    gv += -a * cb + b * ca;
+  }
+  g.u[i] += gu;
+  g.v[i] += gv;
+}
+
+// ---- rk 1 density tendency: tend_rho = -h_div - rdzw (rw_(k+1) - rw_k), per w level
+__global__ void k_tadj_rho(mpasg_mesh m, mpasg_fields g, FastDiv fl1, AdjTendScalars p, double* __restrict__ hdb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * (L + 1)) return;
+  const uint32_t c = fl1.div(i);
+  const int k = (int)(i - c * (L + 1));
+  const size_t oc = (size_t)c * L;
+  if (p.rk_step != 1) return;
+  double a = 0.0;
+  if (k < L) {
+    const double G = g.tend_rho[oc + k];
+    a += G * m.rdzw[k];
+    hdb[oc + k] += -G;
+  }
+  if (k >= 1) a -= g.tend_rho[oc + k - 1] * m.rdzw[k - 1];
+  g.rw[i] += a;
+}
+
+// ---- edges: the mass-flux divergence transposed -> ru
+__global__ void k_tadj_hdiv(mpasg_mesh m, mpasg_fields g, mpasg_transpose t, FastDiv fl, const double* __restrict__ hdb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  const int me = m.maxEdges;
+  double a = 0.0;
+  for (int s = 0; s < 2; ++s) {
+    const int j = t.edgeCellSlot[2 * e + s];
+    if (j < 0) continue;
+    const int c = m.cellsOnEdge[2 * e + s];
+    a += hdb[(size_t)c * L + k] * m.invAreaCell[c] * m.cell_edge_sdv[c * me + j];
+  }
+  g.ru[i] += a;
+}
+
+#define CHECK_RC(x)                  \
+  do {                               \
+    int _rc = (x);                   \
+    if (_rc != MPASG_OK) return _rc; \
+  } while (0)
+
+}  // namespace
+
+int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
+                             const mpasg_transpose* t, int rk_step, const AdjWork& w, cudaStream_t s) {
+  const int L = m->nVertLevels;
+  const long long ncl = (long long)m->nCells * L, nel = (long long)m->nEdges * L;
+  const long long ncw = (long long)m->nCells * (L + 1), nvl = (long long)m->nVertices * L;
+  AdjTendScalars p{};
+  const double cl = c->c_s * c->len_disp;
+  p.cs2 = cl * cl;
+  p.kdiff_cap = (0.01 * (c->len_disp * c->len_disp)) * (1.0 / c->dt);
+  p.smag = c->horiz_mixing_smagorinsky;
+  if (p.smag) {
+    p.h_mom_visc4 = c->visc4_2dsmag * std::pow(c->len_disp, 3.0);
+    p.h_theta_visc4 = p.h_mom_visc4;
+  } else {
+    p.h_mom_visc4 = c->h_mom_eddy_visc4;
+    p.h_theta_visc4 = c->h_theta_eddy_visc4;
+  }
+  p.visc2 = p.smag ? 0.0 : c->h_theta_eddy_visc2;
+  p.del4u_div = c->del4u_div_factor;
+  p.coef3 = c->coef_3rd_order;
+  p.rk_step = rk_step;
+  p.del4 = p.h_mom_visc4 > 0.0 ? 1 : 0;
+  FastDiv fl(L), fl1(L + 1);
+  // work: cells
+  double* hd = w.c[0];
+  double* kd = w.c[1];
+  double* ddb = w.c[2];
+  double* dob = w.c[3];
+  double* tt1b = w.c[4];
+  double* tw1b = w.c[5];
+  double* tweb = w.c[6];
+  double* tteb = w.c[7];
+  double* dsd = w.c[8];
+  double* hdb = w.c[9];
+  double* kdb = w.c[10];
+  double* dsdb = w.c[11];
+  double* dstb = w.c[12];
+  double* dswb = w.c[13];
+  // edges
+  double* fltb = w.e[0];
+  double* flwb = w.e[1];
+  double* qb = w.e[2];
+  double* pke = w.e[3];
+  double* phd = w.e[4];
+  double* prwe = w.e[5];
+  double* ppp = w.e[6];
+  double* pkd = w.e[7];
+  double* udb = w.e[8];
+  double* ud = w.e[9];
+  double* pd4 = w.e[10];
+  double* a4t = w.e[11];
+  double* a4w = w.e[12];
+  double* bt = w.e[13];
+  double* kdt = w.e[14];
+  double* bw = w.e[15];
+  double* kdw = w.e[16];
+  double* gre = w.e[17];
+  // vertices
+  double* dsv = w.v[0];
+  double* dsvb = w.v[1];
+
+  k_tadj_values<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, p, hd, kd, ddb, dob);
+  MPASG_LAUNCH_CHECK();
+  if (rk_step == 1 && p.del4) {
+    k_tadj_udiff<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, fl, ud);
+    MPASG_LAUNCH_CHECK();
+    k_tadj_del4_cells<<<nblocks(ncl), kBlock, 0, s>>>(*m, fl, ud, dsd);
+    MPASG_LAUNCH_CHECK();
+    k_tadj_del4_vertices<<<nblocks(nvl), kBlock, 0, s>>>(*m, fl, ud, dsv);
+    MPASG_LAUNCH_CHECK();
+  }
+  k_tadj_columns<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, *g, fl1, p, tt1b, tw1b, tweb, tteb);
+  MPASG_LAUNCH_CHECK();
+  if (rk_step == 1) {
+    k_tadj_wres<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, *g, fl, tweb);
+    MPASG_LAUNCH_CHECK();
+  }
+  k_tadj_adv_edges<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, p, tt1b, tw1b, fltb, flwb);
+  MPASG_LAUNCH_CHECK();
+  k_tadj_adv_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, *g, *t, fl1, fltb, flwb);
+  MPASG_LAUNCH_CHECK();
+  k_tadj_u<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, fl, p, hd, kd, ud, dsd, dsv, qb, pke, phd, prwe, ppp, pkd, udb,
+                                          pd4);
+  MPASG_LAUNCH_CHECK();
+  k_tadj_u_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *g, fl1, p, pke, phd, prwe, ppp, pkd, pd4, hdb, kdb, dsdb);
+  MPASG_LAUNCH_CHECK();
+  k_tadj_pv<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, qb);
+  MPASG_LAUNCH_CHECK();
+  if (rk_step == 1) {
+    if (p.del4) {
+      k_tadj_dsv<<<nblocks(nvl), kBlock, 0, s>>>(*m, fl, p, pd4, dsvb);
+      MPASG_LAUNCH_CHECK();
+      k_tadj_udiff_b<<<nblocks(nel), kBlock, 0, s>>>(*m, *t, fl, p, dsdb, dsvb, udb);
+      MPASG_LAUNCH_CHECK();
+    }
+    k_tadj_div<<<nblocks(ncl), kBlock, 0, s>>>(*m, *g, fl, udb);
+    MPASG_LAUNCH_CHECK();
+    k_tadj_vort<<<nblocks(nvl), kBlock, 0, s>>>(*m, *g, fl, udb);
+    MPASG_LAUNCH_CHECK();
+    // horizontal mixing of theta and w (del2 with kdiff, del4)
+    k_tadj_mix_a<<<nblocks(nel), kBlock, 0, s>>>(*m, *t, fl, p, tteb, tweb, a4t, a4w);
+    MPASG_LAUNCH_CHECK();
+    k_tadj_mix_b<<<nblocks(ncw), kBlock, 0, s>>>(*m, fl1, a4t, a4w, dstb, dswb);
+    MPASG_LAUNCH_CHECK();
+    k_tadj_mix_c<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, kd, tteb, tweb, dstb, dswb, bt, kdt, bw, kdw, gre);
+    MPASG_LAUNCH_CHECK();
+    k_tadj_mix_d<<<nblocks(ncw), kBlock, 0, s>>>(*m, *g, fl1, bt, kdt, bw, kdw, kdb);
+    MPASG_LAUNCH_CHECK();
+    k_tadj_mix_e<<<nblocks(nel), kBlock, 0, s>>>(*m, *g, fl, gre);
+    MPASG_LAUNCH_CHECK();
+    if (p.smag) {
+      k_tadj_kdiff<<<nblocks(ncl), kBlock, 0, s>>>(*m, fl, p, kdb, ddb, dob);
+      MPASG_LAUNCH_CHECK();
+      k_tadj_deform<<<nblocks(nel), kBlock, 0, s>>>(*m, *g, *t, fl, ddb, dob);
+      MPASG_LAUNCH_CHECK();
+    }
+  }
+  k_tadj_rho<<<nblocks(ncw), kBlock, 0, s>>>(*m, *g, fl1, p, hdb);
+  MPASG_LAUNCH_CHECK();
+  k_tadj_hdiv<<<nblocks(nel), kBlock, 0, s>>>(*m, *g, *t, fl, hdb);
+  MPASG_LAUNCH_CHECK();
+  // the stage's outputs are consumed; at rk 1 so are the Euler tendencies and tend_rho it
+  // creates (later stages passed their cotangents through)
+  CHECK_RC(mpasgi_zero(g->tend_u, (m->nEdges + 1LL) * L, s));
+  CHECK_RC(mpasgi_zero(g->tend_w, (m->nCells + 1LL) * (L + 1), s));
+  CHECK_RC(mpasgi_zero(g->tend_theta, (m->nCells + 1LL) * L, s));
+  if (rk_step == 1) {
+    CHECK_RC(mpasgi_zero(g->tend_u_euler, (m->nEdges + 1LL) * L, s));
+    CHECK_RC(mpasgi_zero(g->tend_w_euler, (m->nCells + 1LL) * (L + 1), s));
+    CHECK_RC(mpasgi_zero(g->tend_theta_euler, (m->nCells + 1LL) * L, s));
+    CHECK_RC(mpasgi_zero(g->tend_rho, (m->nCells + 1LL) * L, s));
+  }
+  return MPASG_OK;
+}
+
+extern "C" int mpasg_dyn_tend_vjp(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
+                                  const mpasg_transpose* t, int rk_step, double* work, void* stream) {
+  if (!m || !c || !f || !g || !t || !work || rk_step < 1 || rk_step > 3 || !adj_supported(m, c)) return MPASG_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (rk_step > 1) {  // the edge mean of theta_m_save the rk 2 / 3 flux reads
+    mpasg_fields fm = *f;
+    CHECK_RC(mpasgi_theta_edge(m, &fm, false, s));
+  }
+  return mpasgi_dyn_tend_vjp_core(m, c, f, g, t, rk_step, adj_work(m, work), s);
+}

@@ -967,6 +967,9 @@ int mpasgi_theta_edge(const mpasg_mesh* m, mpasg_fields* f, bool mixed, cudaStre
   return MPASG_OK;
 }
 
+int mpasgi_acoustic_parts(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int small_step, double dts,
+                          cudaStream_t s, int part);
+
 int mpasgi_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int small_step, double dts,
                          cudaStream_t s, bool copies_current) {
   if (!m || !c || !f || small_step < 1) return MPASG_E_ARG;
@@ -982,25 +985,36 @@ int mpasgi_acoustic_step(const mpasg_mesh* m, const mpasg_config* c, mpasg_field
     k_tri_m<<<nblocks(n), kBlock, 0, s>>>(n, f->a_tri, f->alpha_tri, f->tri_m);  // forward-sweep factor
     MPASG_LAUNCH_CHECK();
   }
+  return mpasgi_acoustic_parts(m, c, f, small_step, dts, s, -1);
+}
+
+// The acoustic substep in two parts (part -1: both): part 0 updates ru_p / ruAvg on the
+// edges and builds the columns' right-hand sides (ac_x holds the tridiagonal right-hand
+// side after it); part 1 solves and finishes the columns.
+int mpasgi_acoustic_parts(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int small_step, double dts,
+                          cudaStream_t s, int part) {
   const int L = m->nVertLevels;
   const double rcv = kRgas / (kCp - kRgas);
   const double c2 = kCp * rcv;
   const double resm = (1.0 - c->epssm) / (1.0 + c->epssm);
   const long long ncw = (long long)m->nCells * (L + 1);
   const bool mixed = c->precision == MPASG_PRECISION_MIXED;
-  if (mixed) {
-    k_acoustic_edges<float><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), small_step,
-                                                                                dts, c2);
-    MPASG_LAUNCH_CHECK();
-    k_ac_prep_mixed<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, (float)dts,
-                                                    (float)c->epssm, (float)resm);
-    MPASG_LAUNCH_CHECK();
-  } else {
-    k_acoustic_edges<double><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), small_step,
-                                                                                 dts, c2);
-    MPASG_LAUNCH_CHECK();
-    k_ac_prep<double><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, dts, c->epssm, resm);
-    MPASG_LAUNCH_CHECK();
+  if (part != 1) {
+    if (mixed) {
+      k_acoustic_edges<float><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), small_step,
+                                                                                  dts, c2);
+      MPASG_LAUNCH_CHECK();
+      k_ac_prep_mixed<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, (float)dts,
+                                                      (float)c->epssm, (float)resm);
+      MPASG_LAUNCH_CHECK();
+    } else {
+      k_acoustic_edges<double><<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, FastDiv(L), small_step,
+                                                                                   dts, c2);
+      MPASG_LAUNCH_CHECK();
+      k_ac_prep<double><<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, FastDiv(L + 1), small_step, dts, c->epssm, resm);
+      MPASG_LAUNCH_CHECK();
+    }
+    if (part == 0) return MPASG_OK;
   }
   // the staged solve needs more than 48 KB of dynamic shared memory: opt in once per
   // device (the first call on a device should come before any stream capture)

@@ -1,0 +1,258 @@
+"""Reverse mode of the dynamics through whole large steps (the reference's
+``run_simulation.vjp`` with respect to the dynamics state, atmosphere_model.py:2101).
+
+``DynamicsAdjoint(model)`` holds, beside the model's own device state, a second device
+state of the same layout for the cotangents, the transposed connectivity of the mesh, the
+derivatives' work buffer and the per-step tape.  ``run_vjp`` runs the forward from the
+loaded primitives with one checkpoint of the step boundary per large step in HBM (the
+reference's per-step checkpoint, autodiff/checkpoint.py:106-254), then, from the last step
+back, restores each step's checkpoint and runs ``mpasg_step_vjp`` (the step recomputed with
+its tape, then its stages backwards: hand-written CUDA kernels, deterministic gathers), and
+finally ``mpasg_prepare_vjp`` for the cold-start preparation.
+
+Supported: float64, dry columns, flat terrain, ``2d_smagorinsky`` or ``2d_fixed`` mixing with
+or without del4, no vertical mixing, CAM or Rayleigh damping of u, any RK order and substep
+counts; the objective may read the step boundary's carried fields.  Everything else is
+rejected before any device work with ``MpasUnsupportedCapabilityError``.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Any, Callable, Mapping
+
+import numpy as np
+import torch
+
+from . import _lib
+from .errors import MpasConfigError, MpasNumericalError, MpasUnsupportedCapabilityError
+
+# fields that carry derivatives from one large step to the next (a step's start state)
+CARRIED = ("u", "v", "ru", "h_edge", "pv_edge", "w", "rw", "theta_m", "rho_zz", "rho_p", "rtheta_p", "exner",
+           "pressure_p", "divergence", "ke", "vorticity")
+# keys of run_simulation's output the objective may differentiate (rho_edge is h_edge)
+DIFFERENTIABLE_OUT = CARRIED + ("rho_edge",)
+TRACKABLE = ("u", "w", "theta", "rho")
+
+
+def _stream() -> C.c_void_p:
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t: torch.Tensor) -> C.c_void_p:
+    return C.c_void_p(t.data_ptr())
+
+
+def check_request(cfg: Mapping[str, Any], merged: Mapping[str, Any], num_scalars: int) -> None:
+    """The dynamics derivative's scope, checked on the host from the configuration and the
+    mesh before any device work (the same limits as ``check_supported``)."""
+    from .device import _int, _np
+    why = []
+    if str(cfg.get("config_precision", "float64")) != "float64":
+        why.append("float64 arithmetic only (config_precision)")
+    ms, me = _int(merged.get("moist_start", 1)), _int(merged.get("moist_end", num_scalars))
+    if not me < ms:
+        why.append("dry columns only (moist_end < moist_start)")
+    for k in ("zb_cell", "zb3_cell"):
+        if k in merged and np.any(_np(merged[k]) != 0.0):
+            why.append("flat terrain only")
+            break
+    for k, label in (("config_v_mom_eddy_visc2", "vertical mixing of u and w"),
+                     ("config_v_theta_eddy_visc2", "vertical mixing of theta"),
+                     ("config_mpas_cam_coef", "CAM damping")):
+        if float(cfg.get(k, 0.0) or 0.0) > 0.0:
+            why.append(f"no {label} ({k})")
+    if str(cfg.get("config_rayleigh_damp_u", False)).strip().lower() in ("true", "1", ".true.", "t"):
+        why.append("no Rayleigh damping of u (config_rayleigh_damp_u)")
+    if why:
+        raise MpasUnsupportedCapabilityError("dynamics derivatives on the GB300 path: " + "; ".join(why))
+
+
+def check_supported(model) -> None:
+    """The dynamics derivative's scope (mpasg.h): raise before any derivative work."""
+    cfg, cs, dm = model.cfg, model.cstruct, model.dmesh
+    why = []
+    if cs.precision != _lib.PRECISIONS["float64"]:
+        why.append("float64 arithmetic only (config_precision)")
+    if not (cs.moist_end < cs.moist_start):
+        why.append("dry columns only (moist_end < moist_start)")
+    if not dm.struct.flatTerrain:
+        why.append("flat terrain only")
+    if cs.v_mom_eddy_visc2 > 0.0 or cs.v_theta_eddy_visc2 > 0.0:
+        why.append("no vertical mixing (config_v_mom_eddy_visc2 / config_v_theta_eddy_visc2)")
+    if cs.mpas_cam_coef > 0.0 and cs.number_cam_damping_levels > 0:
+        why.append("no CAM damping (config_mpas_cam_coef)")
+    if cs.rayleigh_damp_u_levels > 0:
+        why.append("no Rayleigh damping of u (config_rayleigh_damp_u)")
+    if model._perm is not None:
+        why.append("native mesh order only")
+    if why:
+        raise MpasUnsupportedCapabilityError("dynamics derivatives on the GB300 path: " + "; ".join(why))
+    del cfg
+
+
+def transpose_tables(dmesh, mesh_ref: Mapping[str, Any]) -> dict[str, np.ndarray]:
+    """The transposed connectivity the reverse-mode gathers read (mpasg_transpose)."""
+    nc, ne, nv = dmesh.nCells, dmesh.nEdges, dmesh.nVertices
+    me2, vd = dmesh.maxEdges2, dmesh.vertexDegree
+    I = {k: np.asarray(v, dtype=np.int64) for k, v in dmesh.ints.items()}
+    eoc, neoc, coe = I["edgesOnCell"], I["nEdgesOnCell"], I["cellsOnEdge"]
+    eov, voe = I["edgesOnVertex"], I["verticesOnEdge"]
+    eoe, neoe = I["edgesOnEdge"], I["nEdgesOnEdge"]
+    voc, kite = I["verticesOnCell"], I["kiteForCell"]
+    me = eoc.shape[1]
+    edge_cell = np.full((ne, 2), -1, dtype=np.int64)
+    cells = np.arange(nc)
+    for j in range(me):
+        ok = (j < neoc) & (eoc[:, j] < ne)
+        e = eoc[ok, j]
+        c = cells[ok]
+        side = np.where(coe[e, 0] == c, 0, np.where(coe[e, 1] == c, 1, -1))
+        good = side >= 0
+        edge_cell[e[good], side[good]] = j
+    edge_vert = np.full((ne, 2), -1, dtype=np.int64)
+    verts = np.arange(nv)
+    for j in range(vd):
+        ok = eov[:, j] < ne
+        e = eov[ok, j]
+        v = verts[ok]
+        side = np.where(voe[e, 0] == v, 0, np.where(voe[e, 1] == v, 1, -1))
+        good = side >= 0
+        edge_vert[e[good], side[good]] = j
+    eoe_t = np.full((ne, me2), -1, dtype=np.int64)
+    edges = np.arange(ne)
+    for j in range(me2):
+        ok = (j < neoe) & (eoe[:, j] < ne)
+        e, eo = edges[ok], eoe[ok, j]
+        for jt in range(me2):
+            hit = (jt < neoe[eo]) & (eoe[eo, jt] == e) & (eoe_t[e, j] < 0)
+            eoe_t[e[hit], j] = jt
+    if "cellsOnVertex" in mesh_ref:
+        cov_raw = np.asarray(mesh_ref["cellsOnVertex"].detach().cpu() if isinstance(mesh_ref["cellsOnVertex"], torch.Tensor)
+                             else mesh_ref["cellsOnVertex"], dtype=np.int64)[:nv, :vd]
+        cov = np.where((cov_raw >= 1) & (cov_raw <= nc), cov_raw - 1, nc)
+    else:  # from verticesOnCell
+        cov = np.full((nv, vd), nc, dtype=np.int64)
+        fill = np.zeros(nv, dtype=np.int64)
+        for c in range(nc):
+            for j in range(int(neoc[c])):
+                v = voc[c, j]
+                if v < nv and fill[v] < vd:
+                    cov[v, fill[v]] = c
+                    fill[v] += 1
+    vkite = np.full((nv, vd), -1, dtype=np.int64)
+    for s in range(vd):
+        c = cov[:, s]
+        okc = c < nc
+        cc = np.where(okc, c, 0)
+        for j in range(me):
+            hit = okc & (j < neoc[cc]) & (voc[cc, j] == verts) & (vkite[:, s] < 0)
+            vkite[hit, s] = kite[cc[hit], j]
+    from .tracer_adjoint import transport_adjacency
+    adj = transport_adjacency(dmesh)
+    return {"edgeCellSlot": edge_cell.astype(np.int32), "edgeVertexSlot": edge_vert.astype(np.int32),
+            "eoeTransSlot": eoe_t.astype(np.int32), "cellsOnVertex": cov.astype(np.int32),
+            "vertexKite": vkite.astype(np.int32),
+            "advPtr": adj["adj_ptr"].cpu().numpy(), "advIdx": adj["adj_es"].cpu().numpy()}
+
+
+class DynamicsAdjoint:
+    """Cotangent state, transposed connectivity, work buffer and tape of one Model."""
+
+    def __init__(self, model):
+        from .device import DeviceState
+        check_supported(model)
+        self.model = model
+        self.lib = model.lib
+        dm = model.dmesh
+        dev = dm.device
+        tabs = transpose_tables(dm, model.mesh_ref)
+        self._tabs = {k: torch.as_tensor(np.ascontiguousarray(v), device=dev) for k, v in tabs.items()}
+        t = _lib.TransposeStruct()
+        for k in _lib.TRANSPOSE_PTRS:
+            setattr(t, k, self._tabs[k].data_ptr())
+        self.t = t
+        self.g = DeviceState(dm, model.state.num_scalars)
+        self.g.f["rho_zz"].zero_()  # a cotangent: the padding sentinel does not apply
+        n = int(self.lib.mpasg_dyn_vjp_work_doubles(C.byref(dm.struct)))
+        self.work = torch.zeros(n, dtype=torch.float64, device=dev)
+        self.tape: torch.Tensor | None = None
+
+    # -- checkpoints of the step boundary -------------------------------------------
+    def checkpoint(self) -> dict[str, torch.Tensor]:
+        return {k: self.model.state.f[k].clone() for k in CARRIED}
+
+    def restore(self, ck: Mapping[str, torch.Tensor]) -> None:
+        for k in CARRIED:
+            self.model.state.f[k].copy_(ck[k])
+
+    def zero_cotangents(self) -> None:
+        self.g.arena.zero_()
+
+    def _tape(self) -> torch.Tensor:
+        if self.tape is None:
+            n = int(self.lib.mpasg_step_vjp_tape_doubles(C.byref(self.model.dmesh.struct),
+                                                         C.byref(self.model.cstruct)))
+            if n <= 0:
+                raise MpasConfigError("mpasg_step_vjp_tape_doubles: invalid configuration")
+            self.tape = torch.empty(n, dtype=torch.float64, device=self.model.dmesh.device)
+        return self.tape
+
+    # -- one step / preparation -----------------------------------------------------
+    def step_vjp(self) -> None:
+        """Cotangents in g of the state after one step (from the state in the model) ->
+        cotangents of the step's start state; the model's state ends one step later."""
+        m = self.model
+        rc = self.lib.mpasg_step_vjp(C.byref(m.dmesh.struct), C.byref(m.cstruct), C.byref(m.state.struct),
+                                     C.byref(self.g.struct), C.byref(self.t), _p(self._tape()), _p(self.work),
+                                     _stream())
+        _lib.check(rc, "mpasg_step_vjp")
+
+    def prepare_vjp(self, w_in: torch.Tensor) -> dict[str, torch.Tensor]:
+        """Cotangents in g of the prepared state (the model holds it) -> cotangents of the
+        loaded u, w, theta, rho."""
+        m = self.model
+        f = m.state.f
+        out = {k: torch.empty_like(f[n]) for k, n in (("u", "u"), ("w", "w"), ("theta", "theta_m"),
+                                                       ("rho", "rho_zz"))}
+        rc = self.lib.mpasg_prepare_vjp(C.byref(m.dmesh.struct), C.byref(m.cstruct), C.byref(m.state.struct),
+                                        C.byref(self.g.struct), C.byref(self.t), _p(w_in), _p(out["u"]),
+                                        _p(out["w"]), _p(out["theta"]), _p(out["rho"]), _p(self.work), _stream())
+        _lib.check(rc, "mpasg_prepare_vjp")
+        return out
+
+
+def run_vjp(model, loaded: Mapping[str, Any], nsteps: int,
+            cotangents: Callable[[dict], Mapping[str, torch.Tensor]],
+            adj: DynamicsAdjoint | None = None) -> tuple[dict, dict]:
+    """Forward from the loaded primitives through ``nsteps`` large steps with a checkpoint
+    per step, then the reverse sweep.  ``cotangents(out)`` receives the final state (the
+    model's export) and returns cotangents of some of its carried fields.  Returns the
+    cotangents of the loaded u, w, theta, rho and the final state."""
+    adj = adj or DynamicsAdjoint(model)
+    model.prepare(loaded)
+    dev = model.dmesh.device
+    w_in = model.state.f["w"].clone()
+    ckpts = [adj.checkpoint()]
+    for n in range(int(nsteps)):
+        model.step()
+        if n + 1 < nsteps:
+            ckpts.append(adj.checkpoint())
+    bad = model.check_finite()
+    if bad:
+        raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")
+    final = model.export()
+    adj.zero_cotangents()
+    g = cotangents(final)
+    for k, v in g.items():
+        name = "h_edge" if k == "rho_edge" else k
+        if name not in CARRIED:
+            raise MpasUnsupportedCapabilityError(f"no derivative through output {k!r}")
+        dst = adj.g.f[name]
+        dst[: v.shape[0]].add_(v.to(device=dev, dtype=torch.float64))
+    for n in range(int(nsteps) - 1, -1, -1):
+        adj.restore(ckpts[n])
+        adj.step_vjp()
+    adj.restore(ckpts[0])
+    grads = adj.prepare_vjp(w_in)
+    return grads, final

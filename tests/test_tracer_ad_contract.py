@@ -17,11 +17,28 @@ def _case():
     return state, meta
 
 
-def test_vjp_tracks_scalars_only():
+def test_vjp_track_keys_contract():
+    """The scalars, or the dynamics keys u / w / theta / rho, never both; nothing else."""
     state, meta = _case()
-    for keys in (None, ("u",), ("scalars", "theta")):
+    for keys in (None, ("scalars", "theta"), ("theta_m",)):
         with pytest.raises(MpasUnsupportedCapabilityError):
             run_simulation.vjp(state, state, lambda o: o["scalars"].sum(), track_keys=keys, config=meta["config"])
+
+
+@pytest.mark.parametrize("extra", [{"config_v_mom_eddy_visc2": 1.0}, {"config_mpas_cam_coef": 1.0},
+                                   {"config_rayleigh_damp_u": True}, {"config_precision": "mixed"}])
+def test_dynamics_vjp_scope_rejected_before_device_work(extra):
+    state, meta = _case()
+    cfg = dict(meta["config"], **extra)
+    with pytest.raises(MpasUnsupportedCapabilityError):
+        run_simulation.vjp(state, state, lambda o: o["rho_zz"].sum(), track_keys=("u", "theta"), config=cfg)
+
+
+def test_dynamics_vjp_moist_rejected_before_device_work():
+    state, meta = _case()
+    state = dict(state, moist_end=1)
+    with pytest.raises(MpasUnsupportedCapabilityError):
+        run_simulation.vjp(state, state, lambda o: o["rho_zz"].sum(), track_keys=("theta",), config=meta["config"])
 
 
 @pytest.mark.parametrize("extra", [{"config_monotonic": True}, {"config_positive_definite": True},
