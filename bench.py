@@ -336,6 +336,76 @@ def measure_scalar_vjp(args, dev):
             "gradient_finite": bool(torch.isfinite(g0).all())}
 
 
+DYN_VJP_SPEC = dict(level=5, nlev=41, seed=2, n_bumps=8, n_tracers=1, w_sine=0.1, round_wind_bits=16)
+
+
+def measure_dynamics_vjp(args, dev):
+    """The differentiation workload: gradient of the area-weighted squared surface-pressure
+    anomaly after 24 steps (level-5 mesh 10242 cells x 41 levels, dt 900 s, 16-bit wind,
+    0.1 m/s sinusoidal w) with respect to the initial u and theta, by the hand-written
+    reverse mode (preparation, 24 steps with a checkpoint each, the objective's gradient, 24
+    reverse steps each recomputing its step with the tape, the preparation's reverse), against
+    the same 24 forward steps replayed from a CUDA graph; CUDA events on the stream."""
+    import torch
+
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.diagnostics import physics_interface_surface_pressure, surface_pressure_functional
+    from mpas_dycore_pytorch_gb300.dyn_adjoint import DynamicsAdjoint, run_vjp
+    from mpas_dycore_pytorch_gb300.loader import load_case
+
+    cfg = dict(_cfg(WORKLOADS["c2"]), config_monotonic=False)
+    dt, nsteps = 900.0, 24
+    st, _ = load_case(CaseSpec(**DYN_VJP_SPEC), cfg, as_torch=False)
+    nc = int(st["nCells"])
+    m = Model(st, cfg, dt, num_scalars=1, device=dev)
+    m.prepare(st)
+    m.step()
+    m.capture_graph()
+    ms_fwd = _time_steps(m.step, nsteps, args.warmup)
+    del m
+    torch.cuda.empty_cache()
+    m = Model(st, cfg, dt, num_scalars=1, device=dev)
+    adj = DynamicsAdjoint(m)
+    zz = torch.as_tensor(st["zz"], device=dev)
+    zgrid = torch.as_tensor(st["zgrid"], device=dev)
+    area = torch.as_tensor(st["areaCell"], device=dev)
+    m.prepare(st)
+    sp_ref = physics_interface_surface_pressure(
+        nCells=nc, rho_zz=m.state.f["rho_zz"], zz=zz, qv=torch.zeros_like(m.state.f["rho_zz"]),
+        pressure_p=m.state.f["pressure_p"], pressure_base=m.state.f["pressure_base"], zgrid=zgrid).detach().clone()
+
+    def cotangents(final):
+        rz = final["rho_zz"].detach().clone().requires_grad_(True)
+        pp = final["pressure_p"].detach().clone().requires_grad_(True)
+        sp = physics_interface_surface_pressure(nCells=nc, rho_zz=rz, zz=zz, qv=torch.zeros_like(rz), pressure_p=pp,
+                                                pressure_base=final["pressure_base"], zgrid=zgrid)
+        J = surface_pressure_functional(sp, sp_ref, area, nc)
+        g_rz, g_pp = torch.autograd.grad(J, [rz, pp])
+        return {"rho_zz": g_rz, "pressure_p": g_pp}
+
+    ms = []
+    for rep in range(2):  # the second repetition is timed
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        grads, _ = run_vjp(m, st, nsteps, cotangents, adj)
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    cl = st_cells_levels(st)
+    finite = all(bool(torch.isfinite(grads[k]).all()) for k in ("u", "theta"))
+    return {"workload": "level-5 mesh 10242 cells x 41 levels, dry, 16-bit wind, 0.1 m/s sinusoidal w, 24 steps at "
+                        "dt 900 s; gradient of the area-weighted squared surface-pressure anomaly w.r.t. initial u and "
+                        "theta",
+            "value": cl * nsteps / (ms[-1] / 1e3), "unit": UNIT, "ms": ms[-1],
+            "forward_graph_ms": ms_fwd * nsteps, "vjp_over_forward": ms[-1] / (ms_fwd * nsteps),
+            "includes": "preparation, 24 eager forward steps with a checkpoint each, the objective's gradient, 24 "
+                        "reverse steps (each recomputes its step with the tape), the preparation's reverse",
+            "tape_bytes": int(adj.tape.numel() * 8) if adj.tape is not None else 0,
+            "gradient_finite": finite}
+
+
 def measure_ensemble_groups(args, dev):
     """The two-grid mixed-precision ensemble: 96 members of 10242 cells x 41 levels (dt
     900 s) and 32 members of 40962 cells x 55 stretched levels (dt 720 s), 2 monotone
@@ -609,6 +679,8 @@ def run_gb300(args, rank, world):
         torch.cuda.empty_cache()
         forms = measure_forms(args, dev, st, cfg, w, ms / K)
         forms["vjp_scalars"] = measure_scalar_vjp(args, dev)
+        torch.cuda.empty_cache()
+        forms["vjp_dynamics"] = measure_dynamics_vjp(args, dev)
         if args.ensemble_groups:
             forms["batched_two_grids"] = measure_ensemble_groups(args, dev)
 

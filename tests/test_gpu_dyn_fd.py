@@ -1,0 +1,93 @@
+"""The dynamics gradient of the differentiation workload against central differences.
+
+Recipe: level-5 mesh (10242 cells x 41 levels), the analytic dry state with 8 seeded theta
+bumps, a 0.1 m/s sinusoidal w and the wind rounded to 16 significant bits (so that the
+perturbations below are exactly representable where the reference's recipe needs it,
+examples/validate_model.py:216-252), 24 steps at dt 900 s (RK3, 3 x 2 substeps).  The
+functional is the area-weighted squared anomaly of the surface pressure at the final time
+against the initial surface pressure.  Its gradient with respect to the initial u and theta
+(run_simulation.vjp) is checked along a seeded random direction against central differences
+of run_simulation over h = 2^-12 ... 2^-36 (the stated 2^-20 ... 2^-36 and the larger steps
+that show the truncation side of the curve): it must reach a relative error <= 1e-7,
+and a control that drops the theta part of the gradient must miss it by far.
+"""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_helpers import need_gpu
+
+pytestmark = pytest.mark.gpu
+
+SPEC = dict(level=5, nlev=41, seed=2, n_bumps=8, n_tracers=1, w_sine=0.1, round_wind_bits=16)
+CFG = {"config_time_integration_order": 3, "config_len_disp": 120000.0, "config_number_of_sub_steps": 2,
+       "config_dynamics_split_steps": 3, "config_monotonic": False, "config_dt": 900.0}
+NSTEPS = 24
+H = [2.0 ** -e for e in range(12, 37, 2)]
+
+
+def _setup():
+    from mpas_dycore_pytorch_gb300.api import run_simulation
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.diagnostics import physics_interface_surface_pressure, surface_pressure_functional
+    from mpas_dycore_pytorch_gb300.loader import load_case
+    st, mesh = load_case(CaseSpec(**SPEC), CFG, as_torch=True)
+    nc = int(st["nCells"])
+    dev = torch.device("cuda")
+    zz = st["zz"].to(dev, torch.float64)
+    zgrid = st["zgrid"].to(dev, torch.float64)
+    area = st["areaCell"].to(dev, torch.float64)
+
+    def sp_of(out):
+        rz = out["rho_zz"]
+        return physics_interface_surface_pressure(nCells=nc, rho_zz=rz, zz=zz, qv=torch.zeros_like(rz),
+                                                  pressure_p=out["pressure_p"], pressure_base=out["pressure_base"],
+                                                  zgrid=zgrid)
+
+    prepared = run_simulation(st, mesh, CFG, 900.0, nsteps=1, on_initial=lambda s: None)  # warm the path
+    del prepared
+    box = {}
+    run_simulation(st, mesh, CFG, 900.0, nsteps=1,
+                   on_initial=lambda s: box.update({k: v.clone() for k, v in s.items()
+                                                    if isinstance(v, torch.Tensor) and v.is_cuda}))
+    sp_ref = sp_of(box).detach()
+
+    def objective(out):
+        return surface_pressure_functional(sp_of(out), sp_ref, area, nc)
+
+    return st, mesh, objective
+
+
+def test_gradient_matches_central_differences():
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import run_simulation
+    st, mesh, objective = _setup()
+    grads = run_simulation.vjp(st, mesh, objective, track_keys=("u", "theta"), config=CFG, dt=900.0,
+                               nsteps=NSTEPS)
+    rng = np.random.default_rng(2)
+    d = {}
+    for k, scale in (("u", 1.0), ("theta", 0.1)):
+        x = rng.standard_normal(tuple(st[k].shape)) * scale
+        x[-1] = 0.0  # the padding row is not perturbed
+        d[k] = torch.as_tensor(x)
+    dJ = sum(float((grads[k].cpu() * d[k]).sum()) for k in d)
+    rows = []
+    for h in H:
+        Js = []
+        for sgn in (1.0, -1.0):
+            s2 = dict(st)
+            for k in d:
+                s2[k] = st[k] + sgn * h * d[k]
+            Js.append(float(objective(run_simulation(s2, mesh, CFG, 900.0, nsteps=NSTEPS))))
+        fd = (Js[0] - Js[1]) / (2.0 * h)
+        rows.append((h, fd, abs(fd - dJ) / abs(dJ)))
+    for h, fd, err in rows:
+        print(f"FD h=2^{int(round(math.log2(h)))} fd={fd:.12e} adjoint={dJ:.12e} rel_err={err:.3e}")
+    errs = [r[2] for r in rows]
+    assert min(errs) <= 1e-7, errs
+    # failing control: without its theta part the directional derivative misses every point
+    dJ_u = float((grads["u"].cpu() * d["u"]).sum())
+    assert min(abs(fd - dJ_u) / abs(dJ) for _, fd, _ in rows) > 1e-3
