@@ -501,6 +501,14 @@ int mpasg_diag_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, 
  * they do not feed the dynamics. */
 int mpasg_step_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *g,
                    const mpasg_transpose *t, double *tape, double *work, void *stream);
+/* The two halves of mpasg_step_vjp, for callers that keep the tapes of several steps (no
+ * recomputation, the reference's checkpoint_timesteps=False): mpasg_step_tape advances f by
+ * one step writing the tape; mpasg_step_vjp_taped runs the reverse pass from a tape (f
+ * supplies only the base state, moist coefficients and diabatic forcing).  g as for
+ * mpasg_step_vjp. */
+int mpasg_step_tape(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, double *tape, void *stream);
+int mpasg_step_vjp_taped(const mpasg_mesh *m, const mpasg_config *c, const mpasg_fields *f, mpasg_fields *g,
+                         const mpasg_transpose *t, const double *tape, double *work, void *stream);
 /* Reverse mode of the cold-start preparation (mpasg_prepare; init_coupled_diagnostics.py:147
  * and the first diagnostics): f holds the prepared state, u and w the loaded wind (edges) and
  * vertical wind (cells, L+1 levels); g the cotangents of the prepared state (consumed).

@@ -151,7 +151,7 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_surface_pressure_vjp", "mpasg_surface_pressure_jvp", "mpasg_weighted_sq_sum_vjp",
            "mpasg_dyn_vjp_work_doubles", "mpasg_step_vjp_tape_doubles", "mpasg_vimp_vjp", "mpasg_dyn_tend_vjp",
            "mpasg_smlstep_vjp", "mpasg_acoustic_vjp", "mpasg_divdamp_vjp", "mpasg_recover_vjp", "mpasg_diag_vjp",
-           "mpasg_step_vjp", "mpasg_prepare_vjp")
+           "mpasg_step_vjp", "mpasg_prepare_vjp", "mpasg_step_tape", "mpasg_step_vjp_taped")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -228,6 +228,8 @@ def load() -> C.CDLL:
         "mpasg_diag_vjp": ([m, c, f, f, t, C.c_int, vp, vp], C.c_int),
         "mpasg_step_vjp": ([m, c, f, f, t, vp, vp, vp], C.c_int),
         "mpasg_prepare_vjp": ([m, c, f, f, t] + [vp] * 7, C.c_int),
+        "mpasg_step_tape": ([m, c, f, vp, vp], C.c_int),
+        "mpasg_step_vjp_taped": ([m, c, f, f, t, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -746,7 +746,10 @@ def _dynamics_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any] | None, obje
             res[k] = g.detach()
         return res
 
-    grads, _ = run_vjp(model, merged, nsteps, cotangents, adj)
+    # checkpoint_timesteps=False keeps every step's tape (no recomputation), as the reference
+    # keeps the whole graph without its per-step checkpoint (atmosphere_model.py:120-154)
+    mode = "none" if kwargs.get("checkpoint_timesteps") is False else "step"
+    grads, _ = run_vjp(model, merged, nsteps, cotangents, adj, checkpoint=mode)
     res = {}
     for k in keys:
         ref = state[k]

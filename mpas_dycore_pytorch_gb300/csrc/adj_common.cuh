@@ -75,8 +75,8 @@ int mpasgi_acoustic_vjp_core(const mpasg_mesh* m, const mpasg_config* c, mpasg_f
 int mpasgi_acoustic_vjp_fwd(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int small_step, double dts,
                             const AdjWork& w, cudaStream_t s);
 int mpasgi_acoustic_vjp_rev(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, mpasg_fields* g,
-                            const mpasg_transpose* t, int small_step, double dts, const AdjWork& w,
-                            cudaStream_t s);
+                            const mpasg_transpose* t, int small_step, double dts, const double* rt_in,
+                            const double* rwp_in, const AdjWork& w, cudaStream_t s);
 int mpasgi_vimp_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
                          double dts, const AdjWork& w, cudaStream_t s);
 int mpasgi_smlstep_vjp_core(const mpasg_mesh* m, mpasg_fields* g, cudaStream_t s);

@@ -5,11 +5,11 @@
 // The caller restores the step's start state from its checkpoint; the step is then run
 // forward once more while the values its reverse pass needs are kept in the tape: the state
 // at the start of every RK stage (and at the end), the saves of every dynamics substep, every
-// RK stage's tendencies, every implicit-coefficient set and every acoustic substep's inputs.
-// The saves, tendencies and coefficients are written into the tape by the forward kernels
-// themselves (their field pointers point into the tape); the state and acoustic inputs are
-// copied.  The stages then run backwards, each stage VJP reading its forward values from the
-// tape (the acoustic substeps are recomputed from their inputs).
+// RK stage's tendencies, every implicit-coefficient set and every acoustic substep's inputs
+// and outputs.  The saves, tendencies and coefficients are written into the tape by the
+// forward kernels themselves (their field pointers point into the tape); the state and the
+// acoustic fields are copied.  The stages then run backwards, each stage VJP reading its
+// forward values from the tape.
 #include <cmath>
 
 #include "adj_common.cuh"
@@ -84,7 +84,7 @@ StepPlan plan_of(const mpasg_config* c) {
 // Tape layout (doubles, every array rounded to 32 doubles)
 struct Tape {
   long long E, W, C, V, Lr;
-  long long snap_sz, sv_sz, tend_sz, trho_sz, coef_sz, ac_sz;
+  long long snap_sz, sv_sz, tend_sz, trho_sz, coef_sz, ac_sz, aco_sz;
   int n_snap, n_sv, n_tend, n_coef, n_ac;
   double* base = nullptr;
   Tape(const mpasg_mesh* m, const StepPlan& p) {
@@ -100,6 +100,7 @@ struct Tape {
     trho_sz = C;
     coef_sz = Lr + 8 * C + W;
     ac_sz = E + 2 * C + W;
+    aco_sz = E + 2 * W + 3 * C;
     n_snap = 3 * p.split + 1;
     n_sv = p.split;
     n_tend = 3 * p.split;
@@ -107,7 +108,8 @@ struct Tape {
     n_ac = p.n_ac;
   }
   long long doubles() const {
-    return n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + n_sv * trho_sz + n_coef * coef_sz + n_ac * ac_sz;
+    return n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + n_sv * trho_sz + n_coef * coef_sz +
+           n_ac * (ac_sz + aco_sz);
   }
   double* snap(int i) const { return base + i * snap_sz; }
   double* sv(int i) const { return base + n_snap * snap_sz + i * sv_sz; }
@@ -116,9 +118,14 @@ struct Tape {
   double* coef(int i) const {
     return base + n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + n_sv * trho_sz + i * coef_sz;
   }
+  // acoustic substep i: its inputs (ru_p, rho_pp, rtheta_pp, rw_p), then its outputs
+  // (ru_p after the edge update, the undamped solution x, ts, the damped solution rw_p,
+  // rtheta_pp and rtheta_pp_old)
   double* ac(int i) const {
-    return base + n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + n_sv * trho_sz + n_coef * coef_sz + i * ac_sz;
+    return base + n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + n_sv * trho_sz + n_coef * coef_sz +
+           i * (ac_sz + aco_sz);
   }
+  double* aco(int i) const { return ac(i) + ac_sz; }
   // the pointer of snapshot field k inside snapshot block b
   double* snap_field(double* b, int k) const {
     if (k < S_W) return b + k * E;
@@ -197,14 +204,29 @@ int ac_store(const mpasg_mesh* m, const Tape& T, const mpasg_fields& f, int a, c
   return MPASG_OK;
 }
 
-int ac_restore(const mpasg_mesh* m, const Tape& T, mpasg_fields& f, int a, cudaStream_t s) {
+// the substep's outputs the reverse pass reads (after the acoustic step, before damping)
+int aco_store(const mpasg_mesh* m, const Tape& T, const mpasg_fields& f, int a, cudaStream_t s) {
   const long long L = m->nVertLevels;
-  const double* b = T.ac(a);
-  CHECK_RC(dcopy(f.ru_p, b, (m->nEdges + 1LL) * L, s));
-  CHECK_RC(dcopy(f.rho_pp, b + T.E, (m->nCells + 1LL) * L, s));
-  CHECK_RC(dcopy(f.rtheta_pp, b + T.E + T.C, (m->nCells + 1LL) * L, s));
-  CHECK_RC(dcopy(f.rw_p, b + T.E + 2 * T.C, (m->nCells + 1LL) * (L + 1), s));
+  const long long nel = (m->nEdges + 1LL) * L, ncw = (m->nCells + 1LL) * (L + 1), ncl = (m->nCells + 1LL) * L;
+  double* b = T.aco(a);
+  CHECK_RC(dcopy(b, f.ru_p, nel, s));
+  CHECK_RC(dcopy(b + T.E, f.ac_x, ncw, s));
+  CHECK_RC(dcopy(b + T.E + T.W, f.rw_p, ncw, s));
+  CHECK_RC(dcopy(b + T.E + 2 * T.W, f.ac_ts, ncl, s));
+  CHECK_RC(dcopy(b + T.E + 2 * T.W + T.C, f.rtheta_pp, ncl, s));
+  CHECK_RC(dcopy(b + T.E + 2 * T.W + 2 * T.C, f.rtheta_pp_old, ncl, s));
   return MPASG_OK;
+}
+
+// a view whose acoustic fields are substep a's taped outputs
+void aco_view(const Tape& T, mpasg_fields& v, int a) {
+  double* b = T.aco(a);
+  v.ru_p = b;
+  v.ac_x = b + T.E;
+  v.rw_p = b + T.E + T.W;
+  v.ac_ts = b + T.E + 2 * T.W;
+  v.rtheta_pp = b + T.E + 2 * T.W + T.C;
+  v.rtheta_pp_old = b + T.E + 2 * T.W + 2 * T.C;
 }
 
 __global__ void k_fill_row(double* __restrict__ p, int n, double v) {
@@ -296,8 +318,9 @@ int forward_taped(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, co
       CHECK_RC(mpasgi_dyn_tend(m, c, &f, rk, s, true));
       CHECK_RC(mpasg_smlstep_pert(m, c, &f, stream));
       for (int small = 1; small <= p.nsub[rk - 1]; ++small) {
-        CHECK_RC(ac_store(m, T, f, a++, s));
+        CHECK_RC(ac_store(m, T, f, a, s));
         CHECK_RC(mpasgi_acoustic_step(m, c, &f, small, dts, s, true));
+        CHECK_RC(aco_store(m, T, f, a++, s));
         CHECK_RC(mpasgi_divergence_damping(m, c, &f, dts, s, true));
       }
       CHECK_RC(mpasg_recover_large_step(m, c, &f, rk, p.nsub[rk - 1], p.rk_ts[rk - 1], stream));
@@ -334,15 +357,12 @@ int zero_work_cotangents(const mpasg_mesh* m, mpasg_fields* g, cudaStream_t s) {
   return MPASG_OK;
 }
 
-int step_vjp_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin, mpasg_fields* g,
-                  const mpasg_transpose* t, double* tape, double* work, cudaStream_t s) {
-  const StepPlan p = plan_of(c);
-  Tape T(m, p);
-  T.base = tape;
-  const AdjWork w = adj_work(m, work);
+// the reverse pass of one step from its tape (f supplies the static fields: base state,
+// moist coefficients, diabatic forcing; its pointers are redirected into the tape)
+int step_reverse(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* fin, mpasg_fields* g,
+                 const mpasg_transpose* t, const StepPlan& p, const Tape& T, const AdjWork& w, cudaStream_t s) {
   const int L = m->nVertLevels;
-  mpasg_fields f = *fin;  // pointers are redirected into the tape below; the caller's struct stays
-  CHECK_RC(forward_taped(m, c, f, p, T, s));
+  const mpasg_fields f = *fin;
   CHECK_RC(zero_internal(m, g, s));
   int a = p.n_ac;
   for (int sub = p.split; sub >= 1; --sub) {
@@ -359,17 +379,18 @@ int step_vjp_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin,
       snap_view(T, post, T.snap(i + 1));
       CHECK_RC(mpasgi_diag_vjp_core(m, c, &post, g, t, rk, w, s));
       CHECK_RC(mpasgi_recover_vjp_core(m, c, &post, g, rk, p.rk_ts[rk - 1], w, s));
-      // acoustic substeps, last first, each recomputed from its inputs
+      // acoustic substeps, last first, from their taped inputs and outputs
       mpasg_fields pre = fe;
       snap_view(T, pre, T.snap(i));
       coef_view(T, pre, coef_slot(p, sub, rk));
       tend_view(T, pre, i, sub - 1);
       for (int small = p.nsub[rk - 1]; small >= 1; --small) {
         --a;
-        CHECK_RC(ac_restore(m, T, pre, a, s));
-        CHECK_RC(mpasgi_acoustic_vjp_fwd(m, c, &pre, small, dts, w, s));
-        CHECK_RC(mpasgi_divdamp_vjp_core(m, c, &pre, g, dts, w, s));
-        CHECK_RC(mpasgi_acoustic_vjp_rev(m, c, &pre, g, t, small, dts, w, s));
+        mpasg_fields ac = pre;
+        aco_view(T, ac, a);
+        const double* in = T.ac(a);
+        CHECK_RC(mpasgi_divdamp_vjp_core(m, c, &ac, g, dts, w, s));
+        CHECK_RC(mpasgi_acoustic_vjp_rev(m, c, &ac, g, t, small, dts, in + T.E + T.C, in + T.E + 2 * T.C, w, s));
       }
       CHECK_RC(mpasgi_smlstep_vjp_core(m, g, s));
       CHECK_RC(mpasgi_dyn_tend_vjp_core(m, c, &pre, g, t, rk, w, s));
@@ -385,6 +406,12 @@ int step_vjp_impl(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* fin,
   return fold_saves(m, g, s);
 }
 
+bool step_args_ok(const mpasg_mesh* m, const mpasg_config* c) {
+  return adj_supported(m, c) && c->precision == MPASG_PRECISION_FLOAT64 &&
+         (c->time_integration_order == 2 || c->time_integration_order == 3) && c->number_of_sub_steps >= 1 &&
+         c->dynamics_split_steps >= 1;
+}
+
 }  // namespace
 
 extern "C" long long mpasg_step_vjp_tape_doubles(const mpasg_mesh* m, const mpasg_config* c) {
@@ -393,11 +420,29 @@ extern "C" long long mpasg_step_vjp_tape_doubles(const mpasg_mesh* m, const mpas
   return Tape(m, p).doubles();
 }
 
+extern "C" int mpasg_step_tape(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, double* tape,
+                               void* stream) {
+  if (!m || !c || !f || !tape || !step_args_ok(m, c)) return MPASG_E_ARG;
+  const StepPlan p = plan_of(c);
+  Tape T(m, p);
+  T.base = tape;
+  return forward_taped(m, c, *f, p, T, (cudaStream_t)stream);
+}
+
+extern "C" int mpasg_step_vjp_taped(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f,
+                                    mpasg_fields* g, const mpasg_transpose* t, const double* tape, double* work,
+                                    void* stream) {
+  if (!m || !c || !f || !g || !t || !tape || !work || !step_args_ok(m, c)) return MPASG_E_ARG;
+  const StepPlan p = plan_of(c);
+  Tape T(m, p);
+  T.base = const_cast<double*>(tape);  // read only below
+  return step_reverse(m, c, f, g, t, p, T, adj_work(m, work), (cudaStream_t)stream);
+}
+
 extern "C" int mpasg_step_vjp(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, mpasg_fields* g,
                               const mpasg_transpose* t, double* tape, double* work, void* stream) {
-  if (!m || !c || !f || !g || !t || !tape || !work) return MPASG_E_ARG;
-  if (!adj_supported(m, c) || c->precision != MPASG_PRECISION_FLOAT64) return MPASG_E_ARG;
-  if (c->time_integration_order != 2 && c->time_integration_order != 3) return MPASG_E_ARG;
-  if (c->number_of_sub_steps < 1 || c->dynamics_split_steps < 1) return MPASG_E_ARG;
-  return step_vjp_impl(m, c, f, g, t, tape, work, (cudaStream_t)stream);
+  if (!m || !c || !f || !g || !t || !tape || !work || !step_args_ok(m, c)) return MPASG_E_ARG;
+  const int rc = mpasg_step_tape(m, c, f, tape, stream);
+  if (rc != MPASG_OK) return rc;
+  return mpasg_step_vjp_taped(m, c, f, g, t, tape, work, stream);
 }

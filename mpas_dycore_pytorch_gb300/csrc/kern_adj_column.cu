@@ -179,37 +179,100 @@ __global__ void k_ac_vjp_post(mpasg_mesh m, mpasg_fields f, mpasg_fields g, Fast
   rho_ib[ow] = rib;
 }
 
-// Thomas sweeps (autodiff/tridiagonal_solve.py:232-291) transposed, one thread per column:
-// g.ac_x holds the solution's cotangent on entry and the right-hand side's on return; a,
-// alpha and gamma cotangents accumulate.  x is the solution, rhs the right-hand side; the
-// forward-elimination values come back from the solution (u_k = x_k + gamma_k x_(k+1)).
-__global__ void k_ac_vjp_solve(mpasg_mesh m, mpasg_fields f, mpasg_fields g, const double* __restrict__ rhs) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m.nCells) return;
-  const int L = m.nVertLevels;
-  const size_t o = (size_t)c * L, ow = (size_t)c * (L + 1);
-  const double* x = f.ac_x + ow;
-  double* a = g.ac_x + ow;
+// Thomas sweeps (autodiff/tridiagonal_solve.py:232-291) transposed for one column: xb
+// holds the solution's cotangent on entry and the right-hand side's on return; the a, alpha
+// and gamma cotangents accumulate into ga / gal / gg.  The forward-elimination values come
+// back from the solution: u_k = x_k + gamma_k x_(k+1) and t_k = rhs_k - a_k u_(k-1) = u_k / alpha_k.
+// Strides: xs / xbs for the (L+1)-level arrays, cs for the L-level ones.
+MPASG_D void solve_vjp_column(int L, const double* x, int xs, double* xb, int xbs, const double* a,
+                              const double* al, const double* gam, int cs, double* ga, double* gal, double* gg) {
   double prev = 0.0;
   for (int k = 0; k <= L; ++k) {
-    const double au = a[k] - (k > 0 ? f.gamma_tri[o + k - 1] * prev : 0.0);
-    if (k < L) g.gamma_tri[o + k] += -au * x[k + 1];
-    a[k] = au;
+    const double au = xb[k * xbs] - (k > 0 ? gam[(k - 1) * cs] * prev : 0.0);
+    if (k < L) gg[k * cs] += -au * x[(k + 1) * xs];
+    xb[k * xbs] = au;
     prev = au;
   }
   double carry = 0.0;
   for (int k = L - 1; k >= 1; --k) {
-    const double au = a[k] + carry;
-    const double u_km1 = x[k - 1] + f.gamma_tri[o + k - 1] * x[k];
-    const double t = rhs[ow + k] - f.a_tri[o + k] * u_km1;
-    g.alpha_tri[o + k] += au * t;
-    const double at = au * f.alpha_tri[o + k];
-    a[k] = at;
-    g.a_tri[o + k] += -at * u_km1;
-    carry = -at * f.a_tri[o + k];
+    const double au = xb[k * xbs] + carry;
+    const double u_k = x[k * xs] + gam[k * cs] * x[(k + 1) * xs];
+    const double u_km1 = x[(k - 1) * xs] + gam[(k - 1) * cs] * x[k * xs];
+    gal[k * cs] += au * (u_k / al[k * cs]);
+    const double at = au * al[k * cs];
+    xb[k * xbs] = at;
+    ga[k * cs] += -at * u_km1;
+    carry = -at * a[k * cs];
   }
-  a[0] += carry;
+  xb[0] += carry;
 }
+
+// one thread per column, straight from global memory (fallback when the staged kernel's
+// shared memory does not fit)
+__global__ void k_ac_vjp_solve(mpasg_mesh m, mpasg_fields f, mpasg_fields g) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.nCells) return;
+  const int L = m.nVertLevels;
+  const size_t o = (size_t)c * L, ow = (size_t)c * (L + 1);
+  solve_vjp_column(L, f.ac_x + ow, 1, g.ac_x + ow, 1, f.a_tri + o, f.alpha_tri + o, f.gamma_tri + o, 1,
+                   g.a_tri + o, g.alpha_tri + o, g.gamma_tri + o);
+}
+
+// The same with 32 columns staged through shared memory ([level][33] layout, coalesced
+// copies by 4 warps, the sweeps on the first warp), as the forward Thomas kernels do.
+constexpr int kSolveCols = 32;
+constexpr int kSolvePitch = kSolveCols + 1;
+constexpr int kSolveThreads = 128;
+
+__global__ void __launch_bounds__(kSolveThreads) k_ac_vjp_solve_staged(mpasg_mesh m, mpasg_fields f, mpasg_fields g,
+                                                                       FastDiv fl, FastDiv fl1) {
+  extern __shared__ double sm[];
+  const int L = m.nVertLevels;
+  double* sx = sm;                                   // (L+1) x pitch
+  double* sb = sx + (size_t)(L + 1) * kSolvePitch;   // (L+1) x pitch
+  double* sa = sb + (size_t)(L + 1) * kSolvePitch;   // L x pitch each below
+  double* sal = sa + (size_t)L * kSolvePitch;
+  double* sg = sal + (size_t)L * kSolvePitch;
+  double* sga = sg + (size_t)L * kSolvePitch;
+  double* sgal = sga + (size_t)L * kSolvePitch;
+  double* sgg = sgal + (size_t)L * kSolvePitch;
+  const int c0 = blockIdx.x * kSolveCols;
+  const int ncol = min(kSolveCols, m.nCells - c0);
+  const int t = threadIdx.x;
+  const uint32_t nw = (uint32_t)ncol * (L + 1), nl = (uint32_t)ncol * L;
+  const size_t ow0 = (size_t)c0 * (L + 1), o0 = (size_t)c0 * L;
+  for (uint32_t idx = t; idx < nw; idx += kSolveThreads) {
+    const uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
+    sx[k * kSolvePitch + col] = f.ac_x[ow0 + idx];
+    sb[k * kSolvePitch + col] = g.ac_x[ow0 + idx];
+  }
+  for (uint32_t idx = t; idx < nl; idx += kSolveThreads) {
+    const uint32_t col = fl.div(idx), k = idx - col * L;
+    sa[k * kSolvePitch + col] = f.a_tri[o0 + idx];
+    sal[k * kSolvePitch + col] = f.alpha_tri[o0 + idx];
+    sg[k * kSolvePitch + col] = f.gamma_tri[o0 + idx];
+    sga[k * kSolvePitch + col] = 0.0;
+    sgal[k * kSolvePitch + col] = 0.0;
+    sgg[k * kSolvePitch + col] = 0.0;
+  }
+  __syncthreads();
+  if (t < ncol)
+    solve_vjp_column(L, sx + t, kSolvePitch, sb + t, kSolvePitch, sa + t, sal + t, sg + t, kSolvePitch, sga + t,
+                     sgal + t, sgg + t);
+  __syncthreads();
+  for (uint32_t idx = t; idx < nw; idx += kSolveThreads) {
+    const uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
+    g.ac_x[ow0 + idx] = sb[k * kSolvePitch + col];
+  }
+  for (uint32_t idx = t; idx < nl; idx += kSolveThreads) {
+    const uint32_t col = fl.div(idx), k = idx - col * L;
+    g.a_tri[o0 + idx] += sga[k * kSolvePitch + col];
+    g.alpha_tri[o0 + idx] += sgal[k * kSolvePitch + col];
+    g.gamma_tri[o0 + idx] += sgg[k * kSolvePitch + col];
+  }
+}
+
+size_t solve_vjp_smem_bytes(int L) { return (size_t)(2 * (L + 1) + 6 * L) * kSolvePitch * sizeof(double); }
 
 // The tridiagonal right-hand side (acoustic_step.py:675) and rs / ts read backwards, per
 // mass level: -> tend_theta, tend_rho, cofwz, cofwt, the rs / ts cotangents (rsb, tsb), the
@@ -509,8 +572,7 @@ int mpasgi_zero(double* p, long long n, cudaStream_t s) { return zero(p, n, s); 
 
 // ================================================================= internal cores
 // The acoustic substep's forward pass for its reverse mode: keeps the substep's inputs
-// (rho_pp, rtheta_pp, rw_p) and the tridiagonal right-hand side in the work buffer, then
-// leaves f as the forward substep does (ru_p, rho_pp, rtheta_pp, rtheta_pp_old, rw_p
+// (rho_pp, rtheta_pp, rw_p) in the work buffer, then leaves f as the forward substep does (ru_p, rho_pp, rtheta_pp, rtheta_pp_old, rw_p
 // updated; ac_rs / ac_ts / ac_x hold rs, ts and the undamped solution).
 int mpasgi_acoustic_vjp_fwd(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, int small_step, double dts,
                             const AdjWork& w, cudaStream_t s) {
@@ -520,22 +582,17 @@ int mpasgi_acoustic_vjp_fwd(const mpasg_mesh* m, const mpasg_config* c, mpasg_fi
   CHECK_RC(dcopy(w.c[0], f->rho_pp, ncl, s));
   CHECK_RC(dcopy(w.c[1], f->rtheta_pp, ncl, s));
   CHECK_RC(dcopy(w.c[2], f->rw_p, ncw, s));
-  CHECK_RC(mpasgi_acoustic_parts(m, c, f, small_step, dts, s, 0));
-  CHECK_RC(dcopy(w.c[3], f->ac_x, ncw, s));
-  return mpasgi_acoustic_parts(m, c, f, small_step, dts, s, 1);
+  return mpasgi_acoustic_parts(m, c, f, small_step, dts, s, -1);
 }
 
 // The reverse pass proper (after mpasgi_acoustic_vjp_fwd on the same f and work).
 int mpasgi_acoustic_vjp_rev(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, mpasg_fields* g,
-                            const mpasg_transpose* t, int small_step, double dts, const AdjWork& w,
-                            cudaStream_t s) {
+                            const mpasg_transpose* t, int small_step, double dts, const double* rt_in,
+                            const double* rwp_in, const AdjWork& w, cudaStream_t s) {
   const int L = m->nVertLevels;
   const long long ncl = (long long)m->nCells * L, nel = (long long)m->nEdges * L;
   const long long ncw = (long long)m->nCells * (L + 1);
   const bool first = small_step == 1;
-  double* rt_in = w.c[1];
-  double* rwp_in = w.c[2];
-  double* rhs = w.c[3];
   double* rho_ib = w.c[4];
   double* rsb = w.c[5];
   double* tsb = w.c[6];
@@ -545,7 +602,19 @@ int mpasgi_acoustic_vjp_rev(const mpasg_mesh* m, const mpasg_config* c, mpasg_fi
   FastDiv fl(L), fl1(L + 1);
   k_ac_vjp_post<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, *g, fl1, dts, rho_ib);
   MPASG_LAUNCH_CHECK();
-  k_ac_vjp_solve<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f, *g, rhs);
+  // the staged solve needs more than 48 KB of dynamic shared memory: opt in once per device
+  // (the first call on a device should come before any stream capture)
+  const size_t smem = solve_vjp_smem_bytes(L);
+  static bool opt_in[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MPASG_E_CUDA;
+  if (!opt_in[dev])
+    opt_in[dev] = cudaFuncSetAttribute(k_ac_vjp_solve_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       200 * 1024) == cudaSuccess;
+  if (opt_in[dev] && smem <= 200 * 1024)
+    k_ac_vjp_solve_staged<<<nblocks(m->nCells, kSolveCols), kSolveThreads, smem, s>>>(*m, *f, *g, fl, fl1);
+  else
+    k_ac_vjp_solve<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f, *g);
   MPASG_LAUNCH_CHECK();
   k_ac_vjp_cells<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, *g, fl, first ? 1 : 0, dts, resm, rt_in, rho_ib, rsb, tsb);
   MPASG_LAUNCH_CHECK();
@@ -565,7 +634,7 @@ int mpasgi_acoustic_vjp_core(const mpasg_mesh* m, const mpasg_config* c, mpasg_f
                              const mpasg_transpose* t, int small_step, double dts, const AdjWork& w,
                              cudaStream_t s) {
   CHECK_RC(mpasgi_acoustic_vjp_fwd(m, c, f, small_step, dts, w, s));
-  return mpasgi_acoustic_vjp_rev(m, c, f, g, t, small_step, dts, w, s);
+  return mpasgi_acoustic_vjp_rev(m, c, f, g, t, small_step, dts, w.c[1], w.c[2], w, s);
 }
 
 int mpasgi_divdamp_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,

@@ -379,9 +379,9 @@ __global__ void k_tadj_adv_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields g, m
 
 // ---- edges: the u tendency read backwards (vertical transport, PV flux, kinetic-energy
 // gradient, divergence coupling; at rk 1 the pressure gradient and del2 / del4 mixing)
-__global__ void k_tadj_u(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl, AdjTendScalars p,
-                         const double* __restrict__ hd, const double* __restrict__ kd, const double* __restrict__ ud,
-                         const double* __restrict__ dsd, const double* __restrict__ dsv, double* __restrict__ qb_out,
+__global__ void k_tadj_u(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpasg_transpose t, FastDiv fl,
+                         AdjTendScalars p, const double* __restrict__ hd, const double* __restrict__ kd,
+                         const double* __restrict__ ud, const double* __restrict__ dsd, const double* __restrict__ dsv,
                          double* __restrict__ pke, double* __restrict__ phd, double* __restrict__ prwe,
                          double* __restrict__ ppp, double* __restrict__ pkd, double* __restrict__ udb,
                          double* __restrict__ pd4) {
@@ -397,20 +397,32 @@ __global__ void k_tadj_u(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv f
   const double G = Gtu[k];
   const double rho_e = f.h_edge[i];
   const double inv_dc = m.invDcEdge[e];
-  // PV flux
+  // PV flux q_e = 0.5 sum_j w_j u_j (pv_e + pv_j), with its transpose over edgesOnEdge: the
+  // neighbour eo's sum reads u_e and pv_e at its slot jt (cotangent of q_eo: G_eo rho_edge_eo)
   const int n2 = m.nEdgesOnEdge[e], me2 = m.maxEdges2;
-  const double pv_self = f.pv_edge[i];
-  double q = 0.0;
+  const double pv_self = f.pv_edge[i], u_self = ue[k];
+  const double qbe = G * rho_e;
+  double q = 0.0, gpv = 0.0, gu_pv = 0.0;
   for (int j = 0; j < n2; ++j) {
     const int eo = m.edgesOnEdge[e * me2 + j];
-    const double tq = (m.weightsOnEdge[e * me2 + j] * f.u[(size_t)eo * L + k]) * (pv_self + f.pv_edge[(size_t)eo * L + k]);
+    const size_t io = (size_t)eo * L + k;
+    const double w_j = m.weightsOnEdge[e * me2 + j];
+    const double u_o = f.u[io], pv_o = f.pv_edge[io];
+    const double tq = (w_j * u_o) * (pv_self + pv_o);
     q = (j == 0) ? tq : q + tq;
+    gpv += qbe * w_j * u_o * 0.5;
+    const int jt = t.eoeTransSlot[e * me2 + j];
+    if (jt < 0) continue;
+    const double wt = m.weightsOnEdge[(size_t)eo * me2 + jt];
+    const double qbo = g.tend_u[io] * f.h_edge[io];
+    gu_pv += qbo * wt * 0.5 * (pv_o + pv_self);
+    gpv += qbo * wt * u_self * 0.5;
   }
   q = 0.5 * q;
   double gh = G * (q - (f.ke[i2] - f.ke[i1]) * inv_dc);
-  qb_out[i] = G * rho_e;
   pke[i] = G * rho_e * inv_dc;
-  double gu = -G * 0.5 * (hd[i1] + hd[i2]);
+  double gu = -G * 0.5 * (hd[i1] + hd[i2]) + gu_pv;
+  g.pv_edge[i] += gpv;
   phd[i] = -G * ue[k] * 0.5;
   // vertical transport: tu_k = -rdzw_k (wduz_(k+1) - wduz_k)
   auto wduzb = [&](int qq) {
@@ -603,34 +615,6 @@ __global__ void k_tadj_vort(mpasg_mesh m, mpasg_fields g, FastDiv fl, const doub
     a += vertex_side(m, e, (int)v) ? -b : b;
   }
   g.vorticity[i] += a;
-}
-
-// ---- edges: the PV flux q = 0.5 sum_j w_j u_j (pv_e + pv_j) transposed over edgesOnEdge
-__global__ void k_tadj_pv(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpasg_transpose t, FastDiv fl,
-                          const double* __restrict__ qb) {
-  const int L = m.nVertLevels;
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint32_t)m.nEdges * L) return;
-  const uint32_t e = fl.div(i);
-  const int k = (int)(i - e * L);
-  const int n2 = m.nEdgesOnEdge[e], me2 = m.maxEdges2;
-  const double pv = f.pv_edge[i], u = f.u[i], qbe = qb[i];
-  double gu = 0.0, gpv = 0.0;
-  for (int j = 0; j < n2; ++j) {
-    const int eo = m.edgesOnEdge[e * me2 + j];
-    const size_t io = (size_t)eo * L + k;
-    // own sum: d q_e / d pv_e
-    gpv += qbe * m.weightsOnEdge[e * me2 + j] * f.u[io] * 0.5;
-    // neighbour eo's sum reads u_e and pv_e at its slot jt
-    const int jt = t.eoeTransSlot[e * me2 + j];
-    if (jt < 0) continue;
-    const double wt = m.weightsOnEdge[(size_t)eo * me2 + jt];
-    const double qbo = qb[io];
-    gu += qbo * wt * 0.5 * (f.pv_edge[io] + pv);
-    gpv += qbo * wt * u * 0.5;
-  }
-  g.u[i] += gu;
-  g.pv_edge[i] += gpv;
 }
 
 // ---- rk 1 mixing: edges, the del4 parts' cotangents of delsq_theta / delsq_w per edge
@@ -912,7 +896,6 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   // edges
   double* fltb = w.e[0];
   double* flwb = w.e[1];
-  double* qb = w.e[2];
   double* pke = w.e[3];
   double* phd = w.e[4];
   double* prwe = w.e[5];
@@ -952,12 +935,10 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   MPASG_LAUNCH_CHECK();
   k_tadj_adv_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, *g, *t, fl1, fltb, flwb);
   MPASG_LAUNCH_CHECK();
-  k_tadj_u<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, fl, p, hd, kd, ud, dsd, dsv, qb, pke, phd, prwe, ppp, pkd, udb,
-                                          pd4);
+  k_tadj_u<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, p, hd, kd, ud, dsd, dsv, pke, phd, prwe, ppp, pkd,
+                                          udb, pd4);
   MPASG_LAUNCH_CHECK();
   k_tadj_u_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *g, fl1, p, pke, phd, prwe, ppp, pkd, pd4, hdb, kdb, dsdb);
-  MPASG_LAUNCH_CHECK();
-  k_tadj_pv<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, qb);
   MPASG_LAUNCH_CHECK();
   if (rk_step == 1) {
     if (p.del4) {

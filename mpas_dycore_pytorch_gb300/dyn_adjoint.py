@@ -177,6 +177,8 @@ class DynamicsAdjoint:
         n = int(self.lib.mpasg_dyn_vjp_work_doubles(C.byref(dm.struct)))
         self.work = torch.zeros(n, dtype=torch.float64, device=dev)
         self.tape: torch.Tensor | None = None
+        self._graph = None
+        self._warm = False
 
     # -- checkpoints of the step boundary -------------------------------------------
     def checkpoint(self) -> dict[str, torch.Tensor]:
@@ -199,14 +201,58 @@ class DynamicsAdjoint:
         return self.tape
 
     # -- one step / preparation -----------------------------------------------------
+    def _call_step_vjp(self, stream: C.c_void_p) -> int:
+        m = self.model
+        mp, cp, fp, gp = C.byref(m.dmesh.struct), C.byref(m.cstruct), C.byref(m.state.struct), C.byref(self.g.struct)
+        tape = _p(self._tape())
+        rc = self.lib.mpasg_step_tape(mp, cp, fp, tape, stream)
+        if rc != 0:
+            return rc
+        return self.lib.mpasg_step_vjp_taped(mp, cp, fp, gp, C.byref(self.t), tape, _p(self.work), stream)
+
     def step_vjp(self) -> None:
         """Cotangents in g of the state after one step (from the state in the model) ->
-        cotangents of the step's start state; the model's state ends one step later."""
+        cotangents of the step's start state; the model's state ends one step later.  The
+        first call runs eagerly (it also makes the kernels' one-time per-device settings);
+        the second captures the step's tape and reverse pass as one CUDA graph, replayed by
+        every later call (same buffers, so the graph stays valid)."""
+        if self._graph is not None:
+            self._graph.replay()
+            return
+        if not self._warm:
+            _lib.check(self._call_step_vjp(_stream()), "mpasg_step_vjp")
+            self._warm = True
+            return
+        torch.cuda.synchronize()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                rc = self._call_step_vjp(C.c_void_p(s.cuda_stream))
+        _lib.check(rc, "mpasg_step_vjp (capture)")
+        torch.cuda.current_stream().wait_stream(s)
+        self._graph = g
+        g.replay()
+
+    def step_tape(self, tape: torch.Tensor) -> None:
+        """One step of the model with its tape written to ``tape`` (no transport)."""
         m = self.model
-        rc = self.lib.mpasg_step_vjp(C.byref(m.dmesh.struct), C.byref(m.cstruct), C.byref(m.state.struct),
-                                     C.byref(self.g.struct), C.byref(self.t), _p(self._tape()), _p(self.work),
-                                     _stream())
-        _lib.check(rc, "mpasg_step_vjp")
+        rc = self.lib.mpasg_step_tape(C.byref(m.dmesh.struct), C.byref(m.cstruct), C.byref(m.state.struct),
+                                      _p(tape), _stream())
+        _lib.check(rc, "mpasg_step_tape")
+
+    def step_vjp_taped(self, tape: torch.Tensor) -> None:
+        """The reverse pass of one step from its tape."""
+        m = self.model
+        rc = self.lib.mpasg_step_vjp_taped(C.byref(m.dmesh.struct), C.byref(m.cstruct), C.byref(m.state.struct),
+                                           C.byref(self.g.struct), C.byref(self.t), _p(tape), _p(self.work),
+                                           _stream())
+        _lib.check(rc, "mpasg_step_vjp_taped")
+
+    def tape_doubles(self) -> int:
+        return int(self.lib.mpasg_step_vjp_tape_doubles(C.byref(self.model.dmesh.struct),
+                                                        C.byref(self.model.cstruct)))
 
     def prepare_vjp(self, w_in: torch.Tensor) -> dict[str, torch.Tensor]:
         """Cotangents in g of the prepared state (the model holds it) -> cotangents of the
@@ -224,25 +270,52 @@ class DynamicsAdjoint:
 
 def run_vjp(model, loaded: Mapping[str, Any], nsteps: int,
             cotangents: Callable[[dict], Mapping[str, torch.Tensor]],
-            adj: DynamicsAdjoint | None = None) -> tuple[dict, dict]:
-    """Forward from the loaded primitives through ``nsteps`` large steps with a checkpoint
-    per step, then the reverse sweep.  ``cotangents(out)`` receives the final state (the
-    model's export) and returns cotangents of some of its carried fields.  Returns the
-    cotangents of the loaded u, w, theta, rho and the final state."""
+            adj: DynamicsAdjoint | None = None, checkpoint: str = "step") -> tuple[dict, dict]:
+    """Forward from the loaded primitives through ``nsteps`` large steps, then the reverse
+    sweep.  ``cotangents(out)`` receives the final state (the model's export) and returns
+    cotangents of some of its carried fields.  Returns the cotangents of the loaded u, w,
+    theta, rho and the final state.
+
+    ``checkpoint="step"`` (the reference's default, checkpoint_timesteps on): one checkpoint
+    of the step boundary per step in HBM; the reverse pass of each step first recomputes it
+    with its tape.  ``checkpoint="none"`` (checkpoint_timesteps=False): every step's tape is
+    kept from the forward pass (about ``tape_doubles() * 8 * nsteps`` bytes), nothing is
+    recomputed; the forward then advances the dynamics only, so the final state's scalars
+    and reconstructed winds are not part of it."""
+    if checkpoint not in ("step", "none"):
+        raise MpasConfigError(f"checkpoint must be 'step' or 'none', got {checkpoint!r}")
     adj = adj or DynamicsAdjoint(model)
     model.prepare(loaded)
-    dev = model.dmesh.device
     w_in = model.state.f["w"].clone()
-    ckpts = [adj.checkpoint()]
-    for n in range(int(nsteps)):
-        model.step()
-        if n + 1 < nsteps:
-            ckpts.append(adj.checkpoint())
+    ck0 = adj.checkpoint()
+    tapes: list[torch.Tensor] = []
+    ckpts = [ck0]
+    if checkpoint == "step":
+        for n in range(int(nsteps)):
+            model.step()
+            if n == 0 and nsteps > 1 and model._graph is None:
+                model.capture_graph()  # later steps replay the step graph (bitwise the eager step)
+            if n + 1 < nsteps:
+                ckpts.append(adj.checkpoint())
+    else:
+        nd = adj.tape_doubles()
+        free, _ = torch.cuda.mem_get_info(model.dmesh.device)
+        if nd * 8 * int(nsteps) > 0.9 * free:
+            raise MpasConfigError(f"checkpoint='none' needs {nd * 8 * nsteps / 1e9:.1f} GB of tapes; "
+                                  f"{free / 1e9:.1f} GB are free (use checkpoint='step')")
+        for n in range(int(nsteps)):
+            tapes.append(torch.empty(nd, dtype=torch.float64, device=model.dmesh.device))
+            adj.step_tape(tapes[-1])
     bad = model.check_finite()
     if bad:
         raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")
     final = model.export()
+    if checkpoint == "none":
+        for k in ("scalars", "uReconstructX", "uReconstructY", "uReconstructZ", "uReconstructZonal",
+                  "uReconstructMeridional", "ur_cell", "vr_cell"):
+            final.pop(k, None)
     adj.zero_cotangents()
+    dev = model.dmesh.device
     g = cotangents(final)
     for k, v in g.items():
         name = "h_edge" if k == "rho_edge" else k
@@ -251,8 +324,12 @@ def run_vjp(model, loaded: Mapping[str, Any], nsteps: int,
         dst = adj.g.f[name]
         dst[: v.shape[0]].add_(v.to(device=dev, dtype=torch.float64))
     for n in range(int(nsteps) - 1, -1, -1):
-        adj.restore(ckpts[n])
-        adj.step_vjp()
-    adj.restore(ckpts[0])
+        if checkpoint == "step":
+            adj.restore(ckpts[n])
+            adj.step_vjp()
+        else:
+            adj.step_vjp_taped(tapes[n])
+            tapes[n] = None  # free as the sweep goes
+    adj.restore(ck0)
     grads = adj.prepare_vjp(w_in)
     return grads, final
