@@ -18,6 +18,8 @@
  *   mpasg_step                  dynamics/time_integration.py:4897  atm_srk3 (+ :3420 _atm_srk3_impl)
  *   mpasg_prepare               atmosphere_model.py:782  _prepare_timestep_state
  *                               (dynamics/init_coupled_diagnostics.py:147)
+ *   mpasg_prepare_derived       the same from theta_m / rho_zz (init_coupled_diagnostics.py:259)
+ *   mpasg_digest                state.py:72,85 (value binding of a complete step boundary)
  *   mpasg_moist_coefficients    dynamics/moist_coefficients.py:124
  *   mpasg_vert_imp_coefs        dynamics/vert_imp_coefs.py:188
  *   mpasg_dyn_tend              dynamics/dyn_tend.py:10836  atm_compute_dyn_tend_work
@@ -258,6 +260,11 @@ enum {
  * null for dry), then diagnostics and cell-wind reconstruction. */
 int mpasg_prepare(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
                   const double *theta, const double *rho, const double *qv, void *stream);
+/* The same preparation from theta_m and rho_zz themselves (init_coupled_diagnostics.py:259:
+ * the rederivation of a step boundary whose prognostics were edited); the inputs may be
+ * f->theta_m and f->rho_zz. */
+int mpasg_prepare_derived(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f,
+                          const double *theta_m, const double *rho_zz, void *stream);
 /* One large step (atm_srk3), in place on f. */
 int mpasg_step(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, void *stream);
 /* The same step, recording events[i] (cudaEvent_t, timing enabled) at every stage
@@ -517,6 +524,15 @@ int mpasg_step_vjp_taped(const mpasg_mesh *m, const mpasg_config *c, const mpasg
 int mpasg_prepare_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *g,
                       const mpasg_transpose *t, const double *w_in, double *g_u, double *g_w,
                       double *g_theta, double *g_rho, double *work, void *stream);
+
+/* ---- boundary binding ----------------------------------------------------------- */
+/* 128-bit value digest of nbytes bytes at p (device memory, 8-byte aligned) into out[0..1]
+ * (device memory): the lanes A = sum h_i and B = sum mix(h_i ^ 0x5851f42d4c957f2d) modulo
+ * 2^64 over the little-endian 8-byte words w_i (last word zero-padded), h_i = mix(w_i ^
+ * mix(i + 0x9e3779b97f4a7c15)), mix = the SplitMix64 output function.  Independent of the
+ * summation order.  Binds a returned step boundary to its values (the reference keeps the
+ * bytes themselves, state.py:72-141 mark_complete_step_boundary). */
+int mpasg_digest(const void *p, long long nbytes, unsigned long long *out, void *stream);
 
 /* ---- mesh reordering (host functions; no GPU needed) -------------------------------- */
 /* new_to_old[i] = the old index of the i-th point along the 3-D Hilbert curve through

@@ -151,7 +151,8 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_surface_pressure_vjp", "mpasg_surface_pressure_jvp", "mpasg_weighted_sq_sum_vjp",
            "mpasg_dyn_vjp_work_doubles", "mpasg_step_vjp_tape_doubles", "mpasg_vimp_vjp", "mpasg_dyn_tend_vjp",
            "mpasg_smlstep_vjp", "mpasg_acoustic_vjp", "mpasg_divdamp_vjp", "mpasg_recover_vjp", "mpasg_diag_vjp",
-           "mpasg_step_vjp", "mpasg_prepare_vjp", "mpasg_step_tape", "mpasg_step_vjp_taped")
+           "mpasg_step_vjp", "mpasg_prepare_vjp", "mpasg_step_tape", "mpasg_step_vjp_taped",
+           "mpasg_prepare_derived", "mpasg_digest")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
 STATIC_SCRATCH_DOUBLES = 1 << 22
@@ -179,6 +180,8 @@ def load() -> C.CDLL:
         "mpasg_launch_count": ([], C.c_longlong),
         "mpasg_step_timed": ([m, c, f, vp, vp, C.c_int, vp], C.c_int),
         "mpasg_prepare": ([m, c, f, vp, vp, vp, vp], C.c_int),
+        "mpasg_prepare_derived": ([m, c, f, vp, vp, vp], C.c_int),
+        "mpasg_digest": ([vp, C.c_longlong, vp, vp], C.c_int),
         "mpasg_step": ([m, c, f, vp], C.c_int),
         "mpasg_check_finite": ([m, c, f, vp], C.c_int),
         "mpasg_moist_coefficients": ([m, c, f, vp], C.c_int),

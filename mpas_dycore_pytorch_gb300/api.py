@@ -20,6 +20,8 @@ import torch
 
 from . import _lib
 from .device import DeviceMesh, DeviceState, STATE_KEYS, _int, _np
+from .boundary import (MARKER, has_complete_step_boundary, mark_complete_step_boundary,
+                       require_boundary_continuation_identity, require_unedited_boundary_support)
 from .errors import MpasConfigError, MpasDeviceError, MpasNumericalError, MpasUnsupportedCapabilityError
 
 DEFAULTS = {
@@ -310,6 +312,15 @@ class Model:
         self.state.load(state, keys=STATE_KEYS + ("rho_edge",), rows=self._rows_in, pending=self._pending_d2h)
         self.state.f["rho_zz"][self.dmesh.nCells].fill_(1.0)
 
+    def prepare_derived(self, state: Mapping[str, Any]) -> None:
+        """Load a step boundary and re-derive its coupled diagnostics, solve diagnostics and
+        cell winds from its prognostics u, w, theta_m, rho_zz (the reference's treatment of a
+        boundary whose prognostics were edited, init_coupled_diagnostics.py:259)."""
+        self.load_boundary(state)
+        f = self.state.f
+        self.call("mpasg_prepare_derived", C.c_void_p(f["theta_m"].data_ptr()), C.c_void_p(f["rho_zz"].data_ptr()))
+        torch.cuda.current_stream().synchronize()
+
     def export_to(self, host: Mapping[str, torch.Tensor]) -> None:
         """Copy the step boundary (caller's order) into the caller's host tensors, one
         field after another on a copy stream of its own.  The copies run while the
@@ -530,8 +541,34 @@ def _is_prepared(state: Mapping[str, Any]) -> bool:
 
 def _merge(base: Mapping[str, Any], out: Mapping[str, torch.Tensor]) -> dict:
     res = dict(base)
+    res.pop(MARKER, None)
     res.update(out)
     return res
+
+
+def _start(model: "Model", state: Mapping[str, Any], merged: Mapping[str, Any], complete: bool) -> None:
+    """Bring the model to the start boundary as the reference's _prepare_timestep_state
+    does (atmosphere_model.py:782-898): a complete bound boundary continues as it is; any
+    other state is prepared, from theta_m and rho_zz where it has both (a boundary whose
+    prognostics were edited), else from the loaded theta, rho and qv."""
+    if complete:
+        model.load_boundary(state)
+    elif "theta_m" in merged and "rho_zz" in merged and _is_prepared(state):
+        model.prepare_derived(state)
+    else:
+        model.prepare(merged)
+
+
+def _check_boundary(state: Mapping[str, Any], mesh: Mapping[str, Any] | None, cfg: Mapping[str, Any],
+                    dt: float) -> bool:
+    """The continuation checks of a start state (atmosphere_model.py:829-838): a marked
+    state continues only with its own mesh, configuration and time step, and only its
+    prognostics may have been edited.  Returns whether it is a complete boundary."""
+    require_boundary_continuation_identity(state, mesh=mesh, config=cfg, dt=dt)
+    complete = has_complete_step_boundary(state)
+    if not complete:
+        require_unedited_boundary_support(state)
+    return complete
 
 
 def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | None = None,
@@ -550,6 +587,14 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
     hand-written adjoint of the scalar transport into autograd (passive scalars, explicit
     split transport); other inputs requiring grad are rejected before any device work.
     """
+    return _simulate(initial_state, mesh, config, dt, nsteps, device, on_step, differentiable, on_phase, on_initial,
+                     use_cuda_graph, bound=True)
+
+
+def _simulate(initial_state, mesh, config, dt, nsteps, device, on_step, differentiable, on_phase, on_initial,
+              use_cuda_graph, bound: bool) -> dict:
+    """run_simulation's body; ``bound`` False (atm_srk3) continues from the given prepared
+    state as it is and returns an unbound result."""
     reject_unsupported_request(initial_state, mesh, config)
     require_finite_inputs(initial_state)
     if int(nsteps) != nsteps or nsteps < 0:
@@ -557,6 +602,8 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
     if differentiable and _grad_keys(initial_state, mesh) and nsteps > 0:
         return _run_differentiable(initial_state, mesh, config, dt, int(nsteps), device, on_step, on_phase,
                                    on_initial)
+    # a boundary is bound to the mesh the caller passed (none when the state is its own mesh)
+    boundary_mesh = dict(mesh) if mesh is not None else None
     mesh = mesh if mesh is not None else initial_state
     merged = dict(mesh)
     merged.update(initial_state)
@@ -576,12 +623,10 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
             mesh = new_mesh
         merged = dict(mesh)
         merged.update(initial_state)
+    complete = _check_boundary(initial_state, boundary_mesh, cfg, dt) if bound else True
     ns = _int(merged.get("num_scalars", _np(merged["scalars"]).shape[-1]))
     model = Model(merged, cfg, dt, num_scalars=ns, device=device)
-    if _is_prepared(initial_state):
-        model.load_boundary(initial_state)
-    else:
-        model.prepare(merged)
+    _start(model, initial_state, merged, complete)
     if on_initial is not None:
         on_initial(_merge(initial_state, model.export()))
     if on_phase is not None:
@@ -603,7 +648,11 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
     bad = model.check_finite()
     if bad:
         raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")
-    return _merge(initial_state, model.export())
+    out = _merge(initial_state, model.export())
+    if bound:
+        # the returned boundary continues a later call as it is (atmosphere_model.py:2024-2032)
+        mark_complete_step_boundary(out, mesh=boundary_mesh, config=cfg, dt=dt)
+    return out
 
 
 def _scalar_derivative_forward(state: Mapping[str, Any], mesh: Mapping[str, Any] | None, kwargs: dict):
@@ -623,11 +672,9 @@ def _scalar_derivative_forward(state: Mapping[str, Any], mesh: Mapping[str, Any]
     # the Model's defaults: every scalar is a moist species unless moist_end says otherwise
     ms, me = _int(merged.get("moist_start", 1)), _int(merged.get("moist_end", ns))
     check_supported(cfg, ms, me)
+    complete = _check_boundary(state, None if mesh is state else mesh, cfg, dt)
     model = Model(merged, cfg, dt, num_scalars=ns, device=kwargs.get("device", "cuda"))
-    if _is_prepared(state):
-        model.load_boundary(state)
-    else:
-        model.prepare(merged)
+    _start(model, state, merged, complete)
     tape = ScalarTape(model)
     for i in range(nsteps):
         tape.step(model)
@@ -843,5 +890,4 @@ def atm_srk3(state: Mapping[str, Any], mesh: Mapping[str, Any], config: Mapping[
     """One split-explicit RK3 step on a prepared boundary (dynamics/time_integration.py:4897)."""
     if not _is_prepared(state):
         raise MpasConfigError("atm_srk3 needs a prepared step boundary")
-    return run_simulation(state, mesh, config, dt, 1, "cuda", differentiable=differentiable,
-                          use_cuda_graph=False)
+    return _simulate(state, mesh, config, dt, 1, "cuda", None, differentiable, None, None, False, bound=False)

@@ -292,15 +292,25 @@ __global__ void k_fill(double* p, int n, double v) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = v;
 }
 
-__global__ void k_prepare_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, const double* __restrict__ theta,
-                                const double* __restrict__ rho, const double* __restrict__ qv, double rcv) {
+// DERIVED: theta and rho hold theta_m and rho_zz themselves (the rederivation of a step
+// boundary whose prognostics were edited, init_coupled_diagnostics.py:259-261); they may
+// alias f.theta_m and f.rho_zz (each thread reads its element before writing it)
+template <bool DERIVED>
+__global__ void k_prepare_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, const double* theta,
+                                const double* rho, const double* __restrict__ qv, double rcv) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)m.nCells * L) return;
-  double q = qv ? qv[i] : 0.0;
   double zz = m.zz[i];
-  double theta_m = theta[i] * (1.0 + kRvord * q);
-  double rho_zz = rho[i] / zz;
+  double theta_m, rho_zz;
+  if (DERIVED) {
+    theta_m = theta[i];
+    rho_zz = rho[i];
+  } else {
+    double q = qv ? qv[i] : 0.0;
+    theta_m = theta[i] * (1.0 + kRvord * q);
+    rho_zz = rho[i] / zz;
+  }
   double rb = m.rho_base[i], tb = m.theta_base[i];
   double rho_p = rho_zz - rb;
   double rtb = tb * rb;
@@ -412,14 +422,16 @@ int mpasgi_reconstruct(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields*
   return MPASG_OK;
 }
 
-extern "C" int mpasg_prepare(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, const double* theta,
-                             const double* rho, const double* qv, void* stream) {
+namespace {
+template <bool DERIVED>
+int prepare(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, const double* theta, const double* rho,
+            const double* qv, void* stream) {
   if (!m || !c || !f || !theta || !rho) return MPASG_E_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const int L = m->nVertLevels;
   const double rcv = kRgas / (kCp - kRgas);
   FastDiv fl(L), fl1(L + 1);
-  k_prepare_cells<<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, fl, theta, rho, qv, rcv);
+  k_prepare_cells<DERIVED><<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, fl, theta, rho, qv, rcv);
   MPASG_LAUNCH_CHECK();
   // rho_zz padding row stamped to 1.0 (atmosphere_model.py:529-545)
   k_fill<<<1, 128, 0, s>>>(f->rho_zz + (size_t)m->nCells * L, L, 1.0);
@@ -433,6 +445,17 @@ extern "C" int mpasg_prepare(const mpasg_mesh* m, const mpasg_config* c, mpasg_f
   int rc = mpasg_solve_diagnostics(m, &c64, f, 3, stream);
   if (rc) return rc;
   return mpasg_reconstruct_2d(m, &c64, f, stream);
+}
+}  // namespace
+
+extern "C" int mpasg_prepare(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, const double* theta,
+                             const double* rho, const double* qv, void* stream) {
+  return prepare<false>(m, c, f, theta, rho, qv, stream);
+}
+
+extern "C" int mpasg_prepare_derived(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
+                                     const double* theta_m, const double* rho_zz, void* stream) {
+  return prepare<true>(m, c, f, theta_m, rho_zz, nullptr, stream);
 }
 
 extern "C" int mpasg_surface_pressure(int nCells, int rows, int nVertLevels, const double* rho_zz, const double* zz,

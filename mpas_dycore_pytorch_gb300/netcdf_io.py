@@ -415,11 +415,23 @@ def write_restart(state: Mapping[str, Any], mesh: Mapping[str, Any], path: str |
     missing = sorted(k for k in REGISTRY_FIELDS if k not in state and k not in mesh)
     if missing:
         raise MpasMissingFieldError(fields=tuple(missing), source="restart state")
-    complete = _is_complete_boundary(state)
+    snapshot = _is_complete_boundary(state)
     for k in CARRY_FIELDS:  # restart.py:183: a mid-RK3 savepoint is ambiguous
         v = state.get(k)
-        if isinstance(v, (torch.Tensor, np.ndarray)) and not complete and bool(np.any(_host(v) != 0)):
+        if isinstance(v, (torch.Tensor, np.ndarray)) and not snapshot and bool(np.any(_host(v) != 0)):
             raise MpasConfigError(f"write_restart cannot serialize mid-RK3 substep state: field {k!r} is non-zero.")
+    # only a boundary bound by run_simulation / run_timestep (or read from a complete
+    # restart) and unedited since is written as a complete boundary (restart.py:403-416)
+    from .boundary import MARKER, has_complete_step_boundary
+    complete = has_complete_step_boundary(state)
+    if MARKER in state and not complete:
+        raise MpasConfigError("write_restart cannot save an edited timestep boundary with stale diagnostics; "
+                              "advance it through run_timestep before saving the resulting complete boundary.")
+    if complete and not has_complete_step_boundary(state, mesh=mesh, config=config, dt=dt):
+        raise MpasConfigError("complete boundary continuation identity mismatch")
+    if complete and not snapshot:
+        missing = [k for k in SNAPSHOT_FIELDS + ("ruAvg", "wwAvg") if k not in state]
+        raise MpasMissingFieldError(fields=tuple(missing), source="complete restart boundary")
     try:
         timestep = float(dt if dt is not None else (config or {}).get("config_dt", 0.0))
     except (TypeError, ValueError) as exc:
@@ -635,8 +647,10 @@ def read_restart(path: str | os.PathLike, *, mesh: Mapping[str, Any] | None = No
     if complete:
         if a["boundary_prognostics_sha256"] != boundary_prognostics_digest(state, n):
             raise MpasConfigError("restart boundary prognostic digest mismatch")
-        state["_restart_boundary"] = {"mesh": a["mesh_sha256"], "config": a["continuation_configuration_sha256"],
-                                      "dt": timestep}
+        # bound to the file's own identity digests (restart.py:961-969)
+        from .boundary import MARKER, mark_complete_step_boundary
+        mark_complete_step_boundary(state)
+        state[MARKER].update(mesh=a["mesh_sha256"], config=a["continuation_configuration_sha256"], dt=timestep)
     return state, xtime
 
 
