@@ -75,13 +75,12 @@ def _finish(a: int, b: int, nbytes: int) -> str:
 
 
 def _device_lanes(t: torch.Tensor, out: torch.Tensor, slot: int) -> None:
-    from ._lib import lib
+    from ._lib import check, load
     if t.data_ptr() % 8:
         t = t.clone()
-    rc = lib().mpasg_digest(t.data_ptr(), t.numel() * t.element_size(), out[slot].data_ptr(),
-                            torch.cuda.current_stream(t.device).cuda_stream)
-    if rc != 0:
-        raise RuntimeError(f"mpasg_digest failed with status {rc}")
+    rc = load().mpasg_digest(t.data_ptr(), t.numel() * t.element_size(), out[slot].data_ptr(),
+                             torch.cuda.current_stream(t.device).cuda_stream)
+    check(rc, "mpasg_digest")
 
 
 def _snapshot(state: Mapping[str, Any], support_only: bool = False) -> dict[str, tuple]:

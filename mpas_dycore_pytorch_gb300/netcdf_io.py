@@ -427,7 +427,10 @@ def write_restart(state: Mapping[str, Any], mesh: Mapping[str, Any], path: str |
     if MARKER in state and not complete:
         raise MpasConfigError("write_restart cannot save an edited timestep boundary with stale diagnostics; "
                               "advance it through run_timestep before saving the resulting complete boundary.")
-    if complete and not has_complete_step_boundary(state, mesh=mesh, config=config, dt=dt):
+    # the binding holds the full configuration (defaults filled in) the boundary was run with
+    from .api import resolved_config
+    if complete and not has_complete_step_boundary(state, mesh=mesh, dt=dt,
+                                                   config=resolved_config(config) if config is not None else None):
         raise MpasConfigError("complete boundary continuation identity mismatch")
     if complete and not snapshot:
         missing = [k for k in SNAPSHOT_FIELDS + ("ruAvg", "wwAvg") if k not in state]
@@ -458,8 +461,9 @@ def write_restart(state: Mapping[str, Any], mesh: Mapping[str, Any], path: str |
                    upstream_commit=UPSTREAM_COMMIT, runtime_dtype=dtype, runtime_device=device,
                    model_time_seconds=float(model_time_seconds), timestep_seconds=timestep,
                    configuration_sha256=configuration_digest(config))
-    if complete:
-        p.attrs["continuation_configuration_sha256"] = continuation_configuration_digest(config)
+    if complete:  # the identity the boundary is bound to (restart.py:477)
+        p.attrs["continuation_configuration_sha256"] = (state[MARKER].get("config")
+                                                         or continuation_configuration_digest(resolved_config(config)))
     p.attrs.update(mesh_sha256=mesh_digest(mesh), source_provenance=str(source_provenance),
                    complete_step_boundary=int(complete))
     if complete:

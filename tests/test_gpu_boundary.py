@@ -53,12 +53,14 @@ def test_device_digest_equals_host_digest():
 
 def test_continuation_from_the_returned_boundary():
     need_gpu()
-    from mpas_dycore_pytorch_gb300.api import run_simulation
+    from mpas_dycore_pytorch_gb300.api import resolved_config, run_simulation
     from mpas_dycore_pytorch_gb300.boundary import has_complete_step_boundary
     from mpas_dycore_pytorch_gb300.device import STATE_KEYS
     state, cfg, dt = _setup()
     b1 = run_simulation(state, state, cfg, dt, nsteps=1)
-    assert has_complete_step_boundary(b1, mesh=state, config=cfg, dt=dt)
+    # bound to the mesh, the full (defaults filled in) configuration and the time step
+    assert has_complete_step_boundary(b1, mesh=state, config=resolved_config(cfg), dt=dt)
+    assert not has_complete_step_boundary(b1, dt=dt / 2)
     cont = run_simulation(b1, state, cfg, dt, nsteps=1)
     assert has_complete_step_boundary(b1)  # the input boundary is not changed
     straight = run_simulation(state, state, cfg, dt, nsteps=2)

@@ -10,6 +10,7 @@ from fixtures import group, load_case
 
 import mpas_dycore_pytorch_gb300 as gb
 from mpas_dycore_pytorch_gb300 import netcdf_io as io
+from mpas_dycore_pytorch_gb300.api import resolved_config
 from mpas_dycore_pytorch_gb300.boundary import MARKER, has_complete_step_boundary, mark_complete_step_boundary
 
 
@@ -30,7 +31,7 @@ def case():
     state = _torchify(group(st, "prepared"))
     state.update(_torchify(group(st, "step2")))
     # bound as run_timestep binds the boundary it returns
-    mark_complete_step_boundary(state, mesh=mesh, config=meta["config"], dt=float(meta["dt"]))
+    mark_complete_step_boundary(state, mesh=mesh, config=resolved_config(meta["config"]), dt=float(meta["dt"]))
     return state, mesh, meta["config"], float(meta["dt"])
 
 
@@ -64,7 +65,7 @@ def test_restart_round_trip_is_exact(tmp_path, case):
     assert torch.all(back["rho_zz"][nc] == 1.0)
     assert torch.all(back["u"][-1] == 0.0)
     # a complete boundary, bound to the file's identity
-    assert has_complete_step_boundary(back, mesh=mesh, config=cfg, dt=dt)
+    assert has_complete_step_boundary(back, mesh=mesh, config=resolved_config(cfg), dt=dt)
 
 
 def test_restart_file_is_netcdf3_with_the_reference_schema(tmp_path, case):
