@@ -40,6 +40,8 @@
  *   mpasg_step_vjp, mpasg_prepare_vjp, mpasg_*_vjp (dynamics stages)
  *                               torch autograd through atmosphere_model.py:2101 _run_simulation_vjp /
  *                               dynamics/time_integration.py:4897 atm_srk3(differentiable=True)
+ *   mpasg_step_jvp, mpasg_prepare_jvp, mpasg_*_jvp (dynamics stages)
+ *                               torch forward-mode AD through atmosphere_model.py:2041 _run_simulation_jvp
  */
 #ifndef MPASG_H
 #define MPASG_H
@@ -524,6 +526,38 @@ int mpasg_step_vjp_taped(const mpasg_mesh *m, const mpasg_config *c, const mpasg
 int mpasg_prepare_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *g,
                       const mpasg_transpose *t, const double *w_in, double *g_u, double *g_w,
                       double *g_theta, double *g_rho, double *work, void *stream);
+
+/* ---- dynamics derivatives (forward mode) --------------------------------------------
+ * Tangents along the dynamics (the reference's run_simulation.jvp, atmosphere_model.py:2041,
+ * through atm_srk3 under torch forward-mode AD), in the scope of the reverse mode above
+ * (float64, dry, flat terrain, no vertical mixing, CAM or Rayleigh damping of u).  d is a
+ * second mpasg_fields of the same layout holding the tangents under the forward field
+ * names; its padding rows hold zeros.  Every entry advances the values f through the stage
+ * (as the forward entry point does) and the tangents d alongside; the branches the forward
+ * takes (upwind sides, kdiff's cap, the damping layer) are frozen at the values, min ties
+ * split evenly as in the reverse mode.  work: at least (nCells + 1) * (nVertLevels + 1)
+ * doubles of device memory. */
+/* One large step of the dynamics (no transport, no reconstruction): f and d advance. */
+int mpasg_step_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *d,
+                   double *work, void *stream);
+/* Tangents of the cold-start preparation (after mpasg_prepare on f): d->u and d->w hold the
+ * tangents of the loaded u and w, d_theta / d_rho ((nCells+1) x L, or null for zero) those
+ * of the loaded theta and rho; fills d's carried fields and diagnostics. */
+int mpasg_prepare_jvp(const mpasg_mesh *m, const mpasg_config *c, const mpasg_fields *f, mpasg_fields *d,
+                      const double *d_theta, const double *d_rho, void *stream);
+/* Stage tangents (each stage's forward on f, tangents on d). */
+int mpasg_vimp_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *d, double dts,
+                   void *stream);
+int mpasg_dyn_tend_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *d,
+                       int rk_step, void *stream);
+int mpasg_acoustic_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *d,
+                       int small_step, double dts, double *work, void *stream);
+int mpasg_divdamp_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *d, double dts,
+                      void *stream);
+int mpasg_recover_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *d,
+                      int rk_step, int ns, double rk_dt, void *stream);
+int mpasg_diag_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *d, int rk_step,
+                   void *stream);
 
 /* ---- boundary binding ----------------------------------------------------------- */
 /* 128-bit value digest of nbytes bytes at p (device memory, 8-byte aligned) into out[0..1]

@@ -847,18 +847,71 @@ def run_simulation_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any], object
             (g0.to(ref.device) if isinstance(ref, torch.Tensor) else g0.cpu())}
 
 
+def _check_perturbation(state: Mapping[str, Any], perturbation: Mapping[str, Any]) -> None:
+    """The reference's checks of a tangent (atmosphere_model.py:2065-2090)."""
+    for key, tangent in perturbation.items():
+        if not isinstance(tangent, torch.Tensor):
+            raise TypeError(f"Perturbation '{key}' must be a tensor, got {type(tangent).__name__}")
+        if key not in state:
+            raise KeyError(f"Perturbation '{key}' is missing from state")
+        ref = state[key]
+        if not isinstance(ref, torch.Tensor):
+            raise TypeError(f"State entry '{key}' is not a tensor and cannot receive a tangent")
+        if tangent.shape != ref.shape:
+            raise MpasConfigError(f"Perturbation '{key}' has shape {tuple(tangent.shape)}; expected {tuple(ref.shape)}")
+        if tangent.dtype != ref.dtype:
+            raise MpasConfigError(f"Perturbation '{key}' has dtype {tangent.dtype}; expected {ref.dtype}")
+        if tangent.device != ref.device:
+            raise MpasConfigError(f"Perturbation '{key}' is on {tangent.device}; expected {ref.device}")
+
+
+def _dynamics_jvp(state: Mapping[str, Any], mesh: Mapping[str, Any] | None, perturbation: Mapping[str, Any],
+                  kwargs: dict) -> dict:
+    """run_simulation.jvp along the loaded u, w, theta, rho: the hand-written forward mode of
+    the dynamics (dyn_adjoint.py, ``mpasg_step_jvp``)."""
+    from .dyn_adjoint import DynamicsTangent, check_request, run_jvp
+    unknown = set(kwargs) - {"config", "dt", "nsteps", "device", "differentiable", "checkpoint_timesteps",
+                             "checkpoint_use_reentrant", "checkpoint_materialize_final"}
+    if unknown:
+        raise MpasConfigError(f"unsupported keyword arguments for the derivative runs: {sorted(unknown)}")
+    if _is_prepared(state):
+        raise MpasUnsupportedCapabilityError(
+            "dynamics derivatives start from a loaded (unprepared) state: perturb u, w, theta or rho")
+    mesh = mesh if mesh is not None else state
+    merged = dict(mesh)
+    merged.update(state)
+    cfg = resolved_config(kwargs.get("config"))
+    dt = float(cfg["config_dt"] if kwargs.get("dt") is None else kwargs["dt"])
+    nsteps = int(kwargs.get("nsteps", 1))
+    ns = _int(merged.get("num_scalars", _np(merged["scalars"]).shape[-1]))
+    check_request(cfg, merged, ns)
+    model = Model(merged, cfg, dt, num_scalars=ns, device=kwargs.get("device", "cuda"))
+    tangents = run_jvp(model, merged, nsteps, perturbation, DynamicsTangent(model))
+    dev = next(iter(perturbation.values())).device
+    return {k: v.to(dev) for k, v in tangents.items()}
+
+
 def run_simulation_jvp(state: Mapping[str, Any], mesh: Mapping[str, Any], perturbation: Mapping[str, Any],
                        **kwargs) -> dict:
-    """Tangent-linear ``run_simulation`` for the transported scalars (the reference's
-    ``run_simulation.jvp``, atmosphere_model.py:2041): the tangent of the end scalars
-    along ``perturbation["scalars"]``, replayed through each step's recorded transport.
-    Outputs that do not depend on the scalars get no tangent, as in the reference."""
+    """Tangent-linear ``run_simulation`` (the reference's ``run_simulation.jvp``,
+    atmosphere_model.py:2041).
+
+    * a perturbation of any of ``u``, ``w``, ``theta``, ``rho`` (the loaded primitives):
+      tangents of the final dynamics fields (the carried fields and ``rho_edge``) through the
+      preparation and the dynamics (the hand-written forward mode of dyn_adjoint.py: dry,
+      flat terrain, float64).  The scalars' tangent along the winds is not formed;
+    * ``perturbation["scalars"]``: the tangent of the end scalars, replayed through each
+      step's recorded transport.  Outputs that do not depend on the scalars get no tangent,
+      as in the reference."""
     from .tracer_adjoint import scalars_jvp
     reject_unsupported_request(state, mesh, kwargs.get("config"))
+    _check_perturbation(state, perturbation)
+    if perturbation and set(perturbation) <= {"u", "w", "theta", "rho"}:
+        return _dynamics_jvp(state, mesh, perturbation, dict(kwargs))
     if set(perturbation) != {"scalars"}:
         raise MpasUnsupportedCapabilityError(
-            "run_simulation.jvp on the GB300 path takes a 'scalars' perturbation only "
-            f"(got {sorted(perturbation)})")
+            "run_simulation.jvp on the GB300 path takes a 'scalars' perturbation, or one of any of 'u', 'w', "
+            f"'theta', 'rho' (not both kinds at once); got {sorted(perturbation)}")
     v = perturbation["scalars"]
     if not isinstance(v, torch.Tensor):
         raise TypeError(f"Perturbation 'scalars' must be a tensor, got {type(v).__name__}")

@@ -21,7 +21,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libmpasg.so"
 SOURCES = ("kern_column.cu", "kern_tend.cu", "kern_diag.cu", "kern_transport.cu", "driver.cu", "reorder.cu",
            "kern_adjoint.cu", "kern_transport_adj.cu", "kern_adj_column.cu", "kern_adj_tend.cu", "kern_adj_diag.cu",
-           "driver_adj.cu", "kern_digest.cu")
+           "driver_adj.cu", "kern_digest.cu", "kern_tan_column.cu", "kern_tan_tend.cu", "driver_tan.cu")
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
 
 

@@ -85,3 +85,23 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
 int mpasgi_divdamp_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
                             double dts, const AdjWork& w, cudaStream_t s);
 int mpasgi_zero(double* p, long long n, cudaStream_t s);
+
+// internal entry points of the forward mode (tangents; kern_tan_*.cu, driver_tan.cu): d is the
+// tangent state (mpasg_fields layout).  Stages that update their inputs in place run their
+// forward on f inside (acoustic) or after the tangent (divergence damping, recovery); the
+// others read the forward's outputs and run after it (vimp, tendencies, diagnostics, preparation).
+int mpasgi_theta_edge_jvp(const mpasg_mesh* m, const mpasg_fields* f, mpasg_fields* d, cudaStream_t s);
+int mpasgi_vimp_jvp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* d,
+                         double dts, cudaStream_t s);
+int mpasgi_acoustic_jvp_core(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, mpasg_fields* d,
+                             int small_step, double dts, double* ubuf, cudaStream_t s);
+int mpasgi_divdamp_jvp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* d,
+                            double dts, cudaStream_t s);
+int mpasgi_recover_jvp_core(const mpasg_mesh* m, const mpasg_fields* f, mpasg_fields* d, int rk_step, int ns,
+                            double rk_dt, cudaStream_t s);
+int mpasgi_prepare_jvp_core(const mpasg_mesh* m, const mpasg_fields* f, mpasg_fields* d, const double* dth,
+                            const double* drho, cudaStream_t s);
+int mpasgi_dyn_tend_jvp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* d,
+                             int rk_step, cudaStream_t s);
+int mpasgi_diag_jvp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* d,
+                         int rk_step, cudaStream_t s);

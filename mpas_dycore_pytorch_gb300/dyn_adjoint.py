@@ -1,5 +1,6 @@
-"""Reverse mode of the dynamics through whole large steps (the reference's
-``run_simulation.vjp`` with respect to the dynamics state, atmosphere_model.py:2101).
+"""Reverse and forward mode of the dynamics through whole large steps (the reference's
+``run_simulation.vjp`` / ``.jvp`` with respect to the dynamics state,
+atmosphere_model.py:2101 / :2041).
 
 ``DynamicsAdjoint(model)`` holds, beside the model's own device state, a second device
 state of the same layout for the cotangents, the transposed connectivity of the mesh, the
@@ -9,6 +10,11 @@ reference's per-step checkpoint, autodiff/checkpoint.py:106-254), then, from the
 back, restores each step's checkpoint and runs ``mpasg_step_vjp`` (the step recomputed with
 its tape, then its stages backwards: hand-written CUDA kernels, deterministic gathers), and
 finally ``mpasg_prepare_vjp`` for the cold-start preparation.
+
+``DynamicsTangent(model)`` holds the tangent state; ``run_jvp`` prepares the loaded
+primitives with their tangents (``mpasg_prepare_jvp``) and advances values and tangents
+together through every step (``mpasg_step_jvp``: each stage's forward and its hand-written
+tangent kernels), with nothing stored.
 
 Supported: float64, dry columns, flat terrain, ``2d_smagorinsky`` or ``2d_fixed`` mixing with
 or without del4, no vertical mixing, CAM or Rayleigh damping of u, any RK order and substep
@@ -333,3 +339,72 @@ def run_vjp(model, loaded: Mapping[str, Any], nsteps: int,
     adj.restore(ck0)
     grads = adj.prepare_vjp(w_in)
     return grads, final
+
+
+class DynamicsTangent:
+    """Tangent state and work buffer of one Model (forward mode)."""
+
+    def __init__(self, model):
+        from .device import DeviceState
+        check_supported(model)
+        self.model = model
+        self.lib = model.lib
+        dm = model.dmesh
+        self.d = DeviceState(dm, model.state.num_scalars)
+        self.d.arena.zero_()
+        self.work = torch.zeros((dm.nCells + 1) * (dm.nVertLevels + 1), dtype=torch.float64, device=dm.device)
+
+    def _args(self):
+        m = self.model
+        return C.byref(m.dmesh.struct), C.byref(m.cstruct), C.byref(m.state.struct), C.byref(self.d.struct)
+
+    def prepare_jvp(self, dtheta: torch.Tensor | None, drho: torch.Tensor | None) -> None:
+        """Tangents of the prepared state (the model holds it) from the tangents of the loaded
+        u and w (already in the tangent state) and of theta and rho."""
+        rc = self.lib.mpasg_prepare_jvp(*self._args(), _p(dtheta) if dtheta is not None else C.c_void_p(0),
+                                        _p(drho) if drho is not None else C.c_void_p(0), _stream())
+        _lib.check(rc, "mpasg_prepare_jvp")
+
+    def step_jvp(self) -> None:
+        """One step of the model's dynamics with the tangents alongside."""
+        _lib.check(self.lib.mpasg_step_jvp(*self._args(), _p(self.work), _stream()), "mpasg_step_jvp")
+
+
+def run_jvp(model, loaded: Mapping[str, Any], nsteps: int, perturbation: Mapping[str, torch.Tensor],
+            tan: DynamicsTangent | None = None) -> dict[str, torch.Tensor]:
+    """Tangents of the final carried fields (and ``rho_edge``) along ``perturbation`` of the
+    loaded u, w, theta, rho (rows as loaded; padding rows are not perturbed), through the
+    preparation and ``nsteps`` large steps.  The model's state ends with the dynamics of the
+    final step (its scalars are not advanced)."""
+    tan = tan or DynamicsTangent(model)
+    dev = model.dmesh.device
+    model.prepare(loaded)
+    d = tan.d.f
+    tan.d.arena.zero_()
+
+    def device_copy(key, shape):
+        v = perturbation.get(key)
+        if v is None:
+            return None
+        out = torch.zeros(shape, dtype=torch.float64, device=dev)
+        rows = min(int(v.shape[0]), shape[0] - 1)  # the padding row stays unperturbed
+        out[:rows] = v[:rows].to(device=dev, dtype=torch.float64)
+        return out
+
+    for key in ("u", "w"):
+        t = device_copy(key, tuple(d[key].shape))
+        if t is not None:
+            d[key].copy_(t)
+    dth = device_copy("theta", tuple(d["theta_m"].shape))
+    drho = device_copy("rho", tuple(d["rho_zz"].shape))
+    tan.prepare_jvp(dth, drho)
+    for _ in range(int(nsteps)):
+        tan.step_jvp()
+    bad = model.check_finite()
+    if bad:
+        raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")
+    out = {k: d["h_edge" if k == "rho_edge" else k].clone() for k in DIFFERENTIABLE_OUT}
+    for k, v in out.items():
+        if not bool(torch.isfinite(v).all()):
+            raise MpasNumericalError(f"tangent of {k!r} contains nonfinite values")
+    return out

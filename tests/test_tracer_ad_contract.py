@@ -62,8 +62,18 @@ def test_moist_scalars_rejected():
 
 def test_jvp_perturbation_contract():
     state, meta = _case()
-    with pytest.raises(MpasUnsupportedCapabilityError):
-        run_simulation.jvp(state, state, {"u": torch.zeros_like(state["u"])}, config=meta["config"])
+    # the dynamics tangents cover dry columns only
+    moist = dict(state, moist_end=1)
+    with pytest.raises(MpasUnsupportedCapabilityError, match="dry columns"):
+        run_simulation.jvp(moist, moist, {"u": torch.zeros_like(state["u"])}, config=meta["config"])
+    with pytest.raises(MpasUnsupportedCapabilityError, match="not both kinds"):
+        run_simulation.jvp(state, state, {"u": torch.zeros_like(state["u"]),
+                                          "scalars": torch.zeros_like(state["scalars"])}, config=meta["config"])
+    with pytest.raises(KeyError):
+        run_simulation.jvp(state, state, {"theta_m": torch.zeros_like(state["u"])}, config=meta["config"])
+    with pytest.raises(MpasConfigError):
+        run_simulation.jvp(state, state, {"u": torch.zeros_like(state["u"], dtype=torch.float32)},
+                           config=meta["config"])
     with pytest.raises(MpasConfigError):
         run_simulation.jvp(state, state, {"scalars": torch.zeros(3, 2)}, config=meta["config"])
     with pytest.raises(TypeError):
