@@ -439,7 +439,9 @@ int mpasg_tridiag_factor_jvp(long long n, int L, const double *a, const double *
  * layout as the forward fields: g->u is the cotangent of u, and so on.  Every transposed
  * stencil is a deterministic gather (no atomics).  Scope: float64 arithmetic, dry columns
  * (moist_end < moist_start), flat terrain, no vertical mixing, CAM or Rayleigh damping of u;
- * anything else returns MPASG_E_ARG.  The mass-flux averages ruAvg / wwAvg carry no
+ * anything else returns MPASG_E_ARG.  The step entries (mpasg_step_tape / _vjp_taped /
+ * _vjp) also take the mixed form: the tape then holds the mixed form's trajectory (its own
+ * stage calls) and the reverse pass linearises it in float64.  The mass-flux averages ruAvg / wwAvg carry no
  * cotangent: they feed only the scalar transport, whose dependence on the dynamics is not
  * differentiated here.
  */

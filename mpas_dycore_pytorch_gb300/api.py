@@ -766,7 +766,7 @@ def _dynamics_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any] | None, obje
     dt = float(cfg["config_dt"] if kwargs.get("dt") is None else kwargs["dt"])
     nsteps = int(kwargs.get("nsteps", 1))
     ns = _int(merged.get("num_scalars", _np(merged["scalars"]).shape[-1]))
-    check_request(cfg, merged, ns)
+    check_request(cfg, merged, ns, allow_mixed=True)
     model = Model(merged, cfg, dt, num_scalars=ns, device=kwargs.get("device", "cuda"))
     adj = DynamicsAdjoint(model)
 

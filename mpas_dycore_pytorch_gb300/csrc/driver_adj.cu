@@ -278,8 +278,9 @@ int fold_saves(const mpasg_mesh* m, mpasg_fields* g, cudaStream_t s) {
   return MPASG_OK;
 }
 
-// refresh the saves of the coming dynamics substep (writes go to the tape's save block)
-int make_saves(const mpasg_mesh* m, const Tape& T, mpasg_fields& f, int sub, cudaStream_t s) {
+// refresh the saves of the coming dynamics substep (writes go to the tape's save block);
+// mixed: the mixed form's edge reciprocal sums, as its step forms them
+int make_saves(const mpasg_mesh* m, const Tape& T, mpasg_fields& f, int sub, bool mixed, cudaStream_t s) {
   const long long L = m->nVertLevels, nc = m->nCells;
   const long long nel = (m->nEdges + 1LL) * L, ncw = (nc + 1) * (L + 1), ncl = (nc + 1) * L;
   k_fill_row<<<1, 128, 0, s>>>(f.theta_m + nc * L, (int)L, 0.0);
@@ -291,18 +292,22 @@ int make_saves(const mpasg_mesh* m, const Tape& T, mpasg_fields& f, int sub, cud
   CHECK_RC(dcopy(f.rho_p_save, f.rho_p, ncl, s));
   CHECK_RC(dcopy(f.theta_m_save, f.theta_m, ncl, s));
   CHECK_RC(dcopy(f.rr_save, f.rho_p, ncl, s));
-  return mpasgi_theta_edge(m, &f, false, s);
+  return mpasgi_theta_edge(m, &f, mixed, s);
 }
 
 int coef_slot(const StepPlan& p, int sub, int rk) {  // sub 1-based
   return (sub - 1) * p.nvimp_per_sub + ((rk == 1 || p.order == 2) ? 0 : 1);
 }
 
-// the step's dynamics forward with the tape (no transport, no reconstruction)
+// the step's dynamics forward with the tape (no transport, no reconstruction); in the
+// mixed form the same stage calls as its step (float32 copies packed at the step start,
+// kept current by the stages), so the values are that form's trajectory
 int forward_taped(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, const StepPlan& p, const Tape& T,
                   cudaStream_t s) {
   void* stream = (void*)s;
-  CHECK_RC(make_saves(m, T, f, 0, s));
+  const bool mixed = c->precision == MPASG_PRECISION_MIXED;
+  CHECK_RC(make_saves(m, T, f, 0, mixed, s));
+  if (mixed) CHECK_RC(mpasgi_pack_f32(m, &f, s));
   CHECK_RC(mpasg_moist_coefficients(m, c, &f, stream));
   int a = 0;
   for (int sub = 1; sub <= p.split; ++sub) {
@@ -326,7 +331,7 @@ int forward_taped(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, co
       CHECK_RC(mpasg_recover_large_step(m, c, &f, rk, p.nsub[rk - 1], p.rk_ts[rk - 1], stream));
       CHECK_RC(mpasgi_solve_diagnostics(m, c, &f, rk, s, true));
     }
-    if (sub < p.split) CHECK_RC(make_saves(m, T, f, sub, s));
+    if (sub < p.split) CHECK_RC(make_saves(m, T, f, sub, mixed, s));
   }
   return snap_store(m, T, f, T.snap(3 * p.split), s);
 }
@@ -406,8 +411,10 @@ int step_reverse(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields*
   return fold_saves(m, g, s);
 }
 
+// the reverse pass is float64 in both forms: the mixed form's gradient is the float64
+// linearisation about the mixed trajectory
 bool step_args_ok(const mpasg_mesh* m, const mpasg_config* c) {
-  return adj_supported(m, c) && c->precision == MPASG_PRECISION_FLOAT64 &&
+  return adj_supported(m, c) && (c->precision == MPASG_PRECISION_FLOAT64 || c->precision == MPASG_PRECISION_MIXED) &&
          (c->time_integration_order == 2 || c->time_integration_order == 3) && c->number_of_sub_steps >= 1 &&
          c->dynamics_split_steps >= 1;
 }

@@ -49,13 +49,18 @@ def _p(t: torch.Tensor) -> C.c_void_p:
     return C.c_void_p(t.data_ptr())
 
 
-def check_request(cfg: Mapping[str, Any], merged: Mapping[str, Any], num_scalars: int) -> None:
+def check_request(cfg: Mapping[str, Any], merged: Mapping[str, Any], num_scalars: int,
+                  allow_mixed: bool = False) -> None:
     """The dynamics derivative's scope, checked on the host from the configuration and the
-    mesh before any device work (the same limits as ``check_supported``)."""
+    mesh before any device work (the same limits as ``check_supported``).  The reverse mode
+    also takes the mixed form (its trajectory, linearised in float64); the forward mode is
+    float64 only."""
     from .device import _int, _np
     why = []
-    if str(cfg.get("config_precision", "float64")) != "float64":
-        why.append("float64 arithmetic only (config_precision)")
+    prec = str(cfg.get("config_precision", "float64"))
+    if prec != "float64" and not (allow_mixed and prec == "mixed"):
+        why.append("float64 or mixed arithmetic (config_precision)" if allow_mixed
+                   else "float64 arithmetic only (config_precision)")
     ms, me = _int(merged.get("moist_start", 1)), _int(merged.get("moist_end", num_scalars))
     if not me < ms:
         why.append("dry columns only (moist_end < moist_start)")
@@ -74,11 +79,11 @@ def check_request(cfg: Mapping[str, Any], merged: Mapping[str, Any], num_scalars
         raise MpasUnsupportedCapabilityError("dynamics derivatives on the GB300 path: " + "; ".join(why))
 
 
-def check_supported(model) -> None:
+def check_supported(model, allow_mixed: bool = False) -> None:
     """The dynamics derivative's scope (mpasg.h): raise before any derivative work."""
     cfg, cs, dm = model.cfg, model.cstruct, model.dmesh
     why = []
-    if cs.precision != _lib.PRECISIONS["float64"]:
+    if cs.precision != _lib.PRECISIONS["float64"] and not (allow_mixed and cs.precision == _lib.PRECISIONS["mixed"]):
         why.append("float64 arithmetic only (config_precision)")
     if not (cs.moist_end < cs.moist_start):
         why.append("dry columns only (moist_end < moist_start)")
@@ -167,7 +172,7 @@ class DynamicsAdjoint:
 
     def __init__(self, model):
         from .device import DeviceState
-        check_supported(model)
+        check_supported(model, allow_mixed=True)
         self.model = model
         self.lib = model.lib
         dm = model.dmesh

@@ -191,3 +191,26 @@ def test_run_vjp_matches_reference(case):
                                dt=float(z["dt"]), nsteps=int(z["nsteps"]), checkpoint_timesteps=False)
     for k in ("u", "theta"):
         assert torch.equal(again[k], grads[k]), k
+
+
+@pytest.mark.parametrize("case", AD_CASES)
+def test_mixed_form_gradient_within_1e4_of_reference(case):
+    """The mixed form's gradient (float32 stencils in the forward and its taped recompute,
+    the reverse pass in float64 about that trajectory) against the reference's float64 VJP:
+    rel L2 <= 1e-4."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import run_simulation
+    z = _npz(case)
+    mesh, st0 = mesh_and_state(case)
+    nc = int(mesh["nCells"])
+    objective = _reference_objective(mesh, z["sp_ref"], nc)
+    state = {k: torch.as_tensor(v) for k, v in st0.items()}
+    grads = run_simulation.vjp(state, mesh, objective, track_keys=("u", "theta"),
+                               config=dict(config(case), config_precision="mixed"), dt=float(z["dt"]),
+                               nsteps=int(z["nsteps"]))
+    for k in ("u", "theta"):
+        a = to_np(grads[k])[:-1]
+        b = z[f"grad_{k}"][:-1]
+        err = np.linalg.norm(a - b) / np.linalg.norm(b)
+        print(f"{case} mixed grad_{k}: rel L2 vs reference {err:.3e}")
+        assert err <= 1e-4, (case, k, err)

@@ -9,7 +9,11 @@ against the initial surface pressure.  Its gradient with respect to the initial 
 (run_simulation.vjp) is checked along a seeded random direction against central differences
 of run_simulation over h = 2^-12 ... 2^-36 (the stated 2^-20 ... 2^-36 and the larger steps
 that show the truncation side of the curve): it must reach a relative error <= 1e-7,
-and a control that drops the theta part of the gradient must miss it by far.
+and a control that drops the theta part of the gradient must miss it by far.  The same
+directional derivative from the forward mode (run_simulation.jvp, the functional's
+derivative applied to the final tangents) must meet the reverse mode's within 1e-12: the
+JVP/VJP identity on this workload.  The mixed form's gradient (its float32-stencil
+trajectory, linearised in float64) must be within 1e-4 of the float64 gradient.
 """
 
 import math
@@ -74,6 +78,23 @@ def test_gradient_matches_central_differences():
         x[-1] = 0.0  # the padding row is not perturbed
         d[k] = torch.as_tensor(x)
     dJ = sum(float((grads[k].cpu() * d[k]).sum()) for k in d)
+    # forward mode: the final tangents along d, contracted with the functional's derivative
+    tan = run_simulation.jvp(st, mesh, {"u": d["u"], "theta": d["theta"]}, config=CFG, dt=900.0, nsteps=NSTEPS)
+    final = run_simulation(st, mesh, CFG, 900.0, nsteps=NSTEPS)
+    leaves = {k: final[k].detach().clone().requires_grad_(True) for k in ("rho_zz", "pressure_p")}
+    gj = torch.autograd.grad(objective({**final, **leaves}), [leaves["rho_zz"], leaves["pressure_p"]])
+    dJ_fwd = sum(float((g * tan[k].to(g.device)).sum()) for g, k in zip(gj, ("rho_zz", "pressure_p")))
+    ident = abs(dJ_fwd - dJ) / abs(dJ)
+    print(f"JVP/VJP identity: forward {dJ_fwd:.15e} reverse {dJ:.15e} rel {ident:.2e}")
+    assert ident <= 1e-12, (dJ_fwd, dJ, ident)
+    # the mixed form's gradient against the float64 one
+    mixed = run_simulation.vjp(st, mesh, objective, track_keys=("u", "theta"),
+                               config=dict(CFG, config_precision="mixed"), dt=900.0, nsteps=NSTEPS)
+    for k in ("u", "theta"):
+        a, b = mixed[k][:-1].cpu().numpy(), grads[k][:-1].cpu().numpy()
+        err = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        print(f"mixed-form gradient {k}: rel L2 vs float64 {err:.3e}")
+        assert err <= 1e-4, (k, err)
     rows = []
     for h in H:
         Js = []
