@@ -26,12 +26,22 @@ def test_vjp_track_keys_contract():
 
 
 @pytest.mark.parametrize("extra", [{"config_v_mom_eddy_visc2": 1.0}, {"config_mpas_cam_coef": 1.0},
-                                   {"config_rayleigh_damp_u": True}, {"config_precision": "mixed"}])
+                                   {"config_rayleigh_damp_u": True}])
 def test_dynamics_vjp_scope_rejected_before_device_work(extra):
     state, meta = _case()
     cfg = dict(meta["config"], **extra)
     with pytest.raises(MpasUnsupportedCapabilityError):
         run_simulation.vjp(state, state, lambda o: o["rho_zz"].sum(), track_keys=("u", "theta"), config=cfg)
+    with pytest.raises(MpasUnsupportedCapabilityError):
+        run_simulation.jvp(state, state, {"u": torch.zeros_like(state["u"])}, config=cfg)
+
+
+def test_dynamics_jvp_is_float64_only():
+    """The reverse mode takes the mixed form; the forward mode is float64 only."""
+    state, meta = _case()
+    cfg = dict(meta["config"], config_precision="mixed")
+    with pytest.raises(MpasUnsupportedCapabilityError, match="float64"):
+        run_simulation.jvp(state, state, {"u": torch.zeros_like(state["u"])}, config=cfg)
 
 
 def test_dynamics_vjp_moist_rejected_before_device_work():
