@@ -85,6 +85,13 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
 int mpasgi_divdamp_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
                             double dts, const AdjWork& w, cudaStream_t s);
 int mpasgi_zero(double* p, long long n, cudaStream_t s);
+// zero several arrays in one launch (up to kZeroSpans per launch; more take more launches)
+constexpr int kZeroSpans = 16;
+struct ZeroSpan {
+  double* p;
+  long long n;
+};
+int mpasgi_zero_many(const ZeroSpan* spans, int count, cudaStream_t s);
 
 // internal entry points of the forward mode (tangents; kern_tan_*.cu, driver_tan.cu): d is the
 // tangent state (mpasg_fields layout).  Stages that update their inputs in place run their

@@ -99,7 +99,7 @@ struct Tape {
     tend_sz = E + C + W;
     trho_sz = C;
     coef_sz = Lr + 8 * C + W;
-    ac_sz = E + 2 * C + W;
+    ac_sz = 0;  // a substep's inputs are the previous substep's taped outputs (none at the first)
     aco_sz = E + 2 * W + 3 * C;
     n_snap = 3 * p.split + 1;
     n_sv = p.split;
@@ -118,9 +118,8 @@ struct Tape {
   double* coef(int i) const {
     return base + n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + n_sv * trho_sz + i * coef_sz;
   }
-  // acoustic substep i: its inputs (ru_p, rho_pp, rtheta_pp, rw_p), then its outputs
-  // (ru_p after the edge update, the undamped solution x, ts, the damped solution rw_p,
-  // rtheta_pp and rtheta_pp_old)
+  // acoustic substep i: its outputs (ru_p after the edge update, the undamped solution x,
+  // the damped solution rw_p, ts, rtheta_pp and rtheta_pp_old)
   double* ac(int i) const {
     return base + n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + n_sv * trho_sz + n_coef * coef_sz +
            i * (ac_sz + aco_sz);
@@ -152,6 +151,52 @@ int dcopy(double* dst, const double* src, long long n, cudaStream_t s) {
 // copy the carried fields of f into snapshot block b
 int snap_store(const mpasg_mesh* m, const Tape& T, mpasg_fields& f, double* b, cudaStream_t s) {
   for (int k = 0; k < S_COUNT; ++k) CHECK_RC(dcopy(T.snap_field(b, k), *snap_ptr(f, k), snap_len(m, k), s));
+  return MPASG_OK;
+}
+
+// copy the carried fields of snapshot block b back into the fields of f
+int snap_restore(const mpasg_mesh* m, const Tape& T, mpasg_fields& f, const double* b, cudaStream_t s) {
+  for (int k = 0; k < S_COUNT; ++k)
+    CHECK_RC(dcopy(*snap_ptr(f, k), T.snap_field(const_cast<double*>(b), k), snap_len(m, k), s));
+  return MPASG_OK;
+}
+
+// Up to S_COUNT (src, dst, offset, count) copies in one launch (blockIdx.y picks the copy).
+struct CarryList {
+  const double* src[S_COUNT];
+  double* dst[S_COUNT];
+  long long off[S_COUNT], n[S_COUNT];
+};
+__global__ void k_carry(CarryList cl) {
+  const int j = blockIdx.y;
+  const double* a = cl.src[j] + cl.off[j];
+  double* b = cl.dst[j] + cl.off[j];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cl.n[j]; i += (long long)gridDim.x * blockDim.x)
+    b[i] = a[i];
+}
+
+// What the recovery and the diagnostics of RK stage rk leave unwritten in the next snapshot
+// block, carried over from this one: the padding rows of every carried field, the whole of
+// rw (recovery writes its interior interfaces only), and before rk 3 the whole of exner and
+// pressure_p (recovered at rk 3 only) and v (recomputed at rk 3 only).
+int carry_block(const mpasg_mesh* m, const Tape& T, double* b0, double* b1, int rk, cudaStream_t s) {
+  const long long L = m->nVertLevels;
+  CarryList cl{};
+  long long nmax = 0;
+  for (int k = 0; k < S_COUNT; ++k) {
+    const long long len = snap_len(m, k);
+    const long long row = (k == S_W || k == S_RW) ? L + 1 : L;
+    const bool whole = k == S_RW || (rk < 3 && (k == S_EXNER || k == S_PP || k == S_V));
+    cl.src[k] = T.snap_field(b0, k);
+    cl.dst[k] = T.snap_field(b1, k);
+    cl.off[k] = whole ? 0 : len - row;
+    cl.n[k] = whole ? len : row;
+    if (cl.n[k] > nmax) nmax = cl.n[k];
+  }
+  long long gx = (nmax + kBlock - 1) / kBlock;
+  if (gx > 1216) gx = 1216;
+  k_carry<<<dim3((unsigned)gx, S_COUNT), kBlock, 0, s>>>(cl);
+  MPASG_LAUNCH_CHECK();
   return MPASG_OK;
 }
 
@@ -194,27 +239,25 @@ void coef_view(const Tape& T, mpasg_fields& v, int j) {
   v.coftz = b;
 }
 
-int ac_store(const mpasg_mesh* m, const Tape& T, const mpasg_fields& f, int a, cudaStream_t s) {
-  const long long L = m->nVertLevels;
-  double* b = T.ac(a);
-  CHECK_RC(dcopy(b, f.ru_p, (m->nEdges + 1LL) * L, s));
-  CHECK_RC(dcopy(b + T.E, f.rho_pp, (m->nCells + 1LL) * L, s));
-  CHECK_RC(dcopy(b + T.E + T.C, f.rtheta_pp, (m->nCells + 1LL) * L, s));
-  CHECK_RC(dcopy(b + T.E + 2 * T.C, f.rw_p, (m->nCells + 1LL) * (L + 1), s));
-  return MPASG_OK;
+// point the substep's scratch outputs (x, ts, rtheta_pp_old: written, not updated, by the
+// substep) into its tape block, so they need no copy
+void aco_redirect(const Tape& T, mpasg_fields& v, int a) {
+  double* b = T.aco(a);
+  v.ac_x = b + T.E;
+  v.ac_ts = b + T.E + 2 * T.W;
+  v.rtheta_pp_old = b + T.E + 2 * T.W + 2 * T.C;
 }
 
 // the substep's outputs the reverse pass reads (after the acoustic step, before damping)
+// (the updated fields ru_p, rw_p and rtheta_pp are copied; x, ts and rtheta_pp_old were
+// written there directly, aco_redirect)
 int aco_store(const mpasg_mesh* m, const Tape& T, const mpasg_fields& f, int a, cudaStream_t s) {
   const long long L = m->nVertLevels;
   const long long nel = (m->nEdges + 1LL) * L, ncw = (m->nCells + 1LL) * (L + 1), ncl = (m->nCells + 1LL) * L;
   double* b = T.aco(a);
   CHECK_RC(dcopy(b, f.ru_p, nel, s));
-  CHECK_RC(dcopy(b + T.E, f.ac_x, ncw, s));
   CHECK_RC(dcopy(b + T.E + T.W, f.rw_p, ncw, s));
-  CHECK_RC(dcopy(b + T.E + 2 * T.W, f.ac_ts, ncl, s));
   CHECK_RC(dcopy(b + T.E + 2 * T.W + T.C, f.rtheta_pp, ncl, s));
-  CHECK_RC(dcopy(b + T.E + 2 * T.W + 2 * T.C, f.rtheta_pp_old, ncl, s));
   return MPASG_OK;
 }
 
@@ -302,19 +345,25 @@ int coef_slot(const StepPlan& p, int sub, int rk) {  // sub 1-based
 // the step's dynamics forward with the tape (no transport, no reconstruction); in the
 // mixed form the same stage calls as its step (float32 copies packed at the step start,
 // kept current by the stages), so the values are that form's trajectory
+// The carried fields live in the tape's snapshot blocks during the step: block 0 is a copy
+// of the start state, and the recovery and diagnostics of stage i write straight into block
+// i + 1 (after carry_block), so the stage start states are kept without copies.  The end
+// state is copied back into f's own fields.
 int forward_taped(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, const StepPlan& p, const Tape& T,
                   cudaStream_t s) {
   void* stream = (void*)s;
   const bool mixed = c->precision == MPASG_PRECISION_MIXED;
+  const mpasg_fields own = f;
   CHECK_RC(make_saves(m, T, f, 0, mixed, s));
   if (mixed) CHECK_RC(mpasgi_pack_f32(m, &f, s));
   CHECK_RC(mpasg_moist_coefficients(m, c, &f, stream));
+  CHECK_RC(snap_store(m, T, f, T.snap(0), s));
+  snap_view(T, f, T.snap(0));
   int a = 0;
   for (int sub = 1; sub <= p.split; ++sub) {
     for (int rk = 1; rk <= 3; ++rk) {
       const int i = (sub - 1) * 3 + rk - 1;
       const double dts = p.rk_sub[rk - 1];
-      CHECK_RC(snap_store(m, T, f, T.snap(i), s));
       if (rk == 1 || (rk == 2 && p.order == 3)) {
         coef_view(T, f, coef_slot(p, sub, rk));
         CHECK_RC(mpasg_vert_imp_coefs(m, c, &f, dts, stream));
@@ -323,17 +372,20 @@ int forward_taped(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, co
       CHECK_RC(mpasgi_dyn_tend(m, c, &f, rk, s, true));
       CHECK_RC(mpasg_smlstep_pert(m, c, &f, stream));
       for (int small = 1; small <= p.nsub[rk - 1]; ++small) {
-        CHECK_RC(ac_store(m, T, f, a, s));
+        aco_redirect(T, f, a);
         CHECK_RC(mpasgi_acoustic_step(m, c, &f, small, dts, s, true));
         CHECK_RC(aco_store(m, T, f, a++, s));
         CHECK_RC(mpasgi_divergence_damping(m, c, &f, dts, s, true));
       }
+      CHECK_RC(carry_block(m, T, T.snap(i), T.snap(i + 1), rk, s));
+      snap_view(T, f, T.snap(i + 1));
       CHECK_RC(mpasg_recover_large_step(m, c, &f, rk, p.nsub[rk - 1], p.rk_ts[rk - 1], stream));
       CHECK_RC(mpasgi_solve_diagnostics(m, c, &f, rk, s, true));
     }
     if (sub < p.split) CHECK_RC(make_saves(m, T, f, sub, mixed, s));
   }
-  return snap_store(m, T, f, T.snap(3 * p.split), s);
+  mpasg_fields out = own;
+  return snap_restore(m, T, out, T.snap(3 * p.split), s);
 }
 
 // zero every cotangent accumulator of g that is not a carried field
@@ -345,21 +397,19 @@ int zero_internal(const mpasg_mesh* m, mpasg_fields* g, cudaStream_t s) {
   double* c_fields[] = {g->rtheta_p_save, g->rho_p_save, g->theta_m_save, g->rr_save, g->tend_theta,
                         g->tend_theta_euler, g->tend_rho, g->kdiff, g->rho_pp, g->rtheta_pp, g->rtheta_pp_old,
                         g->cofwz, g->cofwt, g->a_tri, g->alpha_tri, g->gamma_tri};
-  for (double* p : e_fields) CHECK_RC(mpasgi_zero(p, nel, s));
-  for (double* p : w_fields) CHECK_RC(mpasgi_zero(p, ncw, s));
-  for (double* p : c_fields) CHECK_RC(mpasgi_zero(p, ncl, s));
-  return MPASG_OK;
+  ZeroSpan zs[27];
+  int n = 0;
+  for (double* p : e_fields) zs[n++] = {p, nel};
+  for (double* p : w_fields) zs[n++] = {p, ncw};
+  for (double* p : c_fields) zs[n++] = {p, ncl};
+  return mpasgi_zero_many(zs, n, s);
 }
 
 int zero_work_cotangents(const mpasg_mesh* m, mpasg_fields* g, cudaStream_t s) {
   const long long L = m->nVertLevels;
   const long long nel = (m->nEdges + 1LL) * L, ncw = (m->nCells + 1LL) * (L + 1), ncl = (m->nCells + 1LL) * L;
-  CHECK_RC(mpasgi_zero(g->ru_p, nel, s));
-  CHECK_RC(mpasgi_zero(g->rw_p, ncw, s));
-  CHECK_RC(mpasgi_zero(g->rho_pp, ncl, s));
-  CHECK_RC(mpasgi_zero(g->rtheta_pp, ncl, s));
-  CHECK_RC(mpasgi_zero(g->rtheta_pp_old, ncl, s));
-  return MPASG_OK;
+  const ZeroSpan zs[] = {{g->ru_p, nel}, {g->rw_p, ncw}, {g->rho_pp, ncl}, {g->rtheta_pp, ncl}, {g->rtheta_pp_old, ncl}};
+  return mpasgi_zero_many(zs, 5, s);
 }
 
 // the reverse pass of one step from its tape (f supplies the static fields: base state,
@@ -393,9 +443,12 @@ int step_reverse(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields*
         --a;
         mpasg_fields ac = pre;
         aco_view(T, ac, a);
-        const double* in = T.ac(a);
+        // the substep's inputs rtheta_pp and rw_p: the previous substep's outputs (the first
+        // substep of a stage starts from zero and reads neither)
+        const double* prev = T.aco(small > 1 ? a - 1 : a);
         CHECK_RC(mpasgi_divdamp_vjp_core(m, c, &ac, g, dts, w, s));
-        CHECK_RC(mpasgi_acoustic_vjp_rev(m, c, &ac, g, t, small, dts, in + T.E + T.C, in + T.E + 2 * T.C, w, s));
+        CHECK_RC(mpasgi_acoustic_vjp_rev(m, c, &ac, g, t, small, dts, prev + T.E + 2 * T.W + T.C, prev + T.E + T.W,
+                                         w, s));
       }
       CHECK_RC(mpasgi_smlstep_vjp_core(m, g, s));
       CHECK_RC(mpasgi_dyn_tend_vjp_core(m, c, &pre, g, t, rk, w, s));

@@ -45,6 +45,69 @@ __global__ void k_vimp_factor_vjp(mpasg_mesh m, mpasg_fields f, mpasg_fields g, 
   gc[o] = 0.0;
 }
 
+// The same with 32 columns staged through shared memory ([level][33] layout, coalesced
+// copies by 4 warps, the sweeps on the first warp), as the forward factorisation does.
+constexpr int kFacCols = 32;
+constexpr int kFacPitch = kFacCols + 1;
+constexpr int kFacThreads = 128;
+
+__global__ void __launch_bounds__(kFacThreads) k_vimp_factor_vjp_staged(mpasg_mesh m, mpasg_fields f, mpasg_fields g,
+                                                                        FastDiv fl, double* __restrict__ gb,
+                                                                        double* __restrict__ gc) {
+  extern __shared__ double sm[];
+  const int L = m.nVertLevels;
+  const size_t plane = (size_t)L * kFacPitch;
+  double* s_gg = sm;              // gamma's cotangent in, c's out
+  double* s_gal = sm + plane;     // alpha's cotangent in, b's out
+  double* s_al = sm + 2 * plane;
+  double* s_c = sm + 3 * plane;
+  double* s_gam = sm + 4 * plane;
+  double* s_a = sm + 5 * plane;
+  double* s_ga = sm + 6 * plane;
+  const int c0 = blockIdx.x * kFacCols;
+  const int ncol = min(kFacCols, m.nCells - c0);
+  const int t = threadIdx.x;
+  const uint32_t nl = (uint32_t)ncol * L;
+  const size_t o0 = (size_t)c0 * L;
+  for (uint32_t idx = t; idx < nl; idx += kFacThreads) {
+    const uint32_t col = fl.div(idx), k = idx - col * L;
+    const size_t q = k * kFacPitch + col;
+    s_gg[q] = g.gamma_tri[o0 + idx];
+    s_gal[q] = g.alpha_tri[o0 + idx];
+    s_al[q] = f.alpha_tri[o0 + idx];
+    s_c[q] = f.c_tri[o0 + idx];
+    s_gam[q] = f.gamma_tri[o0 + idx];
+    s_a[q] = f.a_tri[o0 + idx];
+    s_ga[q] = 0.0;
+  }
+  __syncthreads();
+  if (t < ncol) {
+    double carry = 0.0;
+    for (int k = L - 1; k >= 1; --k) {
+      const size_t q = k * kFacPitch + t;
+      const double ag = s_gg[q] + carry;
+      const double al = s_al[q];
+      s_gg[q] = ag * al;
+      const double d = -(s_gal[q] + ag * s_c[q]) * al * al;
+      s_gal[q] = d;
+      s_ga[q] = -d * s_gam[q - kFacPitch];
+      carry = -d * s_a[q];
+    }
+    s_gg[t] = 0.0;
+    s_gal[t] = 0.0;
+  }
+  __syncthreads();
+  for (uint32_t idx = t; idx < nl; idx += kFacThreads) {
+    const uint32_t col = fl.div(idx), k = idx - col * L;
+    const size_t q = k * kFacPitch + col;
+    gc[o0 + idx] = s_gg[q];
+    gb[o0 + idx] = s_gal[q];
+    g.a_tri[o0 + idx] += s_ga[q];
+  }
+}
+
+size_t vimp_factor_vjp_smem_bytes(int L) { return (size_t)7 * L * kFacPitch * sizeof(double); }
+
 // a / b / c diagonals (vert_imp_coefs.py:388-428) read backwards: total cotangents of
 // cofwz (levels 1..L-1), coftz (0..L) and cofwt (0..L-1), written to wz / tz / wt.
 __global__ void k_vimp_diag_vjp(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl1,
@@ -182,7 +245,8 @@ __global__ void k_ac_vjp_post(mpasg_mesh m, mpasg_fields f, mpasg_fields g, Fast
 // Thomas sweeps (autodiff/tridiagonal_solve.py:232-291) transposed for one column: xb
 // holds the solution's cotangent on entry and the right-hand side's on return; the a, alpha
 // and gamma cotangents accumulate into ga / gal / gg.  The forward-elimination values come
-// back from the solution: u_k = x_k + gamma_k x_(k+1) and t_k = rhs_k - a_k u_(k-1) = u_k / alpha_k.
+// back from the solution: u_k = x_k + gamma_k x_(k+1) and t_k = rhs_k - a_k u_(k-1) = u_k / alpha_k,
+// with 1 / alpha_k by the Newton-refined reciprocal (common.cuh; within 2 ulp, no division).
 // Strides: xs / xbs for the (L+1)-level arrays, cs for the L-level ones.
 MPASG_D void solve_vjp_column(int L, const double* x, int xs, double* xb, int xbs, const double* a,
                               const double* al, const double* gam, int cs, double* ga, double* gal, double* gg) {
@@ -198,7 +262,7 @@ MPASG_D void solve_vjp_column(int L, const double* x, int xs, double* xb, int xb
     const double au = xb[k * xbs] + carry;
     const double u_k = x[k * xs] + gam[k * cs] * x[(k + 1) * xs];
     const double u_km1 = x[(k - 1) * xs] + gam[(k - 1) * cs] * x[k * xs];
-    gal[k * cs] += au * (u_k / al[k * cs]);
+    gal[k * cs] += au * (u_k * rcp_nr(al[k * cs]));
     const double at = au * al[k * cs];
     xb[k * xbs] = at;
     ga[k * cs] += -at * u_km1;
@@ -473,12 +537,13 @@ __global__ void k_recover_vjp_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g
   const uint32_t e = fl.div(i);
   const int k = (int)(i - e * L);
   const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-  const double den = f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k];
+  // one reciprocal of the edge density sum (float64 division is a long instruction sequence)
+  const double rden = 1.0 / (f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k]);
   const double gu = g.u[i];
-  const double gru = g.ru[i] + gu * 2.0 / den;
+  const double gru = g.ru[i] + gu * 2.0 * rden;
   g.ru_save[i] += gru;
   g.ru_p[i] += gru;
-  pden[i] = -gu * f.u[i] / den;
+  pden[i] = -gu * f.u[i] * rden;
   g.u[i] = 0.0;
   g.ru[i] = 0.0;
 }
@@ -497,7 +562,7 @@ __global__ void k_recover_vjp_wlev(mpasg_mesh m, mpasg_fields f, mpasg_fields g,
     const double rho_i = m.fzm[k] * f.rho_zz[o] + m.fzp[k] * f.rho_zz[o - 1];
     const double zz_i = m.fzm[k] * m.zz[o] + m.fzp[k] * m.zz[o - 1];
     const double wmb = gw / rho_i;
-    rib = -gw * f.w[i] / rho_i;
+    rib = -wmb * f.w[i];
     rwpb = (zz_i == 1.0 ? wmb : wmb / zz_i) + g.rw[i];
     g.rw_save[i] += rwpb;
   }
@@ -517,7 +582,8 @@ __global__ void k_recover_vjp_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields g
   const size_t o = i, ow = (size_t)c * (L + 1) + k;
   const double rz = f.rho_zz[o], th = f.theta_m[o], rtp = f.rtheta_p[o], rtb = f.rtheta_base[o];
   const double gth = g.theta_m[o];
-  double rtpb = g.rtheta_p[o] + gth / rz;
+  const double gthr = gth / rz;
+  double rtpb = g.rtheta_p[o] + gthr;
   if (rk_step == 3) {
     const double rcv = kRgas / (kCp - kRgas);
     const double zz = m.zz[o], ex = f.exner[o];
@@ -528,7 +594,7 @@ __global__ void k_recover_vjp_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields g
     g.exner[o] = 0.0;
     g.pressure_p[o] = 0.0;
   }
-  double rzb = g.rho_zz[o] - gth * th / rz;
+  double rzb = g.rho_zz[o] - gthr * th;
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
   for (int j = 0; j < n; ++j) rzb += pden[(size_t)m.edgesOnCell[c * me + j] * L + k];
@@ -569,6 +635,39 @@ int dcopy(double* d, const double* src, long long n, cudaStream_t s) {
 }  // namespace
 
 int mpasgi_zero(double* p, long long n, cudaStream_t s) { return zero(p, n, s); }
+
+namespace {
+struct ZeroList {
+  double* p[kZeroSpans];
+  long long n[kZeroSpans];
+};
+// blockIdx.y picks the array; a grid-stride loop over its length
+__global__ void k_zero_many(ZeroList z) {
+  double* p = z.p[blockIdx.y];
+  const long long n = z.n[blockIdx.y];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] = 0.0;
+}
+}  // namespace
+
+int mpasgi_zero_many(const ZeroSpan* spans, int count, cudaStream_t s) {
+  for (int b = 0; b < count; b += kZeroSpans) {
+    ZeroList z{};
+    long long nmax = 0;
+    const int k = count - b < kZeroSpans ? count - b : kZeroSpans;
+    for (int j = 0; j < k; ++j) {
+      z.p[j] = spans[b + j].p;
+      z.n[j] = spans[b + j].n;
+      if (z.n[j] > nmax) nmax = z.n[j];
+    }
+    if (nmax <= 0) continue;
+    long long gx = (nmax + kBlock - 1) / kBlock;
+    if (gx > 1216) gx = 1216;  // 8 blocks per SM of 152, grid-stride beyond
+    k_zero_many<<<dim3((unsigned)gx, (unsigned)k), kBlock, 0, s>>>(z);
+    MPASG_LAUNCH_CHECK();
+  }
+  return MPASG_OK;
+}
 
 // ================================================================= internal cores
 // The acoustic substep's forward pass for its reverse mode: keeps the substep's inputs
@@ -670,19 +769,28 @@ int mpasgi_vimp_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg
   const long long ncl = (long long)m->nCells * L, ncw = (long long)m->nCells * (L + 1);
   double* gb = w.c[8];
   double* gc = w.c[9];
-  k_vimp_factor_vjp<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f, *g, gb, gc);
+  // the staged kernel needs more than 48 KB of dynamic shared memory: opt in once per device
+  // (the first call on a device should come before any stream capture)
+  const size_t smem = vimp_factor_vjp_smem_bytes(L);
+  static bool opt_in[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MPASG_E_CUDA;
+  if (!opt_in[dev])
+    opt_in[dev] = cudaFuncSetAttribute(k_vimp_factor_vjp_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       200 * 1024) == cudaSuccess;
+  if (opt_in[dev] && smem <= 200 * 1024)
+    k_vimp_factor_vjp_staged<<<nblocks(m->nCells, kFacCols), kFacThreads, smem, s>>>(*m, *f, *g, FastDiv(L), gb, gc);
+  else
+    k_vimp_factor_vjp<<<nblocks(m->nCells, 64), 64, 0, s>>>(*m, *f, *g, gb, gc);
   MPASG_LAUNCH_CHECK();
   k_vimp_diag_vjp<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, *g, FastDiv(L + 1), gb, gc, w.c[10], w.c[11], w.c[7]);
   MPASG_LAUNCH_CHECK();
   k_vimp_coef_vjp<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, *g, FastDiv(L), dts, c->epssm, w.c[10], w.c[11], w.c[7]);
   MPASG_LAUNCH_CHECK();
   // the coefficients' cotangents are consumed
-  CHECK_RC(zero(g->cofwz, ncl, s));
-  CHECK_RC(zero(g->coftz, ncw, s));
-  CHECK_RC(zero(g->cofwt, ncl, s));
-  CHECK_RC(zero(g->a_tri, ncl, s));
-  CHECK_RC(zero(g->alpha_tri, ncl, s));
-  CHECK_RC(zero(g->gamma_tri, ncl, s));
+  const ZeroSpan zs[] = {{g->cofwz, ncl}, {g->coftz, ncw}, {g->cofwt, ncl},
+                         {g->a_tri, ncl}, {g->alpha_tri, ncl}, {g->gamma_tri, ncl}};
+  CHECK_RC(mpasgi_zero_many(zs, 6, s));
   return MPASG_OK;
 }
 

@@ -294,11 +294,10 @@ int mpasgi_diag_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg
   k_dadj_hedge<<<nblocks(ncl), kBlock, 0, s>>>(*m, *g, fl);
   MPASG_LAUNCH_CHECK();
   // the stage's outputs are consumed
-  CHECK_RC(mpasgi_zero(g->h_edge, (m->nEdges + 1LL) * L, s));
-  CHECK_RC(mpasgi_zero(g->pv_edge, (m->nEdges + 1LL) * L, s));
-  CHECK_RC(mpasgi_zero(g->divergence, (m->nCells + 1LL) * L, s));
-  CHECK_RC(mpasgi_zero(g->ke, (m->nCells + 1LL) * L, s));
-  CHECK_RC(mpasgi_zero(g->vorticity, (m->nVertices + 1LL) * L, s));
+  const ZeroSpan zs[] = {{g->h_edge, (m->nEdges + 1LL) * L}, {g->pv_edge, (m->nEdges + 1LL) * L},
+                         {g->divergence, (m->nCells + 1LL) * L}, {g->ke, (m->nCells + 1LL) * L},
+                         {g->vorticity, (m->nVertices + 1LL) * L}};
+  CHECK_RC(mpasgi_zero_many(zs, 5, s));
   return MPASG_OK;
 }
 

@@ -282,17 +282,29 @@ __global__ void k_tadj_wres(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDi
 // the theta flux of the change of ru within the dynamics substep).  Writes the cotangents
 // of the stencil sums (fltb, flwb) for the cell gather, adds to ru, ru_save and the
 // edge-sum cotangent of theta_m_save.
-__global__ void k_tadj_adv_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpasg_transpose t, FastDiv fl,
-                                 AdjTendScalars p, const double* __restrict__ tt1b, const double* __restrict__ tw1b,
-                                 double* __restrict__ fltb, double* __restrict__ flwb) {
+// sgn_x >= 0 by the bits (no float64 comparison): true for +0 and -0
+MPASG_D bool nonneg(double x) {
+  const long long b = __double_as_longlong(x);
+  return b >= 0 || b == (long long)0x8000000000000000ull;
+}
+
+// Each thread forms the w stencil sum of its own level k once and shares the product with
+// its flux cotangent; level k also needs level k+1's (shared memory, recomputed at the
+// block's edge).  The upwind sides of the theta and w stencils are stored as bits in sel
+// for the cell gather.
+__global__ void __launch_bounds__(kBlock) k_tadj_adv_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g,
+                                                           mpasg_transpose t, FastDiv fl, AdjTendScalars p,
+                                                           const double* __restrict__ tt1b,
+                                                           const double* __restrict__ tw1b, double* __restrict__ fltb,
+                                                           double* __restrict__ flwb, uint8_t* __restrict__ sel) {
+  __shared__ double s_pw[kBlock];
   const int L = m.nVertLevels;
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint32_t)m.nEdges * L) return;
-  const uint32_t e = fl.div(i);
-  const int k = (int)(i - e * L);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < (uint32_t)m.nEdges * L;
   const int me = m.maxEdges, na = m.nAdvMax;
-  const int nadv = m.nAdvCellsForEdge[e];
-  const int32_t* cells = m.advCellsForEdge + (size_t)e * na;
+  uint32_t e = 0;
+  int k = 0, nadv = 0;
+  const int32_t* cells = m.advCellsForEdge;
   // cotangents of the edge fluxes from the two cells' sums (x = -sign * flux)
   auto edge_b = [&](const double* src, int kk, size_t pitch) {
     double s = 0.0;
@@ -300,12 +312,12 @@ __global__ void k_tadj_adv_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g, m
       const int j = t.edgeCellSlot[2 * e + q];
       if (j < 0) continue;
       const int c = m.cellsOnEdge[2 * e + q];
-      s += -src[(size_t)c * pitch + kk] * m.edgesOnCell_sign[c * me + j];
+      s -= src[(size_t)c * pitch + kk] * m.edgesOnCell_sign[c * me + j];
     }
     return s;
   };
-  auto adv_sum = [&](const double* fld, int kk, size_t pitch, double sel) {
-    const double* cf = (sel >= 0.0 ? m.adv_coefs_p : m.adv_coefs_m) + (size_t)e * na;
+  auto adv_sum = [&](const double* fld, int kk, size_t pitch, bool up) {
+    const double* cf = (up ? m.adv_coefs_p : m.adv_coefs_m) + (size_t)e * na;
     double acc = 0.0;
     for (int a = 0; a < nadv; ++a) {
       const double tt = cf[a] * fld[(size_t)cells[a] * pitch + kk];
@@ -313,32 +325,50 @@ __global__ void k_tadj_adv_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g, m
     }
     return acc;
   };
+  auto ru_w = [&](int kk) { return m.fzm[kk] * f.ru[(size_t)e * L + kk] + m.fzp[kk] * f.ru[(size_t)e * L + kk - 1]; };
+  auto w_part = [&](int kk, bool* up) {  // fweb_kk * sum_a cf_a w_a, and the flux cotangent's product
+    const double rwk = ru_w(kk);
+    *up = nonneg(rwk);
+    return edge_b(tw1b, kk, L + 1) * adv_sum(f.w, kk, L + 1, *up);
+  };
+  double pw = 0.0;
+  bool up_w = true;
+  if (active) {
+    e = fl.div(i);
+    k = (int)(i - e * L);
+    nadv = m.nAdvCellsForEdge[e];
+    cells = m.advCellsForEdge + (size_t)e * na;
+    if (k >= 1) pw = w_part(k, &up_w);
+  }
+  s_pw[threadIdx.x] = pw;
+  __syncthreads();
+  if (!active) return;
   const double rue = f.ru[i];
+  const bool up_t = nonneg(rue);
   // theta
   const double fteb = edge_b(tt1b, k, L);
-  double gru = fteb * adv_sum(f.theta_m, k, L, rue);
+  double gru = fteb * adv_sum(f.theta_m, k, L, up_t);
   fltb[i] = fteb * rue;
   // w at level k (k >= 1) and k + 1: ru_w = fzm ru_k + fzp ru_(k-1)
-  auto ru_w = [&](int kk) { return m.fzm[kk] * f.ru[(size_t)e * L + kk] + m.fzp[kk] * f.ru[(size_t)e * L + kk - 1]; };
   if (k >= 1) {
-    const double fweb = edge_b(tw1b, k, L + 1);
-    const double rw_k = ru_w(k);
-    gru += fweb * adv_sum(f.w, k, L + 1, rw_k) * m.fzm[k];
-    flwb[i] = fweb * rw_k;
+    gru += pw * m.fzm[k];
+    flwb[i] = edge_b(tw1b, k, L + 1) * ru_w(k);
   } else {
     flwb[i] = 0.0;
   }
   if (k + 1 <= L - 1) {
-    const double fweb = edge_b(tw1b, k + 1, L + 1);
-    gru += fweb * adv_sum(f.w, k + 1, L + 1, ru_w(k + 1)) * m.fzp[k + 1];
+    bool dummy;
+    const double pw1 = threadIdx.x + 1 < blockDim.x ? s_pw[threadIdx.x + 1] : w_part(k + 1, &dummy);
+    gru += pw1 * m.fzp[k + 1];
   }
+  sel[i] = (uint8_t)((up_t ? 1 : 0) | (k >= 1 && up_w ? 2 : 0));
   if (p.rk_step > 1) {  // - sum_j (sign dvEdge)_j (ru_save - ru) theta_edge_save
     double s_sdv = 0.0;
     for (int q = 0; q < 2; ++q) {
       const int j = t.edgeCellSlot[2 * e + q];
       if (j < 0) continue;
       const int c = m.cellsOnEdge[2 * e + q];
-      s_sdv += -tt1b[(size_t)c * L + k] * m.cell_edge_sdv[c * me + j];
+      s_sdv -= tt1b[(size_t)c * L + k] * m.cell_edge_sdv[c * me + j];
     }
     const double the = f.theta_edge_save[i];
     g.ru_save[i] += s_sdv * the;
@@ -348,128 +378,165 @@ __global__ void k_tadj_adv_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g, m
   g.ru[i] += gru;
 }
 
-// ---- cells: the advection stencils transposed (CSR of (edge, slot) readers): theta, w
-__global__ void k_tadj_adv_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpasg_transpose t, FastDiv fl1,
-                                 const double* __restrict__ fltb, const double* __restrict__ flwb) {
+// ---- cells: the advection stencils transposed (CSR of (edge, slot) readers): theta, w;
+// the upwind sides come from sel (bit 0 theta, bit 1 w)
+__global__ void k_tadj_adv_cells(mpasg_mesh m, mpasg_fields g, mpasg_transpose t, FastDiv fl1, FastDiv fna,
+                                 const double* __restrict__ fltb, const double* __restrict__ flwb,
+                                 const uint8_t* __restrict__ sel) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)m.nCells * (L + 1)) return;
   const uint32_t c = fl1.div(i);
   const int k = (int)(i - c * (L + 1));
-  const int na = m.nAdvMax;
   double gth = 0.0, gw = 0.0;
   const int p0 = t.advPtr[c], p1 = t.advPtr[c + 1];
+  const bool th = k < L, wl = k >= 1 && k <= L - 1;
   for (int q = p0; q < p1; ++q) {
     const int es = t.advIdx[q];
-    const int e = es / na;
-    const size_t ie = (size_t)e * L;
-    if (k < L) {
-      const double cf = f.ru[ie + k] >= 0.0 ? m.adv_coefs_p[es] : m.adv_coefs_m[es];
-      gth += cf * fltb[ie + k];
-    }
-    if (k >= 1 && k <= L - 1) {
-      const double rwk = m.fzm[k] * f.ru[ie + k] + m.fzp[k] * f.ru[ie + k - 1];
-      const double cf = rwk >= 0.0 ? m.adv_coefs_p[es] : m.adv_coefs_m[es];
-      gw += cf * flwb[ie + k];
+    const uint32_t e = fna.div((uint32_t)es);
+    const size_t ie = (size_t)e * L + k;
+    const double cp = m.adv_coefs_p[es], cm = m.adv_coefs_m[es];
+    if (th) {
+      const uint8_t b = sel[ie];
+      gth += ((b & 1) ? cp : cm) * fltb[ie];
+      if (wl) gw += ((b & 2) ? cp : cm) * flwb[ie];
     }
   }
-  if (k < L) g.theta_m[(size_t)c * L + k] += gth;
+  if (th) g.theta_m[(size_t)c * L + k] += gth;
   g.w[i] += gw;
 }
 
 // ---- edges: the u tendency read backwards (vertical transport, PV flux, kinetic-energy
 // gradient, divergence coupling; at rk 1 the pressure gradient and del2 / del4 mixing)
-__global__ void k_tadj_u(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpasg_transpose t, FastDiv fl,
-                         AdjTendScalars p, const double* __restrict__ hd, const double* __restrict__ kd,
-                         const double* __restrict__ ud, const double* __restrict__ dsd, const double* __restrict__ dsv,
-                         double* __restrict__ pke, double* __restrict__ phd, double* __restrict__ prwe,
-                         double* __restrict__ ppp, double* __restrict__ pkd, double* __restrict__ udb,
-                         double* __restrict__ pd4) {
+// qa = G rho_edge per edge level: the cotangent of the PV flux q of that edge, which every
+// TRiSK neighbour of the edge reads
+__global__ void k_tadj_qa(int n, const double* __restrict__ gtu, const double* __restrict__ h,
+                          double* __restrict__ qa) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) qa[i] = gtu[i] * h[i];
+}
+
+// The vertical-transport part per interface q of the edge: its flux's cotangent
+// b_q = rdzw_q G_q - rdzw_(q-1) G_(q-1) times the flux's partials with respect to u at
+// levels q-2 .. q+1 (c[0..3]; the second-order interfaces q = 1, L-1 read q-1, q only),
+// and with respect to the interface's rw mean (pr)
+struct WduzPart {
+  double c[4];
+  double pr;
+};
+MPASG_D WduzPart wduz_part(const mpasg_mesh& m, const mpasg_fields& f, const double* ue, const double* Gtu, int c1,
+                           int c2, int q, int L) {
+  WduzPart w = {{0.0, 0.0, 0.0, 0.0}, 0.0};
+  if (q < 1 || q > L - 1) return w;
+  double b = 0.0;
+  if (q <= L - 1) b += Gtu[q] * m.rdzw[q];
+  b -= Gtu[q - 1] * m.rdzw[q - 1];
+  const double rwe = 0.5 * (f.rw[(size_t)c1 * (L + 1) + q] + f.rw[(size_t)c2 * (L + 1) + q]);
+  if (q == 1 || q == L - 1) {
+    const double br = b * rwe;
+    w.c[2] = br * m.fzm[q];
+    w.c[1] = br * m.fzp[q];
+    w.pr = b * (m.fzm[q] * ue[q] + m.fzp[q] * ue[q - 1]);
+    return w;
+  }
+  const Flux3Grad d = flux3_grad(ue[q - 2], ue[q - 1], ue[q], ue[q + 1], rwe, 1.0);
+  w.c[0] = b * d.qm2;
+  w.c[1] = b * d.qm1;
+  w.c[2] = b * d.q0;
+  w.c[3] = b * d.qp1;
+  w.pr = b * d.ua;
+  return w;
+}
+
+// Each thread forms the parts of its own interface k once; level k collects c[3], c[2],
+// c[1], c[0] of interfaces k-1, k, k+1, k+2 from its neighbours in the block (shared
+// memory), recomputing the few that fall outside it.
+__global__ void __launch_bounds__(kBlock) k_tadj_u(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpasg_transpose t,
+                                                   FastDiv fl, AdjTendScalars p, const double* __restrict__ hd,
+                                                   const double* __restrict__ kd, const double* __restrict__ ud,
+                                                   const double* __restrict__ dsd, const double* __restrict__ dsv,
+                                                   double* __restrict__ pke, double* __restrict__ phd,
+                                                   double* __restrict__ prwe, double* __restrict__ ppp,
+                                                   double* __restrict__ pkd, double* __restrict__ udb,
+                                                   double* __restrict__ pd4, const double* __restrict__ qa) {
+  __shared__ double s_c[4][kBlock];
   const int L = m.nVertLevels;
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (uint32_t)m.nEdges * L) return;
-  const uint32_t e = fl.div(i);
-  const int k = (int)(i - e * L);
-  const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < (uint32_t)m.nEdges * L;
+  uint32_t e = 0;
+  int k = 0, c1 = 0, c2 = 0;
+  const double* ue = f.u;
+  const double* Gtu = g.tend_u;
+  WduzPart own = {{0.0, 0.0, 0.0, 0.0}, 0.0};
+  if (active) {
+    e = fl.div(i);
+    k = (int)(i - e * L);
+    c1 = m.cellsOnEdge[2 * e];
+    c2 = m.cellsOnEdge[2 * e + 1];
+    ue = f.u + (size_t)e * L;
+    Gtu = g.tend_u + (size_t)e * L;
+    own = wduz_part(m, f, ue, Gtu, c1, c2, k, L);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) s_c[j][threadIdx.x] = own.c[j];
+  __syncthreads();
+  if (!active) return;
   const size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
-  const double* ue = f.u + (size_t)e * L;
-  const double* Gtu = g.tend_u + (size_t)e * L;
   const double G = Gtu[k];
   const double rho_e = f.h_edge[i];
   const double inv_dc = m.invDcEdge[e];
   // PV flux q_e = 0.5 sum_j w_j u_j (pv_e + pv_j), with its transpose over edgesOnEdge: the
   // neighbour eo's sum reads u_e and pv_e at its slot jt (cotangent of q_eo: G_eo rho_edge_eo)
+  // four sums over the stencil, combined after the loop (six float64 operations per slot):
+  // s1 = sum w u, s2 = sum w u pv, s3 = sum A wt, s4 = sum A wt pv, A = G_eo rho_edge_eo
   const int n2 = m.nEdgesOnEdge[e], me2 = m.maxEdges2;
   const double pv_self = f.pv_edge[i], u_self = ue[k];
-  const double qbe = G * rho_e;
-  double q = 0.0, gpv = 0.0, gu_pv = 0.0;
+  double s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = 0.0;
   for (int j = 0; j < n2; ++j) {
     const int eo = m.edgesOnEdge[e * me2 + j];
     const size_t io = (size_t)eo * L + k;
-    const double w_j = m.weightsOnEdge[e * me2 + j];
-    const double u_o = f.u[io], pv_o = f.pv_edge[io];
-    const double tq = (w_j * u_o) * (pv_self + pv_o);
-    q = (j == 0) ? tq : q + tq;
-    gpv += qbe * w_j * u_o * 0.5;
+    const double pv_o = f.pv_edge[io];
+    const double wu = m.weightsOnEdge[e * me2 + j] * f.u[io];
+    s1 += wu;
+    s2 += wu * pv_o;
     const int jt = t.eoeTransSlot[e * me2 + j];
     if (jt < 0) continue;
-    const double wt = m.weightsOnEdge[(size_t)eo * me2 + jt];
-    const double qbo = g.tend_u[io] * f.h_edge[io];
-    gu_pv += qbo * wt * 0.5 * (pv_o + pv_self);
-    gpv += qbo * wt * u_self * 0.5;
+    const double aw = qa[io] * m.weightsOnEdge[(size_t)eo * me2 + jt];
+    s3 += aw;
+    s4 += aw * pv_o;
   }
-  q = 0.5 * q;
+  const double q = 0.5 * (pv_self * s1 + s2);
   double gh = G * (q - (f.ke[i2] - f.ke[i1]) * inv_dc);
   pke[i] = G * rho_e * inv_dc;
-  double gu = -G * 0.5 * (hd[i1] + hd[i2]) + gu_pv;
-  g.pv_edge[i] += gpv;
-  phd[i] = -G * ue[k] * 0.5;
-  // vertical transport: tu_k = -rdzw_k (wduz_(k+1) - wduz_k)
-  auto wduzb = [&](int qq) {
-    double b = 0.0;
-    if (qq <= L - 1) b += Gtu[qq] * m.rdzw[qq];
-    if (qq - 1 >= 0) b -= Gtu[qq - 1] * m.rdzw[qq - 1];
-    return b;
-  };
-  auto rwe = [&](int qq) {
-    return 0.5 * (f.rw[(size_t)c1 * (L + 1) + qq] + f.rw[(size_t)c2 * (L + 1) + qq]);
-  };
+  double gu = -G * 0.5 * (hd[i1] + hd[i2]) + 0.5 * (pv_self * s3 + s4);
+  g.pv_edge[i] += 0.5 * (G * rho_e * s1 + u_self * s3);
+  phd[i] = -G * u_self * 0.5;
+  // vertical transport: interfaces k-1 .. k+2 of this edge
   for (int qq = k - 1; qq <= k + 2; ++qq) {
     if (qq < 1 || qq > L - 1) continue;
-    const double b = wduzb(qq);
-    if (b == 0.0) continue;
-    if (qq == 1 || qq == L - 1) {
-      if (k == qq) gu += b * rwe(qq) * m.fzm[qq];
-      if (k == qq - 1) gu += b * rwe(qq) * m.fzp[qq];
-    } else {
-      const Flux3Grad d = flux3_grad(ue[qq - 2], ue[qq - 1], ue[qq], ue[qq + 1], rwe(qq), 1.0);
-      const double dq[4] = {d.qm2, d.qm1, d.q0, d.qp1};
-      gu += b * dq[k - (qq - 2)];
-    }
-  }
-  // cotangent of the edge's interface rw (w level k, 1..L-1)
-  double pr = 0.0;
-  if (k >= 1 && k <= L - 1) {
-    const double b = wduzb(k);
-    if (k == 1 || k == L - 1)
-      pr = b * (m.fzm[k] * ue[k] + m.fzp[k] * ue[k - 1]);
+    const int lane = (int)threadIdx.x + (qq - k);
+    const int slot = k - (qq - 2);
+    if (lane >= 0 && lane < (int)blockDim.x)
+      gu += s_c[slot][lane];
     else
-      pr = b * flux3_grad(ue[k - 2], ue[k - 1], ue[k], ue[k + 1], rwe(k), 1.0).ua;
+      gu += wduz_part(m, f, ue, Gtu, c1, c2, qq, L).c[slot];
   }
-  prwe[i] = pr;
+  prwe[i] = (k >= 1 && k <= L - 1) ? own.pr : 0.0;
   if (p.rk_step == 1) {
     const double teub = G + g.tend_u_euler[i];
     const double zzm = 0.5 * (m.zz[i2] + m.zz[i1]);
-    ppp[i] = -teub * f.cqu_e[i] * inv_dc / zzm;
+    const double pg = -teub * f.cqu_e[i] * inv_dc;
+    ppp[i] = zzm == 1.0 ? pg : pg / zzm;
     const int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
     const double r_dv = fmin(m.invDvEdge[e], 4.0 * inv_dc);
     const double u_diff = (f.divergence[i2] - f.divergence[i1]) * inv_dc -
                           (f.vorticity[(size_t)v2 * L + k] - f.vorticity[(size_t)v1 * L + k]) * r_dv;
     const double kdiffu = 0.5 * (kd[i1] + kd[i2]);
     const double msd2 = m.meshScalingDel2[e];
-    gh += teub * kdiffu * u_diff * msd2;
-    pkd[i] = 0.5 * teub * rho_e * u_diff * msd2;
-    udb[i] = teub * rho_e * kdiffu * msd2;
+    const double tm = teub * msd2;
+    gh += tm * kdiffu * u_diff;
+    pkd[i] = 0.5 * tm * rho_e * u_diff;
+    udb[i] = tm * rho_e * kdiffu;
     if (p.del4) {
       const double u_mix = m.meshScalingDel4[e] * p.h_mom_visc4;
       const double r_dc4 = u_mix * p.del4u_div * inv_dc;
@@ -931,12 +998,16 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
     k_tadj_wres<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, *g, fl, tweb);
     MPASG_LAUNCH_CHECK();
   }
-  k_tadj_adv_edges<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, p, tt1b, tw1b, fltb, flwb);
+  uint8_t* sel = reinterpret_cast<uint8_t*>(w.e[2]);  // (E+1) x L bytes within one edge array
+  k_tadj_adv_edges<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, p, tt1b, tw1b, fltb, flwb, sel);
   MPASG_LAUNCH_CHECK();
-  k_tadj_adv_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, *g, *t, fl1, fltb, flwb);
+  k_tadj_adv_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *g, *t, fl1, FastDiv(m->nAdvMax), fltb, flwb, sel);
+  MPASG_LAUNCH_CHECK();
+  double* qa = w.e[2];  // sel's bytes (read by the advection gather above) are no longer needed
+  k_tadj_qa<<<nblocks(nel), kBlock, 0, s>>>((int)nel, g->tend_u, f->h_edge, qa);
   MPASG_LAUNCH_CHECK();
   k_tadj_u<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, p, hd, kd, ud, dsd, dsv, pke, phd, prwe, ppp, pkd,
-                                          udb, pd4);
+                                          udb, pd4, qa);
   MPASG_LAUNCH_CHECK();
   k_tadj_u_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *g, fl1, p, pke, phd, prwe, ppp, pkd, pd4, hdb, kdb, dsdb);
   MPASG_LAUNCH_CHECK();
@@ -975,15 +1046,11 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   MPASG_LAUNCH_CHECK();
   // the stage's outputs are consumed; at rk 1 so are the Euler tendencies and tend_rho it
   // creates (later stages passed their cotangents through)
-  CHECK_RC(mpasgi_zero(g->tend_u, (m->nEdges + 1LL) * L, s));
-  CHECK_RC(mpasgi_zero(g->tend_w, (m->nCells + 1LL) * (L + 1), s));
-  CHECK_RC(mpasgi_zero(g->tend_theta, (m->nCells + 1LL) * L, s));
-  if (rk_step == 1) {
-    CHECK_RC(mpasgi_zero(g->tend_u_euler, (m->nEdges + 1LL) * L, s));
-    CHECK_RC(mpasgi_zero(g->tend_w_euler, (m->nCells + 1LL) * (L + 1), s));
-    CHECK_RC(mpasgi_zero(g->tend_theta_euler, (m->nCells + 1LL) * L, s));
-    CHECK_RC(mpasgi_zero(g->tend_rho, (m->nCells + 1LL) * L, s));
-  }
+  const ZeroSpan zs[] = {{g->tend_u, (m->nEdges + 1LL) * L}, {g->tend_w, (m->nCells + 1LL) * (L + 1)},
+                         {g->tend_theta, (m->nCells + 1LL) * L}, {g->tend_u_euler, (m->nEdges + 1LL) * L},
+                         {g->tend_w_euler, (m->nCells + 1LL) * (L + 1)}, {g->tend_theta_euler, (m->nCells + 1LL) * L},
+                         {g->tend_rho, (m->nCells + 1LL) * L}};
+  CHECK_RC(mpasgi_zero_many(zs, rk_step == 1 ? 7 : 3, s));
   return MPASG_OK;
 }
 
