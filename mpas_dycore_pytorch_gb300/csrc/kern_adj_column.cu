@@ -175,14 +175,16 @@ __global__ void k_vimp_coef_vjp(mpasg_mesh m, mpasg_fields f, mpasg_fields g, Fa
     gt += tz[ow + k + 1] * dtseps * m.fzp[k + 1];
   }
   const double q = f.qtot[o + k];
-  const double x = 0.5 * dtseps * rcv * m.zz[o + k] * kGravity * m.rho_base[o + k] / (1.0 + q);
+  const double x0 = 0.5 * dtseps * rcv * m.zz[o + k] * kGravity * m.rho_base[o + k];
+  const double x = q == 0.0 ? x0 : x0 / (1.0 + q);  // dry columns: no division
   const double pb = f.exner_base[o + k];
   const double den = (f.rtheta_base[o + k] + f.rtheta_p[o + k]) * pb;
   const double w = wt[o + k];
-  gp += w * x / den;
+  const double rden = 1.0 / den;
+  gp += w * x * rden;
   g.exner[o + k] += gp;
   g.theta_m[o + k] += gt;
-  g.rtheta_p[o + k] += w * (-x * f.exner[o + k] * pb / (den * den));
+  g.rtheta_p[o + k] += w * (-x * f.exner[o + k] * pb * rden * rden);
 }
 
 // ---------------------------------------------------------------- small-step perturbation
@@ -292,14 +294,13 @@ __global__ void __launch_bounds__(kSolveThreads) k_ac_vjp_solve_staged(mpasg_mes
                                                                        FastDiv fl, FastDiv fl1) {
   extern __shared__ double sm[];
   const int L = m.nVertLevels;
-  double* sx = sm;                                   // (L+1) x pitch
-  double* sb = sx + (size_t)(L + 1) * kSolvePitch;   // (L+1) x pitch
-  double* sa = sb + (size_t)(L + 1) * kSolvePitch;   // L x pitch each below
+  double* sx = sm;                                   // (L+1) x pitch: the solution x
+  double* sb = sx + (size_t)(L + 1) * kSolvePitch;   // (L+1) x pitch: xb in, the rhs cotangent out
+  double* s1 = sb + (size_t)(L + 1) * kSolvePitch;   // (L+1) x pitch: first sweep's values
+  double* sa = s1 + (size_t)(L + 1) * kSolvePitch;   // L x pitch each below
   double* sal = sa + (size_t)L * kSolvePitch;
   double* sg = sal + (size_t)L * kSolvePitch;
-  double* sga = sg + (size_t)L * kSolvePitch;
-  double* sgal = sga + (size_t)L * kSolvePitch;
-  double* sgg = sgal + (size_t)L * kSolvePitch;
+  double* s2 = sg + (size_t)L * kSolvePitch;         // second sweep's values before the alpha scaling
   const int c0 = blockIdx.x * kSolveCols;
   const int ncol = min(kSolveCols, m.nCells - c0);
   const int t = threadIdx.x;
@@ -315,14 +316,29 @@ __global__ void __launch_bounds__(kSolveThreads) k_ac_vjp_solve_staged(mpasg_mes
     sa[k * kSolvePitch + col] = f.a_tri[o0 + idx];
     sal[k * kSolvePitch + col] = f.alpha_tri[o0 + idx];
     sg[k * kSolvePitch + col] = f.gamma_tri[o0 + idx];
-    sga[k * kSolvePitch + col] = 0.0;
-    sgal[k * kSolvePitch + col] = 0.0;
-    sgg[k * kSolvePitch + col] = 0.0;
   }
   __syncthreads();
-  if (t < ncol)
-    solve_vjp_column(L, sx + t, kSolvePitch, sb + t, kSolvePitch, sa + t, sal + t, sg + t, kSolvePitch, sga + t,
-                     sgal + t, sgg + t);
+  // the two sweeps keep only their recurrences (solve_vjp_column's order of operations):
+  // au_k = xb_k - gamma_(k-1) au_(k-1) upwards, then au'_k = au_k + carry, xb_k = au'_k alpha_k,
+  // carry = -xb_k a_k downwards; the cotangents of a, alpha, gamma follow in parallel
+  if (t < ncol) {
+    double prev = 0.0;
+    for (int k = 0; k <= L; ++k) {
+      const double au = sb[k * kSolvePitch + t] - (k > 0 ? sg[(k - 1) * kSolvePitch + t] * prev : 0.0);
+      s1[k * kSolvePitch + t] = au;
+      prev = au;
+    }
+    double carry = 0.0;
+    for (int k = L - 1; k >= 1; --k) {
+      const double au = s1[k * kSolvePitch + t] + carry;
+      s2[k * kSolvePitch + t] = au;
+      const double at = au * sal[k * kSolvePitch + t];
+      sb[k * kSolvePitch + t] = at;
+      carry = -at * sa[k * kSolvePitch + t];
+    }
+    sb[L * kSolvePitch + t] = s1[L * kSolvePitch + t];
+    sb[t] = s1[t] + carry;
+  }
   __syncthreads();
   for (uint32_t idx = t; idx < nw; idx += kSolveThreads) {
     const uint32_t col = fl1.div(idx), k = idx - col * (L + 1);
@@ -330,13 +346,20 @@ __global__ void __launch_bounds__(kSolveThreads) k_ac_vjp_solve_staged(mpasg_mes
   }
   for (uint32_t idx = t; idx < nl; idx += kSolveThreads) {
     const uint32_t col = fl.div(idx), k = idx - col * L;
-    g.a_tri[o0 + idx] += sga[k * kSolvePitch + col];
-    g.alpha_tri[o0 + idx] += sgal[k * kSolvePitch + col];
-    g.gamma_tri[o0 + idx] += sgg[k * kSolvePitch + col];
+    const size_t q = k * kSolvePitch + col;
+    const double xk1 = sx[q + kSolvePitch];
+    g.gamma_tri[o0 + idx] += -s1[q] * xk1;
+    if (k >= 1) {
+      const double u_k = sx[q] + sg[q] * xk1;
+      const double u_km1 = sx[q - kSolvePitch] + sg[q - kSolvePitch] * sx[q];
+      const double au = s2[q];
+      g.alpha_tri[o0 + idx] += au * (u_k * rcp_nr(sal[q]));
+      g.a_tri[o0 + idx] += -(au * sal[q]) * u_km1;
+    }
   }
 }
 
-size_t solve_vjp_smem_bytes(int L) { return (size_t)(2 * (L + 1) + 6 * L) * kSolvePitch * sizeof(double); }
+size_t solve_vjp_smem_bytes(int L) { return (size_t)(3 * (L + 1) + 4 * L) * kSolvePitch * sizeof(double); }
 
 // The tridiagonal right-hand side (acoustic_step.py:675) and rs / ts read backwards, per
 // mass level: -> tend_theta, tend_rho, cofwz, cofwt, the rs / ts cotangents (rsb, tsb), the
@@ -460,12 +483,14 @@ __global__ void k_ac_vjp_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g, mpa
   const int c1 = m.cellsOnEdge[2 * e], c2i = m.cellsOnEdge[2 * e + 1];
   const size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2i * L + k;
   const double den = 0.5 * (m.zz[i2] + m.zz[i1]);
+  const double rden = den == 1.0 ? 1.0 : 1.0 / den;  // one division for both terms
   const double d = (rt_in[i2] - rt_in[i1]) * m.invDcEdge[e];
-  const double pg1 = den == 1.0 ? d : d / den;
+  const double pg1 = den == 1.0 ? d : d * rden;
   const double exs = f.exner[i1] + f.exner[i2];
   const double cqu = f.cqu_e[i];
   pex[i] = pg * cqu * 0.5 * c2 * pg1;
-  prt[i] = pg * cqu * 0.5 * c2 * exs / den * m.invDcEdge[e];
+  const double pe = pg * cqu * 0.5 * c2 * exs;
+  prt[i] = (den == 1.0 ? pe : pe * rden) * m.invDcEdge[e];
   prho[i] = pg * 0.5 * m.zxu[i] * kGravity;
 }
 
@@ -590,7 +615,7 @@ __global__ void k_recover_vjp_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields g
     const double gp = g.pressure_p[o];
     const double gex = g.exner[o] + gp * zz * kRgas * (rtp + rtb);
     const double E = zz * (kRgas / kP0) * (rtp + rtb);
-    rtpb += gp * zz * kRgas * ex + gex * rcv * ex / E * zz * (kRgas / kP0);
+    rtpb += gp * zz * kRgas * ex + gex * rcv * ex * (zz * (kRgas / kP0) / E);
     g.exner[o] = 0.0;
     g.pressure_p[o] = 0.0;
   }
