@@ -375,7 +375,11 @@ def measure_dynamics_vjp(args, dev):
     0.1 m/s sinusoidal w) with respect to the initial u and theta, by the hand-written
     reverse mode (preparation, 24 steps with a checkpoint each, the objective's gradient, 24
     reverse steps each recomputing its step with the tape, the preparation's reverse), against
-    the same 24 forward steps replayed from a CUDA graph; CUDA events on the stream."""
+    the same 24 forward steps replayed from a CUDA graph; CUDA events on the stream.  Beside
+    it: the same gradient with every step's tape kept (no recompute), the forward mode along
+    a seeded direction with the JVP/VJP identity of the functional, and the mixed form's
+    gradient against the float64 one."""
+    import numpy as np
     import torch
 
     from mpas_dycore_pytorch_gb300.api import Model
@@ -429,6 +433,47 @@ def measure_dynamics_vjp(args, dev):
     ms_none, g_none = timed("none")
     ms_step, grads = timed("step")
     same = all(bool(torch.equal(g_none[k], grads[k])) for k in ("u", "theta"))
+    # forward mode along a seeded direction of u and theta (preparation and 24 steps of
+    # values and tangents), and the JVP/VJP identity of the functional along it
+    from mpas_dycore_pytorch_gb300.dyn_adjoint import DynamicsTangent, run_jvp
+    tan = DynamicsTangent(m)
+    rng = np.random.default_rng(2)
+    pert = {}
+    for k, scale in (("u", 1.0), ("theta", 0.1)):
+        x = rng.standard_normal(tuple(np.asarray(st[k]).shape)) * scale
+        x[-1] = 0.0
+        pert[k] = torch.as_tensor(x)
+    ms_jvp = []
+    for rep in range(2):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        tans = run_jvp(m, st, nsteps, pert, tan)
+        b.record()
+        torch.cuda.synchronize()
+        ms_jvp.append(a.elapsed_time(b))
+    final = {k: v for k, v in m.export().items()}
+    g_out = cotangents(final)
+    dj_fwd = sum(float((g_out[k] * tans[k]).sum()) for k in g_out)
+    dj_rev = sum(float((grads[k][:-1].cpu() * pert[k][:-1]).sum()) for k in pert)
+    del tan
+    torch.cuda.empty_cache()
+    # the mixed form's gradient (its trajectory, linearised in float64) against the float64 one
+    cfg_mixed = dict(cfg, config_precision="mixed")
+    mm = Model(st, cfg_mixed, dt, num_scalars=1, device=dev)
+    adj_m = DynamicsAdjoint(mm)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g_mixed, _ = run_vjp(mm, st, nsteps, cotangents, adj_m, checkpoint="none")
+    a.record()
+    g_mixed, _ = run_vjp(mm, st, nsteps, cotangents, adj_m, checkpoint="none")
+    b.record()
+    torch.cuda.synchronize()
+    ms_mixed = a.elapsed_time(b)
+    mixed_err = {k: float(torch.linalg.norm(g_mixed[k][:-1] - grads[k][:-1]) / torch.linalg.norm(grads[k][:-1]))
+                 for k in ("u", "theta")}
+    del mm, adj_m
+    torch.cuda.empty_cache()
     ms = [ms_step]
     cl = st_cells_levels(st)
     finite = all(bool(torch.isfinite(grads[k]).all()) for k in ("u", "theta"))
@@ -445,7 +490,14 @@ def measure_dynamics_vjp(args, dev):
                              "value": cl * nsteps / (ms_none / 1e3), "tape_bytes": adj.tape_doubles() * 8 * nsteps,
                              "includes": "every step's tape kept from the forward pass (checkpoint_timesteps=False); "
                                          "the forward advances the dynamics only",
-                             "same_gradient_bitwise": same}}
+                             "same_gradient_bitwise": same},
+            "jvp": {"ms": ms_jvp[-1], "jvp_over_forward": ms_jvp[-1] / (ms_fwd * nsteps),
+                    "includes": "preparation and its tangent, 24 steps of the dynamics with their tangents (eager)",
+                    "identity_rel": abs(dj_fwd - dj_rev) / abs(dj_rev)},
+            "mixed": {"ms": ms_mixed, "vjp_over_forward": ms_mixed / (ms_fwd * nsteps),
+                      "gradient_rel_l2_vs_float64": mixed_err,
+                      "includes": "the mixed form's trajectory taped (checkpoint_timesteps=False), the reverse pass in "
+                                  "float64"}}
 
 
 def measure_ensemble_groups(args, dev):
