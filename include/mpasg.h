@@ -518,6 +518,19 @@ int mpasg_step_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, 
  * supplies only the base state, moist coefficients and diabatic forcing).  g as for
  * mpasg_step_vjp. */
 int mpasg_step_tape(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, double *tape, void *stream);
+/* The reverse pass of the dynamics substeps sub_lo..sub_hi (1-based) of one step, for meshes
+ * whose whole-step tape does not fit: f holds the step's start state; the step is recomputed
+ * up to the end of substep sub_hi with only the window taped (tape: at least
+ * mpasg_step_vjp_window_tape_doubles(m, c, sub_hi - sub_lo + 1) doubles), then the window
+ * runs backwards.  g holds the cotangents of the state after substep sub_hi on entry (the
+ * window that ends the step: after the step) and those of the state before substep sub_lo
+ * on return; calling the windows sub_hi = split .. 1 in turn, each from the restored start
+ * state, gives mpasg_step_vjp's result with one substep's tape at a time.  f ends at the
+ * end of substep sub_hi. */
+long long mpasg_step_vjp_window_tape_doubles(const mpasg_mesh *m, const mpasg_config *c, int nsub);
+int mpasg_step_vjp_window(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *g,
+                          const mpasg_transpose *t, double *tape, double *work, int sub_lo, int sub_hi,
+                          void *stream);
 int mpasg_step_vjp_taped(const mpasg_mesh *m, const mpasg_config *c, const mpasg_fields *f, mpasg_fields *g,
                          const mpasg_transpose *t, const double *tape, double *work, void *stream);
 /* Reverse mode of the cold-start preparation (mpasg_prepare; init_coupled_diagnostics.py:147

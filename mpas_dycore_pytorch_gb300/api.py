@@ -794,8 +794,17 @@ def _dynamics_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any] | None, obje
         return res
 
     # checkpoint_timesteps=False keeps every step's tape (no recomputation), as the reference
-    # keeps the whole graph without its per-step checkpoint (atmosphere_model.py:120-154)
-    mode = "none" if kwargs.get("checkpoint_timesteps") is False else "step"
+    # keeps the whole graph without its per-step checkpoint; gradient_checkpointing in the
+    # configuration (the reference's nested recomputation inside the step) recomputes every
+    # dynamics substep from its step's checkpoint and keeps sqrt(nsteps) step checkpoints
+    # (atmosphere_model.py:120-154)
+    if kwargs.get("checkpoint_timesteps") is False:
+        mode = "none"
+    elif "gradient_checkpointing" in (kwargs.get("config") or {}) and \
+            _flag(dict(kwargs["config"]), "gradient_checkpointing"):
+        mode = "sqrt"
+    else:
+        mode = "step"
     grads, _ = run_vjp(model, merged, nsteps, cotangents, adj, checkpoint=mode)
     res = {}
     for k in keys:

@@ -81,14 +81,21 @@ StepPlan plan_of(const mpasg_config* c) {
   return p;
 }
 
-// Tape layout (doubles, every array rounded to 32 doubles)
+// Tape of the dynamics substeps lo..hi (1-based) of one step (doubles, every array rounded
+// to 32 doubles): the carried fields at the start of every RK stage of the window and at
+// its end, the window's substep saves, implicit-coefficient sets and acoustic-substep
+// outputs.  Indices passed to the accessors are the step's own (stage i = 3 (sub-1) + rk-1,
+// substep sub-1, coefficient slot, acoustic substep a); tendencies are not kept (the
+// reverse pass reads none of their values).
 struct Tape {
   long long E, W, C, V, Lr;
-  long long snap_sz, sv_sz, tend_sz, trho_sz, coef_sz, ac_sz, aco_sz;
-  int n_snap, n_sv, n_tend, n_coef, n_ac;
+  long long snap_sz, sv_sz, coef_sz, aco_sz;
+  int lo, hi, n_snap, n_sv, n_coef, n_ac, per_sub_ac, nvimp;
   double* base = nullptr;
-  Tape(const mpasg_mesh* m, const StepPlan& p) {
+  Tape(const mpasg_mesh* m, const StepPlan& p, int lo_ = 1, int hi_ = 0) {
     const long long L = m->nVertLevels;
+    lo = lo_;
+    hi = hi_ > 0 ? hi_ : p.split;
     E = adj_round((m->nEdges + 1LL) * L);
     W = adj_round((m->nCells + 1LL) * (L + 1));
     C = adj_round((m->nCells + 1LL) * L);
@@ -96,35 +103,26 @@ struct Tape {
     Lr = adj_round(L);
     snap_sz = 5 * E + 2 * W + 8 * C + V;
     sv_sz = E + W + 4 * C;
-    tend_sz = E + C + W;
-    trho_sz = C;
     coef_sz = Lr + 8 * C + W;
-    ac_sz = 0;  // a substep's inputs are the previous substep's taped outputs (none at the first)
     aco_sz = E + 2 * W + 3 * C;
-    n_snap = 3 * p.split + 1;
-    n_sv = p.split;
-    n_tend = 3 * p.split;
-    n_coef = p.split * p.nvimp_per_sub;
-    n_ac = p.n_ac;
+    const int nsub = hi - lo + 1;
+    nvimp = p.nvimp_per_sub;
+    per_sub_ac = p.nsub[0] + p.nsub[1] + p.nsub[2];
+    n_snap = 3 * nsub + 1;
+    n_sv = nsub;
+    n_coef = nsub * nvimp;
+    n_ac = nsub * per_sub_ac;
   }
-  long long doubles() const {
-    return n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + n_sv * trho_sz + n_coef * coef_sz +
-           n_ac * (ac_sz + aco_sz);
-  }
-  double* snap(int i) const { return base + i * snap_sz; }
-  double* sv(int i) const { return base + n_snap * snap_sz + i * sv_sz; }
-  double* tend(int i) const { return base + n_snap * snap_sz + n_sv * sv_sz + i * tend_sz; }
-  double* trho(int i) const { return base + n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + i * trho_sz; }
-  double* coef(int i) const {
-    return base + n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + n_sv * trho_sz + i * coef_sz;
-  }
-  // acoustic substep i: its outputs (ru_p after the edge update, the undamped solution x,
+  bool in(int sub) const { return sub >= lo && sub <= hi; }
+  long long doubles() const { return n_snap * snap_sz + n_sv * sv_sz + n_coef * coef_sz + n_ac * aco_sz; }
+  double* snap(int i) const { return base + (i - 3 * (lo - 1)) * snap_sz; }
+  double* sv(int i) const { return base + n_snap * snap_sz + (i - (lo - 1)) * sv_sz; }
+  double* coef(int i) const { return base + n_snap * snap_sz + n_sv * sv_sz + (i - (lo - 1) * nvimp) * coef_sz; }
+  // acoustic substep a: its outputs (ru_p after the edge update, the undamped solution x,
   // the damped solution rw_p, ts, rtheta_pp and rtheta_pp_old)
-  double* ac(int i) const {
-    return base + n_snap * snap_sz + n_sv * sv_sz + n_tend * tend_sz + n_sv * trho_sz + n_coef * coef_sz +
-           i * (ac_sz + aco_sz);
+  double* aco(int a) const {
+    return base + n_snap * snap_sz + n_sv * sv_sz + n_coef * coef_sz + (a - (lo - 1) * per_sub_ac) * aco_sz;
   }
-  double* aco(int i) const { return ac(i) + ac_sz; }
   // the pointer of snapshot field k inside snapshot block b
   double* snap_field(double* b, int k) const {
     if (k < S_W) return b + k * E;
@@ -214,14 +212,6 @@ void sv_view(const Tape& T, mpasg_fields& v, int sub) {
   v.rho_p_save = b + T.E + T.W + T.C;
   v.theta_m_save = b + T.E + T.W + 2 * T.C;
   v.rr_save = b + T.E + T.W + 3 * T.C;
-}
-
-void tend_view(const Tape& T, mpasg_fields& v, int i, int sub) {
-  double* b = T.tend(i);
-  v.tend_u = b;
-  v.tend_theta = b + T.E;
-  v.tend_rw = b + T.E + T.C;
-  v.tend_rho = T.trho(sub);
 }
 
 void coef_view(const Tape& T, mpasg_fields& v, int j) {
@@ -328,7 +318,7 @@ int make_saves(const mpasg_mesh* m, const Tape& T, mpasg_fields& f, int sub, boo
   const long long nel = (m->nEdges + 1LL) * L, ncw = (nc + 1) * (L + 1), ncl = (nc + 1) * L;
   k_fill_row<<<1, 128, 0, s>>>(f.theta_m + nc * L, (int)L, 0.0);
   MPASG_LAUNCH_CHECK();
-  sv_view(T, f, sub);
+  if (T.in(sub + 1)) sv_view(T, f, sub);
   CHECK_RC(dcopy(f.ru_save, f.ru, nel, s));
   CHECK_RC(dcopy(f.rw_save, f.rw, ncw, s));
   CHECK_RC(dcopy(f.rtheta_p_save, f.rtheta_p, ncl, s));
@@ -345,10 +335,12 @@ int coef_slot(const StepPlan& p, int sub, int rk) {  // sub 1-based
 // the step's dynamics forward with the tape (no transport, no reconstruction); in the
 // mixed form the same stage calls as its step (float32 copies packed at the step start,
 // kept current by the stages), so the values are that form's trajectory
-// The carried fields live in the tape's snapshot blocks during the step: block 0 is a copy
-// of the start state, and the recovery and diagnostics of stage i write straight into block
-// i + 1 (after carry_block), so the stage start states are kept without copies.  The end
-// state is copied back into f's own fields.
+// The step's dynamics forward (no transport, no reconstruction) up to the end of the tape's
+// window, taping the window's substeps.  Inside the window the carried fields live in the
+// tape's snapshot blocks: the window's first block is a copy of the state, and the recovery
+// and diagnostics of stage i write straight into block i + 1 (after carry_block), so the
+// stage start states are kept without copies; the window's end state is copied back into
+// f's own fields.  Before the window the stages run on f's own fields as the step does.
 int forward_taped(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, const StepPlan& p, const Tape& T,
                   cudaStream_t s) {
   void* stream = (void*)s;
@@ -357,35 +349,40 @@ int forward_taped(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, co
   CHECK_RC(make_saves(m, T, f, 0, mixed, s));
   if (mixed) CHECK_RC(mpasgi_pack_f32(m, &f, s));
   CHECK_RC(mpasg_moist_coefficients(m, c, &f, stream));
-  CHECK_RC(snap_store(m, T, f, T.snap(0), s));
-  snap_view(T, f, T.snap(0));
   int a = 0;
-  for (int sub = 1; sub <= p.split; ++sub) {
+  for (int sub = 1; sub <= T.hi; ++sub) {
+    const bool taped = T.in(sub);
+    if (sub == T.lo) {
+      CHECK_RC(snap_store(m, T, f, T.snap(3 * (sub - 1)), s));
+      snap_view(T, f, T.snap(3 * (sub - 1)));
+    }
     for (int rk = 1; rk <= 3; ++rk) {
       const int i = (sub - 1) * 3 + rk - 1;
       const double dts = p.rk_sub[rk - 1];
       if (rk == 1 || (rk == 2 && p.order == 3)) {
-        coef_view(T, f, coef_slot(p, sub, rk));
+        if (taped) coef_view(T, f, coef_slot(p, sub, rk));
         CHECK_RC(mpasg_vert_imp_coefs(m, c, &f, dts, stream));
       }
-      tend_view(T, f, i, sub - 1);
       CHECK_RC(mpasgi_dyn_tend(m, c, &f, rk, s, true));
       CHECK_RC(mpasg_smlstep_pert(m, c, &f, stream));
       for (int small = 1; small <= p.nsub[rk - 1]; ++small) {
-        aco_redirect(T, f, a);
+        if (taped) aco_redirect(T, f, a);
         CHECK_RC(mpasgi_acoustic_step(m, c, &f, small, dts, s, true));
-        CHECK_RC(aco_store(m, T, f, a++, s));
+        if (taped) CHECK_RC(aco_store(m, T, f, a, s));
+        ++a;
         CHECK_RC(mpasgi_divergence_damping(m, c, &f, dts, s, true));
       }
-      CHECK_RC(carry_block(m, T, T.snap(i), T.snap(i + 1), rk, s));
-      snap_view(T, f, T.snap(i + 1));
+      if (taped) {
+        CHECK_RC(carry_block(m, T, T.snap(i), T.snap(i + 1), rk, s));
+        snap_view(T, f, T.snap(i + 1));
+      }
       CHECK_RC(mpasg_recover_large_step(m, c, &f, rk, p.nsub[rk - 1], p.rk_ts[rk - 1], stream));
       CHECK_RC(mpasgi_solve_diagnostics(m, c, &f, rk, s, true));
     }
-    if (sub < p.split) CHECK_RC(make_saves(m, T, f, sub, mixed, s));
+    if (sub < p.split && sub < T.hi) CHECK_RC(make_saves(m, T, f, sub, mixed, s));
   }
   mpasg_fields out = own;
-  return snap_restore(m, T, out, T.snap(3 * p.split), s);
+  return snap_restore(m, T, out, T.snap(3 * T.hi), s);
 }
 
 // zero every cotangent accumulator of g that is not a carried field
@@ -418,9 +415,11 @@ int step_reverse(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields*
                  const mpasg_transpose* t, const StepPlan& p, const Tape& T, const AdjWork& w, cudaStream_t s) {
   const int L = m->nVertLevels;
   const mpasg_fields f = *fin;
-  CHECK_RC(zero_internal(m, g, s));
-  int a = p.n_ac;
-  for (int sub = p.split; sub >= 1; --sub) {
+  // the step's last window starts from clean accumulators; a later window continues from the
+  // save cotangents the previous one left (folded at the top of its first substep)
+  if (T.hi == p.split) CHECK_RC(zero_internal(m, g, s));
+  int a = T.hi * T.per_sub_ac;
+  for (int sub = T.hi; sub >= T.lo; --sub) {
     if (sub < p.split) CHECK_RC(fold_saves(m, g, s));
     // the substep's edge mean of theta_m_save and its reciprocal sum, for the stages below
     mpasg_fields fe = f;
@@ -438,7 +437,6 @@ int step_reverse(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields*
       mpasg_fields pre = fe;
       snap_view(T, pre, T.snap(i));
       coef_view(T, pre, coef_slot(p, sub, rk));
-      tend_view(T, pre, i, sub - 1);
       for (int small = p.nsub[rk - 1]; small >= 1; --small) {
         --a;
         mpasg_fields ac = pre;
@@ -461,7 +459,7 @@ int step_reverse(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields*
     MPASG_LAUNCH_CHECK();
     CHECK_RC(mpasgi_zero(g->theta_edge_save, (m->nEdges + 1LL) * L, s));
   }
-  return fold_saves(m, g, s);
+  return T.lo == 1 ? fold_saves(m, g, s) : MPASG_OK;
 }
 
 // the reverse pass is float64 in both forms: the mixed form's gradient is the float64
@@ -505,4 +503,26 @@ extern "C" int mpasg_step_vjp(const mpasg_mesh* m, const mpasg_config* c, mpasg_
   const int rc = mpasg_step_tape(m, c, f, tape, stream);
   if (rc != MPASG_OK) return rc;
   return mpasg_step_vjp_taped(m, c, f, g, t, tape, work, stream);
+}
+
+extern "C" long long mpasg_step_vjp_window_tape_doubles(const mpasg_mesh* m, const mpasg_config* c, int nsub) {
+  if (!m || !c || c->dynamics_split_steps < 1 || c->number_of_sub_steps < 1 || nsub < 1 ||
+      nsub > c->dynamics_split_steps)
+    return -1;
+  const StepPlan p = plan_of(c);
+  return Tape(m, p, 1, nsub).doubles();
+}
+
+extern "C" int mpasg_step_vjp_window(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, mpasg_fields* g,
+                                     const mpasg_transpose* t, double* tape, double* work, int sub_lo, int sub_hi,
+                                     void* stream) {
+  if (!m || !c || !f || !g || !t || !tape || !work || !step_args_ok(m, c)) return MPASG_E_ARG;
+  if (sub_lo < 1 || sub_hi < sub_lo || sub_hi > c->dynamics_split_steps) return MPASG_E_ARG;
+  const StepPlan p = plan_of(c);
+  Tape T(m, p, sub_lo, sub_hi);
+  T.base = tape;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int rc = forward_taped(m, c, *f, p, T, s);
+  if (rc != MPASG_OK) return rc;
+  return step_reverse(m, c, f, g, t, p, T, adj_work(m, work), s);
 }

@@ -190,7 +190,10 @@ ROWS = {"e": lambda m: (m.nEdges + 1, m.nVertLevels),
 class DeviceState:
     """All device fields of one model instance (state, step work arrays and scratch)."""
 
-    def __init__(self, mesh: DeviceMesh, num_scalars: int):
+    def __init__(self, mesh: DeviceMesh, num_scalars: int, only: frozenset | None = None):
+        """``only``: allocate just these fields (a derivative state whose kernels touch no
+        others; every other member of the C struct is a null pointer, and no float32
+        copies are kept)."""
         self.mesh = mesh
         self.num_scalars = int(num_scalars)
         if not 0 <= self.num_scalars <= 8:
@@ -200,30 +203,32 @@ class DeviceState:
         shapes["cs"] = (mesh.nCells + 1, mesh.nVertLevels, S)
         shapes["es"] = (mesh.nEdges + 1, mesh.nVertLevels, S)
         shapes["cws"] = (mesh.nCells + 1, mesh.nVertLevels + 1, S)
-        sizes = {name: int(np.prod(shapes[kind])) for name, kind in _lib.FIELDS}
+        fields = [(n, k) for n, k in _lib.FIELDS if only is None or n in only]
+        sizes = {name: int(np.prod(shapes[kind])) for name, kind in fields}
         total = sum(sizes.values())
         # one arena; each field is a contiguous view (256-byte aligned)
         align = 32
         offs = {}
         pos = 0
-        for name, _ in _lib.FIELDS:
+        for name, _ in fields:
             offs[name] = pos
             pos += (sizes[name] + align - 1) // align * align
         self.arena = torch.zeros(pos, dtype=torch.float64, device=mesh.device)
         self.f: dict[str, torch.Tensor] = {}
         st = _lib.FieldsStruct()
-        for name, kind in _lib.FIELDS:
+        for name, kind in fields:
             view = self.arena[offs[name]:offs[name] + sizes[name]].view(shapes[kind])
             self.f[name] = view
             setattr(st, name, view.data_ptr())
         # float32 members (mixed form), one float32 arena
-        sizes32 = {name: int(np.prod(shapes[kind])) for name, kind in _lib.FIELDS32}
+        fields32 = _lib.FIELDS32 if only is None else []
+        sizes32 = {name: int(np.prod(shapes[kind])) for name, kind in fields32}
         offs32, pos32 = {}, 0
-        for name, _ in _lib.FIELDS32:
+        for name, _ in fields32:
             offs32[name] = pos32
             pos32 += (sizes32[name] + 63) // 64 * 64
         self.arena32 = torch.zeros(pos32, dtype=torch.float32, device=mesh.device)
-        for name, kind in _lib.FIELDS32:
+        for name, kind in fields32:
             view = self.arena32[offs32[name]:offs32[name] + sizes32[name]].view(shapes[kind])
             self.f[name] = view
             setattr(st, name, view.data_ptr())
@@ -232,7 +237,8 @@ class DeviceState:
         self.struct = st
         self.bytes = total * 8 + pos32 * 4
         # rho_zz padding row holds 1.0 (the reference's sentinel)
-        self.f["rho_zz"][mesh.nCells].fill_(1.0)
+        if "rho_zz" in self.f:
+            self.f["rho_zz"][mesh.nCells].fill_(1.0)
         # staging of loads that are gathered into the device order; reused field after
         # field (all on one stream), grown to the largest field
         self._stage = torch.empty(0, dtype=torch.float64, device=mesh.device)
@@ -269,6 +275,8 @@ class DeviceState:
             if not isinstance(src, (np.ndarray, torch.Tensor)):
                 continue
             dst = self.f[name]
+            if dst.numel() == 0:  # a model without scalars ignores the scalars it is given
+                continue
             t = torch.as_tensor(src, dtype=torch.float64)
             if pending and isinstance(src, torch.Tensor):
                 ev = pending.pop(src.data_ptr(), None)

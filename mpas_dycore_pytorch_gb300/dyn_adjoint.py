@@ -38,6 +38,13 @@ CARRIED = ("u", "v", "ru", "h_edge", "pv_edge", "w", "rw", "theta_m", "rho_zz", 
            "pressure_p", "divergence", "ke", "vorticity")
 # keys of run_simulation's output the objective may differentiate (rho_edge is h_edge)
 DIFFERENTIABLE_OUT = CARRIED + ("rho_edge",)
+# every field of the cotangent state the reverse-mode kernels read or write (the rest of the
+# forward's fields are not allocated for it; a test checks this list against the sources)
+COTANGENT_FIELDS = frozenset(CARRIED + (
+    "ru_save", "rw_save", "rtheta_p_save", "rho_p_save", "theta_m_save", "rr_save", "theta_edge_save",
+    "ru_p", "rw_p", "rho_pp", "rtheta_pp", "rtheta_pp_old", "ac_x",
+    "tend_u", "tend_u_euler", "tend_w", "tend_w_euler", "tend_rw", "tend_theta", "tend_theta_euler", "tend_rho",
+    "kdiff", "cofwz", "cofwt", "coftz", "a_tri", "alpha_tri", "gamma_tri"))
 TRACKABLE = ("u", "w", "theta", "rho")
 
 
@@ -183,8 +190,9 @@ class DynamicsAdjoint:
         for k in _lib.TRANSPOSE_PTRS:
             setattr(t, k, self._tabs[k].data_ptr())
         self.t = t
-        self.g = DeviceState(dm, model.state.num_scalars)
+        self.g = DeviceState(dm, model.state.num_scalars, only=COTANGENT_FIELDS)
         self.g.f["rho_zz"].zero_()  # a cotangent: the padding sentinel does not apply
+        self.window_tape: torch.Tensor | None = None
         n = int(self.lib.mpasg_dyn_vjp_work_doubles(C.byref(dm.struct)))
         self.work = torch.zeros(n, dtype=torch.float64, device=dev)
         self.tape: torch.Tensor | None = None
@@ -261,6 +269,21 @@ class DynamicsAdjoint:
                                            _stream())
         _lib.check(rc, "mpasg_step_vjp_taped")
 
+    def step_vjp_window(self, sub: int) -> None:
+        """The reverse pass of dynamics substep ``sub`` (1-based) of the step that starts at the
+        model's state, with only that substep taped (mpasg_step_vjp_window); g holds the
+        cotangents of the state after the substep on entry, before it on return."""
+        m = self.model
+        if self.window_tape is None:
+            n = int(self.lib.mpasg_step_vjp_window_tape_doubles(C.byref(m.dmesh.struct), C.byref(m.cstruct), 1))
+            if n <= 0:
+                raise MpasConfigError("mpasg_step_vjp_window_tape_doubles: invalid configuration")
+            self.window_tape = torch.empty(n, dtype=torch.float64, device=m.dmesh.device)
+        rc = self.lib.mpasg_step_vjp_window(C.byref(m.dmesh.struct), C.byref(m.cstruct), C.byref(m.state.struct),
+                                            C.byref(self.g.struct), C.byref(self.t), _p(self.window_tape),
+                                            _p(self.work), int(sub), int(sub), _stream())
+        _lib.check(rc, "mpasg_step_vjp_window")
+
     def tape_doubles(self) -> int:
         return int(self.lib.mpasg_step_vjp_tape_doubles(C.byref(self.model.dmesh.struct),
                                                         C.byref(self.model.cstruct)))
@@ -292,22 +315,38 @@ def run_vjp(model, loaded: Mapping[str, Any], nsteps: int,
     with its tape.  ``checkpoint="none"`` (checkpoint_timesteps=False): every step's tape is
     kept from the forward pass (about ``tape_doubles() * 8 * nsteps`` bytes), nothing is
     recomputed; the forward then advances the dynamics only, so the final state's scalars
-    and reconstructed winds are not part of it."""
-    if checkpoint not in ("step", "none"):
-        raise MpasConfigError(f"checkpoint must be 'step' or 'none', got {checkpoint!r}")
+    and reconstructed winds are not part of it.  ``checkpoint="sqrt"`` (for meshes whose
+    per-step checkpoints and whole-step tape do not fit): checkpoints every S = ceil(sqrt(
+    nsteps)) steps; each segment is recomputed from its checkpoint with a checkpoint per step,
+    and each step runs backwards one dynamics substep at a time, every substep recomputed
+    from the step's checkpoint with only its own tape (mpasg_step_vjp_window).  Checkpoints
+    held: at most ceil(nsteps / S) + S - 1; the same gradient bit for bit."""
+    if checkpoint not in ("step", "none", "sqrt"):
+        raise MpasConfigError(f"checkpoint must be 'step', 'none' or 'sqrt', got {checkpoint!r}")
     adj = adj or DynamicsAdjoint(model)
     model.prepare(loaded)
     w_in = model.state.f["w"].clone()
     ck0 = adj.checkpoint()
     tapes: list[torch.Tensor] = []
     ckpts = [ck0]
+    seg = max(1, int(np.ceil(np.sqrt(int(nsteps))))) if checkpoint == "sqrt" else 1
+    outer = {0: ck0}
+
+    def forward_step(n):
+        model.step()
+        if n == 0 and nsteps > 1 and model._graph is None:
+            model.capture_graph()  # later steps replay the step graph (bitwise the eager step)
+
     if checkpoint == "step":
         for n in range(int(nsteps)):
-            model.step()
-            if n == 0 and nsteps > 1 and model._graph is None:
-                model.capture_graph()  # later steps replay the step graph (bitwise the eager step)
+            forward_step(n)
             if n + 1 < nsteps:
                 ckpts.append(adj.checkpoint())
+    elif checkpoint == "sqrt":
+        for n in range(int(nsteps)):
+            forward_step(n)
+            if n + 1 < nsteps and (n + 1) % seg == 0:
+                outer[n + 1] = adj.checkpoint()
     else:
         nd = adj.tape_doubles()
         free, _ = torch.cuda.mem_get_info(model.dmesh.device)
@@ -334,7 +373,25 @@ def run_vjp(model, loaded: Mapping[str, Any], nsteps: int,
             raise MpasUnsupportedCapabilityError(f"no derivative through output {k!r}")
         dst = adj.g.f[name]
         dst[: v.shape[0]].add_(v.to(device=dev, dtype=torch.float64))
+    if checkpoint == "sqrt":
+        split = int(model.cstruct.dynamics_split_steps)
+        for start in sorted(outer, reverse=True):
+            end = min(start + seg, int(nsteps))
+            adj.restore(outer[start])
+            inner = [outer[start]]
+            for n in range(start, end - 1):
+                model.step()
+                inner.append(adj.checkpoint())
+            for n in range(end - 1, start - 1, -1):
+                for sub in range(split, 0, -1):
+                    adj.restore(inner[n - start])
+                    adj.step_vjp_window(sub)
+            if start > 0:
+                del outer[start]
+            del inner
     for n in range(int(nsteps) - 1, -1, -1):
+        if checkpoint == "sqrt":
+            break
         if checkpoint == "step":
             adj.restore(ckpts[n])
             adj.step_vjp()

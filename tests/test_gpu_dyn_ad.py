@@ -191,6 +191,15 @@ def test_run_vjp_matches_reference(case):
                                dt=float(z["dt"]), nsteps=int(z["nsteps"]), checkpoint_timesteps=False)
     for k in ("u", "theta"):
         assert torch.equal(again[k], grads[k]), k
+    # nested recomputation (the configuration's gradient_checkpointing): each dynamics
+    # substep recomputed from its step's checkpoint with only its own tape, sqrt(nsteps)
+    # step checkpoints: the same gradients bit for bit
+    state = {k: torch.as_tensor(v) for k, v in st0.items()}
+    nested = run_simulation.vjp(state, mesh, objective, track_keys=("u", "theta"),
+                                config=dict(config(case), gradient_checkpointing=True), dt=float(z["dt"]),
+                                nsteps=int(z["nsteps"]))
+    for k in ("u", "theta"):
+        assert torch.equal(nested[k], grads[k]), k
 
 
 @pytest.mark.parametrize("case", AD_CASES)
