@@ -52,7 +52,7 @@ WORKLOADS = {
     "c4": dict(spec=dict(level=8, nlev=55, dz_bottom=50.0, seed=3, n_bumps=128, n_tracers=3),
                config=dict(config_monotonic=True, config_len_disp=30000.0), dt=180.0,
                name="plain float64 forward, level-8 icosahedral mesh 655362 cells x 55 levels, "
-                    "3 monotone tracers, dt 180 s, split 3 x RK3 x ns 2"),
+                    "3 monotone tracers, dt 180 s, split 3 x RK3 x ns 2", cpu_baseline=False),
     # CPU-runnable case: level-4 mesh, 26 uniform levels, 8 bumps, 1 non-monotone tracer, dt 1800 s
     "c0": dict(spec=dict(level=4, nlev=26, seed=0, n_bumps=8, n_tracers=1),
                config=dict(config_monotonic=False), dt=1800.0,
@@ -500,6 +500,71 @@ def measure_dynamics_vjp(args, dev):
                                   "float64"}}
 
 
+def measure_large_vjp(args, dev, st, cfg, w, nsteps=12):
+    """The large workload's gradient (level-8 mesh 655362 cells x 55 levels, dt 180 s): the
+    area-weighted squared surface-pressure anomaly after 12 steps with respect to the initial
+    u and theta, by the reverse mode with sqrt(N) step checkpoints and one dynamics substep
+    taped at a time (checkpoint="sqrt"), in the mixed form and in float64; the dry dynamics
+    do not read the scalars, so the models hold none.  Reports the time, the peak device
+    memory, the mixed gradient's error against the float64 one, and a forward step of each
+    form (CUDA graph) for the ratio."""
+    import numpy as np
+    import torch
+
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.diagnostics import physics_interface_surface_pressure, surface_pressure_functional
+    from mpas_dycore_pytorch_gb300.dyn_adjoint import DynamicsAdjoint, run_vjp
+
+    nc = int(st["nCells"])
+    zz = torch.as_tensor(st["zz"], device=dev)
+    zgrid = torch.as_tensor(st["zgrid"], device=dev)
+    area = torch.as_tensor(st["areaCell"], device=dev)
+    out, grads = {}, {}
+    for prec in ("mixed", "float64"):
+        c = dict(cfg, config_precision=prec)
+        m = Model(st, c, w["dt"], num_scalars=0, device=dev)
+        m.prepare(st)
+        m.step()
+        m.capture_graph()
+        fwd_ms = _time_steps(m.step, 3, 1)
+        m.prepare(st)
+        sp_ref = physics_interface_surface_pressure(
+            nCells=nc, rho_zz=m.state.f["rho_zz"], zz=zz, qv=torch.zeros_like(m.state.f["rho_zz"]),
+            pressure_p=m.state.f["pressure_p"], pressure_base=m.state.f["pressure_base"], zgrid=zgrid).detach().clone()
+
+        def cotangents(final):
+            rz = final["rho_zz"].detach().clone().requires_grad_(True)
+            pp = final["pressure_p"].detach().clone().requires_grad_(True)
+            sp = physics_interface_surface_pressure(nCells=nc, rho_zz=rz, zz=zz, qv=torch.zeros_like(rz),
+                                                    pressure_p=pp, pressure_base=final["pressure_base"], zgrid=zgrid)
+            g_rz, g_pp = torch.autograd.grad(surface_pressure_functional(sp, sp_ref, area, nc), [rz, pp])
+            return {"rho_zz": g_rz, "pressure_p": g_pp}
+
+        adj = DynamicsAdjoint(m)
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        g, _ = run_vjp(m, st, nsteps, cotangents, adj, checkpoint="sqrt")
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        grads[prec] = {k: g[k][:-1].cpu() for k in ("u", "theta")}
+        out[prec] = {"ms": ms, "forward_graph_ms_per_step": fwd_ms, "vjp_over_forward": ms / (nsteps * fwd_ms),
+                     "peak_device_gb": torch.cuda.max_memory_allocated(dev) / 1e9,
+                     "window_tape_gb": adj.window_tape.numel() * 8 / 1e9 if adj.window_tape is not None else 0.0,
+                     "gradient_finite": all(bool(torch.isfinite(g[k]).all()) for k in ("u", "theta"))}
+        del m, adj, g
+        torch.cuda.empty_cache()
+    out["mixed"]["gradient_rel_l2_vs_float64"] = {
+        k: float(np.linalg.norm((grads["mixed"][k] - grads["float64"][k]).numpy()) /
+                 np.linalg.norm(grads["float64"][k].numpy())) for k in ("u", "theta")}
+    out["workload"] = (f"level-8 mesh {nc} cells x {int(st['nVertLevels'])} levels, dry dynamics, {nsteps} steps at "
+                       f"dt {w['dt']} s; gradient of the area-weighted squared surface-pressure anomaly w.r.t. initial "
+                       f"u and theta; sqrt(N) step checkpoints, one dynamics substep taped at a time")
+    return out
+
+
 def measure_ensemble_groups(args, dev):
     """The two-grid mixed-precision ensemble: 96 members of 10242 cells x 41 levels (dt
     900 s) and 32 members of 40962 cells x 55 stretched levels (dt 720 s), 2 monotone
@@ -623,7 +688,8 @@ def run_gb300(args, rank, world):
     # the CPU baseline: one large step of the oracle on this workload, in a process spawned
     # before any CUDA work that runs while the GPU is measured (one host core of 16)
     cpu_job = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    # (none on the level-8 workload: one step of the oracle there takes most of an hour)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and w.get("cpu_baseline", True):
         case_path, st = _save_case(w)
         cpu_pool = mp.get_context("spawn").Pool(1)
         cpu_job = cpu_pool.apply_async(_oracle_steps, ((case_path, cfg, w["dt"], 1),))
@@ -777,6 +843,10 @@ def run_gb300(args, rank, world):
         forms["vjp_dynamics"] = measure_dynamics_vjp(args, dev)
         if args.ensemble_groups:
             forms["batched_two_grids"] = measure_ensemble_groups(args, dev)
+    elif world == 1 and not args.no_forms and args.workload == "c4":
+        del model, host
+        torch.cuda.empty_cache()
+        forms = {"vjp_sqrt_checkpointed": measure_large_vjp(args, dev, st, cfg, w)}
 
     cpu = None
     if cpu_job is not None:
