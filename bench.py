@@ -565,6 +565,38 @@ def measure_large_vjp(args, dev, st, cfg, w, nsteps=12):
     return out
 
 
+def profile_dynamics_vjp(dev, pairs=2):
+    """For kernel profiles (ncu): the differentiation workload prepared, then ``pairs`` times
+    one taped forward step (mpasg_step_tape) and one reverse step (mpasg_step_vjp_taped)
+    from the prepared state.  Prints the CUDA-event times of the last pair; no bench line."""
+    import torch
+
+    from mpas_dycore_pytorch_gb300.api import Model
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.dyn_adjoint import DynamicsAdjoint
+    from mpas_dycore_pytorch_gb300.loader import load_case
+
+    cfg = dict(_cfg(WORKLOADS["c2"]), config_monotonic=False)
+    st, _ = load_case(CaseSpec(**DYN_VJP_SPEC), cfg, as_torch=False)
+    m = Model(st, cfg, 900.0, num_scalars=1, device=dev)
+    adj = DynamicsAdjoint(m)
+    m.prepare(st)
+    ck = adj.checkpoint()
+    tape = torch.empty(adj.tape_doubles(), dtype=torch.float64, device=dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    for _ in range(int(pairs)):
+        adj.restore(ck)
+        adj.zero_cotangents()
+        torch.cuda.synchronize()
+        ev[0].record()
+        adj.step_tape(tape)
+        ev[1].record()
+        adj.step_vjp_taped(tape)
+        ev[2].record()
+        torch.cuda.synchronize()
+    print(f"taped forward {ev[0].elapsed_time(ev[1]):.3f} ms, reverse {ev[1].elapsed_time(ev[2]):.3f} ms")
+
+
 def measure_ensemble_groups(args, dev):
     """The two-grid mixed-precision ensemble: 96 members of 10242 cells x 41 levels (dt
     900 s) and 32 members of 40962 cells x 55 stretched levels (dt 720 s), 2 monotone
@@ -913,6 +945,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--workload", default="c1", choices=tuple(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-vjp", action="store_true",
+                    help="only run two taped forward + reverse steps of the differentiation workload (for ncu)")
     ap.add_argument("--precision", default="float64", choices=("float64", "mixed"))
     ap.add_argument("--no-forms", action="store_true", help="skip the mixed and batched forms")
     ap.add_argument("--order", default="sfc", choices=("native", "sfc"),
@@ -929,6 +963,10 @@ def main():
         out = run_reference(args, rank, world)
         if out is not None:
             print(json.dumps(out))
+        return
+    if args.profile_vjp:
+        import torch
+        profile_dynamics_vjp(torch.device("cuda", 0))
         return
     if world > 1:
         import torch
