@@ -41,6 +41,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
+from . import detmath as dm
+
 EARTH_RADIUS = 6371229.0
 OMEGA = 7.29212e-5
 GRAVITY = 9.80616
@@ -64,10 +66,10 @@ def _icosahedron():
          [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6], [7, 1, 8],
          [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9],
          [4, 9, 5], [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]], dtype=np.int64)
-    p /= np.linalg.norm(p, axis=1, keepdims=True)
+    p = _unit(p)
     # orient every face counter-clockwise seen from outside
     a, b, c = p[f[:, 0]], p[f[:, 1]], p[f[:, 2]]
-    flip = np.einsum("ij,ij->i", np.cross(b - a, c - a), a + b + c) < 0
+    flip = _dot(_cross(b - a, c - a), a + b + c) < 0
     f[flip] = f[flip][:, [0, 2, 1]]
     return p, f
 
@@ -82,8 +84,7 @@ def icosphere(level: int):
         uniq, inv = np.unique(key, return_inverse=True)
         lo = uniq // (n + 1)
         hi = uniq % (n + 1)
-        mid = p[lo] + p[hi]
-        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        mid = _unit(p[lo] + p[hi])
         mid_id = n + inv
         nf = f.shape[0]
         ab, bc, ca = mid_id[:nf], mid_id[nf:2 * nf], mid_id[2 * nf:]
@@ -95,37 +96,99 @@ def icosphere(level: int):
     return p, f
 
 
+# Vector algebra written out component by component (fixed evaluation order), and the
+# elementary functions of detmath: the generated arrays are bit-identical on every machine.
+
+def _dot(a, b):
+    return a[..., 0] * b[..., 0] + a[..., 1] * b[..., 1] + a[..., 2] * b[..., 2]
+
+
+def _cross(a, b):
+    return np.stack([a[..., 1] * b[..., 2] - a[..., 2] * b[..., 1],
+                     a[..., 2] * b[..., 0] - a[..., 0] * b[..., 2],
+                     a[..., 0] * b[..., 1] - a[..., 1] * b[..., 0]], -1)
+
+
+def _norm(v):
+    return np.sqrt(_dot(v, v))
+
+
 def _unit(v):
-    return v / np.linalg.norm(v, axis=-1, keepdims=True)
+    return v / _norm(v)[..., None]
 
 
 def _arc(a, b):
     """Great-circle angle between unit vectors (robust atan2 form)."""
-    return np.arctan2(np.linalg.norm(np.cross(a, b), axis=-1), np.einsum("...i,...i->...", a, b))
+    return dm.atan2(_norm(_cross(a, b)), _dot(a, b))
 
 
 def _sph_tri_area(a, b, c):
     """Spherical-excess area of unit-sphere triangles (Eriksson's formula)."""
-    num = np.abs(np.einsum("...i,...i->...", a, np.cross(b, c)))
-    den = 1.0 + np.einsum("...i,...i->...", a, b) + np.einsum("...i,...i->...", b, c) \
-        + np.einsum("...i,...i->...", c, a)
-    return 2.0 * np.arctan2(num, den)
+    num = np.abs(_dot(a, _cross(b, c)))
+    den = 1.0 + _dot(a, b) + _dot(b, c) + _dot(c, a)
+    return 2.0 * dm.atan2(num, den)
 
 
 def _latlon(x):
-    lat = np.arcsin(np.clip(x[:, 2], -1.0, 1.0))
-    lon = np.mod(np.arctan2(x[:, 1], x[:, 0]), 2.0 * math.pi)
+    lat = dm.asin(np.clip(x[:, 2], -1.0, 1.0))
+    lon = np.mod(dm.atan2(x[:, 1], x[:, 0]), 2.0 * math.pi)
     return lat, lon
 
 
 def _east_north(x):
     """Local east and north unit vectors at unit positions ``x``."""
     k = np.array([0.0, 0.0, 1.0])
-    east = np.cross(k, x)
-    nrm = np.linalg.norm(east, axis=-1, keepdims=True)
+    east = _cross(k, x)
+    nrm = _norm(east)[..., None]
     east = np.where(nrm > 1e-14, east / np.maximum(nrm, 1e-300), np.array([0.0, 1.0, 0.0]))
-    north = np.cross(x, east)
+    north = _cross(x, east)
     return east, north
+
+
+def _lsq_xx_weights(px, py, valid):
+    """Weights ``w`` (n, m) such that ``sum_j w[:, j] f_j`` is the second derivative in x
+    at the origin of the least-squares quadratic ``a0 + a1 x + a2 y + a3 x^2 + a4 xy +
+    a5 y^2`` through the valid points ``(px, py)``: twice row 3 of the fit's pseudo-inverse.
+    Normal equations in coordinates scaled by the stencil's extent, Cholesky factor, one
+    solve for row 3 of the inverse."""
+    n, m = px.shape
+    h = np.max(np.where(valid, np.maximum(np.abs(px), np.abs(py)), 0.0), axis=1)
+    xs, ys = px / h[:, None], py / h[:, None]
+    B = np.stack([np.ones_like(xs), xs, ys, xs * xs, xs * ys, ys * ys], -1) * valid[..., None]
+    N = np.zeros((n, 6, 6))
+    for i in range(6):
+        for j in range(i + 1):
+            s = B[:, 0, i] * B[:, 0, j]
+            for r in range(1, m):
+                s = s + B[:, r, i] * B[:, r, j]
+            N[:, i, j] = N[:, j, i] = s
+    L = np.zeros((n, 6, 6))
+    for j in range(6):
+        d = N[:, j, j]
+        for k in range(j):
+            d = d - L[:, j, k] * L[:, j, k]
+        L[:, j, j] = np.sqrt(d)
+        for i in range(j + 1, 6):
+            s = N[:, i, j]
+            for k in range(j):
+                s = s - L[:, i, k] * L[:, j, k]
+            L[:, i, j] = s / L[:, j, j]
+    y = np.zeros((n, 6))   # L y = e_3
+    for i in range(6):
+        s = np.full(n, 1.0 if i == 3 else 0.0)
+        for k in range(i):
+            s = s - L[:, i, k] * y[:, k]
+        y[:, i] = s / L[:, i, i]
+    z = np.zeros((n, 6))   # L^T z = y: z = N^-1 e_3
+    for i in reversed(range(6)):
+        s = y[:, i]
+        for k in range(i + 1, 6):
+            s = s - L[:, k, i] * z[:, k]
+        z[:, i] = s / L[:, i, i]
+    w = B[..., 0] * z[:, None, 0]
+    for i in range(1, 6):
+        w = w + B[..., i] * z[:, None, i]
+    return 2.0 * w / (h * h)[:, None]
 
 
 # --------------------------------------------------------------------------------------
@@ -140,7 +203,7 @@ def build_mesh(level: int, radius: float = EARTH_RADIUS) -> dict:
 
     # Voronoi vertices: circumcentres of the CCW triangles
     a, b, c = pc[tri[:, 0]], pc[tri[:, 1]], pc[tri[:, 2]]
-    pv = _unit(np.cross(b - a, c - a))
+    pv = _unit(_cross(b - a, c - a))
 
     # directed half-edges of every triangle: (from, to, face); face lies left of from->to
     h_from = np.concatenate([tri[:, 0], tri[:, 1], tri[:, 2]])
@@ -219,8 +282,8 @@ def build_mesh(level: int, radius: float = EARTH_RADIUS) -> dict:
         e_next = pe[edges_on_vertex[:, i]]
         e_prev = pe[edges_on_vertex[:, (i + 2) % 3]]
         kites[:, i] = _sph_tri_area(cc, e_prev, pv) + _sph_tri_area(cc, pv, e_next)
-    kites *= radius ** 2
-    area_tri = radius ** 2 * _sph_tri_area(a, b, c)
+    kites *= radius * radius
+    area_tri = (radius * radius) * _sph_tri_area(a, b, c)
     area_cell = np.zeros(nc)
     for i in range(3):
         np.add.at(area_cell, tri[:, i], kites[:, i])
@@ -228,14 +291,15 @@ def build_mesh(level: int, radius: float = EARTH_RADIUS) -> dict:
     latc, lonc = _latlon(pc)
     late, lone = _latlon(pe)
     latv, lonv = _latlon(pv)
-    nvec = _unit(pc[c2] - pc[c1] - np.einsum("ij,ij->i", pc[c2] - pc[c1], pe)[:, None] * pe)
+    nvec = _unit(pc[c2] - pc[c1] - _dot(pc[c2] - pc[c1], pe)[:, None] * pe)
     east_e, north_e = _east_north(pe)
-    angle_edge = np.arctan2(np.einsum("ij,ij->i", nvec, north_e), np.einsum("ij,ij->i", nvec, east_e))
+    angle_edge = dm.atan2(_dot(nvec, north_e), _dot(nvec, east_e))
 
     # kite area of cell `cell` at vertex `vtx`
     def kite_of(cell, vtx):
         m = cells_on_vertex[vtx] == cell[..., None]
-        return np.sum(np.where(m, kites[vtx], 0.0), axis=-1)
+        k = np.where(m, kites[vtx], 0.0)
+        return k[..., 0] + k[..., 1] + k[..., 2]
 
     # ---- TRiSK weights ----------------------------------------------------------
     n_eoe = counts[c1] + counts[c2] - 2
@@ -272,18 +336,15 @@ def build_mesh(level: int, radius: float = EARTH_RADIUS) -> dict:
         pts = np.concatenate([cell[:, None], np.where(cells_on_cell[cell] >= 0, cells_on_cell[cell], cell[:, None])], 1)
         pts_valid = np.concatenate([np.ones((ne, 1), bool), cells_on_cell[cell] >= 0], 1)
         x0 = pc[cell]
-        xh = nvec - np.einsum("ij,ij->i", nvec, x0)[:, None] * x0
+        xh = nvec - _dot(nvec, x0)[:, None] * x0
         xh = _unit(xh)
-        yh = np.cross(x0, xh)
+        yh = _cross(x0, xh)
         q = pc[pts]  # (ne, 7, 3)
         # gnomonic-style local coordinates scaled by arc length
         d = q - x0[:, None, :]
-        px = radius * np.einsum("ijk,ik->ij", d, xh)
-        py = radius * np.einsum("ijk,ik->ij", d, yh)
-        A = np.stack([np.ones_like(px), px, py, px * px, px * py, py * py], -1)
-        A = A * pts_valid[..., None]
-        pinv = np.linalg.pinv(A)  # (ne, 6, 7)
-        deriv_two[:, side, : maxe + 1] = 2.0 * pinv[:, 3, :] * pts_valid
+        px = radius * _dot(d, xh[:, None, :])
+        py = radius * _dot(d, yh[:, None, :])
+        deriv_two[:, side, : maxe + 1] = _lsq_xx_weights(px, py, pts_valid) * pts_valid
 
     # ---- Smagorinsky deformation weights ---------------------------------------------
     defc_a = np.zeros((nc, maxe))
@@ -294,9 +355,9 @@ def build_mesh(level: int, radius: float = EARTH_RADIUS) -> dict:
         e = np.where(act, edges_on_cell[:, i], 0)
         s = np.where(c1[e] == rows, 1.0, -1.0)
         nn = nvec[e]
-        th = np.arctan2(np.einsum("ij,ij->i", nn, north_c), np.einsum("ij,ij->i", nn, east_c))
-        defc_a[:, i] = np.where(act, s * dv[e] * np.cos(2.0 * th) / area_cell, 0.0)
-        defc_b[:, i] = np.where(act, s * dv[e] * np.sin(2.0 * th) / area_cell, 0.0)
+        th = dm.atan2(_dot(nn, north_c), _dot(nn, east_c))
+        defc_a[:, i] = np.where(act, s * dv[e] * dm.cos(2.0 * th) / area_cell, 0.0)
+        defc_b[:, i] = np.where(act, s * dv[e] * dm.sin(2.0 * th) / area_cell, 0.0)
 
     one = lambda x: (x + 1).astype(np.int32)
     zero_pad = lambda x: np.where(x >= 0, x + 1, 0).astype(np.int32)
@@ -322,7 +383,7 @@ def build_mesh(level: int, radius: float = EARTH_RADIUS) -> dict:
         "xEdge": radius * pe[:, 0], "yEdge": radius * pe[:, 1], "zEdge": radius * pe[:, 2],
         "xVertex": radius * pv[:, 0], "yVertex": radius * pv[:, 1], "zVertex": radius * pv[:, 2],
         "angleEdge": angle_edge,
-        "fEdge": 2.0 * OMEGA * np.sin(late), "fVertex": 2.0 * OMEGA * np.sin(latv),
+        "fEdge": 2.0 * OMEGA * dm.sin(late), "fVertex": 2.0 * OMEGA * dm.sin(latv),
         "meshDensity": np.ones(nc),
         "indexToCellID": np.arange(1, nc + 1, dtype=np.int32),
         "indexToEdgeID": np.arange(1, ne + 1, dtype=np.int32),
@@ -343,15 +404,21 @@ def vertical_levels(nlev: int, ztop: float = 30000.0, dz_bottom: float | None = 
     if dz_bottom is None:
         return np.linspace(0.0, ztop, nlev + 1)
     # find growth ratio q with dz_bottom * (q**nlev - 1)/(q - 1) = ztop
+    def powers(q):  # q**0 .. q**nlev by repeated multiplication (no libm pow)
+        out = [1.0]
+        for _ in range(nlev):
+            out.append(out[-1] * q)
+        return np.array(out)
+
     lo_q, hi_q = 1.0 + 1e-12, 2.0
     for _ in range(200):
         q = 0.5 * (lo_q + hi_q)
-        tot = dz_bottom * (q ** nlev - 1.0) / (q - 1.0)
+        tot = dz_bottom * (powers(q)[nlev] - 1.0) / (q - 1.0)
         if tot > ztop:
             hi_q = q
         else:
             lo_q = q
-    dz = dz_bottom * q ** np.arange(nlev)
+    dz = dz_bottom * powers(q)[:nlev]
     zw = np.concatenate([[0.0], np.cumsum(dz)])
     zw *= ztop / zw[-1]
     return zw
@@ -406,7 +473,37 @@ def _vertical_metrics(zw: np.ndarray) -> dict:
 def _exner_profile(zmid: np.ndarray, theta0: float, bvf: float, pi_s: np.ndarray) -> np.ndarray:
     """Hydrostatic Exner for theta = theta0 exp(N^2 z/g): d(pi)/dz = -g/(cp theta)."""
     g = GRAVITY
-    return pi_s[:, None] - g * g / (CP * theta0 * bvf * bvf) * (1.0 - np.exp(-bvf * bvf * zmid[None, :] / g))
+    return pi_s[:, None] - g * g / (CP * theta0 * bvf * bvf) * (1.0 - dm.exp(-bvf * bvf * zmid[None, :] / g))
+
+
+def _random_direction(rng) -> np.ndarray:
+    """A uniformly distributed unit vector: uniform points of the cube kept inside the unit
+    ball, normalised (uniform draws and basic arithmetic only)."""
+    while True:
+        v = 2.0 * rng.random(3) - 1.0
+        r2 = float(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+        if 1e-6 < r2 <= 1.0:
+            return v / math.sqrt(r2)
+
+
+def _normal(rng, shape) -> np.ndarray:
+    """Standard normal draws by the Box-Muller transform of uniform draws."""
+    u1 = 1.0 - rng.random(shape)  # (0, 1]
+    u2 = rng.random(shape)
+    return np.sqrt(-2.0 * dm.log(u1)) * dm.cos((2.0 * math.pi) * u2)
+
+
+def damping_coefficients(zgrid: np.ndarray, zd: float = 22000.0, xnutr: float = 0.2) -> np.ndarray:
+    """Rayleigh damping of w above ``zd`` as MPAS init computes it (the reference's
+    initialization.py:333 compute_damping_coefs, mesh density 1): xnutr sin^2(pi/2 (z -
+    zd) / (ztop - zd)) at the layer midpoints above zd, 0 below.  Written into the case's
+    initial-condition arrays so that every loader takes these values as they are."""
+    nlev = zgrid.shape[1] - 1
+    zt = zgrid[:, nlev]
+    zmid = 0.5 * (zgrid[:, :nlev] + zgrid[:, 1:])
+    arg = 0.5 * math.pi * (zmid - zd) / (zt[:, None] - zd)
+    s = dm.sin(arg)
+    return np.where(zmid > zd, xnutr * (s * s), 0.0)
 
 
 def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> dict:
@@ -421,22 +518,23 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
     latc = mesh["latCell"]
 
     # surface Exner balancing the solid-body zonal flow u0 cos(lat) (gradient wind)
-    pi_s = 1.0 - (u0 * (2.0 * OMEGA * radius + u0) * 0.5 * np.sin(latc) ** 2) / (CP * theta0)
-    theta_b = theta0 * np.exp(bvf * bvf * zmid / GRAVITY)[None, :].repeat(nc, 0)
+    sl = dm.sin(latc)
+    pi_s = 1.0 - (u0 * (2.0 * OMEGA * radius + u0) * 0.5 * (sl * sl)) / (CP * theta0)
+    theta_b = theta0 * dm.exp(bvf * bvf * zmid / GRAVITY)[None, :].repeat(nc, 0)
     exner_b = _exner_profile(zmid, theta0, bvf, pi_s)
-    p_b = P0 * exner_b ** (CP / RGAS)
+    p_b = P0 * dm.pow(exner_b, CP / RGAS)
     rho_b = p_b / (RGAS * theta_b * exner_b)
 
     # theta bumps at constant pressure (rho*theta fixed)
     pc = np.stack([mesh["xCell"], mesh["yCell"], mesh["zCell"]], 1) / radius
     theta = theta_b.copy()
-    env = np.sin(math.pi * zmid / spec.ztop)[None, :]
+    env = dm.sin(math.pi * zmid / spec.ztop)[None, :]
     for _ in range(spec.n_bumps):
-        v = rng.normal(size=3)
-        v /= np.linalg.norm(v)
+        v = _random_direction(rng)
         amp = rng.uniform(-1.0, 1.0)
         dist = radius * _arc(pc, v[None, :])
-        theta += amp * np.exp(-((dist / 500.0e3) ** 2))[:, None] * env
+        r = dist / 500.0e3
+        theta += amp * dm.exp(-(r * r))[:, None] * env
     rho = rho_b * theta_b / theta
 
     # edge winds
@@ -444,12 +542,12 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
     c1 = mesh["cellsOnEdge"][:, 0] - 1
     c2 = mesh["cellsOnEdge"][:, 1] - 1
     nvec = pc[c2] - pc[c1]
-    nvec = _unit(nvec - np.einsum("ij,ij->i", nvec, pe)[:, None] * pe)
+    nvec = _unit(nvec - _dot(nvec, pe)[:, None] * pe)
     east_e, _ = _east_north(pe)
-    un = u0 * np.cos(mesh["latEdge"]) * np.einsum("ij,ij->i", east_e, nvec)
+    un = u0 * dm.cos(mesh["latEdge"]) * _dot(east_e, nvec)
     u = np.repeat(un[:, None], nlev, 1)
     if spec.u_noise > 0.0:
-        u = u + spec.u_noise * rng.normal(size=u.shape)
+        u = u + spec.u_noise * _normal(rng, u.shape)
     if spec.round_wind_bits > 0:
         m, e = np.frexp(u)
         scale = float(2 ** spec.round_wind_bits)
@@ -458,8 +556,8 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
     w = np.zeros((nc, nlev + 1))
     if spec.w_sine != 0.0:
         lonc = mesh["lonCell"]
-        w[:, 1:nlev] = spec.w_sine * np.sin(math.pi * zw[None, 1:nlev] / spec.ztop) * np.cos(latc)[:, None] \
-            * np.sin(2.0 * lonc)[:, None]
+        w[:, 1:nlev] = spec.w_sine * dm.sin(math.pi * zw[None, 1:nlev] / spec.ztop) * dm.cos(latc)[:, None] \
+            * dm.sin(2.0 * lonc)[:, None]
 
     # passive tracers in [0, 1]
     lonc = mesh["lonCell"]
@@ -468,19 +566,22 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
         kind = t % 3
         if kind == 0:  # cosine bell centred at (lon, lat) = (3pi/2, 0)
             r = _arc(pc, np.array([0.0, -1.0, 0.0])[None, :])
-            h = np.where(r < 0.5, 0.5 * (1.0 + np.cos(math.pi * r / 0.5)), 0.0)
+            h = np.where(r < 0.5, 0.5 * (1.0 + dm.cos(math.pi * r / 0.5)), 0.0)
         elif kind == 1:  # slotted cylinder centred at (lon, lat) = (pi/2, pi/6)
-            cen = np.array([0.0, math.cos(math.pi / 6), math.sin(math.pi / 6)])
+            cen = np.array([0.0, float(dm.cos(math.pi / 6)), float(dm.sin(math.pi / 6))])
             r = _arc(pc, cen[None, :])
-            dlon = np.angle(np.exp(1j * (lonc - math.pi / 2)))
+            dlon = lonc - math.pi / 2
+            dlon = dlon - (2.0 * math.pi) * np.rint(dlon / (2.0 * math.pi))  # wrapped to [-pi, pi]
             slot = (np.abs(dlon) < 1.0 / 12.0) & (latc < math.pi / 6 + 5.0 / 24.0)
             h = np.where((r < 0.5) & ~slot, 1.0, 0.1)
         else:  # smooth product field
-            h = 0.5 + 0.5 * np.cos(latc) ** 2 * np.cos(2.0 * lonc)
+            cl = dm.cos(latc)
+            h = 0.5 + 0.5 * (cl * cl) * dm.cos(2.0 * lonc)
         tracers.append(np.repeat(h[:, None], nlev, 1))
     qv = np.zeros((nc, nlev))
     if spec.qv_surface > 0.0:  # vapour decaying with a 2.5 km scale height, wetter at the equator
-        qv = spec.qv_surface * np.exp(-zmid / 2500.0)[None, :] * (0.25 + 0.75 * np.cos(latc) ** 2)[:, None]
+        cl = dm.cos(latc)
+        qv = spec.qv_surface * dm.exp(-zmid / 2500.0)[None, :] * (0.25 + 0.75 * (cl * cl))[:, None]
         tracers = [qv] + tracers
     scalars = np.stack(tracers, -1) if tracers else np.zeros((nc, nlev, 0))
 
@@ -495,6 +596,7 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
         "moist_start": 1, "moist_end": 1 if spec.qv_surface > 0.0 else 0,
         "u_init": np.full(nlev, float(spec.uv_init[0])), "v_init": np.full(nlev, float(spec.uv_init[1])),
         "t_init": theta_b.copy(), "qv_init": np.zeros(nlev),
+        "dss": damping_coefficients(zgrid),
     }
     for k, v in vm.items():
         if k in ("dzw", "dzu"):

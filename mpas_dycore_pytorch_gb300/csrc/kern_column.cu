@@ -6,6 +6,7 @@
 // order (mpas_pytorch/dynamics/*.py, cited per kernel); slot sums run in connectivity
 // slot order, left to right, so results are deterministic and need no atomics.
 #include "common.cuh"
+#include "pow_exner.cuh"
 
 namespace {
 
@@ -776,7 +777,7 @@ __global__ void __launch_bounds__(kBlock) k_recover_cells(mpasg_mesh m, mpasg_fi
       const double rcv = kRgas / (kCp - kRgas);
       double zz = m.zz[o];
       if (sizeof(T) == sizeof(double)) {
-        double ex = pow(zz * (kRgas / kP0) * (rtheta_p + rtb), rcv);
+        double ex = mpasg_pow::pow_exner(zz * (kRgas / kP0) * (rtheta_p + rtb), rcv);
         f.exner[o] = ex;
         f.pressure_p[o] = zz * kRgas * __dadd_rn(__dmul_rn(ex, rtheta_p), __dmul_rn(rtb, ex - f.exner_base[o]));
       } else {
@@ -787,7 +788,7 @@ __global__ void __launch_bounds__(kBlock) k_recover_cells(mpasg_mesh m, mpasg_fi
           dex = exb * pow1p_rcv_m1(x);
           ex = exb + dex;
         } else {
-          ex = pow(zz * (kRgas / kP0) * (rtheta_p + rtb), rcv);
+          ex = mpasg_pow::pow_exner(zz * (kRgas / kP0) * (rtheta_p + rtb), rcv);
           dex = ex - exb;
         }
         f.exner[o] = ex;

@@ -2,6 +2,7 @@
 // cell-centre wind reconstruction (dynamics/vector_reconstruction.py:311) and the
 // cold-start coupled diagnostics (dynamics/init_coupled_diagnostics.py:147).
 #include "common.cuh"
+#include "pow_exner.cuh"
 
 namespace {
 
@@ -316,8 +317,8 @@ __global__ void k_prepare_cells(mpasg_mesh m, mpasg_fields f, FastDiv fl, const 
   double rtb = tb * rb;
   // unfused products: rtheta_p cancels to roundoff when the state is near the base state
   double rtp = __dadd_rn(__dmul_rn(theta_m, rho_p), __dmul_rn(rb, theta_m - tb));
-  double ex = pow(zz * (kRgas / kP0) * (rtp + rtb), rcv);
-  double exb = pow(zz * (kRgas / kP0) * rtb, rcv);
+  double ex = mpasg_pow::pow_exner(zz * (kRgas / kP0) * (rtp + rtb), rcv);
+  double exb = mpasg_pow::pow_exner(zz * (kRgas / kP0) * rtb, rcv);
   f.theta_m[i] = theta_m;
   f.rho_zz[i] = rho_zz;
   f.rho_p[i] = rho_p;

@@ -13,6 +13,7 @@
 #include <cmath>
 
 #include "adj_common.cuh"
+#include "pow_exner.cuh"
 
 namespace {
 
@@ -326,7 +327,7 @@ __global__ void k_tan_recover_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields d
     if (rk_step == 3) {
       const double rcv = kRgas / (kCp - kRgas);
       const double zz = m.zz[o];
-      const double ex = pow(zz * (kRgas / kP0) * (rtp + rtb), rcv);
+      const double ex = mpasg_pow::pow_exner(zz * (kRgas / kP0) * (rtp + rtb), rcv);
       const double dex = rcv * ex * drtp / (rtp + rtb);
       d.exner[o] = dex;
       d.pressure_p[o] = zz * kRgas * (dex * rtp + ex * drtp + rtb * dex);

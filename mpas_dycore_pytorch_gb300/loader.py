@@ -234,7 +234,10 @@ def load_arrays(init: Mapping[str, Any], grid: Mapping[str, Any], config: Mappin
         g = src[e0, side]  # (nc, maxe, L+1)
         g = g * slot_ok[..., None]
         out[name + "_cell"] = _pad(g * scale)
-    # Rayleigh damping coefficient
+    # Rayleigh damping coefficient: an initial-condition file's nonzero dss is kept as it
+    # is (ic_loader.py:762-766), else computed (initialization.py:333)
+    given = out.get("dss")
+    keep = isinstance(given, np.ndarray) and given.shape == (nc + 1, nl) and bool(np.any(given[:nc] != 0))
     zgrid = out["zgrid"][:nc, : nl + 1]
     zt = zgrid[:, nl]
     zmid = 0.5 * (zgrid[:, :nl] + zgrid[:, 1:nl + 1])
@@ -242,7 +245,8 @@ def load_arrays(init: Mapping[str, Any], grid: Mapping[str, Any], config: Mappin
     xnutr = float(cfg.get("config_xnutr", 0.2))
     arg = 0.5 * math.acos(-1.0) * (zmid - zd) / (zt[:, None] - zd)
     raw = xnutr * np.sin(arg) ** 2.0 / dens[:nc, None] ** 0.25
-    out["dss"] = _pad(np.where(zmid > zd, raw, 0.0))
+    if not keep:
+        out["dss"] = _pad(np.where(zmid > zd, raw, 0.0))
     # reconstruction geometry
     xc = np.stack([out["xCell"][:nc], out["yCell"][:nc], out["zCell"][:nc]], -1)
     xe = np.stack([out["xEdge"][:ne], out["yEdge"][:ne], out["zEdge"][:ne]], -1)

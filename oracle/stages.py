@@ -13,6 +13,8 @@ slot weight formed before it multiplies the gathered value.
 
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 GRAVITY = 9.80616
@@ -22,6 +24,14 @@ CP = 1004.5
 CV = 717.5
 P0 = 100000.0
 OMEGA = 7.29212e-5
+
+def exner_pow(x, rcv):
+    """x**rcv by the C library's scalar pow, element by element: what the reference's
+    torch pow computes on its default (non-vectorised) CPU path, where NumPy's vectorised
+    power may round the last bit differently."""
+    x = np.asarray(x, dtype=np.float64)
+    return np.fromiter((math.pow(v, rcv) for v in x.ravel()), np.float64, x.size).reshape(x.shape)
+
 
 __all__ = [
     "idx0", "moist_coefficients", "vert_imp_coefs", "tridiagonal_solve",
@@ -329,7 +339,7 @@ def recover_large_step(a):
     if rk_step == 3:
         rcv = RGAS / (CP - RGAS)
         zz = S("zz")
-        exner = (zz * (RGAS / P0) * (rtheta_p + S("rtheta_base"))) ** rcv
+        exner = exner_pow(zz * (RGAS / P0) * (rtheta_p + S("rtheta_base")), rcv)
         pressure_p = zz * RGAS * (exner * rtheta_p + S("rtheta_base") * (exner - S("exner_base")))
         out["exner"] = np.concatenate([exner, np.zeros((1, nl))])
         out["pressure_p"] = np.concatenate([pressure_p, np.zeros((1, nl))])

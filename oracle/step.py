@@ -150,8 +150,8 @@ class Stepper:
         rtheta_base = theta_base * rho_base
         rtheta_p = theta_m * rho_p + rho_base * (theta_m - theta_base)
         rcv = S.RGAS / (S.CP - S.RGAS)
-        exner = (zz * (S.RGAS / S.P0) * (rtheta_p + rtheta_base)) ** rcv
-        exner_base = (zz * (S.RGAS / S.P0) * rtheta_base) ** rcv
+        exner = S.exner_pow(zz * (S.RGAS / S.P0) * (rtheta_p + rtheta_base), rcv)
+        exner_base = S.exner_pow(zz * (S.RGAS / S.P0) * rtheta_base, rcv)
         pressure_p = zz * S.RGAS * (exner * rtheta_p + rtheta_base * (exner - exner_base))
         pressure_base = zz * S.RGAS * exner_base * rtheta_base
 

@@ -36,3 +36,19 @@ def sha256_f64(a) -> str:
 def active(name: str, a: np.ndarray, dims) -> np.ndarray:
     n = dims["nEdges"] if name in EDGE_FIELDS else dims["nVertices"] if name == "vorticity" else dims["nCells"]
     return a[:n]
+
+
+def case_digest_mismatches(meta) -> list[str]:
+    """Raw case arrays (cases.make_case on this machine) whose SHA-256 differs from the one
+    recorded beside the reference run: the run would not start from the reference's inputs."""
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec, make_case
+    init, grid = make_case(CaseSpec(**meta["spec"]))
+    got = {}
+    for tag, d in (("init", init), ("grid", grid)):
+        for k, v in d.items():
+            if isinstance(v, np.ndarray):
+                a = np.ascontiguousarray(v, dtype="<f8" if v.dtype.kind == "f" else "<i8")
+                got[f"{tag}/{k}"] = hashlib.sha256(a.tobytes()).hexdigest()
+    want = meta["case_sha256"]
+    return sorted(k for k in set(want) | set(got) if want.get(k) != got.get(k))
+

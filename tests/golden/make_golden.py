@@ -72,10 +72,10 @@ def _import_reference():
 
 
 CASES = {
-    # configs[0]-style: uniform levels, one cosine-bell tracer, non-monotone transport
+    # like the level-4 CPU-runnable case: uniform levels, one cosine-bell tracer, non-monotone transport
     "g2_explicit": dict(spec=dict(level=2, nlev=12, seed=0, n_bumps=8, n_tracers=1),
                         config=dict(config_monotonic=False), dt=1800.0, nsteps=2),
-    # configs[1]-style: stretched levels, three tracers, monotone transport
+    # like the level-6 headline case: stretched levels, three tracers, monotone transport
     "g2_mono": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=1, n_bumps=8, n_tracers=3),
                     config=dict(config_monotonic=True), dt=1800.0, nsteps=2),
     # moist: water vapour as scalar 0 (moist coefficients cqw / cqu != 1, theta_m != theta)

@@ -1,15 +1,17 @@
 """Reference runs at the benchmark's own sizes, stored as compact fixtures.
 
-* ``full_c0``: configs[0] -- level-4 mesh (2562 cells x 26 levels), seed 0, 8 bumps, one
+* ``full_c0``: the CPU-runnable case -- level-4 mesh (2562 cells x 26 levels), seed 0, 8 bumps, one
   cosine-bell tracer, non-monotone transport, dt 1800 s, 6 steps; the state after steps 2
   and 6;
-* ``full_c1``: configs[1] -- level-6 mesh (40962 cells x 55 levels, lowest layer 50 m), seed
+* ``full_c1``: the headline case -- level-6 mesh (40962 cells x 55 levels, lowest layer 50 m), seed
   1, 32 bumps, 3 monotone tracers, dt 720 s; the state after 2 and 96 steps.
 
 The arrays are too large to commit whole, so each field is stored as every ``stride``-th
 row of the case (the last active row always included) at full precision, with its full active-row
 sum of squares and a SHA-256 of its active rows (little-endian float64).  The loaded
-connectivity's digests are stored too, so a test can check it runs the same mesh.
+connectivity's digests are stored too, and the SHA-256 of every raw array of the synthetic
+case (``cases.make_case``, float arrays as little-endian float64), so that a run on another
+machine can check it starts from the very inputs the reference started from.
 
 Writes ``full_<case>.npz`` and ``full_<case>.json``.  Imports the reference as
 ``make_golden.py`` does (netCDF4 stub, ``MPAS_REFERENCE``).
@@ -67,6 +69,17 @@ def digest(a):
     return hashlib.sha256(a.tobytes()).hexdigest()
 
 
+def case_digests(init, grid):
+    """SHA-256 of every array of the raw case (init/... and grid/...)."""
+    out = {}
+    for tag, d in (("init", init), ("grid", grid)):
+        for k, v in sorted(d.items()):
+            if isinstance(v, np.ndarray):
+                a = np.ascontiguousarray(v, dtype="<f8" if v.dtype.kind == "f" else "<i8")
+                out[f"{tag}/{k}"] = hashlib.sha256(a.tobytes()).hexdigest()
+    return out
+
+
 def record(out, meta, tag, state, dims, stride):
     for k in FIELDS:
         if k not in state:
@@ -90,6 +103,8 @@ def main() -> None:
                 "torch": torch.__version__,
                 "connectivity_sha256": {k: digest(np.asarray(mesh[k].numpy() if hasattr(mesh[k], "numpy") else mesh[k],
                                                               dtype=np.float64)) for k in CONNECTIVITY if k in mesh}}
+        from mpas_dycore_pytorch_gb300.cases import CaseSpec, make_case
+        meta["case_sha256"] = case_digests(*make_case(CaseSpec(**case["spec"])))
         out = {}
         want = set(case["steps"])
         t0 = time.time()

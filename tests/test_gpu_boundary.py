@@ -5,8 +5,8 @@ g2_explicit case (``tests/golden/make_golden_boundary.py``):
 * the device digest of a tensor equals the host digest of the same bytes;
 * one step and one more from the returned (bound) boundary equal two steps, bit for bit;
 * a boundary whose prognostics theta_m and u were edited is re-derived before the step,
-  and matches the reference's continuation of the same edit (relative L2 1e-12; w and rw
-  1e-11, the Exner-function bound of the step parity tests);
+  and matches the reference's continuation of the same edit (relative L2 1e-12, the bound
+  of the step parity tests);
 * an edited diagnostic and another time step are rejected with the reference's messages;
 * the restart writer refuses an edited boundary.
 """

@@ -49,7 +49,7 @@ def test_level4_two_steps_vs_oracle(mono, options):
     for k in ("u", "w", "theta_m", "rho_zz", "scalars", "exner", "pressure_p", "v", "vorticity",
               "divergence", "ke", "pv_edge", "uReconstructZonal", "ruAvg", "wwAvg"):
         err = rel_l2(to_np(got[k])[:-1], rs[k][:-1])
-        assert err <= 1e-11, (k, err)
+        assert err <= 1e-12, (k, err)
 
 
 def test_monotone_tracers_stay_bounded_level5():
@@ -85,5 +85,5 @@ def test_no_scalars_two_steps_vs_oracle():
     got = model.export()
     for k in ("u", "w", "theta_m", "rho_zz", "exner", "v", "divergence", "uReconstructZonal"):
         err = rel_l2(to_np(got[k])[:-1], rs[k][:-1])
-        assert err <= 1e-11, (k, err)
+        assert err <= 1e-12, (k, err)
     assert model.check_finite() == 0

@@ -17,9 +17,10 @@ FUNCS = {
 # outputs that only hold stage scratch in the reference (not part of the step state)
 SCRATCH = {"flux_arr", "scalar_tend", "scalar_old", "scalar_new", "s_max", "s_min", "wdtn",
            "scale_arr", "flux_upwind_tmp", "flux_tmp"}
-# bitwise-identical float64 algorithm except pow(), whose last-bit rounding differs
-# between libm implementations; pressure_p amplifies that by cancellation
-TOL = 1e-13
+# the same float64 algorithm in the same order, the Exner function by the same C library
+# pow: 1276 of the 1302 stage outputs of the eleven cases are bit-identical, the rest
+# within 8.3e-17 relative L2 (NumPy and torch reductions rounding a last bit differently)
+TOL = 1e-15
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -42,7 +43,4 @@ def test_stage_matches_reference(case, key):
                 g = g[:-1]
             assert g.shape == r.shape, (name, g.shape, r.shape)
             rows = r.shape[0] - 1 if r.shape[0] - 1 in n.values() else r.shape[0]
-            if name == "pressure_p":
-                assert np.max(np.abs(g[:rows] - r[:rows])) < 1e-7
-            else:
-                assert rel_l2(g[:rows], r[:rows]) <= TOL, (entry["stage"], entry["index"], name)
+            assert rel_l2(g[:rows], r[:rows]) <= TOL, (entry["stage"], entry["index"], name)

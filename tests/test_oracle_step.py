@@ -27,10 +27,8 @@ def test_prepare_matches_reference(case):
     ref = group(st, "prepared")
     for k in ("theta_m", "rho_zz", "ru", "rw", "rho_p", "rtheta_p", "exner", "v", "vorticity",
               "divergence", "ke", "pv_edge", "rho_edge", "uReconstructZonal",
-              "uReconstructMeridional"):
+              "uReconstructMeridional", "pressure_p"):
         assert rel_l2(prep[k][:-1], ref[k][:-1]) <= 1e-15, k
-    # pressure_p is ~1e-11 Pa here (bumps at constant pressure): compare absolutely
-    assert np.max(np.abs(prep["pressure_p"][:-1] - ref["pressure_p"][:-1])) < 1e-9
 
 
 @pytest.mark.parametrize("case", CASES)
