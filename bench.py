@@ -269,6 +269,15 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
         ends[prec] = {k: m.state.f[k][:-1].clone() for k in STATE_KEYS}
         if prec == "mixed":
             ms_mixed = _time_steps(m.step, K, W)
+            timed = _timed_step_graph(m, m.lib, K)
+            timed[0].replay()
+            torch.cuda.synchronize()
+            stage_ms, calls_per = _stage_ms(timed, K)
+            roof_mixed = _stage_roofline(stage_ms, calls_per, S, int(st["nCells"]), int(st["nVertLevels"]),
+                                         "mixed", dev)
+            roof_mixed["bytes_model"] = ("float64 units, an upper bound for this form: the stencils read "
+                                         "float32 copies of u, w, rw, pv_edge and the geometry")
+            del timed
         del m
         torch.cuda.empty_cache()
     err = {}
@@ -282,7 +291,7 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
                       "speedup_vs_float64": ms_plain / ms_mixed,
                       "max_rel_l2_vs_float64_after_24_steps": max(err.values()),
                       "worst_field": max(err, key=err.get), "dtype": "f32 stencils / f64 state",
-                      "autotune": tune}
+                      "autotune": tune, "roofline": roof_mixed, "stage_ms_per_step": stage_ms}
     if args.ensemble > 0:
         ew = WORKLOADS["c2"]
         ecfg = _cfg(ew)
@@ -694,6 +703,84 @@ def st_cells_levels(st):
     return int(np.asarray(st["nCells"]).reshape(-1)[0]) * int(np.asarray(st["nVertLevels"]).reshape(-1)[0])
 
 
+def _timed_step_graph(model, lib, K, n_b=128):
+    """One CUDA graph of K large steps through the library's timed step
+    (mpasg_step_timed), which records an event at every stage boundary.  Returns (graph,
+    events, stage kinds, event counts); replay it, then read the stages with _stage_ms."""
+    import ctypes as C
+
+    import torch
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n_b)] for _ in range(K)]
+    for row in evs:
+        for e in row:
+            e.record()  # materialise the cudaEvent_t
+    torch.cuda.synchronize()
+    ptrs = [(C.c_void_p * n_b)(*[C.c_void_p(e.cuda_event) for e in row]) for row in evs]
+    kinds = [(C.c_int32 * n_b)() for _ in range(K)]
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    counts = []
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            for k in range(K):
+                counts.append(lib.mpasg_step_timed(C.byref(model.dmesh.struct), C.byref(model.cstruct),
+                                                   C.byref(model.state.struct), ptrs[k], kinds[k], n_b,
+                                                   C.c_void_p(s.cuda_stream)))
+    torch.cuda.current_stream().wait_stream(s)
+    if min(counts) < 0:
+        raise RuntimeError(f"timed step failed: {counts}")
+    return g, evs, kinds, counts, n_b
+
+
+def _stage_ms(timed, K):
+    """ms per step of every stage and calls per step, from a replayed _timed_step_graph."""
+    from mpas_dycore_pytorch_gb300 import _lib
+    _, evs, kinds, counts, n_b = timed
+    stage_ms, stage_calls = {}, {}
+    for k in range(K):
+        for i in range(1, min(counts[k], n_b)):
+            name = _lib.STAGE_NAMES[kinds[k][i]]
+            stage_ms[name] = stage_ms.get(name, 0.0) + evs[k][i - 1].elapsed_time(evs[k][i])
+            stage_calls[name] = stage_calls.get(name, 0) + 1
+    stage_ms = {k: v / K for k, v in sorted(stage_ms.items(), key=lambda kv: -kv[1])}
+    return stage_ms, {k: v // K for k, v in stage_calls.items()}
+
+
+def _stage_roofline(stage_ms, calls_per, S, C_, L_, precision, dev):
+    """HBM roofline of the dominant stage: the byte model's algorithmic bytes per call (every
+    distinct input read and output written once, float64 units) over the stage's measured
+    time per call; for the float64 form also its float64-pipe roofline."""
+    from mpas_dycore_pytorch_gb300.bytes_model import stage_bytes_per_call
+    peak, peak_kind = measured_peak_hbm()
+    merged = dict(stage_ms)
+    merged["dyn_tend"] = merged.pop("dyn_tend", 0.0) + merged.pop("dyn_tend_rk1", 0.0)
+    merged["acoustic_divdamp"] = merged.pop("acoustic_step", 0.0) + merged.pop("divergence_damping", 0.0)
+    calls = dict(calls_per)
+    calls["dyn_tend"] = calls.get("dyn_tend", 0) + calls.get("dyn_tend_rk1", 0)
+    calls["acoustic_divdamp"] = calls.get("acoustic_step", 0)
+    keymap = {"vert_imp_coefs": "vert_imp_coefs", "dyn_tend": "dyn_tend", "smlstep_pert": "smlstep_pert",
+              "acoustic_divdamp": "acoustic_divdamp", "recover": "recover", "diagnostics": "diagnostics"}
+    dom = max((k for k in merged if k in keymap), key=lambda k: merged[k])
+    per_call_ms = merged[dom] / max(calls[dom], 1)
+    bytes_call = stage_bytes_per_call(keymap[dom], S, C_, L_)
+    achieved = bytes_call / (per_call_ms / 1e3) / 1e9
+    traffic = None
+    if dom in TRAFFIC_B_PER_CELL_LEVEL and precision == "float64":
+        traffic = round(TRAFFIC_B_PER_CELL_LEVEL[dom] * C_ * L_)
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"stage:{dom}",
+            "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_call,
+            "launch_ms": round(per_call_ms, 4)}
+    # the float64 form's real bound: the float64 pipe (GB300 runs float64 at 1/64 of
+    # float32).  Executed float64 flops of the stage from an ncu count, against the
+    # float64 peak measured here with the library's own multiply-add kernel.
+    if dom in FP64_FLOP_PER_CELL_LEVEL and precision == "float64":
+        roof["fp64_pipe"] = fp64_roofline(FP64_FLOP_PER_CELL_LEVEL[dom] * C_ * L_,
+                                          FP64_INST_PER_CELL_LEVEL[dom] * C_ * L_, per_call_ms, dev)
+    return roof
+
+
 def measured_peak_hbm():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -710,7 +797,7 @@ def run_gb300(args, rank, world):
 
     from mpas_dycore_pytorch_gb300 import _lib
     from mpas_dycore_pytorch_gb300.api import Model
-    from mpas_dycore_pytorch_gb300.bytes_model import bytes_per_cell_level_step, stage_bytes_per_call
+    from mpas_dycore_pytorch_gb300.bytes_model import bytes_per_cell_level_step
     from mpas_dycore_pytorch_gb300.cases import CaseSpec
     from mpas_dycore_pytorch_gb300.device import STATE_KEYS
     from mpas_dycore_pytorch_gb300.loader import load_case
@@ -743,41 +830,17 @@ def run_gb300(args, rank, world):
 
     # timed graph: K steps with stage-boundary events
     K, W = args.steps, args.warmup
-    n_b = 128
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n_b)] for _ in range(K)]
     model.capture_graph()
     for _ in range(W):
         model.step()
     torch.cuda.synchronize()
 
     stage_ms = None
-    timed_graph = None
+    timed = None
     try:
-        # record events with the library's timed step inside one K-step graph
-        for row in evs:
-            for e in row:
-                e.record()  # materialise the cudaEvent_t
-        torch.cuda.synchronize()
-        ptrs = [(C.c_void_p * n_b)(*[C.c_void_p(e.cuda_event) for e in row]) for row in evs]
-        kinds = [(C.c_int32 * n_b)() for _ in range(K)]
-        s = torch.cuda.Stream()
-        s.wait_stream(torch.cuda.current_stream())
-        g = torch.cuda.CUDAGraph()
-        counts = []
-        with torch.cuda.stream(s):
-            with torch.cuda.graph(g, stream=s):
-                for k in range(K):
-                    rc = lib.mpasg_step_timed(C.byref(model.dmesh.struct), C.byref(model.cstruct),
-                                              C.byref(model.state.struct), ptrs[k], kinds[k], n_b,
-                                              C.c_void_p(s.cuda_stream))
-                    counts.append(rc)
-        torch.cuda.current_stream().wait_stream(s)
-        if min(counts) < 0:
-            raise RuntimeError(f"timed step failed: {counts}")
-        timed_graph = g
+        timed = _timed_step_graph(model, lib, K)
     except Exception as exc:  # fall back to the plain graph; no stage breakdown
         print(f"[bench] stage-event graph unavailable: {exc}", file=sys.stderr)
-        timed_graph = None
 
     if world > 1:
         import torch.distributed as dist
@@ -787,8 +850,8 @@ def run_gb300(args, rank, world):
     end = torch.cuda.Event(enable_timing=True)
     with ClockSampler(torch.cuda.current_device()) as clocks:
         start.record()
-        if timed_graph is not None:
-            timed_graph.replay()
+        if timed is not None:
+            timed[0].replay()
         else:
             for _ in range(K):
                 model.step()
@@ -801,47 +864,11 @@ def run_gb300(args, rank, world):
         dist.barrier()
     bad = model.check_finite()
 
-    if timed_graph is not None:
-        stage_ms = {}
-        stage_calls = {}
-        for k in range(K):
-            n = counts[k]
-            for i in range(1, min(n, n_b)):
-                name = _lib.STAGE_NAMES[kinds[k][i]]
-                stage_ms[name] = stage_ms.get(name, 0.0) + evs[k][i - 1].elapsed_time(evs[k][i])
-                stage_calls[name] = stage_calls.get(name, 0) + 1
-        stage_ms = {k: v / K for k, v in sorted(stage_ms.items(), key=lambda kv: -kv[1])}
-        calls_per = {k: v // K for k, v in stage_calls.items()}
+    if timed is not None:
+        stage_ms, calls_per = _stage_ms(timed, K)
 
     # roofline of the dominant stage
-    peak, peak_kind = measured_peak_hbm()
-    roof = None
-    if stage_ms:
-        merged = dict(stage_ms)
-        merged["dyn_tend"] = merged.pop("dyn_tend", 0.0) + merged.pop("dyn_tend_rk1", 0.0)
-        merged["acoustic_divdamp"] = merged.pop("acoustic_step", 0.0) + merged.pop("divergence_damping", 0.0)
-        calls = dict(calls_per)
-        calls["dyn_tend"] = calls.get("dyn_tend", 0) + calls.get("dyn_tend_rk1", 0)
-        calls["acoustic_divdamp"] = calls.get("acoustic_step", 0)
-        keymap = {"vert_imp_coefs": "vert_imp_coefs", "dyn_tend": "dyn_tend", "smlstep_pert": "smlstep_pert",
-                  "acoustic_divdamp": "acoustic_divdamp", "recover": "recover", "diagnostics": "diagnostics"}
-        dom = max((k for k in merged if k in keymap), key=lambda k: merged[k])
-        per_call_ms = merged[dom] / max(calls[dom], 1)
-        bytes_call = stage_bytes_per_call(keymap[dom], S, C_, L_)
-        achieved = bytes_call / (per_call_ms / 1e3) / 1e9
-        traffic = None
-        if dom in TRAFFIC_B_PER_CELL_LEVEL and args.precision == "float64":
-            traffic = round(TRAFFIC_B_PER_CELL_LEVEL[dom] * C_ * L_)
-        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"stage:{dom}",
-                "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_call,
-                "launch_ms": round(per_call_ms, 4)}
-        # the float64 form's real bound: the float64 pipe (GB300 runs float64 at 1/64 of
-        # float32).  Executed float64 flops of the stage from an ncu count, against the
-        # float64 peak measured here with the library's own multiply-add kernel.
-        if dom in FP64_FLOP_PER_CELL_LEVEL and args.precision == "float64":
-            roof["fp64_pipe"] = fp64_roofline(FP64_FLOP_PER_CELL_LEVEL[dom] * C_ * L_,
-                                              FP64_INST_PER_CELL_LEVEL[dom] * C_ * L_, per_call_ms, dev)
+    roof = _stage_roofline(stage_ms, calls_per, S, C_, L_, args.precision, dev) if stage_ms else None
 
     # end to end through the public API with pinned host buffers
     keys = [k for k in STATE_KEYS]
