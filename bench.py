@@ -275,8 +275,8 @@ def measure_forms(args, dev, st, cfg, w, ms_plain):
             stage_ms, calls_per = _stage_ms(timed, K)
             roof_mixed = _stage_roofline(stage_ms, calls_per, S, int(st["nCells"]), int(st["nVertLevels"]),
                                          "mixed", dev)
-            roof_mixed["bytes_model"] = ("float64 units, an upper bound for this form: the stencils read "
-                                         "float32 copies of u, w, rw, pv_edge and the geometry")
+            roof_mixed["bytes_model"] = ("v1 units weighted by width: u, pv_edge, w, rw read as float32 in "
+                                         "dyn_tend, everything else float64")
             del timed
         del m
         torch.cuda.empty_cache()
@@ -763,7 +763,7 @@ def _stage_roofline(stage_ms, calls_per, S, C_, L_, precision, dev):
               "acoustic_divdamp": "acoustic_divdamp", "recover": "recover", "diagnostics": "diagnostics"}
     dom = max((k for k in merged if k in keymap), key=lambda k: merged[k])
     per_call_ms = merged[dom] / max(calls[dom], 1)
-    bytes_call = stage_bytes_per_call(keymap[dom], S, C_, L_)
+    bytes_call = stage_bytes_per_call(keymap[dom], S, C_, L_, precision=precision)
     achieved = bytes_call / (per_call_ms / 1e3) / 1e9
     traffic = None
     if dom in TRAFFIC_B_PER_CELL_LEVEL and precision == "float64":

@@ -51,5 +51,15 @@ def bytes_per_cell_level_step(S: int, monotonic: bool = True, width: int = 8, **
     return width * units_per_step(S, monotonic, **kw)
 
 
-def stage_bytes_per_call(stage: str, S: int, n_cells: int, n_levels: int, width: int = 8) -> int:
-    return width * UNITS_PER_CALL[stage](S) * n_cells * n_levels
+# Mixed form: units of each stage that its kernels read as float32 copies (4 B) instead of
+# the float64 state (8 B).  dyn_tend reads u and pv_edge (edge fields, 3 units each), w and
+# rw (W-level fields, 1 unit each) as float32; every other field, and every output, stays
+# float64.  Stages not listed are counted in float64 (an upper bound).
+MIXED_F32_UNITS = {"dyn_tend": 8}
+
+
+def stage_bytes_per_call(stage: str, S: int, n_cells: int, n_levels: int, width: int = 8,
+                         precision: str = "float64") -> int:
+    units = UNITS_PER_CALL[stage](S)
+    f32 = MIXED_F32_UNITS.get(stage, 0) if precision == "mixed" else 0
+    return (width * (units - f32) + 4 * f32) * n_cells * n_levels
