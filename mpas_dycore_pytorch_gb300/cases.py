@@ -626,8 +626,10 @@ def write_case_files(spec: CaseSpec, directory, radius: float = EARTH_RADIUS, cl
     d = pathlib.Path(directory)
     d.mkdir(parents=True, exist_ok=True)
     init, grid = make_case(spec, radius)
-    init = dict(init, nCells=grid["nCells"], nEdges=grid["nEdges"], nVertices=grid["nVertices"],
-                maxEdges=grid["maxEdges"], nVertLevels=int(spec.nlev))
+    # an init_atmosphere output file carries the grid's fields too (readers take the mesh
+    # dimensions from them)
+    init = dict(grid, **init)
+    init["nVertLevels"] = int(spec.nlev)
     tag = f"x1.{grid['nCells']}"
     grid_path, init_path = d / f"{tag}.grid.nc", d / f"{tag}.init.nc"
     write_mpas_fields(grid_path, grid, attrs={"sphere_radius": float(radius)}, clobber=clobber)

@@ -60,10 +60,55 @@ __version__ = "0.0-stub"
 '''
 
 
-def _import_reference():
+# A read-only stand-in for the netCDF4 package (absent here; the reference pins 1.7.4): the
+# part of its documented API the reference's CheckpointReader uses -- Dataset(path, "r") as
+# a context manager, .variables / .dimensions, a variable's [:] (native byte order), dtype,
+# shape, size and dimensions -- over scipy's NetCDF-3 reader.  make_golden_files.py uses it
+# so that the reference's own load_initial_state reads the case files this package writes.
+_READER_STUB = '''
+import numpy as _np
+from scipy.io import netcdf_file as _netcdf_file
+
+class Variable:
+    def __init__(self, v):
+        self._v = v
+        self.dimensions = tuple(v.dimensions)
+        self.shape = tuple(v.shape)
+        self.dtype = v.data.dtype.newbyteorder("=")
+        self.size = int(_np.prod(self.shape)) if self.shape else 1
+    def __getitem__(self, idx):
+        a = _np.asarray(self._v.data)
+        a = a.astype(a.dtype.newbyteorder("="))
+        return _np.array(a) if a.ndim == 0 else _np.array(a[idx])
+
+class _Dim:
+    def __init__(self, n):
+        self.size = n
+    def __len__(self):
+        return self.size
+
+class Dataset:
+    def __init__(self, path, mode="r", **kw):
+        if mode != "r":
+            raise RuntimeError("netCDF4 stand-in: read-only")
+        self._f = _netcdf_file(str(path), "r", mmap=False)
+        self.variables = {k: Variable(v) for k, v in self._f.variables.items()}
+        self.dimensions = {k: _Dim(n if n is not None else 1) for k, n in self._f.dimensions.items()}
+    def close(self):
+        self._f.close()
+    def __enter__(self):
+        return self
+    def __exit__(self, *a):
+        self.close()
+
+__version__ = "0.0-scipy-netcdf3-reader"
+'''
+
+
+def _import_reference(stub: str = _STUB):
     stub_dir = pathlib.Path(tempfile.mkdtemp(prefix="ncstub_"))
     (stub_dir / "netCDF4").mkdir()
-    (stub_dir / "netCDF4" / "__init__.py").write_text(_STUB)
+    (stub_dir / "netCDF4" / "__init__.py").write_text(stub)
     sys.path.insert(0, str(stub_dir))
     sys.path.insert(0, str(_reference_root()))
     sys.path.insert(0, str(REPO))
