@@ -5,6 +5,7 @@ stated size (tests/golden/make_golden_dyn_ad_full.py: level-5 mesh 10242 cells x
 * run_simulation.vjp of the area-weighted squared surface-pressure anomaly with respect to
   the initial u and theta, within the stated 1e-10 relative L2 on the fixture's sampled
   rows and by full-field norm, and the functional itself within 1e-12;
+* the mixed form's gradient within the stated 1e-4 of the reference's;
 * run_simulation.jvp along the recorded direction, within 1e-10 or, where larger, the
   tangent's own conditioning (its change when u and theta move by one unit in the last
   place; the Smagorinsky coefficient's derivative follows roundoff, see test_gpu_dyn_jvp).
@@ -92,6 +93,24 @@ def test_gradient_matches_reference_at_workload_size():
     J = float(objective(final))
     print(f"J: {J:.15e} vs reference {meta['J']:.15e}")
     assert abs(J - meta["J"]) <= 1e-12 * abs(meta["J"])
+
+
+def test_mixed_form_gradient_within_1e4_of_reference_at_workload_size():
+    """The mixed form's gradient (float32 stencils in the forward and its taped recompute,
+    the reverse pass in float64 about that trajectory) against the reference's float64 VJP:
+    rel L2 <= 1e-4."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import run_simulation
+    meta, arr = _fixture()
+    st, cfg = _case(meta)
+    state = {k: torch.as_tensor(v) for k, v in st.items() if isinstance(v, np.ndarray)}
+    grads = run_simulation.vjp(state, st, _objective(st, arr["sp_ref"]), track_keys=TRACK,
+                               config=dict(cfg, config_precision="mixed"), dt=float(meta["dt"]),
+                               nsteps=int(meta["nsteps"]))
+    for k in TRACK:
+        err = _compare(meta, arr, f"grad_{k}", to_np(grads[k]))
+        print(f"mixed grad_{k}: rel L2 vs reference {err:.3e}")
+        assert err <= 1e-4, (k, err)
 
 
 def test_tangent_matches_reference_at_workload_size():
