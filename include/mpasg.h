@@ -438,8 +438,11 @@ int mpasg_tridiag_factor_jvp(long long n, int L, const double *a, const double *
  * autodiff/soft_limiter.py:1-10.  Cotangents live in a second mpasg_fields `g` with the same
  * layout as the forward fields: g->u is the cotangent of u, and so on.  Every transposed
  * stencil is a deterministic gather (no atomics).  Scope: float64 arithmetic, dry columns
- * (moist_end < moist_start), flat terrain, no vertical mixing, CAM or Rayleigh damping of u;
- * anything else returns MPASG_E_ARG.  The step entries (mpasg_step_tape / _vjp_taped /
+ * (moist_end < moist_start), flat terrain; every mixing and damping option of the
+ * tendencies (2d_smagorinsky / 2d_fixed del2 and del4, vertical mixing of u, w and theta of
+ * the full state or of the perturbation from the initial profiles, CAM-style top-level
+ * damping, Rayleigh damping of u), the max of the CAM floor frozen as taken (a tie split
+ * evenly); anything else returns MPASG_E_ARG.  The step entries (mpasg_step_tape / _vjp_taped /
  * _vjp) also take the mixed form: the tape then holds the mixed form's trajectory (its own
  * stage calls) and the reverse pass linearises it in float64.  The mass-flux averages ruAvg / wwAvg carry no
  * cotangent: they feed only the scalar transport, whose dependence on the dynamics is not
@@ -545,7 +548,7 @@ int mpasg_prepare_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *
 /* ---- dynamics derivatives (forward mode) --------------------------------------------
  * Tangents along the dynamics (the reference's run_simulation.jvp, atmosphere_model.py:2041,
  * through atm_srk3 under torch forward-mode AD), in the scope of the reverse mode above
- * (float64, dry, flat terrain, no vertical mixing, CAM or Rayleigh damping of u).  d is a
+ * (float64, dry, flat terrain, every mixing and damping option).  d is a
  * second mpasg_fields of the same layout holding the tangents under the forward field
  * names; its padding rows hold zeros.  Every entry advances the values f through the stage
  * (as the forward entry point does) and the tangents d alongside; the branches the forward

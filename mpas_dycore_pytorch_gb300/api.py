@@ -822,8 +822,9 @@ def run_simulation_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any], object
 
     * ``track_keys`` within ``("u", "w", "theta", "rho")``: the loaded wind, vertical wind,
       potential temperature and density, through the preparation and the dynamics (the
-      hand-written reverse mode of dyn_adjoint.py: dry, flat terrain, float64; the
-      objective may read the step boundary's carried fields);
+      hand-written reverse mode of dyn_adjoint.py: dry, flat terrain, float64 or the mixed
+      form, every mixing and damping option; the objective may read the step boundary's
+      carried fields);
     * ``track_keys=("scalars",)``: the transported scalars, by the hand-written transposed
       transport (``mpasg_transport_vjp``; passive scalars, explicit split transport)."""
     from .tracer_adjoint import scalars_vjp

@@ -33,11 +33,46 @@ inline AdjWork adj_work(const mpasg_mesh* m, double* w) {
   return a;
 }
 
-// Supported configurations of the dynamics derivatives (see mpasg.h).
+// Supported configurations of the dynamics derivatives (see mpasg.h): the arrays the
+// vertical mixing reads (zgrid; the initial profiles of its perturbation form) must be there
 inline bool adj_supported(const mpasg_mesh* m, const mpasg_config* c) {
-  return m->flatTerrain && c->moist_end < c->moist_start && !(c->v_mom_eddy_visc2 > 0.0) &&
-         !(c->v_theta_eddy_visc2 > 0.0) && !(c->mpas_cam_coef > 0.0 && c->number_cam_damping_levels > 0) &&
-         c->rayleigh_damp_u_levels <= 0 && m->nVertLevels >= 4;
+  const bool vmix = c->v_mom_eddy_visc2 > 0.0 || c->v_theta_eddy_visc2 > 0.0;
+  if (vmix && !m->zgrid) return false;
+  if (vmix && c->mix_perturbation && (!m->u_init || !m->v_init || !m->angleEdge || !m->t_init)) return false;
+  if (c->number_cam_damping_levels > m->nVertLevels || c->rayleigh_damp_u_levels > m->nVertLevels) return false;
+  return m->flatTerrain && c->moist_end < c->moist_start && m->nVertLevels >= 4;
+}
+
+// Damping options the derivatives differentiate, with the forward's expressions
+// (kern_tend.cu TendScalars): CAM-style top-level kdiff floor base * (1 - (L - (k + 1)) /
+// ncam) for the top ncam levels (dyn_tend.py:3434-3456), Rayleigh damping of u on the top
+// ray_n levels with coefficient ((k + 1) - (L - ray_n)) * ray_coef (dyn_tend.py:2956-2990),
+// vertical mixing coefficients of u / w and theta (0: off)
+struct AdjDamping {
+  double cam_base, ray_coef, v_mom, v_theta;
+  int ncam, ray_n;
+};
+inline AdjDamping adj_damping(const mpasg_config* c) {
+  AdjDamping d;
+  d.ncam = (c->mpas_cam_coef > 0.0 && c->number_cam_damping_levels > 0) ? c->number_cam_damping_levels : 0;
+  d.cam_base = 4.0 * 2.0833 * c->len_disp * c->mpas_cam_coef;
+  d.ray_n = c->rayleigh_damp_u_levels > 0 ? c->rayleigh_damp_u_levels : 0;
+  d.ray_coef = d.ray_n > 0 ? 1.0 / ((double)d.ray_n * (c->rayleigh_damp_u_timescale_days * 86400.0)) : 0.0;
+  d.v_mom = c->v_mom_eddy_visc2 > 0.0 ? c->v_mom_eddy_visc2 : 0.0;
+  d.v_theta = c->v_theta_eddy_visc2 > 0.0 ? c->v_theta_eddy_visc2 : 0.0;
+  return d;
+}
+// the CAM floor of kdiff at level k (k >= L - ncam)
+MPASG_D double adj_cam_floor(const AdjDamping& d, int k, int L) {
+  return d.cam_base * (1.0 - (double)(L - (k + 1)) / (double)d.ncam);
+}
+// derivative factor of max(x, floor) with respect to x: 1, 0 or, on a tie, 1/2 (torch's
+// maximum splits a tie evenly)
+MPASG_D double adj_max_factor(double x, double floor) { return x > floor ? 1.0 : (x == floor ? 0.5 : 0.0); }
+// Rayleigh damping coefficient of u at level k (0 below the damped layer)
+MPASG_D double adj_ray_damp(const AdjDamping& d, int k, int L) {
+  const int k0 = L - d.ray_n;
+  return (d.ray_n <= 0 || k < k0) ? 0.0 : (((double)k + 1.0) - (double)k0) * d.ray_coef;
 }
 
 // 1 when cell c is the second cell (cellsOnEdge[e][1]) of edge e

@@ -21,6 +21,8 @@ namespace {
 struct AdjTendScalars {
   double cs2, kdiff_cap, h_mom_visc4, h_theta_visc4, del4u_div, coef3, visc2;
   int rk_step, smag, del4;
+  int mix_pert;  // vertical mixing of the perturbation from the initial profiles
+  AdjDamping dm;  // CAM floor of kdiff, Rayleigh damping of u, vertical mixing
 };
 
 // ---- values: mass-flux divergence (every rk) and, at rk 1, Smagorinsky deformation and kdiff
@@ -54,11 +56,13 @@ __global__ void k_tadj_values(mpasg_mesh m, mpasg_fields f, FastDiv fl, AdjTendS
       dd = ndd;
       dof = ndo;
     }
-    kd[i] = fmin(__dmul_rn(p.cs2, sqrt(__dadd_rn(__dmul_rn(dd, dd), __dmul_rn(dof, dof)))), p.kdiff_cap);
+    double kdv = fmin(__dmul_rn(p.cs2, sqrt(__dadd_rn(__dmul_rn(dd, dd), __dmul_rn(dof, dof)))), p.kdiff_cap);
+    if (p.dm.ncam > 0 && (int)k >= L - p.dm.ncam) kdv = fmax(kdv, adj_cam_floor(p.dm, (int)k, L));
+    kd[i] = kdv;
     dd_out[i] = dd;
     do_out[i] = dof;
   } else {
-    kd[i] = p.visc2;
+    kd[i] = (p.dm.ncam > 0 && (int)k >= L - p.dm.ncam) ? fmax(p.visc2, adj_cam_floor(p.dm, (int)k, L)) : p.visc2;
   }
 }
 
@@ -509,6 +513,11 @@ __global__ void __launch_bounds__(kBlock) k_tadj_u(mpasg_mesh m, mpasg_fields f,
   double gh = G * (q - (f.ke[i2] - f.ke[i1]) * inv_dc);
   pke[i] = G * rho_e * inv_dc;
   double gu = -G * 0.5 * (hd[i1] + hd[i2]) + 0.5 * (pv_self * s3 + s4);
+  const double ray = adj_ray_damp(p.dm, k, L);  // tu - rho_edge u damp (every RK stage)
+  if (ray != 0.0) {
+    gu -= G * rho_e * ray;
+    gh -= G * u_self * ray;
+  }
   g.pv_edge[i] += 0.5 * (G * rho_e * s1 + u_self * s3);
   phd[i] = -G * u_self * 0.5;
   // vertical transport: interfaces k-1 .. k+2 of this edge
@@ -849,7 +858,11 @@ __global__ void k_tadj_kdiff(mpasg_mesh m, FastDiv fl, AdjTendScalars p, const d
   const double dd = ddb_io[i], dof = dob_io[i];
   const double sq = sqrt(__dadd_rn(__dmul_rn(dd, dd), __dmul_rn(dof, dof)));
   const double A = __dmul_rn(p.cs2, sq);
-  const double gA = A < p.kdiff_cap ? kdb[i] : (A == p.kdiff_cap ? 0.5 * kdb[i] : 0.0);
+  double gk = kdb[i];
+  const int k = (int)(i - fl.div(i) * (uint32_t)L);
+  if (p.dm.ncam > 0 && k >= L - p.dm.ncam)  // max(kdiff, CAM floor): the branch taken
+    gk *= adj_max_factor(fmin(A, p.kdiff_cap), adj_cam_floor(p.dm, k, L));
+  const double gA = A < p.kdiff_cap ? gk : (A == p.kdiff_cap ? 0.5 * gk : 0.0);
   const double gs = sq > 0.0 ? gA * p.cs2 * 0.5 / sq : 0.0;
   ddb_io[i] = gs * 2.0 * dd;
   dob_io[i] = gs * 2.0 * dof;
@@ -914,6 +927,116 @@ __global__ void k_tadj_hdiv(mpasg_mesh m, mpasg_fields g, mpasg_transpose t, Fas
   g.ru[i] += a;
 }
 
+// ---- rk 1: vertical mixing of u (k_tend_u_finish) read backwards.  At level q (1 <= q <=
+// L-2) of an edge: teu += h v (d_up - d_dn) / den, d_up = (u_(q+1) - u_q) / (zp - z0),
+// d_dn = (u_q - u_(q-1)) / (z0 - zm), heights the edge means of the two cells' interfaces;
+// level k gathers the terms of levels k-1, k, k+1.  The perturbation form's initial profiles
+// are constants: they enter only the value d_up - d_dn that rho_edge's cotangent reads.
+__global__ void k_tadj_vmix_u(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl, AdjTendScalars p) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
+  const double* z1p = m.zgrid + (size_t)c1 * (L + 1);
+  const double* z2p = m.zgrid + (size_t)c2 * (L + 1);
+  const size_t oe = (size_t)e * L;
+  const double v = p.dm.v_mom;
+  double gu = 0.0, gh = 0.0;
+  for (int q = k - 1; q <= k + 1; ++q) {
+    if (q < 1 || q > L - 2) continue;
+    const double za = 0.5 * (z1p[q - 1] + z2p[q - 1]), zb = 0.5 * (z1p[q] + z2p[q]);
+    const double zc = 0.5 * (z1p[q + 1] + z2p[q + 1]), zd = 0.5 * (z1p[q + 2] + z2p[q + 2]);
+    const double zm = 0.5 * (za + zb), z0 = 0.5 * (zb + zc), zp = 0.5 * (zc + zd);
+    const double den = 0.5 * (zp - zm);
+    const double G = g.tend_u[oe + q] + g.tend_u_euler[oe + q];  // cotangent of the final teu
+    const double a = G * (f.h_edge[oe + q] * v) / den;
+    if (q == k) {
+      gu -= a / (zp - z0) + a / (z0 - zm);
+      double um = f.u[oe + q - 1], u0 = f.u[oe + q], up = f.u[oe + q + 1];
+      if (p.mix_pert) {
+        const double ca = cos(m.angleEdge[e]), sa = sin(m.angleEdge[e]);
+        um = um - m.u_init[q - 1] * ca - m.v_init[q - 1] * sa;
+        u0 = u0 - m.u_init[q] * ca - m.v_init[q] * sa;
+        up = up - m.u_init[q + 1] * ca - m.v_init[q + 1] * sa;
+      }
+      gh += G * v * ((up - u0) / (zp - z0) - (u0 - um) / (z0 - zm)) / den;
+    } else if (q == k - 1) {
+      gu += a / (zp - z0);
+    } else {
+      gu += a / (z0 - zm);
+    }
+  }
+  g.u[i] += gu;
+  g.h_edge[i] += gh;
+}
+
+// ---- rk 1: vertical mixing of w and theta (k_tend_w_theta) read backwards (index space
+// C x (L+1)).  w at interface q (1 <= q <= L-1): v rho_half (w_up - w_down) rdzu_q with
+// rho_half the mean of rho_zz at q-1, q, w_up = (w_(q+1) - w_q) rdzw_q, w_down = (w_q -
+// w_(q-1)) rdzw_(q-1), cotangent tweb_q; theta at level q (1 <= q <= L-2): v rho_zz_q diff /
+// den, diff = (t_(q+1) - t_q) / (zp - z0) - (t_q - t_(q-1)) / (z0 - zm) from the cell's own
+// heights, cotangent tteb_q.  Interface / level j gathers the terms that read it.
+__global__ void k_tadj_vmix_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl1, AdjTendScalars p,
+                                  const double* __restrict__ tweb, const double* __restrict__ tteb) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * (L + 1)) return;
+  const uint32_t c = fl1.div(i);
+  const int j = (int)(i - c * (L + 1));
+  const size_t oc = (size_t)c * L, ow = (size_t)c * (L + 1);
+  const double* rz = f.rho_zz + oc;
+  if (p.dm.v_mom > 0.0) {
+    const double v = p.dm.v_mom;
+    const double* w = f.w + ow;
+    double gw = 0.0, gr = 0.0;
+    for (int q = j - 1; q <= j + 1; ++q) {
+      if (q < 1 || q > L - 1) continue;
+      const double b = tweb[ow + q] * v * m.rdzu[q];
+      const double rho_half = 0.5 * (rz[q] + rz[q - 1]);
+      if (q == j + 1) gw += b * rho_half * m.rdzw[q - 1];                    // w_(q-1) in w_down
+      if (q == j) gw -= b * rho_half * (m.rdzw[q] + m.rdzw[q - 1]);          // w_q in both
+      if (q == j - 1) gw += b * rho_half * m.rdzw[q];                        // w_(q+1) in w_up
+      if (j < L && (q == j || q == j + 1)) {                                   // rho_zz_j in rho_half
+        const double wu = (w[q + 1] - w[q]) * m.rdzw[q], wd = (w[q] - w[q - 1]) * m.rdzw[q - 1];
+        gr += 0.5 * b * (wu - wd);
+      }
+    }
+    g.w[ow + j] += gw;
+    if (j < L) g.rho_zz[oc + j] += gr;
+  }
+  if (p.dm.v_theta > 0.0 && j < L) {
+    const double v = p.dm.v_theta;
+    const double* zg = m.zgrid + (size_t)c * (L + 1);
+    const double* th = f.theta_m + oc;
+    const double* ti = p.mix_pert ? m.t_init + oc : nullptr;
+    double gt = 0.0, gr = 0.0;
+    for (int q = j - 1; q <= j + 1; ++q) {
+      if (q < 1 || q > L - 2) continue;
+      const double zm = 0.5 * (zg[q - 1] + zg[q]), z0 = 0.5 * (zg[q] + zg[q + 1]), zp = 0.5 * (zg[q + 1] + zg[q + 2]);
+      const double den = 0.5 * (zp - zm);
+      const double a = tteb[oc + q] * (v * 1.0 * rz[q]) / den;
+      if (q == j) {
+        gt -= a / (zp - z0) + a / (z0 - zm);
+        double tm = th[q - 1], t0 = th[q], tp = th[q + 1];
+        if (p.mix_pert) {
+          tm = tm - ti[q - 1];
+          t0 = t0 - ti[q];
+          tp = tp - ti[q + 1];
+        }
+        gr += tteb[oc + q] * v * 1.0 * ((tp - t0) / (zp - z0) - (t0 - tm) / (z0 - zm)) / den;
+      } else if (q == j - 1) {
+        gt += a / (zp - z0);
+      } else {
+        gt += a / (z0 - zm);
+      }
+    }
+    g.theta_m[oc + j] += gt;
+    g.rho_zz[oc + j] += gr;
+  }
+}
+
 #define CHECK_RC(x)                  \
   do {                               \
     int _rc = (x);                   \
@@ -944,6 +1067,8 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   p.coef3 = c->coef_3rd_order;
   p.rk_step = rk_step;
   p.del4 = p.h_mom_visc4 > 0.0 ? 1 : 0;
+  p.mix_pert = c->mix_perturbation ? 1 : 0;
+  p.dm = adj_damping(c);
   FastDiv fl(L), fl1(L + 1);
   // work: cells
   double* hd = w.c[0];
@@ -997,6 +1122,10 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   if (rk_step == 1) {
     k_tadj_wres<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, *g, fl, tweb);
     MPASG_LAUNCH_CHECK();
+    if (p.dm.v_mom > 0.0 || p.dm.v_theta > 0.0) {
+      k_tadj_vmix_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, *g, fl1, p, tweb, tteb);
+      MPASG_LAUNCH_CHECK();
+    }
   }
   uint8_t* sel = reinterpret_cast<uint8_t*>(w.e[2]);  // (E+1) x L bytes within one edge array
   k_tadj_adv_edges<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, p, tt1b, tw1b, fltb, flwb, sel);
@@ -1011,6 +1140,10 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   MPASG_LAUNCH_CHECK();
   k_tadj_u_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *g, fl1, p, pke, phd, prwe, ppp, pkd, pd4, hdb, kdb, dsdb);
   MPASG_LAUNCH_CHECK();
+  if (rk_step == 1 && p.dm.v_mom > 0.0) {
+    k_tadj_vmix_u<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, fl, p);
+    MPASG_LAUNCH_CHECK();
+  }
   if (rk_step == 1) {
     if (p.del4) {
       k_tadj_dsv<<<nblocks(nvl), kBlock, 0, s>>>(*m, fl, p, pd4, dsvb);

@@ -17,6 +17,8 @@ namespace {
 struct TanTendScalars {
   double cs2, kdiff_cap, h_mom_visc4, h_theta_visc4, del4u_div, coef3;
   int rk_step, smag, del4;
+  int mix_pert;   // vertical mixing of the perturbation from the initial profiles
+  AdjDamping dm;  // CAM floor of kdiff, Rayleigh damping of u, vertical mixing
 };
 
 // ---- h_divergence, and at rk 1 tend_rho, dpdz and kdiff (k_tend_cells_a)
@@ -61,6 +63,8 @@ __global__ void k_tan_cells_a(mpasg_mesh m, mpasg_fields f, mpasg_fields d, Fast
     const double dA = sq > 0.0 ? p.cs2 * (dd * tdd + dof * tdo) / sq : 0.0;
     // min(A, cap): the branch taken; a tie splits the derivative evenly (torch's minimum)
     dkd = A < p.kdiff_cap ? dA : (A == p.kdiff_cap ? 0.5 * dA : 0.0);
+    // max(kdiff, CAM floor) on the top levels: the branch taken, ties split evenly
+    if (p.dm.ncam > 0 && k >= L - p.dm.ncam) dkd *= adj_max_factor(fmin(A, p.kdiff_cap), adj_cam_floor(p.dm, k, L));
   }
   d.kdiff[i] = dkd;
 }
@@ -112,6 +116,8 @@ __global__ void k_tan_u(mpasg_mesh m, mpasg_fields f, mpasg_fields d, FastDiv fl
   const double keg = (f.ke[i2] - f.ke[i1]) * inv_dc, dkeg = (d.ke[i2] - d.ke[i1]) * inv_dc;
   dtu += drho_e * (q - keg) + rho_e * (dq - dkeg) - d.u[i] * 0.5 * (f.h_divergence[i1] + f.h_divergence[i2]) -
          f.u[i] * 0.5 * (d.h_divergence[i1] + d.h_divergence[i2]);
+  const double ray = adj_ray_damp(p.dm, k, L);  // tu - rho_edge u damp (every RK stage)
+  if (ray != 0.0) dtu -= (drho_e * f.u[i] + rho_e * d.u[i]) * ray;
   if (p.rk_step == 1) {
     const double zzm = 0.5 * (m.zz[i2] + m.zz[i1]);
     double dP = (d.pressure_p[i2] - d.pressure_p[i1]) * inv_dc;
@@ -164,7 +170,7 @@ __global__ void k_tan_del4_cell(mpasg_mesh m, mpasg_fields d, FastDiv fl) {
   d.delsq_div[i] = acc;
 }
 
-// ---- rk 1: del4 filter of u (k_tend_u_finish without vertical mixing)
+// ---- rk 1: del4 filter and vertical mixing of u (k_tend_u_finish)
 __global__ void k_tan_u_finish(mpasg_mesh m, mpasg_fields f, mpasg_fields d, FastDiv fl, TanTendScalars p) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -183,6 +189,28 @@ __global__ void k_tan_u_finish(mpasg_mesh m, mpasg_fields f, mpasg_fields d, Fas
     const double ud4 = (f.delsq_div[i2] - f.delsq_div[i1]) * r_dc4 - (f.delsq_vort[j2] - f.delsq_vort[j1]) * r_dv4;
     const double dud4 = (d.delsq_div[i2] - d.delsq_div[i1]) * r_dc4 - (d.delsq_vort[j2] - d.delsq_vort[j1]) * r_dv4;
     dteu -= d.h_edge[i] * ud4 + f.h_edge[i] * dud4;
+  }
+  if (p.dm.v_mom > 0.0 && k >= 1 && k + 1 < (uint32_t)L) {
+    // teu += h v (d_up - d_dn) / den; the initial profiles of the perturbation form are constants
+    const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
+    const double* z1p = m.zgrid + (size_t)c1 * (L + 1);
+    const double* z2p = m.zgrid + (size_t)c2 * (L + 1);
+    const double za = 0.5 * (z1p[k - 1] + z2p[k - 1]), zb = 0.5 * (z1p[k] + z2p[k]);
+    const double zc = 0.5 * (z1p[k + 1] + z2p[k + 1]), zd = 0.5 * (z1p[k + 2] + z2p[k + 2]);
+    const double zm = 0.5 * (za + zb), z0 = 0.5 * (zb + zc), zp = 0.5 * (zc + zd);
+    const double* u = f.u + (size_t)e * L;
+    const double* du = d.u + (size_t)e * L;
+    double um = u[k - 1], u0 = u[k], up = u[k + 1];
+    if (p.mix_pert) {
+      const double ca = cos(m.angleEdge[e]), sa = sin(m.angleEdge[e]);
+      um = um - m.u_init[k - 1] * ca - m.v_init[k - 1] * sa;
+      u0 = u0 - m.u_init[k] * ca - m.v_init[k] * sa;
+      up = up - m.u_init[k + 1] * ca - m.v_init[k + 1] * sa;
+    }
+    const double den = 0.5 * (zp - zm), v = p.dm.v_mom;
+    const double s = (up - u0) / (zp - z0) - (u0 - um) / (z0 - zm);
+    const double ds = (du[k + 1] - du[k]) / (zp - z0) - (du[k] - du[k - 1]) / (z0 - zm);
+    dteu += v * (d.h_edge[i] * s + f.h_edge[i] * ds) / den;
   }
   d.tend_u_euler[i] = dteu;
   d.tend_u[i] = d.tend_u[i] + dteu;
@@ -367,6 +395,13 @@ __global__ void k_tan_w_theta(mpasg_mesh m, mpasg_fields f, mpasg_fields d, Fast
       const double dres = m.rdzu[k] * (d.pressure_p[oc + k] - d.pressure_p[oc + k - 1]) -
                           (m.fzm[k] * d.dpdz[oc + k] + m.fzp[k] * d.dpdz[oc + k - 1]);
       dteu -= f.cqw[ow + k] * dres;
+      if (p.dm.v_mom > 0.0) {  // vertical mixing of w: v rho_half (w_up - w_down) rdzu
+        const double rho_half = 0.5 * (f.rho_zz[oc + k] + f.rho_zz[oc + k - 1]);
+        const double drho_half = 0.5 * (d.rho_zz[oc + k] + d.rho_zz[oc + k - 1]);
+        const double wud = (w[k + 1] - w[k]) * m.rdzw[k] - (w[k] - w[k - 1]) * m.rdzw[k - 1];
+        const double dwud = (dw[k + 1] - dw[k]) * m.rdzw[k] - (dw[k] - dw[k - 1]) * m.rdzw[k - 1];
+        dteu += p.dm.v_mom * (drho_half * wud + rho_half * dwud) * m.rdzu[k];
+      }
       d.tend_w_euler[i] = dteu;
     }
     d.tend_w[i] = dtw + dteu;
@@ -394,7 +429,26 @@ __global__ void k_tan_w_theta(mpasg_mesh m, mpasg_fields f, mpasg_fields d, Fast
                        tan_wdtz(m, f.theta_m + oc, f.theta_m_save + oc, f.rw + ow, f.rw_save + ow, d.theta_m + oc,
                                 d.theta_m_save + oc, d.rw + ow, d.rw_save + ow, k, L, p.coef3));
     dtt += d.rho_zz[o] * f.rt_diabatic_tend[o];
-    d.tend_theta[o] = dtt + d.tend_theta_euler[o];
+    double dtte = d.tend_theta_euler[o];
+    if (p.rk_step == 1 && p.dm.v_theta > 0.0 && k >= 1 && k + 1 < L) {
+      // vertical mixing of theta: v rho_zz diff / den, the initial profile a constant
+      const double* zg = m.zgrid + (size_t)c * (L + 1);
+      const double zm = 0.5 * (zg[k - 1] + zg[k]), z0 = 0.5 * (zg[k] + zg[k + 1]), zp = 0.5 * (zg[k + 1] + zg[k + 2]);
+      const double* th = f.theta_m + oc;
+      const double* dth = d.theta_m + oc;
+      double tm = th[k - 1], t0 = th[k], tp = th[k + 1];
+      if (p.mix_pert) {
+        const double* ti = m.t_init + oc;
+        tm = tm - ti[k - 1];
+        t0 = t0 - ti[k];
+        tp = tp - ti[k + 1];
+      }
+      const double diff = (tp - t0) / (zp - z0) - (t0 - tm) / (z0 - zm);
+      const double ddiff = (dth[k + 1] - dth[k]) / (zp - z0) - (dth[k] - dth[k - 1]) / (z0 - zm);
+      dtte += p.dm.v_theta * (d.rho_zz[o] * diff + f.rho_zz[o] * ddiff) / (0.5 * (zp - zm));
+      d.tend_theta_euler[o] = dtte;
+    }
+    d.tend_theta[o] = dtt + dtte;
   }
 }
 
@@ -516,7 +570,9 @@ int mpasgi_dyn_tend_jvp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   p.coef3 = c->coef_3rd_order;
   p.rk_step = rk_step;
   p.del4 = p.h_mom_visc4 > 0.0 ? 1 : 0;
-  const int defer = p.del4;  // vertical mixing is outside the derivatives' scope
+  p.mix_pert = c->mix_perturbation ? 1 : 0;
+  p.dm = adj_damping(c);
+  const int defer = (p.del4 || p.dm.v_mom > 0.0) ? 1 : 0;  // as the forward's TendScalars.defer
   k_tan_cells_a<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, *d, fl, p);
   MPASG_LAUNCH_CHECK();
   k_tan_u<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *d, fl, p, defer);
@@ -527,6 +583,8 @@ int mpasgi_dyn_tend_jvp_core(const mpasg_mesh* m, const mpasg_config* c, const m
       MPASG_LAUNCH_CHECK();
       k_tan_del4_cell<<<nblocks(ncl), kBlock, 0, s>>>(*m, *d, fl);
       MPASG_LAUNCH_CHECK();
+    }
+    if (defer) {
       k_tan_u_finish<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *d, fl, p);
       MPASG_LAUNCH_CHECK();
     }

@@ -16,9 +16,11 @@ primitives with their tangents (``mpasg_prepare_jvp``) and advances values and t
 together through every step (``mpasg_step_jvp``: each stage's forward and its hand-written
 tangent kernels), with nothing stored.
 
-Supported: float64, dry columns, flat terrain, ``2d_smagorinsky`` or ``2d_fixed`` mixing with
-or without del4, no vertical mixing, CAM or Rayleigh damping of u, any RK order and substep
-counts; the objective may read the step boundary's carried fields.  Everything else is
+Supported: float64 (and, in reverse mode, the mixed form), dry columns, flat terrain,
+``2d_smagorinsky`` or ``2d_fixed`` mixing with or without del4, vertical mixing of u, w and
+theta (of the full state or of the perturbation from the initial profiles), CAM-style
+top-level damping and Rayleigh damping of u, any RK order and substep counts; the objective
+may read the step boundary's carried fields.  Everything else is
 rejected before any device work with ``MpasUnsupportedCapabilityError``.
 """
 
@@ -75,13 +77,6 @@ def check_request(cfg: Mapping[str, Any], merged: Mapping[str, Any], num_scalars
         if k in merged and np.any(_np(merged[k]) != 0.0):
             why.append("flat terrain only")
             break
-    for k, label in (("config_v_mom_eddy_visc2", "vertical mixing of u and w"),
-                     ("config_v_theta_eddy_visc2", "vertical mixing of theta"),
-                     ("config_mpas_cam_coef", "CAM damping")):
-        if float(cfg.get(k, 0.0) or 0.0) > 0.0:
-            why.append(f"no {label} ({k})")
-    if str(cfg.get("config_rayleigh_damp_u", False)).strip().lower() in ("true", "1", ".true.", "t"):
-        why.append("no Rayleigh damping of u (config_rayleigh_damp_u)")
     if why:
         raise MpasUnsupportedCapabilityError("dynamics derivatives on the GB300 path: " + "; ".join(why))
 
@@ -96,12 +91,6 @@ def check_supported(model, allow_mixed: bool = False) -> None:
         why.append("dry columns only (moist_end < moist_start)")
     if not dm.struct.flatTerrain:
         why.append("flat terrain only")
-    if cs.v_mom_eddy_visc2 > 0.0 or cs.v_theta_eddy_visc2 > 0.0:
-        why.append("no vertical mixing (config_v_mom_eddy_visc2 / config_v_theta_eddy_visc2)")
-    if cs.mpas_cam_coef > 0.0 and cs.number_cam_damping_levels > 0:
-        why.append("no CAM damping (config_mpas_cam_coef)")
-    if cs.rayleigh_damp_u_levels > 0:
-        why.append("no Rayleigh damping of u (config_rayleigh_damp_u)")
     if model._perm is not None:
         why.append("native mesh order only")
     if why:

@@ -56,6 +56,27 @@ CASES = {
                                   config_horiz_mixing="2d_fixed", config_h_mom_eddy_visc4=1.0e10,
                                   config_h_theta_eddy_visc4=5.0e9, config_h_theta_eddy_visc2=2.0e4),
                       dt=900.0, nsteps=2),
+    # the damping and mixing options: Smagorinsky mixing with CAM-style top-level damping,
+    # Rayleigh damping of u, vertical mixing of the perturbation from nonzero initial profiles
+    # (config_mix_full = false), stretched levels
+    "g2_ad_opts": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=13, n_bumps=6, n_tracers=1, w_sine=0.1,
+                                 round_wind_bits=16, uv_init=(15.0, 2.0)),
+                       config=dict(config_monotonic=False, config_mpas_cam_coef=1.0,
+                                   config_number_cam_damping_levels=4, config_rayleigh_damp_u=True,
+                                   config_rayleigh_damp_u_timescale_days=0.5,
+                                   config_number_rayleigh_damp_u_levels=4, config_mix_full=False,
+                                   config_v_mom_eddy_visc2=2.0, config_v_theta_eddy_visc2=2.0),
+                       dt=900.0, nsteps=2),
+    # fixed-coefficient mixing with CAM damping of the constant coefficient and vertical
+    # mixing of the full state
+    "g2_ad_fixed": dict(spec=dict(level=2, nlev=12, seed=14, n_bumps=6, n_tracers=1, w_sine=0.1,
+                                  round_wind_bits=16),
+                        config=dict(config_monotonic=False, config_horiz_mixing="2d_fixed",
+                                    config_h_mom_eddy_visc4=1.0e10, config_h_theta_eddy_visc4=5.0e9,
+                                    config_h_theta_eddy_visc2=2.0e4, config_mpas_cam_coef=1.0,
+                                    config_number_cam_damping_levels=3, config_v_mom_eddy_visc2=1.0,
+                                    config_v_theta_eddy_visc2=1.0),
+                        dt=900.0, nsteps=2),
 }
 TRACK = ("u", "theta")
 JVP_KEYS = ("rho_zz", "pressure_p", "u", "theta_m", "w")

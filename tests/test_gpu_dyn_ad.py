@@ -15,7 +15,7 @@ import pytest
 import torch
 
 import oracle.dyn_adjoint as D
-from dyn_ad_fixtures import AD_CASES, _npz, config, mesh_and_state
+from dyn_ad_fixtures import AD_CASES, AD_OPTION_CASES, _npz, config, mesh_and_state
 from fixtures import tap_calls
 from gpu_helpers import model_for_case, need_gpu, to_np
 from oracle.step import stage_names
@@ -165,7 +165,7 @@ def _reference_objective(model_mesh, sp_ref, nc):
     return objective
 
 
-@pytest.mark.parametrize("case", AD_CASES)
+@pytest.mark.parametrize("case", AD_CASES + AD_OPTION_CASES)
 def test_run_vjp_matches_reference(case):
     """run_simulation.vjp(track_keys=("u", "theta")) of the surface-pressure functional, against
     the reference's run_simulation.vjp on the same inputs: rel L2 <= 1e-10."""
@@ -202,7 +202,7 @@ def test_run_vjp_matches_reference(case):
         assert torch.equal(nested[k], grads[k]), k
 
 
-@pytest.mark.parametrize("case", AD_CASES)
+@pytest.mark.parametrize("case", AD_CASES + AD_OPTION_CASES)
 def test_mixed_form_gradient_within_1e4_of_reference(case):
     """The mixed form's gradient (float32 stencils in the forward and its taped recompute,
     the reverse pass in float64 about that trajectory) against the reference's float64 VJP:

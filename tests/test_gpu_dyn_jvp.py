@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 import torch
 
-from dyn_ad_fixtures import AD_CASES, _npz, config, mesh_and_state
+from dyn_ad_fixtures import AD_CASES, AD_OPTION_CASES, _npz, config, mesh_and_state
 from gpu_helpers import need_gpu, to_np
 
 pytestmark = pytest.mark.gpu
@@ -32,7 +32,7 @@ def _state(case):
     return mesh, {k: torch.as_tensor(v) for k, v in st0.items()}
 
 
-@pytest.mark.parametrize("case", AD_CASES)
+@pytest.mark.parametrize("case", AD_CASES + AD_OPTION_CASES)
 def test_run_jvp_matches_reference(case):
     need_gpu()
     from mpas_dycore_pytorch_gb300.api import run_simulation
@@ -71,7 +71,7 @@ def _direction(state, seed):
     return d
 
 
-@pytest.mark.parametrize("case", AD_CASES)
+@pytest.mark.parametrize("case", AD_CASES + AD_OPTION_CASES)
 def test_jvp_vjp_identity(case):
     need_gpu()
     from mpas_dycore_pytorch_gb300.api import run_simulation
@@ -110,7 +110,7 @@ def test_jvp_vjp_identity(case):
 
 
 # ---------------------------------------------------------------- stage identities
-STAGE_CASES = ("g2_explicit", "g2_rk2", "g2_split2")
+STAGE_CASES = ("g2_explicit", "g2_rk2", "g2_split2", "g2_fixed", "g2_cam", "g2_rayleigh")
 
 
 def _jvp_call(model, tan, key, inp):

@@ -25,15 +25,18 @@ def test_vjp_track_keys_contract():
             run_simulation.vjp(state, state, lambda o: o["scalars"].sum(), track_keys=keys, config=meta["config"])
 
 
-@pytest.mark.parametrize("extra", [{"config_v_mom_eddy_visc2": 1.0}, {"config_mpas_cam_coef": 1.0},
-                                   {"config_rayleigh_damp_u": True}])
-def test_dynamics_vjp_scope_rejected_before_device_work(extra):
+@pytest.mark.parametrize("extra", [{"config_v_mom_eddy_visc2": 1.0}, {"config_v_theta_eddy_visc2": 1.0},
+                                   {"config_mpas_cam_coef": 1.0}, {"config_rayleigh_damp_u": True},
+                                   {"config_mix_full": False, "config_v_mom_eddy_visc2": 1.0}])
+def test_dynamics_derivative_scope_takes_the_mixing_and_damping_options(extra):
+    """Vertical mixing, CAM and Rayleigh damping are differentiated: the host-side scope
+    check passes them (terrain and moisture are what it still refuses)."""
+    from mpas_dycore_pytorch_gb300.dyn_adjoint import check_request
     state, meta = _case()
     cfg = dict(meta["config"], **extra)
-    with pytest.raises(MpasUnsupportedCapabilityError):
-        run_simulation.vjp(state, state, lambda o: o["rho_zz"].sum(), track_keys=("u", "theta"), config=cfg)
-    with pytest.raises(MpasUnsupportedCapabilityError):
-        run_simulation.jvp(state, state, {"u": torch.zeros_like(state["u"])}, config=cfg)
+    check_request(cfg, state, int(state["scalars"].shape[-1]))
+    with pytest.raises(MpasUnsupportedCapabilityError, match="flat terrain"):
+        check_request(cfg, dict(state, zb_cell=np.ones((3, 2))), int(state["scalars"].shape[-1]))
 
 
 def test_dynamics_jvp_is_float64_only():
