@@ -635,11 +635,20 @@ def dyn_tend_vjp(a, g):
     else:
         h_mom_eddy_visc4 = _f(a, "config_h_mom_eddy_visc4")
         h_theta_eddy_visc4 = _f(a, "config_h_theta_eddy_visc4")
-    for k in ("config_v_mom_eddy_visc2", "config_v_theta_eddy_visc2", "config_mpas_cam_coef"):
-        if k in a and _f(a, k) > 0.0:
-            raise NotImplementedError(f"derivative with {k} > 0")
-    if bool(a.get("config_rayleigh_damp_u", False)):
-        raise NotImplementedError("derivative with Rayleigh damping of u")
+    # dry columns over flat terrain: the moist coefficients and the metric terms are held
+    # constant by this sweep, so other inputs are refused rather than mis-differentiated
+    if "qtot" in a and np.any(np.asarray(a["qtot"]) != 0.0):
+        raise NotImplementedError("derivative in moist columns")
+    if "zxu" in a and np.any(np.asarray(a["zxu"]) != 0.0):
+        raise NotImplementedError("derivative over terrain")
+    # the mixing and damping options (dyn_tend.py:2730-2780, 2956-2990, 3434-3456,
+    # 4636-4648, 5064-5100), differentiated with the forward's branches
+    v_mom = _f(a, "config_v_mom_eddy_visc2") if "config_v_mom_eddy_visc2" in a else 0.0
+    v_th = _f(a, "config_v_theta_eddy_visc2") if "config_v_theta_eddy_visc2" in a else 0.0
+    cam = _f(a, "config_mpas_cam_coef") if "config_mpas_cam_coef" in a else 0.0
+    ncam = _i(a, "config_number_cam_damping_levels") if "config_number_cam_damping_levels" in a else 0
+    mix_full = bool(a.get("config_mix_full", True))
+    ray = bool(a.get("config_rayleigh_damp_u", False))
     fw = S.dyn_tend(a)
     coe = S.idx0(a["cellsOnEdge"][:ne], nc)
     e1, e2 = coe[:, 0], coe[:, 1]
@@ -785,6 +794,19 @@ def dyn_tend_vjp(a, g):
             np.add.at(gth, c2, g_flux * es * rho_edge[e])
             np.add.at(gth, c1, -g_flux * es * rho_edge[e])
             np.add.at(grho_edge, e, g_flux * es * dth)
+        if v_th > 0.0 and nl > 2:  # vertical mixing of theta
+            zg = a["zgrid"][:nc]
+            z1, z2, z3, z4 = zg[:, 0:nl - 2], zg[:, 1:nl - 1], zg[:, 2:nl], zg[:, 3:nl + 1]
+            zm, z0, zp = 0.5 * (z1 + z2), 0.5 * (z2 + z3), 0.5 * (z3 + z4)
+            thv = th[:nc] if mix_full else th[:nc] - a["t_init"][:nc]
+            diff = (thv[:, 2:nl] - thv[:, 1:nl - 1]) / (zp - z0) - (thv[:, 1:nl - 1] - thv[:, :nl - 2]) / (z0 - zm)
+            den = 0.5 * (zp - zm)
+            gt = g_tte[:, 1:nl - 1]
+            grho_zz[:nc, 1:nl - 1] += gt * v_th * diff / den
+            av = gt * v_th * rho_zz[:nc, 1:nl - 1] / den
+            gth[:nc, 2:nl] += av / (zp - z0)
+            gth[:nc, 1:nl - 1] += -av / (zp - z0) - av / (z0 - zm)
+            gth[:nc, :nl - 2] += av / (z0 - zm)
     else:
         out["tend_theta_euler_in"] = np.concatenate([g_tte, np.zeros((1, nl))])
 
@@ -871,6 +893,17 @@ def dyn_tend_vjp(a, g):
             np.add.at(grho_edge, (e, slice(0, nl - 1)), g_rs)
             np.add.at(gw, (c2, slice(1, nl)), g_flux * es * rsum)
             np.add.at(gw, (c1, slice(1, nl)), -g_flux * es * rsum)
+        if v_mom > 0.0:  # vertical mixing of w
+            rz = rho_zz[:nc]
+            w_up = (wc[:, 2:nl + 1] - wc[:, 1:nl]) * rdzw[1:nl]
+            w_down = (wc[:, 1:nl] - wc[:, :nl - 1]) * rdzw[:nl - 1]
+            b = g_twe[:, 1:nl] * v_mom * rdzu[1:nl]
+            grho_zz[:nc, 1:nl] += 0.5 * b * (w_up - w_down)
+            grho_zz[:nc, :nl - 1] += 0.5 * b * (w_up - w_down)
+            av = b * 0.5 * (rz[:, 1:nl] + rz[:, :nl - 1])
+            gw[:nc, 2:nl + 1] += av * rdzw[1:nl]
+            gw[:nc, 1:nl] += -av * rdzw[1:nl] - av * rdzw[:nl - 1]
+            gw[:nc, :nl - 1] += av * rdzw[:nl - 1]
     else:
         gi = np.zeros((nc + 1, nl + 1))
         gi[:nc] = G["tend_w_euler"][:nc]  # passed through at every level
@@ -929,6 +962,13 @@ def dyn_tend_vjp(a, g):
             g_rwe[:, k] += gwd * d[4]
     np.add.at(grw, e1, 0.5 * g_rwe)
     np.add.at(grw, e2, 0.5 * g_rwe)
+    if ray:  # Rayleigh damping of u: tend_u - rho_edge u damp on the top levels
+        nray = _i(a, "config_number_rayleigh_damp_u_levels")
+        coef = 1.0 / (float(nray) * (_f(a, "config_rayleigh_damp_u_timescale_days") * 86400.0))
+        k0 = nl - nray
+        damp = ((np.arange(k0, nl, dtype=np.float64) + 1.0) - float(k0)) * coef
+        grho_edge[:ne, k0:] += -g_tu[:, k0:] * u[:ne, k0:] * damp[None, :]
+        gu[:ne, k0:] += -g_tu[:, k0:] * rho_edge[:ne, k0:] * damp[None, :]
     if rk == 1:
         zzm = 0.5 * (zz[e2] + zz[e1])
         cqu = a["cqu"][:ne]
@@ -986,6 +1026,23 @@ def dyn_tend_vjp(a, g):
                 es = np.where(valid, inv_area[:nc] * dv[e] * sign[:, j], 0.0)[:, None]
                 np.add.at(gdel, e_, gdsd[:nc] * es)
             g_ud = g_ud + gdel[:ne]
+        if v_mom > 0.0 and nl > 2:  # vertical mixing of u
+            zg = a["zgrid"]
+            zi = lambda k0, k1: 0.5 * (zg[e1, k0:k1] + zg[e2, k0:k1])
+            z1, z2, z3, z4 = zi(0, nl - 2), zi(1, nl - 1), zi(2, nl), zi(3, nl + 1)
+            zm, z0, zp = 0.5 * (z1 + z2), 0.5 * (z2 + z3), 0.5 * (z3 + z4)
+            uu = u[:ne]
+            if not mix_full:
+                ang = a["angleEdge"][:ne, None]
+                uu = uu - a["u_init"][None, :nl] * np.cos(ang) - a["v_init"][None, :nl] * np.sin(ang)
+            sdiff = (uu[:, 2:nl] - uu[:, 1:nl - 1]) / (zp - z0) - (uu[:, 1:nl - 1] - uu[:, :nl - 2]) / (z0 - zm)
+            den = 0.5 * (zp - zm)
+            gt = g_teu[:, 1:nl - 1]
+            grho_edge[:ne, 1:nl - 1] += gt * v_mom * sdiff / den
+            av = gt * rho_edge[:ne, 1:nl - 1] * v_mom / den
+            gu[:ne, 2:nl] += av / (zp - z0)
+            gu[:ne, 1:nl - 1] += -av / (zp - z0) - av / (z0 - zm)
+            gu[:ne, :nl - 2] += av / (z0 - zm)
         np.add.at(gdiv, e2, g_ud * r_dc)
         np.add.at(gdiv, e1, -g_ud * r_dc)
         np.add.at(gvort, v2, -g_ud * r_dv)
@@ -1010,6 +1067,13 @@ def dyn_tend_vjp(a, g):
             sq = np.sqrt(s2)
             A_ = (c_s * len_disp) ** 2 * sq
             cap = (0.01 * len_disp ** 2) * inv_dt
+            if cam > 0.0 and ncam > 0:  # max(kdiff, CAM floor) on the top levels: the branch taken
+                kd_s = np.minimum(A_, cap)
+                base = 4.0 * 2.0833 * len_disp * cam
+                gkd_out = gkd_out.copy()
+                for k in range(nl - ncam, nl):
+                    fl = base * (1.0 - float(nl - (k + 1)) / float(ncam))
+                    gkd_out[:, k] *= np.where(kd_s[:, k] > fl, 1.0, np.where(kd_s[:, k] == fl, 0.5, 0.0))
             gA = np.where(A_ < cap, gkd_out, np.where(A_ == cap, 0.5 * gkd_out, 0.0))
             gs = gA * (c_s * len_disp) ** 2 * 0.5 / sq
             gdd = gs * 2.0 * d_diag

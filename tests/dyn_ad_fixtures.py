@@ -9,8 +9,7 @@ import numpy as np
 
 GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
 AD_CASES = ("g2_ad", "g2_ad_rk2")
-# the mixing and damping options (vertical mixing, CAM and Rayleigh damping): the GPU's
-# derivatives against the reference's; the oracle's reverse sweep does not cover them
+# the mixing and damping options (vertical mixing, CAM and Rayleigh damping)
 AD_OPTION_CASES = ("g2_ad_opts", "g2_ad_fixed")
 BASE_CONFIG = {"config_time_integration_order": 3, "config_len_disp": 120000.0,
                "config_number_of_sub_steps": 2, "config_dynamics_split_steps": 3}
