@@ -24,7 +24,10 @@ Conventions follow the MPAS mesh specification:
 * ``defc_a/defc_b`` are the Smagorinsky deformation weights from Gauss' theorem.
 
 Vertical: height coordinate over a flat surface, so ``zz = 1`` and
-``zb = zb3 = zxu = 0``; MPAS vertical metrics (``rdzw, rdzu, fzm, fzp, cf1..cf3``).
+``zb = zb3 = zxu = 0``; MPAS vertical metrics (``rdzw, rdzu, fzm, fzp, cf1..cf3``).  With
+``CaseSpec.terrain`` > 0, terrain-following levels over a cosine hill
+(``zgrid = zw + h (1 - zw / ztop)``) with the metric terms ``zz``, ``zxu``, ``zb``, ``zb3``
+of MPAS init, and every profile evaluated at each layer's own height.
 
 State: dry; ``theta = 300 K exp(N^2 z / g)``; zonal ``u = 20 cos(lat)``; hydrostatic
 Exner with a latitude-dependent surface value for gradient-wind balance of the
@@ -440,6 +443,7 @@ class CaseSpec:
     round_wind_bits: int = 0
     qv_surface: float = 0.0  # > 0: moist case, water vapour as scalar 0 (moist_end = 1)
     uv_init: tuple = (0.0, 0.0)  # initial (u, v) profile values (read by config_mix_full = false)
+    terrain: float = 0.0  # > 0: peak height (m) of a cosine-hill mountain, terrain-following levels
 
 
 def _vertical_metrics(zw: np.ndarray) -> dict:
@@ -471,9 +475,53 @@ def _vertical_metrics(zw: np.ndarray) -> dict:
 
 
 def _exner_profile(zmid: np.ndarray, theta0: float, bvf: float, pi_s: np.ndarray) -> np.ndarray:
-    """Hydrostatic Exner for theta = theta0 exp(N^2 z/g): d(pi)/dz = -g/(cp theta)."""
+    """Hydrostatic Exner for theta = theta0 exp(N^2 z/g): d(pi)/dz = -g/(cp theta); zmid the
+    layer heights, one profile (nlev) or per cell (nc, nlev)."""
     g = GRAVITY
-    return pi_s[:, None] - g * g / (CP * theta0 * bvf * bvf) * (1.0 - dm.exp(-bvf * bvf * zmid[None, :] / g))
+    z = zmid[None, :] if zmid.ndim == 1 else zmid
+    return pi_s[:, None] - g * g / (CP * theta0 * bvf * bvf) * (1.0 - dm.exp(-bvf * bvf * z / g))
+
+
+def _terrain_height(mesh: dict, spec: "CaseSpec", radius: float) -> np.ndarray:
+    """Surface height per cell: a cosine hill of peak ``spec.terrain`` and radius 3000 km
+    centred at (lon, lat) = (90 E, 30 N)."""
+    lat0, lon0 = math.pi / 6, math.pi / 2
+    cl0 = float(dm.cos(lat0))
+    cen = np.array([cl0 * float(dm.cos(lon0)), cl0 * float(dm.sin(lon0)), float(dm.sin(lat0))])
+    pc = np.stack([mesh["xCell"], mesh["yCell"], mesh["zCell"]], 1) / radius
+    r = radius * _arc(pc, cen[None, :]) / 3.0e6
+    return np.where(r < 1.0, spec.terrain * 0.5 * (1.0 + dm.cos(math.pi * r)), 0.0)
+
+
+def _terrain_metrics(mesh: dict, zw: np.ndarray, zgrid: np.ndarray, deriv_two: np.ndarray) -> dict:
+    """Metric terms of terrain-following levels zgrid (C, L+1) over the flat levels zw, as
+    MPAS init writes them: zz = dzw / dz per layer; the edge slope of each w level
+    zx = (z_2 - z_1) / dcEdge and its layer mean zxu; zb, the level's height at the edge
+    relative to each cell, (z_edge - z_cell) dvEdge / areaCell; zb3, its third-order
+    correction -(dcEdge^2 / 12) mean(d2z/dx2 of the two cells) dvEdge / areaCell, the
+    second derivatives from deriv_two (cell itself, then cellsOnCell)."""
+    nc, ne = mesh["nCells"], mesh["nEdges"]
+    c1 = mesh["cellsOnEdge"][:, 0] - 1
+    c2 = mesh["cellsOnEdge"][:, 1] - 1
+    dc, dv, area = mesh["dcEdge"], mesh["dvEdge"], mesh["areaCell"]
+    zz = (zw[1:] - zw[:-1])[None, :] / (zgrid[:, 1:] - zgrid[:, :-1])
+    zx = (zgrid[c2] - zgrid[c1]) / dc[:, None]
+    zxu = 0.5 * (zx[:, 1:] + zx[:, :-1])
+    coc = mesh["cellsOnCell"].astype(np.int64) - 1
+    d2 = []
+    for side, cell in ((0, c1), (1, c2)):
+        nb = coc[cell]  # (ne, maxe), -1 where empty
+        acc = deriv_two[:, side, 0][:, None] * zgrid[cell]
+        for j in range(nb.shape[1]):
+            ok = nb[:, j] >= 0
+            acc = acc + np.where(ok, deriv_two[:, side, j + 1], 0.0)[:, None] * zgrid[np.where(ok, nb[:, j], cell)]
+        d2.append(acc)
+    z_edge = 0.5 * (zgrid[c1] + zgrid[c2])
+    z_edge3 = -(dc * dc / 12.0)[:, None] * (0.5 * (d2[0] + d2[1]))
+    zb = np.stack([(z_edge - zgrid[c1]) * (dv / area[c1])[:, None],
+                   (z_edge - zgrid[c2]) * (dv / area[c2])[:, None]], 1)
+    zb3 = np.stack([z_edge3 * (dv / area[c1])[:, None], z_edge3 * (dv / area[c2])[:, None]], 1)
+    return {"zz": zz, "zxu": zxu, "zb": zb, "zb3": zb3}
 
 
 def _random_direction(rng) -> np.ndarray:
@@ -516,11 +564,19 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
     zmid = 0.5 * (zw[1:] + zw[:-1])
     theta0, bvf, u0 = 300.0, 0.01, 20.0
     latc = mesh["latCell"]
+    # terrain-following levels over a mountain: every profile at the layer's own height
+    hill = _terrain_height(mesh, spec, radius) if spec.terrain > 0.0 else None
+    if hill is not None:
+        zgrid = zw[None, :] + hill[:, None] * (1.0 - zw[None, :] / spec.ztop)
+        zmid = 0.5 * (zgrid[:, 1:] + zgrid[:, :-1])  # (nc, nlev)
 
     # surface Exner balancing the solid-body zonal flow u0 cos(lat) (gradient wind)
     sl = dm.sin(latc)
     pi_s = 1.0 - (u0 * (2.0 * OMEGA * radius + u0) * 0.5 * (sl * sl)) / (CP * theta0)
-    theta_b = theta0 * dm.exp(bvf * bvf * zmid / GRAVITY)[None, :].repeat(nc, 0)
+    if hill is None:
+        theta_b = theta0 * dm.exp(bvf * bvf * zmid / GRAVITY)[None, :].repeat(nc, 0)
+    else:
+        theta_b = theta0 * dm.exp(bvf * bvf * zmid / GRAVITY)
     exner_b = _exner_profile(zmid, theta0, bvf, pi_s)
     p_b = P0 * dm.pow(exner_b, CP / RGAS)
     rho_b = p_b / (RGAS * theta_b * exner_b)
@@ -528,7 +584,8 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
     # theta bumps at constant pressure (rho*theta fixed)
     pc = np.stack([mesh["xCell"], mesh["yCell"], mesh["zCell"]], 1) / radius
     theta = theta_b.copy()
-    env = dm.sin(math.pi * zmid / spec.ztop)[None, :]
+    env = dm.sin(math.pi * zmid / spec.ztop)
+    env = env[None, :] if env.ndim == 1 else env
     for _ in range(spec.n_bumps):
         v = _random_direction(rng)
         amp = rng.uniform(-1.0, 1.0)
@@ -581,17 +638,23 @@ def initial_state(mesh: dict, spec: CaseSpec, radius: float = EARTH_RADIUS) -> d
     qv = np.zeros((nc, nlev))
     if spec.qv_surface > 0.0:  # vapour decaying with a 2.5 km scale height, wetter at the equator
         cl = dm.cos(latc)
-        qv = spec.qv_surface * dm.exp(-zmid / 2500.0)[None, :] * (0.25 + 0.75 * (cl * cl))[:, None]
+        decay = dm.exp(-zmid / 2500.0)
+        qv = spec.qv_surface * (decay[None, :] if decay.ndim == 1 else decay) * (0.25 + 0.75 * (cl * cl))[:, None]
         tracers = [qv] + tracers
     scalars = np.stack(tracers, -1) if tracers else np.zeros((nc, nlev, 0))
 
-    zgrid = np.repeat(zw[None, :], nc, 0)
+    if hill is None:
+        zgrid = np.repeat(zw[None, :], nc, 0)
+        metrics = {"zz": np.ones((nc, nlev)), "zb": np.zeros((ne, 2, nlev + 1)),
+                   "zb3": np.zeros((ne, 2, nlev + 1)), "zxu": np.zeros((ne, nlev))}
+    else:
+        metrics = _terrain_metrics(mesh, zw, zgrid, mesh["deriv_two"])
     init = {
         "u": u, "w": w, "theta": theta, "rho": rho,
         "rho_base": rho_b, "theta_base": theta_b,
-        "zz": np.ones((nc, nlev)), "zgrid": zgrid,
-        "zb": np.zeros((ne, 2, nlev + 1)), "zb3": np.zeros((ne, 2, nlev + 1)),
-        "zxu": np.zeros((ne, nlev)),
+        "zz": metrics["zz"], "zgrid": zgrid,
+        "zb": metrics["zb"], "zb3": metrics["zb3"],
+        "zxu": metrics["zxu"],
         "scalars": scalars, "num_scalars": scalars.shape[-1], "qv": qv,
         "moist_start": 1, "moist_end": 1 if spec.qv_surface > 0.0 else 0,
         "u_init": np.full(nlev, float(spec.uv_init[0])), "v_init": np.full(nlev, float(spec.uv_init[1])),

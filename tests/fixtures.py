@@ -10,7 +10,7 @@ import numpy as np
 
 GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
 CASES = ("g2_explicit", "g2_mono", "g2_moist", "g2_rk2", "g2_fixed", "g2_cam", "g2_split2", "g2_coupled",
-         "g2_rayleigh", "g2_posdef", "g2_noadv")
+         "g2_rayleigh", "g2_posdef", "g2_noadv", "g2_terrain")
 
 # Bound on the relative L2 difference of a field after whole large steps, every field.
 # The reference's Exner function is the C library's pow (its default CPU path); the GPU

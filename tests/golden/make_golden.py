@@ -159,6 +159,10 @@ CASES = {
                                     config_number_rayleigh_damp_u_levels=4, config_mix_full=False,
                                     config_v_mom_eddy_visc2=2.0, config_v_theta_eddy_visc2=2.0),
                         dt=1200.0, nsteps=2),
+    # terrain-following levels over a 1500 m cosine hill (zz != 1, edge slopes zb / zb3 / zxu)
+    "g2_terrain": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=15, n_bumps=6, n_tracers=1,
+                                 terrain=1500.0),
+                       config=dict(config_monotonic=False), dt=1200.0, nsteps=2),
     # positive-definite limiter instead of monotonic (same limited last stage); boundaries only
     "g2_posdef": dict(spec=dict(level=2, nlev=12, seed=8, n_bumps=6, n_tracers=2),
                       config=dict(config_monotonic=False, config_positive_definite=True),
