@@ -67,7 +67,7 @@ enum {
 typedef struct mpasg_mesh {
   int32_t nCells, nEdges, nVertices, nVertLevels;
   int32_t maxEdges, maxEdges2, vertexDegree, nAdvMax;
-  int32_t flatTerrain;   /* 1 when zb_cell == zb3_cell == 0: terrain-slope slot sums are skipped */
+  int32_t flatTerrain;   /* 1 when zb_cell == zb3_cell == zxu == 0: terrain-slope terms are skipped */
   int32_t reserved0;
   double cf1, cf2, cf3;
   /* connectivity (0-based; missing -> padding row) */
@@ -438,7 +438,8 @@ int mpasg_tridiag_factor_jvp(long long n, int L, const double *a, const double *
  * autodiff/soft_limiter.py:1-10.  Cotangents live in a second mpasg_fields `g` with the same
  * layout as the forward fields: g->u is the cotangent of u, and so on.  Every transposed
  * stencil is a deterministic gather (no atomics).  Scope: float64 arithmetic, dry columns
- * (moist_end < moist_start), flat terrain; every mixing and damping option of the
+ * (moist_end < moist_start), flat or terrain-following levels (the slope terms' upwind
+ * selections sgn(flux) frozen as taken); every mixing and damping option of the
  * tendencies (2d_smagorinsky / 2d_fixed del2 and del4, vertical mixing of u, w and theta of
  * the full state or of the perturbation from the initial profiles, CAM-style top-level
  * damping, Rayleigh damping of u), the max of the CAM floor frozen as taken (a tie split
@@ -548,7 +549,7 @@ int mpasg_prepare_vjp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *
 /* ---- dynamics derivatives (forward mode) --------------------------------------------
  * Tangents along the dynamics (the reference's run_simulation.jvp, atmosphere_model.py:2041,
  * through atm_srk3 under torch forward-mode AD), in the scope of the reverse mode above
- * (float64, dry, flat terrain, every mixing and damping option).  d is a
+ * (float64, dry, flat or terrain-following levels, every mixing and damping option).  d is a
  * second mpasg_fields of the same layout holding the tangents under the forward field
  * names; its padding rows hold zeros.  Every entry advances the values f through the stage
  * (as the forward entry point does) and the tangents d alongside; the branches the forward
@@ -568,6 +569,11 @@ int mpasg_vimp_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, 
                    void *stream);
 int mpasg_dyn_tend_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *d,
                        int rk_step, void *stream);
+/* atm_set_smlstep_pert_variables_work (smlstep_pert.py:373) on the tangents: d's tend_w,
+ * tend_u -> tend_rw; f holds the stage's inputs (its tend_u selects the terrain slope
+ * coefficients; f is not written). */
+int mpasg_smlstep_jvp(const mpasg_mesh *m, const mpasg_config *c, const mpasg_fields *f, mpasg_fields *d,
+                      void *stream);
 int mpasg_acoustic_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *d,
                        int small_step, double dts, double *work, void *stream);
 int mpasg_divdamp_jvp(const mpasg_mesh *m, const mpasg_config *c, mpasg_fields *f, mpasg_fields *d, double dts,

@@ -153,7 +153,7 @@ EXPORTS = ("mpasg_abi_version", "mpasg_build_info", "mpasg_launch_count", "mpasg
            "mpasg_smlstep_vjp", "mpasg_acoustic_vjp", "mpasg_divdamp_vjp", "mpasg_recover_vjp", "mpasg_diag_vjp",
            "mpasg_step_vjp", "mpasg_prepare_vjp", "mpasg_step_tape", "mpasg_step_vjp_taped",
            "mpasg_prepare_derived", "mpasg_digest", "mpasg_step_jvp", "mpasg_prepare_jvp", "mpasg_vimp_jvp",
-           "mpasg_dyn_tend_jvp", "mpasg_acoustic_jvp", "mpasg_divdamp_jvp", "mpasg_recover_jvp", "mpasg_diag_jvp",
+           "mpasg_dyn_tend_jvp", "mpasg_smlstep_jvp", "mpasg_acoustic_jvp", "mpasg_divdamp_jvp", "mpasg_recover_jvp", "mpasg_diag_jvp",
            "mpasg_step_vjp_window_tape_doubles", "mpasg_step_vjp_window")
 
 # capacity of the library-owned edge scratch of mpasg_advance_scalars_static (float64 values)
@@ -190,6 +190,7 @@ def load() -> C.CDLL:
         "mpasg_prepare_jvp": ([m, c, f, f, vp, vp, vp], C.c_int),
         "mpasg_vimp_jvp": ([m, c, f, f, C.c_double, vp], C.c_int),
         "mpasg_dyn_tend_jvp": ([m, c, f, f, C.c_int, vp], C.c_int),
+        "mpasg_smlstep_jvp": ([m, c, f, f, vp], C.c_int),
         "mpasg_acoustic_jvp": ([m, c, f, f, C.c_int, C.c_double, vp, vp], C.c_int),
         "mpasg_divdamp_jvp": ([m, c, f, f, C.c_double, vp], C.c_int),
         "mpasg_recover_jvp": ([m, c, f, f, C.c_int, C.c_int, C.c_double, vp], C.c_int),

@@ -822,7 +822,8 @@ def run_simulation_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any], object
 
     * ``track_keys`` within ``("u", "w", "theta", "rho")``: the loaded wind, vertical wind,
       potential temperature and density, through the preparation and the dynamics (the
-      hand-written reverse mode of dyn_adjoint.py: dry, flat terrain, float64 or the mixed
+      hand-written reverse mode of dyn_adjoint.py: dry, flat or terrain-following levels,
+      float64 or the mixed
       form, every mixing and damping option; the objective may read the step boundary's
       carried fields);
     * ``track_keys=("scalars",)``: the transported scalars, by the hand-written transposed
@@ -909,7 +910,7 @@ def run_simulation_jvp(state: Mapping[str, Any], mesh: Mapping[str, Any], pertur
     * a perturbation of any of ``u``, ``w``, ``theta``, ``rho`` (the loaded primitives):
       tangents of the final dynamics fields (the carried fields and ``rho_edge``) through the
       preparation and the dynamics (the hand-written forward mode of dyn_adjoint.py: dry,
-      flat terrain, float64).  The scalars' tangent along the winds is not formed;
+      flat or terrain-following levels, float64).  The scalars' tangent along the winds is not formed;
     * ``perturbation["scalars"]``: the tangent of the end scalars, replayed through each
       step's recorded transport.  Outputs that do not depend on the scalars get no tangent,
       as in the reference."""

@@ -6,7 +6,7 @@
 
 // Work buffer of the dynamics VJPs: kAdjE edge arrays (E+1) x L, kAdjC cell arrays
 // (C+1) x (L+1) and kAdjV vertex arrays (V+1) x L, each 256-byte aligned.
-constexpr int kAdjE = 18, kAdjC = 16, kAdjV = 4;
+constexpr int kAdjE = 19, kAdjC = 16, kAdjV = 4;
 
 struct AdjWork {
   double* e[kAdjE];
@@ -40,7 +40,7 @@ inline bool adj_supported(const mpasg_mesh* m, const mpasg_config* c) {
   if (vmix && !m->zgrid) return false;
   if (vmix && c->mix_perturbation && (!m->u_init || !m->v_init || !m->angleEdge || !m->t_init)) return false;
   if (c->number_cam_damping_levels > m->nVertLevels || c->rayleigh_damp_u_levels > m->nVertLevels) return false;
-  return m->flatTerrain && c->moist_end < c->moist_start && m->nVertLevels >= 4;
+  return c->moist_end < c->moist_start && m->nVertLevels >= 4;
 }
 
 // Damping options the derivatives differentiate, with the forward's expressions
@@ -77,6 +77,13 @@ MPASG_D double adj_ray_damp(const AdjDamping& d, int k, int L) {
 
 // 1 when cell c is the second cell (cellsOnEdge[e][1]) of edge e
 MPASG_D int cell_side(const mpasg_mesh& m, int e, int c) { return m.cellsOnEdge[2 * e] == c ? 0 : 1; }
+// the slot of edge e in edgesOnCell[c] (-1 if absent)
+MPASG_D int cell_slot(const mpasg_mesh& m, int c, int e) {
+  const int me = m.maxEdges, n = m.nEdgesOnCell[c];
+  for (int j = 0; j < n; ++j)
+    if (m.edgesOnCell[c * me + j] == e) return j;
+  return -1;
+}
 // 1 when vertex v is the second vertex (verticesOnEdge[e][1]) of edge e
 MPASG_D int vertex_side(const mpasg_mesh& m, int e, int v) { return m.verticesOnEdge[2 * e] == v ? 0 : 1; }
 
@@ -114,7 +121,11 @@ int mpasgi_acoustic_vjp_rev(const mpasg_mesh* m, const mpasg_config* c, mpasg_fi
                             const double* rwp_in, const AdjWork& w, cudaStream_t s);
 int mpasgi_vimp_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
                          double dts, const AdjWork& w, cudaStream_t s);
-int mpasgi_smlstep_vjp_core(const mpasg_mesh* m, mpasg_fields* g, cudaStream_t s);
+// tend_u's sign for the terrain slope terms: up (1 where tend_u >= 0) if given, else tu
+int mpasgi_smlstep_vjp_core(const mpasg_mesh* m, const double* tu, const uint8_t* up, mpasg_fields* g,
+                            cudaStream_t s);
+// b[i] = x[i] >= 0
+int mpasgi_nonneg_bytes(const double* x, uint8_t* b, long long n, cudaStream_t s);
 int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
                              const mpasg_transpose* t, int rk_step, const AdjWork& w, cudaStream_t s);
 int mpasgi_divdamp_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
@@ -139,6 +150,8 @@ int mpasgi_acoustic_jvp_core(const mpasg_mesh* m, const mpasg_config* c, mpasg_f
                              int small_step, double dts, double* ubuf, cudaStream_t s);
 int mpasgi_divdamp_jvp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* d,
                             double dts, cudaStream_t s);
+// the small-step perturbation on d, its selection from f's tend_u (after the forward one)
+int mpasgi_smlstep_jvp_core(const mpasg_mesh* m, const mpasg_fields* f, mpasg_fields* d, cudaStream_t s);
 int mpasgi_recover_jvp_core(const mpasg_mesh* m, const mpasg_fields* f, mpasg_fields* d, int rk_step, int ns,
                             double rk_dt, cudaStream_t s);
 int mpasgi_prepare_jvp_core(const mpasg_mesh* m, const mpasg_fields* f, mpasg_fields* d, const double* dth,

@@ -89,8 +89,8 @@ StepPlan plan_of(const mpasg_config* c) {
 // reverse pass reads none of their values).
 struct Tape {
   long long E, W, C, V, Lr;
-  long long snap_sz, sv_sz, coef_sz, aco_sz;
-  int lo, hi, n_snap, n_sv, n_coef, n_ac, per_sub_ac, nvimp;
+  long long snap_sz, sv_sz, coef_sz, aco_sz, sg_sz;
+  int lo, hi, n_snap, n_sv, n_coef, n_ac, n_sg, per_sub_ac, nvimp;
   double* base = nullptr;
   Tape(const mpasg_mesh* m, const StepPlan& p, int lo_ = 1, int hi_ = 0) {
     const long long L = m->nVertLevels;
@@ -105,6 +105,9 @@ struct Tape {
     sv_sz = E + W + 4 * C;
     coef_sz = Lr + 8 * C + W;
     aco_sz = E + 2 * W + 3 * C;
+    // over terrain: the sign bytes of every RK stage's tend_u (the small-step slope terms'
+    // selection)
+    sg_sz = m->flatTerrain ? 0 : adj_round(((m->nEdges + 1LL) * L + 7) / 8);
     const int nsub = hi - lo + 1;
     nvimp = p.nvimp_per_sub;
     per_sub_ac = p.nsub[0] + p.nsub[1] + p.nsub[2];
@@ -112,9 +115,17 @@ struct Tape {
     n_sv = nsub;
     n_coef = nsub * nvimp;
     n_ac = nsub * per_sub_ac;
+    n_sg = sg_sz > 0 ? 3 * nsub : 0;
   }
   bool in(int sub) const { return sub >= lo && sub <= hi; }
-  long long doubles() const { return n_snap * snap_sz + n_sv * sv_sz + n_coef * coef_sz + n_ac * aco_sz; }
+  long long doubles() const {
+    return n_snap * snap_sz + n_sv * sv_sz + n_coef * coef_sz + n_ac * aco_sz + n_sg * sg_sz;
+  }
+  // RK stage i's tend_u >= 0 bytes (terrain only)
+  uint8_t* sg(int i) const {
+    return reinterpret_cast<uint8_t*>(base + n_snap * snap_sz + n_sv * sv_sz + n_coef * coef_sz + n_ac * aco_sz +
+                                      (i - 3 * (lo - 1)) * sg_sz);
+  }
   double* snap(int i) const { return base + (i - 3 * (lo - 1)) * snap_sz; }
   double* sv(int i) const { return base + n_snap * snap_sz + (i - (lo - 1)) * sv_sz; }
   double* coef(int i) const { return base + n_snap * snap_sz + n_sv * sv_sz + (i - (lo - 1) * nvimp) * coef_sz; }
@@ -364,6 +375,7 @@ int forward_taped(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, co
         CHECK_RC(mpasg_vert_imp_coefs(m, c, &f, dts, stream));
       }
       CHECK_RC(mpasgi_dyn_tend(m, c, &f, rk, s, true));
+      if (taped && T.n_sg > 0) CHECK_RC(mpasgi_nonneg_bytes(f.tend_u, T.sg(i), (m->nEdges + 1LL) * m->nVertLevels, s));
       CHECK_RC(mpasg_smlstep_pert(m, c, &f, stream));
       for (int small = 1; small <= p.nsub[rk - 1]; ++small) {
         if (taped) aco_redirect(T, f, a);
@@ -448,7 +460,7 @@ int step_reverse(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields*
         CHECK_RC(mpasgi_acoustic_vjp_rev(m, c, &ac, g, t, small, dts, prev + T.E + 2 * T.W + T.C, prev + T.E + T.W,
                                          w, s));
       }
-      CHECK_RC(mpasgi_smlstep_vjp_core(m, g, s));
+      CHECK_RC(mpasgi_smlstep_vjp_core(m, nullptr, T.n_sg > 0 ? T.sg(i) : nullptr, g, s));
       CHECK_RC(mpasgi_dyn_tend_vjp_core(m, c, &pre, g, t, rk, w, s));
       if (rk == 1 || (rk == 2 && p.order == 3)) CHECK_RC(mpasgi_vimp_vjp_core(m, c, &pre, g, dts, w, s));
       // every RK stage starts its acoustic perturbations from zero

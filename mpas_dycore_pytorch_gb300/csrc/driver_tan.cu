@@ -80,7 +80,7 @@ int step_jvp(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields f, mpasg_f
       CHECK_RC(mpasgi_dyn_tend(m, c, &f, rk, s, true));
       CHECK_RC(mpasgi_dyn_tend_jvp_core(m, c, &f, d, rk, s));
       CHECK_RC(mpasg_smlstep_pert(m, c, &f, stream));
-      CHECK_RC(mpasg_smlstep_pert(m, c, d, stream));  // linear over flat terrain: the same map
+      CHECK_RC(mpasgi_smlstep_jvp_core(m, &f, d, s));
       for (int small = 1; small <= nsub[rk - 1]; ++small) {
         CHECK_RC(mpasgi_acoustic_jvp_core(m, c, &f, d, small, dts, ubuf, s));
         CHECK_RC(mpasgi_divdamp_jvp_core(m, c, &f, d, dts, s));
@@ -132,6 +132,12 @@ extern "C" int mpasg_dyn_tend_jvp(const mpasg_mesh* m, const mpasg_config* c, mp
   }
   CHECK_RC(mpasgi_dyn_tend(m, c, f, rk_step, s, false));
   return mpasgi_dyn_tend_jvp_core(m, c, f, d, rk_step, s);
+}
+
+extern "C" int mpasg_smlstep_jvp(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* d,
+                                 void* stream) {
+  if (!m || !c || !f || !d || !jvp_args_ok(m, c)) return MPASG_E_ARG;
+  return mpasgi_smlstep_jvp_core(m, f, d, (cudaStream_t)stream);
 }
 
 extern "C" int mpasg_acoustic_jvp(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, mpasg_fields* d,

@@ -188,7 +188,49 @@ __global__ void k_vimp_coef_vjp(mpasg_mesh m, mpasg_fields f, mpasg_fields g, Fa
 }
 
 // ---------------------------------------------------------------- small-step perturbation
-// flat terrain: tend_rw = zz_i tend_w at interior levels, tend_w itself at the ends
+// Over terrain, interior interface k of cell c: tend_rw = Z (tend_w - sum_j coef_j s_j
+// (fzm tend_u[e_j][k] + fzp tend_u[e_j][k-1])), Z = fzm zz[k] + fzp zz[k-1], coef_j =
+// zb + (tend_u[e_j][k] >= 0 ? 1 : -1) zb3 (smlstep_pert.py:197-373; the selection is
+// constant).  Per edge level k: tend_u's cotangent from the interfaces k (fzm) and k+1
+// (fzp) of both cells, read before k_smlstep_vjp consumes tend_rw's.  The sign of tend_u
+// comes from up (1: >= 0) when given, else from tu.
+__global__ void k_smlstep_vjp_slopes(mpasg_mesh m, mpasg_fields g, FastDiv fl, const double* __restrict__ tu,
+                                     const uint8_t* __restrict__ up) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nEdges * L) return;
+  const uint32_t e = fl.div(i);
+  const int k = (int)(i - e * L);
+  const int me = m.maxEdges;
+  double acc = 0.0;
+  for (int s = 0; s < 2; ++s) {
+    const int c = m.cellsOnEdge[2 * e + s];
+    if (c < 0 || c >= m.nCells) continue;
+    const int j = cell_slot(m, c, (int)e);
+    if (j < 0) continue;
+    const double sign = m.edgesOnCell_sign[c * me + j];
+    const size_t oc = (size_t)c * L, ow = (size_t)c * (L + 1);
+    for (int kw = k; kw <= k + 1; ++kw) {
+      if (kw < 1 || kw > L - 1) continue;
+      const size_t ie = (size_t)e * L + kw;
+      const bool pos = up ? up[ie] != 0 : tu[ie] >= 0.0;
+      const size_t zi = ((size_t)c * me + j) * (L + 1) + kw;
+      const double coef = m.zb_cell[zi] + (pos ? 1.0 : -1.0) * m.zb3_cell[zi];
+      const double Z = m.fzm[kw] * m.zz[oc + kw] + m.fzp[kw] * m.zz[oc + kw - 1];
+      const double wgt = kw == k ? m.fzm[kw] : m.fzp[kw];
+      acc -= coef * sign * wgt * Z * g.tend_rw[ow + kw];
+    }
+  }
+  g.tend_u[i] += acc;
+}
+
+// 1 where tend_u >= 0 (the slope coefficients' selection, kept for the reverse pass)
+__global__ void k_nonneg_bytes(const double* __restrict__ x, uint8_t* __restrict__ b, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = x[i] >= 0.0 ? 1 : 0;
+}
+
+// tend_rw = Z tend_w at interior levels (Z = zz_i), tend_w itself at the ends
 __global__ void k_smlstep_vjp(mpasg_mesh m, mpasg_fields g, FastDiv fl1) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -554,8 +596,41 @@ __global__ void k_divdamp_vjp_cells(mpasg_mesh m, mpasg_fields g, FastDiv fl, co
 }
 
 // ---------------------------------------------------------------- large-step recovery
+// Over terrain, w at interior interface k of cell c is (wo + sum_j s_j c_j fi_j) / R with
+// fi_j = fzm ru[e_j][k] + fzp ru[e_j][k-1], c_j = zb + sgn(fi_j) zb3 (a constant selection),
+// and at the surface w_0 = sum_j s_j cs_j fs_j / (cf1 rho_0 + cf2 rho_1 + cf3 rho_2), fs_j =
+// cf1 ru[e_j][0] + cf2 ru[e_j][1] + cf3 ru[e_j][2] (recover_large_step.py:329-411).  pw
+// holds the cotangent of each interface's numerator (k_recover_vjp_wlev); edge level k
+// reads interfaces k (fzm), k+1 (fzp) and, for k < 3, the surface (cf_(k+1)) of both cells.
+MPASG_D double recover_slope_cotangent(const mpasg_mesh& m, const mpasg_fields& f, const double* __restrict__ pw,
+                                       uint32_t e, int k) {
+  const int L = m.nVertLevels, me = m.maxEdges;
+  const double* ru = f.ru + (size_t)e * L;
+  double acc = 0.0;
+  for (int s = 0; s < 2; ++s) {
+    const int c = m.cellsOnEdge[2 * e + s];
+    if (c < 0 || c >= m.nCells) continue;
+    const int j = cell_slot(m, c, (int)e);
+    if (j < 0) continue;
+    const double sign = m.edgesOnCell_sign[c * me + j];
+    const size_t ow = (size_t)c * (L + 1), zb0 = ((size_t)c * me + j) * (L + 1);
+    for (int kw = k; kw <= k + 1; ++kw) {
+      if (kw < 1 || kw > L - 1) continue;
+      const double fi = m.fzm[kw] * ru[kw] + m.fzp[kw] * ru[kw - 1];
+      const double ci = m.zb_cell[zb0 + kw] + sgn(fi) * m.zb3_cell[zb0 + kw];
+      acc += pw[ow + kw] * sign * ci * (kw == k ? m.fzm[kw] : m.fzp[kw]);
+    }
+    if (k < 3) {
+      const double fs = m.cf1 * ru[0] + m.cf2 * ru[1] + m.cf3 * ru[2];
+      const double cs = m.zb_cell[zb0] + sgn(fs) * m.zb3_cell[zb0];
+      acc += pw[ow] * sign * cs * (k == 0 ? m.cf1 : (k == 1 ? m.cf2 : m.cf3));
+    }
+  }
+  return acc;
+}
+
 __global__ void k_recover_vjp_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl,
-                                    double* __restrict__ pden) {
+                                    double* __restrict__ pden, const double* __restrict__ pw) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)m.nEdges * L) return;
@@ -565,7 +640,8 @@ __global__ void k_recover_vjp_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g
   // one reciprocal of the edge density sum (float64 division is a long instruction sequence)
   const double rden = 1.0 / (f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k]);
   const double gu = g.u[i];
-  const double gru = g.ru[i] + gu * 2.0 * rden;
+  double gru = g.ru[i] + gu * 2.0 * rden;
+  if (pw) gru += recover_slope_cotangent(m, f, pw, e, k);
   g.ru_save[i] += gru;
   g.ru_p[i] += gru;
   pden[i] = -gu * f.u[i] * rden;
@@ -573,14 +649,17 @@ __global__ void k_recover_vjp_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g
   g.ru[i] = 0.0;
 }
 
+// pw (terrain only, else null): the cotangent of each interface's numerator for the
+// slope terms of k_recover_vjp_edges; rho_ib at the surface slot: the cotangent of the
+// surface denominator cf1 rho_0 + cf2 rho_1 + cf3 rho_2
 __global__ void k_recover_vjp_wlev(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl1,
-                                   double* __restrict__ rho_ib) {
+                                   double* __restrict__ rho_ib, double* __restrict__ pw) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)m.nCells * (L + 1)) return;
   const uint32_t c = fl1.div(i);
   const int k = (int)(i - c * (L + 1));
-  double rib = 0.0, rwpb = 0.0;
+  double rib = 0.0, rwpb = 0.0, num = 0.0;
   if (k >= 1 && k <= L - 1) {
     const size_t o = (size_t)c * L + k;
     const double gw = g.w[i];
@@ -590,7 +669,14 @@ __global__ void k_recover_vjp_wlev(mpasg_mesh m, mpasg_fields f, mpasg_fields g,
     rib = -wmb * f.w[i];
     rwpb = (zz_i == 1.0 ? wmb : wmb / zz_i) + g.rw[i];
     g.rw_save[i] += rwpb;
+    num = wmb;
+  } else if (k == 0 && pw) {
+    const size_t o = (size_t)c * L;
+    const double den = m.cf1 * f.rho_zz[o] + m.cf2 * f.rho_zz[o + 1] + m.cf3 * f.rho_zz[o + 2];
+    num = g.w[i] / den;
+    rib = -num * f.w[i];
   }
+  if (pw) pw[i] = num;
   g.rw_p[i] += rwpb;
   rho_ib[i] = rib;
   g.w[i] = 0.0;
@@ -625,6 +711,7 @@ __global__ void k_recover_vjp_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields g
   for (int j = 0; j < n; ++j) rzb += pden[(size_t)m.edgesOnCell[c * me + j] * L + k];
   if (k >= 1) rzb += m.fzm[k] * rho_ib[ow];
   if (k + 1 <= L - 1) rzb += m.fzp[k + 1] * rho_ib[ow + 1];
+  if (!m.flatTerrain && k < 3) rzb += (k == 0 ? m.cf1 : (k == 1 ? m.cf2 : m.cf3)) * rho_ib[(size_t)c * (L + 1)];
   if (rk_step == 3) rzb += -rtpb * rk_dt * f.rt_diabatic_tend[o];
   g.rtheta_p_save[o] += rtpb;
   g.rtheta_pp[o] += rtpb;
@@ -660,6 +747,13 @@ int dcopy(double* d, const double* src, long long n, cudaStream_t s) {
 }  // namespace
 
 int mpasgi_zero(double* p, long long n, cudaStream_t s) { return zero(p, n, s); }
+
+int mpasgi_nonneg_bytes(const double* x, uint8_t* b, long long n, cudaStream_t s) {
+  if (n <= 0) return MPASG_OK;
+  k_nonneg_bytes<<<nblocks(n), kBlock, 0, s>>>(x, b, n);
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
 
 namespace {
 struct ZeroList {
@@ -778,9 +872,10 @@ int mpasgi_recover_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mp
   (void)c;
   const int L = m->nVertLevels;
   FastDiv fl(L), fl1(L + 1);
-  k_recover_vjp_edges<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, *g, fl, w.e[5]);
+  double* pw = m->flatTerrain ? nullptr : w.c[8];  // slope terms: numerator cotangents
+  k_recover_vjp_wlev<<<nblocks((long long)m->nCells * (L + 1)), kBlock, 0, s>>>(*m, *f, *g, fl1, w.c[7], pw);
   MPASG_LAUNCH_CHECK();
-  k_recover_vjp_wlev<<<nblocks((long long)m->nCells * (L + 1)), kBlock, 0, s>>>(*m, *f, *g, fl1, w.c[7]);
+  k_recover_vjp_edges<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *f, *g, fl, w.e[5], pw);
   MPASG_LAUNCH_CHECK();
   k_recover_vjp_cells<<<nblocks((long long)m->nCells * L), kBlock, 0, s>>>(*m, *f, *g, fl, rk_step, rk_dt, w.e[5],
                                                                           w.c[7]);
@@ -819,8 +914,14 @@ int mpasgi_vimp_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const mpasg
   return MPASG_OK;
 }
 
-int mpasgi_smlstep_vjp_core(const mpasg_mesh* m, mpasg_fields* g, cudaStream_t s) {
+int mpasgi_smlstep_vjp_core(const mpasg_mesh* m, const double* tu, const uint8_t* up, mpasg_fields* g,
+                            cudaStream_t s) {
   const int L = m->nVertLevels;
+  if (!m->flatTerrain) {
+    if (!tu && !up) return MPASG_E_ARG;
+    k_smlstep_vjp_slopes<<<nblocks((long long)m->nEdges * L), kBlock, 0, s>>>(*m, *g, FastDiv(L), tu, up);
+    MPASG_LAUNCH_CHECK();
+  }
   k_smlstep_vjp<<<nblocks((long long)m->nCells * (L + 1)), kBlock, 0, s>>>(*m, *g, FastDiv(L + 1));
   MPASG_LAUNCH_CHECK();
   return MPASG_OK;
@@ -841,7 +942,7 @@ extern "C" int mpasg_vimp_vjp(const mpasg_mesh* m, const mpasg_config* c, const 
 extern "C" int mpasg_smlstep_vjp(const mpasg_mesh* m, const mpasg_config* c, const mpasg_fields* f, mpasg_fields* g,
                                  void* stream) {
   if (!m || !c || !f || !g || !adj_supported(m, c)) return MPASG_E_ARG;
-  return mpasgi_smlstep_vjp_core(m, g, (cudaStream_t)stream);
+  return mpasgi_smlstep_vjp_core(m, f->tend_u, nullptr, g, (cudaStream_t)stream);
 }
 
 extern "C" int mpasg_acoustic_vjp(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f, mpasg_fields* g,

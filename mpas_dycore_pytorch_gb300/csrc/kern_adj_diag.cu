@@ -174,6 +174,35 @@ __global__ void k_dadj_hedge(mpasg_mesh m, mpasg_fields g, FastDiv fl) {
 }
 
 // ---------------------------------------------------------------- preparation
+// Over terrain, rw at interior interface k of cell c also has the slope terms
+// - sum_j s_j coef_j flux_j zz_i, flux_j = fzm ru[e_j][k] + fzp ru[e_j][k-1], coef_j = zb +
+// sgn(flux_j) zb3 (a constant selection; init_coupled_diagnostics.py:147): ru's cotangent
+// from the interfaces k (fzm) and k+1 (fzp) of both cells
+MPASG_D double prepare_slope_cotangent(const mpasg_mesh& m, const mpasg_fields& f, const mpasg_fields& g, uint32_t e,
+                                       int k) {
+  const int L = m.nVertLevels, me = m.maxEdges;
+  const double* ru = f.ru + (size_t)e * L;
+  double acc = 0.0;
+  for (int s = 0; s < 2; ++s) {
+    const int c = m.cellsOnEdge[2 * e + s];
+    if (c < 0 || c >= m.nCells) continue;
+    const int j = cell_slot(m, c, (int)e);
+    if (j < 0) continue;
+    const double sign = m.edgesOnCell_sign[c * me + j];
+    const size_t oc = (size_t)c * L, ow = (size_t)c * (L + 1);
+    for (int kw = k; kw <= k + 1; ++kw) {
+      if (kw < 1 || kw > L - 1) continue;
+      const double fzm = m.fzm[kw], fzp = m.fzp[kw];
+      const double flux = fzm * ru[kw] + fzp * ru[kw - 1];
+      const size_t zi = ((size_t)c * me + j) * (L + 1) + kw;
+      const double coef = m.zb_cell[zi] + sgn(flux) * m.zb3_cell[zi];
+      const double zz_i = fzp * m.zz[oc + kw - 1] + fzm * m.zz[oc + kw];
+      acc -= g.rw[ow + kw] * sign * coef * zz_i * (kw == k ? fzm : fzp);
+    }
+  }
+  return acc;
+}
+
 // edges: ru = 0.5 u (rho_1 + rho_2) -> u; the rho partial for the cell gather
 __global__ void k_padj_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl, double* __restrict__ g_u,
                              double* __restrict__ pru) {
@@ -187,12 +216,13 @@ __global__ void k_padj_edges(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastD
   const uint32_t e = fl.div(i);
   const int k = (int)(i - e * L);
   const int c1 = m.cellsOnEdge[2 * e], c2 = m.cellsOnEdge[2 * e + 1];
-  const double gru = g.ru[i];
+  double gru = g.ru[i];
+  if (!m.flatTerrain) gru += prepare_slope_cotangent(m, f, g, e, k);
   g_u[i] = g.u[i] + gru * 0.5 * (f.rho_zz[(size_t)c1 * L + k] + f.rho_zz[(size_t)c2 * L + k]);
   pru[i] = gru * 0.5 * f.u[i];
 }
 
-// w levels: rw = w rho_i zz_i (flat terrain) -> w; rho_i's cotangent
+// w levels: rw = w rho_i zz_i (+ the slope terms, k_padj_edges) -> w; rho_i's cotangent
 __global__ void k_padj_wlev(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl1, const double* __restrict__ w_in,
                             double* __restrict__ g_w, double* __restrict__ rho_ib) {
   const int L = m.nVertLevels;

@@ -462,7 +462,8 @@ __global__ void __launch_bounds__(kBlock) k_tadj_u(mpasg_mesh m, mpasg_fields f,
                                                    double* __restrict__ pke, double* __restrict__ phd,
                                                    double* __restrict__ prwe, double* __restrict__ ppp,
                                                    double* __restrict__ pkd, double* __restrict__ udb,
-                                                   double* __restrict__ pd4, const double* __restrict__ qa) {
+                                                   double* __restrict__ pd4, const double* __restrict__ qa,
+                                                   double* __restrict__ pdz) {
   __shared__ double s_c[4][kBlock];
   const int L = m.nVertLevels;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -536,6 +537,8 @@ __global__ void __launch_bounds__(kBlock) k_tadj_u(mpasg_mesh m, mpasg_fields f,
     const double zzm = 0.5 * (m.zz[i2] + m.zz[i1]);
     const double pg = -teub * f.cqu_e[i] * inv_dc;
     ppp[i] = zzm == 1.0 ? pg : pg / zzm;
+    // terrain: + cqu 0.5 zxu (dpdz_1 + dpdz_2), the same partial for both cells
+    if (pdz) pdz[i] = teub * f.cqu_e[i] * 0.5 * m.zxu[i];
     const int v1 = m.verticesOnEdge[2 * e], v2 = m.verticesOnEdge[2 * e + 1];
     const double r_dv = fmin(m.invDvEdge[e], 4.0 * inv_dc);
     const double u_diff = (f.divergence[i2] - f.divergence[i1]) * inv_dc -
@@ -563,13 +566,15 @@ __global__ void __launch_bounds__(kBlock) k_tadj_u(mpasg_mesh m, mpasg_fields f,
 }
 
 // ---- cells: the u tendency's per-edge partials gathered (index space C x (L+1)):
-// ke, the mass-flux divergence, pressure_p, kdiff, the del4 divergence (mass levels);
-// rw through the edge-interface mean (w levels)
-__global__ void k_tadj_u_cells(mpasg_mesh m, mpasg_fields g, FastDiv fl1, AdjTendScalars p,
+// ke, the mass-flux divergence, pressure_p, kdiff, the del4 divergence, over terrain dpdz
+// (-> rr_save, dpdz = -g (rho_base qtot + rr_save (1 + qtot))) (mass levels); rw through the
+// edge-interface mean (w levels)
+__global__ void k_tadj_u_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields g, FastDiv fl1, AdjTendScalars p,
                                const double* __restrict__ pke, const double* __restrict__ phd,
                                const double* __restrict__ prwe, const double* __restrict__ ppp,
                                const double* __restrict__ pkd, const double* __restrict__ pd4,
-                               double* __restrict__ hdb, double* __restrict__ kdb, double* __restrict__ dsdb) {
+                               const double* __restrict__ pdz, double* __restrict__ hdb, double* __restrict__ kdb,
+                               double* __restrict__ dsdb) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint32_t)m.nCells * (L + 1)) return;
@@ -577,7 +582,7 @@ __global__ void k_tadj_u_cells(mpasg_mesh m, mpasg_fields g, FastDiv fl1, AdjTen
   const int k = (int)(i - c * (L + 1));
   const int me = m.maxEdges;
   const int n = m.nEdgesOnCell[c];
-  double gke = 0.0, ghd = 0.0, gpp = 0.0, gkd = 0.0, gds = 0.0, grw = 0.0;
+  double gke = 0.0, ghd = 0.0, gpp = 0.0, gkd = 0.0, gds = 0.0, grw = 0.0, gdz = 0.0;
   for (int j = 0; j < n; ++j) {
     const int e = m.edgesOnCell[c * me + j];
     const int side = cell_side(m, e, (int)c);
@@ -588,6 +593,7 @@ __global__ void k_tadj_u_cells(mpasg_mesh m, mpasg_fields g, FastDiv fl1, AdjTen
       if (p.rk_step == 1) {
         gpp += side ? ppp[ie] : -ppp[ie];
         gkd += pkd[ie];
+        if (pdz) gdz += pdz[ie];
         if (p.del4) {
           const double inv_dc = m.invDcEdge[e];
           const double r_dc4 = m.meshScalingDel4[e] * p.h_mom_visc4 * p.del4u_div * inv_dc;
@@ -606,6 +612,7 @@ __global__ void k_tadj_u_cells(mpasg_mesh m, mpasg_fields g, FastDiv fl1, AdjTen
     g.pressure_p[o] += gpp;
     kdb[o] = gkd;
     dsdb[o] = gds;
+    if (pdz) g.rr_save[o] += gdz * (-kGravity) * (1.0 + f.qtot[o]);
   }
 }
 
@@ -1103,6 +1110,7 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   double* bw = w.e[15];
   double* kdw = w.e[16];
   double* gre = w.e[17];
+  double* pdz = m->flatTerrain ? nullptr : w.e[18];  // terrain: dpdz partials of the u tendency
   // vertices
   double* dsv = w.v[0];
   double* dsvb = w.v[1];
@@ -1136,9 +1144,10 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   k_tadj_qa<<<nblocks(nel), kBlock, 0, s>>>((int)nel, g->tend_u, f->h_edge, qa);
   MPASG_LAUNCH_CHECK();
   k_tadj_u<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, p, hd, kd, ud, dsd, dsv, pke, phd, prwe, ppp, pkd,
-                                          udb, pd4, qa);
+                                          udb, pd4, qa, pdz);
   MPASG_LAUNCH_CHECK();
-  k_tadj_u_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *g, fl1, p, pke, phd, prwe, ppp, pkd, pd4, hdb, kdb, dsdb);
+  k_tadj_u_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, *g, fl1, p, pke, phd, prwe, ppp, pkd, pd4, pdz, hdb, kdb,
+                                                 dsdb);
   MPASG_LAUNCH_CHECK();
   if (rk_step == 1 && p.dm.v_mom > 0.0) {
     k_tadj_vmix_u<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, fl, p);

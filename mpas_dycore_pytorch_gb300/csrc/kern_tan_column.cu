@@ -296,8 +296,70 @@ __global__ void k_tan_divdamp(mpasg_mesh m, mpasg_fields f, mpasg_fields d, Fast
   d.ru_p[i] = d.ru_p[i] + coef * ((t2 - t1) * f.theta_edge_rsum[i] + (d2 - d1) * d.theta_edge_rsum[i]);
 }
 
+// ---------------------------------------------------------------- small-step perturbation
+// (smlstep_pert.py:197-373) on the tangents: the same linear map, with the slope
+// coefficients' selection (tend_u >= 0) taken from the forward's tend_u
+__global__ void k_tan_smlstep(mpasg_mesh m, mpasg_fields f, mpasg_fields d, FastDiv fl1) {
+  const int L = m.nVertLevels;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)m.nCells * (L + 1)) return;
+  const uint32_t c = fl1.div(i);
+  const int k = (int)(i - c * (L + 1));
+  if (k == 0 || k == L) {
+    d.tend_rw[i] = d.tend_w[i];
+    return;
+  }
+  const int me = m.maxEdges;
+  const double fzm = m.fzm[k], fzp = m.fzp[k];
+  double acc = d.tend_w[i];
+  const int n = m.flatTerrain ? 0 : m.nEdgesOnCell[c];
+  for (int j = 0; j < n; ++j) {
+    const int e = m.edgesOnCell[c * me + j];
+    const size_t o = (size_t)e * L;
+    const double du = fzm * d.tend_u[o + k] + fzp * d.tend_u[o + k - 1];
+    const size_t zi = ((size_t)c * me + j) * (L + 1) + k;
+    const double coef = m.zb_cell[zi] + (f.tend_u[o + k] >= 0.0 ? 1.0 : -1.0) * m.zb3_cell[zi];
+    acc = acc - coef * (m.edgesOnCell_sign[c * me + j] * du);
+  }
+  const size_t o = (size_t)c * L;
+  d.tend_rw[i] = (fzm * m.zz[o + k] + fzp * m.zz[o + k - 1]) * acc;
+}
+
 // ---------------------------------------------------------------- large-step recovery
-// (recover_large_step.py:329-513, flat terrain), before the forward recovery
+// (recover_large_step.py:329-513), before the forward recovery.  Over terrain, w adds the
+// slope fluxes of the new ru = ru_save + ru_p with their selection sgn(flux) held fixed:
+// sum_j s_j (zb + sgn(fi) zb3) fi_j at interior interfaces (fi_j = fzm ru[k] + fzp ru[k-1]),
+// and at the surface w_0 = sum_j s_j (zb + sgn(fs) zb3) fs_j / (cf1 rho_0 + cf2 rho_1 +
+// cf3 rho_2), fs_j = cf1 ru[0] + cf2 ru[1] + cf3 ru[2]; w_0 = 0 over flat terrain.
+struct SlopeSum {
+  double v, d;  // value and tangent
+};
+// kw >= 1: interface kw's flux fzm ru[kw] + fzp ru[kw-1]; kw == 0: the surface flux
+MPASG_D SlopeSum recover_slope_sum(const mpasg_mesh& m, const mpasg_fields& f, const mpasg_fields& d, uint32_t c,
+                                   int kw) {
+  const int L = m.nVertLevels, me = m.maxEdges, n = m.nEdgesOnCell[c];
+  SlopeSum r{0.0, 0.0};
+  for (int j = 0; j < n; ++j) {
+    const int e = m.edgesOnCell[c * me + j];
+    const size_t o = (size_t)e * L;
+    auto ru = [&](int q) { return f.ru_save[o + q] + f.ru_p[o + q]; };
+    auto dru = [&](int q) { return d.ru_save[o + q] + d.ru_p[o + q]; };
+    double fl, dfl;
+    if (kw == 0) {
+      fl = m.cf1 * ru(0) + m.cf2 * ru(1) + m.cf3 * ru(2);
+      dfl = m.cf1 * dru(0) + m.cf2 * dru(1) + m.cf3 * dru(2);
+    } else {
+      fl = m.fzm[kw] * ru(kw) + m.fzp[kw] * ru(kw - 1);
+      dfl = m.fzm[kw] * dru(kw) + m.fzp[kw] * dru(kw - 1);
+    }
+    const size_t zi = ((size_t)c * me + j) * (L + 1) + kw;
+    const double cs = m.edgesOnCell_sign[c * me + j] * (m.zb_cell[zi] + sgn(fl) * m.zb3_cell[zi]);
+    r.v += cs * fl;
+    r.d += cs * dfl;
+  }
+  return r;
+}
+
 __global__ void k_tan_recover_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields d, FastDiv fl1, int rk_step,
                                     double inv_ns, double rk_dt) {
   const int L = m.nVertLevels;
@@ -348,7 +410,20 @@ __global__ void k_tan_recover_cells(mpasg_mesh m, mpasg_fields f, mpasg_fields d
     const double drho_km1 = d.rho_p_save[oc + k - 1] + d.rho_pp[oc + k - 1];
     const double R = m.fzm[k] * rho_k + m.fzp[k] * rho_km1;
     const double dR = m.fzm[k] * drho_k + m.fzp[k] * drho_km1;
-    d.w[ow] = dwo / R - wo * dR / (R * R);
+    double num = wo, dnum = dwo;
+    if (!m.flatTerrain) {
+      const SlopeSum sl = recover_slope_sum(m, f, d, c, k);
+      num = num + sl.v;
+      dnum = dnum + sl.d;
+    }
+    d.w[ow] = dnum / R - num * dR / (R * R);
+  } else if (k == 0 && !m.flatTerrain) {
+    const SlopeSum sl = recover_slope_sum(m, f, d, c, 0);
+    auto rho = [&](int q) { return f.rho_p_save[oc + q] + f.rho_pp[oc + q] + m.rho_base[oc + q]; };
+    auto drho = [&](int q) { return d.rho_p_save[oc + q] + d.rho_pp[oc + q]; };
+    const double D = m.cf1 * rho(0) + m.cf2 * rho(1) + m.cf3 * rho(2);
+    const double dD = m.cf1 * drho(0) + m.cf2 * drho(1) + m.cf3 * drho(2);
+    d.w[ow] = sl.d / D - sl.v * dD / (D * D);
   } else {
     d.w[ow] = 0.0;
   }
@@ -403,7 +478,9 @@ __global__ void k_tan_prepare_ru(mpasg_mesh m, mpasg_fields f, mpasg_fields d, F
   d.ru[i] = 0.5 * (d.u[i] * (f.rho_zz[i1] + f.rho_zz[i2]) + f.u[i] * (d.rho_zz[i1] + d.rho_zz[i2]));
 }
 
-// flat terrain: rw = w rho_i zz_i at interior interfaces
+// rw = (w rho_i - sum_j s_j coef_j flux_j) zz_i at interior interfaces, flux_j = fzm
+// ru[k] + fzp ru[k-1], coef_j = zb + sgn(flux_j) zb3 held fixed (no slope terms over flat
+// terrain); after k_tan_prepare_ru
 __global__ void k_tan_prepare_rw(mpasg_mesh m, mpasg_fields f, mpasg_fields d, FastDiv fl1) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -419,7 +496,19 @@ __global__ void k_tan_prepare_rw(mpasg_mesh m, mpasg_fields f, mpasg_fields d, F
   const double rho_i = fzp * f.rho_zz[oc + k - 1] + fzm * f.rho_zz[oc + k];
   const double drho_i = fzp * d.rho_zz[oc + k - 1] + fzm * d.rho_zz[oc + k];
   const double zz_i = fzp * m.zz[oc + k - 1] + fzm * m.zz[oc + k];
-  d.rw[i] = (d.w[i] * rho_i + f.w[i] * drho_i) * zz_i;
+  double drw = (d.w[i] * rho_i + f.w[i] * drho_i) * zz_i;
+  const int me = m.maxEdges;
+  const int n = m.flatTerrain ? 0 : m.nEdgesOnCell[c];
+  for (int j = 0; j < n; ++j) {
+    const int e = m.edgesOnCell[c * me + j];
+    const size_t o = (size_t)e * L;
+    const double flux = fzm * f.ru[o + k] + fzp * f.ru[o + k - 1];
+    const double dflux = fzm * d.ru[o + k] + fzp * d.ru[o + k - 1];
+    const size_t zi = ((size_t)c * me + j) * (L + 1) + k;
+    const double coef = m.zb_cell[zi] + sgn(flux) * m.zb3_cell[zi];
+    drw -= m.edgesOnCell_sign[c * me + j] * coef * dflux * zz_i;
+  }
+  d.rw[i] = drw;
 }
 
 }  // namespace
@@ -478,6 +567,13 @@ int mpasgi_divdamp_jvp_core(const mpasg_mesh* m, const mpasg_config* c, const mp
 }
 
 // before the forward recovery
+int mpasgi_smlstep_jvp_core(const mpasg_mesh* m, const mpasg_fields* f, mpasg_fields* d, cudaStream_t s) {
+  const int L = m->nVertLevels;
+  k_tan_smlstep<<<nblocks((long long)m->nCells * (L + 1)), kBlock, 0, s>>>(*m, *f, *d, FastDiv(L + 1));
+  MPASG_LAUNCH_CHECK();
+  return MPASG_OK;
+}
+
 int mpasgi_recover_jvp_core(const mpasg_mesh* m, const mpasg_fields* f, mpasg_fields* d, int rk_step, int ns,
                             double rk_dt, cudaStream_t s) {
   const int L = m->nVertLevels;

@@ -105,7 +105,8 @@ class DeviceMesh:
             t = torch.from_numpy(np.ascontiguousarray(dbls[n[:-4]], dtype=np.float32)).to(self.device)
             self._keep[n] = t
             setattr(st, n, t.data_ptr())
-        st.flatTerrain = int(not np.any(dbls["zb_cell"]) and not np.any(dbls["zb3_cell"]))
+        st.flatTerrain = int(not np.any(dbls["zb_cell"]) and not np.any(dbls["zb3_cell"])
+                             and not np.any(dbls["zxu"]))
         self.flat_terrain = bool(st.flatTerrain)
         for n in _lib.MESH_DOUBLES:
             setattr(st, n, float(_np(ref[n]).reshape(-1)[0]))

@@ -16,8 +16,9 @@ primitives with their tangents (``mpasg_prepare_jvp``) and advances values and t
 together through every step (``mpasg_step_jvp``: each stage's forward and its hand-written
 tangent kernels), with nothing stored.
 
-Supported: float64 (and, in reverse mode, the mixed form), dry columns, flat terrain,
-``2d_smagorinsky`` or ``2d_fixed`` mixing with or without del4, vertical mixing of u, w and
+Supported: float64 (and, in reverse mode, the mixed form), dry columns, flat or
+terrain-following levels (the slope terms' upwind selections held fixed, as torch
+differentiates sign), ``2d_smagorinsky`` or ``2d_fixed`` mixing with or without del4, vertical mixing of u, w and
 theta (of the full state or of the perturbation from the initial profiles), CAM-style
 top-level damping and Rayleigh damping of u, any RK order and substep counts; the objective
 may read the step boundary's carried fields.  Everything else is
@@ -73,10 +74,6 @@ def check_request(cfg: Mapping[str, Any], merged: Mapping[str, Any], num_scalars
     ms, me = _int(merged.get("moist_start", 1)), _int(merged.get("moist_end", num_scalars))
     if not me < ms:
         why.append("dry columns only (moist_end < moist_start)")
-    for k in ("zb_cell", "zb3_cell"):
-        if k in merged and np.any(_np(merged[k]) != 0.0):
-            why.append("flat terrain only")
-            break
     if why:
         raise MpasUnsupportedCapabilityError("dynamics derivatives on the GB300 path: " + "; ".join(why))
 
@@ -89,8 +86,6 @@ def check_supported(model, allow_mixed: bool = False) -> None:
         why.append("float64 arithmetic only (config_precision)")
     if not (cs.moist_end < cs.moist_start):
         why.append("dry columns only (moist_end < moist_start)")
-    if not dm.struct.flatTerrain:
-        why.append("flat terrain only")
     if model._perm is not None:
         why.append("native mesh order only")
     if why:

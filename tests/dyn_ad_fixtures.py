@@ -11,6 +11,8 @@ GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
 AD_CASES = ("g2_ad", "g2_ad_rk2")
 # the mixing and damping options (vertical mixing, CAM and Rayleigh damping)
 AD_OPTION_CASES = ("g2_ad_opts", "g2_ad_fixed")
+# terrain-following levels over a cosine hill (the oracle's reverse sweep does not cover them)
+AD_TERRAIN_CASES = ("g2_ad_terrain", "g2_ad_terrain_fixed")
 BASE_CONFIG = {"config_time_integration_order": 3, "config_len_disp": 120000.0,
                "config_number_of_sub_steps": 2, "config_dynamics_split_steps": 3}
 # the case options of make_golden_dyn_ad.CASES (kept here so the tests need no reference tree)
@@ -28,6 +30,10 @@ CASE_CONFIG = {
                         config_h_theta_eddy_visc4=5.0e9, config_h_theta_eddy_visc2=2.0e4,
                         config_mpas_cam_coef=1.0, config_number_cam_damping_levels=3,
                         config_v_mom_eddy_visc2=1.0, config_v_theta_eddy_visc2=1.0),
+    "g2_ad_terrain": dict(config_monotonic=False),
+    "g2_ad_terrain_fixed": dict(config_monotonic=False, config_horiz_mixing="2d_fixed",
+                                config_h_mom_eddy_visc4=1.0e10, config_h_theta_eddy_visc4=5.0e9,
+                                config_h_theta_eddy_visc2=2.0e4),
 }
 DIMS = ("nCells", "nEdges", "nVertices", "nVertLevels", "maxEdges", "maxEdges2", "vertexDegree")
 LOADED_SCALARS = {"c_s": 0.125, "coef_3rd_order": 0.25, "moist_start": 1, "moist_end": 0}

@@ -77,6 +77,18 @@ CASES = {
                                     config_number_cam_damping_levels=3, config_v_mom_eddy_visc2=1.0,
                                     config_v_theta_eddy_visc2=1.0),
                         dt=900.0, nsteps=2),
+    # terrain-following levels over a 1500 m cosine hill (zz != 1, slope terms zb / zb3 / zxu)
+    "g2_ad_terrain": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=16, n_bumps=6, n_tracers=1,
+                                    w_sine=0.1, round_wind_bits=16, terrain=1500.0),
+                          config=dict(config_monotonic=False), dt=900.0, nsteps=2),
+    # the same over fixed-coefficient del2 / del4 mixing (no Smagorinsky coefficient, whose
+    # square root of a near-zero deformation makes the u gradient follow the roundings)
+    "g2_ad_terrain_fixed": dict(spec=dict(level=2, nlev=12, dz_bottom=400.0, seed=17, n_bumps=6, n_tracers=1,
+                                          w_sine=0.1, round_wind_bits=16, terrain=1500.0),
+                                config=dict(config_monotonic=False, config_horiz_mixing="2d_fixed",
+                                            config_h_mom_eddy_visc4=1.0e10, config_h_theta_eddy_visc4=5.0e9,
+                                            config_h_theta_eddy_visc2=2.0e4),
+                                dt=900.0, nsteps=2),
 }
 TRACK = ("u", "theta")
 JVP_KEYS = ("rho_zz", "pressure_p", "u", "theta_m", "w")

@@ -9,15 +9,17 @@ to the loaded u, w, theta, rho; mpasg_step_jvp):
   a deformation made of roundoff, so its derivative's direction follows the roundings);
 * the JVP/VJP dot-product identity <g, J d> = <J^T g, d> through the preparation and the
   whole run, per output field (one seeded cotangent on that field, one seeded direction on
-  u, w, theta, rho), within 1e-12; a zero reverse mode and a crossed pairing of fields are
-  the failing controls.
+  u, w, theta, rho), within 1e-12 (2e-12 over terrain, see _identity_bar); a zero reverse
+  mode and a crossed pairing of fields are the failing controls.
 """
+
+import math
 
 import numpy as np
 import pytest
 import torch
 
-from dyn_ad_fixtures import AD_CASES, AD_OPTION_CASES, _npz, config, mesh_and_state
+from dyn_ad_fixtures import AD_CASES, AD_OPTION_CASES, AD_TERRAIN_CASES, _npz, config, mesh_and_state
 from gpu_helpers import need_gpu, to_np
 
 pytestmark = pytest.mark.gpu
@@ -32,7 +34,7 @@ def _state(case):
     return mesh, {k: torch.as_tensor(v) for k, v in st0.items()}
 
 
-@pytest.mark.parametrize("case", AD_CASES + AD_OPTION_CASES)
+@pytest.mark.parametrize("case", AD_CASES + AD_OPTION_CASES + AD_TERRAIN_CASES)
 def test_run_jvp_matches_reference(case):
     need_gpu()
     from mpas_dycore_pytorch_gb300.api import run_simulation
@@ -71,7 +73,15 @@ def _direction(state, seed):
     return d
 
 
-@pytest.mark.parametrize("case", AD_CASES + AD_OPTION_CASES)
+def _identity_bar(case):
+    """1e-12; over terrain 2e-12: zz != 1 makes every metric division of the implicit
+    acoustic columns round (over flat terrain they divide by exactly 1), and the identity
+    through the final rw measured 1.01e-12 on g2_ad_terrain_fixed (5.3e-13 on g2_ad_terrain;
+    every other field and case <= 2.1e-13), with the products summed exactly."""
+    return 2e-12 if case in AD_TERRAIN_CASES else 1e-12
+
+
+@pytest.mark.parametrize("case", AD_CASES + AD_OPTION_CASES + AD_TERRAIN_CASES)
 def test_jvp_vjp_identity(case):
     need_gpu()
     from mpas_dycore_pytorch_gb300.api import run_simulation
@@ -92,13 +102,15 @@ def test_jvp_vjp_identity(case):
             return (out[k][:-1] * g[:-1].to(out[k].device)).sum()
 
         grads = run_simulation.vjp(state, mesh, objective, track_keys=("u", "w", "theta", "rho"), **kw)
-        lhs = float((g[:-1] * t[:-1].to(g.device)).sum())
-        rhs = sum(float((grads[q][:-1].cpu() * d[q][:-1]).sum()) for q in d)
+        # products summed exactly (one rounding of the whole sum), so the identity measures the
+        # two derivative computations, not the rounding of the dot products
+        lhs = math.fsum((to_np(g)[:-1] * to_np(t)[:-1]).ravel())
+        rhs = math.fsum(np.concatenate([(to_np(grads[q])[:-1] * d[q][:-1].numpy()).ravel() for q in d]))
         err = abs(lhs - rhs) / max(abs(lhs), abs(rhs))
         print(f"{case} identity through {k}: <g, J d> = {lhs:.15e}  <J^T g, d> = {rhs:.15e}  rel {err:.2e}")
         worst = max(worst, err)
         lhs_of[k], rhs_of[k] = lhs, rhs
-        assert err <= 1e-12, (case, k, err)
+        assert err <= _identity_bar(case), (case, k, err)
     # failing controls: a reverse mode returning zeros misses by a relative 1 (every
     # <g, J d> is nonzero), and the cotangent of one field paired with the tangent of another
     # misses by far
@@ -110,7 +122,7 @@ def test_jvp_vjp_identity(case):
 
 
 # ---------------------------------------------------------------- stage identities
-STAGE_CASES = ("g2_explicit", "g2_rk2", "g2_split2", "g2_fixed", "g2_cam", "g2_rayleigh")
+STAGE_CASES = ("g2_explicit", "g2_rk2", "g2_split2", "g2_fixed", "g2_cam", "g2_rayleigh", "g2_terrain")
 
 
 def _jvp_call(model, tan, key, inp):
@@ -122,8 +134,8 @@ def _jvp_call(model, tan, key, inp):
         return lib.mpasg_vimp_jvp(m, c, f, d, float(inp["dts"]), s)
     if key == "dyn_tend":
         return lib.mpasg_dyn_tend_jvp(m, c, f, d, int(inp["rk_step"]), s)
-    if key == "smlstep":  # linear over flat terrain: the stage itself on the tangents
-        return lib.mpasg_smlstep_pert(m, c, d, s)
+    if key == "smlstep":
+        return lib.mpasg_smlstep_jvp(m, c, f, d, s)
     if key == "acoustic":
         return lib.mpasg_acoustic_jvp(m, c, f, d, int(inp["small_step"]), float(inp["dts"]), w, s)
     if key == "divdamp":

@@ -29,14 +29,16 @@ def test_vjp_track_keys_contract():
                                    {"config_mpas_cam_coef": 1.0}, {"config_rayleigh_damp_u": True},
                                    {"config_mix_full": False, "config_v_mom_eddy_visc2": 1.0}])
 def test_dynamics_derivative_scope_takes_the_mixing_and_damping_options(extra):
-    """Vertical mixing, CAM and Rayleigh damping are differentiated: the host-side scope
-    check passes them (terrain and moisture are what it still refuses)."""
+    """Vertical mixing, CAM and Rayleigh damping are differentiated, over terrain too: the
+    host-side scope check passes them (moisture is what it still refuses)."""
     from mpas_dycore_pytorch_gb300.dyn_adjoint import check_request
     state, meta = _case()
     cfg = dict(meta["config"], **extra)
-    check_request(cfg, state, int(state["scalars"].shape[-1]))
-    with pytest.raises(MpasUnsupportedCapabilityError, match="flat terrain"):
-        check_request(cfg, dict(state, zb_cell=np.ones((3, 2))), int(state["scalars"].shape[-1]))
+    n = int(state["scalars"].shape[-1])
+    check_request(cfg, state, n)
+    check_request(cfg, dict(state, zb_cell=np.ones((3, 2))), n)
+    with pytest.raises(MpasUnsupportedCapabilityError, match="dry columns"):
+        check_request(cfg, dict(state, moist_start=0, moist_end=0), n)
 
 
 def test_dynamics_jvp_is_float64_only():
