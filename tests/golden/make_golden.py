@@ -106,6 +106,9 @@ __version__ = "0.0-scipy-netcdf3-reader"
 
 
 def _import_reference(stub: str = _STUB):
+    # the reference tree is read-only input: no bytecode caches written into it (the
+    # environment variable only reaches child processes)
+    sys.dont_write_bytecode = True
     stub_dir = pathlib.Path(tempfile.mkdtemp(prefix="ncstub_"))
     (stub_dir / "netCDF4").mkdir()
     (stub_dir / "netCDF4" / "__init__.py").write_text(stub)
