@@ -582,17 +582,20 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
 
     ``initial_state`` is either a loaded raw state (prepared here, on the device) or a
     complete step boundary returned by a previous call.  Returns the final boundary with
-    the reference's keys; tensors stay on the CUDA device.  With ``differentiable=True``
-    and ``initial_state["scalars"]`` requiring grad, the returned ``scalars`` carry the
+    the reference's keys; tensors stay on the CUDA device.  With ``differentiable=True``:
+    ``initial_state["scalars"]`` requiring grad, the returned ``scalars`` carry the
     hand-written adjoint of the scalar transport into autograd (passive scalars, explicit
-    split transport); other inputs requiring grad are rejected before any device work.
+    split transport); the loaded ``u``, ``w``, ``theta`` or ``rho`` requiring grad, the
+    returned fields carry the hand-written reverse mode of the dynamics (per-step
+    checkpoints, or every step's tape with ``checkpoint_timesteps=False``); other inputs
+    requiring grad are rejected before any device work.
     """
     return _simulate(initial_state, mesh, config, dt, nsteps, device, on_step, differentiable, on_phase, on_initial,
-                     use_cuda_graph, bound=True)
+                     use_cuda_graph, bound=True, checkpoint_timesteps=checkpoint_timesteps)
 
 
 def _simulate(initial_state, mesh, config, dt, nsteps, device, on_step, differentiable, on_phase, on_initial,
-              use_cuda_graph, bound: bool) -> dict:
+              use_cuda_graph, bound: bool, checkpoint_timesteps: bool | None = None) -> dict:
     """run_simulation's body; ``bound`` False (atm_srk3) continues from the given prepared
     state as it is and returns an unbound result."""
     reject_unsupported_request(initial_state, mesh, config)
@@ -601,7 +604,7 @@ def _simulate(initial_state, mesh, config, dt, nsteps, device, on_step, differen
         raise MpasConfigError("nsteps must be a non-negative integer")
     if differentiable and _grad_keys(initial_state, mesh) and nsteps > 0:
         return _run_differentiable(initial_state, mesh, config, dt, int(nsteps), device, on_step, on_phase,
-                                   on_initial)
+                                   on_initial, {"checkpoint_timesteps": checkpoint_timesteps})
     # a boundary is bound to the mesh the caller passed (none when the state is its own mesh)
     boundary_mesh = dict(mesh) if mesh is not None else None
     mesh = mesh if mesh is not None else initial_state
@@ -686,16 +689,22 @@ def _scalar_derivative_forward(state: Mapping[str, Any], mesh: Mapping[str, Any]
     return model, tape, _merge(state, model.export())
 
 
+DYNAMICS_GRAD_KEYS = ("u", "w", "theta", "rho")
+
+
 def _grad_keys(state: Mapping[str, Any], mesh: Mapping[str, Any] | None) -> list[str]:
-    """The inputs that require gradients; only ``scalars`` can (checked before any
-    device work)."""
+    """The inputs that require gradients: ``scalars`` (the hand-written adjoint of the
+    scalar transport) or any of the loaded ``u``, ``w``, ``theta``, ``rho`` (that of the
+    dynamics), not both; checked before any device work."""
     keys = sorted({k for d in (state, mesh or {}) for k, v in d.items()
                    if isinstance(v, torch.Tensor) and v.requires_grad})
-    other = [k for k in keys if k != "scalars"]
-    if other:
+    other = [k for k in keys if k != "scalars" and k not in DYNAMICS_GRAD_KEYS]
+    mesh_keys = [k for k in keys if mesh is not None and k in mesh and k not in state]
+    if other or mesh_keys or ("scalars" in keys and len(keys) > 1):
         raise MpasUnsupportedCapabilityError(
-            "differentiable runs on the GB300 path carry gradients for 'scalars' only (hand-written adjoint of "
-            f"the scalar transport); inputs requiring grad: {other}")
+            "differentiable runs on the GB300 path carry gradients for 'scalars' (hand-written adjoint of the "
+            "scalar transport) or for the loaded u, w, theta, rho (that of the dynamics), not both; inputs "
+            f"requiring grad: {keys}")
     return keys
 
 
@@ -717,12 +726,98 @@ class _ScalarsThroughSteps(torch.autograd.Function):
         return g0.to(ctx.in_device), None, None, None
 
 
-def _run_differentiable(state, mesh, config, dt, nsteps, device, on_step, on_phase, on_initial) -> dict:
-    """run_simulation(differentiable=True) with ``scalars`` requiring grad: the taped
-    forward, and the end scalars attached to the autograd graph through
-    ``_ScalarsThroughSteps`` (passive scalars, explicit split transport)."""
+class _DynamicsThroughSteps(torch.autograd.Function):
+    """The final state of a run as a function of the loaded u, w, theta, rho: forward
+    runs the forward phase of a ``dyn_adjoint.VjpRun`` (the steps with their checkpoints)
+    and returns every floating field of the final state; backward hands the cotangents of
+    the carried fields (and ``rho_edge``) to the run's reverse phase (the hand-written
+    reverse mode) and returns the inputs' gradients.  A nonzero cotangent of any other
+    output (the scalars, the reconstructed winds, ...) is refused: no derivative through it
+    is built, and dropping it would give a wrong gradient."""
+
+    @staticmethod
+    def forward(ctx, run, names, keys, *inputs):  # noqa: D401
+        ctx.set_materialize_grads(False)
+        ctx.run, ctx.names, ctx.keys = run, names, keys
+        ctx.in_meta = [(x.shape[0], x.device) for x in inputs]
+        final = run.final
+        return tuple(final[k] for k in names)
+
+    @staticmethod
+    def backward(ctx, *g_out):
+        from .dyn_adjoint import DIFFERENTIABLE_OUT
+        g = {}
+        for k, v in zip(ctx.names, g_out):
+            if v is None:
+                continue
+            if k not in DIFFERENTIABLE_OUT:
+                if bool(torch.any(v != 0)):
+                    raise MpasUnsupportedCapabilityError(f"the derivative through output {k!r} is not built")
+                continue
+            g[k] = v.detach()
+        grads = ctx.run.reverse(g)
+        res = [grads[k][:rows].to(dev) for k, (rows, dev) in zip(ctx.keys, ctx.in_meta)]
+        return (None, None, None, *res)
+
+
+def _run_differentiable_dynamics(state, mesh, config, dt, nsteps, device, keys, kwargs) -> dict:
+    """run_simulation(differentiable=True) with the loaded u, w, theta or rho requiring grad:
+    the forward phase of the dynamics' reverse mode (per-step checkpoints, or the modes of
+    ``checkpoint_timesteps`` / the configuration's ``gradient_checkpointing`` as for
+    run_simulation.vjp), its final state attached to the autograd graph through
+    ``_DynamicsThroughSteps``."""
+    from .dyn_adjoint import DynamicsAdjoint, VjpRun, check_request
+    if _is_prepared(state):
+        raise MpasUnsupportedCapabilityError(
+            "dynamics derivatives start from a loaded (unprepared) state: track u, w, theta or rho")
+    mesh = mesh if mesh is not None else state
+    plain = {k: (v.detach() if isinstance(v, torch.Tensor) else v) for k, v in state.items()}
+    merged = dict(mesh)
+    merged.update(plain)
+    cfg = resolved_config(config)
+    dt = float(cfg["config_dt"] if dt is None else dt)
+    ns = _int(merged.get("num_scalars", _np(merged["scalars"]).shape[-1]))
+    check_request(cfg, merged, ns, allow_mixed=True)
+    model = Model(merged, cfg, dt, num_scalars=ns, device=device)
+    run = VjpRun(model, merged, nsteps, DynamicsAdjoint(model), checkpoint=_checkpoint_mode(config, kwargs))
+    run.final = run.forward()
+    out = _merge(plain, run.final)
+    names = tuple(k for k, v in run.final.items()
+                  if k not in STATIC_KEYS and isinstance(v, torch.Tensor) and torch.is_floating_point(v))
+    attached = _DynamicsThroughSteps.apply(run, names, tuple(keys), *[state[k] for k in keys])
+    out.update(dict(zip(names, attached)))
+    return out
+
+
+def _checkpoint_mode(config, kwargs) -> str:
+    """checkpoint_timesteps=False keeps every step's tape (no recomputation), as the
+    reference keeps the whole graph without its per-step checkpoint; gradient_checkpointing
+    in the configuration (the reference's nested recomputation inside the step) recomputes
+    every dynamics substep from its step's checkpoint and keeps sqrt(nsteps) step checkpoints
+    (atmosphere_model.py:120-154); otherwise one checkpoint per step."""
+    if kwargs.get("checkpoint_timesteps") is False:
+        return "none"
+    if "gradient_checkpointing" in (config or {}) and _flag(dict(config), "gradient_checkpointing"):
+        return "sqrt"
+    return "step"
+
+
+def _run_differentiable(state, mesh, config, dt, nsteps, device, on_step, on_phase, on_initial,
+                        kwargs=None) -> dict:
+    """run_simulation(differentiable=True) with inputs requiring grad.  ``scalars``: the
+    taped forward, and the end scalars attached to the autograd graph through
+    ``_ScalarsThroughSteps`` (passive scalars, explicit split transport); the loaded u, w,
+    theta, rho: ``_run_differentiable_dynamics``."""
     if on_step is not None or on_initial is not None:
         raise MpasUnsupportedCapabilityError("on_step / on_initial are not available in differentiable runs")
+    keys = _grad_keys(state, mesh)
+    if "scalars" not in keys:
+        if on_phase is not None:
+            on_phase("forecast_integration_begin")
+        out = _run_differentiable_dynamics(state, mesh, config, dt, nsteps, device, keys, kwargs or {})
+        if on_phase is not None:
+            on_phase("forecast_integration_end")
+        return out
     plain = {k: (v.detach() if isinstance(v, torch.Tensor) else v) for k, v in state.items()}
     if on_phase is not None:
         on_phase("forecast_integration_begin")
@@ -793,19 +888,8 @@ def _dynamics_vjp(state: Mapping[str, Any], mesh: Mapping[str, Any] | None, obje
             res[k] = g.detach()
         return res
 
-    # checkpoint_timesteps=False keeps every step's tape (no recomputation), as the reference
-    # keeps the whole graph without its per-step checkpoint; gradient_checkpointing in the
-    # configuration (the reference's nested recomputation inside the step) recomputes every
-    # dynamics substep from its step's checkpoint and keeps sqrt(nsteps) step checkpoints
-    # (atmosphere_model.py:120-154)
-    if kwargs.get("checkpoint_timesteps") is False:
-        mode = "none"
-    elif "gradient_checkpointing" in (kwargs.get("config") or {}) and \
-            _flag(dict(kwargs["config"]), "gradient_checkpointing"):
-        mode = "sqrt"
-    else:
-        mode = "step"
-    grads, _ = run_vjp(model, merged, nsteps, cotangents, adj, checkpoint=mode)
+    grads, _ = run_vjp(model, merged, nsteps, cotangents, adj,
+                       checkpoint=_checkpoint_mode(kwargs.get("config"), kwargs))
     res = {}
     for k in keys:
         ref = state[k]

@@ -286,13 +286,15 @@ class DynamicsAdjoint:
         return out
 
 
-def run_vjp(model, loaded: Mapping[str, Any], nsteps: int,
-            cotangents: Callable[[dict], Mapping[str, torch.Tensor]],
-            adj: DynamicsAdjoint | None = None, checkpoint: str = "step") -> tuple[dict, dict]:
-    """Forward from the loaded primitives through ``nsteps`` large steps, then the reverse
-    sweep.  ``cotangents(out)`` receives the final state (the model's export) and returns
-    cotangents of some of its carried fields.  Returns the cotangents of the loaded u, w,
-    theta, rho and the final state.
+class VjpRun:
+    """The two phases of a reverse-mode run, so that they can happen at different times
+    (``run_vjp``; ``run_simulation(differentiable=True)`` runs the forward phase in its
+    forward and the reverse phase when autograd asks for the inputs' gradients).
+
+    ``forward()`` prepares the loaded primitives and runs ``nsteps`` large steps, keeping
+    what the reverse phase needs under the checkpoint mode; it returns the final state.
+    ``reverse(g)`` takes cotangents of the final state's carried fields (and ``rho_edge``)
+    and returns those of the loaded u, w, theta, rho; it can run once.
 
     ``checkpoint="step"`` (the reference's default, checkpoint_timesteps on): one checkpoint
     of the step boundary per step in HBM; the reverse pass of each step first recomputes it
@@ -305,86 +307,112 @@ def run_vjp(model, loaded: Mapping[str, Any], nsteps: int,
     and each step runs backwards one dynamics substep at a time, every substep recomputed
     from the step's checkpoint with only its own tape (mpasg_step_vjp_window).  Checkpoints
     held: at most ceil(nsteps / S) + S - 1; the same gradient bit for bit."""
-    if checkpoint not in ("step", "none", "sqrt"):
-        raise MpasConfigError(f"checkpoint must be 'step', 'none' or 'sqrt', got {checkpoint!r}")
-    adj = adj or DynamicsAdjoint(model)
-    model.prepare(loaded)
-    w_in = model.state.f["w"].clone()
-    ck0 = adj.checkpoint()
-    tapes: list[torch.Tensor] = []
-    ckpts = [ck0]
-    seg = max(1, int(np.ceil(np.sqrt(int(nsteps))))) if checkpoint == "sqrt" else 1
-    outer = {0: ck0}
 
-    def forward_step(n):
-        model.step()
-        if n == 0 and nsteps > 1 and model._graph is None:
-            model.capture_graph()  # later steps replay the step graph (bitwise the eager step)
+    def __init__(self, model, loaded: Mapping[str, Any], nsteps: int, adj: DynamicsAdjoint | None = None,
+                 checkpoint: str = "step"):
+        if checkpoint not in ("step", "none", "sqrt"):
+            raise MpasConfigError(f"checkpoint must be 'step', 'none' or 'sqrt', got {checkpoint!r}")
+        self.model, self.loaded, self.nsteps, self.mode = model, loaded, int(nsteps), checkpoint
+        self.adj = adj or DynamicsAdjoint(model)
+        self.done = False
 
-    if checkpoint == "step":
-        for n in range(int(nsteps)):
-            forward_step(n)
-            if n + 1 < nsteps:
-                ckpts.append(adj.checkpoint())
-    elif checkpoint == "sqrt":
-        for n in range(int(nsteps)):
-            forward_step(n)
-            if n + 1 < nsteps and (n + 1) % seg == 0:
-                outer[n + 1] = adj.checkpoint()
-    else:
-        nd = adj.tape_doubles()
-        free, _ = torch.cuda.mem_get_info(model.dmesh.device)
-        if nd * 8 * int(nsteps) > 0.9 * free:
-            raise MpasConfigError(f"checkpoint='none' needs {nd * 8 * nsteps / 1e9:.1f} GB of tapes; "
-                                  f"{free / 1e9:.1f} GB are free (use checkpoint='step')")
-        for n in range(int(nsteps)):
-            tapes.append(torch.empty(nd, dtype=torch.float64, device=model.dmesh.device))
-            adj.step_tape(tapes[-1])
-    bad = model.check_finite()
-    if bad:
-        raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")
-    final = model.export()
-    if checkpoint == "none":
-        for k in ("scalars", "uReconstructX", "uReconstructY", "uReconstructZ", "uReconstructZonal",
-                  "uReconstructMeridional", "ur_cell", "vr_cell"):
-            final.pop(k, None)
-    adj.zero_cotangents()
-    dev = model.dmesh.device
-    g = cotangents(final)
-    for k, v in g.items():
-        name = "h_edge" if k == "rho_edge" else k
-        if name not in CARRIED:
-            raise MpasUnsupportedCapabilityError(f"no derivative through output {k!r}")
-        dst = adj.g.f[name]
-        dst[: v.shape[0]].add_(v.to(device=dev, dtype=torch.float64))
-    if checkpoint == "sqrt":
-        split = int(model.cstruct.dynamics_split_steps)
-        for start in sorted(outer, reverse=True):
-            end = min(start + seg, int(nsteps))
-            adj.restore(outer[start])
-            inner = [outer[start]]
-            for n in range(start, end - 1):
-                model.step()
-                inner.append(adj.checkpoint())
-            for n in range(end - 1, start - 1, -1):
-                for sub in range(split, 0, -1):
-                    adj.restore(inner[n - start])
-                    adj.step_vjp_window(sub)
-            if start > 0:
-                del outer[start]
-            del inner
-    for n in range(int(nsteps) - 1, -1, -1):
-        if checkpoint == "sqrt":
-            break
+    def forward(self) -> dict:
+        model, adj, nsteps, checkpoint = self.model, self.adj, self.nsteps, self.mode
+        model.prepare(self.loaded)
+        self.w_in = model.state.f["w"].clone()
+        self.ck0 = adj.checkpoint()
+        self.tapes: list[torch.Tensor | None] = []
+        self.ckpts = [self.ck0]
+        self.seg = max(1, int(np.ceil(np.sqrt(nsteps)))) if checkpoint == "sqrt" else 1
+        self.outer = {0: self.ck0}
+
+        def forward_step(n):
+            model.step()
+            if n == 0 and nsteps > 1 and model._graph is None:
+                model.capture_graph()  # later steps replay the step graph (bitwise the eager step)
+
         if checkpoint == "step":
-            adj.restore(ckpts[n])
-            adj.step_vjp()
+            for n in range(nsteps):
+                forward_step(n)
+                if n + 1 < nsteps:
+                    self.ckpts.append(adj.checkpoint())
+        elif checkpoint == "sqrt":
+            for n in range(nsteps):
+                forward_step(n)
+                if n + 1 < nsteps and (n + 1) % self.seg == 0:
+                    self.outer[n + 1] = adj.checkpoint()
         else:
-            adj.step_vjp_taped(tapes[n])
-            tapes[n] = None  # free as the sweep goes
-    adj.restore(ck0)
-    grads = adj.prepare_vjp(w_in)
-    return grads, final
+            nd = adj.tape_doubles()
+            free, _ = torch.cuda.mem_get_info(model.dmesh.device)
+            if nd * 8 * nsteps > 0.9 * free:
+                raise MpasConfigError(f"checkpoint='none' needs {nd * 8 * nsteps / 1e9:.1f} GB of tapes; "
+                                      f"{free / 1e9:.1f} GB are free (use checkpoint='step')")
+            for n in range(nsteps):
+                self.tapes.append(torch.empty(nd, dtype=torch.float64, device=model.dmesh.device))
+                adj.step_tape(self.tapes[-1])
+        bad = model.check_finite()
+        if bad:
+            raise MpasNumericalError(f"forecast result contains {bad} nonfinite values")
+        final = model.export()
+        if checkpoint == "none":
+            for k in ("scalars", "uReconstructX", "uReconstructY", "uReconstructZ", "uReconstructZonal",
+                      "uReconstructMeridional", "ur_cell", "vr_cell"):
+                final.pop(k, None)
+        return final
+
+    def reverse(self, g: Mapping[str, torch.Tensor]) -> dict:
+        if self.done:
+            raise MpasUnsupportedCapabilityError("the reverse pass of a derivative run can run once")
+        self.done = True
+        model, adj, nsteps, checkpoint = self.model, self.adj, self.nsteps, self.mode
+        adj.zero_cotangents()
+        dev = model.dmesh.device
+        for k, v in g.items():
+            name = "h_edge" if k == "rho_edge" else k
+            if name not in CARRIED:
+                raise MpasUnsupportedCapabilityError(f"no derivative through output {k!r}")
+            dst = adj.g.f[name]
+            dst[: v.shape[0]].add_(v.to(device=dev, dtype=torch.float64))
+        if checkpoint == "sqrt":
+            split = int(model.cstruct.dynamics_split_steps)
+            seg, outer = self.seg, self.outer
+            for start in sorted(outer, reverse=True):
+                end = min(start + seg, nsteps)
+                adj.restore(outer[start])
+                inner = [outer[start]]
+                for n in range(start, end - 1):
+                    model.step()
+                    inner.append(adj.checkpoint())
+                for n in range(end - 1, start - 1, -1):
+                    for sub in range(split, 0, -1):
+                        adj.restore(inner[n - start])
+                        adj.step_vjp_window(sub)
+                if start > 0:
+                    del outer[start]
+                del inner
+        else:
+            for n in range(nsteps - 1, -1, -1):
+                if checkpoint == "step":
+                    adj.restore(self.ckpts[n])
+                    adj.step_vjp()
+                else:
+                    adj.step_vjp_taped(self.tapes[n])
+                    self.tapes[n] = None  # free as the sweep goes
+        self.ckpts = []
+        adj.restore(self.ck0)
+        return adj.prepare_vjp(self.w_in)
+
+
+def run_vjp(model, loaded: Mapping[str, Any], nsteps: int,
+            cotangents: Callable[[dict], Mapping[str, torch.Tensor]],
+            adj: DynamicsAdjoint | None = None, checkpoint: str = "step") -> tuple[dict, dict]:
+    """Forward from the loaded primitives through ``nsteps`` large steps, then the reverse
+    sweep (``VjpRun``, which describes the checkpoint modes).  ``cotangents(out)`` receives
+    the final state (the model's export) and returns cotangents of some of its carried
+    fields.  Returns the cotangents of the loaded u, w, theta, rho and the final state."""
+    run = VjpRun(model, loaded, nsteps, adj, checkpoint)
+    final = run.forward()
+    return run.reverse(cotangents(final)), final
 
 
 class DynamicsTangent:

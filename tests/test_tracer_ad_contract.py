@@ -95,13 +95,21 @@ def test_jvp_perturbation_contract():
         run_simulation.jvp(state, state, {"scalars": np.zeros(3)}, config=meta["config"])
 
 
-def test_differentiable_runs_carry_scalar_gradients_only():
-    """differentiable=True with a non-scalar input requiring grad is rejected before any
-    device work (the GB300 adjoint covers the scalar transport)."""
+def test_differentiable_runs_take_scalars_or_the_dynamics_inputs():
+    """differentiable=True carries gradients for the scalars or for the loaded u, w, theta,
+    rho, not both; any other input requiring grad, and a dynamics input of a moist run,
+    are rejected before any device work."""
     import mpas_dycore_pytorch_gb300 as gb
     from fixtures import group, load_case
     meta, st, _ = load_case("g2_explicit")
     state = {k: torch.as_tensor(v) for k, v in group(st, "loaded").items()}
-    state["u"] = state["u"].clone().requires_grad_(True)
-    with pytest.raises(gb.MpasUnsupportedCapabilityError, match="scalars"):
-        gb.run_simulation(state, state, meta["config"], meta["dt"], nsteps=1, differentiable=True)
+    both = dict(state, u=state["u"].clone().requires_grad_(True),
+                scalars=state["scalars"].clone().requires_grad_(True))
+    with pytest.raises(gb.MpasUnsupportedCapabilityError, match="not both"):
+        gb.run_simulation(both, state, meta["config"], meta["dt"], nsteps=1, differentiable=True)
+    other = dict(state, zgrid=state["zgrid"].clone().requires_grad_(True))
+    with pytest.raises(gb.MpasUnsupportedCapabilityError, match="zgrid"):
+        gb.run_simulation(other, state, meta["config"], meta["dt"], nsteps=1, differentiable=True)
+    moist = dict(state, u=state["u"].clone().requires_grad_(True), moist_end=1)
+    with pytest.raises(gb.MpasUnsupportedCapabilityError, match="dry columns"):
+        gb.run_simulation(moist, state, meta["config"], meta["dt"], nsteps=1, differentiable=True)
