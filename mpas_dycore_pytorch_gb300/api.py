@@ -214,6 +214,15 @@ LATE_KEYS = ("scalars",)
 STATIC_KEYS = ("rtheta_base", "exner_base", "pressure_base", "rt_diabatic_tend")
 
 
+def _copy_stream(device) -> torch.cuda.Stream:
+    """A stream for the host copies of a step boundary, at the highest priority: with a
+    reordered mesh every field copied out or in passes through a row gather (a kernel),
+    and at the default priority those gathers queue behind the blocks of the step's own
+    kernels, so the copies of a step's result stall while the next kernels run (measured:
+    1.6 ms more per level-6 step through ``run_host``)."""
+    return torch.cuda.Stream(device=device, priority=-1)
+
+
 def _stream_ptr(stream: torch.cuda.Stream | None = None) -> C.c_void_p:
     s = stream if stream is not None else torch.cuda.current_stream()
     return C.c_void_p(s.cuda_stream)
@@ -330,7 +339,7 @@ class Model:
         synchronise the device) before reading the host tensors."""
         cur = torch.cuda.current_stream()
         if self._d2h_stream is None:
-            self._d2h_stream = torch.cuda.Stream(device=self.dmesh.device)
+            self._d2h_stream = _copy_stream(self.dmesh.device)
         side = self._d2h_stream
         ex = self.state.export()
         for k, dst in host.items():
@@ -426,9 +435,9 @@ class Model:
         dev = self.dmesh.device
         cur = torch.cuda.current_stream(dev)
         if self._d2h_stream is None:
-            self._d2h_stream = torch.cuda.Stream(device=dev)
+            self._d2h_stream = _copy_stream(dev)
         if self._h2d_stream is None:
-            self._h2d_stream = torch.cuda.Stream(device=dev)
+            self._h2d_stream = _copy_stream(dev)
         down, up = self._d2h_stream, self._h2d_stream
         # the copy streams start after everything issued so far (an earlier call's copies
         # out into these host tensors, loads, steps)
