@@ -117,3 +117,66 @@ def test_gradient_matches_central_differences():
     # failing control: without its theta part the directional derivative misses every point
     dJ_u = float((grads["u"].cpu() * d["u"]).sum())
     assert min(abs(fd - dJ_u) / abs(dJ) for _, fd, _ in rows) > 1e-3
+
+
+def test_terrain_gradient_matches_central_differences():
+    """Over terrain-following levels (a 1500 m cosine hill on the level-4 mesh, 26 levels,
+    fixed-coefficient mixing, 4 steps at dt 1200 s): the gradient with respect to u and
+    theta along a seeded direction against central differences over h = 2^-12 ... 2^-30,
+    best point within 1e-7; the control without the theta part misses by far."""
+    need_gpu()
+    from mpas_dycore_pytorch_gb300.api import run_simulation
+    from mpas_dycore_pytorch_gb300.cases import CaseSpec
+    from mpas_dycore_pytorch_gb300.diagnostics import physics_interface_surface_pressure, surface_pressure_functional
+    from mpas_dycore_pytorch_gb300.loader import load_case
+    spec = dict(level=4, nlev=26, dz_bottom=300.0, seed=6, n_bumps=8, n_tracers=1, w_sine=0.1,
+                round_wind_bits=16, terrain=1500.0)
+    cfg = {"config_time_integration_order": 3, "config_len_disp": 240000.0, "config_number_of_sub_steps": 2,
+           "config_dynamics_split_steps": 3, "config_monotonic": False, "config_dt": 1200.0,
+           "config_horiz_mixing": "2d_fixed", "config_h_mom_eddy_visc4": 1.0e11,
+           "config_h_theta_eddy_visc4": 5.0e10, "config_h_theta_eddy_visc2": 4.0e4}
+    nsteps = 4
+    st, mesh = load_case(CaseSpec(**spec), cfg, as_torch=True)
+    nc = int(st["nCells"])
+    dev = torch.device("cuda")
+    zz, zgrid, area = (st[k].to(dev, torch.float64) for k in ("zz", "zgrid", "areaCell"))
+
+    def sp_of(out):
+        rz = out["rho_zz"]
+        return physics_interface_surface_pressure(nCells=nc, rho_zz=rz, zz=zz, qv=torch.zeros_like(rz),
+                                                  pressure_p=out["pressure_p"], pressure_base=out["pressure_base"],
+                                                  zgrid=zgrid)
+
+    box = {}
+    run_simulation(st, mesh, cfg, 1200.0, nsteps=1,
+                   on_initial=lambda s: box.update({k: v.clone() for k, v in s.items()
+                                                    if isinstance(v, torch.Tensor) and v.is_cuda}))
+    sp_ref = sp_of(box).detach()
+
+    def objective(out):
+        return surface_pressure_functional(sp_of(out), sp_ref, area, nc)
+
+    grads = run_simulation.vjp(st, mesh, objective, track_keys=("u", "theta"), config=cfg, dt=1200.0,
+                               nsteps=nsteps)
+    rng = np.random.default_rng(6)
+    d = {}
+    for k, scale in (("u", 1.0), ("theta", 0.1)):
+        x = rng.standard_normal(tuple(st[k].shape)) * scale
+        x[-1] = 0.0
+        d[k] = torch.as_tensor(x)
+    dJ = sum(float((grads[k].cpu() * d[k]).sum()) for k in d)
+    rows = []
+    for h in [2.0 ** -e for e in range(12, 31, 2)]:
+        Js = []
+        for sgn in (1.0, -1.0):
+            s2 = dict(st)
+            for k in d:
+                s2[k] = st[k] + sgn * h * d[k]
+            Js.append(float(objective(run_simulation(s2, mesh, cfg, 1200.0, nsteps=nsteps))))
+        fd = (Js[0] - Js[1]) / (2.0 * h)
+        rows.append((h, fd, abs(fd - dJ) / abs(dJ)))
+    for h, fd, err in rows:
+        print(f"terrain FD h=2^{int(round(math.log2(h)))} fd={fd:.12e} adjoint={dJ:.12e} rel_err={err:.3e}")
+    assert min(r[2] for r in rows) <= 1e-7, [r[2] for r in rows]
+    dJ_u = float((grads["u"].cpu() * d["u"]).sum())
+    assert min(abs(fd - dJ_u) / abs(dJ) for _, fd, _ in rows) > 1e-3
