@@ -596,7 +596,8 @@ def run_simulation(initial_state: Mapping[str, Any], mesh: Mapping[str, Any] | N
     hand-written adjoint of the scalar transport into autograd (passive scalars, explicit
     split transport); the loaded ``u``, ``w``, ``theta`` or ``rho`` requiring grad, the
     returned fields carry the hand-written reverse mode of the dynamics (per-step
-    checkpoints, or every step's tape with ``checkpoint_timesteps=False``); other inputs
+    checkpoints, or every step's tape with ``checkpoint_timesteps=False``, whose forward
+    advances the dynamics only, so its result has no scalars or reconstructed winds); other inputs
     requiring grad are rejected before any device work.
     """
     return _simulate(initial_state, mesh, config, dt, nsteps, device, on_step, differentiable, on_phase, on_initial,
@@ -791,6 +792,13 @@ def _run_differentiable_dynamics(state, mesh, config, dt, nsteps, device, keys, 
     run = VjpRun(model, merged, nsteps, DynamicsAdjoint(model), checkpoint=_checkpoint_mode(config, kwargs))
     run.final = run.forward()
     out = _merge(plain, run.final)
+    # with every step's tape kept (checkpoint_timesteps=False) the forward advances the
+    # dynamics only: the scalars and the reconstructed winds are not part of the result
+    # (not the loaded ones passed through)
+    for k in ("scalars", "uReconstructX", "uReconstructY", "uReconstructZ", "uReconstructZonal",
+              "uReconstructMeridional", "ur_cell", "vr_cell"):
+        if k not in run.final:
+            out.pop(k, None)
     names = tuple(k for k, v in run.final.items()
                   if k not in STATIC_KEYS and isinstance(v, torch.Tensor) and torch.is_floating_point(v))
     attached = _DynamicsThroughSteps.apply(run, names, tuple(keys), *[state[k] for k in keys])

@@ -261,6 +261,8 @@ def test_differentiable_run_backward_is_the_hand_written_vjp(case):
         state["theta"] = state["theta"].clone().requires_grad_(True)
         out = run_simulation(state, mesh, differentiable=True, checkpoint_timesteps=not tape_all, **kw)
         assert out["rho_zz"].requires_grad and out["u"].requires_grad
+        # the tape-all forward advances the dynamics only: no stale scalars in its result
+        assert ("scalars" in out) != tape_all
         objective(out).backward()
         for k in ("u", "theta"):
             g = state[k].grad
