@@ -101,6 +101,16 @@ MPASG_D T wduz_at(const T* __restrict__ u, T rwe, int kk, int L, const T* fzm, c
   return flux3<T>(u[kk - 2], u[kk - 1], u[kk], u[kk + 1], rwe, T(1));
 }
 
+// pv_edge * u at every edge level, the neighbour factor of the float64 PV flux sum (below),
+// formed once per tendency stage instead of once per reading edge; stored in ke_edge (the
+// diagnostics' edge kinetic-energy scratch, free between two diagnostics stages)
+template <typename T>
+__global__ void k_pvu(mpasg_mesh m, mpasg_fields f, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  fpw<T>(f.ke_edge, f.ke_edge_f32)[i] = fp<T>(f.pv_edge, f.pv_edge_f32)[i] * fp<T>(f.u, f.u_f32)[i];
+}
+
 // RAY: Rayleigh damping of u compiled in (a run-time test would cost float64 work in
 // every thread of the hot kernel once the compiler predicates it)
 template <typename T, bool RAY = false>
@@ -140,21 +150,36 @@ __global__ void __launch_bounds__(kBlock) k_tend_u(mpasg_mesh m, mpasg_fields f,
     wd_k1 = wduz_at<T>(ue, rwe_k1, k + 1, L, fzm, fzp);
   }
   T tu = -G(rdzw)[k] * (wd_k1 - wd_k);
-  // nonlinear Coriolis / PV flux over the TRiSK stencil:
-  // sum_j (w_j u_j) * 0.5 (pv_self + pv_j), with the exact power-of-two factor 0.5
-  // applied once to the sum (scaling by 0.5 commutes with every rounding of the sum)
+  // nonlinear Coriolis / PV flux over the TRiSK stencil, sum_j w_j u_j 0.5 (pv_self + pv_j)
+  // over the slots in order.  float64: as 0.5 (pv_self sum_j w_j u_j + sum_j w_j (pv u)_j),
+  // two multiply-adds per neighbour on the float64 pipe that bounds the kernel, (pv u)
+  // formed once per edge level by k_pvu; float32: as written, the exact power-of-two
+  // factor 0.5 applied once to the sum (the extra pass would cost more than it saves)
   const int n2 = m.nEdgesOnEdge[e];
   const int me2 = m.maxEdges2;
   const T* pv = fp<T>(f.pv_edge, f.pv_edge_f32);
   const T* woe = G(weightsOnEdge);
   const T pv_self = pv[i];
-  T q = T(0);
-  for (int j = 0; j < n2; ++j) {
-    int eo = m.edgesOnEdge[e * me2 + j];
-    T t = (woe[e * me2 + j] * u[(size_t)eo * L + k]) * (pv_self + pv[(size_t)eo * L + k]);
-    q = (j == 0) ? t : q + t;
+  T q;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    const double* pvu = f.ke_edge;
+    T sa = T(0), sb = T(0);
+    for (int j = 0; j < n2; ++j) {
+      const size_t io = (size_t)m.edgesOnEdge[e * me2 + j] * L + k;
+      const T w = woe[e * me2 + j];
+      sa = (j == 0) ? w * u[io] : sa + w * u[io];
+      sb = (j == 0) ? w * pvu[io] : sb + w * pvu[io];
+    }
+    q = T(0.5) * (pv_self * sa + sb);
+  } else {
+    q = T(0);
+    for (int j = 0; j < n2; ++j) {
+      int eo = m.edgesOnEdge[e * me2 + j];
+      T t = (woe[e * me2 + j] * u[(size_t)eo * L + k]) * (pv_self + pv[(size_t)eo * L + k]);
+      q = (j == 0) ? t : q + t;
+    }
+    q = T(0.5) * q;
   }
-  q = T(0.5) * q;
   const size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
   const T inv_dc = G(invDcEdge)[e];
   const T rho_e = cv<T>(f.h_edge[i]);
@@ -213,12 +238,15 @@ __global__ void __launch_bounds__(kBlock) k_tend_u_chunk(mpasg_mesh m, mpasg_fie
   const int n2 = m.nEdgesOnEdge[e];
   const int me2 = m.maxEdges2;
   const T* pv = fp<T>(f.pv_edge, f.pv_edge_f32);
+  const T* pvu = fp<T>(f.ke_edge, f.ke_edge_f32);  // float64 only (k_tend_u)
   const T* woe = G(weightsOnEdge);
-  T pv_self[V], q[V];
+  constexpr bool kSplit = sizeof(T) == sizeof(double);
+  T pv_self[V], sa[V], sb[V];
 #pragma unroll
   for (int v = 0; v < V; ++v) {
     pv_self[v] = (k0 + v < L) ? pv[(size_t)e * L + k0 + v] : T(0);
-    q[v] = T(0);
+    sa[v] = T(0);
+    sb[v] = T(0);
   }
   for (int j = 0; j < n2; ++j) {
     const int eo = m.edgesOnEdge[e * me2 + j];
@@ -227,8 +255,13 @@ __global__ void __launch_bounds__(kBlock) k_tend_u_chunk(mpasg_mesh m, mpasg_fie
     for (int v = 0; v < V; ++v) {
       if (k0 + v < L) {
         const size_t oo = (size_t)eo * L + k0 + v;
-        T t = (w * u[oo]) * (pv_self[v] + pv[oo]);
-        q[v] = (j == 0) ? t : q[v] + t;
+        if (kSplit) {
+          sa[v] = (j == 0) ? w * u[oo] : sa[v] + w * u[oo];
+          sb[v] = (j == 0) ? w * pvu[oo] : sb[v] + w * pvu[oo];
+        } else {
+          const T t = (w * u[oo]) * (pv_self[v] + pv[oo]);
+          sa[v] = (j == 0) ? t : sa[v] + t;
+        }
       }
     }
   }
@@ -239,7 +272,7 @@ __global__ void __launch_bounds__(kBlock) k_tend_u_chunk(mpasg_mesh m, mpasg_fie
     if (k >= L) break;
     const size_t ie = (size_t)e * L + k;
     T tu = -G(rdzw)[k] * ((k + 1 >= L ? T(0) : wd[v + 1]) - wd[v]);
-    const T qv = T(0.5) * q[v];
+    const T qv = kSplit ? T(0.5) * (pv_self[v] * sa[v] + sb[v]) : T(0.5) * sa[v];
     const size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
     const T rho_e = cv<T>(f.h_edge[ie]);
     tu = tu + rho_e * (qv - dif<T>(f.ke[i2], f.ke[i1]) * inv_dc) -
@@ -786,6 +819,10 @@ int launch_dyn_tend(const mpasg_mesh* m, mpasg_fields* f, const TendScalars& p, 
   else
     k_tend_cells_a<T><<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, fl, p);
   MPASG_LAUNCH_CHECK();
+  if (sizeof(T) == sizeof(double)) {  // the float64 PV flux reads pv_edge * u (k_tend_u)
+    k_pvu<T><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, nel);
+    MPASG_LAUNCH_CHECK();
+  }
   const int vt = tile_levels(c_tile);  // levels per thread of k_tend_u (autotuner choice)
   const bool ray = p.ray_n > 0;
   if (vt == 1) {
@@ -901,8 +938,8 @@ int mpasgi_dyn_tend(const mpasg_mesh* m, const mpasg_config* c, mpasg_fields* f,
 
 // Autotuner: times the u-tendency kernel with 1, 2 and 4 levels per thread on the current
 // state (rk-2 form, 3 launches each after one warm-up) and keeps the fastest in
-// c->tile_tend_u.  Host-synchronising: call it outside stream capture.  The kernel only
-// writes its outputs (tend_u, ...), so the state is unchanged.
+// c->tile_tend_u.  Host-synchronising: call it outside stream capture.  The kernels only
+// write their outputs (tend_u, ...) and the ke_edge scratch, so the state is unchanged.
 extern "C" int mpasg_autotune(const mpasg_mesh* m, mpasg_config* c, mpasg_fields* f, float* times_ms,
                               void* stream) {
   if (!m || !c || !f) return MPASG_E_ARG;
@@ -919,6 +956,11 @@ extern "C" int mpasg_autotune(const mpasg_mesh* m, mpasg_config* c, mpasg_fields
   const long long nel = (long long)m->nEdges * L;
   cudaEvent_t a, b;
   if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return MPASG_E_CUDA;
+  if (!mixed) {
+    k_pvu<double><<<nblocks(nel), kBlock, 0, s>>>(*m, *f, nel);
+    mpasg_count_launch();
+    if (cudaGetLastError() != cudaSuccess) return MPASG_E_LAUNCH;
+  }
   const int tiles[3] = {1, 2, 4};
   float best = 1e30f;
   int best_tile = 1;
