@@ -6,7 +6,7 @@
 
 // Work buffer of the dynamics VJPs: kAdjE edge arrays (E+1) x L, kAdjC cell arrays
 // (C+1) x (L+1) and kAdjV vertex arrays (V+1) x L, each 256-byte aligned.
-constexpr int kAdjE = 19, kAdjC = 16, kAdjV = 4;
+constexpr int kAdjE = 21, kAdjC = 16, kAdjV = 4;
 
 struct AdjWork {
   double* e[kAdjE];

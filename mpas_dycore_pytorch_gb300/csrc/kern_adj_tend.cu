@@ -414,10 +414,18 @@ __global__ void k_tadj_adv_cells(mpasg_mesh m, mpasg_fields g, mpasg_transpose t
 // gradient, divergence coupling; at rk 1 the pressure gradient and del2 / del4 mixing)
 // qa = G rho_edge per edge level: the cotangent of the PV flux q of that edge, which every
 // TRiSK neighbour of the edge reads
+// per edge level, the factors the PV-flux transpose reads at every neighbour: qa = G
+// rho_edge (the cotangent of that edge's PV flux sum), qa pv_edge, and pv_edge u (the
+// forward sum's neighbour factor), so each neighbour costs four multiply-adds
 __global__ void k_tadj_qa(int n, const double* __restrict__ gtu, const double* __restrict__ h,
-                          double* __restrict__ qa) {
+                          const double* __restrict__ pv, const double* __restrict__ u, double* __restrict__ qa,
+                          double* __restrict__ qapv, double* __restrict__ pvu) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) qa[i] = gtu[i] * h[i];
+  if (i >= n) return;
+  const double q = gtu[i] * h[i];
+  qa[i] = q;
+  qapv[i] = q * pv[i];
+  pvu[i] = pv[i] * u[i];
 }
 
 // The vertical-transport part per interface q of the edge: its flux's cotangent
@@ -463,7 +471,8 @@ __global__ void __launch_bounds__(kBlock) k_tadj_u(mpasg_mesh m, mpasg_fields f,
                                                    double* __restrict__ prwe, double* __restrict__ ppp,
                                                    double* __restrict__ pkd, double* __restrict__ udb,
                                                    double* __restrict__ pd4, const double* __restrict__ qa,
-                                                   double* __restrict__ pdz) {
+                                                   double* __restrict__ pdz, const double* __restrict__ qapv,
+                                                   const double* __restrict__ pvu) {
   __shared__ double s_c[4][kBlock];
   const int L = m.nVertLevels;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -492,23 +501,23 @@ __global__ void __launch_bounds__(kBlock) k_tadj_u(mpasg_mesh m, mpasg_fields f,
   const double inv_dc = m.invDcEdge[e];
   // PV flux q_e = 0.5 sum_j w_j u_j (pv_e + pv_j), with its transpose over edgesOnEdge: the
   // neighbour eo's sum reads u_e and pv_e at its slot jt (cotangent of q_eo: G_eo rho_edge_eo)
-  // four sums over the stencil, combined after the loop (six float64 operations per slot):
-  // s1 = sum w u, s2 = sum w u pv, s3 = sum A wt, s4 = sum A wt pv, A = G_eo rho_edge_eo
+  // four sums over the stencil, combined after the loop (four multiply-adds per slot, the
+  // per-edge products from k_tadj_qa): s1 = sum w u, s2 = sum w (pv u), s3 = sum wt A,
+  // s4 = sum wt (A pv), A = G_eo rho_edge_eo
   const int n2 = m.nEdgesOnEdge[e], me2 = m.maxEdges2;
   const double pv_self = f.pv_edge[i], u_self = ue[k];
   double s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = 0.0;
   for (int j = 0; j < n2; ++j) {
     const int eo = m.edgesOnEdge[e * me2 + j];
     const size_t io = (size_t)eo * L + k;
-    const double pv_o = f.pv_edge[io];
-    const double wu = m.weightsOnEdge[e * me2 + j] * f.u[io];
-    s1 += wu;
-    s2 += wu * pv_o;
+    const double w = m.weightsOnEdge[e * me2 + j];
+    s1 = fma(w, f.u[io], s1);
+    s2 = fma(w, pvu[io], s2);
     const int jt = t.eoeTransSlot[e * me2 + j];
     if (jt < 0) continue;
-    const double aw = qa[io] * m.weightsOnEdge[(size_t)eo * me2 + jt];
-    s3 += aw;
-    s4 += aw * pv_o;
+    const double wt = m.weightsOnEdge[(size_t)eo * me2 + jt];
+    s3 = fma(wt, qa[io], s3);
+    s4 = fma(wt, qapv[io], s4);
   }
   const double q = 0.5 * (pv_self * s1 + s2);
   double gh = G * (q - (f.ke[i2] - f.ke[i1]) * inv_dc);
@@ -1141,10 +1150,12 @@ int mpasgi_dyn_tend_vjp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   k_tadj_adv_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *g, *t, fl1, FastDiv(m->nAdvMax), fltb, flwb, sel);
   MPASG_LAUNCH_CHECK();
   double* qa = w.e[2];  // sel's bytes (read by the advection gather above) are no longer needed
-  k_tadj_qa<<<nblocks(nel), kBlock, 0, s>>>((int)nel, g->tend_u, f->h_edge, qa);
+  double* qapv = w.e[19];
+  double* pvu = w.e[20];
+  k_tadj_qa<<<nblocks(nel), kBlock, 0, s>>>((int)nel, g->tend_u, f->h_edge, f->pv_edge, f->u, qa, qapv, pvu);
   MPASG_LAUNCH_CHECK();
   k_tadj_u<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *g, *t, fl, p, hd, kd, ud, dsd, dsv, pke, phd, prwe, ppp, pkd,
-                                          udb, pd4, qa, pdz);
+                                          udb, pd4, qa, pdz, qapv, pvu);
   MPASG_LAUNCH_CHECK();
   k_tadj_u_cells<<<nblocks(ncw), kBlock, 0, s>>>(*m, *f, *g, fl1, p, pke, phd, prwe, ppp, pkd, pd4, pdz, hdb, kdb,
                                                  dsdb);
