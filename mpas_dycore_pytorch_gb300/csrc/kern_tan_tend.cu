@@ -87,6 +87,17 @@ MPASG_D double tan_wduz(const mpasg_mesh& m, const mpasg_fields& f, const mpasg_
 
 // ---- u tendency (k_tend_u): vertical transport, PV flux, KE gradient, divergence coupling,
 // and at rk 1 the pressure gradient and del2 mixing
+// pv u and its tangent pv du + u dpv at every edge level (the PV flux sum's neighbour
+// factors, formed once per stage), into the ke_edge scratch of f and d (free outside the
+// diagnostics)
+__global__ void k_tan_pvu(mpasg_fields f, mpasg_fields d, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double pv = f.pv_edge[i], u = f.u[i];
+  f.ke_edge[i] = pv * u;
+  d.ke_edge[i] = pv * d.u[i] + u * d.pv_edge[i];
+}
+
 __global__ void k_tan_u(mpasg_mesh m, mpasg_fields f, mpasg_fields d, FastDiv fl, TanTendScalars p, int defer) {
   const int L = m.nVertLevels;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -98,18 +109,22 @@ __global__ void k_tan_u(mpasg_mesh m, mpasg_fields f, mpasg_fields d, FastDiv fl
   double dtu = -m.rdzw[k] * (tan_wduz(m, f, d, c1, c2, oe, k + 1, L) - tan_wduz(m, f, d, c1, c2, oe, k, L));
   const int n2 = m.nEdgesOnEdge[e];
   const int me2 = m.maxEdges2;
+  // q = 0.5 sum_j w_j u_j (pv_self + pv_j) = 0.5 (pv_self sum w u + sum w (pv u)) and its
+  // tangent 0.5 (dpv_self sum w u + pv_self sum w du + sum w d(pv u)): four multiply-adds
+  // per neighbour over the per-edge factors of k_tan_pvu
   const double pv_self = f.pv_edge[i], dpv_self = d.pv_edge[i];
-  double q = 0.0, dq = 0.0;
+  double su = 0.0, sp = 0.0, sdu = 0.0, sdp = 0.0;
   for (int j = 0; j < n2; ++j) {
     const int eo = m.edgesOnEdge[e * me2 + j];
     const size_t io = (size_t)eo * L + k;
     const double w = m.weightsOnEdge[e * me2 + j];
-    const double s = pv_self + f.pv_edge[io];
-    q += (w * f.u[io]) * s;
-    dq += w * (d.u[io] * s + f.u[io] * (dpv_self + d.pv_edge[io]));
+    su = fma(w, f.u[io], su);
+    sp = fma(w, f.ke_edge[io], sp);
+    sdu = fma(w, d.u[io], sdu);
+    sdp = fma(w, d.ke_edge[io], sdp);
   }
-  q *= 0.5;
-  dq *= 0.5;
+  const double q = 0.5 * (pv_self * su + sp);
+  const double dq = 0.5 * ((dpv_self * su + pv_self * sdu) + sdp);
   const size_t i1 = (size_t)c1 * L + k, i2 = (size_t)c2 * L + k;
   const double inv_dc = m.invDcEdge[e];
   const double rho_e = f.h_edge[i], drho_e = d.h_edge[i];
@@ -574,6 +589,8 @@ int mpasgi_dyn_tend_jvp_core(const mpasg_mesh* m, const mpasg_config* c, const m
   p.dm = adj_damping(c);
   const int defer = (p.del4 || p.dm.v_mom > 0.0) ? 1 : 0;  // as the forward's TendScalars.defer
   k_tan_cells_a<<<nblocks(ncl), kBlock, 0, s>>>(*m, *f, *d, fl, p);
+  MPASG_LAUNCH_CHECK();
+  k_tan_pvu<<<nblocks(nel), kBlock, 0, s>>>(*f, *d, nel);
   MPASG_LAUNCH_CHECK();
   k_tan_u<<<nblocks(nel), kBlock, 0, s>>>(*m, *f, *d, fl, p, defer);
   MPASG_LAUNCH_CHECK();
