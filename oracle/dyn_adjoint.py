@@ -14,9 +14,10 @@ the cotangents of the stage's floating-point inputs.  Transposed stencils are wr
 scatters (``np.add.at``); the CUDA kernels use the equivalent deterministic gathers.
 
 Scope (the configurations the dynamics derivative supports): dry columns
-(``moist_end < moist_start``), flat terrain (``zb = zb3 = zxu = 0``), horizontal mixing
-``2d_smagorinsky`` or ``2d_fixed`` with or without the del4 filter, no vertical mixing, no
-CAM damping, no Rayleigh damping of u; any RK order, substep and split counts.
+(``moist_end < moist_start``), flat or terrain-following levels (the slope terms'
+upwind selections held fixed), horizontal mixing ``2d_smagorinsky`` or ``2d_fixed``
+with or without the del4 filter, vertical mixing, CAM and Rayleigh damping; any RK
+order, substep and split counts.
 
 This module is test infrastructure: only ``tests/`` read it.
 """
@@ -441,13 +442,41 @@ def recover_vjp(a, g):
     out = {k: np.zeros_like(a[k], dtype=np.float64) for k in
            ("rho_p_save", "rho_pp", "rtheta_p_save", "rtheta_pp", "rw_save", "rw_p", "wwAvg", "ru_save",
             "ru_p", "ruAvg")}
-    # w (interior levels; the surface and top values are zero over flat terrain)
+    # w: interior levels (omega-derived part plus the slope fluxes of the new ru over the
+    # interface density), the surface (slope fluxes of the cf-weighted ru over the
+    # cf-weighted density; zero over flat terrain), the top (zero)
     gw = gget("w", a["rw_save"])[:nc]
     g_wmid = gw[:, 1:nl] / rho_i
     g_rho_i = -gw[:, 1:nl] * w[:, 1:nl] / rho_i
     g_rho_zz[:, 1:] += fzm[1:] * g_rho_i
     g_rho_zz[:, :-1] += fzp[1:] * g_rho_i
     g_rwmid = g_wmid / zz_i
+    cf1, cf2, cf3 = _f(a, "cf1"), _f(a, "cf2"), _f(a, "cf3")
+    den0 = cf1 * rho_zz[:, 0] + cf2 * rho_zz[:, 1] + cf3 * rho_zz[:, 2]
+    g_surf = gw[:, 0] / den0
+    g_den0 = -g_surf * w[:, 0]
+    for q, cf in enumerate((cf1, cf2, cf3)):
+        g_rho_zz[:, q] += cf * g_den0
+    g_ru_slope = np.zeros((ne + 1, nl))
+    eoc = S.idx0(a["edgesOnCell"][:nc], ne)
+    n_eoc = np.asarray(a["nEdgesOnCell"][:nc]).astype(np.int64)
+    sign = a["edgesOnCell_sign"][:nc]
+    zb, zb3 = a["zb_cell"], a["zb3_cell"]
+    ru_pad = np.concatenate([ru, np.zeros((1, nl))])
+    for j in range(eoc.shape[1]):
+        valid = (j < n_eoc) & (eoc[:, j] < ne)
+        e = np.where(valid, eoc[:, j], ne)
+        rs = ru_pad[e]
+        fs = cf1 * rs[:, 0] + cf2 * rs[:, 1] + cf3 * rs[:, 2]
+        cs = zb[:nc, j, 0] + _sgn(fs) * zb3[:nc, j, 0]
+        g_fs = np.where(valid, g_surf * sign[:, j] * cs, 0.0)
+        for q, cf in enumerate((cf1, cf2, cf3)):
+            np.add.at(g_ru_slope, (e, q), cf * g_fs)
+        fi = fzm[1:] * rs[:, 1:nl] + fzp[1:] * rs[:, :nl - 1]
+        ci = zb[:nc, j, 1:nl] + _sgn(fi) * zb3[:nc, j, 1:nl]
+        g_fi = np.where(valid[:, None], g_wmid * sign[:, j, None] * ci, 0.0)
+        np.add.at(g_ru_slope, (e, slice(1, nl)), fzm[1:] * g_fi)
+        np.add.at(g_ru_slope, (e, slice(0, nl - 1)), fzp[1:] * g_fi)
     # rw: interior levels recovered; its bottom and top levels are zero (no derivative)
     grw = gget("rw", a["rw_save"])[:nc]
     g_rwmid = g_rwmid + grw[:, 1:nl]
@@ -460,7 +489,7 @@ def recover_vjp(a, g):
     out["wwAvg"][:nc, nl] += gww[:, nl]
     # edges
     gu = gget("u", a["ru_save"])[:ne]
-    g_ru = gget("ru", a["ru_save"])[:ne] + gu * 2.0 / den_u
+    g_ru = gget("ru", a["ru_save"])[:ne] + gu * 2.0 / den_u + g_ru_slope[:ne]
     g_den = -gu * 2.0 * ru / (den_u * den_u)
     gz = np.zeros((nc + 1, nl))
     np.add.at(gz, coe[:, 0], g_den)
@@ -635,12 +664,10 @@ def dyn_tend_vjp(a, g):
     else:
         h_mom_eddy_visc4 = _f(a, "config_h_mom_eddy_visc4")
         h_theta_eddy_visc4 = _f(a, "config_h_theta_eddy_visc4")
-    # dry columns over flat terrain: the moist coefficients and the metric terms are held
-    # constant by this sweep, so other inputs are refused rather than mis-differentiated
+    # dry columns: the moist coefficients are held constant by this sweep, so moist
+    # columns are refused rather than mis-differentiated
     if "qtot" in a and np.any(np.asarray(a["qtot"]) != 0.0):
         raise NotImplementedError("derivative in moist columns")
-    if "zxu" in a and np.any(np.asarray(a["zxu"]) != 0.0):
-        raise NotImplementedError("derivative over terrain")
     # the mixing and damping options (dyn_tend.py:2730-2780, 2956-2990, 3434-3456,
     # 4636-4648, 5064-5100), differentiated with the forward's branches
     v_mom = _f(a, "config_v_mom_eddy_visc2") if "config_v_mom_eddy_visc2" in a else 0.0
@@ -1312,7 +1339,7 @@ def prepare_vjp(stepper, st, dt, g):
     g_th_m = g_th_m + g_rtp * (rho_p + rb)
     g_rho_p = g_rho_p + g_rtp * theta_m
     g_rz += g_rho_p
-    # rw (interior, flat terrain) = w rho_i zz_i
+    # rw (interior) = w rho_i zz_i + the slope terms (below)
     fzm, fzp = m["fzm"][:nl], m["fzp"][:nl]
     g_rw = z("rw")
     rho_i = fzp[None, 1:] * rho_zz[:, :nl - 1] + fzm[None, 1:] * rho_zz[:, 1:]
@@ -1323,11 +1350,28 @@ def prepare_vjp(stepper, st, dt, g):
     g_rho_i = g_rw[:, 1:nl] * st["w"][:nc, 1:nl] * zz_i
     g_rz[:, 1:] += fzm[None, 1:] * g_rho_i
     g_rz[:, :nl - 1] += fzp[None, 1:] * g_rho_i
+    # the slope terms of rw: - sum_j s_j (zb + sgn(flux_j) zb3) flux_j zz_i, flux_j = fzm
+    # ru[k] + fzp ru[k-1] of the prepared ru (the selection held fixed)
+    g_ru_slope = np.zeros((ne + 1, nl))
+    eoc = S.idx0(m["edgesOnCell"][:nc], ne)
+    n_eoc = np.asarray(m["nEdgesOnCell"][:nc]).astype(np.int64)
+    sign = m["edgesOnCell_sign"][:nc]
+    zb, zb3 = m["zb_cell"], m["zb3_cell"]
+    ru_pad = np.concatenate([prep["ru"][:ne], np.zeros((1, nl))])
+    for j in range(eoc.shape[1]):
+        valid = (j < n_eoc) & (eoc[:, j] < ne)
+        e = np.where(valid, eoc[:, j], ne)
+        rs = ru_pad[e]
+        flux = fzm[1:] * rs[:, 1:nl] + fzp[1:] * rs[:, :nl - 1]
+        coef = zb[:nc, j, 1:nl] + _sgn(flux) * zb3[:nc, j, 1:nl]
+        g_fl = np.where(valid[:, None], -g_rw[:, 1:nl] * sign[:, j, None] * coef * zz_i, 0.0)
+        np.add.at(g_ru_slope, (e, slice(1, nl)), fzm[1:] * g_fl)
+        np.add.at(g_ru_slope, (e, slice(0, nl - 1)), fzp[1:] * g_fl)
     # ru = 0.5 u (rho_1 + rho_2)
     coe = S.idx0(m["cellsOnEdge"][:ne], nc)
     u = st["u"]
     rz_pad = np.concatenate([rho_zz, np.zeros((1, nl))])
-    g_ru = (acc.take("ru") if "ru" in acc else np.zeros((ne + 1, nl)))[:ne]
+    g_ru = (acc.take("ru") if "ru" in acc else np.zeros((ne + 1, nl)))[:ne] + g_ru_slope[:ne]
     g_u = np.zeros((ne + 1, nl))
     g_u[:ne] = (acc.take("u") if "u" in acc else np.zeros((ne + 1, nl)))[:ne]
     g_u[:ne] += g_ru * 0.5 * (rz_pad[coe[:, 0]] + rz_pad[coe[:, 1]])

@@ -24,7 +24,7 @@ pytestmark = pytest.mark.gpu
 
 PRE = "_vertical_implicit_coefficients_"
 # dry cases whose options the derivative covers
-STAGE_CASES = ("g2_explicit", "g2_mono", "g2_rk2", "g2_split2", "g2_fixed", "g2_cam", "g2_rayleigh")
+STAGE_CASES = ("g2_explicit", "g2_mono", "g2_rk2", "g2_split2", "g2_fixed", "g2_cam", "g2_rayleigh", "g2_terrain")
 # per stage: the C entry point's scalar arguments, the output cotangents seeded (reference
 # names) and the inputs compared (reference names)
 STAGE_SPEC = {

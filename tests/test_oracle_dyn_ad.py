@@ -6,11 +6,11 @@ tests/golden/make_golden_dyn_ad.py)."""
 import numpy as np
 import pytest
 
-from dyn_ad_fixtures import AD_CASES, AD_OPTION_CASES, load_ad_case, objective_cotangents
+from dyn_ad_fixtures import AD_CASES, AD_OPTION_CASES, AD_TERRAIN_CASES, load_ad_case, objective_cotangents
 import oracle.dyn_adjoint as D
 
 
-@pytest.mark.parametrize("case", AD_CASES + AD_OPTION_CASES)
+@pytest.mark.parametrize("case", AD_CASES + AD_OPTION_CASES + AD_TERRAIN_CASES)
 def test_oracle_run_vjp_matches_reference(case):
     z, stepper, st0, dt, nsteps = load_ad_case(case)
     _, final = D.run_vjp(stepper, st0, dt, nsteps, {})
@@ -22,9 +22,9 @@ def test_oracle_run_vjp_matches_reference(case):
         assert np.linalg.norm(a - b) <= 1e-11 * np.linalg.norm(b), k
 
 
-@pytest.mark.parametrize("extra", [{"qtot": np.full((2, 4), 1e-3)}, {"zxu": np.full((2, 4), 1e-3)}])
+@pytest.mark.parametrize("extra", [{"qtot": np.full((2, 4), 1e-3)}])
 def test_oracle_stage_vjp_scope_is_enforced(extra):
-    """Moist columns and terrain are refused, not silently mis-differentiated."""
+    """Moist columns are refused, not silently mis-differentiated."""
     with pytest.raises(NotImplementedError):
         D.dyn_tend_vjp(dict({"nCells": 1, "nEdges": 1, "nVertices": 1, "nVertLevels": 4, "rk_step": 1,
                              "dt": 1.0, "coef_3rd_order": 0.25, "c_s": 0.125, "config_len_disp": 1.0,
